@@ -1,0 +1,1177 @@
+/*
+ * hdg_oracle.c -- CPU FP64 restatement of GridapHybrid.jl's hybridization path.
+ *
+ * TEST INFRASTRUCTURE ONLY (the checker).  Loaded by tests/, smoke() and the
+ * CPU-baseline leg of bench.py; never by the GPU product path.
+ *
+ * Reference files are cited as path:line inside the GridapHybrid.jl repository.
+ * Gridap.jl (0.18.2, branch exploring_hybridization, tree d7c0d281) is a
+ * dependency that is not vendored with the reference; where its behaviour is
+ * restated (node ordering, face numbering, quadrature, assembly) the comment
+ * says so.
+ */
+#include "hdg_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define MAXD 3
+#define MAXK 6
+
+static double wtime(void) {
+#ifdef _OPENMP
+  return omp_get_wtime();
+#else
+  return 0.0;
+#endif
+}
+
+int orc_max_threads(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+void orc_set_threads(int nthreads) {
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+  (void)nthreads;
+#endif
+}
+
+/* ------------------------------------------------------------------------ */
+/* Reference element: Gridap's Lagrangian node order on n-cubes.             */
+/* ------------------------------------------------------------------------ */
+
+static int ipow(int b, int e) {
+  int r = 1;
+  for (int i = 0; i < e; ++i) r *= b;
+  return r;
+}
+
+int orc_num_nodes(int D, int k) { return ipow(k + 1, D); }
+
+typedef struct {
+  int free_mask; /* bit d set: dimension d is a parameter of the face */
+  int fixed;     /* bit d: coordinate value (0/1) of a fixed dimension */
+} cube_face;
+
+static int popc(int x) {
+  int c = 0;
+  while (x) {
+    c += x & 1;
+    x >>= 1;
+  }
+  return c;
+}
+
+/* Faces of the D-cube in Gridap's ExtrusionPolytope order: the (d+1)-cube's
+ * faces are the d-cube's faces at x_d = 0, then at x_d = 1, then extruded
+ * along x_d, stably sorted by dimension.  For QUAD this gives vertices
+ * (0,0),(1,0),(0,1),(1,1), edges [y=0, y=1, x=0, x=1]; for HEX the facets
+ * [z=0, z=1, y=0, y=1, x=0, x=1] (Gridap.ReferenceFEs polytope conventions,
+ * used by test/DarcyHDGTests.jl through CartesianDiscreteModel). */
+static int cube_faces(int D, cube_face *out) {
+  cube_face cur[27], tmp[81];
+  int n = 1;
+  cur[0].free_mask = 0;
+  cur[0].fixed = 0;
+  for (int d = 0; d < D; ++d) {
+    int m = 0;
+    for (int i = 0; i < n; ++i) tmp[m++] = cur[i];
+    for (int i = 0; i < n; ++i) {
+      tmp[m] = cur[i];
+      tmp[m].fixed |= (1 << d);
+      ++m;
+    }
+    for (int i = 0; i < n; ++i) {
+      tmp[m] = cur[i];
+      tmp[m].free_mask |= (1 << d);
+      ++m;
+    }
+    n = 0;
+    for (int dim = 0; dim <= d + 1; ++dim)
+      for (int i = 0; i < m; ++i)
+        if (popc(tmp[i].free_mask) == dim) cur[n++] = tmp[i];
+  }
+  memcpy(out, cur, sizeof(cube_face) * n);
+  return n;
+}
+
+/* Node lattice indices (i_0..i_{D-1}, each in 0..k) in Gridap's node order:
+ * nodes are owned by faces in face order; a face's own nodes are the interior
+ * lattice points of that face, first face parameter fastest. */
+int orc_lagrange_lattice(int D, int k, int *lattice) {
+  if (D < 1 || D > MAXD || k < 1 || k > MAXK) return -1;
+  cube_face faces[27];
+  int nfaces = cube_faces(D, faces);
+  int cnt = 0;
+  for (int fi = 0; fi < nfaces; ++fi) {
+    int fm = faces[fi].free_mask;
+    int nfree = popc(fm);
+    int free_dims[MAXD];
+    int t = 0;
+    for (int d = 0; d < D; ++d)
+      if (fm & (1 << d)) free_dims[t++] = d;
+    int nint = ipow(k - 1, nfree);
+    for (int s = 0; s < nint; ++s) {
+      int r = s;
+      int idx[MAXD];
+      for (int d = 0; d < D; ++d) idx[d] = (faces[fi].fixed & (1 << d)) ? k : 0;
+      for (int j = 0; j < nfree; ++j) {
+        idx[free_dims[j]] = 1 + r % (k - 1);
+        r /= (k - 1);
+      }
+      for (int d = 0; d < D; ++d) lattice[cnt * D + d] = idx[d];
+      ++cnt;
+    }
+  }
+  return cnt;
+}
+
+/* 1D Lagrange polynomial on equispaced nodes t_j = j/k, and its derivative. */
+static void lag1d(int k, int i, double x, double *val, double *der) {
+  double v = 1.0, dv = 0.0;
+  double ti = (double)i / k;
+  for (int j = 0; j <= k; ++j) {
+    if (j == i) continue;
+    double tj = (double)j / k;
+    double f = (x - tj) / (ti - tj);
+    double df = 1.0 / (ti - tj);
+    dv = dv * f + v * df;
+    v = v * f;
+  }
+  *val = v;
+  *der = dv;
+}
+
+/* Gauss-Legendre rule on [0,1] (Gridap's tensor-product quadrature uses
+ * ceil((degree+1)/2) Gauss-Legendre points per direction). */
+void orc_gauss_legendre01(int npts, double *x, double *w) {
+  const double pi = 3.14159265358979323846;
+  for (int i = 0; i < npts; ++i) {
+    double z = cos(pi * (i + 0.75) / (npts + 0.5));
+    double dp = 1.0;
+    for (int it = 0; it < 100; ++it) {
+      double p0 = 1.0, p1 = z;
+      for (int j = 2; j <= npts; ++j) {
+        double p2 = ((2.0 * j - 1.0) * z * p1 - (j - 1.0) * p0) / j;
+        p0 = p1;
+        p1 = p2;
+      }
+      if (npts == 1) {
+        p1 = z;
+        p0 = 1.0;
+      }
+      dp = npts * (z * p1 - p0) / (z * z - 1.0);
+      double dz = p1 / dp;
+      z -= dz;
+      if (fabs(dz) < 1e-16) break;
+    }
+    {
+      double p0 = 1.0, p1 = z;
+      for (int j = 2; j <= npts; ++j) {
+        double p2 = ((2.0 * j - 1.0) * z * p1 - (j - 1.0) * p0) / j;
+        p0 = p1;
+        p1 = p2;
+      }
+      if (npts == 1) {
+        p1 = z;
+        p0 = 1.0;
+      }
+      dp = npts * (z * p1 - p0) / (z * z - 1.0);
+    }
+    x[npts - 1 - i] = 0.5 * (1.0 + z);
+    w[npts - 1 - i] = 1.0 / ((1.0 - z * z) * dp * dp);
+  }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Cartesian mesh in Gridap numbering.                                       */
+/* ------------------------------------------------------------------------ */
+
+int orc_cart_counts(int D, const int *n, int *ncells, int *nfacets) {
+  if (D < 1 || D > MAXD) return -1;
+  long nc = 1, nfc = 0;
+  for (int d = 0; d < D; ++d) nc *= n[d];
+  for (int d = 0; d < D; ++d) nfc += nc / n[d] * (n[d] + 1);
+  *ncells = (int)nc;
+  *nfacets = (int)nfc;
+  return 0;
+}
+
+/* local facet index of (normal dimension d, side s) in Gridap order */
+static int lface_of(int D, int d, int s) { return 2 * (D - 1 - d) + s; }
+
+/* Facet numbering of Gridap's grid topology (faces are numbered in the order
+ * they are first met when looping cells and their local faces); cells around
+ * a facet are listed in increasing cell id, so facet_cells[2f] is the owner
+ * used by get_cell_owner_normal_vector (src/Skeleton.jl:549-556,
+ * src/SkeletonArrays.jl:219-229) and by the recovery glue
+ * (src/HybridAffineFEOperators.jl:210-224). */
+int orc_cart_topology(int D, const int *n, int *cell_facets, int *facet_cells,
+                      int *facet_is_boundary) {
+  int ncells, nfacets;
+  if (orc_cart_counts(D, n, &ncells, &nfacets)) return -1;
+  int stride[MAXD];
+  stride[0] = 1;
+  for (int d = 1; d < D; ++d) stride[d] = stride[d - 1] * n[d - 1];
+  int next = 0;
+  for (int c = 0; c < ncells; ++c) {
+    int idx[MAXD], r = c;
+    for (int d = 0; d < D; ++d) {
+      idx[d] = r % n[d];
+      r /= n[d];
+    }
+    for (int lf = 0; lf < 2 * D; ++lf) {
+      int d = D - 1 - lf / 2, s = lf % 2;
+      int f;
+      if (s == 0 && idx[d] > 0) {
+        f = cell_facets[(c - stride[d]) * 2 * D + lface_of(D, d, 1)];
+        facet_cells[2 * f + 1] = c;
+        facet_is_boundary[f] = 0;
+      } else {
+        f = next++;
+        facet_cells[2 * f] = c;
+        facet_cells[2 * f + 1] = -1;
+        facet_is_boundary[f] = 1;
+        if (s == 1 && idx[d] < n[d] - 1) facet_is_boundary[f] = 0;
+      }
+      cell_facets[c * 2 * D + lf] = f;
+    }
+  }
+  return next == nfacets ? 0 : -2;
+}
+
+/* DOF numbering of the L2-conforming facet space with Dirichlet tags on the
+ * boundary (test/DarcyHDGTests.jl:44-47): facets in order, each facet's DOFs
+ * consecutive, free and Dirichlet DOFs numbered separately. */
+int orc_facet_dofs(int D, int k, int nfacets, const int *facet_is_boundary,
+                   int *facet_dofs, int *nfree, int *ndir) {
+  int nfd = ipow(k + 1, D - 1);
+  int fr = 0, di = 0;
+  for (int f = 0; f < nfacets; ++f)
+    for (int a = 0; a < nfd; ++a)
+      facet_dofs[f * nfd + a] = facet_is_boundary[f] ? -1 - (di++) : fr++;
+  *nfree = fr;
+  *ndir = di;
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Reference tables and manufactured problems.                               */
+/* ------------------------------------------------------------------------ */
+
+typedef struct {
+  int D, k, nk, nfd, ni, nf, n, n1, nqv, nqf;
+  int lat[216 * 3];  /* cell lattice (nk x D) */
+  int flat[36 * 2];  /* facet lattice (nfd x (D-1)) */
+  double *qv_xi;     /* nqv x D */
+  double *qv_w;      /* nqv */
+  double *phi;       /* nqv x nk */
+  double *dphi;      /* nqv x nk x D (reference gradient) */
+  double *qf_w;      /* nqf */
+  double *fphi;      /* 2D x nqf x nk : cell basis on facet points */
+  double *fxi;       /* 2D x nqf x D : cell-local coordinates of facet points */
+  double *mu;        /* nqf x nfd : facet basis */
+} reftab;
+
+static void basis_eval(const reftab *t, const double *xi, double *val,
+                       double *grad) {
+  int D = t->D, k = t->k;
+  for (int a = 0; a < t->nk; ++a) {
+    double l[MAXD], dl[MAXD];
+    for (int d = 0; d < D; ++d) lag1d(k, t->lat[a * D + d], xi[d], &l[d], &dl[d]);
+    double v = 1.0;
+    for (int d = 0; d < D; ++d) v *= l[d];
+    val[a] = v;
+    if (grad)
+      for (int e = 0; e < D; ++e) {
+        double g = dl[e];
+        for (int d = 0; d < D; ++d)
+          if (d != e) g *= l[d];
+        grad[a * D + e] = g;
+      }
+  }
+}
+
+static void reftab_free(reftab *t) {
+  free(t->qv_xi);
+  free(t->qv_w);
+  free(t->phi);
+  free(t->dphi);
+  free(t->qf_w);
+  free(t->fphi);
+  free(t->fxi);
+  free(t->mu);
+}
+
+static int reftab_init(reftab *t, int D, int k) {
+  memset(t, 0, sizeof(*t));
+  if (D < 2 || D > 3 || k < 1 || k > MAXK) return -1;
+  t->D = D;
+  t->k = k;
+  t->nk = ipow(k + 1, D);
+  t->nfd = ipow(k + 1, D - 1);
+  t->ni = (D + 1) * t->nk;
+  t->nf = 2 * D * t->nfd;
+  t->n = t->ni + t->nf;
+  /* test/DarcyHDGTests.jl:54-55: degree = 2*(order+1) */
+  int degree = 2 * (k + 1);
+  t->n1 = (degree + 2) / 2; /* ceil((degree+1)/2) */
+  t->nqv = ipow(t->n1, D);
+  t->nqf = ipow(t->n1, D - 1);
+  orc_lagrange_lattice(D, k, t->lat);
+  orc_lagrange_lattice(D - 1, k, t->flat);
+  double x1[16], w1[16];
+  orc_gauss_legendre01(t->n1, x1, w1);
+  t->qv_xi = malloc(sizeof(double) * t->nqv * D);
+  t->qv_w = malloc(sizeof(double) * t->nqv);
+  t->phi = malloc(sizeof(double) * t->nqv * t->nk);
+  t->dphi = malloc(sizeof(double) * t->nqv * t->nk * D);
+  t->qf_w = malloc(sizeof(double) * t->nqf);
+  t->fphi = malloc(sizeof(double) * 2 * D * t->nqf * t->nk);
+  t->fxi = malloc(sizeof(double) * 2 * D * t->nqf * D);
+  t->mu = malloc(sizeof(double) * t->nqf * t->nfd);
+  for (int q = 0; q < t->nqv; ++q) {
+    int r = q;
+    double w = 1.0;
+    for (int d = 0; d < D; ++d) {
+      t->qv_xi[q * D + d] = x1[r % t->n1];
+      w *= w1[r % t->n1];
+      r /= t->n1;
+    }
+    t->qv_w[q] = w;
+    basis_eval(t, &t->qv_xi[q * D], &t->phi[q * t->nk], &t->dphi[q * t->nk * D]);
+  }
+  for (int q = 0; q < t->nqf; ++q) {
+    int r = q;
+    double w = 1.0, s[MAXD];
+    for (int d = 0; d < D - 1; ++d) {
+      s[d] = x1[r % t->n1];
+      w *= w1[r % t->n1];
+      r /= t->n1;
+    }
+    t->qf_w[q] = w;
+    for (int b = 0; b < t->nfd; ++b) {
+      double v = 1.0, dl;
+      for (int d = 0; d < D - 1; ++d) {
+        double l;
+        lag1d(k, t->flat[b * (D - 1) + d], s[d], &l, &dl);
+        v *= l;
+      }
+      t->mu[q * t->nfd + b] = v;
+    }
+    /* facet parameters are the non-normal dimensions in increasing order */
+    for (int lf = 0; lf < 2 * D; ++lf) {
+      int dn = D - 1 - lf / 2, side = lf % 2, j = 0;
+      double *xi = &t->fxi[(lf * t->nqf + q) * D];
+      for (int d = 0; d < D; ++d) xi[d] = (d == dn) ? (double)side : s[j++];
+      basis_eval(t, xi, &t->fphi[(lf * t->nqf + q) * t->nk], NULL);
+    }
+  }
+  return 0;
+}
+
+enum { PROB_REF_LINEAR = 0, PROB_LINEAR = 1, PROB_SIN = 2 };
+
+/* Exact pressure, flux, flux-equation source f_u and mass source g for
+ * kappa^{-1} q + grad p = f_u, div q = g.  PROB_REF_LINEAR is the manufactured
+ * solution of test/DarcyHDGTests.jl:8-13 (u = (1+x,1+y), p = -3.14, f = u + grad p,
+ * g = div u). */
+static void exact(int problem, int D, const double *x, double kappa, double *p,
+                  double *q, double *fu, double *g) {
+  const double pi = 3.14159265358979323846;
+  if (problem == PROB_REF_LINEAR) {
+    *p = -3.14;
+    for (int d = 0; d < D; ++d) {
+      q[d] = 1.0 + x[d];
+      fu[d] = q[d] / kappa;
+    }
+    *g = (double)D;
+  } else if (problem == PROB_LINEAR) {
+    double s = 0.0;
+    for (int d = 0; d < D; ++d) s += x[d];
+    *p = s;
+    for (int d = 0; d < D; ++d) {
+      q[d] = -kappa;
+      fu[d] = 0.0;
+    }
+    *g = 0.0;
+  } else {
+    double sv[MAXD], cv[MAXD], prod = 1.0;
+    for (int d = 0; d < D; ++d) {
+      sv[d] = sin(pi * x[d]);
+      cv[d] = cos(pi * x[d]);
+      prod *= sv[d];
+    }
+    *p = prod;
+    for (int d = 0; d < D; ++d) {
+      double gd = pi * cv[d];
+      for (int e = 0; e < D; ++e)
+        if (e != d) gd *= sv[e];
+      q[d] = -kappa * gd;
+      fu[d] = 0.0;
+    }
+    *g = kappa * D * pi * pi * prod;
+  }
+}
+
+int orc_cell_sizes(int D, int k, int *ni, int *nf) {
+  if (D < 2 || D > 3 || k < 1 || k > MAXK) return -1;
+  *ni = (D + 1) * ipow(k + 1, D);
+  *nf = 2 * D * ipow(k + 1, D - 1);
+  return 0;
+}
+
+static void cell_geom(int D, const int *n, const double *domain, int c,
+                      double *x0, double *h) {
+  int r = c;
+  for (int d = 0; d < D; ++d) {
+    int i = r % n[d];
+    r /= n[d];
+    h[d] = (domain[2 * d + 1] - domain[2 * d]) / n[d];
+    x0[d] = domain[2 * d] + i * h[d];
+  }
+}
+
+/* Per-cell matrix and vector of the Darcy HDG weak form of
+ * test/DarcyHDGTests.jl:125-135 (stab_mode 1: tau*(n.n_o) terms exactly as
+ * written there; stab_mode 0: the textbook LDG-H stabilisation tau*(p-l)),
+ * with a per-cell permeability kappa in the flux mass term.  Volume and facet
+ * contributions are integrated point by point (Gridap IntegrationMap over
+ * the facet blocks, src/GridapAPIExtensions.jl:418-451), summed over facets
+ * (src/SumFacetsMap.jl:19-30) and merged with the volume part into one cell
+ * block (src/HybridAffineFEOperators.jl:254-286).  A is column-major n x n. */
+static void integrate_cell(const reftab *t, int c, const int *n,
+                           const double *domain, double tau, int stab_mode,
+                           int problem, double kappa, const int *facet_cells,
+                           const int *cell_facets, double *A, double *b) {
+  int D = t->D, nk = t->nk, nfd = t->nfd, ni = t->ni, N = t->n;
+  double x0[MAXD], h[MAXD];
+  cell_geom(D, n, domain, c, x0, h);
+  double detJ = 1.0;
+  for (int d = 0; d < D; ++d) detJ *= h[d];
+  memset(A, 0, sizeof(double) * N * N);
+  memset(b, 0, sizeof(double) * N);
+#define AIJ(i, j) A[(size_t)(i) + (size_t)N * (j)]
+  /* volume: vh.uh/kappa - (div vh) ph - grad(qh).uh ; vh.f_u + qh g */
+  for (int q = 0; q < t->nqv; ++q) {
+    const double *ph = &t->phi[q * nk];
+    const double *dph = &t->dphi[q * nk * D];
+    double wq = t->qv_w[q] * detJ;
+    double x[MAXD], pe, qe[MAXD], fu[MAXD], g;
+    for (int d = 0; d < D; ++d) x[d] = x0[d] + h[d] * t->qv_xi[q * D + d];
+    exact(problem, D, x, kappa, &pe, qe, fu, &g);
+    for (int a = 0; a < nk; ++a) {
+      for (int bb = 0; bb < nk; ++bb) {
+        double m = wq * ph[a] * ph[bb] / kappa;
+        for (int d = 0; d < D; ++d) AIJ(d * nk + a, d * nk + bb) += m;
+        for (int d = 0; d < D; ++d) {
+          /* physical derivative of an affine box map: d/dx_d = (1/h_d) d/dxi_d */
+          AIJ(d * nk + a, D * nk + bb) -= wq * (dph[a * D + d] / h[d]) * ph[bb];
+          AIJ(D * nk + a, d * nk + bb) -= wq * (dph[a * D + d] / h[d]) * ph[bb];
+        }
+      }
+      for (int d = 0; d < D; ++d) b[d * nk + a] += wq * ph[a] * fu[d];
+      b[D * nk + a] += wq * ph[a] * g;
+    }
+  }
+  /* facets of the cell boundary dK */
+  for (int lf = 0; lf < 2 * D; ++lf) {
+    int dn = D - 1 - lf / 2, side = lf % 2;
+    double nrm[MAXD] = {0, 0, 0};
+    nrm[dn] = side ? 1.0 : -1.0;
+    double detF = 1.0;
+    for (int d = 0; d < D; ++d)
+      if (d != dn) detF *= h[d];
+    int f = cell_facets[c * 2 * D + lf];
+    /* n.n_o = +1 on the facet owner (first cell around the facet), -1 otherwise */
+    double s = 1.0;
+    if (stab_mode == 1) s = (facet_cells[2 * f] == c) ? 1.0 : -1.0;
+    int off = ni + lf * nfd;
+    for (int q = 0; q < t->nqf; ++q) {
+      const double *ph = &t->fphi[(lf * t->nqf + q) * nk];
+      const double *mu = &t->mu[q * nfd];
+      double wq = t->qf_w[q] * detF;
+      for (int a = 0; a < nk; ++a) {
+        /* (vh.n) lh and mh (uh.n) */
+        for (int bb = 0; bb < nfd; ++bb) {
+          for (int d = 0; d < D; ++d) {
+            double v = wq * ph[a] * nrm[d] * mu[bb];
+            AIJ(d * nk + a, off + bb) += v;
+            AIJ(off + bb, d * nk + a) += v;
+          }
+          /* -tau qh lh (n.no) and +tau mh ph (n.no) */
+          AIJ(D * nk + a, off + bb) -= wq * tau * s * ph[a] * mu[bb];
+          AIJ(off + bb, D * nk + a) += wq * tau * s * mu[bb] * ph[a];
+        }
+        for (int bb = 0; bb < nk; ++bb) {
+          /* qh (uh.n) and tau qh ph (n.no) */
+          for (int d = 0; d < D; ++d)
+            AIJ(D * nk + a, d * nk + bb) += wq * ph[a] * ph[bb] * nrm[d];
+          AIJ(D * nk + a, D * nk + bb) += wq * tau * s * ph[a] * ph[bb];
+        }
+      }
+      /* -tau mh lh (n.no) */
+      for (int a = 0; a < nfd; ++a)
+        for (int bb = 0; bb < nfd; ++bb)
+          AIJ(off + a, off + bb) -= wq * tau * s * mu[a] * mu[bb];
+    }
+  }
+#undef AIJ
+}
+
+int orc_integrate_darcy(int D, int k, const int *n, const double *domain,
+                        double tau, int stab_mode, int problem,
+                        const double *kappa, const int *facet_cells,
+                        const int *cell_facets, double *A, double *b) {
+  reftab t;
+  if (reftab_init(&t, D, k)) return -1;
+  int ncells, nfacets;
+  orc_cart_counts(D, n, &ncells, &nfacets);
+  size_t N = t.n;
+#pragma omp parallel for schedule(static)
+  for (int c = 0; c < ncells; ++c)
+    integrate_cell(&t, c, n, domain, tau, stab_mode, problem,
+                   kappa ? kappa[c] : 1.0, facet_cells, cell_facets,
+                   A + (size_t)c * N * N, b + (size_t)c * N);
+  reftab_free(&t);
+  return 0;
+}
+
+/* Dirichlet values of the trial skeleton space TrialFESpace(M, p)
+ * (test/DarcyHDGTests.jl:52): nodal interpolation of p at the facet
+ * Lagrange nodes. */
+int orc_dirichlet_values(int D, int k, const int *n, const double *domain,
+                         int problem, int nfacets, const int *facet_is_boundary,
+                         const int *facet_dofs, int ndir, double *vals) {
+  int ncells, nf2;
+  orc_cart_counts(D, n, &ncells, &nf2);
+  int *cell_facets = malloc(sizeof(int) * ncells * 2 * D);
+  int *facet_cells = malloc(sizeof(int) * nfacets * 2);
+  int *isb = malloc(sizeof(int) * nfacets);
+  orc_cart_topology(D, n, cell_facets, facet_cells, isb);
+  int flat[36 * 2];
+  orc_lagrange_lattice(D - 1, k, flat);
+  int nfd = ipow(k + 1, D - 1);
+  for (int c = 0; c < ncells; ++c) {
+    double x0[MAXD], h[MAXD];
+    cell_geom(D, n, domain, c, x0, h);
+    for (int lf = 0; lf < 2 * D; ++lf) {
+      int f = cell_facets[c * 2 * D + lf];
+      if (!facet_is_boundary[f]) continue;
+      int dn = D - 1 - lf / 2, side = lf % 2;
+      for (int a = 0; a < nfd; ++a) {
+        int id = facet_dofs[f * nfd + a];
+        if (id >= 0) continue;
+        double x[MAXD];
+        int j = 0;
+        for (int d = 0; d < D; ++d) {
+          double xi = (d == dn) ? (double)side : (double)flat[a * (D - 1) + j++] / k;
+          x[d] = x0[d] + h[d] * xi;
+        }
+        double p, q[MAXD], fu[MAXD], g;
+        exact(problem, D, x, 1.0, &p, q, fu, &g);
+        if (-1 - id < ndir) vals[-1 - id] = p;
+      }
+    }
+  }
+  free(cell_facets);
+  free(facet_cells);
+  free(isb);
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* LAPACK/BLAS restatements used by the maps.                                */
+/* ------------------------------------------------------------------------ */
+
+/* dgetrf (unblocked dgetf2 form): partial pivoting on the first maximal
+ * |a_ij| (idamax), row swaps over the full row, scaling by the reciprocal
+ * pivot, rank-1 update.  Returns LAPACK's info (0 or first zero pivot). */
+static int getrf(int n, double *A, int lda, int *ipiv) {
+  int info = 0;
+  for (int j = 0; j < n; ++j) {
+    int p = j;
+    double amax = fabs(A[j + (size_t)lda * j]);
+    for (int i = j + 1; i < n; ++i) {
+      double v = fabs(A[i + (size_t)lda * j]);
+      if (v > amax) {
+        amax = v;
+        p = i;
+      }
+    }
+    ipiv[j] = p;
+    if (A[p + (size_t)lda * j] != 0.0) {
+      if (p != j)
+        for (int c = 0; c < n; ++c) {
+          double tmp = A[j + (size_t)lda * c];
+          A[j + (size_t)lda * c] = A[p + (size_t)lda * c];
+          A[p + (size_t)lda * c] = tmp;
+        }
+      double r = 1.0 / A[j + (size_t)lda * j];
+      for (int i = j + 1; i < n; ++i) A[i + (size_t)lda * j] *= r;
+    } else if (info == 0) {
+      info = j + 1;
+    }
+    for (int c = j + 1; c < n; ++c) {
+      double u = A[j + (size_t)lda * c];
+      if (u != 0.0)
+        for (int i = j + 1; i < n; ++i)
+          A[i + (size_t)lda * c] -= A[i + (size_t)lda * j] * u;
+    }
+  }
+  return info;
+}
+
+/* dgetrs('N'): row interchanges, unit-lower forward solve, upper back solve. */
+static void getrs(int n, int nrhs, const double *LU, int lda, const int *ipiv,
+                  double *B, int ldb) {
+  for (int c = 0; c < nrhs; ++c) {
+    double *x = B + (size_t)ldb * c;
+    for (int i = 0; i < n; ++i)
+      if (ipiv[i] != i) {
+        double tmp = x[i];
+        x[i] = x[ipiv[i]];
+        x[ipiv[i]] = tmp;
+      }
+    for (int j = 0; j < n; ++j) {
+      double xj = x[j];
+      if (xj != 0.0)
+        for (int i = j + 1; i < n; ++i) x[i] -= xj * LU[i + (size_t)lda * j];
+    }
+    for (int j = n - 1; j >= 0; --j) {
+      if (x[j] != 0.0) {
+        x[j] /= LU[j + (size_t)lda * j];
+        double xj = x[j];
+        for (int i = 0; i < j; ++i) x[i] -= xj * LU[i + (size_t)lda * j];
+      }
+    }
+  }
+}
+
+/* C = C - A*B (dgemm 'N','N', alpha = -1, beta = 1; reference loop order) */
+static void gemm_sub(int m, int nn, int kk, const double *A, int lda,
+                     const double *B, int ldb, double *C, int ldc) {
+  for (int j = 0; j < nn; ++j)
+    for (int l = 0; l < kk; ++l) {
+      double tmp = -B[l + (size_t)ldb * j];
+      if (tmp != 0.0)
+        for (int i = 0; i < m; ++i) C[i + (size_t)ldc * j] += tmp * A[i + (size_t)lda * l];
+    }
+}
+
+/* y = y - A*x (dgemv 'N', alpha = -1, beta = 1) */
+static void gemv_sub(int m, int nn, const double *A, int lda, const double *x,
+                     double *y) {
+  for (int j = 0; j < nn; ++j) {
+    double tmp = -x[j];
+    if (tmp != 0.0)
+      for (int i = 0; i < m; ++i) y[i] += tmp * A[i + (size_t)lda * j];
+  }
+}
+
+static void copy_block(const double *A, int lda, int r0, int c0, int m, int nn,
+                       double *out) {
+  for (int j = 0; j < nn; ++j)
+    for (int i = 0; i < m; ++i) out[i + (size_t)m * j] = A[(r0 + i) + (size_t)lda * (c0 + j)];
+}
+
+/* StaticCondensationMap evaluate! (src/StaticCondensationMap.jl:146-196),
+ * op for op: A11 = L11 U11 (getrf, :179), A12 = A11^{-1} A12 (getrs, :183),
+ * A22 -= A21 A12 (gemm, :186), b1 = A11^{-1} b1 (getrs, :189),
+ * b2 -= A21 b1 (gemv, :192); returns (A22, b2) = (S, g). */
+static int static_condensation_cell(int ni, int nf, const double *A,
+                                    const double *b, double *S, double *g,
+                                    double *work, int *ipiv) {
+  int n = ni + nf;
+  double *A11 = work, *A12 = A11 + (size_t)ni * ni, *A21 = A12 + (size_t)ni * nf,
+         *b1 = A21 + (size_t)nf * ni;
+  copy_block(A, n, 0, 0, ni, ni, A11);
+  copy_block(A, n, 0, ni, ni, nf, A12);
+  copy_block(A, n, ni, 0, nf, ni, A21);
+  copy_block(A, n, ni, ni, nf, nf, S);
+  memcpy(b1, b, sizeof(double) * ni);
+  memcpy(g, b + ni, sizeof(double) * nf);
+  int info = getrf(ni, A11, ni, ipiv);
+  getrs(ni, nf, A11, ni, ipiv, A12, ni);
+  gemm_sub(nf, nf, ni, A21, nf, A12, ni, S, nf);
+  getrs(ni, 1, A11, ni, ipiv, b1, ni);
+  gemv_sub(nf, ni, A21, nf, b1, g);
+  return info;
+}
+
+int orc_static_condensation(int ncells, int ni, int nf, const double *A,
+                            const double *b, double *S, double *g, int *info) {
+  int n = ni + nf, bad = 0;
+#pragma omp parallel reduction(+ : bad)
+  {
+    double *work = malloc(sizeof(double) * ((size_t)ni * ni + 2 * (size_t)ni * nf + ni));
+    int *ipiv = malloc(sizeof(int) * ni);
+#pragma omp for schedule(static)
+    for (int c = 0; c < ncells; ++c) {
+      int inf = static_condensation_cell(ni, nf, A + (size_t)c * n * n, b + (size_t)c * n,
+                                         S + (size_t)c * nf * nf, g + (size_t)c * nf, work, ipiv);
+      if (info) info[c] = inf;
+      if (inf) ++bad;
+    }
+    free(work);
+    free(ipiv);
+  }
+  return bad ? 1 : 0;
+}
+
+/* BackwardStaticCondensationMap evaluate! (src/BackwardStaticCondensationMap.jl:61-102):
+ * b2 = x (:88); b1 -= A12 b2 (gemv, :91); A11 = L11 U11 (getrf, :95, the map
+ * refactorises); b1 = A11^{-1} b1 (getrs, :99).  Output u = b1 (the interior
+ * block of the re-blocked [b1; x] vector, :133-151). */
+static int backward_cell(int ni, int nf, const double *A, const double *b,
+                         const double *x, double *u, double *work, int *ipiv) {
+  int n = ni + nf;
+  double *A11 = work, *A12 = A11 + (size_t)ni * ni;
+  copy_block(A, n, 0, 0, ni, ni, A11);
+  copy_block(A, n, 0, ni, ni, nf, A12);
+  memcpy(u, b, sizeof(double) * ni);
+  gemv_sub(ni, nf, A12, ni, x, u);
+  int info = getrf(ni, A11, ni, ipiv);
+  getrs(ni, 1, A11, ni, ipiv, u, ni);
+  return info;
+}
+
+int orc_backward_static_condensation(int ncells, int ni, int nf,
+                                     const double *A, const double *b,
+                                     const double *x, double *u, int *info) {
+  int n = ni + nf, bad = 0;
+#pragma omp parallel reduction(+ : bad)
+  {
+    double *work = malloc(sizeof(double) * ((size_t)ni * ni + (size_t)ni * nf));
+    int *ipiv = malloc(sizeof(int) * ni);
+#pragma omp for schedule(static)
+    for (int c = 0; c < ncells; ++c) {
+      int inf = backward_cell(ni, nf, A + (size_t)c * n * n, b + (size_t)c * n,
+                              x + (size_t)c * nf, u + (size_t)c * ni, work, ipiv);
+      if (info) info[c] = inf;
+      if (inf) ++bad;
+    }
+    free(work);
+    free(ipiv);
+  }
+  return bad ? 1 : 0;
+}
+
+/* SumFacetsMap (src/SumFacetsMap.jl:19-30): fold the facet blocks with (+). */
+int orc_sum_facets(int nfacets, int len, const double *blocks, double *out) {
+  if (nfacets < 2) return -1; /* the reference map needs at least two blocks */
+  for (int i = 0; i < len; ++i) out[i] = blocks[i] + blocks[len + i];
+  for (int f = 2; f < nfacets; ++f)
+    for (int i = 0; i < len; ++i) out[i] += blocks[(size_t)f * len + i];
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Assembly and skeleton solve.                                              */
+/* ------------------------------------------------------------------------ */
+
+static int cmp_int(const void *a, const void *b) {
+  int x = *(const int *)a, y = *(const int *)b;
+  return (x > y) - (x < y);
+}
+
+/* Sparsity pattern of Gridap's SparseMatrixAssembler on the skeleton space
+ * (src/HybridAffineFEOperators.jl:38-46): every pair of free skeleton DOFs
+ * that share a cell, rows = free DOFs, sorted columns.  The cell DOF ids
+ * are the cell's facets' DOFs in local facet order
+ * (src/HybridAffineFEOperators.jl:424-434).  rowptr==NULL: count only. */
+int orc_csr_pattern(int D, int k, int ncells, int nfacets,
+                    const int *cell_facets, const int *facet_dofs, int nfree,
+                    int64_t *rowptr, int32_t *colind, int64_t *nnz) {
+  int nfd = ipow(k + 1, D - 1), nl = 2 * D;
+  /* facet -> cells */
+  int *fc = malloc(sizeof(int) * 2 * nfacets);
+  for (int f = 0; f < 2 * nfacets; ++f) fc[f] = -1;
+  for (int c = 0; c < ncells; ++c)
+    for (int lf = 0; lf < nl; ++lf) {
+      int f = cell_facets[c * nl + lf];
+      if (fc[2 * f] < 0) fc[2 * f] = c;
+      else fc[2 * f + 1] = c;
+    }
+  int *cols = malloc(sizeof(int) * 2 * nl * nfd);
+  int64_t total = 0;
+  if (rowptr) rowptr[0] = 0;
+  /* rows are numbered by free DOF id; gather per row via its facet */
+  int *dof_facet = malloc(sizeof(int) * (nfree > 0 ? nfree : 1));
+  int *dof_local = malloc(sizeof(int) * (nfree > 0 ? nfree : 1));
+  for (int f = 0; f < nfacets; ++f)
+    for (int a = 0; a < nfd; ++a) {
+      int id = facet_dofs[f * nfd + a];
+      if (id >= 0) {
+        dof_facet[id] = f;
+        dof_local[id] = a;
+      }
+    }
+  for (int r = 0; r < nfree; ++r) {
+    int f = dof_facet[r], nc = 0;
+    for (int s = 0; s < 2; ++s) {
+      int c = fc[2 * f + s];
+      if (c < 0) continue;
+      for (int lf = 0; lf < nl; ++lf) {
+        int g = cell_facets[c * nl + lf];
+        for (int bb = 0; bb < nfd; ++bb) {
+          int id = facet_dofs[g * nfd + bb];
+          if (id >= 0) cols[nc++] = id;
+        }
+      }
+    }
+    qsort(cols, nc, sizeof(int), cmp_int);
+    int m = 0;
+    for (int i = 0; i < nc; ++i)
+      if (m == 0 || cols[i] != cols[m - 1]) cols[m++] = cols[i];
+    if (colind)
+      for (int i = 0; i < m; ++i) colind[total + i] = cols[i];
+    total += m;
+    if (rowptr) rowptr[r + 1] = total;
+  }
+  *nnz = total;
+  free(fc);
+  free(cols);
+  free(dof_facet);
+  free(dof_local);
+  return 0;
+}
+
+static int64_t find_col(const int64_t *rowptr, const int32_t *colind, int r, int c) {
+  int64_t lo = rowptr[r], hi = rowptr[r + 1] - 1;
+  while (lo <= hi) {
+    int64_t mid = (lo + hi) / 2;
+    if (colind[mid] == c) return mid;
+    if (colind[mid] < c) lo = mid + 1;
+    else hi = mid - 1;
+  }
+  return -1;
+}
+
+/* assemble_matrix_and_vector with the Dirichlet lift of _attach_dirichlet
+ * (src/HybridAffineFEOperators.jl:41-46): g_c -= S_c x_D with the Dirichlet
+ * values on Dirichlet DOFs and 0 elsewhere, then add free rows/cols, serially
+ * in cell order. */
+int orc_assemble(int D, int k, int ncells, const int *cell_facets,
+                 const int *facet_dofs, int nfree, const double *dir_vals,
+                 const double *S, const double *g, const int64_t *rowptr,
+                 const int32_t *colind, double *val, double *rhs) {
+  int nfd = ipow(k + 1, D - 1), nl = 2 * D, nf = nl * nfd;
+  memset(val, 0, sizeof(double) * rowptr[nfree]);
+  memset(rhs, 0, sizeof(double) * nfree);
+  int ids[64];
+  double gl[64];
+  for (int c = 0; c < ncells; ++c) {
+    const double *Sc = S + (size_t)c * nf * nf;
+    for (int lf = 0; lf < nl; ++lf)
+      for (int a = 0; a < nfd; ++a) ids[lf * nfd + a] = facet_dofs[cell_facets[c * nl + lf] * nfd + a];
+    for (int i = 0; i < nf; ++i) gl[i] = g[(size_t)c * nf + i];
+    for (int j = 0; j < nf; ++j)
+      if (ids[j] < 0) {
+        double xd = dir_vals[-1 - ids[j]];
+        for (int i = 0; i < nf; ++i) gl[i] -= Sc[i + (size_t)nf * j] * xd;
+      }
+    for (int i = 0; i < nf; ++i) {
+      if (ids[i] < 0) continue;
+      rhs[ids[i]] += gl[i];
+      for (int j = 0; j < nf; ++j) {
+        if (ids[j] < 0) continue;
+        int64_t p = find_col(rowptr, colind, ids[i], ids[j]);
+        if (p < 0) return -1;
+        val[p] += Sc[i + (size_t)nf * j];
+      }
+    }
+  }
+  return 0;
+}
+
+/* Dense LU solve of the assembled system (stands in for Gridap's sparse
+ * direct A\b, src/HybridAffineFEOperators.jl:74, at small sizes). */
+int orc_dense_solve(int n, const int64_t *rowptr, const int32_t *colind,
+                    const double *val, const double *rhs, double *x) {
+  double *M = calloc((size_t)n * n, sizeof(double));
+  int *ipiv = malloc(sizeof(int) * (n > 0 ? n : 1));
+  if (!M || !ipiv) return -1;
+  for (int r = 0; r < n; ++r)
+    for (int64_t p = rowptr[r]; p < rowptr[r + 1]; ++p) M[r + (size_t)n * colind[p]] = val[p];
+  int info = getrf(n, M, n, ipiv);
+  memcpy(x, rhs, sizeof(double) * n);
+  if (!info) getrs(n, 1, M, n, ipiv, x, n);
+  free(M);
+  free(ipiv);
+  return info;
+}
+
+static void spmv(int n, const int64_t *rowptr, const int32_t *colind,
+                 const double *val, const double *x, double *y, double sign) {
+#pragma omp parallel for schedule(static)
+  for (int r = 0; r < n; ++r) {
+    double s = 0.0;
+    for (int64_t p = rowptr[r]; p < rowptr[r + 1]; ++p) s += val[p] * x[colind[p]];
+    y[r] = sign * s;
+  }
+}
+
+static double dot(int n, const double *a, const double *b) {
+  double s = 0.0;
+#pragma omp parallel for reduction(+ : s) schedule(static)
+  for (int i = 0; i < n; ++i) s += a[i] * b[i];
+  return s;
+}
+
+/* Block-Jacobi preconditioned CG on (sign*A) x = sign*rhs with bs x bs
+ * diagonal blocks (one block per facet).  A stand-in for the reference's
+ * sparse direct solve at sizes where a direct factorisation is impractical. */
+int orc_pcg(int n, int bs, const int64_t *rowptr, const int32_t *colind,
+            const double *val, const double *rhs, double *x, double sign,
+            double rtol, int maxit, int *iters, double *relres) {
+  if (n % bs) return -1;
+  int nb = n / bs;
+  double *Binv = malloc(sizeof(double) * (size_t)nb * bs * bs);
+  double *r = malloc(sizeof(double) * n), *z = malloc(sizeof(double) * n);
+  double *p = malloc(sizeof(double) * n), *Ap = malloc(sizeof(double) * n);
+  int bad = 0;
+#pragma omp parallel for schedule(static) reduction(+ : bad)
+  for (int blk = 0; blk < nb; ++blk) {
+    double M[36 * 36], I[36 * 36];
+    for (int i = 0; i < bs; ++i)
+      for (int j = 0; j < bs; ++j) {
+        int r0 = blk * bs + i, c0 = blk * bs + j;
+        double v = 0.0;
+        for (int64_t q = rowptr[r0]; q < rowptr[r0 + 1]; ++q)
+          if (colind[q] == c0) v = val[q];
+        M[i * bs + j] = sign * v;
+        I[i * bs + j] = (i == j);
+      }
+    for (int c = 0; c < bs; ++c) { /* Gauss-Jordan with partial pivoting */
+      int pr = c;
+      for (int i = c + 1; i < bs; ++i)
+        if (fabs(M[i * bs + c]) > fabs(M[pr * bs + c])) pr = i;
+      if (M[pr * bs + c] == 0.0) {
+        ++bad;
+        break;
+      }
+      for (int j = 0; j < bs; ++j) {
+        double t = M[c * bs + j]; M[c * bs + j] = M[pr * bs + j]; M[pr * bs + j] = t;
+        t = I[c * bs + j]; I[c * bs + j] = I[pr * bs + j]; I[pr * bs + j] = t;
+      }
+      double piv = 1.0 / M[c * bs + c];
+      for (int j = 0; j < bs; ++j) { M[c * bs + j] *= piv; I[c * bs + j] *= piv; }
+      for (int i = 0; i < bs; ++i) {
+        if (i == c) continue;
+        double f = M[i * bs + c];
+        if (f != 0.0)
+          for (int j = 0; j < bs; ++j) { M[i * bs + j] -= f * M[c * bs + j]; I[i * bs + j] -= f * I[c * bs + j]; }
+      }
+    }
+    memcpy(&Binv[(size_t)blk * bs * bs], I, sizeof(double) * bs * bs);
+  }
+  int it = 0;
+  double bnorm = sqrt(dot(n, rhs, rhs)), rr = 0.0;
+  for (int i = 0; i < n; ++i) { x[i] = 0.0; r[i] = sign * rhs[i]; }
+  if (bad || bnorm == 0.0) {
+    *iters = 0;
+    *relres = 0.0;
+    free(Binv); free(r); free(z); free(p); free(Ap);
+    return bad ? -2 : 0;
+  }
+#define PRECOND(dst, src)                                                         \
+  _Pragma("omp parallel for schedule(static)") for (int blk = 0; blk < nb; ++blk) \
+    for (int i = 0; i < bs; ++i) {                                                \
+      double s_ = 0.0;                                                            \
+      for (int j = 0; j < bs; ++j) s_ += Binv[((size_t)blk * bs + i) * bs + j] * src[blk * bs + j]; \
+      dst[blk * bs + i] = s_;                                                     \
+    }
+  PRECOND(z, r);
+  memcpy(p, z, sizeof(double) * n);
+  double rz = dot(n, r, z);
+  rr = sqrt(dot(n, r, r));
+  while (rr > rtol * bnorm && it < maxit) {
+    spmv(n, rowptr, colind, val, p, Ap, sign);
+    double alpha = rz / dot(n, p, Ap);
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; ++i) { x[i] += alpha * p[i]; r[i] -= alpha * Ap[i]; }
+    PRECOND(z, r);
+    double rz1 = dot(n, r, z);
+    double beta = rz1 / rz;
+    rz = rz1;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; ++i) p[i] = z[i] + beta * p[i];
+    rr = sqrt(dot(n, r, r));
+    ++it;
+  }
+#undef PRECOND
+  *iters = it;
+  *relres = rr / bnorm;
+  free(Binv); free(r); free(z); free(p); free(Ap);
+  return rr <= rtol * bnorm ? 0 : 1;
+}
+
+/* Cell-wise skeleton values lh_K = get_cell_dof_values(lh, dK)
+ * (src/HybridAffineFEOperators.jl:113): free values from the solution,
+ * Dirichlet values from the trial space. */
+int orc_cell_skeleton_values(int D, int k, int ncells, const int *cell_facets,
+                             const int *facet_dofs, const double *xfree,
+                             const double *dir_vals, double *xcell) {
+  int nfd = ipow(k + 1, D - 1), nl = 2 * D, nf = nl * nfd;
+#pragma omp parallel for schedule(static)
+  for (int c = 0; c < ncells; ++c)
+    for (int lf = 0; lf < nl; ++lf)
+      for (int a = 0; a < nfd; ++a) {
+        int id = facet_dofs[cell_facets[c * nl + lf] * nfd + a];
+        xcell[(size_t)c * nf + lf * nfd + a] = id >= 0 ? xfree[id] : dir_vals[-1 - id];
+      }
+  return 0;
+}
+
+/* L2 errors sqrt(sum(int((u-uh).(u-uh))dOmega)) (test/DarcyHDGTests.jl:141-142)
+ * for the flux and the pressure; uint holds ni interior values per cell. */
+int orc_l2_errors(int D, int k, const int *n, const double *domain,
+                  int problem, const double *kappa, const double *uint,
+                  double *err_flux, double *err_pres) {
+  reftab t;
+  if (reftab_init(&t, D, k)) return -1;
+  int ncells, nfacets;
+  orc_cart_counts(D, n, &ncells, &nfacets);
+  double ef = 0.0, ep = 0.0;
+#pragma omp parallel for reduction(+ : ef, ep) schedule(static)
+  for (int c = 0; c < ncells; ++c) {
+    double x0[MAXD], h[MAXD], detJ = 1.0;
+    cell_geom(D, n, domain, c, x0, h);
+    for (int d = 0; d < D; ++d) detJ *= h[d];
+    const double *u = uint + (size_t)c * t.ni;
+    double kap = kappa ? kappa[c] : 1.0;
+    for (int q = 0; q < t.nqv; ++q) {
+      double x[MAXD], p, qe[MAXD], fu[MAXD], g;
+      for (int d = 0; d < D; ++d) x[d] = x0[d] + h[d] * t.qv_xi[q * D + d];
+      exact(problem, D, x, kap, &p, qe, fu, &g);
+      double qh[MAXD] = {0, 0, 0}, ph = 0.0;
+      for (int a = 0; a < t.nk; ++a) {
+        double v = t.phi[q * t.nk + a];
+        for (int d = 0; d < D; ++d) qh[d] += u[d * t.nk + a] * v;
+        ph += u[D * t.nk + a] * v;
+      }
+      double w = t.qv_w[q] * detJ, e2 = 0.0;
+      for (int d = 0; d < D; ++d) e2 += (qe[d] - qh[d]) * (qe[d] - qh[d]);
+      ef += w * e2;
+      ep += w * (p - ph) * (p - ph);
+    }
+  }
+  *err_flux = sqrt(ef);
+  *err_pres = sqrt(ep);
+  reftab_free(&t);
+  return 0;
+}
+
+/* Whole path as the reference runs it (src/HybridAffineFEOperators.jl:10-50 and
+ * :72-150): integrate + condense per cell, assemble, solve the skeleton
+ * system (solver 0: dense LU, 1: block-Jacobi PCG on -S), then re-integrate
+ * and run BackwardStaticCondensationMap per cell (the reference re-evaluates
+ * the weak form and refactorises A_ii in solve!).  Cell matrices are never
+ * stored for the whole mesh (one per thread).  uint_out: ncells x ni or NULL;
+ * lambda_out: nfree or NULL; times_out[5]: integrate+condense, assemble,
+ * solve, recover, total (s). */
+int orc_solve_darcy(int D, int k, const int *n, const double *domain,
+                    double tau, int stab_mode, int problem, const double *kappa,
+                    int solver, double rtol, int maxit, double *uint_out,
+                    double *lambda_out, double *times_out, int *iters,
+                    double *relres, double *err_flux, double *err_pres) {
+  reftab t;
+  if (reftab_init(&t, D, k)) return -1;
+  double t0 = wtime();
+  int ncells, nfacets, nfree, ndir;
+  orc_cart_counts(D, n, &ncells, &nfacets);
+  int nl = 2 * D, nfd = t.nfd, ni = t.ni, nf = t.nf, N = t.n;
+  int *cell_facets = malloc(sizeof(int) * ncells * nl);
+  int *facet_cells = malloc(sizeof(int) * nfacets * 2);
+  int *isb = malloc(sizeof(int) * nfacets);
+  int *fdofs = malloc(sizeof(int) * nfacets * nfd);
+  orc_cart_topology(D, n, cell_facets, facet_cells, isb);
+  orc_facet_dofs(D, k, nfacets, isb, fdofs, &nfree, &ndir);
+  double *dvals = malloc(sizeof(double) * (ndir > 0 ? ndir : 1));
+  orc_dirichlet_values(D, k, n, domain, problem, nfacets, isb, fdofs, ndir, dvals);
+  double *S = malloc(sizeof(double) * (size_t)ncells * nf * nf);
+  double *g = malloc(sizeof(double) * (size_t)ncells * nf);
+  int bad = 0;
+  double t1 = wtime();
+#pragma omp parallel reduction(+ : bad)
+  {
+    double *A = malloc(sizeof(double) * (size_t)N * N), *b = malloc(sizeof(double) * N);
+    double *work = malloc(sizeof(double) * ((size_t)ni * ni + 2 * (size_t)ni * nf + ni));
+    int *ipiv = malloc(sizeof(int) * ni);
+#pragma omp for schedule(static)
+    for (int c = 0; c < ncells; ++c) {
+      integrate_cell(&t, c, n, domain, tau, stab_mode, problem, kappa ? kappa[c] : 1.0,
+                     facet_cells, cell_facets, A, b);
+      if (static_condensation_cell(ni, nf, A, b, S + (size_t)c * nf * nf, g + (size_t)c * nf, work, ipiv))
+        ++bad;
+    }
+    free(A); free(b); free(work); free(ipiv);
+  }
+  double t2 = wtime();
+  int64_t nnz;
+  int64_t *rowptr = malloc(sizeof(int64_t) * (nfree + 1));
+  orc_csr_pattern(D, k, ncells, nfacets, cell_facets, fdofs, nfree, NULL, NULL, &nnz);
+  int32_t *colind = malloc(sizeof(int32_t) * (nnz > 0 ? nnz : 1));
+  double *val = malloc(sizeof(double) * (nnz > 0 ? nnz : 1));
+  double *rhs = malloc(sizeof(double) * (nfree > 0 ? nfree : 1));
+  double *lam = malloc(sizeof(double) * (nfree > 0 ? nfree : 1));
+  orc_csr_pattern(D, k, ncells, nfacets, cell_facets, fdofs, nfree, rowptr, colind, &nnz);
+  int rc = orc_assemble(D, k, ncells, cell_facets, fdofs, nfree, dvals, S, g, rowptr, colind, val, rhs);
+  double t3 = wtime();
+  int it = 0;
+  double rel = 0.0;
+  if (!rc) {
+    if (solver == 0) rc = orc_dense_solve(nfree, rowptr, colind, val, rhs, lam);
+    else rc = orc_pcg(nfree, nfd, rowptr, colind, val, rhs, lam, -1.0, rtol, maxit, &it, &rel);
+  }
+  double t4 = wtime();
+  double *ucells = uint_out ? uint_out : malloc(sizeof(double) * (size_t)ncells * ni);
+#pragma omp parallel reduction(+ : bad)
+  {
+    double *A = malloc(sizeof(double) * (size_t)N * N), *b = malloc(sizeof(double) * N);
+    double *work = malloc(sizeof(double) * ((size_t)ni * ni + (size_t)ni * nf));
+    double *xc = malloc(sizeof(double) * nf);
+    int *ipiv = malloc(sizeof(int) * ni);
+#pragma omp for schedule(static)
+    for (int c = 0; c < ncells; ++c) {
+      for (int lf = 0; lf < nl; ++lf)
+        for (int a = 0; a < nfd; ++a) {
+          int id = fdofs[cell_facets[c * nl + lf] * nfd + a];
+          xc[lf * nfd + a] = id >= 0 ? lam[id] : dvals[-1 - id];
+        }
+      integrate_cell(&t, c, n, domain, tau, stab_mode, problem, kappa ? kappa[c] : 1.0,
+                     facet_cells, cell_facets, A, b);
+      if (backward_cell(ni, nf, A, b, xc, ucells + (size_t)c * ni, work, ipiv)) ++bad;
+    }
+    free(A); free(b); free(work); free(xc); free(ipiv);
+  }
+  double t5 = wtime();
+  if (times_out) {
+    times_out[0] = t2 - t1;
+    times_out[1] = t3 - t2;
+    times_out[2] = t4 - t3;
+    times_out[3] = t5 - t4;
+    times_out[4] = t5 - t0;
+  }
+  if (iters) *iters = it;
+  if (relres) *relres = rel;
+  if (err_flux && err_pres) orc_l2_errors(D, k, n, domain, problem, kappa, ucells, err_flux, err_pres);
+  if (lambda_out) memcpy(lambda_out, lam, sizeof(double) * nfree);
+  if (!uint_out) free(ucells);
+  free(cell_facets); free(facet_cells); free(isb); free(fdofs); free(dvals);
+  free(S); free(g); free(rowptr); free(colind); free(val); free(rhs); free(lam);
+  reftab_free(&t);
+  if (bad) return 2;
+  return rc;
+}
