@@ -1,0 +1,319 @@
+"""Benchmark of the hybridization hot path on one GB300.
+
+Workload: 3D Darcy HDG on [0,1]^3, 32x32x32 hexes (32,768 cells), k = 2
+(108 interior + 54 facet DOFs per cell), tau = 1, per-cell permeability
+lognormal(0, 1) from seed 0, manufactured p = sin(pi x) sin(pi y) sin(pi z),
+skeleton PCG to 1e-10 relative residual.  Synthetic inputs (no dataset).
+
+One step = the whole path: integrate + condense every cell, assemble the
+skeleton CSR system, facet-block-Jacobi PCG, recover the interiors.
+
+  value : cells / s of a step with inputs resident in HBM (CUDA events on the
+          library's stream around K steps).  The step's working set (cell
+          blocks, factors, CSR: > 10 GB) is far larger than L2, so no flush is
+          needed between steps.
+  e2e   : the same metric through hdg_solve() with HOST buffers: permeability
+          copied in and the full free-DOF vector copied out every step.
+
+--impl reference times the CPU restatement of the reference (the oracle:
+GridapHybrid.jl's Julia path cannot run on this machine: no Julia toolchain)
+on all host cores.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "gridaphybrid.jl_gb300"))
+
+N_SIDE = 32
+K_ORDER = 2
+RTOL = 1e-10
+MAXIT = 20000
+SEED = 0
+METRIC = "HDG cells condensed/s (full integrate+condense+assemble+PCG+recover step)"
+UNIT = "cells/s"
+
+
+def workload_config(precision):
+    return {
+        "workload": "3D Darcy HDG 32x32x32 hex, k=2 (108 interior + 54 facet DOFs/cell), tau=1, "
+                    "lognormal(0,1) per-cell permeability seed 0, p=sin(pi x)sin(pi y)sin(pi z), "
+                    "skeleton PCG to 1e-10",
+        "cells": N_SIDE ** 3,
+        "precision": precision,
+        "l2": "working set > L2 (cell blocks + factors + CSR ~ 13 GB); no flush needed",
+    }
+
+
+def kappa_field():
+    return np.exp(np.random.default_rng(SEED).normal(0.0, 1.0, N_SIDE ** 3))
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def cpu_baseline_sample(threads=None):
+    """The oracle (C, FP64, OpenMP) on the host cores: the whole 32^3 path once."""
+    from oracle import oracle
+
+    if threads:
+        oracle.set_threads(threads)
+    nthreads = oracle.max_threads()
+    kappa = kappa_field()
+    t0 = time.perf_counter()
+    r = oracle.solve_darcy(3, K_ORDER, (N_SIDE,) * 3, problem=oracle.PROBLEM_SIN, kappa=kappa, solver=1,
+                           rtol=RTOL, maxit=MAXIT, want_solution=False)
+    dt = time.perf_counter() - t0
+    return {
+        "value": N_SIDE ** 3 / dt,
+        "unit": UNIT,
+        "cores": nthreads,
+        "kind": "port",
+        "sample": "one full 32^3 k=2 solve (integrate+condense, assemble, PCG %d its, re-integrate + "
+                  "backward map as the reference does) in %.1f s" % (r["iters"], dt),
+        "phases_s": {k: round(float(v), 3) for k, v in zip(
+            ["integrate_condense", "assemble", "solve", "recover", "total"], r["times"])},
+    }
+
+
+def run_reference(args):
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    from oracle import oracle
+
+    oracle.build()
+    kappa = kappa_field()
+    times = []
+    for it in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        r = oracle.solve_darcy(3, K_ORDER, (N_SIDE,) * 3, problem=oracle.PROBLEM_SIN, kappa=kappa, solver=1,
+                               rtol=RTOL, maxit=MAXIT, want_solution=False)
+        dt = time.perf_counter() - t0
+        if it >= args.warmup:
+            times.append(dt)
+    ms = 1000.0 * statistics.mean(times)
+    value = N_SIDE ** 3 / (ms / 1000.0)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config("fp64"),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": oracle.max_threads(), "kind": "port",
+                         "sample": "full 32^3 k=2 solve per step (C restatement of the reference path; "
+                                   "Julia/Gridap are not installed on this machine)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "pcg_iters": r["iters"],
+    }
+    print(json.dumps(line))
+
+
+def run_gpu(args):
+    import gridaphybrid_gb300 as gh
+    from gridaphybrid_gb300 import _lib
+
+    prec = {"fp64": _lib.HDG_PREC_FP64, "mixed": _lib.HDG_PREC_FP32_REFINED}[args.precision]
+    ctx = gh.Context(0)
+    lib = ctx.lib
+    h = ctypes.c_void_p()
+    cells = np.array([N_SIDE] * 3, dtype=np.int32)
+    dom = np.array([0, 1, 0, 1, 0, 1], dtype=np.float64)
+    ctx.check(lib.hdg_problem_create_cartesian(ctx.handle, 3, _lib.ptr(cells), _lib.ptr(dom), K_ORDER,
+                                               ctypes.byref(h)))
+    info = np.zeros(8, dtype=np.int64)
+    ctx.check(lib.hdg_problem_info(h, _lib.ptr(info)))
+    ncells, nfacets, ni, nf, nfree, ndir, nnz, nfd = (int(v) for v in info)
+    ctx.check(lib.hdg_set_darcy(h, _lib.HDG_STAB_TEXTBOOK, 1.0, _lib.HDG_PROBLEM_SIN))
+    kappa = kappa_field()
+    ctx.check(lib.hdg_set_permeability(h, _lib.ptr(kappa)))
+
+    def step():
+        ctx.check(lib.hdg_assemble(h, prec, None))
+        it = ctypes.c_int()
+        rel = ctypes.c_double()
+        ctx.check(lib.hdg_solve_skeleton(h, _lib.HDG_SOLVER_PCG, RTOL, MAXIT, ctypes.byref(it), ctypes.byref(rel)))
+        ctx.check(lib.hdg_recover(h))
+        return it.value, rel.value
+
+    for _ in range(args.warmup):
+        step()
+    ctx.synchronize()
+    launches0 = ctx.launches
+    sampler = ClockSampler()
+    sampler.start()
+    ctx.check(lib.hdg_context_record(ctx.handle, 0))
+    phase = np.zeros(5)
+    iters = []
+    for _ in range(args.steps):
+        it, rel = step()
+        iters.append(it)
+        t = np.zeros(5)
+        lib.hdg_get_timings(h, _lib.ptr(t))
+        phase += t
+    ctx.check(lib.hdg_context_record(ctx.handle, 1))
+    ctx.synchronize()
+    clocks = sampler.stop()
+    ms_total = ctypes.c_double()
+    ctx.check(lib.hdg_context_elapsed_ms(ctx.handle, 0, 1, ctypes.byref(ms_total)))
+    launches = ctx.launches - launches0
+    ms = ms_total.value / args.steps
+    phase /= args.steps
+
+    # end to end through hdg_solve with host (pinned) buffers
+    try:
+        import torch
+        kap_h = torch.from_numpy(kappa.copy()).pin_memory()
+        out_h = torch.empty(ncells * ni + nfree, dtype=torch.float64).pin_memory()
+        kp, op = _lib.ptr(kap_h), _lib.ptr(out_h)
+        pinned = True
+    except Exception:
+        kap_h = kappa.copy()
+        out_h = np.empty(ncells * ni + nfree)
+        kp, op = _lib.ptr(kap_h), _lib.ptr(out_h)
+        pinned = False
+    stats = np.zeros(7)
+    e2e_times = []
+    for i in range(args.e2e_steps + 1 if args.e2e_steps > 0 else 0):
+        t0 = time.perf_counter()
+        ctx.check(lib.hdg_solve(h, prec, _lib.HDG_SOLVER_PCG, RTOL, MAXIT, kp, op, _lib.ptr(stats)))
+        if i > 0:
+            e2e_times.append(time.perf_counter() - t0)
+    e2e_s = statistics.mean(e2e_times) if e2e_times else None
+
+    # dominant HBM kernel: the skeleton SpMV, timed alone on the library's stream
+    spmv_ms = ctypes.c_double()
+    ctx.check(lib.hdg_time_kernel(h, 3, 20, ctypes.byref(spmv_ms)))
+    # values + one column list per facet block row + block-row pointers + p gathered once + q written
+    nblockrows = nfree // nfd
+    spmv_bytes = nnz * 8 + (nnz // nfd) * 4 + nblockrows * 16 + 2 * nfree * 8
+    asm_ms = ctypes.c_double()
+    ctx.check(lib.hdg_time_kernel(h, 2, 5, ctypes.byref(asm_ms)))
+    asm_bytes = ncells * (nf * nf + nf) * 8 + nnz * 8 + nfree * 8
+    cond_ms = ctypes.c_double()
+    ctx.check(lib.hdg_time_kernel(h, 1, 2, ctypes.byref(cond_ms)))
+    peaks, peak_kind = measured_peaks()
+    hbm = float(peaks["hbm_gbs"])
+    spmv_gbs = spmv_bytes / (spmv_ms.value * 1e-3) / 1e9
+    asm_gbs = asm_bytes / (asm_ms.value * 1e-3) / 1e9
+    cond_flop = ni ** 3 * 2 / 3 + 2 * ni * ni * nf + 2 * nf * nf * ni + 2 * ni * ni + 2 * nf * ni
+    mean_iters = statistics.mean(iters)
+    line = {
+        "metric": METRIC, "value": ncells / (ms / 1000.0), "unit": UNIT, "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(args.precision),
+        "phases_ms": {"integrate": phase[0], "condense": phase[1], "assemble": phase[2],
+                      "skeleton_pcg": phase[3], "recover": phase[4]},
+        "condense_cells_per_s": ncells / ((phase[0] + phase[1]) / 1000.0),
+        "pcg_iters": mean_iters,
+        "pcg_relres": rel,
+        "full_solve_ms": ms,
+        "roofline": {"bound": "hbm", "kernel": "pcg_spmv_kernel", "achieved": spmv_gbs, "peak": hbm,
+                     "unit": "GB/s", "frac": spmv_gbs / hbm, "traffic": None,
+                     "peak_source": peak_kind,
+                     "bytes_per_launch": spmv_bytes,
+                     "ms_per_launch": spmv_ms.value},
+        "assembly_roofline": {"bound": "hbm", "achieved": asm_gbs, "peak": hbm, "unit": "GB/s",
+                              "frac": asm_gbs / hbm, "bytes_per_launch": asm_bytes, "ms_per_launch": asm_ms.value},
+        "condense_fp64": {"ms_per_launch": cond_ms.value, "gflops": cond_flop * ncells / (cond_ms.value * 1e-3) / 1e9},
+        "clocks": clocks,
+        "e2e": None if e2e_s is None else {
+            "value": ncells / e2e_s, "unit": UNIT, "h2d_bytes_per_step": ncells * 8,
+            "d2h_bytes_per_step": (ncells * ni + nfree) * 8, "ms_per_step": e2e_s * 1000.0,
+            "host_buffers": "pinned" if pinned else "pageable"},
+        "gpu_launches": launches,
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline_sample()
+    print(json.dumps(line))
+    lib.hdg_problem_destroy(h)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    rank = int(os.environ.get("RANK", "0"))
+    if args.gpus > 1 and rank != 0:
+        # replicas only: the path does not shard across GPUs in this build
+        return
+    run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

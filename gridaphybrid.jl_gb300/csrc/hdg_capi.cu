@@ -1,0 +1,882 @@
+// hdg_capi.cu -- the extern "C" entry points of libgridaphybrid_gb300.
+// Everything numeric runs on the GPU; the host side validates arguments,
+// stages host buffers, builds the mesh/pattern once per problem and drives
+// the kernels on the context's stream.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+
+#include "hdg_internal.h"
+#include "hdg_kernels.h"
+
+using namespace hdg;
+
+#define CUDA_TRY(ctx, call)                                                          \
+  do {                                                                               \
+    cudaError_t e_ = (call);                                                         \
+    if (e_ != cudaSuccess)                                                           \
+      return (ctx)->fail(e_ == cudaErrorMemoryAllocation ? HDG_ERR_NOMEM : HDG_ERR_CUDA, \
+                         "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+  } while (0)
+
+namespace {
+
+bool is_device_ptr(const void *p) {
+  if (!p) return false;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+// Device view of a caller buffer: the pointer itself when it is device memory,
+// else a staging buffer (filled from host when `in`).
+template <typename T>
+int stage_in(hdg_context *ctx, DBuf &buf, const T *src, size_t count, const T **out) {
+  if (is_device_ptr(src)) {
+    *out = src;
+    return HDG_OK;
+  }
+  CUDA_TRY(ctx, buf.reserve(sizeof(T) * count));
+  if (count) CUDA_TRY(ctx, cudaMemcpyAsync(buf.ptr, src, sizeof(T) * count, cudaMemcpyHostToDevice, ctx->stream));
+  *out = buf.as<T>();
+  return HDG_OK;
+}
+
+template <typename T>
+int stage_out(hdg_context *ctx, DBuf &buf, T *dst, size_t count, T **out) {
+  if (is_device_ptr(dst)) {
+    *out = dst;
+    return HDG_OK;
+  }
+  CUDA_TRY(ctx, buf.reserve(sizeof(T) * (count ? count : 1)));
+  *out = buf.as<T>();
+  return HDG_OK;
+}
+
+template <typename T>
+int finish_out(hdg_context *ctx, const T *dev, T *dst, size_t count) {
+  if (!dst || dev == dst || count == 0) return HDG_OK;
+  CUDA_TRY(ctx, cudaMemcpyAsync(dst, dev, sizeof(T) * count, cudaMemcpyDeviceToHost, ctx->stream));
+  return HDG_OK;
+}
+
+template <typename T>
+int upload(hdg_context *ctx, DBuf &buf, const std::vector<T> &v) {
+  CUDA_TRY(ctx, buf.reserve(sizeof(T) * (v.empty() ? 1 : v.size())));
+  if (!v.empty())
+    CUDA_TRY(ctx, cudaMemcpyAsync(buf.ptr, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, ctx->stream));
+  return HDG_OK;
+}
+
+CellArgs cell_args(hdg_problem *pb) {
+  const RefTables &t = pb->tab;
+  const double *tb = pb->d_tab.as<double>();
+  CellArgs a{};
+  a.D = t.D;
+  a.k = t.k;
+  a.nk = t.nk;
+  a.nfd = t.nfd;
+  a.ni = t.ni;
+  a.nf = t.nf;
+  a.n = t.n;
+  a.nqv = t.nqv;
+  a.ncells = pb->mesh.ncells;
+  a.M = tb + pb->toff.M;
+  a.G = tb + pb->toff.G;
+  a.F = tb + pb->toff.F;
+  a.H = tb + pb->toff.H;
+  a.L = tb + pb->toff.L;
+  a.qxi = tb + pb->toff.qxi;
+  a.qw = tb + pb->toff.qw;
+  a.qphi = tb + pb->toff.qphi;
+  a.origin = pb->d_origin.as<double>();
+  a.jac = pb->d_jac.as<double>();
+  a.kappa = pb->d_kappa.ptr ? pb->d_kappa.as<double>() : nullptr;
+  a.cell_facets = pb->d_cell_facets.as<int>();
+  a.facet_cell = pb->d_facet_cell.as<int>();
+  a.facet_dofs = pb->d_facet_dofs.as<int>();
+  a.tau = pb->tau;
+  a.stab_mode = pb->stab_mode;
+  a.problem = pb->problem;
+  return a;
+}
+
+AssembleArgs assemble_args(hdg_problem *pb) {
+  const RefTables &t = pb->tab;
+  AssembleArgs as{};
+  as.nf = t.nf;
+  as.nfd = t.nfd;
+  as.nl = 2 * t.D;
+  as.nblockrows = pb->pat.nblockrows;
+  as.ncells = pb->mesh.ncells;
+  as.nblocks = pb->pat.nblocks;
+  as.blk_off = pb->d_blk_off.as<int64_t>();
+  as.blk_rowlen = pb->d_blk_rowlen.as<int>();
+  as.blk_src = pb->d_blk_src.as<int>();
+  as.br_row0 = pb->d_br_row0.as<int>();
+  as.br_src = pb->d_br_src.as<int>();
+  as.dir_cells = pb->d_dir_cells.as<int>();
+  as.ndir_cells = (int)pb->pat.dir_cells.size();
+  as.cell_facets = pb->d_cell_facets.as<int>();
+  as.facet_dofs = pb->d_facet_dofs.as<int>();
+  as.dirvals = pb->d_dirvals.as<double>();
+  return as;
+}
+
+// Nodal interpolation of the exact pressure at the Dirichlet facet nodes
+// (TrialFESpace(M, p), test/DarcyHDGTests.jl:52).
+void interpolate_dirichlet(const hdg_problem *pb, std::vector<double> &vals) {
+  const HostMesh &m = pb->mesh;
+  const RefTables &t = pb->tab;
+  const int D = m.D, nfd = m.nfd, k = m.k;
+  vals.assign(m.ndir > 0 ? m.ndir : 1, 0.0);
+  for (int f = 0; f < m.nfacets; ++f) {
+    if (m.facet_first_dof[f] >= 0) continue;
+    const int c = m.facet_cell[2 * (size_t)f], lf = m.facet_lface[2 * (size_t)f];
+    const int dn = D - 1 - lf / 2, side = lf % 2;
+    for (int b = 0; b < nfd; ++b) {
+      const int id = m.facet_dofs[(size_t)f * nfd + b];
+      double xi[3], x[3];
+      for (int d = 0, j = 0; d < D; ++d)
+        xi[d] = (d == dn) ? double(side) : double(t.flat[b * (D - 1) + j++]) / k;
+      for (int d = 0; d < D; ++d) {
+        x[d] = m.origin[(size_t)c * D + d];
+        for (int e = 0; e < D; ++e) x[d] += m.jac[(size_t)c * D * D + e * D + d] * xi[e];
+      }
+      double p, q[3], fu[3], g;
+      exact_solution(pb->problem, D, x, 1.0, p, q, fu, g);
+      vals[-1 - id] = p;
+    }
+  }
+}
+
+int upload_dirichlet(hdg_problem *pb) {
+  std::vector<double> vals;
+  interpolate_dirichlet(pb, vals);
+  return upload(pb->ctx, pb->d_dirvals, vals);
+}
+
+int setup_problem(hdg_problem *pb) {
+  hdg_context *ctx = pb->ctx;
+  std::string err;
+  if (build_ref_tables(pb->mesh.D, pb->mesh.k, pb->tab)) return ctx->fail(HDG_ERR_INVALID, "unsupported D/k");
+  int rc = build_pattern(pb->mesh, pb->pat, err);
+  if (rc) return ctx->fail(rc, "%s", err.c_str());
+  std::vector<double> packed;
+  pb->toff = pack_tables(pb->tab, packed);
+  if ((rc = upload(ctx, pb->d_tab, packed))) return rc;
+  if ((rc = upload(ctx, pb->d_origin, pb->mesh.origin))) return rc;
+  if ((rc = upload(ctx, pb->d_jac, pb->mesh.jac))) return rc;
+  if ((rc = upload(ctx, pb->d_cell_facets, pb->mesh.cell_facets))) return rc;
+  if ((rc = upload(ctx, pb->d_facet_dofs, pb->mesh.facet_dofs))) return rc;
+  if ((rc = upload(ctx, pb->d_facet_cell, pb->mesh.facet_cell))) return rc;
+  const HostPattern &p = pb->pat;
+  if ((rc = upload(ctx, pb->d_rowptr, p.rowptr))) return rc;
+  if ((rc = upload(ctx, pb->d_colind, p.colind))) return rc;
+  if ((rc = upload(ctx, pb->d_br_row0, p.br_row0))) return rc;
+  if ((rc = upload(ctx, pb->d_br_src, p.br_src))) return rc;
+  if ((rc = upload(ctx, pb->d_blk_off, p.blk_off))) return rc;
+  if ((rc = upload(ctx, pb->d_blk_rowlen, p.blk_rowlen))) return rc;
+  if ((rc = upload(ctx, pb->d_blk_src, p.blk_src))) return rc;
+  if ((rc = upload(ctx, pb->d_diag_blk, p.diag_blk))) return rc;
+  if ((rc = upload(ctx, pb->d_dir_cells, p.dir_cells))) return rc;
+  if ((rc = upload_dirichlet(pb))) return rc;
+  CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return HDG_OK;
+}
+
+}  // namespace
+
+hdg_problem::~hdg_problem() {
+  if (pcg_graph) cudaGraphExecDestroy(pcg_graph);
+  if (h_pinned.ptr) {
+    cudaFreeHost(h_pinned.ptr);
+    h_pinned.ptr = nullptr;
+    h_pinned.bytes = 0;
+  }
+}
+
+extern "C" {
+
+int hdg_version(void) { return 100; }
+
+int hdg_context_create(int device, hdg_context **out) {
+  if (!out) return HDG_ERR_INVALID;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return HDG_ERR_NODEVICE;
+  }
+  if (device < 0 || device >= ndev) return HDG_ERR_NODEVICE;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return HDG_ERR_NODEVICE;
+  // the library carries sm_103a code only
+  if (prop.major != 10 || prop.minor != 3) return HDG_ERR_NODEVICE;
+  if (cudaSetDevice(device) != cudaSuccess) return HDG_ERR_NODEVICE;
+  hdg_context *ctx = new (std::nothrow) hdg_context();
+  if (!ctx) return HDG_ERR_NOMEM;
+  ctx->device = device;
+  ctx->num_sms = prop.multiProcessorCount;
+  ctx->smem_optin = prop.sharedMemPerBlockOptin;
+  if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete ctx;
+    return HDG_ERR_CUDA;
+  }
+  for (auto &e : ctx->ev) cudaEventCreate(&e);
+  for (auto &e : ctx->user_ev) cudaEventCreate(&e);
+  *out = ctx;
+  return HDG_OK;
+}
+
+int hdg_context_destroy(hdg_context *ctx) {
+  if (!ctx) return HDG_OK;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  for (auto &b : ctx->scratch) b.release();
+  for (auto &e : ctx->ev)
+    if (e) cudaEventDestroy(e);
+  for (auto &e : ctx->user_ev)
+    if (e) cudaEventDestroy(e);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return HDG_OK;
+}
+
+const char *hdg_last_error(const hdg_context *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int hdg_context_synchronize(hdg_context *ctx) {
+  if (!ctx) return HDG_ERR_INVALID;
+  CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return HDG_OK;
+}
+
+long long hdg_launch_count(const hdg_context *ctx) { return ctx ? ctx->launches : -1; }
+
+int hdg_context_record(hdg_context *ctx, int slot) {
+  if (!ctx) return HDG_ERR_INVALID;
+  if (slot < 0 || slot > 3) return ctx->fail(HDG_ERR_INVALID, "event slot must be 0..3");
+  cudaSetDevice(ctx->device);
+  CUDA_TRY(ctx, cudaEventRecord(ctx->user_ev[slot], ctx->stream));
+  return HDG_OK;
+}
+
+int hdg_context_elapsed_ms(hdg_context *ctx, int slot_from, int slot_to, double *ms) {
+  if (!ctx || !ms) return HDG_ERR_INVALID;
+  if (slot_from < 0 || slot_from > 3 || slot_to < 0 || slot_to > 3)
+    return ctx->fail(HDG_ERR_INVALID, "event slot must be 0..3");
+  cudaSetDevice(ctx->device);
+  CUDA_TRY(ctx, cudaEventSynchronize(ctx->user_ev[slot_to]));
+  float f = 0.f;
+  CUDA_TRY(ctx, cudaEventElapsedTime(&f, ctx->user_ev[slot_from], ctx->user_ev[slot_to]));
+  *ms = f;
+  return HDG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Map level
+// ---------------------------------------------------------------------------
+int hdg_static_condensation(hdg_context *ctx, int precision, int ncells, int ni, int nf,
+                            const double *A, const double *b, double *S, double *g,
+                            int *info) {
+  if (!ctx) return HDG_ERR_INVALID;
+  if (ncells < 0 || ni < 1 || nf < 0 || !A || !b || !S || !g)
+    return ctx->fail(HDG_ERR_INVALID, "hdg_static_condensation: bad arguments");
+  if (precision != HDG_PREC_FP64 && precision != HDG_PREC_FP32_REFINED)
+    return ctx->fail(HDG_ERR_INVALID, "unknown precision %d", precision);
+  if (ncells == 0) return HDG_OK;
+  const int n = ni + nf;
+  if ((size_t)n * (n + 1) * sizeof(double) > ctx->smem_optin - 1024)
+    return ctx->fail(HDG_ERR_INVALID, "cell block %d x %d exceeds the shared-memory condensation kernel", n, n);
+  cudaSetDevice(ctx->device);
+  const double *dA, *db;
+  double *dS, *dg;
+  int *dinfo;
+  int rc;
+  if ((rc = stage_in(ctx, ctx->scratch[0], A, (size_t)ncells * n * n, &dA))) return rc;
+  if ((rc = stage_in(ctx, ctx->scratch[1], b, (size_t)ncells * n, &db))) return rc;
+  if ((rc = stage_out(ctx, ctx->scratch[2], S, (size_t)ncells * nf * nf, &dS))) return rc;
+  if ((rc = stage_out(ctx, ctx->scratch[3], g, (size_t)ncells * nf, &dg))) return rc;
+  CUDA_TRY(ctx, ctx->scratch[4].reserve(sizeof(int) * ncells));
+  dinfo = ctx->scratch[4].as<int>();
+  // both precisions share the FP64 elimination on caller-provided blocks
+  CUDA_TRY(ctx, launch_condense_fp64(ncells, ni, nf, dA, db, dS, dg, nullptr, dinfo, ctx->stream,
+                                     ctx->num_sms, &ctx->launches));
+  if ((rc = finish_out(ctx, dS, S, (size_t)ncells * nf * nf))) return rc;
+  if ((rc = finish_out(ctx, dg, g, (size_t)ncells * nf))) return rc;
+  std::vector<int> hinfo(ncells);
+  CUDA_TRY(ctx, cudaMemcpyAsync(hinfo.data(), dinfo, sizeof(int) * ncells, cudaMemcpyDeviceToHost, ctx->stream));
+  CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  bool bad = false;
+  for (int c = 0; c < ncells; ++c) bad |= hinfo[c] != 0;
+  if (info) {
+    if (is_device_ptr(info))
+      CUDA_TRY(ctx, cudaMemcpy(info, dinfo, sizeof(int) * ncells, cudaMemcpyDeviceToDevice));
+    else
+      memcpy(info, hinfo.data(), sizeof(int) * ncells);
+  }
+  if (bad) return ctx->fail(HDG_ERR_SINGULAR, "zero pivot in an interior block (see info)");
+  return HDG_OK;
+}
+
+int hdg_backward_static_condensation(hdg_context *ctx, int precision, int ncells, int ni,
+                                     int nf, const double *A, const double *b,
+                                     const double *x, double *u, int *info) {
+  if (!ctx) return HDG_ERR_INVALID;
+  if (ncells < 0 || ni < 1 || nf < 0 || !A || !b || !u || (nf > 0 && !x))
+    return ctx->fail(HDG_ERR_INVALID, "hdg_backward_static_condensation: bad arguments");
+  if (precision != HDG_PREC_FP64 && precision != HDG_PREC_FP32_REFINED)
+    return ctx->fail(HDG_ERR_INVALID, "unknown precision %d", precision);
+  if (ncells == 0) return HDG_OK;
+  const int n = ni + nf;
+  if ((size_t)ni * (ni + 1) * sizeof(double) > ctx->smem_optin - 1024)
+    return ctx->fail(HDG_ERR_INVALID, "interior block %d exceeds the shared-memory kernel", ni);
+  cudaSetDevice(ctx->device);
+  const double *dA, *db, *dx = nullptr;
+  double *du;
+  int rc;
+  if ((rc = stage_in(ctx, ctx->scratch[0], A, (size_t)ncells * n * n, &dA))) return rc;
+  if ((rc = stage_in(ctx, ctx->scratch[1], b, (size_t)ncells * n, &db))) return rc;
+  if (nf > 0 && (rc = stage_in(ctx, ctx->scratch[5], x, (size_t)ncells * nf, &dx))) return rc;
+  if ((rc = stage_out(ctx, ctx->scratch[2], u, (size_t)ncells * ni, &du))) return rc;
+  CUDA_TRY(ctx, ctx->scratch[4].reserve(sizeof(int) * ncells));
+  int *dinfo = ctx->scratch[4].as<int>();
+  CUDA_TRY(ctx, launch_backward_fp64(ncells, ni, nf, dA, db, dx, du, dinfo, ctx->stream, ctx->num_sms,
+                                     &ctx->launches));
+  if ((rc = finish_out(ctx, du, u, (size_t)ncells * ni))) return rc;
+  std::vector<int> hinfo(ncells);
+  CUDA_TRY(ctx, cudaMemcpyAsync(hinfo.data(), dinfo, sizeof(int) * ncells, cudaMemcpyDeviceToHost, ctx->stream));
+  CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  bool bad = false;
+  for (int c = 0; c < ncells; ++c) bad |= hinfo[c] != 0;
+  if (info) memcpy(info, hinfo.data(), sizeof(int) * ncells);
+  if (bad) return ctx->fail(HDG_ERR_SINGULAR, "zero pivot in an interior block (see info)");
+  return HDG_OK;
+}
+
+int hdg_sum_facets(hdg_context *ctx, int nitems, int nfacets, int len, const double *blocks,
+                   double *out) {
+  if (!ctx) return HDG_ERR_INVALID;
+  if (nitems < 0 || nfacets < 2 || len < 0 || !blocks || !out)
+    return ctx->fail(HDG_ERR_INVALID, "hdg_sum_facets: bad arguments (nfacets must be >= 2)");
+  if (nitems == 0 || len == 0) return HDG_OK;
+  cudaSetDevice(ctx->device);
+  const double *db;
+  double *dout;
+  int rc;
+  if ((rc = stage_in(ctx, ctx->scratch[0], blocks, (size_t)nitems * nfacets * len, &db))) return rc;
+  if ((rc = stage_out(ctx, ctx->scratch[2], out, (size_t)nitems * len, &dout))) return rc;
+  CUDA_TRY(ctx, launch_sum_facets(nitems, nfacets, len, db, dout, ctx->stream, &ctx->launches));
+  if ((rc = finish_out(ctx, dout, out, (size_t)nitems * len))) return rc;
+  CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return HDG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Problems
+// ---------------------------------------------------------------------------
+int hdg_problem_create_cartesian(hdg_context *ctx, int D, const int *cells, const double *domain,
+                                 int k, hdg_problem **out) {
+  if (!ctx) return HDG_ERR_INVALID;
+  if (!cells || !domain || !out) return ctx->fail(HDG_ERR_INVALID, "null argument");
+  *out = nullptr;
+  cudaSetDevice(ctx->device);
+  hdg_problem *pb = new (std::nothrow) hdg_problem();
+  if (!pb) return ctx->fail(HDG_ERR_NOMEM, "host allocation failed");
+  pb->ctx = ctx;
+  std::string err;
+  int rc = build_cartesian_mesh(D, cells, domain, k, pb->mesh, err);
+  if (rc) {
+    delete pb;
+    return ctx->fail(rc, "%s", err.c_str());
+  }
+  if ((rc = setup_problem(pb))) {
+    delete pb;
+    return rc;
+  }
+  *out = pb;
+  return HDG_OK;
+}
+
+int hdg_problem_create(hdg_context *ctx, int D, int k, int ncells, int nfacets,
+                       const double *cell_origin, const double *cell_jacobian,
+                       const int *cell_facets, const int *facet_dofs, hdg_problem **out) {
+  if (!ctx) return HDG_ERR_INVALID;
+  if (!out || !cell_origin || !cell_jacobian || !cell_facets || !facet_dofs)
+    return ctx->fail(HDG_ERR_INVALID, "null argument");
+  if (D < 2 || D > 3 || k < 1 || k > kMaxK || ncells < 1 || nfacets < 1)
+    return ctx->fail(HDG_ERR_INVALID, "bad sizes");
+  *out = nullptr;
+  cudaSetDevice(ctx->device);
+  hdg_problem *pb = new (std::nothrow) hdg_problem();
+  if (!pb) return ctx->fail(HDG_ERR_NOMEM, "host allocation failed");
+  pb->ctx = ctx;
+  HostMesh &m = pb->mesh;
+  m.D = D;
+  m.k = k;
+  m.ncells = ncells;
+  m.nfacets = nfacets;
+  m.nfd = 1;
+  for (int d = 0; d < D - 1; ++d) m.nfd *= (k + 1);
+  m.origin.assign(cell_origin, cell_origin + (size_t)ncells * D);
+  m.jac.assign(cell_jacobian, cell_jacobian + (size_t)ncells * D * D);
+  m.cell_facets.assign(cell_facets, cell_facets + (size_t)ncells * 2 * D);
+  m.facet_dofs.assign(facet_dofs, facet_dofs + (size_t)nfacets * m.nfd);
+  std::string err;
+  int rc = finish_mesh(m, err);
+  if (rc) {
+    delete pb;
+    return ctx->fail(rc, "%s", err.c_str());
+  }
+  if ((rc = setup_problem(pb))) {
+    delete pb;
+    return rc;
+  }
+  *out = pb;
+  return HDG_OK;
+}
+
+int hdg_problem_destroy(hdg_problem *pb) {
+  if (!pb) return HDG_OK;
+  cudaSetDevice(pb->ctx->device);
+  cudaStreamSynchronize(pb->ctx->stream);
+  delete pb;
+  return HDG_OK;
+}
+
+int hdg_problem_info(const hdg_problem *pb, long long *info) {
+  if (!pb || !info) return HDG_ERR_INVALID;
+  info[0] = pb->mesh.ncells;
+  info[1] = pb->mesh.nfacets;
+  info[2] = pb->tab.ni;
+  info[3] = pb->tab.nf;
+  info[4] = pb->mesh.nfree;
+  info[5] = pb->mesh.ndir;
+  info[6] = pb->pat.nnz;
+  info[7] = pb->mesh.nfd;
+  return HDG_OK;
+}
+
+int hdg_get_topology(const hdg_problem *pb, int *cell_facets, int *facet_cells, int *facet_dofs) {
+  if (!pb) return HDG_ERR_INVALID;
+  const HostMesh &m = pb->mesh;
+  if (cell_facets) memcpy(cell_facets, m.cell_facets.data(), sizeof(int) * m.cell_facets.size());
+  if (facet_cells) memcpy(facet_cells, m.facet_cell.data(), sizeof(int) * m.facet_cell.size());
+  if (facet_dofs) memcpy(facet_dofs, m.facet_dofs.data(), sizeof(int) * m.facet_dofs.size());
+  return HDG_OK;
+}
+
+int hdg_set_darcy(hdg_problem *pb, int stab_mode, double tau, int problem) {
+  if (!pb) return HDG_ERR_INVALID;
+  hdg_context *ctx = pb->ctx;
+  if (stab_mode != HDG_STAB_TEXTBOOK && stab_mode != HDG_STAB_OWNER_SIGN)
+    return ctx->fail(HDG_ERR_INVALID, "unknown stabilisation %d", stab_mode);
+  if (!(tau > 0.0) || !std::isfinite(tau)) return ctx->fail(HDG_ERR_INVALID, "tau must be > 0");
+  if (problem < 0 || problem > 2) return ctx->fail(HDG_ERR_INVALID, "unknown problem %d", problem);
+  cudaSetDevice(ctx->device);
+  pb->stab_mode = stab_mode;
+  pb->tau = tau;
+  pb->problem = problem;
+  pb->form_set = true;
+  pb->assembled = pb->solved = pb->recovered = false;
+  int rc = upload_dirichlet(pb);
+  if (rc) return rc;
+  CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return HDG_OK;
+}
+
+int hdg_set_permeability(hdg_problem *pb, const double *kappa) {
+  if (!pb) return HDG_ERR_INVALID;
+  hdg_context *ctx = pb->ctx;
+  cudaSetDevice(ctx->device);
+  const size_t nc = pb->mesh.ncells;
+  if (!kappa) {
+    pb->d_kappa.release();
+  } else {
+    CUDA_TRY(ctx, pb->d_kappa.reserve(sizeof(double) * nc));
+    CUDA_TRY(ctx, cudaMemcpyAsync(pb->d_kappa.ptr, kappa, sizeof(double) * nc, cudaMemcpyDefault, ctx->stream));
+  }
+  pb->assembled = pb->solved = pb->recovered = false;
+  return HDG_OK;
+}
+
+int hdg_set_dirichlet_values(hdg_problem *pb, const double *vals) {
+  if (!pb) return HDG_ERR_INVALID;
+  hdg_context *ctx = pb->ctx;
+  if (!vals) return ctx->fail(HDG_ERR_INVALID, "null values");
+  cudaSetDevice(ctx->device);
+  const size_t nd = pb->mesh.ndir;
+  CUDA_TRY(ctx, pb->d_dirvals.reserve(sizeof(double) * (nd ? nd : 1)));
+  if (nd) CUDA_TRY(ctx, cudaMemcpyAsync(pb->d_dirvals.ptr, vals, sizeof(double) * nd, cudaMemcpyDefault, ctx->stream));
+  pb->assembled = pb->solved = pb->recovered = false;
+  return HDG_OK;
+}
+
+static float elapsed(cudaEvent_t a, cudaEvent_t b) {
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, a, b);
+  return ms;
+}
+
+int hdg_assemble(hdg_problem *pb, int precision, int *info) {
+  if (!pb) return HDG_ERR_INVALID;
+  hdg_context *ctx = pb->ctx;
+  if (precision != HDG_PREC_FP64 && precision != HDG_PREC_FP32_REFINED)
+    return ctx->fail(HDG_ERR_INVALID, "unknown precision %d", precision);
+  if (precision == HDG_PREC_FP32_REFINED)
+    return ctx->fail(HDG_ERR_INVALID, "FP32+refinement operator path not built yet");
+  cudaSetDevice(ctx->device);
+  const RefTables &t = pb->tab;
+  const size_t nc = pb->mesh.ncells, n = t.n, ni = t.ni, nf = t.nf;
+  if (n * (n + 1) * sizeof(double) > ctx->smem_optin - 1024)
+    return ctx->fail(HDG_ERR_INVALID, "cell block %zu exceeds the FP64 shared-memory kernel", n);
+  CUDA_TRY(ctx, pb->d_A.reserve(sizeof(double) * nc * n * n));
+  CUDA_TRY(ctx, pb->d_b.reserve(sizeof(double) * nc * n));
+  CUDA_TRY(ctx, pb->d_S.reserve(sizeof(double) * nc * nf * nf));
+  CUDA_TRY(ctx, pb->d_g.reserve(sizeof(double) * nc * nf));
+  CUDA_TRY(ctx, pb->d_aux.reserve(sizeof(double) * nc * nf));
+  CUDA_TRY(ctx, pb->d_fact.reserve(sizeof(double) * nc * ni * (n + 1)));
+  CUDA_TRY(ctx, pb->d_info.reserve(sizeof(int) * nc));
+  CUDA_TRY(ctx, pb->d_val.reserve(sizeof(double) * (pb->pat.nnz ? pb->pat.nnz : 1)));
+  CUDA_TRY(ctx, pb->d_rhs.reserve(sizeof(double) * (pb->mesh.nfree ? pb->mesh.nfree : 1)));
+  CellArgs a = cell_args(pb);
+  cudaEvent_t *ev = ctx->ev;
+  CUDA_TRY(ctx, cudaEventRecord(ev[0], ctx->stream));
+  CUDA_TRY(ctx, launch_integrate_fp64(a, pb->d_A.as<double>(), pb->d_b.as<double>(), ctx->stream,
+                                      ctx->num_sms, &ctx->launches));
+  CUDA_TRY(ctx, cudaEventRecord(ev[1], ctx->stream));
+  CUDA_TRY(ctx, launch_condense_fp64((int)nc, (int)ni, (int)nf, pb->d_A.as<double>(), pb->d_b.as<double>(),
+                                     pb->d_S.as<double>(), pb->d_g.as<double>(), pb->d_fact.as<double>(),
+                                     pb->d_info.as<int>(), ctx->stream, ctx->num_sms, &ctx->launches));
+  CUDA_TRY(ctx, cudaEventRecord(ev[2], ctx->stream));
+  AssembleArgs as = assemble_args(pb);
+  CUDA_TRY(ctx, launch_assemble(as, pb->d_S.as<double>(), pb->d_g.as<double>(), pb->d_aux.as<double>(),
+                                pb->d_val.as<double>(), pb->d_rhs.as<double>(), ctx->stream, ctx->num_sms,
+                                &ctx->launches));
+  CUDA_TRY(ctx, cudaEventRecord(ev[3], ctx->stream));
+  std::vector<int> hinfo(nc);
+  CUDA_TRY(ctx, cudaMemcpyAsync(hinfo.data(), pb->d_info.ptr, sizeof(int) * nc, cudaMemcpyDeviceToHost, ctx->stream));
+  CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  pb->timings[0] = elapsed(ev[0], ev[1]);
+  pb->timings[1] = elapsed(ev[1], ev[2]);
+  pb->timings[2] = elapsed(ev[2], ev[3]);
+  pb->precision = precision;
+  bool bad = false;
+  for (size_t c = 0; c < nc; ++c) bad |= hinfo[c] != 0;
+  if (info) memcpy(info, hinfo.data(), sizeof(int) * nc);
+  if (bad) return ctx->fail(HDG_ERR_SINGULAR, "zero pivot in an interior block (see info)");
+  pb->assembled = true;
+  pb->solved = pb->recovered = false;
+  return HDG_OK;
+}
+
+int hdg_get_skeleton_system(hdg_problem *pb, long long *rowptr, int *colind, double *val,
+                            double *rhs) {
+  if (!pb) return HDG_ERR_INVALID;
+  hdg_context *ctx = pb->ctx;
+  if (!pb->assembled) return ctx->fail(HDG_ERR_STATE, "assemble first");
+  cudaSetDevice(ctx->device);
+  const HostPattern &p = pb->pat;
+  if (rowptr)
+    CUDA_TRY(ctx, cudaMemcpyAsync(rowptr, p.rowptr.data(), sizeof(long long) * p.rowptr.size(), cudaMemcpyDefault, ctx->stream));
+  if (colind && p.nnz)
+    CUDA_TRY(ctx, cudaMemcpyAsync(colind, p.colind.data(), sizeof(int) * p.nnz, cudaMemcpyDefault, ctx->stream));
+  if (val && p.nnz)
+    CUDA_TRY(ctx, cudaMemcpyAsync(val, pb->d_val.ptr, sizeof(double) * p.nnz, cudaMemcpyDefault, ctx->stream));
+  if (rhs && pb->mesh.nfree)
+    CUDA_TRY(ctx, cudaMemcpyAsync(rhs, pb->d_rhs.ptr, sizeof(double) * pb->mesh.nfree, cudaMemcpyDefault, ctx->stream));
+  CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return HDG_OK;
+}
+
+static PcgArgs pcg_args(hdg_problem *pb) {
+  PcgArgs a{};
+  a.n = pb->mesh.nfree;
+  a.nfd = pb->mesh.nfd;
+  a.nblockrows = pb->pat.nblockrows;
+  a.rowptr = pb->d_rowptr.as<int64_t>();
+  a.colind = pb->d_colind.as<int>();
+  a.val = pb->d_val.as<double>();
+  a.rhs = pb->d_rhs.as<double>();
+  a.Binv = pb->d_Binv.as<double>();
+  a.x = pb->d_x.as<double>();
+  a.r = pb->d_r.as<double>();
+  a.z = pb->d_z.as<double>();
+  a.p = pb->d_p.as<double>();
+  a.q = pb->d_q.as<double>();
+  a.partials = pb->d_partials.as<double>();
+  a.scal = pb->d_scal.as<double>();
+  a.nparts = pb->ctx->num_sms * 4;
+  a.diag_blk = pb->d_diag_blk.as<int>();
+  a.blk_off = pb->d_blk_off.as<int64_t>();
+  a.blk_rowlen = pb->d_blk_rowlen.as<int>();
+  a.sign = -1.0;  // the condensed skeleton operator of these forms is negative definite
+  return a;
+}
+
+int hdg_solve_skeleton(hdg_problem *pb, int solver, double rtol, int maxit, int *iters,
+                       double *relres) {
+  if (!pb) return HDG_ERR_INVALID;
+  hdg_context *ctx = pb->ctx;
+  if (!pb->assembled) return ctx->fail(HDG_ERR_STATE, "assemble first");
+  if (solver != HDG_SOLVER_PCG && solver != HDG_SOLVER_DIRECT)
+    return ctx->fail(HDG_ERR_INVALID, "unknown solver %d", solver);
+  if (solver == HDG_SOLVER_PCG && (!(rtol > 0.0) || maxit < 1))
+    return ctx->fail(HDG_ERR_INVALID, "PCG needs rtol > 0 and maxit >= 1");
+  cudaSetDevice(ctx->device);
+  const size_t n = pb->mesh.nfree, nfd = pb->mesh.nfd;
+  CUDA_TRY(ctx, pb->d_x.reserve(sizeof(double) * (n ? n : 1)));
+  cudaEvent_t *ev = ctx->ev;
+  CUDA_TRY(ctx, cudaEventRecord(ev[4], ctx->stream));
+  int it = 0;
+  double rel = 0.0;
+  int status = HDG_OK;
+  if (n == 0) {
+    // nothing to solve
+  } else if (solver == HDG_SOLVER_DIRECT) {
+    if (n > 16384) return ctx->fail(HDG_ERR_INVALID, "direct solver limited to 16384 unknowns");
+    CUDA_TRY(ctx, pb->d_z.reserve(sizeof(double) * n * (n + 1)));
+    CUDA_TRY(ctx, pb->d_info.reserve(sizeof(int) * std::max<size_t>(pb->mesh.ncells, 1)));
+    CUDA_TRY(ctx, launch_dense_solve((int)n, pb->d_rowptr.as<int64_t>(), pb->d_colind.as<int>(),
+                                     pb->d_val.as<double>(), pb->d_rhs.as<double>(), pb->d_z.as<double>(),
+                                     pb->d_x.as<double>(), pb->d_info.as<int>(), ctx->stream, &ctx->launches));
+    int hinfo = 0;
+    CUDA_TRY(ctx, cudaMemcpyAsync(&hinfo, pb->d_info.ptr, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    if (hinfo) status = ctx->fail(HDG_ERR_SINGULAR, "singular skeleton system (pivot %d)", hinfo);
+    pb->d_z.release();
+  } else {
+    if (pb->pat.max_rowlen > 288)
+      return ctx->fail(HDG_ERR_INVALID, "skeleton rows of %d entries exceed the SpMV kernel's 288", pb->pat.max_rowlen);
+    if (nfd > 25) return ctx->fail(HDG_ERR_INVALID, "facet blocks larger than 25 DOFs are not supported by PCG");
+    CUDA_TRY(ctx, pb->d_Binv.reserve(sizeof(double) * pb->pat.nblockrows * nfd * nfd));
+    CUDA_TRY(ctx, pb->d_r.reserve(sizeof(double) * n));
+    CUDA_TRY(ctx, pb->d_z.reserve(sizeof(double) * n));
+    CUDA_TRY(ctx, pb->d_p.reserve(sizeof(double) * n));
+    CUDA_TRY(ctx, pb->d_q.reserve(sizeof(double) * n));
+    CUDA_TRY(ctx, pb->d_partials.reserve(sizeof(double) * 3 * ctx->num_sms * 4));
+    CUDA_TRY(ctx, pb->d_scal.reserve(sizeof(double) * 16));
+    if (!pb->h_pinned.ptr) {
+      CUDA_TRY(ctx, cudaMallocHost(&pb->h_pinned.ptr, 4096));
+      pb->h_pinned.bytes = 4096;
+    }
+    PcgArgs a = pcg_args(pb);
+    CUDA_TRY(ctx, launch_pcg_setup(a, rtol, ctx->stream, ctx->num_sms, &ctx->launches));
+    const int chunk = 16;
+    if (!pb->pcg_graph) {
+      cudaGraph_t g;
+      long long dummy = 0;
+      CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+      for (int i = 0; i < chunk; ++i) launch_pcg_iteration(a, ctx->stream, ctx->num_sms, &dummy);
+      CUDA_TRY(ctx, cudaStreamEndCapture(ctx->stream, &g));
+      cudaError_t e = cudaGraphInstantiate(&pb->pcg_graph, g, 0);
+      cudaGraphDestroy(g);
+      CUDA_TRY(ctx, e);
+      pb->pcg_graph_chunk = chunk;
+    }
+    double *h = static_cast<double *>(pb->h_pinned.ptr);
+    for (;;) {
+      CUDA_TRY(ctx, cudaGraphLaunch(pb->pcg_graph, ctx->stream));
+      ctx->launches += 5LL * pb->pcg_graph_chunk;
+      CUDA_TRY(ctx, cudaMemcpyAsync(h, pb->d_scal.ptr, sizeof(double) * 16, cudaMemcpyDeviceToHost, ctx->stream));
+      CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+      it = (int)h[8];
+      rel = h[5] > 0 ? std::sqrt(h[4] / h[5]) : 0.0;
+      if (h[7] != 0.0) break;
+      if (it >= maxit) {
+        status = ctx->fail(HDG_ERR_NOT_CONVERGED, "PCG: relative residual %.3e after %d iterations", rel, it);
+        break;
+      }
+      if (!std::isfinite(rel)) {
+        status = ctx->fail(HDG_ERR_NOT_CONVERGED, "PCG breakdown (non-finite residual)");
+        break;
+      }
+    }
+  }
+  CUDA_TRY(ctx, cudaEventRecord(ev[5], ctx->stream));
+  CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  pb->timings[3] = elapsed(ev[4], ev[5]);
+  pb->last_iters = it;
+  pb->last_relres = rel;
+  if (iters) *iters = it;
+  if (relres) *relres = rel;
+  pb->solved = (status == HDG_OK);
+  pb->recovered = false;
+  return status;
+}
+
+int hdg_recover(hdg_problem *pb) {
+  if (!pb) return HDG_ERR_INVALID;
+  hdg_context *ctx = pb->ctx;
+  if (!pb->solved) return ctx->fail(HDG_ERR_STATE, "solve the skeleton system first");
+  cudaSetDevice(ctx->device);
+  const size_t nc = pb->mesh.ncells, ni = pb->tab.ni;
+  CUDA_TRY(ctx, pb->d_uint.reserve(sizeof(double) * nc * ni));
+  CellArgs a = cell_args(pb);
+  cudaEvent_t *ev = ctx->ev;
+  CUDA_TRY(ctx, cudaEventRecord(ev[6], ctx->stream));
+  CUDA_TRY(ctx, launch_recover_fp64(a, pb->d_fact.as<double>(), pb->d_x.as<double>(),
+                                    pb->d_dirvals.as<double>(), pb->d_uint.as<double>(), ctx->stream,
+                                    ctx->num_sms, &ctx->launches));
+  CUDA_TRY(ctx, cudaEventRecord(ev[7], ctx->stream));
+  CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  pb->timings[4] = elapsed(ev[6], ev[7]);
+  pb->recovered = true;
+  return HDG_OK;
+}
+
+int hdg_get_cell_interior_values(hdg_problem *pb, double *out) {
+  if (!pb) return HDG_ERR_INVALID;
+  hdg_context *ctx = pb->ctx;
+  if (!pb->recovered) return ctx->fail(HDG_ERR_STATE, "recover first");
+  if (!out) return ctx->fail(HDG_ERR_INVALID, "null output");
+  cudaSetDevice(ctx->device);
+  CUDA_TRY(ctx, cudaMemcpyAsync(out, pb->d_uint.ptr, sizeof(double) * pb->mesh.ncells * pb->tab.ni,
+                                cudaMemcpyDefault, ctx->stream));
+  CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return HDG_OK;
+}
+
+int hdg_get_skeleton_values(hdg_problem *pb, double *out) {
+  if (!pb) return HDG_ERR_INVALID;
+  hdg_context *ctx = pb->ctx;
+  if (!pb->solved) return ctx->fail(HDG_ERR_STATE, "solve first");
+  if (!out) return ctx->fail(HDG_ERR_INVALID, "null output");
+  cudaSetDevice(ctx->device);
+  if (pb->mesh.nfree)
+    CUDA_TRY(ctx, cudaMemcpyAsync(out, pb->d_x.ptr, sizeof(double) * pb->mesh.nfree, cudaMemcpyDefault, ctx->stream));
+  CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return HDG_OK;
+}
+
+int hdg_get_free_dof_values(hdg_problem *pb, double *out) {
+  if (!pb) return HDG_ERR_INVALID;
+  hdg_context *ctx = pb->ctx;
+  if (!pb->recovered) return ctx->fail(HDG_ERR_STATE, "recover first");
+  if (!out) return ctx->fail(HDG_ERR_INVALID, "null output");
+  cudaSetDevice(ctx->device);
+  const size_t nc = pb->mesh.ncells, ni = pb->tab.ni, nk = pb->tab.nk, D = pb->tab.D;
+  const double *u = pb->d_uint.as<double>();
+  // [flux of all cells | pressure of all cells | free skeleton values]
+  CUDA_TRY(ctx, cudaMemcpy2DAsync(out, D * nk * sizeof(double), u, ni * sizeof(double), D * nk * sizeof(double),
+                                  nc, cudaMemcpyDefault, ctx->stream));
+  CUDA_TRY(ctx, cudaMemcpy2DAsync(out + nc * D * nk, nk * sizeof(double), u + D * nk, ni * sizeof(double),
+                                  nk * sizeof(double), nc, cudaMemcpyDefault, ctx->stream));
+  if (pb->mesh.nfree)
+    CUDA_TRY(ctx, cudaMemcpyAsync(out + nc * ni, pb->d_x.ptr, sizeof(double) * pb->mesh.nfree, cudaMemcpyDefault,
+                                  ctx->stream));
+  CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return HDG_OK;
+}
+
+int hdg_l2_errors(hdg_problem *pb, double *err_flux, double *err_pres) {
+  if (!pb) return HDG_ERR_INVALID;
+  hdg_context *ctx = pb->ctx;
+  if (!pb->recovered) return ctx->fail(HDG_ERR_STATE, "recover first");
+  cudaSetDevice(ctx->device);
+  const size_t nc = pb->mesh.ncells;
+  DBuf errs;
+  CUDA_TRY(ctx, errs.reserve(sizeof(double) * 2 * nc));
+  CellArgs a = cell_args(pb);
+  CUDA_TRY(ctx, launch_l2_errors(a, pb->d_uint.as<double>(), errs.as<double>(), ctx->stream, ctx->num_sms,
+                                 &ctx->launches));
+  std::vector<double> h(2 * nc);
+  CUDA_TRY(ctx, cudaMemcpyAsync(h.data(), errs.ptr, sizeof(double) * 2 * nc, cudaMemcpyDeviceToHost, ctx->stream));
+  CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  double ef = 0.0, ep = 0.0;
+  for (size_t c = 0; c < nc; ++c) {
+    ef += h[2 * c];
+    ep += h[2 * c + 1];
+  }
+  if (err_flux) *err_flux = std::sqrt(ef);
+  if (err_pres) *err_pres = std::sqrt(ep);
+  return HDG_OK;
+}
+
+int hdg_solve(hdg_problem *pb, int precision, int solver, double rtol, int maxit,
+              const double *kappa, double *free_dof_values, double *stats) {
+  if (!pb) return HDG_ERR_INVALID;
+  int rc;
+  if (kappa && (rc = hdg_set_permeability(pb, kappa))) return rc;
+  if ((rc = hdg_assemble(pb, precision, nullptr))) return rc;
+  int it = 0;
+  double rel = 0.0;
+  if ((rc = hdg_solve_skeleton(pb, solver, rtol, maxit, &it, &rel))) return rc;
+  if ((rc = hdg_recover(pb))) return rc;
+  if (free_dof_values && (rc = hdg_get_free_dof_values(pb, free_dof_values))) return rc;
+  if (stats) {
+    stats[0] = it;
+    stats[1] = rel;
+    stats[2] = pb->timings[0] + pb->timings[1];
+    stats[3] = pb->timings[2];
+    stats[4] = pb->timings[3];
+    stats[5] = pb->timings[4];
+    stats[6] = pb->timings[0] + pb->timings[1] + pb->timings[2] + pb->timings[3] + pb->timings[4];
+  }
+  return HDG_OK;
+}
+
+int hdg_get_timings(const hdg_problem *pb, double *ms) {
+  if (!pb || !ms) return HDG_ERR_INVALID;
+  for (int i = 0; i < 5; ++i) ms[i] = pb->timings[i];
+  return HDG_OK;
+}
+
+int hdg_time_kernel(hdg_problem *pb, int which, int reps, double *ms_per_launch) {
+  if (!pb || !ms_per_launch) return HDG_ERR_INVALID;
+  hdg_context *ctx = pb->ctx;
+  if (reps < 1 || which < 0 || which > 4) return ctx->fail(HDG_ERR_INVALID, "bad kernel id or reps");
+  if (!pb->assembled) return ctx->fail(HDG_ERR_STATE, "assemble first");
+  if ((which == 3 || which == 4) && !pb->solved) return ctx->fail(HDG_ERR_STATE, "solve first");
+  if (which == 3 && !pb->d_q.ptr) return ctx->fail(HDG_ERR_STATE, "SpMV timing needs a PCG solve first");
+  cudaSetDevice(ctx->device);
+  const RefTables &t = pb->tab;
+  const int nc = pb->mesh.ncells;
+  CellArgs a = cell_args(pb);
+  AssembleArgs as = assemble_args(pb);
+  PcgArgs pa{};
+  DBuf zero_scal;
+  if (which == 3) {
+    pa = pcg_args(pb);
+    CUDA_TRY(ctx, zero_scal.reserve(sizeof(double) * 16));
+    CUDA_TRY(ctx, cudaMemsetAsync(zero_scal.ptr, 0, sizeof(double) * 16, ctx->stream));
+    pa.scal = zero_scal.as<double>();  // an SC_DONE of 0 keeps the kernel active
+  }
+  auto launch = [&]() -> cudaError_t {
+    switch (which) {
+      case 0:
+        return launch_integrate_fp64(a, pb->d_A.as<double>(), pb->d_b.as<double>(), ctx->stream, ctx->num_sms,
+                                     &ctx->launches);
+      case 1:
+        return launch_condense_fp64(nc, t.ni, t.nf, pb->d_A.as<double>(), pb->d_b.as<double>(),
+                                    pb->d_S.as<double>(), pb->d_g.as<double>(), pb->d_fact.as<double>(),
+                                    pb->d_info.as<int>(), ctx->stream, ctx->num_sms, &ctx->launches);
+      case 2:
+        return launch_assemble(as, pb->d_S.as<double>(), pb->d_g.as<double>(), pb->d_aux.as<double>(),
+                               pb->d_val.as<double>(), pb->d_rhs.as<double>(), ctx->stream, ctx->num_sms,
+                               &ctx->launches);
+      case 3:
+        return launch_spmv(pa, ctx->stream, &ctx->launches);
+      default:
+        return launch_recover_fp64(a, pb->d_fact.as<double>(), pb->d_x.as<double>(), pb->d_dirvals.as<double>(),
+                                   pb->d_uint.ptr ? pb->d_uint.as<double>() : nullptr, ctx->stream, ctx->num_sms,
+                                   &ctx->launches);
+    }
+  };
+  if (which == 4 && !pb->d_uint.ptr) return ctx->fail(HDG_ERR_STATE, "recover first");
+  CUDA_TRY(ctx, launch());  // warm-up
+  CUDA_TRY(ctx, cudaEventRecord(ctx->ev[0], ctx->stream));
+  for (int r = 0; r < reps; ++r) CUDA_TRY(ctx, launch());
+  CUDA_TRY(ctx, cudaEventRecord(ctx->ev[1], ctx->stream));
+  CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  *ms_per_launch = elapsed(ctx->ev[0], ctx->ev[1]) / reps;
+  return HDG_OK;
+}
+
+}  // extern "C"

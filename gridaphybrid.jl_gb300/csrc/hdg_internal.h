@@ -1,0 +1,171 @@
+// hdg_internal.h -- internal types of libgridaphybrid_gb300 (not installed).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/hdg_gb300.h"
+
+namespace hdg {
+
+constexpr int kMaxD = 3;
+constexpr int kMaxK = 4;
+
+// ---------------------------------------------------------------------------
+// Device buffer owned by a context or problem.
+// ---------------------------------------------------------------------------
+struct DBuf {
+  void *ptr = nullptr;
+  size_t bytes = 0;
+  DBuf() = default;
+  DBuf(const DBuf &) = delete;
+  DBuf &operator=(const DBuf &) = delete;
+  ~DBuf() { release(); }
+  void release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+  }
+  // grows (never shrinks); returns cudaSuccess or the allocation error
+  cudaError_t reserve(size_t nbytes) {
+    if (nbytes <= bytes && ptr) return cudaSuccess;
+    release();
+    if (nbytes == 0) nbytes = 16;
+    cudaError_t e = cudaMalloc(&ptr, nbytes);
+    if (e != cudaSuccess) {
+      ptr = nullptr;
+      return e;
+    }
+    bytes = nbytes;
+    return cudaSuccess;
+  }
+  template <typename T>
+  T *as() const {
+    return static_cast<T *>(ptr);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Reference-element tables (host FP64).  The quadrature sums over reference
+// points are contracted once; on an affine cell with cell-constant
+// coefficients the cell integrals are these tables times per-cell scalars.
+// ---------------------------------------------------------------------------
+struct RefTables {
+  int D = 0, k = 0, nk = 0, nfd = 0, ni = 0, nf = 0, n = 0, n1 = 0, nqv = 0;
+  std::vector<int> lat;    // nk x D cell node lattice (Gridap node order)
+  std::vector<int> flat;   // nfd x (D-1) facet node lattice
+  std::vector<double> M;   // nk x nk      int phi_a phi_b
+  std::vector<double> G;   // D x nk x nk  int d_e phi_a phi_b
+  std::vector<double> F;   // 2D x nk x nk int_F phi_a phi_b (unit facet measure)
+  std::vector<double> H;   // 2D x nk x nfd int_F phi_a mu_b
+  std::vector<double> L;   // nfd x nfd    int_F mu_a mu_b
+  std::vector<double> qxi; // nqv x D volume points
+  std::vector<double> qw;  // nqv
+  std::vector<double> qphi;// nqv x nk
+};
+int build_ref_tables(int D, int k, RefTables &t);
+
+// Offsets (in doubles) of each table inside the packed device table buffer.
+struct TableOffsets {
+  int M, G, F, H, L, qxi, qw, qphi, total;
+};
+TableOffsets pack_tables(const RefTables &t, std::vector<double> &packed);
+
+// ---------------------------------------------------------------------------
+// Mesh + skeleton space + assembly pattern (host side, built once).
+// ---------------------------------------------------------------------------
+struct HostMesh {
+  int D = 0, k = 0, ncells = 0, nfacets = 0, nfd = 0, nfree = 0, ndir = 0;
+  bool cartesian = false;
+  int cells[kMaxD] = {0, 0, 0};
+  double domain[2 * kMaxD] = {0, 0, 0, 0, 0, 0};
+  std::vector<double> origin;     // ncells x D
+  std::vector<double> jac;        // ncells x D x D (column-major per cell)
+  std::vector<int> cell_facets;   // ncells x 2D
+  std::vector<int> facet_dofs;    // nfacets x nfd
+  std::vector<int> facet_cell;    // nfacets x 2 : cells around (first = owner), -1
+  std::vector<int> facet_lface;   // nfacets x 2 : local facet index in that cell
+  std::vector<int> facet_first_dof; // nfacets: first free DOF or -1
+};
+int build_cartesian_mesh(int D, const int *cells, const double *domain, int k,
+                         HostMesh &m, std::string &err);
+int finish_mesh(HostMesh &m, std::string &err);  // derives facet_cell etc.
+
+// Skeleton CSR pattern and the block maps used by the deterministic gather.
+struct HostPattern {
+  int nrows = 0;
+  int64_t nnz = 0;
+  int nblockrows = 0;                // free facets
+  int64_t nblocks = 0;
+  std::vector<int64_t> rowptr;       // nrows+1
+  std::vector<int32_t> colind;       // nnz
+  std::vector<int> br_facet;         // block row -> facet
+  std::vector<int> br_row0;          // block row -> first row (free DOF)
+  std::vector<int> br_src;           // block row -> 2 x (cell*2D + lf) or -1 (rhs)
+  std::vector<int64_t> blk_off;      // block -> val offset of entry (0,0)
+  std::vector<int> blk_rowlen;       // block -> row length of its block row
+  std::vector<int> blk_src;          // block -> 2 x (cell*(2D)^2 + lf_row*2D + lf_col) or -1
+  std::vector<int> diag_blk;         // block row -> index of its diagonal block
+  std::vector<int> dir_cells;        // cells touching a Dirichlet DOF
+  int max_rowlen = 0;                // longest skeleton row
+};
+int build_pattern(const HostMesh &m, HostPattern &p, std::string &err);
+
+}  // namespace hdg
+
+// ---------------------------------------------------------------------------
+// Public opaque types.
+// ---------------------------------------------------------------------------
+struct hdg_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  long long launches = 0;
+  int num_sms = 0;
+  size_t smem_optin = 0;
+  hdg::DBuf scratch[6];  // Map-level staging buffers
+  cudaEvent_t ev[8] = {nullptr};
+  cudaEvent_t user_ev[4] = {nullptr};
+  int fail(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    err = buf;
+    return code;
+  }
+};
+
+struct hdg_problem {
+  hdg_context *ctx = nullptr;
+  hdg::HostMesh mesh;
+  hdg::RefTables tab;
+  hdg::TableOffsets toff{};
+  hdg::HostPattern pat;
+  int stab_mode = HDG_STAB_TEXTBOOK;
+  int problem = HDG_PROBLEM_LINEAR;
+  double tau = 1.0;
+  bool form_set = false, assembled = false, solved = false, recovered = false;
+  int precision = HDG_PREC_FP64;
+  double timings[5] = {0, 0, 0, 0, 0};
+  int last_iters = 0;
+  double last_relres = 0.0;
+  // device state
+  hdg::DBuf d_tab, d_origin, d_jac, d_cell_facets, d_facet_dofs, d_facet_cell;
+  hdg::DBuf d_kappa, d_dirvals;
+  hdg::DBuf d_A, d_b, d_S, d_g, d_fact, d_info, d_aux;
+  hdg::DBuf d_rowptr, d_colind, d_val, d_rhs;
+  hdg::DBuf d_br_row0, d_br_src, d_blk_off, d_blk_rowlen, d_blk_src, d_diag_blk,
+      d_dir_cells;
+  hdg::DBuf d_Binv, d_x, d_r, d_z, d_p, d_q, d_partials, d_scal;
+  hdg::DBuf d_uint;
+  hdg::DBuf h_pinned;  // host staging
+  cudaGraphExec_t pcg_graph = nullptr;
+  int pcg_graph_chunk = 0;
+  ~hdg_problem();
+};

@@ -1,0 +1,138 @@
+// hdg_kernels.h -- launch wrappers of the sm_103a kernels (host-callable).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace hdg {
+
+// Exact solutions / sources of the built-in manufactured problems, shared by
+// the kernels and the host-side Dirichlet interpolation.
+//   kappa^{-1} q + grad p = f_u,  div q = g.
+#if defined(__CUDACC__)
+#define HDG_HD __host__ __device__ __forceinline__
+#else
+#define HDG_HD inline
+#endif
+HDG_HD void exact_solution(int problem, int D, const double *x, double kappa,
+                           double &p, double *q, double *fu, double &g) {
+  const double pi = 3.14159265358979323846;
+  if (problem == 0) {  // test/DarcyHDGTests.jl:8-13
+    p = -3.14;
+    for (int d = 0; d < D; ++d) {
+      q[d] = 1.0 + x[d];
+      fu[d] = q[d] / kappa;
+    }
+    g = (double)D;
+  } else if (problem == 1) {
+    p = 0.0;
+    for (int d = 0; d < D; ++d) {
+      p += x[d];
+      q[d] = -kappa;
+      fu[d] = 0.0;
+    }
+    g = 0.0;
+  } else {
+    double s[3], c[3], prod = 1.0;
+    for (int d = 0; d < D; ++d) {
+      s[d] = sin(pi * x[d]);
+      c[d] = cos(pi * x[d]);
+      prod *= s[d];
+    }
+    p = prod;
+    for (int d = 0; d < D; ++d) {
+      double gd = pi * c[d];
+      for (int e = 0; e < D; ++e)
+        if (e != d) gd *= s[e];
+      q[d] = -kappa * gd;
+      fu[d] = 0.0;
+    }
+    g = kappa * D * pi * pi * prod;
+  }
+}
+
+// Everything the cell kernels read, as plain device pointers.
+struct CellArgs {
+  int D, k, nk, nfd, ni, nf, n, nqv, ncells;
+  const double *M, *G, *F, *H, *L, *qxi, *qw, *qphi;  // reference tables
+  const double *origin, *jac, *kappa;                // per cell
+  const int *cell_facets, *facet_cell;               // topology
+  const int *facet_dofs;
+  double tau;
+  int stab_mode, problem;
+};
+
+// FP64 integration of the cell matrices/vectors (column-major n x n, n).
+cudaError_t launch_integrate_fp64(const CellArgs &a, double *A, double *b,
+                                  cudaStream_t s, int num_sms, long long *launches);
+// FP64 condensation of caller-provided cells.  fact (ncells x ni x (n+1)) may
+// be null; it receives [U11 | U12 | y] for the recovery.
+cudaError_t launch_condense_fp64(int ncells, int ni, int nf, const double *A,
+                                 const double *b, double *S, double *g,
+                                 double *fact, int *info, cudaStream_t s,
+                                 int num_sms, long long *launches);
+// Map-level backward condensation (refactorises A_ii, as the reference map).
+cudaError_t launch_backward_fp64(int ncells, int ni, int nf, const double *A,
+                                 const double *b, const double *x, double *u,
+                                 int *info, cudaStream_t s, int num_sms,
+                                 long long *launches);
+// Recovery from stored factors and the global skeleton solution.
+cudaError_t launch_recover_fp64(const CellArgs &a, const double *fact,
+                                const double *lambda, const double *dirvals,
+                                double *uint, cudaStream_t s, int num_sms,
+                                long long *launches);
+cudaError_t launch_sum_facets(int nitems, int nfacets, int len,
+                              const double *blocks, double *out, cudaStream_t s,
+                              long long *launches);
+// Per-cell squared L2 errors -> errs[2*ncells]
+cudaError_t launch_l2_errors(const CellArgs &a, const double *uint, double *errs,
+                             cudaStream_t s, int num_sms, long long *launches);
+
+// Mixed precision (FP32 LU + float-float refinement) fused cell kernel.
+struct MixedOut {
+  double *S, *g;      // condensed block / vector (FP64)
+  float *fact;        // FP32 factors for the recovery, or null
+  int *info;
+};
+
+// Skeleton side --------------------------------------------------------------
+struct AssembleArgs {
+  int nf, nfd, nl, nblockrows, ncells;
+  int64_t nblocks;
+  const int64_t *blk_off;
+  const int *blk_rowlen, *blk_src, *br_row0, *br_src;
+  const int *dir_cells;
+  int ndir_cells;
+  const int *cell_facets, *facet_dofs;
+  const double *dirvals;
+};
+cudaError_t launch_assemble(const AssembleArgs &a, const double *S,
+                            const double *g, double *glift, double *val,
+                            double *rhs, cudaStream_t s, int num_sms,
+                            long long *launches);
+
+struct PcgArgs {
+  int n, nfd, nblockrows;
+  const int64_t *rowptr;
+  const int *colind;
+  const double *val;
+  const double *rhs;
+  double *Binv, *x, *r, *z, *p, *q, *partials, *scal;
+  int nparts;
+  const int *diag_blk;
+  const int64_t *blk_off;
+  const int *blk_rowlen;
+  double sign;
+};
+cudaError_t launch_pcg_setup(const PcgArgs &a, double rtol, cudaStream_t s,
+                             int num_sms, long long *launches);
+cudaError_t launch_pcg_iteration(const PcgArgs &a, cudaStream_t s, int num_sms,
+                                 long long *launches);
+// one skeleton SpMV q = sign*A p (+ partial dots), as launched inside PCG
+cudaError_t launch_spmv(const PcgArgs &a, cudaStream_t s, long long *launches);
+// dense LU solve of a CSR system (small n), one CTA
+cudaError_t launch_dense_solve(int n, const int64_t *rowptr, const int *colind,
+                               const double *val, const double *rhs, double *work,
+                               double *x, int *info, cudaStream_t s,
+                               long long *launches);
+
+}  // namespace hdg

@@ -1,0 +1,510 @@
+// k_skeleton.cu -- skeleton-side kernels for sm_103a: deterministic assembly
+// of the condensed cell blocks into the skeleton CSR matrix (gather through
+// precomputed per-block source maps, no atomics), the Dirichlet lift, a
+// facet-block-Jacobi PCG whose scalars never leave the device, and a dense LU
+// solve for small (possibly indefinite) skeleton systems.
+#include <cuda_runtime.h>
+
+#include "hdg_kernels.h"
+
+namespace hdg {
+
+// ---------------------------------------------------------------------------
+// Assembly.
+// ---------------------------------------------------------------------------
+
+// glift_c -= S_c x_D for every cell touching a Dirichlet facet (the lift of
+// Gridap's _attach_dirichlet, src/HybridAffineFEOperators.jl:41-42).
+__global__ void dirichlet_lift_kernel(AssembleArgs a, const double *__restrict__ S,
+                                      double *glift) {
+  const int nf = a.nf, nfd = a.nfd, nl = a.nl;
+  __shared__ double xd[6 * 64];
+  for (int t = blockIdx.x; t < a.ndir_cells; t += gridDim.x) {
+    const int c = a.dir_cells[t];
+    for (int j = threadIdx.x; j < nf; j += blockDim.x) {
+      const int lf = j / nfd, b = j - lf * nfd;
+      const int id = a.facet_dofs[(size_t)a.cell_facets[(size_t)c * nl + lf] * nfd + b];
+      xd[j] = id < 0 ? a.dirvals[-1 - id] : 0.0;
+    }
+    __syncthreads();
+    const double *Sc = S + (size_t)c * nf * nf;
+    for (int i = threadIdx.x; i < nf; i += blockDim.x) {
+      double v = glift[(size_t)c * nf + i];
+      for (int j = 0; j < nf; ++j) v -= Sc[i + (size_t)nf * j] * xd[j];
+      glift[(size_t)c * nf + i] = v;
+    }
+    __syncthreads();
+  }
+}
+
+// One warp per skeleton block (f,g): val = sum over the (one or two)
+// contributing cells of their condensed sub-block, cells in increasing order.
+__global__ void assemble_blocks_kernel(AssembleArgs a, const double *__restrict__ S,
+                                       double *__restrict__ val) {
+  const int lane = threadIdx.x & 31;
+  const int64_t wid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const int nf = a.nf, nfd = a.nfd, nl = a.nl, nb = nfd * nfd;
+  for (int64_t blk = wid; blk < a.nblocks; blk += nw) {
+    const int64_t off = a.blk_off[blk];
+    const int rowlen = a.blk_rowlen[blk];
+    const int s0 = a.blk_src[2 * blk], s1 = a.blk_src[2 * blk + 1];
+    const double *S0 = S + (size_t)(s0 / (nl * nl)) * nf * nf;
+    const int r0 = ((s0 / nl) % nl) * nfd, c0 = (s0 % nl) * nfd;
+    const double *S1 = nullptr;
+    int r1 = 0, c1 = 0;
+    if (s1 >= 0) {
+      S1 = S + (size_t)(s1 / (nl * nl)) * nf * nf;
+      r1 = ((s1 / nl) % nl) * nfd;
+      c1 = (s1 % nl) * nfd;
+    }
+    for (int e = lane; e < nb; e += 32) {
+      const int ra = e / nfd, cb = e - ra * nfd;
+      double v = S0[(r0 + ra) + (size_t)nf * (c0 + cb)];
+      if (S1) v += S1[(r1 + ra) + (size_t)nf * (c1 + cb)];
+      val[off + (int64_t)ra * rowlen + cb] = v;
+    }
+  }
+}
+
+__global__ void assemble_rhs_kernel(AssembleArgs a, const double *__restrict__ glift,
+                                    double *rhs) {
+  const int nfd = a.nfd, nf = a.nf, nl = a.nl;
+  const int nrows = a.nblockrows * nfd;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nrows; r += gridDim.x * blockDim.x) {
+    const int br = r / nfd, i = r - br * nfd;
+    double v = 0.0;
+    for (int s = 0; s < 2; ++s) {
+      const int src = a.br_src[2 * br + s];
+      if (src < 0) continue;
+      const int c = src / nl, lf = src - c * nl;
+      v += glift[(size_t)c * nf + lf * nfd + i];
+    }
+    rhs[a.br_row0[br] + i] = v;
+  }
+}
+
+cudaError_t launch_assemble(const AssembleArgs &a, const double *S, const double *g,
+                            double *glift, double *val, double *rhs, cudaStream_t s,
+                            int num_sms, long long *launches) {
+  if (a.nf > 6 * 64) return cudaErrorInvalidValue;
+  cudaError_t e = cudaMemcpyAsync(glift, g, sizeof(double) * (size_t)a.ncells * a.nf,
+                                  cudaMemcpyDeviceToDevice, s);
+  if (e != cudaSuccess) return e;
+  if (a.ndir_cells > 0) {
+    int grid = a.ndir_cells < num_sms * 8 ? a.ndir_cells : num_sms * 8;
+    dirichlet_lift_kernel<<<grid, 64, 0, s>>>(a, S, glift);
+    ++*launches;
+  }
+  {
+    int64_t warps = a.nblocks;
+    int64_t grid = (warps * 32 + 255) / 256;
+    if (grid > (int64_t)num_sms * 16) grid = (int64_t)num_sms * 16;
+    if (grid < 1) grid = 1;
+    assemble_blocks_kernel<<<(int)grid, 256, 0, s>>>(a, S, val);
+    ++*launches;
+  }
+  {
+    int nrows = a.nblockrows * a.nfd;
+    int grid = (nrows + 255) / 256;
+    if (grid > num_sms * 8) grid = num_sms * 8;
+    if (grid < 1) grid = 1;
+    assemble_rhs_kernel<<<grid, 256, 0, s>>>(a, glift, rhs);
+    ++*launches;
+  }
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// PCG on (sign*A) x = sign*rhs with facet-block-Jacobi preconditioning.
+// Device scalars (scal[]):
+enum {
+  SC_RZ = 0,     // (r, z)
+  SC_PAP = 1,    // (p, A p)
+  SC_ALPHA = 2,
+  SC_BETA = 3,
+  SC_RR = 4,     // (r, r)
+  SC_BB = 5,     // (b, b)
+  SC_TOL2 = 6,   // rtol^2 (b, b)
+  SC_DONE = 7,   // 1 once converged
+  SC_ITERS = 8,  // completed iterations
+  SC_NSCAL = 16
+};
+// Every kernel of an iteration is a no-op once SC_DONE is set, so a CUDA graph
+// of a fixed number of iterations can be replayed until convergence.
+// ---------------------------------------------------------------------------
+
+constexpr int kPcgThreads = 256;
+
+__device__ __forceinline__ double block_sum(double v, double *red) {
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += red[i];
+  return s;  // valid in thread 0
+}
+
+// Inverse of each facet's diagonal block of sign*A (Gauss-Jordan, partial pivoting).
+__global__ void binv_kernel(PcgArgs a) {
+  const int nfd = a.nfd;
+  double M[25 * 25], I[25 * 25];
+  for (int br = blockIdx.x * blockDim.x + threadIdx.x; br < a.nblockrows;
+       br += gridDim.x * blockDim.x) {
+    const int blk = a.diag_blk[br];
+    const int64_t off = a.blk_off[blk];
+    const int rl = a.blk_rowlen[blk];
+    for (int i = 0; i < nfd; ++i)
+      for (int j = 0; j < nfd; ++j) {
+        M[i * nfd + j] = a.sign * a.val[off + (int64_t)i * rl + j];
+        I[i * nfd + j] = (i == j) ? 1.0 : 0.0;
+      }
+    for (int c = 0; c < nfd; ++c) {
+      int pr = c;
+      for (int i = c + 1; i < nfd; ++i)
+        if (fabs(M[i * nfd + c]) > fabs(M[pr * nfd + c])) pr = i;
+      if (M[pr * nfd + c] == 0.0) {
+        for (int i = 0; i < nfd * nfd; ++i) I[i] = (i % (nfd + 1) == 0) ? 1.0 : 0.0;
+        break;
+      }
+      if (pr != c)
+        for (int j = 0; j < nfd; ++j) {
+          double t = M[c * nfd + j];
+          M[c * nfd + j] = M[pr * nfd + j];
+          M[pr * nfd + j] = t;
+          t = I[c * nfd + j];
+          I[c * nfd + j] = I[pr * nfd + j];
+          I[pr * nfd + j] = t;
+        }
+      const double piv = 1.0 / M[c * nfd + c];
+      for (int j = 0; j < nfd; ++j) {
+        M[c * nfd + j] *= piv;
+        I[c * nfd + j] *= piv;
+      }
+      for (int i = 0; i < nfd; ++i) {
+        if (i == c) continue;
+        const double fct = M[i * nfd + c];
+        if (fct != 0.0)
+          for (int j = 0; j < nfd; ++j) {
+            M[i * nfd + j] -= fct * M[c * nfd + j];
+            I[i * nfd + j] -= fct * I[c * nfd + j];
+          }
+      }
+    }
+    for (int i = 0; i < nfd * nfd; ++i) a.Binv[(size_t)br * nfd * nfd + i] = I[i];
+  }
+}
+
+// z = Binv r for the block rows handled by this CTA (rows staged in smem).
+// Called with blockDim.x = rows_per_cta*nfd.
+__device__ __forceinline__ double apply_binv(const PcgArgs &a, int row, int nrows,
+                                             double rval, double *rs) {
+  const int nfd = a.nfd;
+  rs[threadIdx.x] = rval;
+  __syncthreads();
+  double z = 0.0;
+  if (row < nrows) {
+    const int lr = threadIdx.x, br = row / nfd, i = row - br * nfd;
+    const int first = lr - i;
+    const double *B = a.Binv + (size_t)br * nfd * nfd + (size_t)i * nfd;
+    for (int j = 0; j < nfd; ++j) z += B[j] * rs[first + j];
+  }
+  __syncthreads();
+  return z;
+}
+
+__global__ void pcg_init_kernel(PcgArgs a) {
+  __shared__ double rs[1024];
+  __shared__ double red[32];
+  const int tile = (blockDim.x / a.nfd) * a.nfd;
+  double rz = 0.0, rr = 0.0, bb = 0.0;
+  for (int base = blockIdx.x * tile; base < a.n; base += gridDim.x * tile) {
+    const int row = base + (int)threadIdx.x;
+    const bool act = threadIdx.x < (unsigned)tile && row < a.n;
+    double r = 0.0;
+    if (act) {
+      const double b = a.rhs[row];
+      r = a.sign * b;
+      a.x[row] = 0.0;
+      a.r[row] = r;
+      bb += b * b;
+      rr += r * r;
+    }
+    double z = apply_binv(a, act ? row : a.n, a.n, r, rs);
+    if (act) {
+      a.z[row] = z;
+      a.p[row] = z;
+      rz += r * z;
+    }
+  }
+  double s;
+  s = block_sum(rz, red);
+  if (threadIdx.x == 0) a.partials[blockIdx.x] = s;
+  s = block_sum(rr, red);
+  if (threadIdx.x == 0) a.partials[a.nparts + blockIdx.x] = s;
+  s = block_sum(bb, red);
+  if (threadIdx.x == 0) a.partials[2 * a.nparts + blockIdx.x] = s;
+}
+
+__global__ void pcg_init_reduce_kernel(PcgArgs a, double rtol) {
+  __shared__ double red[32];
+  double v[3];
+  for (int k = 0; k < 3; ++k) {
+    double s = 0.0;
+    for (int i = threadIdx.x; i < a.nparts; i += blockDim.x) s += a.partials[k * a.nparts + i];
+    v[k] = block_sum(s, red);
+  }
+  if (threadIdx.x == 0) {
+    a.scal[SC_RZ] = v[0];
+    a.scal[SC_RR] = v[1];
+    a.scal[SC_BB] = v[2];
+    a.scal[SC_TOL2] = rtol * rtol * v[2];
+    a.scal[SC_ITERS] = 0.0;
+    a.scal[SC_DONE] = (v[1] <= rtol * rtol * v[2]) ? 1.0 : 0.0;
+  }
+}
+
+// q = sign*A p, partial (p, q).  One warp per facet block row: the nfd rows
+// of a free facet share one column list (the DOFs of the facets sharing a cell
+// with it), so the warp reads that list once, gathers p into shared memory,
+// and streams the block row's nfd*rowlen contiguous values.
+constexpr int kMaxRowLen = 288;  // 11 neighbour facets x 25 DOFs (3D, k=4) fits
+__global__ void __launch_bounds__(kPcgThreads) pcg_spmv_kernel(PcgArgs a) {
+  __shared__ double red[32];
+  __shared__ double xs[kPcgThreads / 32][kMaxRowLen];
+  if (a.scal[SC_DONE] != 0.0) return;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  const int nfd = a.nfd;
+  double acc = 0.0;
+  for (int br = wid; br < a.nblockrows; br += nw) {
+    const int row0 = br * nfd;
+    const int64_t base = a.rowptr[row0];
+    const int rowlen = (int)(a.rowptr[row0 + 1] - base);
+    for (int j = lane; j < rowlen; j += 32) xs[w][j] = a.p[a.colind[base + j]];
+    __syncwarp();
+    for (int r = 0; r < nfd; ++r) {
+      const double *vr = a.val + base + (int64_t)r * rowlen;
+      double s = 0.0;
+      for (int j = lane; j < rowlen; j += 32) s += __ldcs(vr + j) * xs[w][j];
+      for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
+      if (lane == 0) {
+        const double q = a.sign * s;
+        a.q[row0 + r] = q;
+        acc += q * a.p[row0 + r];
+      }
+    }
+    __syncwarp();
+  }
+  const double t = block_sum(acc, red);
+  if (threadIdx.x == 0) a.partials[blockIdx.x] = t;
+}
+
+__global__ void pcg_alpha_kernel(PcgArgs a) {
+  __shared__ double red[32];
+  if (a.scal[SC_DONE] != 0.0) return;
+  double s = 0.0;
+  for (int i = threadIdx.x; i < a.nparts; i += blockDim.x) s += a.partials[i];
+  s = block_sum(s, red);
+  if (threadIdx.x == 0) {
+    a.scal[SC_PAP] = s;
+    a.scal[SC_ALPHA] = a.scal[SC_RZ] / s;
+  }
+}
+
+// x += alpha p; r -= alpha q; z = Binv r; partial (r,z), (r,r)
+__global__ void pcg_update_kernel(PcgArgs a) {
+  __shared__ double rs[1024];
+  __shared__ double red[32];
+  if (a.scal[SC_DONE] != 0.0) return;
+  const double alpha = a.scal[SC_ALPHA];
+  const int tile = (blockDim.x / a.nfd) * a.nfd;
+  double rz = 0.0, rr = 0.0;
+  for (int base = blockIdx.x * tile; base < a.n; base += gridDim.x * tile) {
+    const int row = base + (int)threadIdx.x;
+    const bool act = threadIdx.x < (unsigned)tile && row < a.n;
+    double r = 0.0;
+    if (act) {
+      a.x[row] += alpha * a.p[row];
+      r = a.r[row] - alpha * a.q[row];
+      a.r[row] = r;
+      rr += r * r;
+    }
+    const double z = apply_binv(a, act ? row : a.n, a.n, r, rs);
+    if (act) {
+      a.z[row] = z;
+      rz += r * z;
+    }
+  }
+  double s = block_sum(rz, red);
+  if (threadIdx.x == 0) a.partials[blockIdx.x] = s;
+  s = block_sum(rr, red);
+  if (threadIdx.x == 0) a.partials[a.nparts + blockIdx.x] = s;
+}
+
+__global__ void pcg_beta_kernel(PcgArgs a) {
+  __shared__ double red[32];
+  if (a.scal[SC_DONE] != 0.0) return;
+  double v[2];
+  for (int k = 0; k < 2; ++k) {
+    double s = 0.0;
+    for (int i = threadIdx.x; i < a.nparts; i += blockDim.x) s += a.partials[k * a.nparts + i];
+    v[k] = block_sum(s, red);
+  }
+  if (threadIdx.x == 0) {
+    a.scal[SC_BETA] = v[0] / a.scal[SC_RZ];
+    a.scal[SC_RZ] = v[0];
+    a.scal[SC_RR] = v[1];
+    a.scal[SC_ITERS] += 1.0;
+    if (v[1] <= a.scal[SC_TOL2]) a.scal[SC_DONE] = 1.0;
+  }
+}
+
+// p = z + beta p (runs in the converging iteration too; harmless)
+__global__ void pcg_p_kernel(PcgArgs a) {
+  if (a.scal[SC_DONE] != 0.0) return;
+  const double beta = a.scal[SC_BETA];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x)
+    a.p[i] = a.z[i] + beta * a.p[i];
+}
+
+// Threads of the vector-update kernels: a tile of whole facet blocks
+// (kPcgThreads / nfd * nfd rows) rounded up to full warps -- block_sum's
+// full-mask shuffles need every lane of every warp to exist.
+static int update_threads(int nfd) {
+  (void)nfd;
+  return kPcgThreads;
+}
+
+cudaError_t launch_pcg_setup(const PcgArgs &a, double rtol, cudaStream_t s,
+                             int num_sms, long long *launches) {
+  if (a.nfd > 25) return cudaErrorInvalidValue;
+  int g = (a.nblockrows + 127) / 128;
+  if (g < 1) g = 1;
+  binv_kernel<<<g, 128, 0, s>>>(a);
+  pcg_init_kernel<<<a.nparts, update_threads(a.nfd), 0, s>>>(a);
+  pcg_init_reduce_kernel<<<1, 1024, 0, s>>>(a, rtol);
+  *launches += 3;
+  (void)num_sms;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_spmv(const PcgArgs &a, cudaStream_t s, long long *launches) {
+  pcg_spmv_kernel<<<a.nparts, kPcgThreads, 0, s>>>(a);
+  ++*launches;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pcg_iteration(const PcgArgs &a, cudaStream_t s, int num_sms,
+                                 long long *launches) {
+  pcg_spmv_kernel<<<a.nparts, kPcgThreads, 0, s>>>(a);
+  pcg_alpha_kernel<<<1, 1024, 0, s>>>(a);
+  pcg_update_kernel<<<a.nparts, update_threads(a.nfd), 0, s>>>(a);
+  pcg_beta_kernel<<<1, 1024, 0, s>>>(a);
+  pcg_p_kernel<<<a.nparts, 256, 0, s>>>(a);
+  *launches += 5;
+  (void)num_sms;
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Dense LU solve (small systems; any sign/definiteness): one CTA, the
+// augmented matrix [A | b] in global scratch (column-major, ld = n).
+// ---------------------------------------------------------------------------
+__global__ void dense_fill_kernel(int n, const int64_t *rowptr, const int *colind,
+                                  const double *val, const double *rhs, double *W) {
+  const size_t total = (size_t)n * (n + 1);
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total;
+       e += (size_t)gridDim.x * blockDim.x)
+    W[e] = 0.0;
+}
+
+__global__ void dense_scatter_kernel(int n, const int64_t *rowptr, const int *colind,
+                                     const double *val, const double *rhs, double *W) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+    for (int64_t p = rowptr[r]; p < rowptr[r + 1]; ++p) W[r + (size_t)n * colind[p]] = val[p];
+    W[r + (size_t)n * n] = rhs[r];
+  }
+}
+
+__global__ void __launch_bounds__(1024) dense_lu_kernel(int n, double *W, double *x, int *info) {
+  __shared__ int s_piv;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int inf = 0;
+  for (int j = 0; j < n; ++j) {
+    if (warp == 0) {
+      double best = -1.0;
+      int bi = j;
+      for (int i = j + lane; i < n; i += 32) {
+        double v = fabs(W[i + (size_t)n * j]);
+        if (v > best) {
+          best = v;
+          bi = i;
+        }
+      }
+      for (int off = 16; off > 0; off >>= 1) {
+        double ov = __shfl_down_sync(0xffffffffu, best, off);
+        int oi = __shfl_down_sync(0xffffffffu, bi, off);
+        if (ov > best || (ov == best && oi < bi)) {
+          best = ov;
+          bi = oi;
+        }
+      }
+      if (lane == 0) s_piv = best > 0.0 ? bi : -1;
+    }
+    __syncthreads();
+    const int p = s_piv;
+    if (p < 0) {
+      if (!inf) inf = j + 1;
+      __syncthreads();
+      continue;
+    }
+    if (p != j)
+      for (int c = j + threadIdx.x; c <= n; c += blockDim.x) {
+        double t = W[j + (size_t)n * c];
+        W[j + (size_t)n * c] = W[p + (size_t)n * c];
+        W[p + (size_t)n * c] = t;
+      }
+    __syncthreads();
+    const double r = 1.0 / W[j + (size_t)n * j];
+    for (int i = j + 1 + threadIdx.x; i < n; i += blockDim.x) W[i + (size_t)n * j] *= r;
+    __syncthreads();
+    for (int c = j + 1 + warp; c <= n; c += nw) {
+      const double u = W[j + (size_t)n * c];
+      if (u != 0.0)
+        for (int i = j + 1 + lane; i < n; i += 32) W[i + (size_t)n * c] -= W[i + (size_t)n * j] * u;
+    }
+    __syncthreads();
+  }
+  double *rhs = W + (size_t)n * n;
+  for (int j = n - 1; j >= 0; --j) {
+    __syncthreads();
+    const double diag = W[j + (size_t)n * j];
+    const double uj = diag != 0.0 ? rhs[j] / diag : 0.0;
+    __syncthreads();
+    if (threadIdx.x == 0) rhs[j] = uj;
+    for (int i = threadIdx.x; i < j; i += blockDim.x) rhs[i] -= W[i + (size_t)n * j] * uj;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = rhs[i];
+  if (threadIdx.x == 0) *info = inf;
+}
+
+cudaError_t launch_dense_solve(int n, const int64_t *rowptr, const int *colind,
+                               const double *val, const double *rhs, double *work,
+                               double *x, int *info, cudaStream_t s, long long *launches) {
+  int g = (int)(((size_t)n * (n + 1) + 255) / 256);
+  if (g > 4096) g = 4096;
+  if (g < 1) g = 1;
+  dense_fill_kernel<<<g, 256, 0, s>>>(n, rowptr, colind, val, rhs, work);
+  dense_scatter_kernel<<<(n + 255) / 256 > 0 ? (n + 255) / 256 : 1, 256, 0, s>>>(n, rowptr, colind, val, rhs, work);
+  dense_lu_kernel<<<1, 1024, 0, s>>>(n, work, x, info);
+  *launches += 3;
+  return cudaGetLastError();
+}
+
+}  // namespace hdg

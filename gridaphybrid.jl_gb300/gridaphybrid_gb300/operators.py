@@ -1,0 +1,279 @@
+"""HybridAffineFEOperator / solve on the GPU (the operator level of GridapHybrid.jl).
+
+Mirrors the reference's user API (test/DarcyHDGTests.jl:27-142):
+
+    model = CartesianDiscreteModel((0,1,0,1), (2,2))
+    dK    = Skeleton(model)
+    reffe_u = ReferenceFE(lagrangian, VectorValue, order)  ...
+    V = TestFESpace(Omega, reffe_u, conformity="L2") ...
+    X = MultiFieldFESpace([U, P, L]);  Y = MultiFieldFESpace([V, Q, M])
+    op = HybridAffineFEOperator(DarcyHDG(tau=1.0), X, Y, [1, 2], [3])
+    xh = solve(op)
+
+Python cannot evaluate Gridap weak-form closures, so the weak form is a
+descriptor of the Darcy HDG form the reference's tests write out
+(test/DarcyHDGTests.jl:125-135), with the textbook stabilisation as an option
+and a per-cell permeability.  Integration, condensation, assembly, the
+skeleton solve and the recovery all run in libgridaphybrid_gb300.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+
+lagrangian = "lagrangian"
+VectorValue = "VectorValue"
+Float64 = "Float64"
+
+
+class CartesianDiscreteModel:
+    """CartesianDiscreteModel(domain, partition): uniform quads/hexes, cells
+    numbered lexicographically (x fastest), Gridap's facet numbering."""
+
+    def __init__(self, domain, partition):
+        self.partition = tuple(int(n) for n in partition)
+        self.D = len(self.partition)
+        if self.D not in (2, 3) or len(domain) != 2 * self.D:
+            raise ValueError("domain must be (x0,x1,y0,y1[,z0,z1]) for 2 or 3 dimensions")
+        self.domain = tuple(float(x) for x in domain)
+
+    def num_cell_dims(self):
+        return self.D
+
+    def num_cells(self):
+        return int(np.prod(self.partition))
+
+    def cell_jacobians(self):
+        h = [(self.domain[2 * d + 1] - self.domain[2 * d]) / self.partition[d] for d in range(self.D)]
+        return np.broadcast_to(np.diag(h), (self.num_cells(), self.D, self.D))
+
+
+class Triangulation:
+    def __init__(self, model, dim=None):
+        self.model = model
+        self.dim = model.D if dim is None else dim
+
+
+class SkeletonTriangulation(Triangulation):
+    """Skeleton(model): each cell seen as the set of its facets (src/Skeleton.jl:113-147)."""
+
+    def __init__(self, model):
+        super().__init__(model, model.D - 1)
+
+
+def Skeleton(model):
+    return SkeletonTriangulation(model)
+
+
+def _reference_normals(D):
+    """Outward reference normals in Gridap local facet order [.., y0, y1, x0, x1]."""
+    out = np.zeros((2 * D, D))
+    for lf in range(2 * D):
+        out[lf, D - 1 - lf // 2] = 1.0 if lf % 2 else -1.0
+    return out
+
+
+def get_cell_normal_vector(skel):
+    """Unit outward normal per (cell, local facet): push_normal(J^{-T}, n_ref)
+    (src/Skeleton.jl:524-527, 564-585).  Shape (ncells, 2D, D)."""
+    m = skel.model
+    Jinv_t = np.linalg.inv(np.asarray(m.cell_jacobians())).transpose(0, 2, 1)
+    v = np.einsum("cij,fj->cfi", Jinv_t, _reference_normals(m.D))
+    return v / np.linalg.norm(v, axis=2, keepdims=True)
+
+
+def get_cell_owner_normal_vector(skel, facet_cells=None, cell_facets=None):
+    """The owner cell's outward normal seen from each (cell, local facet): n on the
+    facet's first cell, -n on the other (src/Skeleton.jl:549-556,
+    src/SkeletonArrays.jl:219-229).  The glue comes from the library's topology."""
+    n = get_cell_normal_vector(skel)
+    if facet_cells is None or cell_facets is None:
+        ctx = _lib.default_context()
+        pb = _Problem(ctx, skel.model, 1)
+        cell_facets, facet_cells, _ = pb.topology()
+        pb.close()
+    owner = facet_cells[cell_facets, 0]
+    sign = np.where(owner == np.arange(n.shape[0])[:, None], 1.0, -1.0)
+    return n * sign[:, :, None]
+
+
+class ReferenceFE:
+    def __init__(self, kind, value_type, order, space="Q"):
+        if kind != lagrangian:
+            raise ValueError("only lagrangian reference FEs are supported")
+        if space != "Q":
+            raise ValueError("only Q_k (space='Q') tensor-product Lagrangian spaces are supported")
+        self.value_type = value_type
+        self.order = int(order)
+
+
+class FESpace:
+    def __init__(self, trian, reffe, conformity="L2", dirichlet_tags=None, dirichlet_value=None):
+        if conformity != "L2":
+            raise ValueError("hybridizable spaces are L2-conforming")
+        self.trian = trian
+        self.reffe = reffe
+        self.dirichlet_tags = dirichlet_tags
+        self.dirichlet_value = dirichlet_value
+
+
+def TestFESpace(trian, reffe, conformity="L2", dirichlet_tags=None):
+    return FESpace(trian, reffe, conformity, dirichlet_tags)
+
+
+def TrialFESpace(space, dirichlet_value=None):
+    return FESpace(space.trian, space.reffe, "L2", space.dirichlet_tags, dirichlet_value)
+
+
+class MultiFieldFESpace:
+    def __init__(self, spaces):
+        self.spaces = list(spaces)
+
+    def __getitem__(self, i):
+        return self.spaces[i]
+
+    def __len__(self):
+        return len(self.spaces)
+
+
+class DarcyHDG:
+    """The Darcy HDG weak form of test/DarcyHDGTests.jl:125-135 with a per-cell
+    permeability kappa:
+      (v.u/kappa) - (div v) p - grad(q).u  on Omega,
+      (v.n) l + q(u.n) + tau s q (p - l) + m(u.n) + tau s m (p - l)  on dK,
+    s = n.n_o (stabilization="owner_sign", as the reference test) or 1
+    ("textbook" LDG-H).  `problem` selects the built-in manufactured source,
+    Dirichlet data and exact solution."""
+
+    STABS = {"textbook": _lib.HDG_STAB_TEXTBOOK, "owner_sign": _lib.HDG_STAB_OWNER_SIGN}
+    PROBLEMS = {"ref_linear": _lib.HDG_PROBLEM_REF_LINEAR, "linear": _lib.HDG_PROBLEM_LINEAR,
+                "sin": _lib.HDG_PROBLEM_SIN}
+
+    def __init__(self, tau=1.0, stabilization="textbook", problem="linear", kappa=None):
+        self.tau = float(tau)
+        self.stab = self.STABS[stabilization]
+        self.problem = self.PROBLEMS[problem]
+        self.kappa = None if kappa is None else np.ascontiguousarray(kappa, dtype=np.float64)
+
+
+class _Problem:
+    """Owns an hdg_problem handle."""
+
+    def __init__(self, ctx, model, k):
+        self.ctx = ctx
+        h = ctypes.c_void_p()
+        cells = np.array(model.partition, dtype=np.int32)
+        dom = np.array(model.domain, dtype=np.float64)
+        ctx.check(ctx.lib.hdg_problem_create_cartesian(ctx.handle, model.D, _lib.ptr(cells),
+                                                       _lib.ptr(dom), k, ctypes.byref(h)))
+        self.h = h
+        info = np.zeros(8, dtype=np.int64)
+        ctx.check(ctx.lib.hdg_problem_info(h, _lib.ptr(info)))
+        (self.ncells, self.nfacets, self.ni, self.nf, self.nfree, self.ndir, self.nnz,
+         self.nfd) = (int(v) for v in info)
+        self.D = model.D
+
+    def topology(self):
+        cf = np.empty((self.ncells, 2 * self.D), dtype=np.int32)
+        fc = np.empty((self.nfacets, 2), dtype=np.int32)
+        fd = np.empty((self.nfacets, self.nfd), dtype=np.int32)
+        self.ctx.check(self.ctx.lib.hdg_get_topology(self.h, _lib.ptr(cf), _lib.ptr(fc), _lib.ptr(fd)))
+        return cf, fc, fd
+
+    def close(self):
+        if self.h:
+            self.ctx.lib.hdg_problem_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class HybridAffineFEOperator:
+    """HybridAffineFEOperator(weakform, trial, test, bulk_fields, skeleton_fields)
+    (src/HybridAffineFEOperators.jl:10-50): integrates, condenses every cell
+    (keeping the factors on the GPU) and assembles the skeleton system."""
+
+    def __init__(self, weakform, trial, test, bulk_fields, skeleton_fields,
+                 precision=_lib.HDG_PREC_FP64, context=None):
+        if list(bulk_fields) != [1, 2] or list(skeleton_fields) != [3]:
+            raise ValueError("the Darcy HDG operator expects bulk_fields=[1,2] (flux, pressure) "
+                             "and skeleton_fields=[3] (trace)")
+        self.weakform, self.trial, self.test = weakform, trial, test
+        self.bulk_fields, self.skeleton_fields = list(bulk_fields), list(skeleton_fields)
+        self.precision = precision
+        model = trial[0].trian.model
+        orders = {s.reffe.order for s in trial.spaces}
+        if len(orders) != 1:
+            raise ValueError("flux, pressure and trace must share the order k (Q_k / Q_k / Q_k)")
+        self.k = orders.pop()
+        self.model = model
+        self.ctx = context or _lib.default_context()
+        self.pb = _Problem(self.ctx, model, self.k)
+        c = self.ctx
+        c.check(c.lib.hdg_set_darcy(self.pb.h, weakform.stab, weakform.tau, weakform.problem))
+        c.check(c.lib.hdg_set_permeability(self.pb.h, _lib.ptr(weakform.kappa)))
+        self.info = np.zeros(self.pb.ncells, dtype=np.int32)
+        c.check(c.lib.hdg_assemble(self.pb.h, precision, _lib.ptr(self.info)))
+
+    def skeleton_system(self):
+        """(rowptr, colind, val, rhs) of op.skeleton_op, CSR with sorted columns."""
+        pb, c = self.pb, self.ctx
+        rowptr = np.empty(pb.nfree + 1, dtype=np.int64)
+        colind = np.empty(pb.nnz, dtype=np.int32)
+        val = np.empty(pb.nnz)
+        rhs = np.empty(pb.nfree)
+        c.check(c.lib.hdg_get_skeleton_system(pb.h, _lib.ptr(rowptr), _lib.ptr(colind), _lib.ptr(val),
+                                              _lib.ptr(rhs)))
+        return rowptr, colind, val, rhs
+
+
+class HybridFEFunction:
+    """The multi-field solution: free DOF values in Gridap's layout
+    [flux | pressure | skeleton] plus per-cell views."""
+
+    def __init__(self, op, iters, relres):
+        pb, c = op.pb, op.ctx
+        self.op = op
+        self.iterations = iters
+        self.relres = relres
+        self.free_dof_values = np.empty(pb.ncells * pb.ni + pb.nfree)
+        c.check(c.lib.hdg_get_free_dof_values(pb.h, _lib.ptr(self.free_dof_values)))
+        self.cell_interior = np.empty((pb.ncells, pb.ni))
+        c.check(c.lib.hdg_get_cell_interior_values(pb.h, _lib.ptr(self.cell_interior)))
+        self.skeleton = self.free_dof_values[pb.ncells * pb.ni:]
+
+    def l2_errors(self):
+        """(||q - q_h||, ||p - p_h||) against the problem's exact solution."""
+        ef, ep = ctypes.c_double(), ctypes.c_double()
+        c = self.op.ctx
+        c.check(c.lib.hdg_l2_errors(self.op.pb.h, ctypes.byref(ef), ctypes.byref(ep)))
+        return ef.value, ep.value
+
+
+def solve(op, solver="pcg", rtol=1e-10, maxit=20000):
+    """solve(op::HybridAffineFEOperator) (src/HybridAffineFEOperators.jl:67-100):
+    skeleton solve, then recovery of the interior fields from the stored factors."""
+    s = {"pcg": _lib.HDG_SOLVER_PCG, "direct": _lib.HDG_SOLVER_DIRECT}[solver]
+    it, rel = ctypes.c_int(), ctypes.c_double()
+    c = op.ctx
+    c.check(c.lib.hdg_solve_skeleton(op.pb.h, s, rtol, maxit, ctypes.byref(it), ctypes.byref(rel)))
+    c.check(c.lib.hdg_recover(op.pb.h))
+    return HybridFEFunction(op, it.value, rel.value)
+
+
+def darcy_spaces(model, k):
+    """The spaces of the Darcy HDG test: Q_k flux, Q_k pressure, Q_k trace with
+    Dirichlet facets on the whole boundary (test/DarcyHDGTests.jl:32-52)."""
+    Omega = Triangulation(model)
+    Gamma = Triangulation(model, model.D - 1)
+    V = TestFESpace(Omega, ReferenceFE(lagrangian, VectorValue, k), conformity="L2")
+    Q = TestFESpace(Omega, ReferenceFE(lagrangian, Float64, k), conformity="L2")
+    M = TestFESpace(Gamma, ReferenceFE(lagrangian, Float64, k), conformity="L2", dirichlet_tags="boundary")
+    Y = MultiFieldFESpace([V, Q, M])
+    X = MultiFieldFESpace([TrialFESpace(V), TrialFESpace(Q), TrialFESpace(M, "exact")])
+    return X, Y

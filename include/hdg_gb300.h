@@ -1,0 +1,216 @@
+/*
+ * hdg_gb300.h -- C ABI of the GB300 (sm_103a) cellwise hybridization library
+ * (libgridaphybrid_gb300.so).
+ *
+ * The library replaces, on one GPU, the hot path of GridapHybrid.jl:
+ * per-cell integration of the cell + facet bilinear forms (SumFacetsMap path),
+ * StaticCondensationMap, assembly of the skeleton system, the skeleton solve,
+ * and BackwardStaticCondensationMap.  Each entry point names the reference
+ * interface it stands in for (paths relative to the GridapHybrid.jl repo).
+ *
+ * Conventions
+ *  - Every function returns an int status (HDG_OK == 0).  A failing call
+ *    leaves a message in hdg_last_error(ctx).
+ *  - Pointer arguments may point to host memory (pageable or pinned) or to
+ *    device memory of the context's GPU; the library detects which.  Outputs
+ *    are written when the call returns (calls are synchronous unless noted).
+ *  - Dense cell blocks are column-major (Julia layout).  Per cell the DOF
+ *    order is [interior fields | skeleton fields], the interior fields in
+ *    the order of `bulk_fields` and each field's DOFs in its reference-FE
+ *    order, the skeleton DOFs in cell-local facet order
+ *    (src/HybridAffineFEOperators.jl:424-434).
+ *  - Facet DOF ids follow Gridap's sign convention shifted to 0-based:
+ *    id >= 0 is a free DOF, id < 0 is Dirichlet DOF number (-1 - id).
+ *  - No entry point falls back to the CPU: without a usable sm_103a device
+ *    hdg_context_create fails with HDG_ERR_NODEVICE.
+ */
+#ifndef HDG_GB300_H
+#define HDG_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HDG_OK 0
+#define HDG_ERR_INVALID 1       /* bad argument or size */
+#define HDG_ERR_CUDA 2          /* CUDA runtime error */
+#define HDG_ERR_NOMEM 3         /* device allocation failed */
+#define HDG_ERR_SINGULAR 4      /* zero pivot in a cell's interior block (info > 0) */
+#define HDG_ERR_NOT_CONVERGED 5 /* skeleton solver did not reach the tolerance */
+#define HDG_ERR_STATE 6         /* call out of order (e.g. solve before assemble) */
+#define HDG_ERR_NODEVICE 7      /* no usable CUDA device */
+
+/* Arithmetic of the cell-local work. */
+#define HDG_PREC_FP64 0          /* FP64 integration, LU and Schur complement */
+#define HDG_PREC_FP32_REFINED 1  /* FP32 LU, refined with high-precision residuals */
+
+/* Stabilisation of the Darcy HDG form. */
+#define HDG_STAB_TEXTBOOK 0     /* tau*(p - l) on every facet side (LDG-H) */
+#define HDG_STAB_OWNER_SIGN 1   /* tau*(p - l)*(n.n_o), test/DarcyHDGTests.jl:125-135 */
+
+/* Built-in manufactured problems (sources, Dirichlet data, exact solution). */
+#define HDG_PROBLEM_REF_LINEAR 0 /* u=(1+x,1+y[,1+z]), p=-3.14 (test/DarcyHDGTests.jl:8-13) */
+#define HDG_PROBLEM_LINEAR 1     /* p = x+y[+z], q = -kappa grad p, f = 0 */
+#define HDG_PROBLEM_SIN 2        /* p = prod sin(pi x_d), q = -kappa grad p, f = div q */
+
+/* Skeleton solvers. */
+#define HDG_SOLVER_PCG 0        /* facet-block-Jacobi PCG on -S (SPD forms) */
+#define HDG_SOLVER_DIRECT 1     /* dense LU with partial pivoting (small systems, any form) */
+
+typedef struct hdg_context hdg_context;
+typedef struct hdg_problem hdg_problem;
+
+/* Library version (major*10000 + minor*100 + patch). */
+int hdg_version(void);
+
+/* Context: one GPU, one stream, a device memory pool.  One context per host
+ * thread.  No reference counterpart (the reference is single-threaded Julia). */
+int hdg_context_create(int device, hdg_context **out);
+int hdg_context_destroy(hdg_context *ctx);
+const char *hdg_last_error(const hdg_context *ctx);
+int hdg_context_synchronize(hdg_context *ctx);
+/* Number of this library's kernels launched on ctx so far. */
+long long hdg_launch_count(const hdg_context *ctx);
+/* CUDA events on the context's stream for timing a sequence of calls:
+ * record into slot 0..3, then the device time between two recorded slots. */
+int hdg_context_record(hdg_context *ctx, int slot);
+int hdg_context_elapsed_ms(hdg_context *ctx, int slot_from, int slot_to, double *ms);
+
+/* ---------------------------------------------------------------------- */
+/* Map level (batched over cells).                                          */
+/* ---------------------------------------------------------------------- */
+
+/* StaticCondensationMap: Gridap.Arrays.evaluate!(cache, k, A, b)
+ * (src/StaticCondensationMap.jl:146-196; cache :41-70).  For each of ncells
+ * cells, A is (ni+nf)^2 column-major and b is (ni+nf); outputs
+ * S = A_ff - A_fi A_ii^{-1} A_if (nf x nf, column-major) and
+ * g = b_f - A_fi A_ii^{-1} b_i (nf).  info[c] is LAPACK's getrf info of the
+ * cell's A_ii (0 = ok), which the reference checks with @check info==0
+ * (:180); a non-zero info makes the call return HDG_ERR_SINGULAR.
+ * info may be NULL. */
+int hdg_static_condensation(hdg_context *ctx, int precision, int ncells, int ni,
+                            int nf, const double *A, const double *b, double *S,
+                            double *g, int *info);
+
+/* BackwardStaticCondensationMap: evaluate!(cache, k, A, b, x)
+ * (src/BackwardStaticCondensationMap.jl:61-102): u_i = A_ii^{-1}(b_i - A_if x)
+ * for each cell; x is nf per cell, u is ni per cell (the interior blocks of the
+ * re-blocked vector, :133-151). */
+int hdg_backward_static_condensation(hdg_context *ctx, int precision,
+                                     int ncells, int ni, int nf,
+                                     const double *A, const double *b,
+                                     const double *x, double *u, int *info);
+
+/* SumFacetsMap: evaluate!(cache, k, a) (src/SumFacetsMap.jl:19-30).  For each
+ * of nitems items, sums nfacets blocks of len values each:
+ * out[i] = sum_f blocks[(i*nfacets + f)*len + :].  nfacets >= 2. */
+int hdg_sum_facets(hdg_context *ctx, int nitems, int nfacets, int len,
+                   const double *blocks, double *out);
+
+/* ---------------------------------------------------------------------- */
+/* Operator level: HybridAffineFEOperator / solve.                          */
+/* ---------------------------------------------------------------------- */
+
+/* Skeleton(model) + the L2 facet space of order k with Dirichlet facets on the
+ * boundary, for CartesianDiscreteModel(domain, cells) (src/Skeleton.jl:113-147;
+ * test/DarcyHDGTests.jl:27-52).  Cells, facets and DOFs are numbered as
+ * Gridap numbers them; domain is (x0,x1,y0,y1[,z0,z1]). */
+int hdg_problem_create_cartesian(hdg_context *ctx, int D, const int *cells,
+                                 const double *domain, int k,
+                                 hdg_problem **out);
+
+/* Same from an explicit affine mesh: cell_origin (ncells x D), cell_jacobian
+ * (ncells x D x D, column-major per cell), cell_facets (ncells x 2D, 0-based,
+ * Gridap local facet order), facet_dofs (nfacets x (k+1)^(D-1), sign convention
+ * above; each free facet's DOFs consecutive and increasing).  These are the
+ * arrays the reference obtains from get_faces(topo, D, D-1) and
+ * get_cell_dof_ids(L) (src/HybridAffineFEOperators.jl:152-162, :436-439).
+ * Facets must be seen with the same vertex order from both sides. */
+int hdg_problem_create(hdg_context *ctx, int D, int k, int ncells, int nfacets,
+                       const double *cell_origin, const double *cell_jacobian,
+                       const int *cell_facets, const int *facet_dofs,
+                       hdg_problem **out);
+int hdg_problem_destroy(hdg_problem *pb);
+
+/* info[0..7] = ncells, nfacets, ni, nf, nfree, ndirichlet, nnz, nfacet_dofs */
+int hdg_problem_info(const hdg_problem *pb, long long *info);
+
+/* The skeleton glue of the problem: cell_facets (ncells x 2D, Gridap local facet
+ * order), facet_cells (nfacets x 2, cells around each facet in increasing order,
+ * -1 if none; the first is the owner of get_cell_owner_normal_vector), facet_dofs
+ * (nfacets x nfacet_dofs).  get_faces(topo, D, D-1) / get_faces(topo, D-1, D) /
+ * get_cell_dof_ids(L) (src/HybridAffineFEOperators.jl:152-162; src/Skeleton.jl:549-556).
+ * Any pointer may be NULL. */
+int hdg_get_topology(const hdg_problem *pb, int *cell_facets, int *facet_cells,
+                     int *facet_dofs);
+
+/* The weak form (test/DarcyHDGTests.jl:125-135 with a per-cell permeability
+ * in the flux mass term): stab_mode HDG_STAB_*, tau > 0, problem HDG_PROBLEM_*
+ * (sources + Dirichlet data).  kappa: ncells values (NULL = 1). */
+int hdg_set_darcy(hdg_problem *pb, int stab_mode, double tau, int problem);
+int hdg_set_permeability(hdg_problem *pb, const double *kappa);
+/* Dirichlet values of the trial skeleton space, ndirichlet values
+ * (TrialFESpace(M, p), test/DarcyHDGTests.jl:52).  hdg_set_darcy interpolates
+ * the problem's exact pressure; this call overrides it. */
+int hdg_set_dirichlet_values(hdg_problem *pb, const double *vals);
+
+/* HybridAffineFEOperator(weakform, X, Y, bulk, skel)
+ * (src/HybridAffineFEOperators.jl:10-50): integrate, condense (keeping the
+ * factors of every A_ii on the device) and assemble the skeleton system with
+ * the Dirichlet lift.  info: ncells values or NULL. */
+int hdg_assemble(hdg_problem *pb, int precision, int *info);
+
+/* The assembled skeleton system of op.skeleton_op (:46-48) as CSR with sorted
+ * columns: rowptr (nfree+1), colind (nnz), val (nnz), rhs (nfree).  Any
+ * pointer may be NULL.  Gridap stores the same matrix as SparseMatrixCSC;
+ * for the symmetric forms here the arrays coincide. */
+int hdg_get_skeleton_system(hdg_problem *pb, long long *rowptr, int *colind,
+                            double *val, double *rhs);
+
+/* solve(op.skeleton_op) (src/HybridAffineFEOperators.jl:74).  rtol is the
+ * relative residual of PCG; iters/relres may be NULL. */
+int hdg_solve_skeleton(hdg_problem *pb, int solver, double rtol, int maxit,
+                       int *iters, double *relres);
+
+/* Interior recovery _compute_hybridizable_from_skeleton_free_dof_values
+ * (src/HybridAffineFEOperators.jl:102-150) with the stored factors. */
+int hdg_recover(hdg_problem *pb);
+
+/* Free DOF values of the multi-field trial space in Gridap's consecutive
+ * layout [flux of all cells | pressure of all cells | free skeleton DOFs]
+ * (FEFunction(op.trial, free_dof_values), :99).  Length
+ * ncells*ni + nfree. */
+int hdg_get_free_dof_values(hdg_problem *pb, double *out);
+/* Interior values per cell (ncells x ni) and free skeleton values (nfree). */
+int hdg_get_cell_interior_values(hdg_problem *pb, double *out);
+int hdg_get_skeleton_values(hdg_problem *pb, double *out);
+
+/* sqrt(sum(int((u-uh).(u-uh))dOmega)) (test/DarcyHDGTests.jl:141-142) for the
+ * flux and the pressure against the problem's exact solution. */
+int hdg_l2_errors(hdg_problem *pb, double *err_flux, double *err_pres);
+
+/* solve(op) in one call (src/HybridAffineFEOperators.jl:67-100):
+ * set kappa (may be NULL), assemble, solve the skeleton, recover, and copy the
+ * free DOF values (may be NULL) out.  stats (may be NULL) receives
+ * [pcg iterations, relative residual, ms integrate+condense, ms assemble,
+ *  ms skeleton solve, ms recover, ms total]. */
+int hdg_solve(hdg_problem *pb, int precision, int solver, double rtol,
+              int maxit, const double *kappa, double *free_dof_values,
+              double *stats);
+
+/* Device-event timings of the last hdg_assemble/solve_skeleton/recover calls
+ * in ms: [integrate, condense, assemble, skeleton solve, recover]. */
+int hdg_get_timings(const hdg_problem *pb, double *ms);
+
+/* Benchmark support (no reference counterpart): relaunches one kernel of the
+ * path `reps` times between CUDA events on the library's stream and returns
+ * the mean device time per launch in ms.  which: 0 integrate, 1 condense,
+ * 2 assemble (gather + rhs), 3 skeleton SpMV, 4 recover.  The problem must
+ * have been assembled (and solved for 3, 4); state is recomputed, not
+ * changed. */
+int hdg_time_kernel(hdg_problem *pb, int which, int reps, double *ms_per_launch);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -547,6 +547,26 @@ int orc_integrate_darcy(int D, int k, const int *n, const double *domain,
   return 0;
 }
 
+/* Same for a subset of cells (cells[0..nsel)), output packed in that order. */
+int orc_integrate_darcy_cells(int D, int k, const int *n, const double *domain,
+                              double tau, int stab_mode, int problem,
+                              const double *kappa, const int *facet_cells,
+                              const int *cell_facets, int nsel, const int *cells,
+                              double *A, double *b) {
+  reftab t;
+  if (reftab_init(&t, D, k)) return -1;
+  size_t N = t.n;
+#pragma omp parallel for schedule(static)
+  for (int s = 0; s < nsel; ++s) {
+    int c = cells[s];
+    integrate_cell(&t, c, n, domain, tau, stab_mode, problem,
+                   kappa ? kappa[c] : 1.0, facet_cells, cell_facets,
+                   A + (size_t)s * N * N, b + (size_t)s * N);
+  }
+  reftab_free(&t);
+  return 0;
+}
+
 /* Dirichlet values of the trial skeleton space TrialFESpace(M, p)
  * (test/DarcyHDGTests.jl:52): nodal interpolation of p at the facet
  * Lagrange nodes. */

@@ -50,6 +50,11 @@ int orc_integrate_darcy(int D, int k, const int *n, const double *domain,
                         double tau, int stab_mode, int problem,
                         const double *kappa, const int *facet_cells,
                         const int *cell_facets, double *A, double *b);
+int orc_integrate_darcy_cells(int D, int k, const int *n, const double *domain,
+                              double tau, int stab_mode, int problem,
+                              const double *kappa, const int *facet_cells,
+                              const int *cell_facets, int nsel, const int *cells,
+                              double *A, double *b);
 int orc_dirichlet_values(int D, int k, const int *n, const double *domain,
                          int problem, int nfacets, const int *facet_is_boundary,
                          const int *facet_dofs, int ndir, double *vals);

@@ -1,0 +1,220 @@
+"""Python access to the CPU FP64 oracle (oracle/hdg_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py as the checker; the GPU product never uses it.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "hdg_oracle.c")
+LIB = os.path.join(HERE, "liboracle.so")
+
+PROBLEM_REF_LINEAR, PROBLEM_LINEAR, PROBLEM_SIN = 0, 1, 2
+STAB_TEXTBOOK, STAB_OWNER_SIGN = 0, 1
+
+
+def build(force=False):
+    """gcc -O2 -fopenmp -shared oracle/hdg_oracle.c -> oracle/liboracle.so"""
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(
+            os.path.getmtime(SRC), os.path.getmtime(os.path.join(HERE, "hdg_oracle.h"))):
+        return LIB
+    tmp = LIB + ".tmp"
+    cmd = ["gcc", "-O2", "-fopenmp", "-fPIC", "-shared", "-o", tmp, SRC, "-lm"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + res.stderr)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+_L = None
+
+
+def lib():
+    global _L
+    if _L is None:
+        build()
+        _L = ctypes.CDLL(LIB)
+        _L.orc_solve_darcy.restype = ctypes.c_int
+    return _L
+
+
+def P(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def lattice(D, k):
+    out = np.zeros(((k + 1) ** D, max(D, 1)), dtype=np.int32)
+    n = lib().orc_lagrange_lattice(D, k, P(out))
+    return out[:n]
+
+
+def cell_sizes(D, k):
+    ni, nf = ctypes.c_int(), ctypes.c_int()
+    lib().orc_cell_sizes(D, k, ctypes.byref(ni), ctypes.byref(nf))
+    return ni.value, nf.value
+
+
+class Mesh:
+    """Cartesian mesh in Gridap numbering, as the oracle builds it."""
+
+    def __init__(self, D, n, k, domain=None):
+        L = lib()
+        self.D, self.k = D, k
+        self.n = np.array(n, dtype=np.int32)
+        self.domain = np.array(domain if domain is not None else [0.0, 1.0] * D, dtype=np.float64)
+        nc, nfc = ctypes.c_int(), ctypes.c_int()
+        L.orc_cart_counts(D, P(self.n), ctypes.byref(nc), ctypes.byref(nfc))
+        self.ncells, self.nfacets = nc.value, nfc.value
+        self.cell_facets = np.zeros((self.ncells, 2 * D), dtype=np.int32)
+        self.facet_cells = np.zeros((self.nfacets, 2), dtype=np.int32)
+        self.facet_is_boundary = np.zeros(self.nfacets, dtype=np.int32)
+        L.orc_cart_topology(D, P(self.n), P(self.cell_facets), P(self.facet_cells), P(self.facet_is_boundary))
+        self.nfd = (k + 1) ** (D - 1)
+        self.facet_dofs = np.zeros((self.nfacets, self.nfd), dtype=np.int32)
+        nfree, ndir = ctypes.c_int(), ctypes.c_int()
+        L.orc_facet_dofs(D, k, self.nfacets, P(self.facet_is_boundary), P(self.facet_dofs),
+                         ctypes.byref(nfree), ctypes.byref(ndir))
+        self.nfree, self.ndir = nfree.value, ndir.value
+        self.ni, self.nf = cell_sizes(D, k)
+
+    def integrate(self, tau=1.0, stab=STAB_TEXTBOOK, problem=PROBLEM_LINEAR, kappa=None):
+        n = self.ni + self.nf
+        A = np.zeros((self.ncells, n, n))  # A[c, j, i] = A_c(i, j): column-major per cell
+        b = np.zeros((self.ncells, n))
+        kap = None if kappa is None else np.ascontiguousarray(kappa, dtype=np.float64)
+        rc = lib().orc_integrate_darcy(self.D, self.k, P(self.n), P(self.domain), ctypes.c_double(tau), stab,
+                                       problem, P(kap), P(self.facet_cells), P(self.cell_facets), P(A), P(b))
+        assert rc == 0
+        return A, b
+
+    def integrate_cells(self, cells, tau=1.0, stab=STAB_TEXTBOOK, problem=PROBLEM_LINEAR, kappa=None):
+        cells = np.ascontiguousarray(cells, dtype=np.int32)
+        n = self.ni + self.nf
+        A = np.zeros((len(cells), n, n))
+        b = np.zeros((len(cells), n))
+        kap = None if kappa is None else np.ascontiguousarray(kappa, dtype=np.float64)
+        rc = lib().orc_integrate_darcy_cells(self.D, self.k, P(self.n), P(self.domain), ctypes.c_double(tau),
+                                             stab, problem, P(kap), P(self.facet_cells), P(self.cell_facets),
+                                             len(cells), P(cells), P(A), P(b))
+        assert rc == 0
+        return A, b
+
+    def dirichlet_values(self, problem):
+        vals = np.zeros(max(self.ndir, 1))
+        lib().orc_dirichlet_values(self.D, self.k, P(self.n), P(self.domain), problem, self.nfacets,
+                                   P(self.facet_is_boundary), P(self.facet_dofs), self.ndir, P(vals))
+        return vals[:self.ndir] if self.ndir else vals[:0]
+
+    def csr_pattern(self):
+        nnz = ctypes.c_int64()
+        L = lib()
+        L.orc_csr_pattern(self.D, self.k, self.ncells, self.nfacets, P(self.cell_facets), P(self.facet_dofs),
+                          self.nfree, None, None, ctypes.byref(nnz))
+        rowptr = np.zeros(self.nfree + 1, dtype=np.int64)
+        colind = np.zeros(nnz.value, dtype=np.int32)
+        L.orc_csr_pattern(self.D, self.k, self.ncells, self.nfacets, P(self.cell_facets), P(self.facet_dofs),
+                          self.nfree, P(rowptr), P(colind), ctypes.byref(nnz))
+        return rowptr, colind
+
+    def assemble(self, S, g, dirvals):
+        rowptr, colind = self.csr_pattern()
+        val = np.zeros(len(colind))
+        rhs = np.zeros(self.nfree)
+        dv = np.ascontiguousarray(dirvals if len(dirvals) else np.zeros(1))
+        rc = lib().orc_assemble(self.D, self.k, self.ncells, P(self.cell_facets), P(self.facet_dofs), self.nfree,
+                                P(dv), P(np.ascontiguousarray(S)), P(np.ascontiguousarray(g)), P(rowptr),
+                                P(colind), P(val), P(rhs))
+        assert rc == 0
+        return rowptr, colind, val, rhs
+
+    def cell_skeleton_values(self, lam, dirvals):
+        x = np.zeros((self.ncells, self.nf))
+        dv = np.ascontiguousarray(dirvals if len(dirvals) else np.zeros(1))
+        lib().orc_cell_skeleton_values(self.D, self.k, self.ncells, P(self.cell_facets), P(self.facet_dofs),
+                                       P(np.ascontiguousarray(lam)), P(dv), P(x))
+        return x
+
+    def l2_errors(self, problem, uint, kappa=None):
+        ef, ep = ctypes.c_double(), ctypes.c_double()
+        kap = None if kappa is None else np.ascontiguousarray(kappa, dtype=np.float64)
+        lib().orc_l2_errors(self.D, self.k, P(self.n), P(self.domain), problem, P(kap),
+                            P(np.ascontiguousarray(uint)), ctypes.byref(ef), ctypes.byref(ep))
+        return ef.value, ep.value
+
+
+def static_condensation(A, b, ni):
+    """A: (ncells, n, n) column-major per cell (A[c, j, i]); returns S (column-major), g, info."""
+    ncells, n, _ = A.shape
+    nf = n - ni
+    S = np.zeros((ncells, nf, nf))
+    g = np.zeros((ncells, nf))
+    info = np.zeros(ncells, dtype=np.int32)
+    lib().orc_static_condensation(ncells, ni, nf, P(np.ascontiguousarray(A)), P(np.ascontiguousarray(b)),
+                                  P(S), P(g), P(info))
+    return S, g, info
+
+
+def backward_static_condensation(A, b, x, ni):
+    ncells, n, _ = A.shape
+    u = np.zeros((ncells, ni))
+    info = np.zeros(ncells, dtype=np.int32)
+    lib().orc_backward_static_condensation(ncells, ni, n - ni, P(np.ascontiguousarray(A)),
+                                           P(np.ascontiguousarray(b)), P(np.ascontiguousarray(x)), P(u),
+                                           P(info))
+    return u, info
+
+
+def sum_facets(blocks):
+    blocks = np.ascontiguousarray(blocks, dtype=np.float64)
+    out = np.zeros(blocks[0].size)
+    rc = lib().orc_sum_facets(blocks.shape[0], blocks[0].size, P(blocks), P(out))
+    assert rc == 0
+    return out.reshape(blocks[0].shape)
+
+
+def dense_solve(rowptr, colind, val, rhs):
+    x = np.zeros(len(rhs))
+    rc = lib().orc_dense_solve(len(rhs), P(rowptr), P(colind), P(val), P(rhs), P(x))
+    assert rc == 0, "singular skeleton system"
+    return x
+
+
+def pcg(rowptr, colind, val, rhs, bs, rtol=1e-12, maxit=100000):
+    x = np.zeros(len(rhs))
+    it, rel = ctypes.c_int(), ctypes.c_double()
+    rc = lib().orc_pcg(len(rhs), bs, P(rowptr), P(colind), P(val), P(rhs), P(x), ctypes.c_double(-1.0),
+                       ctypes.c_double(rtol), maxit, ctypes.byref(it), ctypes.byref(rel))
+    return x, it.value, rel.value, rc
+
+
+def solve_darcy(D, k, n, tau=1.0, stab=STAB_TEXTBOOK, problem=PROBLEM_LINEAR, kappa=None, solver=0,
+                rtol=1e-12, maxit=100000, want_solution=True, domain=None):
+    """The whole path on the CPU; returns a dict with the interior values per cell
+    (ncells x ni), the free skeleton values, timings and errors."""
+    L = lib()
+    n = np.array(n, dtype=np.int32)
+    dom = np.array(domain if domain is not None else [0.0, 1.0] * D, dtype=np.float64)
+    m = Mesh(D, n, k, dom)
+    uint = np.zeros((m.ncells, m.ni)) if want_solution else None
+    lam = np.zeros(max(m.nfree, 1)) if want_solution else None
+    times = np.zeros(5)
+    it, rel, ef, ep = ctypes.c_int(), ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    kap = None if kappa is None else np.ascontiguousarray(kappa, dtype=np.float64)
+    rc = L.orc_solve_darcy(D, k, P(n), P(dom), ctypes.c_double(tau), stab, problem, P(kap), solver,
+                           ctypes.c_double(rtol), maxit, P(uint), P(lam), P(times), ctypes.byref(it),
+                           ctypes.byref(rel), ctypes.byref(ef), ctypes.byref(ep))
+    return dict(rc=rc, uint=uint, lam=None if lam is None else lam[:m.nfree], times=times, iters=it.value,
+                relres=rel.value, err_flux=ef.value, err_pres=ep.value, mesh=m)
+
+
+def set_threads(n):
+    lib().orc_set_threads(int(n))
+
+
+def max_threads():
+    return int(lib().orc_max_threads())

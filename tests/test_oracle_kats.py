@@ -1,0 +1,155 @@
+"""CPU tests that pin the oracle to the reference.
+
+The reference (Julia + Gridap) cannot run here; these tests pin the oracle to
+the reference's own known-answer tests and to golden vectors produced by an
+independent LAPACK executing the reference's call sequence.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "static_condensation_lapack.npz")
+
+
+def test_lagrange_node_order_quad():
+    # Gridap QUAD: vertices (0,0),(1,0),(0,1),(1,1); edges [y=0, y=1, x=0, x=1]; interior
+    assert oracle.lattice(2, 1).tolist() == [[0, 0], [1, 0], [0, 1], [1, 1]]
+    assert oracle.lattice(2, 2).tolist() == [[0, 0], [2, 0], [0, 2], [2, 2], [1, 0], [1, 2], [0, 1], [2, 1], [1, 1]]
+    # SEGMENT order 3: vertices then interior nodes from the first vertex on
+    assert oracle.lattice(1, 3)[:, 0].tolist() == [0, 3, 1, 2]
+
+
+def test_lagrange_node_order_hex():
+    lat = oracle.lattice(3, 2).tolist()
+    vertices = [[0, 0, 0], [2, 0, 0], [0, 2, 0], [2, 2, 0], [0, 0, 2], [2, 0, 2], [0, 2, 2], [2, 2, 2]]
+    # HEX edges (1,2),(3,4),(1,3),(2,4),(5,6),(7,8),(5,7),(6,8),(1,5),(2,6),(3,7),(4,8)
+    edges = [[1, 0, 0], [1, 2, 0], [0, 1, 0], [2, 1, 0], [1, 0, 2], [1, 2, 2], [0, 1, 2], [2, 1, 2],
+             [0, 0, 1], [2, 0, 1], [0, 2, 1], [2, 2, 1]]
+    # HEX facets [z=0, z=1, y=0, y=1, x=0, x=1]
+    faces = [[1, 1, 0], [1, 1, 2], [1, 0, 1], [1, 2, 1], [0, 1, 1], [2, 1, 1]]
+    assert lat == vertices + edges + faces + [[1, 1, 1]]
+    assert len(oracle.lattice(3, 3)) == 64
+
+
+@pytest.mark.parametrize("npts", [1, 2, 3, 4, 5, 6])
+def test_gauss_legendre_exactness(npts):
+    import ctypes
+    x = np.zeros(npts)
+    w = np.zeros(npts)
+    oracle.lib().orc_gauss_legendre01(npts, oracle.P(x), oracle.P(w))
+    for j in range(2 * npts):
+        assert abs(np.sum(w * x ** j) - 1.0 / (j + 1)) < 1e-14
+
+
+def test_cartesian_topology_gridap_numbering():
+    m = oracle.Mesh(2, (2, 2), 1)
+    # local facets [y0, y1, x0, x1]; facets numbered in first-encounter order
+    assert m.cell_facets.tolist() == [[0, 1, 2, 3], [4, 5, 3, 6], [1, 7, 8, 9], [5, 10, 9, 11]]
+    assert m.facet_cells[3].tolist() == [0, 1] and m.facet_cells[1].tolist() == [0, 2]
+    assert m.nfacets == 12 and m.nfree == 4 * 2 and m.ndir == 8 * 2
+    m3 = oracle.Mesh(3, (32, 32, 32), 2)
+    assert m3.ncells == 32768 and m3.nfree == 857088
+    r, c = oracle.Mesh(3, (4, 4, 4), 2).csr_pattern()
+    assert np.all(np.diff(r) > 0) and all(np.all(np.diff(c[r[i]:r[i + 1]]) > 0) for i in range(len(r) - 1))
+
+
+def test_csr_sizes_match_configs():
+    m = oracle.Mesh(2, (8, 8), 1)
+    r, c = m.csr_pattern()
+    assert m.nfree == 224 and len(c) == 2784  # config 1: 224 free DOFs, 2,784 nnz
+
+
+def test_sum_facets_kat():
+    """test/SumFacetMapTests.jl:29: four equal facet blocks sum to 4a."""
+    a = np.random.default_rng(0).random((2, 4))
+    assert np.allclose(oracle.sum_facets(np.stack([a, a, a, a])) - 4 * a, 0.0)
+
+
+def test_golden_lapack_vectors():
+    """The oracle's restatement of getrf/getrs/gemm/gemv reproduces scipy LAPACK
+    executing the reference's sequence."""
+    z = np.load(GOLDEN)
+    for i in range(int(z["ncases"])):
+        A, b, ni = z["A%d" % i], z["b%d" % i], int(z["ni%d" % i])
+        Acm = np.ascontiguousarray(A.T)[None]  # column-major per cell
+        S, g, info = oracle.static_condensation(Acm, b[None], ni)
+        assert info[0] == 0
+        S = S[0].T
+        assert np.abs(S - z["S%d" % i]).max() <= 1e-13 * np.abs(z["S%d" % i]).max()
+        assert np.abs(g[0] - z["g%d" % i]).max() <= 1e-13 * np.abs(z["g%d" % i]).max()
+        u, info = oracle.backward_static_condensation(Acm, b[None], z["x%d" % i][None], ni)
+        assert np.abs(u[0] - z["u%d" % i]).max() <= 1e-13 * np.abs(z["u%d" % i]).max()
+
+
+def test_static_condensation_identities():
+    """Forward then backward solves the full block system (the property the
+    reference's StaticCondensationMapTests exercises without asserting)."""
+    rng = np.random.default_rng(1)
+    ni, nf = 27, 12
+    n = ni + nf
+    A = rng.normal(size=(n, n)) + 3 * np.sqrt(n) * np.eye(n)
+    b = rng.normal(size=n)
+    S, g, _ = oracle.static_condensation(np.ascontiguousarray(A.T)[None], b[None], ni)
+    xf = np.linalg.solve(S[0].T, g[0])
+    u, _ = oracle.backward_static_condensation(np.ascontiguousarray(A.T)[None], b[None], xf[None], ni)
+    full = np.linalg.solve(A, b)
+    assert np.abs(full[:ni] - u[0]).max() < 1e-12 * np.abs(full).max()
+    assert np.abs(full[ni:] - xf).max() < 1e-12 * np.abs(full).max()
+
+
+def test_zero_pivot_info():
+    ni, nf = 3, 2
+    A = np.eye(5)
+    A[1, 1] = 0.0
+    A[2, 2] = 0.0
+    S, g, info = oracle.static_condensation(np.ascontiguousarray(A.T)[None], np.ones((1, 5)), ni)
+    assert info[0] == 2  # LAPACK info: first zero pivot (1-based)
+
+
+@pytest.mark.parametrize("D,n", [(2, (2, 2)), (3, (2, 2, 2))])
+def test_darcy_hdg_reference_exactness(D, n):
+    """test/DarcyHDGTests.jl:137-142: u=(1+x,1+y), p=-3.14, the reference's
+    n.n_o stabilisation, 2x2 mesh: L2 flux error < 1e-12."""
+    r = oracle.solve_darcy(D, 1, n, stab=oracle.STAB_OWNER_SIGN, problem=oracle.PROBLEM_REF_LINEAR, solver=0)
+    assert r["rc"] == 0
+    assert r["err_flux"] < 1e-12 and r["err_pres"] < 1e-12
+
+
+def test_cfg1_linear_pressure_exact():
+    r = oracle.solve_darcy(2, 1, (8, 8), problem=oracle.PROBLEM_LINEAR, solver=0)
+    assert r["err_flux"] < 1e-12 and r["err_pres"] < 1e-12
+
+
+@pytest.mark.parametrize("k", [1, 2, 3])
+def test_textbook_hdg_convergence_rates(k):
+    errs = [oracle.solve_darcy(2, k, (n, n), problem=oracle.PROBLEM_SIN, solver=0) for n in (4, 8, 16)]
+    ef = [e["err_flux"] for e in errs]
+    ep = [e["err_pres"] for e in errs]
+    rate_f = np.log2(ef[1] / ef[2])
+    rate_p = np.log2(ep[1] / ep[2])
+    assert rate_f > k + 1 - 0.25 and rate_p > k + 1 - 0.25
+
+
+def test_skeleton_operator_negative_definite():
+    """The textbook form's condensed skeleton operator is symmetric negative
+    definite (why PCG runs on -S)."""
+    m = oracle.Mesh(2, (4, 4), 2)
+    A, b = m.integrate(problem=oracle.PROBLEM_SIN)
+    S, g, _ = oracle.static_condensation(A, b, m.ni)
+    r, c, v, rhs = m.assemble(S, g, m.dirichlet_values(oracle.PROBLEM_SIN))
+    Md = np.zeros((m.nfree, m.nfree))
+    for i in range(m.nfree):
+        Md[i, c[r[i]:r[i + 1]]] = v[r[i]:r[i + 1]]
+    assert np.abs(Md - Md.T).max() < 1e-12 * np.abs(Md).max()
+    assert np.linalg.eigvalsh(Md).max() < 0
+
+
+def test_pcg_matches_dense():
+    kappa = np.exp(np.random.default_rng(2).normal(size=27))
+    r0 = oracle.solve_darcy(3, 1, (3, 3, 3), problem=oracle.PROBLEM_SIN, kappa=kappa, solver=0)
+    r1 = oracle.solve_darcy(3, 1, (3, 3, 3), problem=oracle.PROBLEM_SIN, kappa=kappa, solver=1, rtol=1e-14)
+    assert np.abs(r0["lam"] - r1["lam"]).max() < 1e-11 * np.abs(r0["lam"]).max()
+    assert np.abs(r0["uint"] - r1["uint"]).max() < 1e-11 * np.abs(r0["uint"]).max()
