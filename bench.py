@@ -178,7 +178,8 @@ def run_gpu(args):
     import gridaphybrid_gb300 as gh
     from gridaphybrid_gb300 import _lib
 
-    prec = {"fp64": _lib.HDG_PREC_FP64, "mixed": _lib.HDG_PREC_FP32_REFINED}[args.precision]
+    precs = {"fp64": _lib.HDG_PREC_FP64, "mixed": _lib.HDG_PREC_FP32_REFINED}
+    prec = precs[args.precision]
     ctx = gh.Context(0)
     lib = ctx.lib
     h = ctypes.c_void_p()
@@ -193,102 +194,121 @@ def run_gpu(args):
     kappa = kappa_field()
     ctx.check(lib.hdg_set_permeability(h, _lib.ptr(kappa)))
 
-    def step():
-        ctx.check(lib.hdg_assemble(h, prec, None))
+    def step(p, rtol=RTOL):
+        ctx.check(lib.hdg_assemble(h, p, None))
         it = ctypes.c_int()
         rel = ctypes.c_double()
-        ctx.check(lib.hdg_solve_skeleton(h, _lib.HDG_SOLVER_PCG, RTOL, MAXIT, ctypes.byref(it), ctypes.byref(rel)))
+        ctx.check(lib.hdg_solve_skeleton(h, _lib.HDG_SOLVER_PCG, rtol, MAXIT, ctypes.byref(it), ctypes.byref(rel)))
         ctx.check(lib.hdg_recover(h))
         return it.value, rel.value
 
+    def timed(p, steps):
+        ctx.synchronize()
+        l0 = ctx.launches
+        ctx.check(lib.hdg_context_record(ctx.handle, 0))
+        phase = np.zeros(5)
+        its = []
+        rel = None
+        for _ in range(steps):
+            it, rel = step(p)
+            its.append(it)
+            t = np.zeros(5)
+            lib.hdg_get_timings(h, _lib.ptr(t))
+            phase += t
+        ctx.check(lib.hdg_context_record(ctx.handle, 1))
+        ctx.synchronize()
+        ms = ctypes.c_double()
+        ctx.check(lib.hdg_context_elapsed_ms(ctx.handle, 0, 1, ctypes.byref(ms)))
+        return ms.value / steps, phase / steps, statistics.mean(its), rel, ctx.launches - l0
+
     for _ in range(args.warmup):
-        step()
-    ctx.synchronize()
-    launches0 = ctx.launches
+        step(prec)
     sampler = ClockSampler()
     sampler.start()
-    ctx.check(lib.hdg_context_record(ctx.handle, 0))
-    phase = np.zeros(5)
-    iters = []
-    for _ in range(args.steps):
-        it, rel = step()
-        iters.append(it)
-        t = np.zeros(5)
-        lib.hdg_get_timings(h, _lib.ptr(t))
-        phase += t
-    ctx.check(lib.hdg_context_record(ctx.handle, 1))
-    ctx.synchronize()
+    ms, phase, mean_iters, rel, launches = timed(prec, args.steps)
     clocks = sampler.stop()
-    ms_total = ctypes.c_double()
-    ctx.check(lib.hdg_context_elapsed_ms(ctx.handle, 0, 1, ctypes.byref(ms_total)))
-    launches = ctx.launches - launches0
-    ms = ms_total.value / args.steps
-    phase /= args.steps
+
+    # kernel timings on this precision's buffers (dominant HBM kernel: the SpMV)
+    spmv_ms, asm_ms, cond_ms = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    ctx.check(lib.hdg_time_kernel(h, 3, 20, ctypes.byref(spmv_ms)))
+    ctx.check(lib.hdg_time_kernel(h, 2, 5, ctypes.byref(asm_ms)))
+    ctx.check(lib.hdg_time_kernel(h, 1, 2, ctypes.byref(cond_ms)))
+
+    # the plain FP64 GPU path on the same workload, and the accuracy of the
+    # selected path against it (both solved to 1e-13)
+    compare = None
+    if args.precision != "fp64" and not args.no_fp64_compare:
+        step(precs["fp64"])
+        ms64, phase64, iters64, _, _ = timed(precs["fp64"], max(1, min(args.steps, 2)))
+        step(precs["fp64"], rtol=1e-13)
+        ref = np.empty(ncells * ni + nfree)
+        ctx.check(lib.hdg_get_free_dof_values(h, _lib.ptr(ref)))
+        step(prec, rtol=1e-13)
+        got = np.empty_like(ref)
+        ctx.check(lib.hdg_get_free_dof_values(h, _lib.ptr(got)))
+        compare = {
+            "fp64_ms_per_step": ms64,
+            "fp64_phases_ms": dict(zip(["integrate", "condense", "assemble", "skeleton_pcg", "recover"],
+                                       [float(x) for x in phase64])),
+            "speedup_vs_fp64_gpu": ms64 / ms,
+            "rel_err_vs_fp64": float(np.abs(got - ref).max() / np.abs(ref).max()),
+            "rel_err_note": "max |x - x_fp64| / max |x_fp64| over all free DOFs, both solved to 1e-13",
+        }
 
     # end to end through hdg_solve with host (pinned) buffers
-    try:
-        import torch
-        kap_h = torch.from_numpy(kappa.copy()).pin_memory()
-        out_h = torch.empty(ncells * ni + nfree, dtype=torch.float64).pin_memory()
+    e2e = None
+    if args.e2e_steps > 0:
+        try:
+            import torch
+            kap_h = torch.from_numpy(kappa.copy()).pin_memory()
+            out_h = torch.empty(ncells * ni + nfree, dtype=torch.float64).pin_memory()
+            pinned = True
+        except Exception:
+            kap_h = kappa.copy()
+            out_h = np.empty(ncells * ni + nfree)
+            pinned = False
         kp, op = _lib.ptr(kap_h), _lib.ptr(out_h)
-        pinned = True
-    except Exception:
-        kap_h = kappa.copy()
-        out_h = np.empty(ncells * ni + nfree)
-        kp, op = _lib.ptr(kap_h), _lib.ptr(out_h)
-        pinned = False
-    stats = np.zeros(7)
-    e2e_times = []
-    for i in range(args.e2e_steps + 1 if args.e2e_steps > 0 else 0):
-        t0 = time.perf_counter()
-        ctx.check(lib.hdg_solve(h, prec, _lib.HDG_SOLVER_PCG, RTOL, MAXIT, kp, op, _lib.ptr(stats)))
-        if i > 0:
-            e2e_times.append(time.perf_counter() - t0)
-    e2e_s = statistics.mean(e2e_times) if e2e_times else None
+        stats = np.zeros(7)
+        times = []
+        for i in range(args.e2e_steps + 1):
+            t0 = time.perf_counter()
+            ctx.check(lib.hdg_solve(h, prec, _lib.HDG_SOLVER_PCG, RTOL, MAXIT, kp, op, _lib.ptr(stats)))
+            if i > 0:
+                times.append(time.perf_counter() - t0)
+        e2e_s = statistics.mean(times)
+        e2e = {"value": ncells / e2e_s, "unit": UNIT, "h2d_bytes_per_step": ncells * 8,
+               "d2h_bytes_per_step": (ncells * ni + nfree) * 8, "ms_per_step": e2e_s * 1000.0,
+               "host_buffers": "pinned" if pinned else "pageable"}
 
-    # dominant HBM kernel: the skeleton SpMV, timed alone on the library's stream
-    spmv_ms = ctypes.c_double()
-    ctx.check(lib.hdg_time_kernel(h, 3, 20, ctypes.byref(spmv_ms)))
-    # values + one column list per facet block row + block-row pointers + p gathered once + q written
-    nblockrows = nfree // nfd
-    spmv_bytes = nnz * 8 + (nnz // nfd) * 4 + nblockrows * 16 + 2 * nfree * 8
-    asm_ms = ctypes.c_double()
-    ctx.check(lib.hdg_time_kernel(h, 2, 5, ctypes.byref(asm_ms)))
-    asm_bytes = ncells * (nf * nf + nf) * 8 + nnz * 8 + nfree * 8
-    cond_ms = ctypes.c_double()
-    ctx.check(lib.hdg_time_kernel(h, 1, 2, ctypes.byref(cond_ms)))
     peaks, peak_kind = measured_peaks()
     hbm = float(peaks["hbm_gbs"])
+    # SpMV: values + one column list per facet block row + block-row pointers + p gathered once + q written
+    nblockrows = nfree // nfd
+    spmv_bytes = nnz * 8 + (nnz // nfd) * 4 + nblockrows * 16 + 2 * nfree * 8
     spmv_gbs = spmv_bytes / (spmv_ms.value * 1e-3) / 1e9
+    # assembly: condensed blocks + vectors read, CSR values + rhs written
+    asm_bytes = ncells * (nf * nf + nf) * 8 + nnz * 8 + nfree * 8
     asm_gbs = asm_bytes / (asm_ms.value * 1e-3) / 1e9
-    cond_flop = ni ** 3 * 2 / 3 + 2 * ni * ni * nf + 2 * nf * nf * ni + 2 * ni * ni + 2 * nf * ni
-    mean_iters = statistics.mean(iters)
     line = {
         "metric": METRIC, "value": ncells / (ms / 1000.0), "unit": UNIT, "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": workload_config(args.precision),
-        "phases_ms": {"integrate": phase[0], "condense": phase[1], "assemble": phase[2],
-                      "skeleton_pcg": phase[3], "recover": phase[4]},
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+ff-refined" if args.precision == "mixed" else "f64",
+        "data": "synthetic", "config": workload_config(args.precision),
+        "phases_ms": dict(zip(["integrate", "condense", "assemble", "skeleton_pcg", "recover"],
+                              [float(x) for x in phase])),
         "condense_cells_per_s": ncells / ((phase[0] + phase[1]) / 1000.0),
-        "pcg_iters": mean_iters,
-        "pcg_relres": rel,
-        "full_solve_ms": ms,
+        "pcg_iters": mean_iters, "pcg_relres": rel, "full_solve_ms": ms,
         "roofline": {"bound": "hbm", "kernel": "pcg_spmv_kernel", "achieved": spmv_gbs, "peak": hbm,
-                     "unit": "GB/s", "frac": spmv_gbs / hbm, "traffic": None,
-                     "peak_source": peak_kind,
-                     "bytes_per_launch": spmv_bytes,
-                     "ms_per_launch": spmv_ms.value},
+                     "unit": "GB/s", "frac": spmv_gbs / hbm, "traffic": None, "peak_source": peak_kind,
+                     "bytes_per_launch": spmv_bytes, "ms_per_launch": spmv_ms.value},
         "assembly_roofline": {"bound": "hbm", "achieved": asm_gbs, "peak": hbm, "unit": "GB/s",
                               "frac": asm_gbs / hbm, "bytes_per_launch": asm_bytes, "ms_per_launch": asm_ms.value},
-        "condense_fp64": {"ms_per_launch": cond_ms.value, "gflops": cond_flop * ncells / (cond_ms.value * 1e-3) / 1e9},
-        "clocks": clocks,
-        "e2e": None if e2e_s is None else {
-            "value": ncells / e2e_s, "unit": UNIT, "h2d_bytes_per_step": ncells * 8,
-            "d2h_bytes_per_step": (ncells * ni + nfree) * 8, "ms_per_step": e2e_s * 1000.0,
-            "host_buffers": "pinned" if pinned else "pageable"},
-        "gpu_launches": launches,
+        "condense_ms_per_launch": cond_ms.value,
+        "clocks": clocks, "e2e": e2e, "gpu_launches": launches,
     }
+    if compare:
+        line["fp64_compare"] = compare
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample()
     print(json.dumps(line))
@@ -301,7 +321,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--no-fp64-compare", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()

@@ -107,6 +107,61 @@ CellArgs cell_args(hdg_problem *pb) {
   return a;
 }
 
+MixedTables mixed_tables(hdg_problem *pb) {
+  const float *t = pb->d_tabf.as<float>();
+  const TableOffsetsF &o = pb->toff_f;
+  MixedTables T{};
+  T.Mh = t + o.Mh;
+  T.Ml = t + o.Ml;
+  T.Gh = t + o.Gh;
+  T.Gl = t + o.Gl;
+  T.Fh = t + o.Fh;
+  T.Fl = t + o.Fl;
+  T.Hh = t + o.Hh;
+  T.Hl = t + o.Hl;
+  T.Lh = t + o.Lh;
+  T.Ll = t + o.Ll;
+  return T;
+}
+
+// Phase launches on the problem's buffers, for the precision of the last assemble.
+cudaError_t run_integrate(hdg_problem *pb) {
+  hdg_context *ctx = pb->ctx;
+  CellArgs a = cell_args(pb);
+  const size_t nc = pb->mesh.ncells, n = pb->tab.n;
+  if (pb->precision == HDG_PREC_FP64)
+    return launch_integrate_fp64(a, pb->d_A.as<double>(), pb->d_b.as<double>(), ctx->stream, ctx->num_sms,
+                                 &ctx->launches);
+  float *Ahi = pb->d_A.as<float>(), *bhi = pb->d_b.as<float>();
+  return launch_integrate_mixed(a, mixed_tables(pb), Ahi, Ahi + nc * n * n, bhi, bhi + nc * n, ctx->stream,
+                                ctx->num_sms, &ctx->launches);
+}
+
+cudaError_t run_condense(hdg_problem *pb) {
+  hdg_context *ctx = pb->ctx;
+  const size_t nc = pb->mesh.ncells, n = pb->tab.n, ni = pb->tab.ni, nf = pb->tab.nf;
+  if (pb->precision == HDG_PREC_FP64)
+    return launch_condense_fp64((int)nc, (int)ni, (int)nf, pb->d_A.as<double>(), pb->d_b.as<double>(),
+                                pb->d_S.as<double>(), pb->d_g.as<double>(), pb->d_fact.as<double>(),
+                                pb->d_info.as<int>(), ctx->stream, ctx->num_sms, &ctx->launches);
+  float *Ahi = pb->d_A.as<float>(), *bhi = pb->d_b.as<float>(), *Xhi = pb->d_fact.as<float>();
+  return launch_condense_mixed((int)nc, (int)ni, (int)nf, Ahi, Ahi + nc * n * n, bhi, bhi + nc * n,
+                               pb->d_S.as<double>(), pb->d_g.as<double>(), Xhi, Xhi + nc * ni * (nf + 1),
+                               pb->d_info.as<int>(), ctx->stream, ctx->num_sms, &ctx->launches);
+}
+
+cudaError_t run_recover(hdg_problem *pb) {
+  hdg_context *ctx = pb->ctx;
+  CellArgs a = cell_args(pb);
+  const size_t nc = pb->mesh.ncells, ni = pb->tab.ni, nf = pb->tab.nf;
+  if (pb->precision == HDG_PREC_FP64)
+    return launch_recover_fp64(a, pb->d_fact.as<double>(), pb->d_x.as<double>(), pb->d_dirvals.as<double>(),
+                               pb->d_uint.as<double>(), ctx->stream, ctx->num_sms, &ctx->launches);
+  const float *Xhi = pb->d_fact.as<float>();
+  return launch_recover_mixed(a, Xhi, Xhi + nc * ni * (nf + 1), pb->d_x.as<double>(), pb->d_dirvals.as<double>(),
+                              pb->d_uint.as<double>(), ctx->stream, ctx->num_sms, &ctx->launches);
+}
+
 AssembleArgs assemble_args(hdg_problem *pb) {
   const RefTables &t = pb->tab;
   AssembleArgs as{};
@@ -171,6 +226,9 @@ int setup_problem(hdg_problem *pb) {
   std::vector<double> packed;
   pb->toff = pack_tables(pb->tab, packed);
   if ((rc = upload(ctx, pb->d_tab, packed))) return rc;
+  std::vector<float> packed_f;
+  pb->toff_f = pack_tables_ff(pb->tab, packed_f);
+  if ((rc = upload(ctx, pb->d_tabf, packed_f))) return rc;
   if ((rc = upload(ctx, pb->d_origin, pb->mesh.origin))) return rc;
   if ((rc = upload(ctx, pb->d_jac, pb->mesh.jac))) return rc;
   if ((rc = upload(ctx, pb->d_cell_facets, pb->mesh.cell_facets))) return rc;
@@ -292,7 +350,9 @@ int hdg_static_condensation(hdg_context *ctx, int precision, int ncells, int ni,
     return ctx->fail(HDG_ERR_INVALID, "unknown precision %d", precision);
   if (ncells == 0) return HDG_OK;
   const int n = ni + nf;
-  if ((size_t)n * (n + 1) * sizeof(double) > ctx->smem_optin - 1024)
+  const size_t need = precision == HDG_PREC_FP64 ? (size_t)n * (n + 1) * sizeof(double)
+                                                 : condense_mixed_smem(ni, nf);
+  if (need > ctx->smem_optin - 1024)
     return ctx->fail(HDG_ERR_INVALID, "cell block %d x %d exceeds the shared-memory condensation kernel", n, n);
   cudaSetDevice(ctx->device);
   const double *dA, *db;
@@ -305,9 +365,19 @@ int hdg_static_condensation(hdg_context *ctx, int precision, int ncells, int ni,
   if ((rc = stage_out(ctx, ctx->scratch[3], g, (size_t)ncells * nf, &dg))) return rc;
   CUDA_TRY(ctx, ctx->scratch[4].reserve(sizeof(int) * ncells));
   dinfo = ctx->scratch[4].as<int>();
-  // both precisions share the FP64 elimination on caller-provided blocks
-  CUDA_TRY(ctx, launch_condense_fp64(ncells, ni, nf, dA, db, dS, dg, nullptr, dinfo, ctx->stream,
-                                     ctx->num_sms, &ctx->launches));
+  if (precision == HDG_PREC_FP64) {
+    CUDA_TRY(ctx, launch_condense_fp64(ncells, ni, nf, dA, db, dS, dg, nullptr, dinfo, ctx->stream,
+                                       ctx->num_sms, &ctx->launches));
+  } else {
+    // split the caller's FP64 blocks into float-float pairs, then FP32 LU + refinement
+    const size_t na = (size_t)ncells * n * n, nb = (size_t)ncells * n;
+    CUDA_TRY(ctx, ctx->scratch[5].reserve(sizeof(float) * 2 * (na + nb)));
+    float *Ahi = ctx->scratch[5].as<float>(), *Alo = Ahi + na, *bhi = Alo + na, *blo = bhi + nb;
+    CUDA_TRY(ctx, launch_split_fp64(na, dA, Ahi, Alo, ctx->stream, ctx->num_sms, &ctx->launches));
+    CUDA_TRY(ctx, launch_split_fp64(nb, db, bhi, blo, ctx->stream, ctx->num_sms, &ctx->launches));
+    CUDA_TRY(ctx, launch_condense_mixed(ncells, ni, nf, Ahi, Alo, bhi, blo, dS, dg, nullptr, nullptr, dinfo,
+                                        ctx->stream, ctx->num_sms, &ctx->launches));
+  }
   if ((rc = finish_out(ctx, dS, S, (size_t)ncells * nf * nf))) return rc;
   if ((rc = finish_out(ctx, dg, g, (size_t)ncells * nf))) return rc;
   std::vector<int> hinfo(ncells);
@@ -529,31 +599,31 @@ int hdg_assemble(hdg_problem *pb, int precision, int *info) {
   hdg_context *ctx = pb->ctx;
   if (precision != HDG_PREC_FP64 && precision != HDG_PREC_FP32_REFINED)
     return ctx->fail(HDG_ERR_INVALID, "unknown precision %d", precision);
-  if (precision == HDG_PREC_FP32_REFINED)
-    return ctx->fail(HDG_ERR_INVALID, "FP32+refinement operator path not built yet");
   cudaSetDevice(ctx->device);
   const RefTables &t = pb->tab;
   const size_t nc = pb->mesh.ncells, n = t.n, ni = t.ni, nf = t.nf;
-  if (n * (n + 1) * sizeof(double) > ctx->smem_optin - 1024)
-    return ctx->fail(HDG_ERR_INVALID, "cell block %zu exceeds the FP64 shared-memory kernel", n);
+  const bool mixed = precision == HDG_PREC_FP32_REFINED;
+  const size_t need = mixed ? condense_mixed_smem((int)ni, (int)nf) : n * (n + 1) * sizeof(double);
+  if (need > ctx->smem_optin - 1024)
+    return ctx->fail(HDG_ERR_INVALID, "cell block %zu exceeds the shared-memory condensation kernel", n);
+  // cell blocks: FP64, or (hi, lo) float pairs in the same bytes
   CUDA_TRY(ctx, pb->d_A.reserve(sizeof(double) * nc * n * n));
   CUDA_TRY(ctx, pb->d_b.reserve(sizeof(double) * nc * n));
   CUDA_TRY(ctx, pb->d_S.reserve(sizeof(double) * nc * nf * nf));
   CUDA_TRY(ctx, pb->d_g.reserve(sizeof(double) * nc * nf));
   CUDA_TRY(ctx, pb->d_aux.reserve(sizeof(double) * nc * nf));
-  CUDA_TRY(ctx, pb->d_fact.reserve(sizeof(double) * nc * ni * (n + 1)));
+  // recovery factors: FP64 [U11 | U12 | y], or the float-float pair X1 = (X0, delta)
+  CUDA_TRY(ctx, pb->d_fact.reserve(mixed ? sizeof(float) * 2 * nc * ni * (nf + 1) : sizeof(double) * nc * ni * (n + 1)));
   CUDA_TRY(ctx, pb->d_info.reserve(sizeof(int) * nc));
   CUDA_TRY(ctx, pb->d_val.reserve(sizeof(double) * (pb->pat.nnz ? pb->pat.nnz : 1)));
   CUDA_TRY(ctx, pb->d_rhs.reserve(sizeof(double) * (pb->mesh.nfree ? pb->mesh.nfree : 1)));
-  CellArgs a = cell_args(pb);
   cudaEvent_t *ev = ctx->ev;
+  pb->precision = precision;
+  pb->assembled = pb->solved = pb->recovered = false;
   CUDA_TRY(ctx, cudaEventRecord(ev[0], ctx->stream));
-  CUDA_TRY(ctx, launch_integrate_fp64(a, pb->d_A.as<double>(), pb->d_b.as<double>(), ctx->stream,
-                                      ctx->num_sms, &ctx->launches));
+  CUDA_TRY(ctx, run_integrate(pb));
   CUDA_TRY(ctx, cudaEventRecord(ev[1], ctx->stream));
-  CUDA_TRY(ctx, launch_condense_fp64((int)nc, (int)ni, (int)nf, pb->d_A.as<double>(), pb->d_b.as<double>(),
-                                     pb->d_S.as<double>(), pb->d_g.as<double>(), pb->d_fact.as<double>(),
-                                     pb->d_info.as<int>(), ctx->stream, ctx->num_sms, &ctx->launches));
+  CUDA_TRY(ctx, run_condense(pb));
   CUDA_TRY(ctx, cudaEventRecord(ev[2], ctx->stream));
   AssembleArgs as = assemble_args(pb);
   CUDA_TRY(ctx, launch_assemble(as, pb->d_S.as<double>(), pb->d_g.as<double>(), pb->d_aux.as<double>(),
@@ -609,9 +679,12 @@ static PcgArgs pcg_args(hdg_problem *pb) {
   a.r = pb->d_r.as<double>();
   a.z = pb->d_z.as<double>();
   a.p = pb->d_p.as<double>();
+  a.p2 = pb->d_p2.as<double>();
   a.q = pb->d_q.as<double>();
   a.partials = pb->d_partials.as<double>();
   a.scal = pb->d_scal.as<double>();
+  a.counter = pb->d_counter.as<unsigned int>();
+  a.val32 = nullptr;
   a.nparts = pb->ctx->num_sms * 4;
   a.diag_blk = pb->d_diag_blk.as<int>();
   a.blk_off = pb->d_blk_off.as<int64_t>();
@@ -654,36 +727,39 @@ int hdg_solve_skeleton(hdg_problem *pb, int solver, double rtol, int maxit, int 
   } else {
     if (pb->pat.max_rowlen > 288)
       return ctx->fail(HDG_ERR_INVALID, "skeleton rows of %d entries exceed the SpMV kernel's 288", pb->pat.max_rowlen);
-    if (nfd > 25) return ctx->fail(HDG_ERR_INVALID, "facet blocks larger than 25 DOFs are not supported by PCG");
+    if (!pcg_supports_nfd((int)nfd))
+      return ctx->fail(HDG_ERR_INVALID, "PCG has no kernel for %zu DOFs per facet", nfd);
     CUDA_TRY(ctx, pb->d_Binv.reserve(sizeof(double) * pb->pat.nblockrows * nfd * nfd));
     CUDA_TRY(ctx, pb->d_r.reserve(sizeof(double) * n));
     CUDA_TRY(ctx, pb->d_z.reserve(sizeof(double) * n));
     CUDA_TRY(ctx, pb->d_p.reserve(sizeof(double) * n));
+    CUDA_TRY(ctx, pb->d_p2.reserve(sizeof(double) * n));
     CUDA_TRY(ctx, pb->d_q.reserve(sizeof(double) * n));
     CUDA_TRY(ctx, pb->d_partials.reserve(sizeof(double) * 3 * ctx->num_sms * 4));
     CUDA_TRY(ctx, pb->d_scal.reserve(sizeof(double) * 16));
+    CUDA_TRY(ctx, pb->d_counter.reserve(sizeof(unsigned int) * 4));
     if (!pb->h_pinned.ptr) {
       CUDA_TRY(ctx, cudaMallocHost(&pb->h_pinned.ptr, 4096));
       pb->h_pinned.bytes = 4096;
     }
     PcgArgs a = pcg_args(pb);
     CUDA_TRY(ctx, launch_pcg_setup(a, rtol, ctx->stream, ctx->num_sms, &ctx->launches));
-    const int chunk = 16;
+    const int pairs = 8;  // 16 iterations per graph replay
     if (!pb->pcg_graph) {
       cudaGraph_t g;
       long long dummy = 0;
       CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-      for (int i = 0; i < chunk; ++i) launch_pcg_iteration(a, ctx->stream, ctx->num_sms, &dummy);
+      for (int i = 0; i < pairs; ++i) launch_pcg_iteration_pair(a, ctx->stream, ctx->num_sms, &dummy);
       CUDA_TRY(ctx, cudaStreamEndCapture(ctx->stream, &g));
       cudaError_t e = cudaGraphInstantiate(&pb->pcg_graph, g, 0);
       cudaGraphDestroy(g);
       CUDA_TRY(ctx, e);
-      pb->pcg_graph_chunk = chunk;
+      pb->pcg_graph_chunk = 2 * pairs;
     }
     double *h = static_cast<double *>(pb->h_pinned.ptr);
     for (;;) {
       CUDA_TRY(ctx, cudaGraphLaunch(pb->pcg_graph, ctx->stream));
-      ctx->launches += 5LL * pb->pcg_graph_chunk;
+      ctx->launches += 2LL * pb->pcg_graph_chunk;
       CUDA_TRY(ctx, cudaMemcpyAsync(h, pb->d_scal.ptr, sizeof(double) * 16, cudaMemcpyDeviceToHost, ctx->stream));
       CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
       it = (int)h[8];
@@ -718,12 +794,9 @@ int hdg_recover(hdg_problem *pb) {
   cudaSetDevice(ctx->device);
   const size_t nc = pb->mesh.ncells, ni = pb->tab.ni;
   CUDA_TRY(ctx, pb->d_uint.reserve(sizeof(double) * nc * ni));
-  CellArgs a = cell_args(pb);
   cudaEvent_t *ev = ctx->ev;
   CUDA_TRY(ctx, cudaEventRecord(ev[6], ctx->stream));
-  CUDA_TRY(ctx, launch_recover_fp64(a, pb->d_fact.as<double>(), pb->d_x.as<double>(),
-                                    pb->d_dirvals.as<double>(), pb->d_uint.as<double>(), ctx->stream,
-                                    ctx->num_sms, &ctx->launches));
+  CUDA_TRY(ctx, run_recover(pb));
   CUDA_TRY(ctx, cudaEventRecord(ev[7], ctx->stream));
   CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   pb->timings[4] = elapsed(ev[6], ev[7]);
@@ -835,10 +908,8 @@ int hdg_time_kernel(hdg_problem *pb, int which, int reps, double *ms_per_launch)
   if (!pb->assembled) return ctx->fail(HDG_ERR_STATE, "assemble first");
   if ((which == 3 || which == 4) && !pb->solved) return ctx->fail(HDG_ERR_STATE, "solve first");
   if (which == 3 && !pb->d_q.ptr) return ctx->fail(HDG_ERR_STATE, "SpMV timing needs a PCG solve first");
+  if (which == 4 && !pb->recovered) return ctx->fail(HDG_ERR_STATE, "recover first");
   cudaSetDevice(ctx->device);
-  const RefTables &t = pb->tab;
-  const int nc = pb->mesh.ncells;
-  CellArgs a = cell_args(pb);
   AssembleArgs as = assemble_args(pb);
   PcgArgs pa{};
   DBuf zero_scal;
@@ -851,12 +922,9 @@ int hdg_time_kernel(hdg_problem *pb, int which, int reps, double *ms_per_launch)
   auto launch = [&]() -> cudaError_t {
     switch (which) {
       case 0:
-        return launch_integrate_fp64(a, pb->d_A.as<double>(), pb->d_b.as<double>(), ctx->stream, ctx->num_sms,
-                                     &ctx->launches);
+        return run_integrate(pb);
       case 1:
-        return launch_condense_fp64(nc, t.ni, t.nf, pb->d_A.as<double>(), pb->d_b.as<double>(),
-                                    pb->d_S.as<double>(), pb->d_g.as<double>(), pb->d_fact.as<double>(),
-                                    pb->d_info.as<int>(), ctx->stream, ctx->num_sms, &ctx->launches);
+        return run_condense(pb);
       case 2:
         return launch_assemble(as, pb->d_S.as<double>(), pb->d_g.as<double>(), pb->d_aux.as<double>(),
                                pb->d_val.as<double>(), pb->d_rhs.as<double>(), ctx->stream, ctx->num_sms,
@@ -864,12 +932,9 @@ int hdg_time_kernel(hdg_problem *pb, int which, int reps, double *ms_per_launch)
       case 3:
         return launch_spmv(pa, ctx->stream, &ctx->launches);
       default:
-        return launch_recover_fp64(a, pb->d_fact.as<double>(), pb->d_x.as<double>(), pb->d_dirvals.as<double>(),
-                                   pb->d_uint.ptr ? pb->d_uint.as<double>() : nullptr, ctx->stream, ctx->num_sms,
-                                   &ctx->launches);
+        return run_recover(pb);
     }
   };
-  if (which == 4 && !pb->d_uint.ptr) return ctx->fail(HDG_ERR_STATE, "recover first");
   CUDA_TRY(ctx, launch());  // warm-up
   CUDA_TRY(ctx, cudaEventRecord(ctx->ev[0], ctx->stream));
   for (int r = 0; r < reps; ++r) CUDA_TRY(ctx, launch());

@@ -226,6 +226,26 @@ TableOffsets pack_tables(const RefTables &t, std::vector<double> &packed) {
   return o;
 }
 
+TableOffsetsF pack_tables_ff(const RefTables &t, std::vector<float> &packed) {
+  TableOffsetsF o{};
+  packed.clear();
+  auto put = [&](const std::vector<double> &v, int &hi_off, int &lo_off) {
+    hi_off = (int)packed.size();
+    for (double x : v) packed.push_back((float)x);
+    while (packed.size() % 8) packed.push_back(0.0f);
+    lo_off = (int)packed.size();
+    for (double x : v) packed.push_back((float)(x - (double)(float)x));
+    while (packed.size() % 8) packed.push_back(0.0f);
+  };
+  put(t.M, o.Mh, o.Ml);
+  put(t.G, o.Gh, o.Gl);
+  put(t.F, o.Fh, o.Fl);
+  put(t.H, o.Hh, o.Hl);
+  put(t.L, o.Lh, o.Ll);
+  o.total = (int)packed.size();
+  return o;
+}
+
 // ---------------------------------------------------------------------------
 // Cartesian mesh with Gridap's numbering: cells lexicographic (x fastest);
 // facets numbered in the order they are first met looping cells and their

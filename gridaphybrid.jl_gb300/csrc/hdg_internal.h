@@ -74,6 +74,12 @@ struct TableOffsets {
   int M, G, F, H, L, qxi, qw, qphi, total;
 };
 TableOffsets pack_tables(const RefTables &t, std::vector<double> &packed);
+// The same tables as float-float pairs: for each table its hi then lo floats,
+// at the offsets returned (in floats).
+struct TableOffsetsF {
+  int Mh, Ml, Gh, Gl, Fh, Fl, Hh, Hl, Lh, Ll, total;
+};
+TableOffsetsF pack_tables_ff(const RefTables &t, std::vector<float> &packed);
 
 // ---------------------------------------------------------------------------
 // Mesh + skeleton space + assembly pattern (host side, built once).
@@ -146,6 +152,8 @@ struct hdg_problem {
   hdg::HostMesh mesh;
   hdg::RefTables tab;
   hdg::TableOffsets toff{};
+  hdg::TableOffsetsF toff_f{};
+  hdg::DBuf d_tabf;
   hdg::HostPattern pat;
   int stab_mode = HDG_STAB_TEXTBOOK;
   int problem = HDG_PROBLEM_LINEAR;
@@ -162,7 +170,7 @@ struct hdg_problem {
   hdg::DBuf d_rowptr, d_colind, d_val, d_rhs;
   hdg::DBuf d_br_row0, d_br_src, d_blk_off, d_blk_rowlen, d_blk_src, d_diag_blk,
       d_dir_cells;
-  hdg::DBuf d_Binv, d_x, d_r, d_z, d_p, d_q, d_partials, d_scal;
+  hdg::DBuf d_Binv, d_x, d_r, d_z, d_p, d_p2, d_q, d_partials, d_scal, d_counter;
   hdg::DBuf d_uint;
   hdg::DBuf h_pinned;  // host staging
   cudaGraphExec_t pcg_graph = nullptr;

@@ -87,12 +87,25 @@ cudaError_t launch_sum_facets(int nitems, int nfacets, int len,
 cudaError_t launch_l2_errors(const CellArgs &a, const double *uint, double *errs,
                              cudaStream_t s, int num_sms, long long *launches);
 
-// Mixed precision (FP32 LU + float-float refinement) fused cell kernel.
-struct MixedOut {
-  double *S, *g;      // condensed block / vector (FP64)
-  float *fact;        // FP32 factors for the recovery, or null
-  int *info;
+// Reference tables split into float-float pairs (hi, lo) for the mixed path.
+struct MixedTables {
+  const float *Mh, *Ml, *Gh, *Gl, *Fh, *Fl, *Hh, *Hl, *Lh, *Ll;
 };
+// Mixed precision: float-float integration -> (A_hi, A_lo), (b_hi, b_lo)
+cudaError_t launch_integrate_mixed(const CellArgs &a, const MixedTables &T, float *Ahi, float *Alo,
+                                   float *bhi, float *blo, cudaStream_t s, int num_sms,
+                                   long long *launches);
+cudaError_t launch_split_fp64(size_t count, const double *x, float *hi, float *lo, cudaStream_t s,
+                              int num_sms, long long *launches);
+// FP32 LU + one float-float refinement step; Xhi/Xlo (ncells x ni x (nf+1)) may be null
+size_t condense_mixed_smem(int ni, int nf);
+cudaError_t launch_condense_mixed(int ncells, int ni, int nf, const float *Ahi, const float *Alo,
+                                  const float *bhi, const float *blo, double *S, double *g,
+                                  float *Xhi, float *Xlo, int *info, cudaStream_t s, int num_sms,
+                                  long long *launches);
+cudaError_t launch_recover_mixed(const CellArgs &a, const float *Xhi, const float *Xlo,
+                                 const double *lambda, const double *dirvals, double *uint,
+                                 cudaStream_t s, int num_sms, long long *launches);
 
 // Skeleton side --------------------------------------------------------------
 struct AssembleArgs {
@@ -114,9 +127,11 @@ struct PcgArgs {
   int n, nfd, nblockrows;
   const int64_t *rowptr;
   const int *colind;
-  const double *val;
+  const double *val;   // FP64 skeleton matrix values
+  const float *val32;  // FP32 copy used by the SpMV when non-null
   const double *rhs;
-  double *Binv, *x, *r, *z, *p, *q, *partials, *scal;
+  double *Binv, *x, *r, *z, *p, *p2, *q, *partials, *scal;
+  unsigned int *counter;  // last-CTA arrival counter (0 between launches)
   int nparts;
   const int *diag_blk;
   const int64_t *blk_off;
@@ -125,10 +140,13 @@ struct PcgArgs {
 };
 cudaError_t launch_pcg_setup(const PcgArgs &a, double rtol, cudaStream_t s,
                              int num_sms, long long *launches);
-cudaError_t launch_pcg_iteration(const PcgArgs &a, cudaStream_t s, int num_sms,
-                                 long long *launches);
-// one skeleton SpMV q = sign*A p (+ partial dots), as launched inside PCG
+// two PCG iterations (the double-buffered p returns to its starting buffer)
+cudaError_t launch_pcg_iteration_pair(const PcgArgs &a, cudaStream_t s, int num_sms,
+                                      long long *launches);
+// one skeleton SpMV q = sign*A p (+ its dot product), as launched inside PCG
 cudaError_t launch_spmv(const PcgArgs &a, cudaStream_t s, long long *launches);
+// facet block sizes the PCG kernels are instantiated for
+bool pcg_supports_nfd(int nfd);
 // dense LU solve of a CSR system (small n), one CTA
 cudaError_t launch_dense_solve(int n, const int64_t *rowptr, const int *colind,
                                const double *val, const double *rhs, double *work,

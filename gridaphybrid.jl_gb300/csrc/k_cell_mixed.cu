@@ -1,0 +1,547 @@
+// k_cell_mixed.cu -- FP32 local factorisation with high-precision refinement,
+// for sm_103a.
+//
+// GB300 runs FP64 at ~1/62 of its FP32 rate, so "high precision" here is
+// float-float arithmetic (a value is an unevaluated sum hi + lo of two FP32
+// numbers, ~48 significant bits) executed on the FP32 pipes:
+//  * integration produces every cell block as (A_hi, A_lo) FP32 pairs;
+//  * the LU of A_ii and the solves run in plain FP32 on A_hi;
+//  * one refinement step: X0 = A_ii^{-1}[A_if | b_i] (FP32), residual
+//    R = [A_if | b_i] - A_ii X0 in float-float, X1 = X0 + A_ii^{-1} R (FP32
+//    correction), then S = A_ff - A_fi X1 and g = b_f - A_fi y1 in
+//    float-float, returned in FP64.  On 32^3 k=2 cells this brings S from
+//    ~3e-7 (FP32 alone) to ~5e-13 relative;
+//  * X1 (as the pair X0, delta) is kept for the recovery u = y1 - X1_f x_f.
+#include <cuda_runtime.h>
+
+#include "hdg_kernels.h"
+
+namespace hdg {
+
+// ---------------------------------------------------------------------------
+// float-float helpers (Knuth two-sum, fma two-product)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+// (acc_hi, acc_lo) += (a_hi + a_lo) * x
+__device__ __forceinline__ void ff_mac(float &acc_hi, float &acc_lo, float a_hi, float a_lo, float x) {
+  const float p = a_hi * x;
+  float pe = fmaf(a_hi, x, -p);
+  pe = fmaf(a_lo, x, pe);
+  float s, e;
+  two_sum(acc_hi, p, s, e);
+  acc_hi = s;
+  acc_lo += e + pe;
+}
+
+// (acc_hi, acc_lo) += (a_hi + a_lo) * (x_hi + x_lo)
+__device__ __forceinline__ void ff_mac2(float &acc_hi, float &acc_lo, float a_hi, float a_lo, float x_hi,
+                                        float x_lo) {
+  const float p = a_hi * x_hi;
+  float pe = fmaf(a_hi, x_hi, -p);
+  pe = fmaf(a_lo, x_hi, pe);
+  pe = fmaf(a_hi, x_lo, pe);
+  float s, e;
+  two_sum(acc_hi, p, s, e);
+  acc_hi = s;
+  acc_lo += e + pe;
+}
+
+__device__ __forceinline__ void split_double(double v, float &hi, float &lo) {
+  hi = (float)v;
+  lo = (float)(v - (double)hi);
+}
+
+// ---------------------------------------------------------------------------
+// Integration in float-float: entry (i, j) = sum over terms of
+// coefficient (cell scalar, float-float) x reference table (float-float).
+// ---------------------------------------------------------------------------
+struct CellFactorsFF {
+  float cm[2];
+  float cg[3][3][2];
+  float cn[6][3][2];
+  float ct[6][2];
+  double detJ, x0[3], J[3][3];
+};
+
+__device__ void cell_factors_ff(const CellArgs &a, int c, CellFactorsFF &f) {
+  const int D = a.D;
+  double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, Ji[3][3];
+  for (int col = 0; col < D; ++col)
+    for (int row = 0; row < D; ++row) J[row][col] = a.jac[(size_t)c * D * D + col * D + row];
+  double det;
+  if (D == 2) {
+    det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+    Ji[0][0] = J[1][1] / det;
+    Ji[0][1] = -J[0][1] / det;
+    Ji[1][0] = -J[1][0] / det;
+    Ji[1][1] = J[0][0] / det;
+  } else {
+    const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+    const double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+    const double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+    det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+    Ji[0][0] = c00 / det;
+    Ji[1][0] = c01 / det;
+    Ji[2][0] = c02 / det;
+    Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / det;
+    Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / det;
+    Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / det;
+    Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det;
+    Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / det;
+    Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
+  }
+  const double adet = fabs(det);
+  const double kap = a.kappa ? a.kappa[c] : 1.0;
+  f.detJ = adet;
+  split_double(adet / kap, f.cm[0], f.cm[1]);
+  for (int e = 0; e < 3; ++e)
+    for (int d = 0; d < 3; ++d) {
+      const double v = (e < D && d < D) ? -adet * Ji[e][d] : 0.0;
+      split_double(v, f.cg[e][d][0], f.cg[e][d][1]);
+    }
+  for (int d = 0; d < D; ++d) {
+    f.x0[d] = a.origin[(size_t)c * D + d];
+    for (int e = 0; e < D; ++e) f.J[d][e] = J[d][e];
+  }
+  for (int lf = 0; lf < 2 * D; ++lf) {
+    const int dn = D - 1 - lf / 2;
+    const double sg = (lf % 2) ? 1.0 : -1.0;
+    double v[3], nv = 0.0;
+    for (int d = 0; d < D; ++d) {
+      v[d] = sg * Ji[dn][d];
+      nv += v[d] * v[d];
+    }
+    nv = sqrt(nv);
+    const double area = adet * nv;
+    for (int d = 0; d < 3; ++d) {
+      const double cnv = d < D ? area * (v[d] / nv) : 0.0;
+      split_double(cnv, f.cn[lf][d][0], f.cn[lf][d][1]);
+    }
+    double s = 1.0;
+    if (a.stab_mode == 1) {
+      const int fct = a.cell_facets[(size_t)c * 2 * D + lf];
+      s = (a.facet_cell[2 * (size_t)fct] == c) ? 1.0 : -1.0;
+    }
+    split_double(a.tau * s * area, f.ct[lf][0], f.ct[lf][1]);
+  }
+}
+
+__device__ __forceinline__ void decode_row(int i, int D, int nk, int ni, int nfd, int &type, int &sub,
+                                           int &idx) {
+  if (i < D * nk) {
+    type = 0;
+    sub = i / nk;
+    idx = i - sub * nk;
+  } else if (i < ni) {
+    type = 1;
+    sub = 0;
+    idx = i - D * nk;
+  } else {
+    type = 2;
+    sub = (i - ni) / nfd;
+    idx = i - ni - sub * nfd;
+  }
+}
+
+// acc += coef * table[k]   (coef, table entries float-float)
+__device__ __forceinline__ void ff_term(float &h, float &l, const float *coef, const float *Th, const float *Tl,
+                                        int k) {
+  if (coef[0] == 0.0f) return;
+  ff_mac2(h, l, Th[k], Tl[k], coef[0], coef[1]);
+}
+
+__device__ void cell_entry_ff(const CellArgs &a, const MixedTables &T, const CellFactorsFF &f, int ti, int si,
+                              int ii, int tj, int sj, int jj, float &h, float &l) {
+  const int D = a.D, nk = a.nk, nfd = a.nfd, nl = 2 * D;
+  h = 0.0f;
+  l = 0.0f;
+  float neg[2];
+  if (ti == 0) {
+    if (tj == 0) {
+      if (si == sj) ff_term(h, l, f.cm, T.Mh, T.Ml, ii * nk + jj);
+    } else if (tj == 1) {
+      for (int e = 0; e < D; ++e) ff_term(h, l, f.cg[e][si], T.Gh, T.Gl, (e * nk + ii) * nk + jj);
+    } else {
+      ff_term(h, l, f.cn[sj][si], T.Hh, T.Hl, (sj * nk + ii) * nfd + jj);
+    }
+  } else if (ti == 1) {
+    if (tj == 0) {
+      for (int e = 0; e < D; ++e) ff_term(h, l, f.cg[e][sj], T.Gh, T.Gl, (e * nk + ii) * nk + jj);
+      for (int lf = 0; lf < nl; ++lf) ff_term(h, l, f.cn[lf][sj], T.Fh, T.Fl, (lf * nk + ii) * nk + jj);
+    } else if (tj == 1) {
+      for (int lf = 0; lf < nl; ++lf) ff_term(h, l, f.ct[lf], T.Fh, T.Fl, (lf * nk + ii) * nk + jj);
+    } else {
+      neg[0] = -f.ct[sj][0];
+      neg[1] = -f.ct[sj][1];
+      ff_term(h, l, neg, T.Hh, T.Hl, (sj * nk + ii) * nfd + jj);
+    }
+  } else {
+    if (tj == 0) {
+      ff_term(h, l, f.cn[si][sj], T.Hh, T.Hl, (si * nk + jj) * nfd + ii);
+    } else if (tj == 1) {
+      ff_term(h, l, f.ct[si], T.Hh, T.Hl, (si * nk + jj) * nfd + ii);
+    } else if (si == sj) {
+      neg[0] = -f.ct[si][0];
+      neg[1] = -f.ct[si][1];
+      ff_term(h, l, neg, T.Lh, T.Ll, ii * nfd + jj);
+    }
+  }
+  // renormalise so that |lo| <= ulp(hi)/2
+  float s, e;
+  two_sum(h, l, s, e);
+  h = s;
+  l = e;
+}
+
+__global__ void __launch_bounds__(256) integrate_mixed_kernel(CellArgs a, MixedTables T, float *Ahi, float *Alo,
+                                                              float *bhi, float *blo) {
+  __shared__ CellFactorsFF f;
+  __shared__ double fq[512 * 4];
+  const int n = a.n, D = a.D;
+  for (int c = blockIdx.x; c < a.ncells; c += gridDim.x) {
+    if (threadIdx.x == 0) cell_factors_ff(a, c, f);
+    __syncthreads();
+    // the manufactured source is not polynomial: evaluated point by point in FP64
+    const double kap = a.kappa ? a.kappa[c] : 1.0;
+    for (int q = threadIdx.x; q < a.nqv; q += blockDim.x) {
+      double x[3], p, qe[3], fu[3], g;
+      for (int d = 0; d < D; ++d) {
+        x[d] = f.x0[d];
+        for (int e = 0; e < D; ++e) x[d] += f.J[d][e] * a.qxi[q * D + e];
+      }
+      exact_solution(a.problem, D, x, kap, p, qe, fu, g);
+      const double w = a.qw[q] * f.detJ;
+      for (int d = 0; d < D; ++d) fq[q * (D + 1) + d] = w * fu[d];
+      fq[q * (D + 1) + D] = w * g;
+    }
+    __syncthreads();
+    const size_t base = (size_t)c * n * n;
+    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
+      const int j = e / n, i = e - j * n;
+      int ti, si, ii, tj, sj, jj;
+      decode_row(i, D, a.nk, a.ni, a.nfd, ti, si, ii);
+      decode_row(j, D, a.nk, a.ni, a.nfd, tj, sj, jj);
+      float h, l;
+      cell_entry_ff(a, T, f, ti, si, ii, tj, sj, jj, h, l);
+      Ahi[base + e] = h;
+      Alo[base + e] = l;
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+      int ti, si, ii;
+      decode_row(i, D, a.nk, a.ni, a.nfd, ti, si, ii);
+      double v = 0.0;
+      if (ti < 2) {
+        const int comp = ti == 0 ? si : D;
+        for (int q = 0; q < a.nqv; ++q) v += fq[q * (D + 1) + comp] * a.qphi[q * a.nk + ii];
+      }
+      float h, l;
+      split_double(v, h, l);
+      bhi[(size_t)c * n + i] = h;
+      blo[(size_t)c * n + i] = l;
+    }
+    __syncthreads();
+  }
+}
+
+cudaError_t launch_integrate_mixed(const CellArgs &a, const MixedTables &T, float *Ahi, float *Alo, float *bhi,
+                                   float *blo, cudaStream_t s, int num_sms, long long *launches) {
+  if (a.nqv > 512) return cudaErrorInvalidValue;
+  int grid = a.ncells < num_sms * 8 ? a.ncells : num_sms * 8;
+  integrate_mixed_kernel<<<grid, 256, 0, s>>>(a, T, Ahi, Alo, bhi, blo);
+  ++*launches;
+  return cudaGetLastError();
+}
+
+// FP64 cell blocks (Map-level callers) -> float-float pairs
+__global__ void split_fp64_kernel(size_t count, const double *__restrict__ x, float *hi, float *lo) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x) {
+    float h, l;
+    split_double(x[i], h, l);
+    hi[i] = h;
+    lo[i] = l;
+  }
+}
+
+cudaError_t launch_split_fp64(size_t count, const double *x, float *hi, float *lo, cudaStream_t s, int num_sms,
+                              long long *launches) {
+  size_t g = (count + 255) / 256;
+  if (g > (size_t)num_sms * 32) g = (size_t)num_sms * 32;
+  if (g < 1) g = 1;
+  split_fp64_kernel<<<(int)g, 256, 0, s>>>(count, x, hi, lo);
+  ++*launches;
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Condensation: FP32 LU of A_ii with one float-float refinement step.
+// Shared memory: W = [A_ii | A_if | b_i] (ni x (n+1), FP32, column-major,
+// ld = ni) factorised in place, R (ni x (nf+1)) for the residual/correction.
+// ---------------------------------------------------------------------------
+constexpr int kMixedThreads = 256;
+constexpr int kColChunk = 28;  // right-hand-side columns per thread in the float-float products
+
+__device__ int lu_fp32_interior(float *W, int ni, int ncols, int *ipiv, int *s_piv) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int info = 0;
+  for (int j = 0; j < ni; ++j) {
+    if (warp == 0) {
+      float best = -1.0f;
+      int bi = j;
+      for (int i = j + lane; i < ni; i += 32) {
+        const float v = fabsf(W[i + ni * j]);
+        if (v > best) {
+          best = v;
+          bi = i;
+        }
+      }
+      for (int off = 16; off > 0; off >>= 1) {
+        const float ov = __shfl_down_sync(0xffffffffu, best, off);
+        const int oi = __shfl_down_sync(0xffffffffu, bi, off);
+        if (ov > best || (ov == best && oi < bi)) {
+          best = ov;
+          bi = oi;
+        }
+      }
+      if (lane == 0) {
+        *s_piv = best > 0.0f ? bi : -1;
+        ipiv[j] = best > 0.0f ? bi : j;
+      }
+    }
+    __syncthreads();
+    const int p = *s_piv;
+    if (p < 0) {
+      if (!info) info = j + 1;
+      __syncthreads();
+      continue;
+    }
+    if (p != j)
+      for (int c = threadIdx.x; c < ncols; c += blockDim.x) {  // whole rows: L stays consistent
+        const float t = W[j + ni * c];
+        W[j + ni * c] = W[p + ni * c];
+        W[p + ni * c] = t;
+      }
+    __syncthreads();
+    const float r = 1.0f / W[j + ni * j];
+    for (int i = j + 1 + threadIdx.x; i < ni; i += blockDim.x) W[i + ni * j] *= r;
+    __syncthreads();
+    for (int c = j + 1 + warp; c < ncols; c += nw) {
+      const float u = W[j + ni * c];
+      if (u != 0.0f)
+        for (int i = j + 1 + lane; i < ni; i += 32) W[i + ni * c] = fmaf(-W[i + ni * j], u, W[i + ni * c]);
+    }
+    __syncthreads();
+  }
+  return info;
+}
+
+// B (ni x nb, ld ldb) <- U^{-1} B with U the upper triangle of W (ld ni)
+__device__ void upper_solve(const float *W, int ni, float *B, int ldb, int nb) {
+  for (int j = ni - 1; j >= 0; --j) {
+    const float d = 1.0f / W[j + ni * j];
+    for (int c = threadIdx.x; c < nb; c += blockDim.x) B[j + ldb * c] *= d;
+    __syncthreads();
+    const int work = j * nb;
+    for (int e = threadIdx.x; e < work; e += blockDim.x) {
+      const int c = e / j, i = e - c * j;
+      B[i + ldb * c] = fmaf(-W[i + ni * j], B[j + ldb * c], B[i + ldb * c]);
+    }
+    __syncthreads();
+  }
+}
+
+// B <- L^{-1} P B (unit lower L in W's strict lower triangle, LAPACK ipiv)
+__device__ void lower_solve_perm(const float *W, int ni, const int *ipiv, float *B, int ldb, int nb) {
+  for (int c = threadIdx.x; c < nb; c += blockDim.x)
+    for (int j = 0; j < ni; ++j) {
+      const int p = ipiv[j];
+      if (p != j) {
+        const float t = B[j + ldb * c];
+        B[j + ldb * c] = B[p + ldb * c];
+        B[p + ldb * c] = t;
+      }
+    }
+  __syncthreads();
+  for (int j = 0; j < ni; ++j) {
+    const int rows = ni - j - 1;
+    const int work = rows * nb;
+    for (int e = threadIdx.x; e < work; e += blockDim.x) {
+      const int c = e / rows, i = j + 1 + (e - c * rows);
+      B[i + ldb * c] = fmaf(-W[i + ni * j], B[j + ldb * c], B[i + ldb * c]);
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(kMixedThreads) condense_mixed_kernel(
+    int ncells, int ni, int nf, const float *__restrict__ Ahi, const float *__restrict__ Alo,
+    const float *__restrict__ bhi, const float *__restrict__ blo, double *S, double *g, float *Xhi, float *Xlo,
+    int *info) {
+  extern __shared__ float smem[];
+  __shared__ int s_piv;
+  const int n = ni + nf, nc = nf + 1;
+  float *W = smem;                                         // ni x (n+1)
+  float *R = W + (size_t)ni * (n + 1);                     // ni x nc
+  int *ipiv = reinterpret_cast<int *>(R + (size_t)ni * nc);  // ni
+  float *X0 = W + (size_t)ni * ni;                         // columns ni..n of W after the solve
+  const int half = blockDim.x / 2, grp = threadIdx.x / half, lt = threadIdx.x - grp * half;
+  const int nchunks = (nc + kColChunk - 1) / kColChunk;
+  for (int c = blockIdx.x; c < ncells; c += gridDim.x) {
+    const float *Ah = Ahi + (size_t)c * n * n, *Al = Alo + (size_t)c * n * n;
+    const float *bh = bhi + (size_t)c * n, *bl = blo + (size_t)c * n;
+    // 1. W = [A_ii | A_if | b_i] (hi parts)
+    for (int e = threadIdx.x; e < ni * n; e += blockDim.x) {
+      const int j = e / ni, i = e - j * ni;
+      W[e] = Ah[i + (size_t)n * j];
+    }
+    for (int i = threadIdx.x; i < ni; i += blockDim.x) W[(size_t)ni * n + i] = bh[i];
+    __syncthreads();
+    // 2. FP32 LU with partial pivoting; U12 and y become L^{-1} P [A_if | b_i]
+    const int inf = lu_fp32_interior(W, ni, n + 1, ipiv, &s_piv);
+    // 3. X0 = U^{-1} [U12 | y]
+    upper_solve(W, ni, X0, ni, nc);
+    // 4. R = [A_if | b_i] - A_ii X0 in float-float (A in original row order)
+    for (int chunk = grp; chunk < nchunks; chunk += 2) {
+      const int c0 = chunk * kColChunk;
+      const int ncol = min(kColChunk, nc - c0);
+      for (int i = lt; i < ni; i += half) {
+        float hs[kColChunk], ls[kColChunk];
+#pragma unroll
+        for (int q = 0; q < kColChunk; ++q) {
+          hs[q] = 0.0f;
+          ls[q] = 0.0f;
+        }
+        for (int k = 0; k < ni; ++k) {
+          const float ah = Ah[i + (size_t)n * k], al = Al[i + (size_t)n * k];
+#pragma unroll
+          for (int q = 0; q < kColChunk; ++q)
+            if (q < ncol) ff_mac(hs[q], ls[q], ah, al, X0[k + ni * (c0 + q)]);
+        }
+#pragma unroll
+        for (int q = 0; q < kColChunk; ++q)
+          if (q < ncol) {
+            const int col = c0 + q;
+            const float rh = col < nf ? Ah[i + (size_t)n * (ni + col)] : bh[i];
+            const float rl = col < nf ? Al[i + (size_t)n * (ni + col)] : bl[i];
+            // r = (rh + rl) - (hs + ls), hi part only is kept
+            R[i + ni * col] = ((rh - hs[q]) + rl) - ls[q];
+          }
+      }
+    }
+    __syncthreads();
+    // 5. delta = A_ii^{-1} R with the FP32 factors
+    lower_solve_perm(W, ni, ipiv, R, ni, nc);
+    upper_solve(W, ni, R, ni, nc);
+    // 6. S = A_ff - A_fi (X0 + delta), g = b_f - A_fi (y0 + delta_y), float-float
+    for (int chunk = grp; chunk < nchunks; chunk += 2) {
+      const int c0 = chunk * kColChunk;
+      const int ncol = min(kColChunk, nc - c0);
+      for (int a = lt; a < nf; a += half) {
+        float hs[kColChunk], ls[kColChunk];
+#pragma unroll
+        for (int q = 0; q < kColChunk; ++q) {
+          hs[q] = 0.0f;
+          ls[q] = 0.0f;
+        }
+        for (int k = 0; k < ni; ++k) {
+          const float ah = Ah[(ni + a) + (size_t)n * k], al = Al[(ni + a) + (size_t)n * k];
+#pragma unroll
+          for (int q = 0; q < kColChunk; ++q)
+            if (q < ncol) ff_mac2(hs[q], ls[q], ah, al, X0[k + ni * (c0 + q)], R[k + ni * (c0 + q)]);
+        }
+#pragma unroll
+        for (int q = 0; q < kColChunk; ++q)
+          if (q < ncol) {
+            const int col = c0 + q;
+            const double rhs = col < nf ? (double)Ah[(ni + a) + (size_t)n * (ni + col)] +
+                                              (double)Al[(ni + a) + (size_t)n * (ni + col)]
+                                        : (double)bh[ni + a] + (double)bl[ni + a];
+            const double v = rhs - ((double)hs[q] + (double)ls[q]);
+            if (col < nf)
+              S[(size_t)c * nf * nf + a + (size_t)nf * col] = v;
+            else
+              g[(size_t)c * nf + a] = v;
+          }
+      }
+    }
+    // 7. keep X1 = (X0, delta) for the recovery
+    if (Xhi) {
+      float *xh = Xhi + (size_t)c * ni * nc, *xl = Xlo + (size_t)c * ni * nc;
+      for (int e = threadIdx.x; e < ni * nc; e += blockDim.x) {
+        xh[e] = X0[e];
+        xl[e] = R[e];
+      }
+    }
+    if (info && threadIdx.x == 0) info[c] = inf;
+    __syncthreads();
+  }
+}
+
+size_t condense_mixed_smem(int ni, int nf) {
+  const int n = ni + nf;
+  return sizeof(float) * ((size_t)ni * (n + 1) + (size_t)ni * (nf + 1)) + sizeof(int) * ni;
+}
+
+cudaError_t launch_condense_mixed(int ncells, int ni, int nf, const float *Ahi, const float *Alo,
+                                  const float *bhi, const float *blo, double *S, double *g, float *Xhi,
+                                  float *Xlo, int *info, cudaStream_t s, int num_sms, long long *launches) {
+  const size_t smem = condense_mixed_smem(ni, nf);
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(condense_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  const int per_sm = (int)((228 * 1024) / (smem + 1024));
+  int grid = num_sms * (per_sm > 0 ? per_sm : 1);
+  if (grid > ncells) grid = ncells;
+  if (grid < 1) grid = 1;
+  condense_mixed_kernel<<<grid, kMixedThreads, smem, s>>>(ncells, ni, nf, Ahi, Alo, bhi, blo, S, g, Xhi, Xlo,
+                                                          info);
+  ++*launches;
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Recovery: u = y1 - X1_f x_f in float-float, X1 = (X0 + delta) from the
+// condensation, x_f the cell's skeleton values (FP64, split).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(128) recover_mixed_kernel(CellArgs a, const float *__restrict__ Xhi,
+                                                            const float *__restrict__ Xlo,
+                                                            const double *__restrict__ lambda,
+                                                            const double *__restrict__ dirvals, double *uint) {
+  __shared__ float xf[2][6 * 64];
+  const int ni = a.ni, nf = a.nf, nfd = a.nfd, nl = 2 * a.D, nc = nf + 1;
+  for (int c = blockIdx.x; c < a.ncells; c += gridDim.x) {
+    for (int e = threadIdx.x; e < nf; e += blockDim.x) {
+      const int lf = e / nfd, j = e - lf * nfd;
+      const int id = a.facet_dofs[(size_t)a.cell_facets[(size_t)c * nl + lf] * nfd + j];
+      const double v = id >= 0 ? lambda[id] : dirvals[-1 - id];
+      split_double(v, xf[0][e], xf[1][e]);
+    }
+    __syncthreads();
+    const float *xh = Xhi + (size_t)c * ni * nc, *xl = Xlo + (size_t)c * ni * nc;
+    for (int i = threadIdx.x; i < ni; i += blockDim.x) {
+      float h = 0.0f, l = 0.0f;
+      for (int j = 0; j < nf; ++j) ff_mac2(h, l, xh[i + ni * j], xl[i + ni * j], xf[0][j], xf[1][j]);
+      const double y = (double)xh[i + ni * nf] + (double)xl[i + ni * nf];
+      uint[(size_t)c * ni + i] = y - ((double)h + (double)l);
+    }
+    __syncthreads();
+  }
+}
+
+cudaError_t launch_recover_mixed(const CellArgs &a, const float *Xhi, const float *Xlo, const double *lambda,
+                                 const double *dirvals, double *uint, cudaStream_t s, int num_sms,
+                                 long long *launches) {
+  if (a.nf > 6 * 64) return cudaErrorInvalidValue;
+  int grid = a.ncells < num_sms * 8 ? a.ncells : num_sms * 8;
+  recover_mixed_kernel<<<grid, 128, 0, s>>>(a, Xhi, Xlo, lambda, dirvals, uint);
+  ++*launches;
+  return cudaGetLastError();
+}
+
+}  // namespace hdg

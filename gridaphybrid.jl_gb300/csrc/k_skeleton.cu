@@ -116,8 +116,16 @@ cudaError_t launch_assemble(const AssembleArgs &a, const double *S, const double
 }
 
 // ---------------------------------------------------------------------------
-// PCG on (sign*A) x = sign*rhs with facet-block-Jacobi preconditioning.
-// Device scalars (scal[]):
+// PCG on (sign*A) x = sign*rhs with facet-block-Jacobi preconditioning, two
+// kernels per iteration:
+//   spmv:   p_new = z + beta p_old (formed while gathering), q = sign*A p_new,
+//           alpha = (r,z) / (p_new,q)
+//   update: x += alpha p_new, r -= alpha q, z = Binv r, beta, convergence
+// Each kernel's dot products are finished by its last CTA, which sums the
+// per-CTA partials in index order (deterministic for a fixed grid).  p is
+// double-buffered, so a CUDA graph of an even number of iterations can be
+// replayed; once SC_DONE is set every kernel returns immediately.
+// ---------------------------------------------------------------------------
 enum {
   SC_RZ = 0,     // (r, z)
   SC_PAP = 1,    // (p, A p)
@@ -130,9 +138,6 @@ enum {
   SC_ITERS = 8,  // completed iterations
   SC_NSCAL = 16
 };
-// Every kernel of an iteration is a no-op once SC_DONE is set, so a CUDA graph
-// of a fixed number of iterations can be replayed until convergence.
-// ---------------------------------------------------------------------------
 
 constexpr int kPcgThreads = 256;
 
@@ -146,6 +151,23 @@ __device__ __forceinline__ double block_sum(double v, double *red) {
   if (threadIdx.x == 0)
     for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += red[i];
   return s;  // valid in thread 0
+}
+
+// After every CTA has stored its partials: true in the CTA that arrives last.
+__device__ __forceinline__ bool last_cta(unsigned int *counter) {
+  __shared__ bool is_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) is_last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  __syncthreads();
+  return is_last;
+}
+
+// sum of partials[k*nparts + 0..nparts) in index order, by the last CTA
+__device__ __forceinline__ double sum_partials(const double *partials, int nparts, int k, double *red) {
+  double s = 0.0;
+  for (int i = threadIdx.x; i < nparts; i += blockDim.x) s += __ldcg(partials + (size_t)k * nparts + i);
+  return block_sum(s, red);
 }
 
 // Inverse of each facet's diagonal block of sign*A (Gauss-Jordan, partial pivoting).
@@ -198,17 +220,15 @@ __global__ void binv_kernel(PcgArgs a) {
   }
 }
 
-// z = Binv r for the block rows handled by this CTA (rows staged in smem).
-// Called with blockDim.x = rows_per_cta*nfd.
-__device__ __forceinline__ double apply_binv(const PcgArgs &a, int row, int nrows,
-                                             double rval, double *rs) {
+// z = Binv r for the block rows of this CTA's tile (rows staged in smem).
+__device__ __forceinline__ double apply_binv(const PcgArgs &a, int row, int nrows, double rval, double *rs) {
   const int nfd = a.nfd;
   rs[threadIdx.x] = rval;
   __syncthreads();
   double z = 0.0;
   if (row < nrows) {
-    const int lr = threadIdx.x, br = row / nfd, i = row - br * nfd;
-    const int first = lr - i;
+    const int br = row / nfd, i = row - br * nfd;
+    const int first = (int)threadIdx.x - i;
     const double *B = a.Binv + (size_t)br * nfd * nfd + (size_t)i * nfd;
     for (int j = 0; j < nfd; ++j) z += B[j] * rs[first + j];
   }
@@ -216,10 +236,11 @@ __device__ __forceinline__ double apply_binv(const PcgArgs &a, int row, int nrow
   return z;
 }
 
-__global__ void pcg_init_kernel(PcgArgs a) {
-  __shared__ double rs[1024];
+// x = 0, r = sign*rhs, z = Binv r, p buffers = 0; scalars by the last CTA
+__global__ void __launch_bounds__(kPcgThreads) pcg_init_kernel(PcgArgs a, double rtol) {
+  __shared__ double rs[kPcgThreads];
   __shared__ double red[32];
-  const int tile = (blockDim.x / a.nfd) * a.nfd;
+  const int tile = (kPcgThreads / a.nfd) * a.nfd;
   double rz = 0.0, rr = 0.0, bb = 0.0;
   for (int base = blockIdx.x * tile; base < a.n; base += gridDim.x * tile) {
     const int row = base + (int)threadIdx.x;
@@ -230,106 +251,121 @@ __global__ void pcg_init_kernel(PcgArgs a) {
       r = a.sign * b;
       a.x[row] = 0.0;
       a.r[row] = r;
+      a.p[row] = 0.0;
+      a.p2[row] = 0.0;
       bb += b * b;
       rr += r * r;
     }
-    double z = apply_binv(a, act ? row : a.n, a.n, r, rs);
+    const double z = apply_binv(a, act ? row : a.n, a.n, r, rs);
     if (act) {
       a.z[row] = z;
-      a.p[row] = z;
       rz += r * z;
     }
   }
-  double s;
-  s = block_sum(rz, red);
+  double s = block_sum(rz, red);
   if (threadIdx.x == 0) a.partials[blockIdx.x] = s;
   s = block_sum(rr, red);
   if (threadIdx.x == 0) a.partials[a.nparts + blockIdx.x] = s;
   s = block_sum(bb, red);
   if (threadIdx.x == 0) a.partials[2 * a.nparts + blockIdx.x] = s;
-}
-
-__global__ void pcg_init_reduce_kernel(PcgArgs a, double rtol) {
-  __shared__ double red[32];
-  double v[3];
-  for (int k = 0; k < 3; ++k) {
-    double s = 0.0;
-    for (int i = threadIdx.x; i < a.nparts; i += blockDim.x) s += a.partials[k * a.nparts + i];
-    v[k] = block_sum(s, red);
-  }
-  if (threadIdx.x == 0) {
-    a.scal[SC_RZ] = v[0];
-    a.scal[SC_RR] = v[1];
-    a.scal[SC_BB] = v[2];
-    a.scal[SC_TOL2] = rtol * rtol * v[2];
-    a.scal[SC_ITERS] = 0.0;
-    a.scal[SC_DONE] = (v[1] <= rtol * rtol * v[2]) ? 1.0 : 0.0;
+  if (last_cta(a.counter)) {
+    const double vrz = sum_partials(a.partials, a.nparts, 0, red);
+    const double vrr = sum_partials(a.partials, a.nparts, 1, red);
+    const double vbb = sum_partials(a.partials, a.nparts, 2, red);
+    if (threadIdx.x == 0) {
+      a.scal[SC_RZ] = vrz;
+      a.scal[SC_RR] = vrr;
+      a.scal[SC_BB] = vbb;
+      a.scal[SC_TOL2] = rtol * rtol * vbb;
+      a.scal[SC_BETA] = 0.0;
+      a.scal[SC_ITERS] = 0.0;
+      a.scal[SC_DONE] = (vrr <= rtol * rtol * vbb) ? 1.0 : 0.0;
+      *a.counter = 0u;
+    }
   }
 }
 
-// q = sign*A p, partial (p, q).  One warp per facet block row: the nfd rows
-// of a free facet share one column list (the DOFs of the facets sharing a cell
-// with it), so the warp reads that list once, gathers p into shared memory,
-// and streams the block row's nfd*rowlen contiguous values.
+// p_new = z + beta p_old ; q = sign*A p_new ; alpha = rz / (p_new, q).
+// One warp per facet block row: its nfd rows share one column list, read
+// once; p_new on those columns is formed in shared memory, then the block
+// row's nfd*rowlen contiguous values are streamed.
 constexpr int kMaxRowLen = 288;  // 11 neighbour facets x 25 DOFs (3D, k=4) fits
-__global__ void __launch_bounds__(kPcgThreads) pcg_spmv_kernel(PcgArgs a) {
+template <typename V, int NFD>
+__global__ void __launch_bounds__(kPcgThreads) pcg_spmv_kernel(PcgArgs a, const V *__restrict__ val,
+                                                               const double *__restrict__ p_old,
+                                                               double *__restrict__ p_new) {
   __shared__ double red[32];
   __shared__ double xs[kPcgThreads / 32][kMaxRowLen];
   if (a.scal[SC_DONE] != 0.0) return;
+  const double beta = a.scal[SC_BETA];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nw = (gridDim.x * blockDim.x) >> 5;
-  const int nfd = a.nfd;
   double acc = 0.0;
   for (int br = wid; br < a.nblockrows; br += nw) {
-    const int row0 = br * nfd;
+    const int row0 = br * NFD;
     const int64_t base = a.rowptr[row0];
     const int rowlen = (int)(a.rowptr[row0 + 1] - base);
-    for (int j = lane; j < rowlen; j += 32) xs[w][j] = a.p[a.colind[base + j]];
+    for (int j = lane; j < rowlen; j += 32) {
+      const int col = a.colind[base + j];
+      xs[w][j] = a.z[col] + beta * p_old[col];
+    }
+    double pown = 0.0;
+    if (lane < NFD) {
+      pown = a.z[row0 + lane] + beta * p_old[row0 + lane];
+      p_new[row0 + lane] = pown;
+    }
     __syncwarp();
-    for (int r = 0; r < nfd; ++r) {
-      const double *vr = a.val + base + (int64_t)r * rowlen;
-      double s = 0.0;
-      for (int j = lane; j < rowlen; j += 32) s += __ldcs(vr + j) * xs[w][j];
-      for (int off = 16; off > 0; off >>= 1) s += __shfl_xor_sync(0xffffffffu, s, off);
-      if (lane == 0) {
-        const double q = a.sign * s;
-        a.q[row0 + r] = q;
-        acc += q * a.p[row0 + r];
-      }
+    // every row's loads are issued before any reduction (NFD independent streams)
+    double s[NFD];
+#pragma unroll
+    for (int r = 0; r < NFD; ++r) s[r] = 0.0;
+    for (int j = lane; j < rowlen; j += 32) {
+      const double xv = xs[w][j];
+      const V *vj = val + base + j;
+#pragma unroll
+      for (int r = 0; r < NFD; ++r) s[r] += (double)__ldcs(vj + (int64_t)r * rowlen) * xv;
+    }
+    double mine = 0.0;
+#pragma unroll
+    for (int r = 0; r < NFD; ++r) {
+      double t = s[r];
+      for (int off = 16; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
+      if (lane == r) mine = t;
+    }
+    if (lane < NFD) {
+      const double q = a.sign * mine;
+      a.q[row0 + lane] = q;
+      acc += q * pown;
     }
     __syncwarp();
   }
   const double t = block_sum(acc, red);
   if (threadIdx.x == 0) a.partials[blockIdx.x] = t;
-}
-
-__global__ void pcg_alpha_kernel(PcgArgs a) {
-  __shared__ double red[32];
-  if (a.scal[SC_DONE] != 0.0) return;
-  double s = 0.0;
-  for (int i = threadIdx.x; i < a.nparts; i += blockDim.x) s += a.partials[i];
-  s = block_sum(s, red);
-  if (threadIdx.x == 0) {
-    a.scal[SC_PAP] = s;
-    a.scal[SC_ALPHA] = a.scal[SC_RZ] / s;
+  if (last_cta(a.counter)) {
+    const double pq = sum_partials(a.partials, a.nparts, 0, red);
+    if (threadIdx.x == 0) {
+      a.scal[SC_PAP] = pq;
+      a.scal[SC_ALPHA] = a.scal[SC_RZ] / pq;
+      *a.counter = 0u;
+    }
   }
 }
 
-// x += alpha p; r -= alpha q; z = Binv r; partial (r,z), (r,r)
-__global__ void pcg_update_kernel(PcgArgs a) {
-  __shared__ double rs[1024];
+// x += alpha p; r -= alpha q; z = Binv r; beta = (r,z)_new / (r,z); convergence
+__global__ void __launch_bounds__(kPcgThreads) pcg_update_kernel(PcgArgs a, const double *__restrict__ p) {
+  __shared__ double rs[kPcgThreads];
   __shared__ double red[32];
   if (a.scal[SC_DONE] != 0.0) return;
   const double alpha = a.scal[SC_ALPHA];
-  const int tile = (blockDim.x / a.nfd) * a.nfd;
+  const int tile = (kPcgThreads / a.nfd) * a.nfd;
   double rz = 0.0, rr = 0.0;
   for (int base = blockIdx.x * tile; base < a.n; base += gridDim.x * tile) {
     const int row = base + (int)threadIdx.x;
     const bool act = threadIdx.x < (unsigned)tile && row < a.n;
     double r = 0.0;
     if (act) {
-      a.x[row] += alpha * a.p[row];
+      a.x[row] += alpha * p[row];
       r = a.r[row] - alpha * a.q[row];
       a.r[row] = r;
       rr += r * r;
@@ -344,69 +380,78 @@ __global__ void pcg_update_kernel(PcgArgs a) {
   if (threadIdx.x == 0) a.partials[blockIdx.x] = s;
   s = block_sum(rr, red);
   if (threadIdx.x == 0) a.partials[a.nparts + blockIdx.x] = s;
-}
-
-__global__ void pcg_beta_kernel(PcgArgs a) {
-  __shared__ double red[32];
-  if (a.scal[SC_DONE] != 0.0) return;
-  double v[2];
-  for (int k = 0; k < 2; ++k) {
-    double s = 0.0;
-    for (int i = threadIdx.x; i < a.nparts; i += blockDim.x) s += a.partials[k * a.nparts + i];
-    v[k] = block_sum(s, red);
-  }
-  if (threadIdx.x == 0) {
-    a.scal[SC_BETA] = v[0] / a.scal[SC_RZ];
-    a.scal[SC_RZ] = v[0];
-    a.scal[SC_RR] = v[1];
-    a.scal[SC_ITERS] += 1.0;
-    if (v[1] <= a.scal[SC_TOL2]) a.scal[SC_DONE] = 1.0;
+  if (last_cta(a.counter)) {
+    const double vrz = sum_partials(a.partials, a.nparts, 0, red);
+    const double vrr = sum_partials(a.partials, a.nparts, 1, red);
+    if (threadIdx.x == 0) {
+      a.scal[SC_BETA] = vrz / a.scal[SC_RZ];
+      a.scal[SC_RZ] = vrz;
+      a.scal[SC_RR] = vrr;
+      a.scal[SC_ITERS] += 1.0;
+      if (vrr <= a.scal[SC_TOL2] || !(vrr == vrr)) a.scal[SC_DONE] = 1.0;
+      *a.counter = 0u;
+    }
   }
 }
 
-// p = z + beta p (runs in the converging iteration too; harmless)
-__global__ void pcg_p_kernel(PcgArgs a) {
-  if (a.scal[SC_DONE] != 0.0) return;
-  const double beta = a.scal[SC_BETA];
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x)
-    a.p[i] = a.z[i] + beta * a.p[i];
-}
-
-// Threads of the vector-update kernels: a tile of whole facet blocks
-// (kPcgThreads / nfd * nfd rows) rounded up to full warps -- block_sum's
-// full-mask shuffles need every lane of every warp to exist.
-static int update_threads(int nfd) {
-  (void)nfd;
-  return kPcgThreads;
-}
-
-cudaError_t launch_pcg_setup(const PcgArgs &a, double rtol, cudaStream_t s,
-                             int num_sms, long long *launches) {
+cudaError_t launch_pcg_setup(const PcgArgs &a, double rtol, cudaStream_t s, int num_sms,
+                             long long *launches) {
   if (a.nfd > 25) return cudaErrorInvalidValue;
   int g = (a.nblockrows + 127) / 128;
   if (g < 1) g = 1;
+  cudaError_t e = cudaMemsetAsync(a.counter, 0, sizeof(unsigned int), s);
+  if (e != cudaSuccess) return e;
   binv_kernel<<<g, 128, 0, s>>>(a);
-  pcg_init_kernel<<<a.nparts, update_threads(a.nfd), 0, s>>>(a);
-  pcg_init_reduce_kernel<<<1, 1024, 0, s>>>(a, rtol);
-  *launches += 3;
+  pcg_init_kernel<<<a.nparts, kPcgThreads, 0, s>>>(a, rtol);
+  *launches += 2;
   (void)num_sms;
   return cudaGetLastError();
 }
 
-cudaError_t launch_spmv(const PcgArgs &a, cudaStream_t s, long long *launches) {
-  pcg_spmv_kernel<<<a.nparts, kPcgThreads, 0, s>>>(a);
-  ++*launches;
+template <typename V>
+static cudaError_t spmv_dispatch(const PcgArgs &a, const V *val, const double *po, double *pn, cudaStream_t s) {
+  switch (a.nfd) {
+#define HDG_SPMV_CASE(N) \
+  case N:                \
+    pcg_spmv_kernel<V, N><<<a.nparts, kPcgThreads, 0, s>>>(a, val, po, pn); break;
+    HDG_SPMV_CASE(2)
+    HDG_SPMV_CASE(3)
+    HDG_SPMV_CASE(4)
+    HDG_SPMV_CASE(5)
+    HDG_SPMV_CASE(9)
+    HDG_SPMV_CASE(16)
+    HDG_SPMV_CASE(25)
+#undef HDG_SPMV_CASE
+    default:
+      return cudaErrorInvalidValue;
+  }
   return cudaGetLastError();
 }
 
-cudaError_t launch_pcg_iteration(const PcgArgs &a, cudaStream_t s, int num_sms,
-                                 long long *launches) {
-  pcg_spmv_kernel<<<a.nparts, kPcgThreads, 0, s>>>(a);
-  pcg_alpha_kernel<<<1, 1024, 0, s>>>(a);
-  pcg_update_kernel<<<a.nparts, update_threads(a.nfd), 0, s>>>(a);
-  pcg_beta_kernel<<<1, 1024, 0, s>>>(a);
-  pcg_p_kernel<<<a.nparts, 256, 0, s>>>(a);
-  *launches += 5;
+static cudaError_t spmv_any(const PcgArgs &a, const double *po, double *pn, cudaStream_t s) {
+  return a.val32 ? spmv_dispatch<float>(a, a.val32, po, pn, s) : spmv_dispatch<double>(a, a.val, po, pn, s);
+}
+
+bool pcg_supports_nfd(int nfd) {
+  return nfd == 2 || nfd == 3 || nfd == 4 || nfd == 5 || nfd == 9 || nfd == 16 || nfd == 25;
+}
+
+cudaError_t launch_spmv(const PcgArgs &a, cudaStream_t s, long long *launches) {
+  ++*launches;
+  return spmv_any(a, a.p, a.p2, s);
+}
+
+// Two PCG iterations (p buffers swap back to where they started).
+cudaError_t launch_pcg_iteration_pair(const PcgArgs &a, cudaStream_t s, int num_sms,
+                                      long long *launches) {
+  for (int half = 0; half < 2; ++half) {
+    const double *po = half ? a.p2 : a.p;
+    double *pn = half ? a.p : a.p2;
+    cudaError_t e = spmv_any(a, po, pn, s);
+    if (e != cudaSuccess) return e;
+    pcg_update_kernel<<<a.nparts, kPcgThreads, 0, s>>>(a, pn);
+  }
+  *launches += 4;
   (void)num_sms;
   return cudaGetLastError();
 }

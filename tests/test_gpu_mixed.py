@@ -1,0 +1,107 @@
+"""GPU tests of the FP32 + float-float-refined path against the FP64 oracle.
+
+Tolerances (stated per the mixed-precision contract):
+  * condensed cell blocks S, g: <= 1e-10 relative to the block's largest entry
+    (one refinement step measures ~5e-13 on 32^3 k=2 blocks);
+  * whole solves: <= 1e-8 relative error vs the FP64 oracle (both solved to a
+    residual of 1e-14 or by dense LU).
+"""
+import numpy as np
+import pytest
+
+import gridaphybrid_gb300 as gh
+from gridaphybrid_gb300 import _lib
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+RTOL_MIXED_CELL = 1e-10
+RTOL_MIXED_SOLVE = 1e-8
+
+
+def relmax(a, b):
+    return np.abs(np.asarray(a) - np.asarray(b)).max() / max(np.abs(np.asarray(b)).max(), 1e-300)
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    return gh.default_context()
+
+
+def _condense(ctx, A, b, ni, precision):
+    ncells, n, _ = A.shape
+    nf = n - ni
+    S = np.empty((ncells, nf, nf))
+    g = np.empty((ncells, nf))
+    info = np.zeros(ncells, dtype=np.int32)
+    rc = ctx.lib.hdg_static_condensation(ctx.handle, precision, ncells, ni, nf, _lib.ptr(np.ascontiguousarray(A)),
+                                         _lib.ptr(np.ascontiguousarray(b)), _lib.ptr(S), _lib.ptr(g),
+                                         _lib.ptr(info))
+    return rc, S, g, info
+
+
+@pytest.mark.parametrize("D,k,n", [(2, 1, (4, 3)), (2, 2, (3, 3)), (2, 3, (3, 2)), (3, 1, (2, 2, 2)), (3, 2, (3, 2, 2))])
+def test_mixed_condensation_hdg_blocks(ctx, D, k, n):
+    m = oracle.Mesh(D, n, k)
+    kappa = np.exp(np.random.default_rng(3).normal(size=m.ncells))
+    A, b = m.integrate(problem=oracle.PROBLEM_SIN, kappa=kappa)
+    S0, g0, _ = oracle.static_condensation(A, b, m.ni)
+    rc, S, g, info = _condense(ctx, A, b, m.ni, _lib.HDG_PREC_FP32_REFINED)
+    assert rc == 0 and (info == 0).all()
+    for c in range(m.ncells):
+        assert relmax(S[c], S0[c]) < RTOL_MIXED_CELL
+        assert relmax(g[c], g0[c]) < RTOL_MIXED_CELL
+
+
+def test_mixed_condensation_random_blocks(ctx):
+    rng = np.random.default_rng(8)
+    ni, nf, ncells = 48, 16, 40
+    n = ni + nf
+    A = rng.normal(size=(ncells, n, n))
+    A[:, np.arange(ni), np.arange(ni)] += 2.0 * np.sqrt(n)
+    b = rng.normal(size=(ncells, n))
+    S0, g0, _ = oracle.static_condensation(A, b, ni)
+    rc, S, g, info = _condense(ctx, A, b, ni, _lib.HDG_PREC_FP32_REFINED)
+    assert rc == 0
+    assert relmax(S, S0) < RTOL_MIXED_CELL and relmax(g, g0) < RTOL_MIXED_CELL
+
+
+def _op(D, k, n, kappa, precision, problem="sin"):
+    model = gh.CartesianDiscreteModel((0, 1) * D, n)
+    X, Y = gh.darcy_spaces(model, k)
+    return gh.HybridAffineFEOperator(gh.DarcyHDG(tau=1.0, problem=problem, kappa=kappa), X, Y, [1, 2], [3],
+                                     precision=precision)
+
+
+@pytest.mark.parametrize("D,k,n", [(2, 1, (8, 8)), (2, 2, (6, 6)), (2, 3, (5, 4)), (3, 1, (4, 4, 4)), (3, 2, (4, 4, 3))])
+def test_mixed_solution_vs_fp64_oracle(ctx, D, k, n):
+    kappa = np.exp(np.random.default_rng(12).normal(size=int(np.prod(n))))
+    op = _op(D, k, n, kappa, _lib.HDG_PREC_FP32_REFINED)
+    xh = gh.solve(op, solver="pcg", rtol=1e-14, maxit=5000)
+    ref = oracle.solve_darcy(D, k, n, problem=oracle.PROBLEM_SIN, kappa=kappa, solver=0)
+    assert relmax(xh.skeleton, ref["lam"]) < RTOL_MIXED_SOLVE
+    assert relmax(xh.cell_interior, ref["uint"]) < RTOL_MIXED_SOLVE
+    ef, ep = xh.l2_errors()
+    assert abs(ef - ref["err_flux"]) <= 0.01 * ref["err_flux"]
+
+
+def test_mixed_reference_exactness(ctx):
+    """The reference's exactness KAT (n.n_o stabilisation, linear u) through the
+    mixed path: still exact to 1e-8."""
+    model = gh.CartesianDiscreteModel((0, 1, 0, 1), (2, 2))
+    X, Y = gh.darcy_spaces(model, 1)
+    op = gh.HybridAffineFEOperator(gh.DarcyHDG(tau=1.0, stabilization="owner_sign", problem="ref_linear"),
+                                   X, Y, [1, 2], [3], precision=_lib.HDG_PREC_FP32_REFINED)
+    xh = gh.solve(op, solver="direct")
+    ef, ep = xh.l2_errors()
+    assert ef < 1e-8 and ep < 1e-8
+
+
+def test_mixed_assembled_system_symmetric_and_close(ctx):
+    kappa = np.exp(np.random.default_rng(13).normal(size=64))
+    op64 = _op(3, 2, (4, 4, 4), kappa, _lib.HDG_PREC_FP64)
+    op32 = _op(3, 2, (4, 4, 4), kappa, _lib.HDG_PREC_FP32_REFINED)
+    r64, c64, v64, rhs64 = op64.skeleton_system()
+    r32, c32, v32, rhs32 = op32.skeleton_system()
+    assert np.array_equal(r64, r32) and np.array_equal(c64, c32)
+    assert relmax(v32, v64) < RTOL_MIXED_CELL and relmax(rhs32, rhs64) < RTOL_MIXED_CELL
