@@ -51,6 +51,7 @@ SIGNATURES = {
     "hdg_static_condensation": (_i, [_vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp]),
     "hdg_backward_static_condensation": (_i, [_vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp]),
     "hdg_sum_facets": (_i, [_vp, _i, _i, _i, _vp, _vp]),
+    "hdg_static_condensation_noalloc": (_i, [_vp, _i, _i, _i, _vp, _vp, _vp, _vp, _vp]),
     "hdg_problem_create_cartesian": (_i, [_vp, _i, _vp, _vp, _i, ctypes.POINTER(_vp)]),
     "hdg_problem_create": (_i, [_vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp, ctypes.POINTER(_vp)]),
     "hdg_problem_destroy": (_i, [_vp]),

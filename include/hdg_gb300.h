@@ -107,6 +107,27 @@ int hdg_backward_static_condensation(hdg_context *ctx, int precision,
 int hdg_sum_facets(hdg_context *ctx, int nitems, int nfacets, int len,
                    const double *blocks, double *out);
 
+/* hdg_static_condensation with HDG_PREC_FP32_REFINED, for callers that cannot
+ * allocate device memory (a host framework whose caching allocator already
+ * holds the device's free memory, or a pipeline step where an allocation would
+ * synchronise the device).  No counterpart in the reference.
+ *  - Allocates nothing: A, b, S, g (and info, if not NULL) must be device
+ *    pointers; the temporaries (the FP32 hi/lo staging of every cell block)
+ *    live in one fixed device array of HDG_NOALLOC_SCRATCH_BYTES bytes that
+ *    every GPU loading this library keeps until the process exits.
+ *  - A batch needs 8*ncells*((ni+nf)^2 + ni+nf) bytes plus a little, and
+ *    4*ncells more when info is NULL; a larger batch is rejected with
+ *    HDG_ERR_INVALID (split it).
+ *  - The first call on a device looks the array's address up
+ *    (cudaGetSymbolAddress); make that first call before any stream capture.
+ *  - Every call uses the same array: calls that overlap on the GPU race, so
+ *    issue them on one stream (the context's) or order them with events.
+ * Results equal hdg_static_condensation(ctx, HDG_PREC_FP32_REFINED, ...). */
+#define HDG_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
+int hdg_static_condensation_noalloc(hdg_context *ctx, int ncells, int ni, int nf,
+                                    const double *A, const double *b, double *S,
+                                    double *g, int *info);
+
 /* ---------------------------------------------------------------------- */
 /* Operator level: HybridAffineFEOperator / solve.                          */
 /* ---------------------------------------------------------------------- */
