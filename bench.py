@@ -282,9 +282,12 @@ def run_gpu(args):
 
     peaks, peak_kind = measured_peaks()
     hbm = float(peaks["hbm_gbs"])
-    # SpMV: values + one column list per facet block row + block-row pointers + p gathered once + q written
+    # SpMV of the PCG iterations (FP32 inner SpMV on the refined path): values + one column
+    # list per facet block row + two row pointers per block row + z and p_old gathered once
+    # + p_new and q written once
     nblockrows = nfree // nfd
-    spmv_bytes = nnz * 8 + (nnz // nfd) * 4 + nblockrows * 16 + 2 * nfree * 8
+    vb = 4 if args.precision == "mixed" else 8
+    spmv_bytes = nnz * vb + (nnz // nfd) * 4 + nblockrows * 16 + 4 * nfree * vb
     spmv_gbs = spmv_bytes / (spmv_ms.value * 1e-3) / 1e9
     # assembly: condensed blocks + vectors read, CSR values + rhs written
     asm_bytes = ncells * (nf * nf + nf) * 8 + nnz * 8 + nfree * 8
@@ -299,7 +302,9 @@ def run_gpu(args):
                               [float(x) for x in phase])),
         "condense_cells_per_s": ncells / ((phase[0] + phase[1]) / 1000.0),
         "pcg_iters": mean_iters, "pcg_relres": rel, "full_solve_ms": ms,
-        "roofline": {"bound": "hbm", "kernel": "pcg_spmv_kernel", "achieved": spmv_gbs, "peak": hbm,
+        "roofline": {"bound": "hbm",
+                     "kernel": "pcg32_spmv_kernel" if args.precision == "mixed" else "pcg_spmv_kernel",
+                     "achieved": spmv_gbs, "peak": hbm,
                      "unit": "GB/s", "frac": spmv_gbs / hbm, "traffic": None, "peak_source": peak_kind,
                      "bytes_per_launch": spmv_bytes, "ms_per_launch": spmv_ms.value},
         "assembly_roofline": {"bound": "hbm", "achieved": asm_gbs, "peak": hbm, "unit": "GB/s",

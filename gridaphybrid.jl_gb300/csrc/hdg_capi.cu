@@ -181,6 +181,7 @@ AssembleArgs assemble_args(hdg_problem *pb) {
   as.cell_facets = pb->d_cell_facets.as<int>();
   as.facet_dofs = pb->d_facet_dofs.as<int>();
   as.dirvals = pb->d_dirvals.as<double>();
+  as.val32 = pb->precision == HDG_PREC_FP32_REFINED ? pb->d_val32.as<float>() : nullptr;
   return as;
 }
 
@@ -253,6 +254,7 @@ int setup_problem(hdg_problem *pb) {
 
 hdg_problem::~hdg_problem() {
   if (pcg_graph) cudaGraphExecDestroy(pcg_graph);
+  if (pcg32_graph) cudaGraphExecDestroy(pcg32_graph);
   if (h_pinned.ptr) {
     cudaFreeHost(h_pinned.ptr);
     h_pinned.ptr = nullptr;
@@ -617,6 +619,7 @@ int hdg_assemble(hdg_problem *pb, int precision, int *info) {
   CUDA_TRY(ctx, pb->d_info.reserve(sizeof(int) * nc));
   CUDA_TRY(ctx, pb->d_val.reserve(sizeof(double) * (pb->pat.nnz ? pb->pat.nnz : 1)));
   CUDA_TRY(ctx, pb->d_rhs.reserve(sizeof(double) * (pb->mesh.nfree ? pb->mesh.nfree : 1)));
+  if (mixed) CUDA_TRY(ctx, pb->d_val32.reserve(sizeof(float) * (pb->pat.nnz ? pb->pat.nnz : 1)));
   cudaEvent_t *ev = ctx->ev;
   pb->precision = precision;
   pb->assembled = pb->solved = pb->recovered = false;
@@ -693,6 +696,114 @@ static PcgArgs pcg_args(hdg_problem *pb) {
   return a;
 }
 
+static Pcg32Args pcg32_args(hdg_problem *pb) {
+  const size_t n = pb->mesh.nfree;
+  float *v = pb->d_v32.as<float>();
+  Pcg32Args ia{};
+  ia.n = (int)n;
+  ia.nfd = pb->mesh.nfd;
+  ia.nblockrows = pb->pat.nblockrows;
+  ia.rowptr = pb->d_rowptr.as<int64_t>();
+  ia.colind = pb->d_colind.as<int>();
+  ia.val32 = pb->d_val32.as<float>();
+  ia.Binv32 = pb->d_Binv32.as<float>();
+  ia.rhs = pb->d_r.as<double>();  // the outer residual
+  ia.x = v;
+  ia.r = v + n;
+  ia.z = v + 2 * n;
+  ia.p = v + 3 * n;
+  ia.p2 = v + 4 * n;
+  ia.q = v + 5 * n;
+  ia.partials = pb->d_partials.as<double>();
+  ia.scal = pb->d_scal.as<double>();
+  ia.counter = pb->d_counter.as<unsigned int>();
+  ia.nparts = pb->ctx->num_sms * 4;
+  ia.sign = -1.0;
+  return ia;
+}
+
+// Mixed-precision skeleton solve: FP32 inner PCG inside an FP64 residual loop.
+// Requires launch_pcg_setup to have produced the FP64 block inverses.
+static int solve_pcg_refined(hdg_problem *pb, double rtol, int maxit, int *it_out, double *rel_out) {
+  hdg_context *ctx = pb->ctx;
+  const size_t n = pb->mesh.nfree, nfd = pb->mesh.nfd, nbr = pb->pat.nblockrows;
+  if (!pb->d_val32.ptr) return ctx->fail(HDG_ERR_STATE, "the FP32 matrix copy is missing (assemble in FP32_REFINED)");
+  CUDA_TRY(ctx, pb->d_Binv32.reserve(sizeof(float) * nbr * nfd * nfd));
+  CUDA_TRY(ctx, pb->d_v32.reserve(sizeof(float) * 6 * n));
+  CUDA_TRY(ctx, pb->d_scal2.reserve(sizeof(double) * 16));
+  CUDA_TRY(ctx, launch_binv_to_f32(nbr * nfd * nfd, pb->d_Binv.as<double>(), pb->d_Binv32.as<float>(), ctx->stream,
+                                   &ctx->launches));
+  Pcg32Args ia = pcg32_args(pb);
+  OuterArgs oa{};
+  oa.n = (int)n;
+  oa.nfd = (int)nfd;
+  oa.nblockrows = (int)nbr;
+  oa.rowptr = ia.rowptr;
+  oa.colind = ia.colind;
+  oa.val = pb->d_val.as<double>();
+  oa.rhs = pb->d_rhs.as<double>();
+  oa.x = pb->d_x.as<double>();
+  oa.r = pb->d_r.as<double>();
+  oa.partials = ia.partials;
+  oa.scal = pb->d_scal2.as<double>();
+  oa.counter = ia.counter;
+  oa.nparts = ia.nparts;
+  oa.sign = -1.0;
+  const int pairs = 8;
+  if (!pb->pcg32_graph) {
+    cudaGraph_t g;
+    long long dummy = 0;
+    CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    for (int i = 0; i < pairs; ++i) launch_pcg32_iteration_pair(ia, ctx->stream, &dummy);
+    CUDA_TRY(ctx, cudaStreamEndCapture(ctx->stream, &g));
+    cudaError_t e = cudaGraphInstantiate(&pb->pcg32_graph, g, 0);
+    cudaGraphDestroy(g);
+    CUDA_TRY(ctx, e);
+  }
+  double *h = static_cast<double *>(pb->h_pinned.ptr);
+  double *ho = h + 16;
+  CUDA_TRY(ctx, launch_outer_init(oa, ctx->stream, &ctx->launches));
+  CUDA_TRY(ctx, cudaMemcpyAsync(ho, oa.scal, sizeof(double) * 2, cudaMemcpyDeviceToHost, ctx->stream));
+  CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  const double cc = ho[0];
+  double rr = ho[1];
+  int total = 0, outer = 0;
+  int status = HDG_OK;
+  while (cc > 0.0 && rr > rtol * rtol * cc) {
+    if (total >= maxit || outer >= 30) {
+      status = ctx->fail(HDG_ERR_NOT_CONVERGED, "refined PCG: relative residual %.3e after %d iterations",
+                         std::sqrt(rr / cc), total);
+      break;
+    }
+    // ask the inner solve for the reduction still missing (FP32 cannot go much below 1e-5)
+    const double eta = std::max(1e-5, 0.3 * rtol * std::sqrt(cc / rr));
+    CUDA_TRY(ctx, launch_pcg32_init(ia, eta, ctx->stream, &ctx->launches));
+    int inner = 0;
+    for (;;) {
+      CUDA_TRY(ctx, cudaGraphLaunch(pb->pcg32_graph, ctx->stream));
+      ctx->launches += 4LL * pairs;
+      CUDA_TRY(ctx, cudaMemcpyAsync(h, ia.scal, sizeof(double) * 16, cudaMemcpyDeviceToHost, ctx->stream));
+      CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+      inner = (int)h[8];
+      if (h[7] != 0.0 || total + inner >= maxit || !std::isfinite(h[4])) break;
+    }
+    total += inner;
+    ++outer;
+    CUDA_TRY(ctx, launch_outer_update(oa, ia.x, ctx->stream, &ctx->launches));
+    CUDA_TRY(ctx, cudaMemcpyAsync(ho, oa.scal, sizeof(double) * 2, cudaMemcpyDeviceToHost, ctx->stream));
+    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    rr = ho[1];
+    if (!std::isfinite(rr)) {
+      status = ctx->fail(HDG_ERR_NOT_CONVERGED, "refined PCG breakdown (non-finite residual)");
+      break;
+    }
+  }
+  pb->last_outer = outer;
+  *it_out = total;
+  *rel_out = cc > 0.0 ? std::sqrt(rr / cc) : 0.0;
+  return status;
+}
+
 int hdg_solve_skeleton(hdg_problem *pb, int solver, double rtol, int maxit, int *iters,
                        double *relres) {
   if (!pb) return HDG_ERR_INVALID;
@@ -745,6 +856,10 @@ int hdg_solve_skeleton(hdg_problem *pb, int solver, double rtol, int maxit, int 
     PcgArgs a = pcg_args(pb);
     CUDA_TRY(ctx, launch_pcg_setup(a, rtol, ctx->stream, ctx->num_sms, &ctx->launches));
     const int pairs = 8;  // 16 iterations per graph replay
+    if (pb->precision == HDG_PREC_FP32_REFINED) {
+      status = solve_pcg_refined(pb, rtol, maxit, &it, &rel);
+      if (status == HDG_ERR_CUDA) return status;
+    } else {
     if (!pb->pcg_graph) {
       cudaGraph_t g;
       long long dummy = 0;
@@ -773,6 +888,7 @@ int hdg_solve_skeleton(hdg_problem *pb, int solver, double rtol, int maxit, int 
         status = ctx->fail(HDG_ERR_NOT_CONVERGED, "PCG breakdown (non-finite residual)");
         break;
       }
+    }
     }
   }
   CUDA_TRY(ctx, cudaEventRecord(ev[5], ctx->stream));
@@ -912,12 +1028,17 @@ int hdg_time_kernel(hdg_problem *pb, int which, int reps, double *ms_per_launch)
   cudaSetDevice(ctx->device);
   AssembleArgs as = assemble_args(pb);
   PcgArgs pa{};
+  Pcg32Args pa32{};
   DBuf zero_scal;
+  const bool mixed_spmv = which == 3 && pb->precision == HDG_PREC_FP32_REFINED;
+  if (mixed_spmv && !pb->d_v32.ptr) return ctx->fail(HDG_ERR_STATE, "SpMV timing needs a refined PCG solve first");
   if (which == 3) {
     pa = pcg_args(pb);
+    pa32 = pcg32_args(pb);
     CUDA_TRY(ctx, zero_scal.reserve(sizeof(double) * 16));
     CUDA_TRY(ctx, cudaMemsetAsync(zero_scal.ptr, 0, sizeof(double) * 16, ctx->stream));
     pa.scal = zero_scal.as<double>();  // an SC_DONE of 0 keeps the kernel active
+    pa32.scal = zero_scal.as<double>();
   }
   auto launch = [&]() -> cudaError_t {
     switch (which) {
@@ -930,7 +1051,9 @@ int hdg_time_kernel(hdg_problem *pb, int which, int reps, double *ms_per_launch)
                                pb->d_val.as<double>(), pb->d_rhs.as<double>(), ctx->stream, ctx->num_sms,
                                &ctx->launches);
       case 3:
-        return launch_spmv(pa, ctx->stream, &ctx->launches);
+        // the SpMV the solve iterates: FP32 inner SpMV on the refined path
+        return mixed_spmv ? launch_pcg32_spmv(pa32, ctx->stream, &ctx->launches)
+                          : launch_spmv(pa, ctx->stream, &ctx->launches);
       default:
         return run_recover(pb);
     }

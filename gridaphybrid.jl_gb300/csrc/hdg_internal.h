@@ -171,6 +171,11 @@ struct hdg_problem {
   hdg::DBuf d_br_row0, d_br_src, d_blk_off, d_blk_rowlen, d_blk_src, d_diag_blk,
       d_dir_cells;
   hdg::DBuf d_Binv, d_x, d_r, d_z, d_p, d_p2, d_q, d_partials, d_scal, d_counter;
+  // mixed-precision skeleton solve: FP32 matrix copy, FP32 block inverses,
+  // inner vectors (x, r, z, p, p2, q), outer scalars
+  hdg::DBuf d_val32, d_Binv32, d_v32, d_scal2;
+  cudaGraphExec_t pcg32_graph = nullptr;
+  int last_outer = 0;
   hdg::DBuf d_uint;
   hdg::DBuf h_pinned;  // host staging
   cudaGraphExec_t pcg_graph = nullptr;

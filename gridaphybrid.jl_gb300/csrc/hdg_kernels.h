@@ -117,6 +117,7 @@ struct AssembleArgs {
   int ndir_cells;
   const int *cell_facets, *facet_dofs;
   const double *dirvals;
+  float *val32;  // when non-null, also receives the values rounded to FP32
 };
 cudaError_t launch_assemble(const AssembleArgs &a, const double *S,
                             const double *g, double *glift, double *val,
@@ -147,6 +148,43 @@ cudaError_t launch_pcg_iteration_pair(const PcgArgs &a, cudaStream_t s, int num_
 cudaError_t launch_spmv(const PcgArgs &a, cudaStream_t s, long long *launches);
 // facet block sizes the PCG kernels are instantiated for
 bool pcg_supports_nfd(int nfd);
+
+// Inner FP32 PCG of the mixed-precision skeleton solve (solves M e = rhs,
+// M = sign*A, with FP32 values and vectors; dot products in FP64).
+struct Pcg32Args {
+  int n, nfd, nblockrows;
+  const int64_t *rowptr;
+  const int *colind;
+  const float *val32;
+  const float *Binv32;
+  const double *rhs;  // inner right-hand side, already in the M frame
+  float *x, *r, *z, *p, *p2, *q;
+  double *partials, *scal;
+  unsigned int *counter;
+  int nparts;
+  double sign;
+};
+// Outer FP64 refinement: x, r = sign*rhs - M x with the FP64 matrix.
+struct OuterArgs {
+  int n, nfd, nblockrows;
+  const int64_t *rowptr;
+  const int *colind;
+  const double *val;
+  const double *rhs;
+  double *x, *r;
+  double *partials, *scal;  // scal[0] = |c|^2, scal[1] = |r|^2
+  unsigned int *counter;
+  int nparts;
+  double sign;
+};
+cudaError_t launch_binv_to_f32(size_t count, const double *Binv, float *Binv32, cudaStream_t s,
+                               long long *launches);
+cudaError_t launch_pcg32_init(const Pcg32Args &a, double eta, cudaStream_t s, long long *launches);
+cudaError_t launch_pcg32_iteration_pair(const Pcg32Args &a, cudaStream_t s, long long *launches);
+cudaError_t launch_pcg32_spmv(const Pcg32Args &a, cudaStream_t s, long long *launches);
+cudaError_t launch_outer_init(const OuterArgs &a, cudaStream_t s, long long *launches);
+// x += e, then r = c - M x and |r|^2
+cudaError_t launch_outer_update(const OuterArgs &a, const float *e, cudaStream_t s, long long *launches);
 // dense LU solve of a CSR system (small n), one CTA
 cudaError_t launch_dense_solve(int n, const int64_t *rowptr, const int *colind,
                                const double *val, const double *rhs, double *work,

@@ -1,0 +1,105 @@
+// k_pcg_common.cuh -- device helpers shared by the skeleton PCG kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace hdg {
+
+// Device scalars of a PCG solve (double array).
+enum {
+  SC_RZ = 0,     // (r, z)
+  SC_PAP = 1,    // (p, A p)
+  SC_ALPHA = 2,
+  SC_BETA = 3,
+  SC_RR = 4,     // (r, r)
+  SC_BB = 5,     // (b, b)
+  SC_TOL2 = 6,   // rtol^2 (b, b)
+  SC_DONE = 7,   // 1 once converged
+  SC_ITERS = 8,  // completed iterations
+  SC_NSCAL = 16
+};
+
+constexpr int kPcgThreads = 256;
+constexpr int kMaxRowLen = 288;  // 11 neighbour facets x 25 DOFs (3D, k=4) fits
+
+__device__ __forceinline__ double block_sum(double v, double *red) {
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) red[w] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += red[i];
+  return s;  // valid in thread 0
+}
+
+// After every CTA has stored its partials: true in the CTA that arrives last.
+__device__ __forceinline__ bool last_cta(unsigned int *counter) {
+  __shared__ bool is_last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) is_last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  __syncthreads();
+  return is_last;
+}
+
+// sum of partials[k*nparts + 0..nparts) in index order (called by the last CTA)
+__device__ __forceinline__ double sum_partials(const double *partials, int nparts, int k, double *red) {
+  double s = 0.0;
+  for (int i = threadIdx.x; i < nparts; i += blockDim.x) s += __ldcg(partials + (size_t)k * nparts + i);
+  return block_sum(s, red);
+}
+
+template <int N>
+struct Pow2Ceil {
+  static constexpr int v = N <= 1 ? 1 : N <= 2 ? 2 : N <= 4 ? 4 : N <= 8 ? 8 : N <= 16 ? 16 : 32;
+};
+
+// Warp reduce-scatter of P per-lane partial sums (P a power of two <= 32):
+// each butterfly step keeps half of the remaining entries, so a lane does
+// P/2 + P/4 + ... + 1 (+ the remaining plain steps) additions instead of
+// 5 per entry.  Afterwards lane l holds the warp-wide total of entry
+// reduce_scatter_row<P>(l); the 32/P lanes with equal high bits share it.
+template <typename T, int P>
+__device__ __forceinline__ T warp_reduce_scatter(T (&v)[P], int lane) {
+  int cnt = P;
+#pragma unroll
+  for (int off = 16; off >= 1; off >>= 1) {
+    if (cnt > 1) {
+      const int half = cnt / 2;
+      const bool upper = (lane & off) != 0;
+#pragma unroll
+      for (int i = 0; i < half; ++i) {
+        const T send = upper ? v[i] : v[i + half];
+        const T keep = upper ? v[i + half] : v[i];
+        v[i] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+      }
+      cnt = half;
+    } else {
+      v[0] += __shfl_xor_sync(0xffffffffu, v[0], off);
+    }
+  }
+  return v[0];
+}
+
+template <int P>
+__device__ __forceinline__ int reduce_scatter_row(int lane) {
+  int r = 0, cnt = P;
+#pragma unroll
+  for (int off = 16; off >= 1; off >>= 1) {
+    if (cnt > 1) {
+      const int half = cnt / 2;
+      if (lane & off) r += half;
+      cnt = half;
+    }
+  }
+  return r;
+}
+
+// the lowest lane holding each entry after warp_reduce_scatter<P>
+template <int P>
+__device__ __forceinline__ bool reduce_scatter_writer(int lane) {
+  return (lane & (32 / P - 1)) == 0;
+}
+
+}  // namespace hdg

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include "hdg_kernels.h"
+#include "k_pcg_common.cuh"
 
 namespace hdg {
 
@@ -63,6 +64,7 @@ __global__ void assemble_blocks_kernel(AssembleArgs a, const double *__restrict_
       double v = S0[(r0 + ra) + (size_t)nf * (c0 + cb)];
       if (S1) v += S1[(r1 + ra) + (size_t)nf * (c1 + cb)];
       val[off + (int64_t)ra * rowlen + cb] = v;
+      if (a.val32) a.val32[off + (int64_t)ra * rowlen + cb] = (float)v;
     }
   }
 }
@@ -126,50 +128,6 @@ cudaError_t launch_assemble(const AssembleArgs &a, const double *S, const double
 // double-buffered, so a CUDA graph of an even number of iterations can be
 // replayed; once SC_DONE is set every kernel returns immediately.
 // ---------------------------------------------------------------------------
-enum {
-  SC_RZ = 0,     // (r, z)
-  SC_PAP = 1,    // (p, A p)
-  SC_ALPHA = 2,
-  SC_BETA = 3,
-  SC_RR = 4,     // (r, r)
-  SC_BB = 5,     // (b, b)
-  SC_TOL2 = 6,   // rtol^2 (b, b)
-  SC_DONE = 7,   // 1 once converged
-  SC_ITERS = 8,  // completed iterations
-  SC_NSCAL = 16
-};
-
-constexpr int kPcgThreads = 256;
-
-__device__ __forceinline__ double block_sum(double v, double *red) {
-  for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
-  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  __syncthreads();
-  if (l == 0) red[w] = v;
-  __syncthreads();
-  double s = 0.0;
-  if (threadIdx.x == 0)
-    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += red[i];
-  return s;  // valid in thread 0
-}
-
-// After every CTA has stored its partials: true in the CTA that arrives last.
-__device__ __forceinline__ bool last_cta(unsigned int *counter) {
-  __shared__ bool is_last;
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) is_last = atomicAdd(counter, 1u) == gridDim.x - 1;
-  __syncthreads();
-  return is_last;
-}
-
-// sum of partials[k*nparts + 0..nparts) in index order, by the last CTA
-__device__ __forceinline__ double sum_partials(const double *partials, int nparts, int k, double *red) {
-  double s = 0.0;
-  for (int i = threadIdx.x; i < nparts; i += blockDim.x) s += __ldcg(partials + (size_t)k * nparts + i);
-  return block_sum(s, red);
-}
-
 // Inverse of each facet's diagonal block of sign*A (Gauss-Jordan, partial pivoting).
 __global__ void binv_kernel(PcgArgs a) {
   const int nfd = a.nfd;
@@ -289,7 +247,6 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_init_kernel(PcgArgs a, double
 // One warp per facet block row: its nfd rows share one column list, read
 // once; p_new on those columns is formed in shared memory, then the block
 // row's nfd*rowlen contiguous values are streamed.
-constexpr int kMaxRowLen = 288;  // 11 neighbour facets x 25 DOFs (3D, k=4) fits
 template <typename V, int NFD>
 __global__ void __launch_bounds__(kPcgThreads) pcg_spmv_kernel(PcgArgs a, const V *__restrict__ val,
                                                                const double *__restrict__ p_old,
@@ -326,17 +283,17 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_spmv_kernel(PcgArgs a, const 
 #pragma unroll
       for (int r = 0; r < NFD; ++r) s[r] += (double)__ldcs(vj + (int64_t)r * rowlen) * xv;
     }
-    double mine = 0.0;
+    constexpr int P = Pow2Ceil<NFD>::v;
+    double v[P];
 #pragma unroll
-    for (int r = 0; r < NFD; ++r) {
-      double t = s[r];
-      for (int off = 16; off > 0; off >>= 1) t += __shfl_xor_sync(0xffffffffu, t, off);
-      if (lane == r) mine = t;
-    }
-    if (lane < NFD) {
-      const double q = a.sign * mine;
-      a.q[row0 + lane] = q;
-      acc += q * pown;
+    for (int r = 0; r < P; ++r) v[r] = r < NFD ? s[r] : 0.0;
+    const double tot = warp_reduce_scatter<double, P>(v, lane);
+    const int myrow = reduce_scatter_row<P>(lane);
+    const double pmine = __shfl_sync(0xffffffffu, pown, myrow < NFD ? myrow : 0);
+    if (myrow < NFD && reduce_scatter_writer<P>(lane)) {
+      const double q = a.sign * tot;
+      a.q[row0 + myrow] = q;
+      acc += q * pmine;
     }
     __syncwarp();
   }
