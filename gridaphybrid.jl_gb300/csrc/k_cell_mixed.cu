@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include "hdg_kernels.h"
+#include "k_condense_mixed_rt.cuh"
 
 namespace hdg {
 
@@ -486,9 +487,42 @@ size_t condense_mixed_smem(int ni, int nf) {
   return sizeof(float) * ((size_t)ni * (n + 1) + (size_t)ni * (nf + 1)) + sizeof(int) * ni;
 }
 
+template <class C>
+static cudaError_t launch_rt(int ncells, const float *Ahi, const float *Alo, const float *bhi, const float *blo,
+                             double *S, double *g, float *Xhi, float *Xlo, int *info, cudaStream_t s, int num_sms) {
+  const size_t smem = C::smem_bytes;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(rt::condense_mixed_rt_kernel<C>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  int per_sm = (int)((228 * 1024) / (smem + 1024));
+  const int by_threads = 2048 / C::NT;
+  if (per_sm > by_threads) per_sm = by_threads;
+  if (per_sm < 1) per_sm = 1;
+  int grid = num_sms * per_sm;
+  if (grid > ncells) grid = ncells;
+  if (grid < 1) grid = 1;
+  rt::condense_mixed_rt_kernel<C><<<grid, C::NT, smem, s>>>(ncells, Ahi, Alo, bhi, blo, S, g, Xhi, Xlo, info);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_condense_mixed(int ncells, int ni, int nf, const float *Ahi, const float *Alo,
                                   const float *bhi, const float *blo, double *S, double *g, float *Xhi,
                                   float *Xlo, int *info, cudaStream_t s, int num_sms, long long *launches) {
+  // register-tiled kernel for the cell sizes of the Darcy HDG spaces
+  // (2D k = 1, 2, 3; 3D k = 1, 2); the shared-memory kernel below otherwise
+#define HDG_RT_CASE(NI, NF, TR, TC)                                                                      \
+  if (ni == NI && nf == NF) {                                                                            \
+    ++*launches;                                                                                         \
+    return launch_rt<rt::Cfg<NI, NF, TR, TC>>(ncells, Ahi, Alo, bhi, blo, S, g, Xhi, Xlo, info, s, num_sms); \
+  }
+  HDG_RT_CASE(108, 54, 16, 16)
+  HDG_RT_CASE(48, 16, 16, 8)
+  HDG_RT_CASE(32, 24, 16, 8)
+  HDG_RT_CASE(27, 12, 8, 8)
+  HDG_RT_CASE(12, 8, 4, 8)
+#undef HDG_RT_CASE
   const size_t smem = condense_mixed_smem(ni, nf);
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(condense_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
