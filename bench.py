@@ -178,7 +178,7 @@ def run_gpu(args):
     import gridaphybrid_gb300 as gh
     from gridaphybrid_gb300 import _lib
 
-    precs = {"fp64": _lib.HDG_PREC_FP64, "mixed": _lib.HDG_PREC_FP32_REFINED}
+    precs = {"fp64": _lib.HDG_PREC_FP64, "mixed": _lib.HDG_PREC_FP32_REFINED, "ffblock": _lib.HDG_PREC_FF_BLOCK}
     prec = precs[args.precision]
     ctx = gh.Context(0)
     lib = ctx.lib
@@ -286,7 +286,7 @@ def run_gpu(args):
     # list per facet block row + two row pointers per block row + z and p_old gathered once
     # + p_new and q written once
     nblockrows = nfree // nfd
-    vb = 4 if args.precision == "mixed" else 8
+    vb = 8 if args.precision == "fp64" else 4
     spmv_bytes = nnz * vb + (nnz // nfd) * 4 + nblockrows * 16 + 4 * nfree * vb
     spmv_gbs = spmv_bytes / (spmv_ms.value * 1e-3) / 1e9
     # assembly: condensed blocks + vectors read, CSR values + rhs written
@@ -296,14 +296,14 @@ def run_gpu(args):
         "metric": METRIC, "value": ncells / (ms / 1000.0), "unit": UNIT, "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32+ff-refined" if args.precision == "mixed" else "f64",
+        "dtype": {"fp64": "f64", "mixed": "f32+ff-refined", "ffblock": "ff(2xf32)+f32-pcg"}[args.precision],
         "data": "synthetic", "config": workload_config(args.precision),
         "phases_ms": dict(zip(["integrate", "condense", "assemble", "skeleton_pcg", "recover"],
                               [float(x) for x in phase])),
         "condense_cells_per_s": ncells / ((phase[0] + phase[1]) / 1000.0),
         "pcg_iters": mean_iters, "pcg_relres": rel, "full_solve_ms": ms,
         "roofline": {"bound": "hbm",
-                     "kernel": "pcg32_spmv_kernel" if args.precision == "mixed" else "pcg_spmv_kernel",
+                     "kernel": "pcg_spmv_kernel" if args.precision == "fp64" else "pcg32_spmv_kernel",
                      "achieved": spmv_gbs, "peak": hbm,
                      "unit": "GB/s", "frac": spmv_gbs / hbm, "traffic": None, "peak_source": peak_kind,
                      "bytes_per_launch": spmv_bytes, "ms_per_launch": spmv_ms.value},
@@ -326,7 +326,10 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="mixed", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="ffblock", choices=["fp64", "mixed", "ffblock"],
+                    help="fp64: plain FP64 path; mixed: FP32 LU + float-float refinement; "
+                         "ffblock: Darcy block elimination in float-float (both fast paths use the FP32 "
+                         "inner PCG with FP64 residual refinement)")
     ap.add_argument("--no-fp64-compare", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -145,6 +145,16 @@ cudaError_t run_condense(hdg_problem *pb) {
                                 pb->d_S.as<double>(), pb->d_g.as<double>(), pb->d_fact.as<double>(),
                                 pb->d_info.as<int>(), ctx->stream, ctx->num_sms, &ctx->launches);
   float *Ahi = pb->d_A.as<float>(), *bhi = pb->d_b.as<float>(), *Xhi = pb->d_fact.as<float>();
+  if (pb->precision == HDG_PREC_FF_BLOCK) {
+    CellArgs a = cell_args(pb);
+    cudaError_t e = launch_inv_mass_scale(a, pb->d_invm.as<double>(), ctx->stream, &ctx->launches);
+    if (e != cudaSuccess) return e;
+    const float *Mh = pb->d_minv.as<float>(), *Ml = Mh + (size_t)pb->tab.nk * pb->tab.nk;
+    return launch_condense_ffblock(pb->tab.D, pb->tab.k, (int)nc, Ahi, Ahi + nc * n * n, bhi, bhi + nc * n, Mh, Ml,
+                                   pb->d_invm.as<double>(), pb->d_S.as<double>(), pb->d_g.as<double>(), Xhi,
+                                   Xhi + nc * ni * (nf + 1), pb->d_info.as<int>(), ctx->stream, ctx->num_sms,
+                                   &ctx->launches);
+  }
   return launch_condense_mixed((int)nc, (int)ni, (int)nf, Ahi, Ahi + nc * n * n, bhi, bhi + nc * n,
                                pb->d_S.as<double>(), pb->d_g.as<double>(), Xhi, Xhi + nc * ni * (nf + 1),
                                pb->d_info.as<int>(), ctx->stream, ctx->num_sms, &ctx->launches);
@@ -181,7 +191,7 @@ AssembleArgs assemble_args(hdg_problem *pb) {
   as.cell_facets = pb->d_cell_facets.as<int>();
   as.facet_dofs = pb->d_facet_dofs.as<int>();
   as.dirvals = pb->d_dirvals.as<double>();
-  as.val32 = pb->precision == HDG_PREC_FP32_REFINED ? pb->d_val32.as<float>() : nullptr;
+  as.val32 = pb->precision != HDG_PREC_FP64 ? pb->d_val32.as<float>() : nullptr;
   return as;
 }
 
@@ -230,6 +240,15 @@ int setup_problem(hdg_problem *pb) {
   std::vector<float> packed_f;
   pb->toff_f = pack_tables_ff(pb->tab, packed_f);
   if ((rc = upload(ctx, pb->d_tabf, packed_f))) return rc;
+  {  // M_ref^{-1} as (hi, lo) floats for the block-elimination path
+    const std::vector<double> &Mi = pb->tab.Minv;
+    std::vector<float> mf(2 * Mi.size());
+    for (size_t i = 0; i < Mi.size(); ++i) {
+      mf[i] = (float)Mi[i];
+      mf[Mi.size() + i] = (float)(Mi[i] - (double)mf[i]);
+    }
+    if ((rc = upload(ctx, pb->d_minv, mf))) return rc;
+  }
   if ((rc = upload(ctx, pb->d_origin, pb->mesh.origin))) return rc;
   if ((rc = upload(ctx, pb->d_jac, pb->mesh.jac))) return rc;
   if ((rc = upload(ctx, pb->d_cell_facets, pb->mesh.cell_facets))) return rc;
@@ -599,15 +618,20 @@ static float elapsed(cudaEvent_t a, cudaEvent_t b) {
 int hdg_assemble(hdg_problem *pb, int precision, int *info) {
   if (!pb) return HDG_ERR_INVALID;
   hdg_context *ctx = pb->ctx;
-  if (precision != HDG_PREC_FP64 && precision != HDG_PREC_FP32_REFINED)
+  if (precision != HDG_PREC_FP64 && precision != HDG_PREC_FP32_REFINED && precision != HDG_PREC_FF_BLOCK)
     return ctx->fail(HDG_ERR_INVALID, "unknown precision %d", precision);
   cudaSetDevice(ctx->device);
   const RefTables &t = pb->tab;
   const size_t nc = pb->mesh.ncells, n = t.n, ni = t.ni, nf = t.nf;
-  const bool mixed = precision == HDG_PREC_FP32_REFINED;
-  const size_t need = mixed ? condense_mixed_smem((int)ni, (int)nf) : n * (n + 1) * sizeof(double);
+  const bool mixed = precision != HDG_PREC_FP64;
+  if (precision == HDG_PREC_FF_BLOCK && !ffblock_supported(t.D, t.k))
+    return ctx->fail(HDG_ERR_INVALID, "block elimination is built for D=2, k<=3 and D=3, k<=2");
+  const size_t need = precision == HDG_PREC_FP32_REFINED ? condense_mixed_smem((int)ni, (int)nf)
+                      : precision == HDG_PREC_FP64       ? n * (n + 1) * sizeof(double)
+                                                         : 0;
   if (need > ctx->smem_optin - 1024)
     return ctx->fail(HDG_ERR_INVALID, "cell block %zu exceeds the shared-memory condensation kernel", n);
+  if (precision == HDG_PREC_FF_BLOCK) CUDA_TRY(ctx, pb->d_invm.reserve(sizeof(double) * nc));
   // cell blocks: FP64, or (hi, lo) float pairs in the same bytes
   CUDA_TRY(ctx, pb->d_A.reserve(sizeof(double) * nc * n * n));
   CUDA_TRY(ctx, pb->d_b.reserve(sizeof(double) * nc * n));
@@ -856,7 +880,7 @@ int hdg_solve_skeleton(hdg_problem *pb, int solver, double rtol, int maxit, int 
     PcgArgs a = pcg_args(pb);
     CUDA_TRY(ctx, launch_pcg_setup(a, rtol, ctx->stream, ctx->num_sms, &ctx->launches));
     const int pairs = 8;  // 16 iterations per graph replay
-    if (pb->precision == HDG_PREC_FP32_REFINED) {
+    if (pb->precision != HDG_PREC_FP64) {
       status = solve_pcg_refined(pb, rtol, maxit, &it, &rel);
       if (status == HDG_ERR_CUDA) return status;
     } else {
@@ -1030,7 +1054,7 @@ int hdg_time_kernel(hdg_problem *pb, int which, int reps, double *ms_per_launch)
   PcgArgs pa{};
   Pcg32Args pa32{};
   DBuf zero_scal;
-  const bool mixed_spmv = which == 3 && pb->precision == HDG_PREC_FP32_REFINED;
+  const bool mixed_spmv = which == 3 && pb->precision != HDG_PREC_FP64;
   if (mixed_spmv && !pb->d_v32.ptr) return ctx->fail(HDG_ERR_STATE, "SpMV timing needs a refined PCG solve first");
   if (which == 3) {
     pa = pcg_args(pb);

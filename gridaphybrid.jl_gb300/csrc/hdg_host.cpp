@@ -168,6 +168,36 @@ int build_ref_tables(int D, int k, RefTables &t) {
         for (int e = 0; e < D; ++e) t.G[(e * nk + a) * nk + b] += wq * grad[a * D + e] * val[b];
       }
   }
+  // M^{-1} (Gauss-Jordan with partial pivoting, FP64) for the block-elimination path
+  {
+    std::vector<double> Mw(t.M), Iv(nk * nk, 0.0);
+    for (int i = 0; i < nk; ++i) Iv[i * nk + i] = 1.0;
+    for (int c = 0; c < nk; ++c) {
+      int pr = c;
+      for (int i = c + 1; i < nk; ++i)
+        if (std::fabs(Mw[i * nk + c]) > std::fabs(Mw[pr * nk + c])) pr = i;
+      if (pr != c)
+        for (int j = 0; j < nk; ++j) {
+          std::swap(Mw[c * nk + j], Mw[pr * nk + j]);
+          std::swap(Iv[c * nk + j], Iv[pr * nk + j]);
+        }
+      const double piv = Mw[c * nk + c];
+      for (int j = 0; j < nk; ++j) {
+        Mw[c * nk + j] /= piv;
+        Iv[c * nk + j] /= piv;
+      }
+      for (int i = 0; i < nk; ++i) {
+        if (i == c) continue;
+        const double f = Mw[i * nk + c];
+        if (f != 0.0)
+          for (int j = 0; j < nk; ++j) {
+            Mw[i * nk + j] -= f * Mw[c * nk + j];
+            Iv[i * nk + j] -= f * Iv[c * nk + j];
+          }
+      }
+    }
+    t.Minv = Iv;
+  }
   // facet tables: facet parameters are the non-normal directions, increasing
   const int nqf = ipow(t.n1, D - 1);
   t.F.assign(2 * D * nk * nk, 0.0);

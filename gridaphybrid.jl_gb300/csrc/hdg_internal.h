@@ -66,6 +66,7 @@ struct RefTables {
   std::vector<double> qxi; // nqv x D volume points
   std::vector<double> qw;  // nqv
   std::vector<double> qphi;// nqv x nk
+  std::vector<double> Minv;// nk x nk inverse of M (block elimination path)
 };
 int build_ref_tables(int D, int k, RefTables &t);
 
@@ -174,6 +175,8 @@ struct hdg_problem {
   // mixed-precision skeleton solve: FP32 matrix copy, FP32 block inverses,
   // inner vectors (x, r, z, p, p2, q), outer scalars
   hdg::DBuf d_val32, d_Binv32, d_v32, d_scal2;
+  // block-elimination path: M_ref^{-1} as (hi, lo) floats, 1/m per cell
+  hdg::DBuf d_minv, d_invm;
   cudaGraphExec_t pcg32_graph = nullptr;
   int last_outer = 0;
   hdg::DBuf d_uint;

@@ -103,6 +103,14 @@ cudaError_t launch_condense_mixed(int ncells, int ni, int nf, const float *Ahi, 
                                   const float *bhi, const float *blo, double *S, double *g,
                                   float *Xhi, float *Xlo, int *info, cudaStream_t s, int num_sms,
                                   long long *launches);
+// Darcy block elimination in float-float (HDG_PREC_FF_BLOCK)
+bool ffblock_supported(int D, int k);
+cudaError_t launch_inv_mass_scale(const CellArgs &a, double *inv_m, cudaStream_t s, long long *launches);
+cudaError_t launch_condense_ffblock(int D, int k, int ncells, const float *Ahi, const float *Alo,
+                                    const float *bhi, const float *blo, const float *Minv_h,
+                                    const float *Minv_l, const double *inv_m, double *S, double *g,
+                                    float *Xhi, float *Xlo, int *info, cudaStream_t s, int num_sms,
+                                    long long *launches);
 cudaError_t launch_recover_mixed(const CellArgs &a, const float *Xhi, const float *Xlo,
                                  const double *lambda, const double *dirvals, double *uint,
                                  cudaStream_t s, int num_sms, long long *launches);

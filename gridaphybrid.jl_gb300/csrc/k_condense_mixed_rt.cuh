@@ -2,14 +2,18 @@
 // (the fast form of condense_mixed for the cell sizes it is instantiated for).
 //
 // One CTA per cell.  The interior rows of [A_ii | A_if | b_i] (NI x (N+1))
-// live in registers: thread (tr, tc) of a TR x TC grid owns rows
-// i = tr + TR*a and columns c = tc + TC*b.  Partial pivoting is implicit:
-// the pivot row of step j is "retired" (its rank is j) instead of being
-// swapped, so no data moves; each step publishes the pivot row and the
+// live in registers for the whole kernel: thread (tr, tc) of a TR x TC grid
+// owns rows i = tr + TR*a and columns c = tc + TC*b.  Partial pivoting is
+// implicit: the pivot row of step j is "retired" (its rank is j) instead of
+// being swapped, so no data moves; each step publishes the pivot row and the
 // multipliers through shared memory and updates the owned tile in registers.
-// The triangular solves with the right-hand-side columns run in the same
-// layout.  The float-float residual and Schur product run afterwards, with
-// the factors parked in shared memory and the registers reused.
+// After the factorisation the L\U part of the tile stays put and only the
+// right-hand-side columns are rewritten by the solves:
+//   X0 = A_ii^{-1} [A_if | b_i]                       (FP32)
+//   repeat NSTEP times:  R = [A_if | b_i] - A_ii X     (float-float)
+//                        X += A_ii^{-1} R              (FP32 correction)
+//   S = A_ff - A_fi X,  g = b_f - A_fi y               (float-float)
+// X is held as the unevaluated pair (X0, sum of corrections).
 #pragma once
 #include <cuda_runtime.h>
 
@@ -54,10 +58,11 @@ struct Cfg {
   static constexpr int RPT = (NI + TR - 1) / TR;
   static constexpr int CPT = (NCOL + TC - 1) / TC;
   static constexpr int NT = TR * TC;
-  static constexpr int CC = 14;  // right-hand-side columns per task in the float-float products
+  static constexpr int CC = 7;  // right-hand-side columns per task in the float-float products
   static constexpr int NCHUNK = (NC + CC - 1) / CC;
-  static constexpr size_t smem_floats = (size_t)NI * NI + 2 * (size_t)NI * NC + 2 * NI + 2 * NCOL + NI;
-  static constexpr size_t smem_bytes = smem_floats * 4 + 2 * NI * 4;
+  static constexpr int NSTEP = 2;  // refinement steps
+  static constexpr size_t smem_floats = 3 * (size_t)NI * NC + 2 * NI + 2 * NCOL + NI;
+  static constexpr size_t smem_bytes = smem_floats * 4 + (NI + 2) * 4;
 };
 
 constexpr int kRetiredNot = INT_MAX;
@@ -95,8 +100,8 @@ __device__ __forceinline__ void colset(float (&row)[CPT], int b, float v) {
     if (y == b) row[y] = v;
 }
 
-// Back substitution with the RHS columns (c >= NI) of the tile: U x = y in rank
-// order; x_m ends up in the row of rank m.  lbuf/ubuf double-buffered.
+// Back substitution on the RHS columns (c >= NI): U x = y in rank order; x_m
+// ends up in the row of rank m.  lbuf/ubuf double-buffered by step parity.
 template <class C>
 __device__ __forceinline__ void back_substitute(float (&W)[C::RPT][C::CPT], const int (&rk)[C::RPT],
                                                 const int *perm, const float *rdiag, float *lbuf,
@@ -142,6 +147,83 @@ __device__ __forceinline__ void back_substitute(float (&W)[C::RPT][C::CPT], cons
   __syncthreads();
 }
 
+// Forward elimination L^{-1} P on the RHS columns (rows in rank order).
+template <class C>
+__device__ __forceinline__ void forward_eliminate(float (&W)[C::RPT][C::CPT], const int (&rk)[C::RPT],
+                                                  const int *perm, float *lbuf, float *ubuf, int tr, int tc) {
+  for (int j = 0; j < C::NI; ++j) {
+    const int buf = j & 1;
+    const int p = perm[j];
+    const int trp = p % C::TR, ap = p / C::TR;
+    if (tr == trp) {
+#pragma unroll
+      for (int b = 0; b < C::CPT; ++b) {
+        const int c = tc + C::TC * b;
+        if (c >= C::NI && c < C::NCOL) ubuf[buf * C::NCOL + c] = pick(W, ap, b);
+      }
+    }
+    const int tcj = j % C::TC, bj = j / C::TC;
+    if (tc == tcj) {
+#pragma unroll
+      for (int a = 0; a < C::RPT; ++a) {
+        const int i = tr + C::TR * a;
+        if (i < C::NI && rk[a] > j) lbuf[buf * C::NI + i] = colget(W[a], bj);
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int a = 0; a < C::RPT; ++a) {
+      const int i = tr + C::TR * a;
+      if (i < C::NI && rk[a] > j) {
+        const float l = lbuf[buf * C::NI + i];
+#pragma unroll
+        for (int b = 0; b < C::CPT; ++b) {
+          const int c = tc + C::TC * b;
+          if (c >= C::NI && c < C::NCOL) W[a][b] = fmaf(-l, ubuf[buf * C::NCOL + c], W[a][b]);
+        }
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// Rs (natural row order) = [A_if | b_i] - A_ii (X0s + Ds) in float-float;
+// with_d = false ignores Ds (first step).
+template <class C>
+__device__ __forceinline__ void residual(const float *__restrict__ Ah, const float *__restrict__ Al,
+                                         const float *__restrict__ bh, const float *__restrict__ bl,
+                                         const float *X0s, const float *Ds, float *Rs, bool with_d) {
+  constexpr int NI = C::NI, NF = C::NF, N = C::N, NC = C::NC, CC = C::CC;
+  for (int task = threadIdx.x; task < NI * C::NCHUNK; task += C::NT) {
+    const int i = task % NI, c0 = (task / NI) * CC;
+    float hs[CC], ls[CC];
+#pragma unroll
+    for (int q = 0; q < CC; ++q) hs[q] = ls[q] = 0.0f;
+    for (int k = 0; k < NI; ++k) {
+      const float ah = __ldg(Ah + i + (size_t)N * k), al = __ldg(Al + i + (size_t)N * k);
+      if (with_d) {
+#pragma unroll
+        for (int q = 0; q < CC; ++q)
+          if (c0 + q < NC) ff_mac2(hs[q], ls[q], ah, al, X0s[k + NI * (c0 + q)], Ds[k + NI * (c0 + q)]);
+      } else {
+#pragma unroll
+        for (int q = 0; q < CC; ++q)
+          if (c0 + q < NC) ff_mac(hs[q], ls[q], ah, al, X0s[k + NI * (c0 + q)]);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < CC; ++q) {
+      const int col = c0 + q;
+      if (col < NC) {
+        const float rh = col < NF ? __ldg(Ah + i + (size_t)N * (NI + col)) : bh[i];
+        const float rl = col < NF ? __ldg(Al + i + (size_t)N * (NI + col)) : bl[i];
+        Rs[i + NI * col] = ((rh - hs[q]) + rl) - ls[q];
+      }
+    }
+  }
+  __syncthreads();
+}
+
 template <class C>
 __global__ void __launch_bounds__(C::NT, (C::NT <= 128 ? 4 : 2))
     condense_mixed_rt_kernel(int ncells, const float *__restrict__ Ahi, const float *__restrict__ Alo,
@@ -150,10 +232,10 @@ __global__ void __launch_bounds__(C::NT, (C::NT <= 128 ? 4 : 2))
   constexpr int NI = C::NI, NF = C::NF, N = C::N, NC = C::NC, NCOL = C::NCOL, RPT = C::RPT, CPT = C::CPT;
   constexpr int TR = C::TR, TC = C::TC, CC = C::CC, NCHUNK = C::NCHUNK;
   extern __shared__ float smem[];
-  float *LUs = smem;                 // NI x NI, row r = rank r (packed L\U of P A_ii)
-  float *X0s = LUs + NI * NI;        // NI x NC column-major, unknown order
-  float *Ds = X0s + NI * NC;         // NI x NC column-major: residual, then correction
-  float *lbuf = Ds + NI * NC;        // 2 x NI
+  float *X0s = smem;                 // NI x NC column-major, unknown order
+  float *Ds = X0s + NI * NC;         // NI x NC, sum of the corrections, unknown order
+  float *Rs = Ds + NI * NC;          // NI x NC, residual, natural row order
+  float *lbuf = Rs + NI * NC;        // 2 x NI
   float *ubuf = lbuf + 2 * NI;       // 2 x NCOL
   float *rdiag = ubuf + 2 * NCOL;    // NI
   int *perm = reinterpret_cast<int *>(rdiag + NI);  // NI: pivot row of step j
@@ -257,103 +339,48 @@ __global__ void __launch_bounds__(C::NT, (C::NT <= 128 ? 4 : 2))
     __syncthreads();
     // ---------------- X0 = U^{-1} (L^{-1} P [A_if | b_i]) ----------------
     back_substitute<C>(W, rk, perm, rdiag, lbuf, ubuf, tr, tc);
-    // park the factors (by rank) and X0 (unknown order) in shared memory
 #pragma unroll
     for (int a = 0; a < RPT; ++a) {
       const int i = tr + TR * a;
       if (i >= NI) continue;
-      const int r = rk[a];
 #pragma unroll
       for (int b = 0; b < CPT; ++b) {
         const int c = tc + TC * b;
-        if (c < NI) LUs[r * NI + c] = W[a][b];
-        else if (c < NCOL) X0s[r + NI * (c - NI)] = W[a][b];
+        if (c >= NI && c < NCOL) X0s[rk[a] + NI * (c - NI)] = W[a][b];
       }
     }
     __syncthreads();
-    // ---------------- R = [A_if | b_i] - A_ii X0 in float-float ----------------
-    for (int task = t; task < NI * NCHUNK; task += C::NT) {
-      const int i = task % NI, c0 = (task / NI) * CC;
-      float hs[CC], ls[CC];
-#pragma unroll
-      for (int q = 0; q < CC; ++q) hs[q] = ls[q] = 0.0f;
-      for (int k = 0; k < NI; ++k) {
-        const float ah = __ldg(Ah + i + (size_t)N * k), al = __ldg(Al + i + (size_t)N * k);
-#pragma unroll
-        for (int q = 0; q < CC; ++q)
-          if (c0 + q < NC) ff_mac(hs[q], ls[q], ah, al, X0s[k + NI * (c0 + q)]);
-      }
-#pragma unroll
-      for (int q = 0; q < CC; ++q) {
-        const int col = c0 + q;
-        if (col < NC) {
-          const float rh = col < NF ? __ldg(Ah + i + (size_t)N * (NI + col)) : bh[i];
-          const float rl = col < NF ? __ldg(Al + i + (size_t)N * (NI + col)) : bl[i];
-          Ds[i + NI * col] = ((rh - hs[q]) + rl) - ls[q];
-        }
-      }
-    }
-    __syncthreads();
-    // ---------------- delta = A_ii^{-1} R with the FP32 factors ----------------
-#pragma unroll
-    for (int a = 0; a < RPT; ++a) {
-      const int i = tr + TR * a;
-#pragma unroll
-      for (int b = 0; b < CPT; ++b) {
-        const int c = tc + TC * b;
-        float v = 0.0f;
-        if (i < NI) v = (c < NI) ? LUs[rk[a] * NI + c] : (c < NCOL ? Ds[i + NI * (c - NI)] : 0.0f);
-        W[a][b] = v;
-      }
-    }
-    __syncthreads();
-    for (int j = 0; j < NI; ++j) {  // forward: L^{-1} P, rows in rank order
-      const int buf = j & 1;
-      const int p = perm[j];
-      const int trp = p % TR, ap = p / TR;
-      if (tr == trp) {
-#pragma unroll
-        for (int b = 0; b < CPT; ++b) {
-          const int c = tc + TC * b;
-          if (c >= NI && c < NCOL) ubuf[buf * NCOL + c] = pick(W, ap, b);
-        }
-      }
-      const int tcj = j % TC, bj = j / TC;
-      if (tc == tcj) {
-#pragma unroll
-        for (int a = 0; a < RPT; ++a) {
-          const int i = tr + TR * a;
-          if (i < NI && rk[a] > j) lbuf[buf * NI + i] = colget(W[a], bj);
-        }
-      }
-      __syncthreads();
+    // ---------------- refinement: X += A_ii^{-1} ([A_if | b_i] - A_ii X) ----------------
+    for (int step = 0; step < C::NSTEP; ++step) {
+      residual<C>(Ah, Al, bh, bl, X0s, Ds, Rs, step > 0);
+      // the L\U part of the tile is untouched; reload only the RHS columns
 #pragma unroll
       for (int a = 0; a < RPT; ++a) {
         const int i = tr + TR * a;
-        if (i < NI && rk[a] > j) {
-          const float l = lbuf[buf * NI + i];
 #pragma unroll
-          for (int b = 0; b < CPT; ++b) {
-            const int c = tc + TC * b;
-            if (c >= NI && c < NCOL) W[a][b] = fmaf(-l, ubuf[buf * NCOL + c], W[a][b]);
+        for (int b = 0; b < CPT; ++b) {
+          const int c = tc + TC * b;
+          if (i < NI && c >= NI && c < NCOL) W[a][b] = Rs[i + NI * (c - NI)];
+        }
+      }
+      forward_eliminate<C>(W, rk, perm, lbuf, ubuf, tr, tc);
+      back_substitute<C>(W, rk, perm, rdiag, lbuf, ubuf, tr, tc);
+#pragma unroll
+      for (int a = 0; a < RPT; ++a) {
+        const int i = tr + TR * a;
+        if (i >= NI) continue;
+#pragma unroll
+        for (int b = 0; b < CPT; ++b) {
+          const int c = tc + TC * b;
+          if (c >= NI && c < NCOL) {
+            const int e = rk[a] + NI * (c - NI);
+            Ds[e] = step == 0 ? W[a][b] : Ds[e] + W[a][b];
           }
         }
       }
+      __syncthreads();
     }
-    __syncthreads();
-    back_substitute<C>(W, rk, perm, rdiag, lbuf, ubuf, tr, tc);
-#pragma unroll
-    for (int a = 0; a < RPT; ++a) {
-      const int i = tr + TR * a;
-      if (i >= NI) continue;
-#pragma unroll
-      for (int b = 0; b < CPT; ++b) {
-        const int c = tc + TC * b;
-        if (c >= NI && c < NCOL) Ds[rk[a] + NI * (c - NI)] = W[a][b];
-      }
-    }
-    __syncthreads();
-    // ---------------- S = A_ff - A_fi X1, g = b_f - A_fi y1 (float-float) ----------------
+    // ---------------- S = A_ff - A_fi X, g = b_f - A_fi y (float-float) ----------------
     for (int task = t; task < NF * NCHUNK; task += C::NT) {
       const int ar = task % NF, c0 = (task / NF) * CC;
       float hs[CC], ls[CC];

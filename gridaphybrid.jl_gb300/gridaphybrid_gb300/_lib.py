@@ -21,6 +21,7 @@ HDG_ERR_NODEVICE = 7
 
 HDG_PREC_FP64 = 0
 HDG_PREC_FP32_REFINED = 1
+HDG_PREC_FF_BLOCK = 2
 HDG_STAB_TEXTBOOK = 0
 HDG_STAB_OWNER_SIGN = 1
 HDG_PROBLEM_REF_LINEAR = 0

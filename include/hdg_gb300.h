@@ -43,6 +43,11 @@ extern "C" {
 /* Arithmetic of the cell-local work. */
 #define HDG_PREC_FP64 0          /* FP64 integration, LU and Schur complement */
 #define HDG_PREC_FP32_REFINED 1  /* FP32 LU, refined with high-precision residuals */
+/* Operator path only (hdg_assemble): the Darcy cell matrix's flux block is
+ * (|J|/kappa)(I (x) M_ref), so the condensation is done by block elimination
+ * (a small pressure-Schur LU and dense products) entirely in float-float on
+ * the FP32 pipes; skeleton solve and recovery as for HDG_PREC_FP32_REFINED. */
+#define HDG_PREC_FF_BLOCK 2
 
 /* Stabilisation of the Darcy HDG form. */
 #define HDG_STAB_TEXTBOOK 0     /* tau*(p - l) on every facet side (LDG-H) */

@@ -73,10 +73,14 @@ def _op(D, k, n, kappa, precision, problem="sin"):
                                      precision=precision)
 
 
+FAST_PRECISIONS = [_lib.HDG_PREC_FP32_REFINED, _lib.HDG_PREC_FF_BLOCK]
+
+
+@pytest.mark.parametrize("precision", FAST_PRECISIONS)
 @pytest.mark.parametrize("D,k,n", [(2, 1, (8, 8)), (2, 2, (6, 6)), (2, 3, (5, 4)), (3, 1, (4, 4, 4)), (3, 2, (4, 4, 3))])
-def test_mixed_solution_vs_fp64_oracle(ctx, D, k, n):
+def test_mixed_solution_vs_fp64_oracle(ctx, D, k, n, precision):
     kappa = np.exp(np.random.default_rng(12).normal(size=int(np.prod(n))))
-    op = _op(D, k, n, kappa, _lib.HDG_PREC_FP32_REFINED)
+    op = _op(D, k, n, kappa, precision)
     xh = gh.solve(op, solver="pcg", rtol=1e-14, maxit=5000)
     ref = oracle.solve_darcy(D, k, n, problem=oracle.PROBLEM_SIN, kappa=kappa, solver=0)
     assert relmax(xh.skeleton, ref["lam"]) < RTOL_MIXED_SOLVE
@@ -97,11 +101,31 @@ def test_mixed_reference_exactness(ctx):
     assert ef < 1e-8 and ep < 1e-8
 
 
-def test_mixed_assembled_system_symmetric_and_close(ctx):
+@pytest.mark.parametrize("precision", FAST_PRECISIONS)
+def test_mixed_assembled_system_close_to_fp64(ctx, precision):
     kappa = np.exp(np.random.default_rng(13).normal(size=64))
     op64 = _op(3, 2, (4, 4, 4), kappa, _lib.HDG_PREC_FP64)
-    op32 = _op(3, 2, (4, 4, 4), kappa, _lib.HDG_PREC_FP32_REFINED)
+    op32 = _op(3, 2, (4, 4, 4), kappa, precision)
     r64, c64, v64, rhs64 = op64.skeleton_system()
     r32, c32, v32, rhs32 = op32.skeleton_system()
     assert np.array_equal(r64, r32) and np.array_equal(c64, c32)
     assert relmax(v32, v64) < RTOL_MIXED_CELL and relmax(rhs32, rhs64) < RTOL_MIXED_CELL
+
+
+@pytest.mark.parametrize("D,k,n", [(2, 1, (5, 3)), (2, 2, (4, 4)), (2, 3, (3, 3)), (3, 1, (3, 3, 2)), (3, 2, (3, 3, 3))])
+def test_ffblock_condensed_blocks_match_fp64(ctx, D, k, n):
+    """Block elimination in float-float: assembled skeleton values within 1e-12
+    of the FP64 path (float-float carries ~48 bits), on high-contrast kappa."""
+    kappa = np.exp(2.0 * np.random.default_rng(17).normal(size=int(np.prod(n))))
+    op64 = _op(D, k, n, kappa, _lib.HDG_PREC_FP64)
+    opff = _op(D, k, n, kappa, _lib.HDG_PREC_FF_BLOCK)
+    _, _, v64, rhs64 = op64.skeleton_system()
+    _, _, vff, rhsff = opff.skeleton_system()
+    assert relmax(vff, v64) < 1e-12 and relmax(rhsff, rhs64) < 1e-12
+
+
+def test_ffblock_rejected_at_map_level(ctx):
+    A = np.zeros((1, 20, 20))
+    b = np.zeros((1, 20))
+    rc, S, g, info = _condense(ctx, A, b, 12, _lib.HDG_PREC_FF_BLOCK)
+    assert rc == _lib.HDG_ERR_INVALID
