@@ -282,12 +282,21 @@ def run_gpu(args):
 
     peaks, peak_kind = measured_peaks()
     hbm = float(peaks["hbm_gbs"])
-    # SpMV of the PCG iterations (FP32 inner SpMV on the refined path): values + one column
-    # list per facet block row + two row pointers per block row + z and p_old gathered once
-    # + p_new and q written once
+    # SpMV of the PCG iterations.  FP64 path: CSR values + one column list per
+    # facet block row + two row pointers per block row + z and p_old gathered
+    # once + p_new and q written once.  Fast paths (unassembled FP32 cell
+    # operator): the cell records (upper facet blocks, padded to 16 bytes) +
+    # the cell->block-row map + z and p_old read once + p_new written once +
+    # the per-cell products written.
     nblockrows = nfree // nfd
-    vb = 8 if args.precision == "fp64" else 4
-    spmv_bytes = nnz * vb + (nnz // nfd) * 4 + nblockrows * 16 + 4 * nfree * vb
+    nl = 6
+    if args.precision == "fp64":
+        spmv_bytes = nnz * 8 + (nnz // nfd) * 4 + nblockrows * 16 + 4 * nfree * 8
+        spmv_kernel = "pcg_spmv_kernel<double,9>"
+    else:
+        rec = (nl * (nl + 1) // 2 * nfd * nfd + 3) // 4 * 4
+        spmv_bytes = ncells * rec * 4 + ncells * nl * 4 + 3 * nfree * 4 + ncells * nf * 4
+        spmv_kernel = "cell_spmv32_kernel<6,9>"
     spmv_gbs = spmv_bytes / (spmv_ms.value * 1e-3) / 1e9
     # assembly: condensed blocks + vectors read, CSR values + rhs written
     asm_bytes = ncells * (nf * nf + nf) * 8 + nnz * 8 + nfree * 8
@@ -303,7 +312,7 @@ def run_gpu(args):
         "condense_cells_per_s": ncells / ((phase[0] + phase[1]) / 1000.0),
         "pcg_iters": mean_iters, "pcg_relres": rel, "full_solve_ms": ms,
         "roofline": {"bound": "hbm",
-                     "kernel": "pcg_spmv_kernel" if args.precision == "fp64" else "pcg32_spmv_kernel",
+                     "kernel": spmv_kernel,
                      "achieved": spmv_gbs, "peak": hbm,
                      "unit": "GB/s", "frac": spmv_gbs / hbm, "traffic": None, "peak_source": peak_kind,
                      "bytes_per_launch": spmv_bytes, "ms_per_launch": spmv_ms.value},

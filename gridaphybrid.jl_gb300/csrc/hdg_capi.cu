@@ -191,7 +191,6 @@ AssembleArgs assemble_args(hdg_problem *pb) {
   as.cell_facets = pb->d_cell_facets.as<int>();
   as.facet_dofs = pb->d_facet_dofs.as<int>();
   as.dirvals = pb->d_dirvals.as<double>();
-  as.val32 = pb->precision != HDG_PREC_FP64 ? pb->d_val32.as<float>() : nullptr;
   return as;
 }
 
@@ -264,6 +263,7 @@ int setup_problem(hdg_problem *pb) {
   if ((rc = upload(ctx, pb->d_blk_src, p.blk_src))) return rc;
   if ((rc = upload(ctx, pb->d_diag_blk, p.diag_blk))) return rc;
   if ((rc = upload(ctx, pb->d_dir_cells, p.dir_cells))) return rc;
+  if ((rc = upload(ctx, pb->d_cell_blk, p.cell_blk))) return rc;
   if ((rc = upload_dirichlet(pb))) return rc;
   CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   return HDG_OK;
@@ -643,7 +643,10 @@ int hdg_assemble(hdg_problem *pb, int precision, int *info) {
   CUDA_TRY(ctx, pb->d_info.reserve(sizeof(int) * nc));
   CUDA_TRY(ctx, pb->d_val.reserve(sizeof(double) * (pb->pat.nnz ? pb->pat.nnz : 1)));
   CUDA_TRY(ctx, pb->d_rhs.reserve(sizeof(double) * (pb->mesh.nfree ? pb->mesh.nfree : 1)));
-  if (mixed) CUDA_TRY(ctx, pb->d_val32.reserve(sizeof(float) * (pb->pat.nnz ? pb->pat.nnz : 1)));
+  const int nl = 2 * t.D;
+  if (mixed && !cellop_supported(nl, (int)t.nfd))
+    return ctx->fail(HDG_ERR_INVALID, "no unassembled FP32 operator for %d facets of %zu DOFs", nl, t.nfd);
+  if (mixed) CUDA_TRY(ctx, pb->d_cellop.reserve(sizeof(float) * nc * cellop_rec(nl, (int)t.nfd)));
   cudaEvent_t *ev = ctx->ev;
   pb->precision = precision;
   pb->assembled = pb->solved = pb->recovered = false;
@@ -656,6 +659,10 @@ int hdg_assemble(hdg_problem *pb, int precision, int *info) {
   CUDA_TRY(ctx, launch_assemble(as, pb->d_S.as<double>(), pb->d_g.as<double>(), pb->d_aux.as<double>(),
                                 pb->d_val.as<double>(), pb->d_rhs.as<double>(), ctx->stream, ctx->num_sms,
                                 &ctx->launches));
+  if (mixed)  // the FP32 operator of the inner skeleton iterations, in the SPD frame
+    CUDA_TRY(ctx, launch_pack_cell_blocks((int)nc, nl, (int)t.nfd, -1.0, pb->d_S.as<double>(),
+                                          pb->d_cellop.as<float>(), ctx->smem_optin, ctx->stream, ctx->num_sms,
+                                          &ctx->launches));
   CUDA_TRY(ctx, cudaEventRecord(ev[3], ctx->stream));
   std::vector<int> hinfo(nc);
   CUDA_TRY(ctx, cudaMemcpyAsync(hinfo.data(), pb->d_info.ptr, sizeof(int) * nc, cudaMemcpyDeviceToHost, ctx->stream));
@@ -727,9 +734,6 @@ static Pcg32Args pcg32_args(hdg_problem *pb) {
   ia.n = (int)n;
   ia.nfd = pb->mesh.nfd;
   ia.nblockrows = pb->pat.nblockrows;
-  ia.rowptr = pb->d_rowptr.as<int64_t>();
-  ia.colind = pb->d_colind.as<int>();
-  ia.val32 = pb->d_val32.as<float>();
   ia.Binv32 = pb->d_Binv32.as<float>();
   ia.rhs = pb->d_r.as<double>();  // the outer residual
   ia.x = v;
@@ -737,12 +741,20 @@ static Pcg32Args pcg32_args(hdg_problem *pb) {
   ia.z = v + 2 * n;
   ia.p = v + 3 * n;
   ia.p2 = v + 4 * n;
-  ia.q = v + 5 * n;
   ia.partials = pb->d_partials.as<double>();
   ia.scal = pb->d_scal.as<double>();
   ia.counter = pb->d_counter.as<unsigned int>();
   ia.nparts = pb->ctx->num_sms * 4;
-  ia.sign = -1.0;
+  ia.ncells = pb->mesh.ncells;
+  ia.nl = 2 * pb->mesh.D;
+  ia.rec = cellop_rec(ia.nl, ia.nfd);
+  ia.blocks = pb->d_cellop.as<float>();
+  ia.cell_blk = pb->d_cell_blk.as<int>();
+  ia.br_src = pb->d_br_src.as<int>();
+  ia.qc = pb->d_qc.as<float>();
+  ia.nstage = pb->cellop_nstage;
+  ia.ctas = pb->cellop_ctas;
+  ia.error = pb->d_counter.as<unsigned int>() + 1;
   return ia;
 }
 
@@ -751,9 +763,16 @@ static Pcg32Args pcg32_args(hdg_problem *pb) {
 static int solve_pcg_refined(hdg_problem *pb, double rtol, int maxit, int *it_out, double *rel_out) {
   hdg_context *ctx = pb->ctx;
   const size_t n = pb->mesh.nfree, nfd = pb->mesh.nfd, nbr = pb->pat.nblockrows;
-  if (!pb->d_val32.ptr) return ctx->fail(HDG_ERR_STATE, "the FP32 matrix copy is missing (assemble in FP32_REFINED)");
+  if (!pb->d_cellop.ptr) return ctx->fail(HDG_ERR_STATE, "the FP32 cell operator is missing (assemble in a fast precision)");
+  const int nl = 2 * pb->mesh.D;
+  CUDA_TRY(ctx, cellop_configure(nl, (int)nfd, ctx->smem_optin, ctx->num_sms, &pb->cellop_nstage, &pb->cellop_ctas));
+  if (pb->cellop_ctas > ctx->num_sms * 4)
+    return ctx->fail(HDG_ERR_INVALID, "cell operator grid exceeds the partials buffer");
   CUDA_TRY(ctx, pb->d_Binv32.reserve(sizeof(float) * nbr * nfd * nfd));
-  CUDA_TRY(ctx, pb->d_v32.reserve(sizeof(float) * 6 * n));
+  CUDA_TRY(ctx, pb->d_v32.reserve(sizeof(float) * 5 * n));
+  CUDA_TRY(ctx, pb->d_qc.reserve(sizeof(float) * pb->mesh.ncells * nl * nfd));
+  // last-CTA counter and the bulk-copy error flag start at zero
+  CUDA_TRY(ctx, cudaMemsetAsync(pb->d_counter.ptr, 0, sizeof(unsigned int) * 2, ctx->stream));
   CUDA_TRY(ctx, pb->d_scal2.reserve(sizeof(double) * 16));
   CUDA_TRY(ctx, launch_binv_to_f32(nbr * nfd * nfd, pb->d_Binv.as<double>(), pb->d_Binv32.as<float>(), ctx->stream,
                                    &ctx->launches));
@@ -762,8 +781,8 @@ static int solve_pcg_refined(hdg_problem *pb, double rtol, int maxit, int *it_ou
   oa.n = (int)n;
   oa.nfd = (int)nfd;
   oa.nblockrows = (int)nbr;
-  oa.rowptr = ia.rowptr;
-  oa.colind = ia.colind;
+  oa.rowptr = pb->d_rowptr.as<int64_t>();
+  oa.colind = pb->d_colind.as<int>();
   oa.val = pb->d_val.as<double>();
   oa.rhs = pb->d_rhs.as<double>();
   oa.x = pb->d_x.as<double>();
@@ -821,6 +840,13 @@ static int solve_pcg_refined(hdg_problem *pb, double rtol, int maxit, int *it_ou
       status = ctx->fail(HDG_ERR_NOT_CONVERGED, "refined PCG breakdown (non-finite residual)");
       break;
     }
+  }
+  {
+    unsigned int herr = 0;
+    CUDA_TRY(ctx, cudaMemcpyAsync(&herr, pb->d_counter.as<unsigned int>() + 1, sizeof(herr), cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    if (herr) status = ctx->fail(HDG_ERR_CUDA, "a bulk copy of cell blocks did not complete");
   }
   pb->last_outer = outer;
   *it_out = total;
@@ -1055,7 +1081,8 @@ int hdg_time_kernel(hdg_problem *pb, int which, int reps, double *ms_per_launch)
   Pcg32Args pa32{};
   DBuf zero_scal;
   const bool mixed_spmv = which == 3 && pb->precision != HDG_PREC_FP64;
-  if (mixed_spmv && !pb->d_v32.ptr) return ctx->fail(HDG_ERR_STATE, "SpMV timing needs a refined PCG solve first");
+  if (mixed_spmv && (!pb->d_v32.ptr || !pb->d_qc.ptr || !pb->cellop_ctas))
+    return ctx->fail(HDG_ERR_STATE, "SpMV timing needs a refined PCG solve first");
   if (which == 3) {
     pa = pcg_args(pb);
     pa32 = pcg32_args(pb);
@@ -1075,7 +1102,7 @@ int hdg_time_kernel(hdg_problem *pb, int which, int reps, double *ms_per_launch)
                                pb->d_val.as<double>(), pb->d_rhs.as<double>(), ctx->stream, ctx->num_sms,
                                &ctx->launches);
       case 3:
-        // the SpMV the solve iterates: FP32 inner SpMV on the refined path
+        // the SpMV the solve iterates: the FP32 cell-operator SpMV on the fast paths
         return mixed_spmv ? launch_pcg32_spmv(pa32, ctx->stream, &ctx->launches)
                           : launch_spmv(pa, ctx->stream, &ctx->launches);
       default:

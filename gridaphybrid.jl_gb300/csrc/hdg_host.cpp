@@ -512,6 +512,16 @@ int build_pattern(const HostMesh &m, HostPattern &p, std::string &err) {
       has = m.facet_first_dof[m.cell_facets[(size_t)c * nl + lf]] < 0;
     if (has) p.dir_cells.push_back(c);
   }
+  // per (cell, local facet): the facet's block row (free facets are numbered
+  // in block-row order, first DOF = block row * nfd) and whether the cell owns it
+  p.cell_blk.assign((size_t)m.ncells * nl, -1);
+  for (int c = 0; c < m.ncells; ++c)
+    for (int lf = 0; lf < nl; ++lf) {
+      const int f = m.cell_facets[(size_t)c * nl + lf];
+      const int first = m.facet_first_dof[f];
+      if (first < 0) continue;
+      p.cell_blk[(size_t)c * nl + lf] = 2 * (first / nfd) + (m.facet_cell[2 * (size_t)f] == c ? 1 : 0);
+    }
   return HDG_OK;
 }
 

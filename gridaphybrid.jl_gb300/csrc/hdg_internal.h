@@ -118,6 +118,7 @@ struct HostPattern {
   std::vector<int> blk_src;          // block -> 2 x (cell*(2D)^2 + lf_row*2D + lf_col) or -1
   std::vector<int> diag_blk;         // block row -> index of its diagonal block
   std::vector<int> dir_cells;        // cells touching a Dirichlet DOF
+  std::vector<int> cell_blk;         // cell x lf -> 2*block row + owns, -1 (Dirichlet)
   int max_rowlen = 0;                // longest skeleton row
 };
 int build_pattern(const HostMesh &m, HostPattern &p, std::string &err);
@@ -172,12 +173,14 @@ struct hdg_problem {
   hdg::DBuf d_br_row0, d_br_src, d_blk_off, d_blk_rowlen, d_blk_src, d_diag_blk,
       d_dir_cells;
   hdg::DBuf d_Binv, d_x, d_r, d_z, d_p, d_p2, d_q, d_partials, d_scal, d_counter;
-  // mixed-precision skeleton solve: FP32 matrix copy, FP32 block inverses,
-  // inner vectors (x, r, z, p, p2, q), outer scalars
-  hdg::DBuf d_val32, d_Binv32, d_v32, d_scal2;
+  // mixed-precision skeleton solve: the FP32 operator as symmetric cell
+  // blocks, its cell map and per-cell products, FP32 block inverses, inner
+  // vectors (x, r, z, p, p2), outer scalars
+  hdg::DBuf d_cellop, d_cell_blk, d_qc, d_Binv32, d_v32, d_scal2;
   // block-elimination path: M_ref^{-1} as (hi, lo) floats, 1/m per cell
   hdg::DBuf d_minv, d_invm;
   cudaGraphExec_t pcg32_graph = nullptr;
+  int cellop_nstage = 0, cellop_ctas = 0;  // streaming-kernel pipeline depth and grid
   int last_outer = 0;
   hdg::DBuf d_uint;
   hdg::DBuf h_pinned;  // host staging

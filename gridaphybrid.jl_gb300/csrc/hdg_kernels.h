@@ -125,7 +125,6 @@ struct AssembleArgs {
   int ndir_cells;
   const int *cell_facets, *facet_dofs;
   const double *dirvals;
-  float *val32;  // when non-null, also receives the values rounded to FP32
 };
 cudaError_t launch_assemble(const AssembleArgs &a, const double *S,
                             const double *g, double *glift, double *val,
@@ -158,20 +157,36 @@ cudaError_t launch_spmv(const PcgArgs &a, cudaStream_t s, long long *launches);
 bool pcg_supports_nfd(int nfd);
 
 // Inner FP32 PCG of the mixed-precision skeleton solve (solves M e = rhs,
-// M = sign*A, with FP32 values and vectors; dot products in FP64).
+// M = sign*A, with FP32 values and vectors; dot products in FP64).  M is
+// applied unassembled: per cell the upper triangle of facet blocks of
+// sign*(S_c + S_c^T)/2 in FP32, streamed with bulk async copies; the two
+// cells of a facet are summed in the update kernel.
 struct Pcg32Args {
   int n, nfd, nblockrows;
-  const int64_t *rowptr;
-  const int *colind;
-  const float *val32;
   const float *Binv32;
   const double *rhs;  // inner right-hand side, already in the M frame
-  float *x, *r, *z, *p, *p2, *q;
+  float *x, *r, *z, *p, *p2;
   double *partials, *scal;
   unsigned int *counter;
-  int nparts;
-  double sign;
+  int nparts;             // grid of the vector kernels
+  int ncells, nl, rec;    // rec: floats per cell record
+  const float *blocks;    // ncells x rec
+  const int *cell_blk;    // ncells x nl: 2*block row + (cell owns the facet), -1 on Dirichlet facets
+  const int *br_src;      // nblockrows x 2: cell*nl + local facet, second -1 on the boundary
+  float *qc;              // ncells x nl*nfd per-cell products
+  int nstage, ctas;       // pipeline depth and grid of the streaming kernel
+  unsigned int *error;    // set to 1 when a bulk copy never completed
 };
+// Cell-operator layout: threads per cell, cells per CTA stage, floats per record.
+HDG_HD constexpr int cellop_tpc(int nf) { return nf <= 8 ? 8 : nf <= 16 ? 16 : ((nf + 31) / 32) * 32; }
+HDG_HD constexpr int cellop_cps(int nf) { return cellop_tpc(nf) >= 256 ? 1 : 256 / cellop_tpc(nf); }
+HDG_HD constexpr int cellop_rec(int nl, int nfd) { return (nl * (nl + 1) / 2 * nfd * nfd + 3) / 4 * 4; }
+bool cellop_supported(int nl, int nfd);
+// pipeline depth and grid for the streaming kernel (sets its shared-memory limit)
+cudaError_t cellop_configure(int nl, int nfd, size_t smem_optin, int num_sms, int *nstage, int *ctas);
+// packs sign*(S_c + S_c^T)/2 (column-major FP64 cell blocks) into cell records
+cudaError_t launch_pack_cell_blocks(int ncells, int nl, int nfd, double sign, const double *S, float *out,
+                                    size_t smem_optin, cudaStream_t s, int num_sms, long long *launches);
 // Outer FP64 refinement: x, r = sign*rhs - M x with the FP64 matrix.
 struct OuterArgs {
   int n, nfd, nblockrows;
@@ -189,6 +204,7 @@ cudaError_t launch_binv_to_f32(size_t count, const double *Binv, float *Binv32, 
                                long long *launches);
 cudaError_t launch_pcg32_init(const Pcg32Args &a, double eta, cudaStream_t s, long long *launches);
 cudaError_t launch_pcg32_iteration_pair(const Pcg32Args &a, cudaStream_t s, long long *launches);
+// one unassembled SpMV (+ its dot product) as launched inside the inner PCG
 cudaError_t launch_pcg32_spmv(const Pcg32Args &a, cudaStream_t s, long long *launches);
 cudaError_t launch_outer_init(const OuterArgs &a, cudaStream_t s, long long *launches);
 // x += e, then r = c - M x and |r|^2

@@ -4,14 +4,17 @@
 //   outer (FP64):  x = 0, r = c  (c = sign*rhs, the SPD frame M = sign*A)
 //                  repeat: solve M e ~= r with the inner PCG; x += e;
 //                          r = c - M x with the FP64 matrix; until |r| <= rtol |c|
-//   inner (FP32):  facet-block-Jacobi PCG on the FP32 copy of the matrix with
-//                  FP32 vectors; its dot products accumulate in FP64.
+//   inner (FP32):  facet-block-Jacobi PCG with FP32 vectors on the FP32
+//                  operator held as unassembled symmetric cell blocks; its dot
+//                  products accumulate in FP64.
 // GB300 executes FP64 at 1/62 of its FP32 rate, which makes even an FP64
 // SpMV arithmetic-bound; the inner iterations stay on the FP32 pipes and
-// stream half the bytes, the FP64 residual runs once per outer step.
+// stream about a quarter of the FP64 CSR bytes (FP32, upper blocks only),
+// the FP64 CSR residual runs once per outer step.
 #include <cuda_runtime.h>
 
 #include "hdg_kernels.h"
+#include "k_bulk.cuh"
 #include "k_pcg_common.cuh"
 
 namespace hdg {
@@ -82,56 +85,146 @@ __global__ void __launch_bounds__(kPcgThreads) pcg32_init_kernel(Pcg32Args a, do
   }
 }
 
-// p_new = z + beta p_old ; q = M32 p_new ; alpha = (r,z)/(p_new,q)
-template <int NFD>
-__global__ void __launch_bounds__(kPcgThreads) pcg32_spmv_kernel(Pcg32Args a, const float *__restrict__ p_old,
-                                                                 float *__restrict__ p_new) {
+// ---------------------------------------------------------------------------
+// The unassembled FP32 operator.
+//
+// Cell record: the upper triangle of facet blocks (a <= b, row-major order of
+// (a, b)) of sign*(S_c + S_c^T)/2, each block nfd x nfd row-major, padded to a
+// multiple of four floats (16 bytes) so records can be bulk-copied.  The
+// symmetric storage streams 21/36 of the full 3D cell matrix; the lower
+// blocks are read transposed from shared memory.
+// ---------------------------------------------------------------------------
+__global__ void pack_cell_blocks_kernel(int ncells, int nl, int nfd, int rec, double sign,
+                                        const double *__restrict__ S, float *__restrict__ out) {
+  extern __shared__ double Ss[];
+  const int nf = nl * nfd, nb = nfd * nfd, nblk = nl * (nl + 1) / 2;
+  for (int c = blockIdx.x; c < ncells; c += gridDim.x) {
+    const double *Sc = S + (size_t)c * nf * nf;
+    for (int e = threadIdx.x; e < nf * nf; e += blockDim.x) Ss[e] = Sc[e];
+    __syncthreads();
+    float *o = out + (size_t)c * rec;
+    for (int e = threadIdx.x; e < rec; e += blockDim.x) {
+      float v = 0.0f;
+      if (e < nblk * nb) {
+        const int blk = e / nb, w = e - blk * nb, r = w / nfd, s = w - r * nfd;
+        int lo = 0, rem = blk;
+        while (rem >= nl - lo) {
+          rem -= nl - lo;
+          ++lo;
+        }
+        const int i = lo * nfd + r, j = (lo + rem) * nfd + s;
+        v = (float)(0.5 * sign * (Ss[i + (size_t)nf * j] + Ss[j + (size_t)nf * i]));
+      }
+      o[e] = v;
+    }
+    __syncthreads();
+  }
+}
+
+constexpr int kMaxBulkStages = 8;
+
+template <int NL, int NFD>
+struct CellOp {
+  static constexpr int NF = NL * NFD;
+  static constexpr int TPC = cellop_tpc(NF);
+  static constexpr int CPS = cellop_cps(NF);
+  static constexpr int THREADS = CPS * TPC;
+  static constexpr int REC = cellop_rec(NL, NFD);
+};
+
+// p_new = z + beta p_old (formed while gathering, stored by the owning cell);
+// qc_c = M_c p_c for every cell; alpha = (r,z) / sum_c (p_c, qc_c).
+// Persistent CTAs take stages of CPS consecutive cells round-robin; thread 0
+// keeps `nstage` stages of cell records in flight with bulk copies (L2
+// evict-first: the records are read once per iteration, the vectors stay).
+template <int NL, int NFD>
+__global__ void __launch_bounds__(CellOp<NL, NFD>::THREADS)
+    cell_spmv32_kernel(Pcg32Args a, const float *__restrict__ p_old, float *__restrict__ p_new) {
+  using C = CellOp<NL, NFD>;
+  extern __shared__ __align__(128) float ring[];
+  __shared__ __align__(8) uint64_t bars[kMaxBulkStages];
+  __shared__ float ps[C::CPS][C::TPC];
   __shared__ double red[32];
-  __shared__ float xs[kPcgThreads / 32][kMaxRowLen];
+  __shared__ int abort_flag;
   if (a.scal[SC_DONE] != 0.0) return;
   const float beta = (float)a.scal[SC_BETA];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nw = (gridDim.x * blockDim.x) >> 5;
-  double acc = 0.0;
-  for (int br = wid; br < a.nblockrows; br += nw) {
-    const int row0 = br * NFD;
-    const int64_t base = a.rowptr[row0];
-    const int rowlen = (int)(a.rowptr[row0 + 1] - base);
-    for (int j = lane; j < rowlen; j += 32) {
-      const int col = a.colind[base + j];
-      xs[w][j] = fmaf(beta, p_old[col], a.z[col]);
-    }
-    float pown = 0.0f;
-    if (lane < NFD) {
-      pown = fmaf(beta, p_old[row0 + lane], a.z[row0 + lane]);
-      p_new[row0 + lane] = pown;
-    }
-    __syncwarp();
-    constexpr int P = Pow2Ceil<NFD>::v;
-    float v[P];
-#pragma unroll
-    for (int r = 0; r < P; ++r) v[r] = 0.0f;
-    for (int j = lane; j < rowlen; j += 32) {
-      const float xv = xs[w][j];
-      const float *vj = a.val32 + base + j;
-#pragma unroll
-      for (int r = 0; r < NFD; ++r) v[r] = fmaf(__ldcs(vj + (int64_t)r * rowlen), xv, v[r]);
-    }
-    const float tot = warp_reduce_scatter<float, P>(v, lane);
-    const int myrow = reduce_scatter_row<P>(lane);
-    const float pmine = __shfl_sync(0xffffffffu, pown, myrow < NFD ? myrow : 0);
-    if (myrow < NFD && reduce_scatter_writer<P>(lane)) {
-      const float q = (float)a.sign * tot;
-      a.q[row0 + myrow] = q;
-      acc += (double)q * pmine;
-    }
-    __syncwarp();
+  const int g = threadIdx.x / C::TPC, i = threadIdx.x - g * C::TPC;
+  const int lf = i / NFD, r = i - lf * NFD;
+  const int nunits = (a.ncells + C::CPS - 1) / C::CPS;
+  const int mine = (int)blockIdx.x < nunits ? (nunits - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+  const int nstage = a.nstage;
+  uint64_t pol = 0;
+  int issued = 0;  // meaningful in thread 0
+  auto issue = [&](int t) {
+    const int c0 = ((int)blockIdx.x + t * (int)gridDim.x) * C::CPS;
+    const int nc = min(C::CPS, a.ncells - c0);
+    const uint32_t bytes = (uint32_t)nc * C::REC * 4u;
+    const int slot = t % nstage;
+    mbar_arrive_expect_tx(&bars[slot], bytes);
+    bulk_copy_g2s(ring + (size_t)slot * C::CPS * C::REC, a.blocks + (size_t)c0 * C::REC, bytes, &bars[slot], pol);
+  };
+  if (threadIdx.x == 0) {
+    abort_flag = 0;
+    for (int s = 0; s < nstage; ++s) mbar_init(&bars[s], 1);
+    mbar_init_fence();
+    pol = l2_evict_first_policy();
+    for (; issued < min(nstage, mine); ++issued) issue(issued);
   }
-  const double t = block_sum(acc, red);
-  if (threadIdx.x == 0) a.partials[blockIdx.x] = t;
+  __syncthreads();
+  double acc = 0.0;
+  for (int t = 0; t < mine; ++t) {
+    const int slot = t % nstage;
+    const int c = ((int)blockIdx.x + t * (int)gridDim.x) * C::CPS + g;
+    const bool act = i < C::NF && c < a.ncells;
+    float pv = 0.0f;
+    if (act) {
+      const int ent = a.cell_blk[(size_t)c * NL + lf];
+      if (ent >= 0) {
+        const int row = (ent >> 1) * NFD + r;
+        pv = fmaf(beta, p_old[row], a.z[row]);
+        if (ent & 1) p_new[row] = pv;
+      }
+    }
+    ps[g][i] = pv;
+    if (!mbar_wait_bounded(&bars[slot], (uint32_t)(t / nstage) & 1u)) abort_flag = 1;
+    __syncthreads();
+    if (abort_flag) {
+      // a copy never landed: record it, give the copies in flight a bounded
+      // chance to finish (they target this CTA's shared memory) and stop
+      if (threadIdx.x == 0) {
+        atomicExch(a.error, 1u);
+        for (int u = t; u < issued; ++u) mbar_wait_bounded(&bars[u % nstage], (uint32_t)(u / nstage) & 1u);
+      }
+      return;
+    }
+    if (act) {
+      const float *B = ring + (size_t)slot * C::CPS * C::REC + (size_t)g * C::REC;
+      float q = 0.0f;
+#pragma unroll
+      for (int b = 0; b < NL; ++b) {
+        // block (lf, b) is stored for b >= lf; below the diagonal read (b, lf) transposed
+        const bool up = b >= lf;
+        const int lo = up ? lf : b, hi = up ? b : lf;
+        const int blk = lo * NL - (lo * (lo - 1)) / 2 + (hi - lo);
+        const float *Bb = B + blk * NFD * NFD + (up ? r * NFD : r);
+        const int st = up ? 1 : NFD;
+#pragma unroll
+        for (int s = 0; s < NFD; ++s) q = fmaf(Bb[s * st], ps[g][b * NFD + s], q);
+      }
+      a.qc[(size_t)c * C::NF + i] = q;
+      acc += (double)pv * q;
+    }
+    __syncthreads();  // the slot and ps are free again
+    if (threadIdx.x == 0 && issued < mine) {
+      async_proxy_fence();
+      issue(issued);
+      ++issued;
+    }
+  }
+  const double tsum = block_sum(acc, red);
+  if (threadIdx.x == 0) a.partials[blockIdx.x] = tsum;
   if (last_cta(a.counter)) {
-    const double pq = sum_partials(a.partials, a.nparts, 0, red);
+    const double pq = sum_partials(a.partials, (int)gridDim.x, 0, red);
     if (threadIdx.x == 0) {
       a.scal[SC_PAP] = pq;
       a.scal[SC_ALPHA] = a.scal[SC_RZ] / pq;
@@ -140,29 +233,47 @@ __global__ void __launch_bounds__(kPcgThreads) pcg32_spmv_kernel(Pcg32Args a, co
   }
 }
 
-// x += alpha p; r -= alpha q; z = Binv r; beta; convergence against eta |rhs|
-__global__ void __launch_bounds__(kPcgThreads) pcg32_update_kernel(Pcg32Args a, const float *__restrict__ p) {
+// q = qc(owner) + qc(other) per free row; x += alpha p; r -= alpha q;
+// z = Binv r with the tile's block inverses staged in shared memory; beta;
+// convergence against eta |rhs|
+template <int NFD>
+__global__ void __launch_bounds__(kPcgThreads) pcg32_update_cells_kernel(Pcg32Args a, const float *__restrict__ p) {
+  constexpr int BPT = kPcgThreads / NFD;  // block rows per tile
   __shared__ float rs[kPcgThreads];
+  __shared__ float Bs[BPT * NFD * NFD];
   __shared__ double red[32];
   if (a.scal[SC_DONE] != 0.0) return;
   const float alpha = (float)a.scal[SC_ALPHA];
-  const int tile = (kPcgThreads / a.nfd) * a.nfd;
+  const int lb = threadIdx.x / NFD, i = threadIdx.x - lb * NFD;
   double rz = 0.0, rr = 0.0;
-  for (int base = blockIdx.x * tile; base < a.n; base += gridDim.x * tile) {
-    const int row = base + (int)threadIdx.x;
-    const bool act = threadIdx.x < (unsigned)tile && row < a.n;
-    float r = 0.0f;
+  for (int br0 = blockIdx.x * BPT; br0 < a.nblockrows; br0 += gridDim.x * BPT) {
+    const int nb = min(BPT, a.nblockrows - br0);
+    const float *Bg = a.Binv32 + (size_t)br0 * NFD * NFD;
+    for (int e = threadIdx.x; e < nb * NFD * NFD; e += blockDim.x) Bs[e] = Bg[e];
+    const bool act = lb < nb;
+    const int br = br0 + lb, row = br * NFD + i;
+    float rv = 0.0f;
     if (act) {
+      const int s0 = a.br_src[2 * br], s1 = a.br_src[2 * br + 1];
+      float q = a.qc[(size_t)s0 * NFD + i];
+      if (s1 >= 0) q += a.qc[(size_t)s1 * NFD + i];
       a.x[row] = fmaf(alpha, p[row], a.x[row]);
-      r = fmaf(-alpha, a.q[row], a.r[row]);
-      a.r[row] = r;
-      rr += (double)r * r;
+      rv = fmaf(-alpha, q, a.r[row]);
+      a.r[row] = rv;
+      rr += (double)rv * rv;
     }
-    const float z = apply_binv32(a, act ? row : a.n, r, rs);
+    rs[threadIdx.x] = rv;
+    __syncthreads();
     if (act) {
+      const float *B = Bs + lb * NFD * NFD + i * NFD;
+      const float *rl = rs + lb * NFD;
+      float z = 0.0f;
+#pragma unroll
+      for (int j = 0; j < NFD; ++j) z = fmaf(B[j], rl[j], z);
       a.z[row] = z;
-      rz += (double)r * z;
+      rz += (double)rv * z;
     }
+    __syncthreads();
   }
   double s = block_sum(rz, red);
   if (threadIdx.x == 0) a.partials[blockIdx.x] = s;
@@ -277,42 +388,103 @@ cudaError_t launch_pcg32_init(const Pcg32Args &a, double eta, cudaStream_t s, lo
   return cudaGetLastError();
 }
 
-template <int NFD>
+template <int NL, int NFD>
+static size_t cellop_dyn_smem(int nstage) {
+  using C = CellOp<NL, NFD>;
+  return (size_t)nstage * C::CPS * C::REC * sizeof(float);
+}
+
+#define HDG_CELLOP_CASES(X) \
+  X(4, 2) X(4, 3) X(4, 4) X(4, 5) X(6, 4) X(6, 9) X(6, 16) X(6, 25)
+
+bool cellop_supported(int nl, int nfd) {
+#define X(L, F) \
+  if (nl == L && nfd == F) return true;
+  HDG_CELLOP_CASES(X)
+#undef X
+  return false;
+}
+
+template <int NL, int NFD>
+static cudaError_t cellop_configure_t(size_t smem_optin, int num_sms, int *nstage, int *ctas) {
+  using C = CellOp<NL, NFD>;
+  const size_t stage = (size_t)C::CPS * C::REC * sizeof(float);
+  // about 108 KB of records in flight per CTA, two CTAs per SM where they fit
+  int ns = (int)((110 * 1024) / stage);
+  ns = ns > kMaxBulkStages ? kMaxBulkStages : ns;
+  if (ns < 2) ns = 2;
+  while (ns > 2 && (size_t)ns * stage + 4096 > smem_optin) --ns;
+  if ((size_t)ns * stage + 4096 > smem_optin) return cudaErrorInvalidValue;
+  const size_t dyn = cellop_dyn_smem<NL, NFD>(ns);
+  cudaError_t e = cudaFuncSetAttribute(cell_spmv32_kernel<NL, NFD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cell_spmv32_kernel<NL, NFD>, C::THREADS, dyn);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) return cudaErrorInvalidValue;
+  if (per_sm > 4) per_sm = 4;
+  *nstage = ns;
+  *ctas = per_sm * num_sms;
+  return cudaSuccess;
+}
+
+cudaError_t cellop_configure(int nl, int nfd, size_t smem_optin, int num_sms, int *nstage, int *ctas) {
+#define X(L, F) \
+  if (nl == L && nfd == F) return cellop_configure_t<L, F>(smem_optin, num_sms, nstage, ctas);
+  HDG_CELLOP_CASES(X)
+#undef X
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_pack_cell_blocks(int ncells, int nl, int nfd, double sign, const double *S, float *out,
+                                    size_t smem_optin, cudaStream_t s, int num_sms, long long *launches) {
+  const int nf = nl * nfd;
+  const size_t smem = sizeof(double) * nf * nf;
+  if (smem > smem_optin) return cudaErrorInvalidValue;
+  cudaError_t e = cudaFuncSetAttribute(pack_cell_blocks_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int grid = ncells < num_sms * 16 ? ncells : num_sms * 16;
+  if (grid < 1) grid = 1;
+  pack_cell_blocks_kernel<<<grid, 256, smem, s>>>(ncells, nl, nfd, cellop_rec(nl, nfd), sign, S, out);
+  ++*launches;
+  return cudaGetLastError();
+}
+
+template <int NL, int NFD>
+static void cell_spmv(const Pcg32Args &a, const float *po, float *pn, cudaStream_t s) {
+  cell_spmv32_kernel<NL, NFD><<<a.ctas, CellOp<NL, NFD>::THREADS, cellop_dyn_smem<NL, NFD>(a.nstage), s>>>(a, po, pn);
+}
+
+template <int NL, int NFD>
 static void pcg32_pair(const Pcg32Args &a, cudaStream_t s) {
-  pcg32_spmv_kernel<NFD><<<a.nparts, kPcgThreads, 0, s>>>(a, a.p, a.p2);
-  pcg32_update_kernel<<<a.nparts, kPcgThreads, 0, s>>>(a, a.p2);
-  pcg32_spmv_kernel<NFD><<<a.nparts, kPcgThreads, 0, s>>>(a, a.p2, a.p);
-  pcg32_update_kernel<<<a.nparts, kPcgThreads, 0, s>>>(a, a.p);
+  cell_spmv<NL, NFD>(a, a.p, a.p2, s);
+  pcg32_update_cells_kernel<NFD><<<a.nparts, kPcgThreads, 0, s>>>(a, a.p2);
+  cell_spmv<NL, NFD>(a, a.p2, a.p, s);
+  pcg32_update_cells_kernel<NFD><<<a.nparts, kPcgThreads, 0, s>>>(a, a.p);
 }
 
 cudaError_t launch_pcg32_iteration_pair(const Pcg32Args &a, cudaStream_t s, long long *launches) {
-  switch (a.nfd) {
-    case 2: pcg32_pair<2>(a, s); break;
-    case 3: pcg32_pair<3>(a, s); break;
-    case 4: pcg32_pair<4>(a, s); break;
-    case 5: pcg32_pair<5>(a, s); break;
-    case 9: pcg32_pair<9>(a, s); break;
-    case 16: pcg32_pair<16>(a, s); break;
-    case 25: pcg32_pair<25>(a, s); break;
-    default: return cudaErrorInvalidValue;
+#define X(L, F)                    \
+  if (a.nl == L && a.nfd == F) {   \
+    pcg32_pair<L, F>(a, s);        \
+    *launches += 4;                \
+    return cudaGetLastError();     \
   }
-  *launches += 4;
-  return cudaGetLastError();
+  HDG_CELLOP_CASES(X)
+#undef X
+  return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_pcg32_spmv(const Pcg32Args &a, cudaStream_t s, long long *launches) {
-  switch (a.nfd) {
-    case 2: pcg32_spmv_kernel<2><<<a.nparts, kPcgThreads, 0, s>>>(a, a.p, a.p2); break;
-    case 3: pcg32_spmv_kernel<3><<<a.nparts, kPcgThreads, 0, s>>>(a, a.p, a.p2); break;
-    case 4: pcg32_spmv_kernel<4><<<a.nparts, kPcgThreads, 0, s>>>(a, a.p, a.p2); break;
-    case 5: pcg32_spmv_kernel<5><<<a.nparts, kPcgThreads, 0, s>>>(a, a.p, a.p2); break;
-    case 9: pcg32_spmv_kernel<9><<<a.nparts, kPcgThreads, 0, s>>>(a, a.p, a.p2); break;
-    case 16: pcg32_spmv_kernel<16><<<a.nparts, kPcgThreads, 0, s>>>(a, a.p, a.p2); break;
-    case 25: pcg32_spmv_kernel<25><<<a.nparts, kPcgThreads, 0, s>>>(a, a.p, a.p2); break;
-    default: return cudaErrorInvalidValue;
+#define X(L, F)                    \
+  if (a.nl == L && a.nfd == F) {   \
+    cell_spmv<L, F>(a, a.p, a.p2, s); \
+    ++*launches;                   \
+    return cudaGetLastError();     \
   }
-  ++*launches;
-  return cudaGetLastError();
+  HDG_CELLOP_CASES(X)
+#undef X
+  return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_outer_init(const OuterArgs &a, cudaStream_t s, long long *launches) {

@@ -64,7 +64,6 @@ __global__ void assemble_blocks_kernel(AssembleArgs a, const double *__restrict_
       double v = S0[(r0 + ra) + (size_t)nf * (c0 + cb)];
       if (S1) v += S1[(r1 + ra) + (size_t)nf * (c1 + cb)];
       val[off + (int64_t)ra * rowlen + cb] = v;
-      if (a.val32) a.val32[off + (int64_t)ra * rowlen + cb] = (float)v;
     }
   }
 }

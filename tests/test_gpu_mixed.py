@@ -129,3 +129,18 @@ def test_ffblock_rejected_at_map_level(ctx):
     b = np.zeros((1, 20))
     rc, S, g, info = _condense(ctx, A, b, 12, _lib.HDG_PREC_FF_BLOCK)
     assert rc == _lib.HDG_ERR_INVALID
+
+
+@pytest.mark.parametrize("precision", FAST_PRECISIONS)
+def test_fast_solve_is_deterministic(ctx, precision):
+    """Two solves of the same problem give bitwise-identical skeleton values
+    and iteration counts (fixed-order reductions, no atomics on values)."""
+    kappa = np.exp(np.random.default_rng(21).normal(size=5 * 5 * 4))
+    runs = []
+    for _ in range(2):
+        op = _op(3, 2, (5, 5, 4), kappa, precision)
+        xh = gh.solve(op, solver="pcg", rtol=1e-12, maxit=5000)
+        runs.append((xh.skeleton.copy(), xh.cell_interior.copy(), xh.iterations))
+    assert np.array_equal(runs[0][0], runs[1][0])
+    assert np.array_equal(runs[0][1], runs[1][1])
+    assert runs[0][2] == runs[1][2]
