@@ -84,8 +84,9 @@ struct Cfg {
   static constexpr int D = D_, NK = NK_, NFD = NFD_;
   static constexpr int NU = D * NK, NI = (D + 1) * NK, NF = 2 * D * NFD, N = NI + NF, NC = NF + 1;
   static constexpr int NT = 256;
-  // shared memory (floats): Y (D NK NK), P (NK NK), Z (D NK NC), Q (NK NC), each hi + lo
-  static constexpr size_t smem_floats = 2 * ((size_t)D * NK * NK + NK * NK + (size_t)D * NK * NC + NK * NC);
+  // shared memory (floats): Y (D NK NK), P (NK NK), Z (D NK NC), Q (NK NC), M^{-1} (NK NK), each hi + lo
+  static constexpr size_t smem_floats =
+      2 * ((size_t)D * NK * NK + NK * NK + (size_t)D * NK * NC + NK * NC + (size_t)NK * NK);
   static constexpr size_t smem_bytes = smem_floats * 4 + 64 * 4;
 };
 
@@ -106,8 +107,16 @@ __global__ void __launch_bounds__(C::NT, 2)
   float *Ph = Yl + D * NK * NK, *Pl = Ph + NK * NK;  // [a][b]
   float *Zh = Pl + NK * NK, *Zl = Zh + D * NK * NC;  // [d][a][c]
   float *Qh = Zl + D * NK * NC, *Ql = Qh + NK * NC;  // [a][c]
-  int *sflag = reinterpret_cast<int *>(Ql + NK * NC);  // [0] pivot row, [1] info
+  float *Mh = Ql + NK * NC, *Ml = Mh + NK * NK;       // [a][k]
+  int *sflag = reinterpret_cast<int *>(Ml + NK * NK);  // [0] pivot row, [1] info
   const int t = threadIdx.x;
+  for (int e = t; e < NK * NK; e += NT) {
+    Mh[e] = Minv_h[e];
+    Ml[e] = Minv_l[e];
+  }
+  // Threads run fastest over the row index of each output, so the
+  // column-major A entries they read are broadcast (one column entry per
+  // warp) or contiguous (consecutive rows of one column).
   for (int cell = blockIdx.x; cell < ncells; cell += gridDim.x) {
     const float *Ah = Ahi + (size_t)cell * N * N, *Al = Alo + (size_t)cell * N * N;
     const float *bh = bhi + (size_t)cell * N, *bl = blo + (size_t)cell * N;
@@ -118,20 +127,20 @@ __global__ void __launch_bounds__(C::NT, 2)
       iml = (float)(v - (double)imh);
     }
     // Y_d = (1/m) M^{-1} G_d  and  Z_d = (1/m) M^{-1} R_{u_d}
+    __syncthreads();  // M^{-1} staged (first cell) / previous cell done
     for (int o = t; o < D * NK * (NK + NC); o += NT) {
-      const int d = o / (NK * (NK + NC)), rem = o - d * NK * (NK + NC);
-      const int a = rem / (NK + NC), c = rem - a * (NK + NC);
+      const int a = o % NK, rest = o / NK;
+      const int c = rest % (NK + NC), d = rest / (NK + NC);
       float h = 0.0f, l = 0.0f;
       if (c < NK) {  // G_d column c (pressure DOF c)
         for (int k = 0; k < NK; ++k)
-          mac(h, l, __ldg(Minv_h + a * NK + k), __ldg(Minv_l + a * NK + k), AH(d * NK + k, NU + c),
-              AL(d * NK + k, NU + c));
+          mac(h, l, Mh[a * NK + k], Ml[a * NK + k], AH(d * NK + k, NU + c), AL(d * NK + k, NU + c));
       } else {
         const int cc = c - NK;  // right-hand-side column (skeleton DOF or b)
         for (int k = 0; k < NK; ++k) {
           const float rh = cc < NF ? AH(d * NK + k, NI + cc) : bh[d * NK + k];
           const float rl = cc < NF ? AL(d * NK + k, NI + cc) : bl[d * NK + k];
-          mac(h, l, __ldg(Minv_h + a * NK + k), __ldg(Minv_l + a * NK + k), rh, rl);
+          mac(h, l, Mh[a * NK + k], Ml[a * NK + k], rh, rl);
         }
       }
       float ph, pl;
@@ -148,7 +157,7 @@ __global__ void __launch_bounds__(C::NT, 2)
     __syncthreads();
     // P = T - sum_d G'_d Y_d ;  Q = R_p - sum_d G'_d Z_d
     for (int o = t; o < NK * (NK + NC); o += NT) {
-      const int a = o / (NK + NC), c = o - a * (NK + NC);
+      const int a = o % NK, c = o / NK;
       float h = 0.0f, l = 0.0f;
       if (c < NK) {
         for (int d = 0; d < D; ++d)
@@ -284,7 +293,7 @@ __global__ void __launch_bounds__(C::NT, 2)
     __syncthreads();
     // S = A_ff - A_fi X, g = b_f - A_fi y
     for (int o = t; o < NF * NC; o += NT) {
-      const int f = o / NC, c = o - f * NC;
+      const int f = o % NF, c = o / NF;
       float h = 0.0f, l = 0.0f;
       for (int k = 0; k < NU; ++k)
         mac(h, l, AH(NI + f, k), AL(NI + f, k), Zh[k * NC + c], Zl[k * NC + c]);
@@ -326,8 +335,9 @@ static cudaError_t launch_cfg(int ncells, const float *Ahi, const float *Alo, co
                                          (int)smem);
     if (e != cudaSuccess) return e;
   }
-  int per_sm = (int)((228 * 1024) / (smem + 1024));
-  if (per_sm > 2) per_sm = 2;
+  int per_sm = 0;
+  cudaError_t oe = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, condense_ffblock_kernel<C>, C::NT, smem);
+  if (oe != cudaSuccess) return oe;
   if (per_sm < 1) per_sm = 1;
   int grid = num_sms * per_sm;
   if (grid > ncells) grid = ncells;

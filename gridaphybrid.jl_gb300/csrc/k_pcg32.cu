@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(CellOp<NL, NFD>::THREADS)
   using C = CellOp<NL, NFD>;
   extern __shared__ __align__(128) float ring[];
   __shared__ __align__(8) uint64_t bars[kMaxBulkStages];
-  __shared__ float ps[C::CPS][C::TPC];
+  __shared__ __align__(16) float ps[C::CPS][C::TPC];
   __shared__ double red[32];
   __shared__ int abort_flag;
   if (a.scal[SC_DONE] != 0.0) return;
@@ -200,16 +200,41 @@ __global__ void __launch_bounds__(CellOp<NL, NFD>::THREADS)
     if (act) {
       const float *B = ring + (size_t)slot * C::CPS * C::REC + (size_t)g * C::REC;
       float q = 0.0f;
+      if constexpr (C::NF <= 64) {
+        // the cell's p in registers (vector loads), so the inner loop only reads B
+        constexpr int NV = (C::NF + 3) / 4;
+        float pr[4 * NV];
+        const float4 *p4 = reinterpret_cast<const float4 *>(&ps[g][0]);
 #pragma unroll
-      for (int b = 0; b < NL; ++b) {
-        // block (lf, b) is stored for b >= lf; below the diagonal read (b, lf) transposed
-        const bool up = b >= lf;
-        const int lo = up ? lf : b, hi = up ? b : lf;
-        const int blk = lo * NL - (lo * (lo - 1)) / 2 + (hi - lo);
-        const float *Bb = B + blk * NFD * NFD + (up ? r * NFD : r);
-        const int st = up ? 1 : NFD;
+        for (int v = 0; v < NV; ++v) {
+          const float4 t4 = p4[v];
+          pr[4 * v] = t4.x;
+          pr[4 * v + 1] = t4.y;
+          pr[4 * v + 2] = t4.z;
+          pr[4 * v + 3] = t4.w;
+        }
 #pragma unroll
-        for (int s = 0; s < NFD; ++s) q = fmaf(Bb[s * st], ps[g][b * NFD + s], q);
+        for (int b = 0; b < NL; ++b) {
+          // block (lf, b) is stored for b >= lf; below the diagonal read (b, lf) transposed
+          const bool up = b >= lf;
+          const int lo = up ? lf : b, hi = up ? b : lf;
+          const int blk = lo * NL - (lo * (lo - 1)) / 2 + (hi - lo);
+          const float *Bb = B + blk * NFD * NFD + (up ? r * NFD : r);
+          const int st = up ? 1 : NFD;
+#pragma unroll
+          for (int s = 0; s < NFD; ++s) q = fmaf(Bb[s * st], pr[b * NFD + s], q);
+        }
+      } else {
+#pragma unroll
+        for (int b = 0; b < NL; ++b) {
+          const bool up = b >= lf;
+          const int lo = up ? lf : b, hi = up ? b : lf;
+          const int blk = lo * NL - (lo * (lo - 1)) / 2 + (hi - lo);
+          const float *Bb = B + blk * NFD * NFD + (up ? r * NFD : r);
+          const int st = up ? 1 : NFD;
+#pragma unroll
+          for (int s = 0; s < NFD; ++s) q = fmaf(Bb[s * st], ps[g][b * NFD + s], q);
+        }
       }
       a.qc[(size_t)c * C::NF + i] = q;
       acc += (double)pv * q;

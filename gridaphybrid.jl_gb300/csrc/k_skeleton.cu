@@ -40,30 +40,49 @@ __global__ void dirichlet_lift_kernel(AssembleArgs a, const double *__restrict__
 
 // One warp per skeleton block (f,g): val = sum over the (one or two)
 // contributing cells of their condensed sub-block, cells in increasing order.
-__global__ void assemble_blocks_kernel(AssembleArgs a, const double *__restrict__ S,
-                                       double *__restrict__ val) {
+// Block shapes are compile-time so the index arithmetic is shifts and
+// multiplies and every lane issues all of its loads before its stores.
+template <int NL, int NFD>
+__global__ void __launch_bounds__(256) assemble_blocks_kernel(AssembleArgs a, const double *__restrict__ S,
+                                                              double *__restrict__ val) {
+  constexpr int NB = NFD * NFD, NF = NL * NFD, PER = (NB + 31) / 32;
   const int lane = threadIdx.x & 31;
   const int64_t wid = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  const int nf = a.nf, nfd = a.nfd, nl = a.nl, nb = nfd * nfd;
   for (int64_t blk = wid; blk < a.nblocks; blk += nw) {
     const int64_t off = a.blk_off[blk];
     const int rowlen = a.blk_rowlen[blk];
     const int s0 = a.blk_src[2 * blk], s1 = a.blk_src[2 * blk + 1];
-    const double *S0 = S + (size_t)(s0 / (nl * nl)) * nf * nf;
-    const int r0 = ((s0 / nl) % nl) * nfd, c0 = (s0 % nl) * nfd;
-    const double *S1 = nullptr;
-    int r1 = 0, c1 = 0;
-    if (s1 >= 0) {
-      S1 = S + (size_t)(s1 / (nl * nl)) * nf * nf;
-      r1 = ((s1 / nl) % nl) * nfd;
-      c1 = (s1 % nl) * nfd;
+    const double *S0 = S + (size_t)(s0 / (NL * NL)) * NF * NF + ((s0 / NL) % NL) * NFD + (size_t)NF * ((s0 % NL) * NFD);
+    const double *S1 =
+        s1 >= 0 ? S + (size_t)(s1 / (NL * NL)) * NF * NF + ((s1 / NL) % NL) * NFD + (size_t)NF * ((s1 % NL) * NFD)
+                : nullptr;
+    double v[PER];
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+      const int e = lane + 32 * k;
+      if (e < NB) {
+        const int ra = e / NFD, cb = e - ra * NFD;
+        v[k] = S0[ra + NF * cb];
+      }
     }
-    for (int e = lane; e < nb; e += 32) {
-      const int ra = e / nfd, cb = e - ra * nfd;
-      double v = S0[(r0 + ra) + (size_t)nf * (c0 + cb)];
-      if (S1) v += S1[(r1 + ra) + (size_t)nf * (c1 + cb)];
-      val[off + (int64_t)ra * rowlen + cb] = v;
+    if (S1) {
+#pragma unroll
+      for (int k = 0; k < PER; ++k) {
+        const int e = lane + 32 * k;
+        if (e < NB) {
+          const int ra = e / NFD, cb = e - ra * NFD;
+          v[k] += S1[ra + NF * cb];
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < PER; ++k) {
+      const int e = lane + 32 * k;
+      if (e < NB) {
+        const int ra = e / NFD, cb = e - ra * NFD;
+        val[off + (int64_t)ra * rowlen + cb] = v[k];
+      }
     }
   }
 }
@@ -102,7 +121,14 @@ cudaError_t launch_assemble(const AssembleArgs &a, const double *S, const double
     int64_t grid = (warps * 32 + 255) / 256;
     if (grid > (int64_t)num_sms * 16) grid = (int64_t)num_sms * 16;
     if (grid < 1) grid = 1;
-    assemble_blocks_kernel<<<(int)grid, 256, 0, s>>>(a, S, val);
+#define HDG_ASM(L, F) \
+  else if (a.nl == L && a.nfd == F) assemble_blocks_kernel<L, F><<<(int)grid, 256, 0, s>>>(a, S, val);
+    if (false) {
+    }
+    HDG_ASM(4, 2) HDG_ASM(4, 3) HDG_ASM(4, 4) HDG_ASM(4, 5) HDG_ASM(6, 1) HDG_ASM(6, 4) HDG_ASM(6, 9)
+    HDG_ASM(6, 16) HDG_ASM(6, 25) HDG_ASM(4, 1)
+    else return cudaErrorInvalidValue;
+#undef HDG_ASM
     ++*launches;
   }
   {
