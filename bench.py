@@ -174,6 +174,38 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def run_serving(args, prec, prec64):
+    """The serving workload: a seeded Poisson stream of 2D/3D Darcy solves of
+    different sizes, orders and permeability fields submitted at their arrival
+    times to the native request loop; p50/p99 latency and solves/s, for the
+    selected precision and (over the first part of the same stream) the plain
+    FP64 path."""
+    from gridaphybrid_gb300 import serving
+    trace = serving.poisson_trace(rate=args.serve_rate, seconds=args.serve_seconds, seed=0)
+    out = {
+        "workload": "Poisson %.0f req/s for %.0f s (seed 0): 2D with p=%.2f, n=round(exp(N(ln %g, %g^2))) in "
+                    "[%d,%d], k in %s; 3D n=round(exp(N(ln %g, %g^2))) in [%d,%d], k in %s; kappa=exp(N(0,1)) "
+                    "per cell; PCG to 1e-10" % (
+                        args.serve_rate, args.serve_seconds, serving.P_2D, serving.N2D_MU, serving.N2D_SIGMA,
+                        *serving.N2D_RANGE, list(serving.K2D), serving.N3D_MU, serving.N3D_SIGMA,
+                        *serving.N3D_RANGE, list(serving.K3D)),
+        "requests": len(trace), "slots": args.serve_slots,
+    }
+    runs = [(args.precision, prec, None)]
+    if args.precision != "fp64" and args.serve_fp64_seconds > 0:
+        runs.append(("fp64", prec64, args.serve_fp64_seconds))
+    for name, p, limit in runs:
+        with serving.Server(slots=args.serve_slots) as srv:
+            resp, wall = serving.run_trace(srv, trace, p, max_seconds=limit)
+            st = srv.stats()
+        summ = serving.latency_summary(resp, wall)
+        summ.update({"seconds_of_trace": limit or args.serve_seconds, "peak_hbm_gb": st["peak_bytes"] / 1e9,
+                     "max_concurrent": int(st["max_concurrent"]), "mesh_hits": int(st["mesh_hits"]),
+                     "evictions": int(st["evictions"])})
+        out[name] = summ
+    return out
+
+
 def run_gpu(args):
     import gridaphybrid_gb300 as gh
     from gridaphybrid_gb300 import _lib
@@ -280,6 +312,8 @@ def run_gpu(args):
                "d2h_bytes_per_step": (ncells * ni + nfree) * 8, "ms_per_step": e2e_s * 1000.0,
                "host_buffers": "pinned" if pinned else "pageable"}
 
+    serving_out = run_serving(args, prec, precs["fp64"]) if args.serve_seconds > 0 else None
+
     peaks, peak_kind = measured_peaks()
     hbm = float(peaks["hbm_gbs"])
     # SpMV of the PCG iterations.  FP64 path: CSR values + one column list per
@@ -323,6 +357,8 @@ def run_gpu(args):
     }
     if compare:
         line["fp64_compare"] = compare
+    if serving_out:
+        line["serving"] = serving_out
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline_sample()
     print(json.dumps(line))
@@ -342,6 +378,12 @@ def main():
     ap.add_argument("--no-fp64-compare", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--serve-seconds", type=float, default=60.0,
+                    help="length of the serving stream (0 skips serving)")
+    ap.add_argument("--serve-fp64-seconds", type=float, default=20.0,
+                    help="part of the stream replayed on the plain FP64 path")
+    ap.add_argument("--serve-rate", type=float, default=200.0)
+    ap.add_argument("--serve-slots", type=int, default=8)
     ap.add_argument("--n-side", type=int, default=32,
                     help="cells per side (32 is the benchmark workload; smaller sizes are for profiling)")
     args = ap.parse_args()

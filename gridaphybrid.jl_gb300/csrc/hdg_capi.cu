@@ -1020,13 +1020,13 @@ int hdg_l2_errors(hdg_problem *pb, double *err_flux, double *err_pres) {
   if (!pb->recovered) return ctx->fail(HDG_ERR_STATE, "recover first");
   cudaSetDevice(ctx->device);
   const size_t nc = pb->mesh.ncells;
-  DBuf errs;
-  CUDA_TRY(ctx, errs.reserve(sizeof(double) * 2 * nc));
+  CUDA_TRY(ctx, pb->d_errs.reserve(sizeof(double) * 2 * nc));
   CellArgs a = cell_args(pb);
-  CUDA_TRY(ctx, launch_l2_errors(a, pb->d_uint.as<double>(), errs.as<double>(), ctx->stream, ctx->num_sms,
+  CUDA_TRY(ctx, launch_l2_errors(a, pb->d_uint.as<double>(), pb->d_errs.as<double>(), ctx->stream, ctx->num_sms,
                                  &ctx->launches));
   std::vector<double> h(2 * nc);
-  CUDA_TRY(ctx, cudaMemcpyAsync(h.data(), errs.ptr, sizeof(double) * 2 * nc, cudaMemcpyDeviceToHost, ctx->stream));
+  CUDA_TRY(ctx, cudaMemcpyAsync(h.data(), pb->d_errs.ptr, sizeof(double) * 2 * nc, cudaMemcpyDeviceToHost,
+                                ctx->stream));
   CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   double ef = 0.0, ep = 0.0;
   for (size_t c = 0; c < nc; ++c) {
@@ -1058,6 +1058,28 @@ int hdg_solve(hdg_problem *pb, int precision, int solver, double rtol, int maxit
     stats[5] = pb->timings[4];
     stats[6] = pb->timings[0] + pb->timings[1] + pb->timings[2] + pb->timings[3] + pb->timings[4];
   }
+  return HDG_OK;
+}
+
+int hdg_problem_device_bytes(const hdg_problem *pb, double *bytes) {
+  if (!pb || !bytes) return HDG_ERR_INVALID;
+  const DBuf *bufs[] = {&pb->d_tabf, &pb->d_tab, &pb->d_origin, &pb->d_jac, &pb->d_cell_facets, &pb->d_facet_dofs,
+                        &pb->d_facet_cell, &pb->d_kappa, &pb->d_dirvals, &pb->d_A, &pb->d_b, &pb->d_S, &pb->d_g,
+                        &pb->d_fact, &pb->d_info, &pb->d_aux, &pb->d_rowptr, &pb->d_colind, &pb->d_val,
+                        &pb->d_rhs, &pb->d_br_row0, &pb->d_br_src, &pb->d_blk_off, &pb->d_blk_rowlen,
+                        &pb->d_blk_src, &pb->d_diag_blk, &pb->d_dir_cells, &pb->d_Binv, &pb->d_x, &pb->d_r,
+                        &pb->d_z, &pb->d_p, &pb->d_p2, &pb->d_q, &pb->d_partials, &pb->d_scal, &pb->d_counter,
+                        &pb->d_cellop, &pb->d_cell_blk, &pb->d_qc, &pb->d_Binv32, &pb->d_v32, &pb->d_scal2,
+                        &pb->d_minv, &pb->d_invm, &pb->d_uint, &pb->d_errs};
+  double s = 0.0;
+  for (const DBuf *b : bufs) s += (double)b->bytes;
+  *bytes = s;
+  return HDG_OK;
+}
+
+int hdg_footprint(int D, int n, int k, int precision, int solver, double *bytes) {
+  if (!bytes || D < 2 || D > 3 || n < 1 || k < 1 || k > kMaxK) return HDG_ERR_INVALID;
+  *bytes = footprint_bound(D, n, k, precision, solver);
   return HDG_OK;
 }
 

@@ -123,6 +123,13 @@ struct HostPattern {
 };
 int build_pattern(const HostMesh &m, HostPattern &p, std::string &err);
 
+// Whether the library has kernels for this (D, k, precision, solver) on a
+// device with `smem_optin` bytes of shared memory per CTA; `why` says what is missing.
+bool shape_supported(int D, int k, int precision, int solver, size_t smem_optin, std::string &why);
+// Upper bound of the device bytes of a Cartesian problem n^D, order k, solved
+// with (precision, solver).
+double footprint_bound(int D, int n, int k, int precision, int solver);
+
 }  // namespace hdg
 
 // ---------------------------------------------------------------------------
@@ -182,7 +189,7 @@ struct hdg_problem {
   cudaGraphExec_t pcg32_graph = nullptr;
   int cellop_nstage = 0, cellop_ctas = 0;  // streaming-kernel pipeline depth and grid
   int last_outer = 0;
-  hdg::DBuf d_uint;
+  hdg::DBuf d_uint, d_errs;
   hdg::DBuf h_pinned;  // host staging
   cudaGraphExec_t pcg_graph = nullptr;
   int pcg_graph_chunk = 0;

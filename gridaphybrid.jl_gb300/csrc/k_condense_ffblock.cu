@@ -84,9 +84,10 @@ struct Cfg {
   static constexpr int D = D_, NK = NK_, NFD = NFD_;
   static constexpr int NU = D * NK, NI = (D + 1) * NK, NF = 2 * D * NFD, N = NI + NF, NC = NF + 1;
   static constexpr int NT = 256;
-  // shared memory (floats): Y (D NK NK), P (NK NK), Z (D NK NC), Q (NK NC), M^{-1} (NK NK), each hi + lo
-  static constexpr size_t smem_floats =
-      2 * ((size_t)D * NK * NK + NK * NK + (size_t)D * NK * NC + NK * NC + (size_t)NK * NK);
+  // shared memory (floats): Y (D NK NK), P (NK NK; holds M^{-1} until P is
+  // formed), Z (D NK NC), Q (NK NC), each hi + lo -- 71 KB for 3D k=2, three
+  // CTAs per SM
+  static constexpr size_t smem_floats = 2 * ((size_t)D * NK * NK + NK * NK + (size_t)D * NK * NC + NK * NC);
   static constexpr size_t smem_bytes = smem_floats * 4 + 64 * 4;
 };
 
@@ -95,7 +96,7 @@ struct Cfg {
 #define AL(r, c) __ldg(Al + (size_t)(r) + (size_t)N * (c))
 
 template <class C>
-__global__ void __launch_bounds__(C::NT, 2)
+__global__ void __launch_bounds__(C::NT, 3)
     condense_ffblock_kernel(int ncells, const float *__restrict__ Ahi, const float *__restrict__ Alo,
                             const float *__restrict__ bhi, const float *__restrict__ blo,
                             const float *__restrict__ Minv_h, const float *__restrict__ Minv_l,
@@ -107,13 +108,9 @@ __global__ void __launch_bounds__(C::NT, 2)
   float *Ph = Yl + D * NK * NK, *Pl = Ph + NK * NK;  // [a][b]
   float *Zh = Pl + NK * NK, *Zl = Zh + D * NK * NC;  // [d][a][c]
   float *Qh = Zl + D * NK * NC, *Ql = Qh + NK * NC;  // [a][c]
-  float *Mh = Ql + NK * NC, *Ml = Mh + NK * NK;       // [a][k]
-  int *sflag = reinterpret_cast<int *>(Ml + NK * NK);  // [0] pivot row, [1] info
+  const float *Mh = Ph, *Ml = Pl;                      // M^{-1} [a][k], until P is formed
+  int *sflag = reinterpret_cast<int *>(Ql + NK * NC);  // [0] pivot row, [1] info
   const int t = threadIdx.x;
-  for (int e = t; e < NK * NK; e += NT) {
-    Mh[e] = Minv_h[e];
-    Ml[e] = Minv_l[e];
-  }
   // Threads run fastest over the row index of each output, so the
   // column-major A entries they read are broadcast (one column entry per
   // warp) or contiguous (consecutive rows of one column).
@@ -127,7 +124,11 @@ __global__ void __launch_bounds__(C::NT, 2)
       iml = (float)(v - (double)imh);
     }
     // Y_d = (1/m) M^{-1} G_d  and  Z_d = (1/m) M^{-1} R_{u_d}
-    __syncthreads();  // M^{-1} staged (first cell) / previous cell done
+    for (int e = t; e < NK * NK; e += NT) {
+      Ph[e] = __ldg(Minv_h + e);
+      Pl[e] = __ldg(Minv_l + e);
+    }
+    __syncthreads();
     for (int o = t; o < D * NK * (NK + NC); o += NT) {
       const int a = o % NK, rest = o / NK;
       const int c = rest % (NK + NC), d = rest / (NK + NC);

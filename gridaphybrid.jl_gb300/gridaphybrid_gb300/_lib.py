@@ -72,7 +72,29 @@ SIGNATURES = {
     "hdg_solve": (_i, [_vp, _i, _i, _d, _i, _vp, _vp, _vp]),
     "hdg_get_timings": (_i, [_vp, _vp]),
     "hdg_time_kernel": (_i, [_vp, _i, _i, _vp]),
+    "hdg_problem_device_bytes": (_i, [_vp, _vp]),
+    "hdg_footprint": (_i, [_i, _i, _i, _i, _i, _vp]),
+    "hdg_server_create": (_i, [_i, _i, _d, ctypes.POINTER(_vp)]),
+    "hdg_server_destroy": (_i, [_vp]),
+    "hdg_server_submit": (_i, [_vp, _vp, _vp]),
+    "hdg_server_poll": (_i, [_vp, _vp, _i, _d, _vp]),
+    "hdg_server_drain": (_i, [_vp, _d]),
+    "hdg_server_stats": (_i, [_vp, _vp]),
+    "hdg_server_last_error": (ctypes.c_char_p, [_vp]),
 }
+
+
+class Request(ctypes.Structure):
+    """struct hdg_request."""
+    _fields_ = [("D", _i), ("n", _i), ("k", _i), ("problem", _i), ("stab_mode", _i), ("precision", _i),
+                ("solver", _i), ("maxit", _i), ("tau", _d), ("rtol", _d), ("kappa", _vp), ("solution", _vp)]
+
+
+class Response(ctypes.Structure):
+    """struct hdg_response."""
+    _fields_ = [("ticket", _ll), ("status", _i), ("iters", _i), ("relres", _d), ("err_flux", _d),
+                ("err_pressure", _d), ("queue_ms", _d), ("run_ms", _d), ("latency_ms", _d),
+                ("footprint_bytes", _d), ("reused_mesh", _i), ("slot", _i)]
 
 
 class HdgError(RuntimeError):

@@ -236,6 +236,71 @@ int hdg_get_timings(const hdg_problem *pb, double *ms);
  * changed. */
 int hdg_time_kernel(hdg_problem *pb, int which, int reps, double *ms_per_launch);
 
+/* Device bytes currently reserved by the problem (all its buffers). */
+int hdg_problem_device_bytes(const hdg_problem *pb, double *bytes);
+
+/* ------------------------------------------------------------------------
+ * Serving (no reference counterpart: the reference solves one problem per
+ * `solve(op)` call).  A server owns `slots` worker threads; each runs one
+ * request at a time on its own stream, so admitted requests overlap on the
+ * device.  Requests are admitted in arrival order (a smaller one may pass a
+ * larger one that does not fit yet, a bounded number of times) as slots and
+ * the HBM budget free up; a request's footprint is hdg_footprint().  Meshes
+ * stay resident after a solve (connectivity, CSR pattern, buffers) and are
+ * reused by the next request with the same (D, n, k); idle resident meshes
+ * are evicted least-recently-used when the budget is needed.  A result does
+ * not depend on what else was running (deterministic kernels).
+ * ------------------------------------------------------------------------ */
+typedef struct hdg_server hdg_server;
+
+typedef struct hdg_request {
+  int D, n, k;         /* unit square/cube, n cells per side, order k */
+  int problem;         /* HDG_PROBLEM_* manufactured solution */
+  int stab_mode;       /* HDG_STAB_* */
+  int precision;       /* HDG_PREC_* */
+  int solver;          /* HDG_SOLVER_* */
+  int maxit;
+  double tau, rtol;
+  const double *kappa; /* n^D per-cell permeabilities (copied at submit) or NULL (all 1) */
+  double *solution;    /* NULL, or host buffer of ncells*ni + nfree free DOF values,
+                          written before the response is posted */
+} hdg_request;
+
+typedef struct hdg_response {
+  long long ticket;
+  int status;            /* HDG_OK or the failing call's code */
+  int iters;
+  double relres;
+  double err_flux, err_pressure; /* L2 errors against the manufactured solution */
+  double queue_ms;       /* submit -> admitted */
+  double run_ms;         /* admitted -> done */
+  double latency_ms;     /* submit -> done */
+  double footprint_bytes;/* reserved at admission */
+  int reused_mesh;       /* 1 if the mesh was already resident */
+  int slot;              /* worker that ran it */
+} hdg_response;
+
+/* Upper bound of the device bytes one request of this shape needs. */
+int hdg_footprint(int D, int n, int k, int precision, int solver, double *bytes);
+
+/* hbm_budget_bytes <= 0 selects 85% of the device's free memory. */
+int hdg_server_create(int device, int slots, double hbm_budget_bytes, hdg_server **out);
+/* Stops the workers after the running requests finish; queued requests are
+ * answered with HDG_ERR_STATE. */
+int hdg_server_destroy(hdg_server *s);
+/* Non-blocking.  Rejects (HDG_ERR_INVALID) shapes the library cannot solve
+ * and requests larger than the whole budget. */
+int hdg_server_submit(hdg_server *s, const hdg_request *req, long long *ticket);
+/* Moves up to `max` finished responses into out; waits up to timeout_ms for
+ * the first one when none is ready. */
+int hdg_server_poll(hdg_server *s, hdg_response *out, int max, double timeout_ms, int *count);
+/* Waits until no request is queued or running (HDG_ERR_NOT_CONVERGED on timeout). */
+int hdg_server_drain(hdg_server *s, double timeout_ms);
+/* [submitted, completed, failed, running, queued, bytes in use, budget,
+ *  peak bytes in use, mesh hits, mesh misses, evictions, max concurrent] */
+int hdg_server_stats(hdg_server *s, double *stats);
+const char *hdg_server_last_error(hdg_server *s);
+
 #ifdef __cplusplus
 }
 #endif
