@@ -327,10 +327,15 @@ def run_gpu(args):
     if args.precision == "fp64":
         spmv_bytes = nnz * 8 + (nnz // nfd) * 4 + nblockrows * 16 + 4 * nfree * 8
         spmv_kernel = "pcg_spmv_kernel<double,9>"
+        spmv_traffic = None  # not captured
     else:
         rec = (nl * (nl + 1) // 2 * nfd * nfd + 3) // 4 * 4
         spmv_bytes = ncells * rec * 4 + ncells * nl * 4 + 3 * nfree * 4 + ncells * nf * 4
         spmv_kernel = "cell_spmv32_kernel<6,9>"
+        # DRAM read + write of one launch from an ncu capture at 24^3 (99.83 MB over
+        # 13,824 cells), scaled by cells: the kernel streams each cell record once,
+        # so traffic grows with the cells
+        spmv_traffic = 99.83e6 / 13824 * ncells
     spmv_gbs = spmv_bytes / (spmv_ms.value * 1e-3) / 1e9
     # assembly: condensed blocks + vectors read, CSR values + rhs written
     asm_bytes = ncells * (nf * nf + nf) * 8 + nnz * 8 + nfree * 8
@@ -348,7 +353,7 @@ def run_gpu(args):
         "roofline": {"bound": "hbm",
                      "kernel": spmv_kernel,
                      "achieved": spmv_gbs, "peak": hbm,
-                     "unit": "GB/s", "frac": spmv_gbs / hbm, "traffic": None, "peak_source": peak_kind,
+                     "unit": "GB/s", "frac": spmv_gbs / hbm, "traffic": spmv_traffic, "peak_source": peak_kind,
                      "bytes_per_launch": spmv_bytes, "ms_per_launch": spmv_ms.value},
         "assembly_roofline": {"bound": "hbm", "achieved": asm_gbs, "peak": hbm, "unit": "GB/s",
                               "frac": asm_gbs / hbm, "bytes_per_launch": asm_bytes, "ms_per_launch": asm_ms.value},

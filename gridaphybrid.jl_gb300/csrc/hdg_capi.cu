@@ -310,6 +310,18 @@ int hdg_context_create(int device, hdg_context **out) {
   }
   for (auto &e : ctx->ev) cudaEventCreate(&e);
   for (auto &e : ctx->user_ev) cudaEventCreate(&e);
+  for (auto &b : ctx->scratch) b.stream = ctx->stream;
+  {
+    // freed pool memory stays with this process for reuse instead of being
+    // returned at every synchronisation (a property of the process's pool,
+    // gone when the process ends)
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+      uint64_t keep = UINT64_MAX;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    cudaGetLastError();
+  }
   *out = ctx;
   return HDG_OK;
 }
@@ -319,6 +331,7 @@ int hdg_context_destroy(hdg_context *ctx) {
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   for (auto &b : ctx->scratch) b.release();
+  cudaStreamSynchronize(ctx->stream);
   for (auto &e : ctx->ev)
     if (e) cudaEventDestroy(e);
   for (auto &e : ctx->user_ev)
@@ -408,7 +421,10 @@ int hdg_static_condensation(hdg_context *ctx, int precision, int ncells, int ni,
   for (int c = 0; c < ncells; ++c) bad |= hinfo[c] != 0;
   if (info) {
     if (is_device_ptr(info))
-      CUDA_TRY(ctx, cudaMemcpy(info, dinfo, sizeof(int) * ncells, cudaMemcpyDeviceToDevice));
+    {
+      CUDA_TRY(ctx, cudaMemcpyAsync(info, dinfo, sizeof(int) * ncells, cudaMemcpyDeviceToDevice, ctx->stream));
+      CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    }
     else
       memcpy(info, hinfo.data(), sizeof(int) * ncells);
   }
@@ -481,6 +497,7 @@ int hdg_problem_create_cartesian(hdg_context *ctx, int D, const int *cells, cons
   hdg_problem *pb = new (std::nothrow) hdg_problem();
   if (!pb) return ctx->fail(HDG_ERR_NOMEM, "host allocation failed");
   pb->ctx = ctx;
+  for (DBuf *b : pb->device_buffers()) b->stream = ctx->stream;
   std::string err;
   int rc = build_cartesian_mesh(D, cells, domain, k, pb->mesh, err);
   if (rc) {
@@ -508,6 +525,7 @@ int hdg_problem_create(hdg_context *ctx, int D, int k, int ncells, int nfacets,
   hdg_problem *pb = new (std::nothrow) hdg_problem();
   if (!pb) return ctx->fail(HDG_ERR_NOMEM, "host allocation failed");
   pb->ctx = ctx;
+  for (DBuf *b : pb->device_buffers()) b->stream = ctx->stream;
   HostMesh &m = pb->mesh;
   m.D = D;
   m.k = k;
@@ -536,8 +554,10 @@ int hdg_problem_create(hdg_context *ctx, int D, int k, int ncells, int nfacets,
 int hdg_problem_destroy(hdg_problem *pb) {
   if (!pb) return HDG_OK;
   cudaSetDevice(pb->ctx->device);
-  cudaStreamSynchronize(pb->ctx->stream);
-  delete pb;
+  cudaStream_t st = pb->ctx->stream;
+  cudaStreamSynchronize(st);
+  delete pb;  // stream-ordered frees
+  cudaStreamSynchronize(st);
   return HDG_OK;
 }
 
@@ -699,6 +719,17 @@ int hdg_get_skeleton_system(hdg_problem *pb, long long *rowptr, int *colind, dou
   return HDG_OK;
 }
 
+// Grid of the PCG vector and SpMV kernels: four CTAs per SM for large
+// skeletons, fewer for small ones (about two 256-row tiles per CTA) so that
+// the kernels of concurrent small problems share the GPU.
+static int pcg_grid(const hdg_problem *pb) {
+  const long long rows = pb->mesh.nfree;
+  long long g = (rows + 511) / 512;
+  const long long cap = (long long)pb->ctx->num_sms * 4;
+  if (g > cap) g = cap;
+  return g < 1 ? 1 : (int)g;
+}
+
 static PcgArgs pcg_args(hdg_problem *pb) {
   PcgArgs a{};
   a.n = pb->mesh.nfree;
@@ -719,7 +750,7 @@ static PcgArgs pcg_args(hdg_problem *pb) {
   a.scal = pb->d_scal.as<double>();
   a.counter = pb->d_counter.as<unsigned int>();
   a.val32 = nullptr;
-  a.nparts = pb->ctx->num_sms * 4;
+  a.nparts = pcg_grid(pb);
   a.diag_blk = pb->d_diag_blk.as<int>();
   a.blk_off = pb->d_blk_off.as<int64_t>();
   a.blk_rowlen = pb->d_blk_rowlen.as<int>();
@@ -744,7 +775,7 @@ static Pcg32Args pcg32_args(hdg_problem *pb) {
   ia.partials = pb->d_partials.as<double>();
   ia.scal = pb->d_scal.as<double>();
   ia.counter = pb->d_counter.as<unsigned int>();
-  ia.nparts = pb->ctx->num_sms * 4;
+  ia.nparts = pcg_grid(pb);
   ia.ncells = pb->mesh.ncells;
   ia.nl = 2 * pb->mesh.D;
   ia.rec = cellop_rec(ia.nl, ia.nfd);
@@ -766,6 +797,12 @@ static int solve_pcg_refined(hdg_problem *pb, double rtol, int maxit, int *it_ou
   if (!pb->d_cellop.ptr) return ctx->fail(HDG_ERR_STATE, "the FP32 cell operator is missing (assemble in a fast precision)");
   const int nl = 2 * pb->mesh.D;
   CUDA_TRY(ctx, cellop_configure(nl, (int)nfd, ctx->smem_optin, ctx->num_sms, &pb->cellop_nstage, &pb->cellop_ctas));
+  {  // at least two stages of cells per CTA on small problems
+    const int cps = cellop_cps(nl * (int)nfd);
+    const long long units = (pb->mesh.ncells + cps - 1) / cps;
+    const long long want = (units + 1) / 2;
+    if (want < pb->cellop_ctas) pb->cellop_ctas = want < 1 ? 1 : (int)want;
+  }
   if (pb->cellop_ctas > ctx->num_sms * 4)
     return ctx->fail(HDG_ERR_INVALID, "cell operator grid exceeds the partials buffer");
   CUDA_TRY(ctx, pb->d_Binv32.reserve(sizeof(float) * nbr * nfd * nfd));
@@ -1063,16 +1100,8 @@ int hdg_solve(hdg_problem *pb, int precision, int solver, double rtol, int maxit
 
 int hdg_problem_device_bytes(const hdg_problem *pb, double *bytes) {
   if (!pb || !bytes) return HDG_ERR_INVALID;
-  const DBuf *bufs[] = {&pb->d_tabf, &pb->d_tab, &pb->d_origin, &pb->d_jac, &pb->d_cell_facets, &pb->d_facet_dofs,
-                        &pb->d_facet_cell, &pb->d_kappa, &pb->d_dirvals, &pb->d_A, &pb->d_b, &pb->d_S, &pb->d_g,
-                        &pb->d_fact, &pb->d_info, &pb->d_aux, &pb->d_rowptr, &pb->d_colind, &pb->d_val,
-                        &pb->d_rhs, &pb->d_br_row0, &pb->d_br_src, &pb->d_blk_off, &pb->d_blk_rowlen,
-                        &pb->d_blk_src, &pb->d_diag_blk, &pb->d_dir_cells, &pb->d_Binv, &pb->d_x, &pb->d_r,
-                        &pb->d_z, &pb->d_p, &pb->d_p2, &pb->d_q, &pb->d_partials, &pb->d_scal, &pb->d_counter,
-                        &pb->d_cellop, &pb->d_cell_blk, &pb->d_qc, &pb->d_Binv32, &pb->d_v32, &pb->d_scal2,
-                        &pb->d_minv, &pb->d_invm, &pb->d_uint, &pb->d_errs};
   double s = 0.0;
-  for (const DBuf *b : bufs) s += (double)b->bytes;
+  for (const DBuf *b : const_cast<hdg_problem *>(pb)->device_buffers()) s += (double)b->bytes;
   *bytes = s;
   return HDG_OK;
 }

@@ -18,15 +18,26 @@ constexpr int kMaxK = 4;
 // ---------------------------------------------------------------------------
 // Device buffer owned by a context or problem.
 // ---------------------------------------------------------------------------
+// With `stream` set, allocation and release are stream-ordered
+// (cudaMallocAsync / cudaFreeAsync from the device's pool), so growing or
+// freeing one problem's buffers does not synchronise the device while other
+// streams run; every use of the buffer must then be ordered after the
+// allocation on that stream (the library uses one stream per context).
 struct DBuf {
   void *ptr = nullptr;
   size_t bytes = 0;
+  cudaStream_t stream = nullptr;
   DBuf() = default;
   DBuf(const DBuf &) = delete;
   DBuf &operator=(const DBuf &) = delete;
   ~DBuf() { release(); }
   void release() {
-    if (ptr) cudaFree(ptr);
+    if (ptr) {
+      if (stream)
+        cudaFreeAsync(ptr, stream);
+      else
+        cudaFree(ptr);
+    }
     ptr = nullptr;
     bytes = 0;
   }
@@ -35,7 +46,7 @@ struct DBuf {
     if (nbytes <= bytes && ptr) return cudaSuccess;
     release();
     if (nbytes == 0) nbytes = 16;
-    cudaError_t e = cudaMalloc(&ptr, nbytes);
+    cudaError_t e = stream ? cudaMallocAsync(&ptr, nbytes, stream) : cudaMalloc(&ptr, nbytes);
     if (e != cudaSuccess) {
       ptr = nullptr;
       return e;
@@ -193,5 +204,13 @@ struct hdg_problem {
   hdg::DBuf h_pinned;  // host staging
   cudaGraphExec_t pcg_graph = nullptr;
   int pcg_graph_chunk = 0;
+  // every device buffer of the problem (not the pinned host staging)
+  std::vector<hdg::DBuf *> device_buffers() {
+    return {&d_tabf, &d_tab, &d_origin, &d_jac, &d_cell_facets, &d_facet_dofs, &d_facet_cell, &d_kappa,
+            &d_dirvals, &d_A, &d_b, &d_S, &d_g, &d_fact, &d_info, &d_aux, &d_rowptr, &d_colind, &d_val,
+            &d_rhs, &d_br_row0, &d_br_src, &d_blk_off, &d_blk_rowlen, &d_blk_src, &d_diag_blk, &d_dir_cells,
+            &d_Binv, &d_x, &d_r, &d_z, &d_p, &d_p2, &d_q, &d_partials, &d_scal, &d_counter, &d_cellop,
+            &d_cell_blk, &d_qc, &d_Binv32, &d_v32, &d_scal2, &d_minv, &d_invm, &d_uint, &d_errs};
+  }
   ~hdg_problem();
 };

@@ -138,6 +138,8 @@ namespace {
 using Clock = std::chrono::steady_clock;
 
 constexpr int kMaxBypass = 8;
+// resident meshes that are idle may hold at most this share of the budget
+constexpr double kIdleShare = 0.5;
 
 double ms_between(Clock::time_point a, Clock::time_point b) {
   return std::chrono::duration<double, std::milli>(b - a).count();
@@ -173,7 +175,7 @@ struct hdg_server {
   std::deque<hdg_response> done;
   std::vector<std::unique_ptr<Resident>> idle;  // resident meshes not in use
   std::vector<std::thread> workers;
-  double in_use = 0.0, peak = 0.0;
+  double in_use = 0.0, peak = 0.0, busy_ms = 0.0;
   long long next_ticket = 1;
   long long submitted = 0, completed = 0, failed = 0;
   int running = 0, max_running = 0;
@@ -295,13 +297,28 @@ struct hdg_server {
           in_use += res->bytes;
           peak = std::max(peak, in_use);
           idle.push_back(std::move(res));
+          // keep the idle meshes within their share of the budget (LRU out)
+          double idle_bytes = evictable(nullptr);
+          while (idle_bytes > kIdleShare * budget && idle.size() > 1) {
+            size_t victim = 0;
+            for (size_t i = 1; i < idle.size(); ++i)
+              if (idle[i]->last_use < idle[victim]->last_use) victim = i;
+            idle_bytes -= idle[victim]->bytes;
+            in_use -= idle[victim]->bytes;
+            trash.push_back(std::move(idle[victim]));
+            idle.erase(idle.begin() + (long)victim);
+            ++evictions;
+          }
         }
         --running;
         ++completed;
         if (rc != HDG_OK) ++failed;
+        busy_ms += r.run_ms;
         done.push_back(r);
       }
       if (res) destroy_resident(res.get());  // a failed request does not keep its mesh
+      for (auto &t : trash) destroy_resident(t.get());
+      trash.clear();
       cv_done.notify_all();
       cv_work.notify_all();
     }
@@ -446,6 +463,7 @@ int hdg_server_stats(hdg_server *s, double *st) {
   st[9] = (double)s->mesh_misses;
   st[10] = (double)s->evictions;
   st[11] = (double)s->max_running;
+  st[12] = s->busy_ms;
   return HDG_OK;
 }
 

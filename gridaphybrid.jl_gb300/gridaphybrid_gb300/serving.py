@@ -77,10 +77,10 @@ class Server:
         self.check(self.lib.hdg_server_drain(self.h, float(timeout_ms)))
 
     def stats(self):
-        st = np.zeros(12)
+        st = np.zeros(13)
         self.check(self.lib.hdg_server_stats(self.h, _lib.ptr(st)))
         keys = ["submitted", "completed", "failed", "running", "queued", "bytes_in_use", "budget",
-                "peak_bytes", "mesh_hits", "mesh_misses", "evictions", "max_concurrent"]
+                "peak_bytes", "mesh_hits", "mesh_misses", "evictions", "max_concurrent", "busy_ms"]
         return dict(zip(keys, st.tolist()))
 
     def close(self):
@@ -172,4 +172,5 @@ def latency_summary(resp, wall_s):
         "solves_per_s": ok / wall_s, "cells_per_s": cells / wall_s, "wall_s": wall_s,
         "mesh_reuse": float(np.mean([r["reused_mesh"] for r in resp if r["status"] == 0])),
         "queue_p50_ms": float(np.percentile([r["queue_ms"] for r in resp if r["status"] == 0], 50)),
+        "run_p50_ms": float(np.percentile([r["run_ms"] for r in resp if r["status"] == 0], 50)),
     }

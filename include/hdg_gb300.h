@@ -248,7 +248,8 @@ int hdg_problem_device_bytes(const hdg_problem *pb, double *bytes);
  * the HBM budget free up; a request's footprint is hdg_footprint().  Meshes
  * stay resident after a solve (connectivity, CSR pattern, buffers) and are
  * reused by the next request with the same (D, n, k); idle resident meshes
- * are evicted least-recently-used when the budget is needed.  A result does
+ * are evicted least-recently-used when the budget is needed or when they hold
+ * more than half of it.  A result does
  * not depend on what else was running (deterministic kernels).
  * ------------------------------------------------------------------------ */
 typedef struct hdg_server hdg_server;
@@ -297,7 +298,8 @@ int hdg_server_poll(hdg_server *s, hdg_response *out, int max, double timeout_ms
 /* Waits until no request is queued or running (HDG_ERR_NOT_CONVERGED on timeout). */
 int hdg_server_drain(hdg_server *s, double timeout_ms);
 /* [submitted, completed, failed, running, queued, bytes in use, budget,
- *  peak bytes in use, mesh hits, mesh misses, evictions, max concurrent] */
+ *  peak bytes in use, mesh hits, mesh misses, evictions, max concurrent,
+ *  summed run ms of finished requests] (13 values) */
 int hdg_server_stats(hdg_server *s, double *stats);
 const char *hdg_server_last_error(hdg_server *s);
 

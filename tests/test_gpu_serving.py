@@ -57,23 +57,43 @@ def test_same_result_alone_and_in_the_mix(precision):
 
 
 def test_admission_respects_budget_and_reuses_meshes():
-    shapes = [(3, 10, 2), (3, 10, 2), (2, 48, 2), (3, 10, 2), (2, 48, 2), (3, 12, 1)]
-    fp = []
-    for D, n, k in shapes:
+    """Budget for one (3, 10, 2) request: its resident mesh is reused by the next
+    request of that shape and evicted to admit a different one."""
+    def fp(D, n, k):
         b = ctypes.c_double()
         assert _lib.load().hdg_footprint(D, n, k, _lib.HDG_PREC_FF_BLOCK, _lib.HDG_SOLVER_PCG, ctypes.byref(b)) == 0
-        fp.append(b.value)
-    budget = 1.6 * max(fp)  # room for one large request (plus a little) at a time
-    with Server(slots=4, budget_bytes=budget) as srv:
+        return b.value
+
+    shapes = [(3, 10, 2), (3, 10, 2), (3, 12, 1), (3, 10, 2)]
+    budget = 1.02 * fp(3, 10, 2)
+    assert fp(3, 12, 1) < budget
+    with Server(slots=1, budget_bytes=budget) as srv:
         for i, (D, n, k) in enumerate(shapes):
             srv.submit(D, n, k, kappa=kappa_for(D, n, i), precision=_lib.HDG_PREC_FF_BLOCK)
         srv.drain()
-        res = srv.poll(max_items=16)
+        res = sorted(srv.poll(max_items=16), key=lambda r: r["ticket"])
         st = srv.stats()
     assert len(res) == len(shapes) and all(r["status"] == 0 for r in res)
+    assert [r["reused_mesh"] for r in res][:2] == [0, 1]
     assert st["peak_bytes"] <= budget
-    assert st["mesh_hits"] >= 1
-    assert st["evictions"] >= 1
+    assert st["mesh_hits"] >= 1 and st["evictions"] >= 1
+
+
+def test_requests_overlap_under_a_budget():
+    """Eight slots, a budget for about three of the requests at a time: the
+    requests run concurrently and the reserved bytes never exceed the budget."""
+    b = ctypes.c_double()
+    assert _lib.load().hdg_footprint(2, 40, 1, _lib.HDG_PREC_FF_BLOCK, _lib.HDG_SOLVER_PCG, ctypes.byref(b)) == 0
+    budget = 3.2 * b.value
+    with Server(slots=8, budget_bytes=budget) as srv:
+        for i in range(12):
+            srv.submit(2, 40 + (i % 4), 1, kappa=kappa_for(2, 40 + (i % 4), i), precision=_lib.HDG_PREC_FF_BLOCK)
+        srv.drain()
+        res = srv.poll(max_items=16)
+        st = srv.stats()
+    assert len(res) == 12 and all(r["status"] == 0 for r in res)
+    assert 2 <= st["max_concurrent"] <= 3
+    assert st["peak_bytes"] <= budget
 
 
 def test_mesh_reuse_gives_the_fresh_result():
