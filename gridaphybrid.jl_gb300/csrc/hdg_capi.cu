@@ -4,6 +4,8 @@
 // the kernels on the context's stream.
 #include <cuda_runtime.h>
 
+#include <chrono>
+
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -631,16 +633,22 @@ int hdg_set_dirichlet_values(hdg_problem *pb, const double *vals) {
 
 static float elapsed(cudaEvent_t a, cudaEvent_t b) {
   float ms = 0.f;
-  cudaEventElapsedTime(&ms, a, b);
+  if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) {
+    cudaGetLastError();  // not a failure of the computation: leave no error behind
+    ms = 0.f;
+  }
   return ms;
 }
 
-int hdg_assemble(hdg_problem *pb, int precision, int *info) {
-  if (!pb) return HDG_ERR_INVALID;
+}  // extern "C"
+
+// Validates the precision for this problem and reserves the buffers of an
+// assembly.  cell_blocks: the separate integrate / condense kernels keep the
+// cell blocks A, b in HBM (the batched fused kernels do not).
+static int assemble_prepare(hdg_problem *pb, int precision, bool cell_blocks) {
   hdg_context *ctx = pb->ctx;
   if (precision != HDG_PREC_FP64 && precision != HDG_PREC_FP32_REFINED && precision != HDG_PREC_FF_BLOCK)
     return ctx->fail(HDG_ERR_INVALID, "unknown precision %d", precision);
-  cudaSetDevice(ctx->device);
   const RefTables &t = pb->tab;
   const size_t nc = pb->mesh.ncells, n = t.n, ni = t.ni, nf = t.nf;
   const bool mixed = precision != HDG_PREC_FP64;
@@ -651,10 +659,15 @@ int hdg_assemble(hdg_problem *pb, int precision, int *info) {
                                                          : 0;
   if (need > ctx->smem_optin - 1024)
     return ctx->fail(HDG_ERR_INVALID, "cell block %zu exceeds the shared-memory condensation kernel", n);
-  if (precision == HDG_PREC_FF_BLOCK) CUDA_TRY(ctx, pb->d_invm.reserve(sizeof(double) * nc));
-  // cell blocks: FP64, or (hi, lo) float pairs in the same bytes
-  CUDA_TRY(ctx, pb->d_A.reserve(sizeof(double) * nc * n * n));
-  CUDA_TRY(ctx, pb->d_b.reserve(sizeof(double) * nc * n));
+  const int nl = 2 * t.D;
+  if (mixed && !cellop_supported(nl, (int)t.nfd))
+    return ctx->fail(HDG_ERR_INVALID, "no unassembled FP32 operator for %d facets of %zu DOFs", nl, t.nfd);
+  if (precision == HDG_PREC_FF_BLOCK && cell_blocks) CUDA_TRY(ctx, pb->d_invm.reserve(sizeof(double) * nc));
+  if (cell_blocks) {
+    // cell blocks: FP64, or (hi, lo) float pairs in the same bytes
+    CUDA_TRY(ctx, pb->d_A.reserve(sizeof(double) * nc * n * n));
+    CUDA_TRY(ctx, pb->d_b.reserve(sizeof(double) * nc * n));
+  }
   CUDA_TRY(ctx, pb->d_S.reserve(sizeof(double) * nc * nf * nf));
   CUDA_TRY(ctx, pb->d_g.reserve(sizeof(double) * nc * nf));
   CUDA_TRY(ctx, pb->d_aux.reserve(sizeof(double) * nc * nf));
@@ -663,26 +676,44 @@ int hdg_assemble(hdg_problem *pb, int precision, int *info) {
   CUDA_TRY(ctx, pb->d_info.reserve(sizeof(int) * nc));
   CUDA_TRY(ctx, pb->d_val.reserve(sizeof(double) * (pb->pat.nnz ? pb->pat.nnz : 1)));
   CUDA_TRY(ctx, pb->d_rhs.reserve(sizeof(double) * (pb->mesh.nfree ? pb->mesh.nfree : 1)));
-  const int nl = 2 * t.D;
-  if (mixed && !cellop_supported(nl, (int)t.nfd))
-    return ctx->fail(HDG_ERR_INVALID, "no unassembled FP32 operator for %d facets of %zu DOFs", nl, t.nfd);
   if (mixed) CUDA_TRY(ctx, pb->d_cellop.reserve(sizeof(float) * nc * cellop_rec(nl, (int)t.nfd)));
-  cudaEvent_t *ev = ctx->ev;
   pb->precision = precision;
   pb->assembled = pb->solved = pb->recovered = false;
+  return HDG_OK;
+}
+
+// Skeleton side of an assembly: the CSR gather + Dirichlet lift, and on the
+// fast paths the FP32 cell operator of the inner skeleton iterations.
+static cudaError_t assemble_skeleton(hdg_problem *pb) {
+  hdg_context *ctx = pb->ctx;
+  const RefTables &t = pb->tab;
+  AssembleArgs as = assemble_args(pb);
+  cudaError_t e = launch_assemble(as, pb->d_S.as<double>(), pb->d_g.as<double>(), pb->d_aux.as<double>(),
+                                  pb->d_val.as<double>(), pb->d_rhs.as<double>(), ctx->stream, ctx->num_sms,
+                                  &ctx->launches);
+  if (e != cudaSuccess || pb->precision == HDG_PREC_FP64) return e;
+  // the operator in the SPD frame
+  return launch_pack_cell_blocks(pb->mesh.ncells, 2 * t.D, t.nfd, -1.0, pb->d_S.as<double>(),
+                                 pb->d_cellop.as<float>(), ctx->smem_optin, ctx->stream, ctx->num_sms,
+                                 &ctx->launches);
+}
+
+extern "C" {
+
+int hdg_assemble(hdg_problem *pb, int precision, int *info) {
+  if (!pb) return HDG_ERR_INVALID;
+  hdg_context *ctx = pb->ctx;
+  cudaSetDevice(ctx->device);
+  int rc = assemble_prepare(pb, precision, true);
+  if (rc) return rc;
+  const size_t nc = pb->mesh.ncells;
+  cudaEvent_t *ev = ctx->ev;
   CUDA_TRY(ctx, cudaEventRecord(ev[0], ctx->stream));
   CUDA_TRY(ctx, run_integrate(pb));
   CUDA_TRY(ctx, cudaEventRecord(ev[1], ctx->stream));
   CUDA_TRY(ctx, run_condense(pb));
   CUDA_TRY(ctx, cudaEventRecord(ev[2], ctx->stream));
-  AssembleArgs as = assemble_args(pb);
-  CUDA_TRY(ctx, launch_assemble(as, pb->d_S.as<double>(), pb->d_g.as<double>(), pb->d_aux.as<double>(),
-                                pb->d_val.as<double>(), pb->d_rhs.as<double>(), ctx->stream, ctx->num_sms,
-                                &ctx->launches));
-  if (mixed)  // the FP32 operator of the inner skeleton iterations, in the SPD frame
-    CUDA_TRY(ctx, launch_pack_cell_blocks((int)nc, nl, (int)t.nfd, -1.0, pb->d_S.as<double>(),
-                                          pb->d_cellop.as<float>(), ctx->smem_optin, ctx->stream, ctx->num_sms,
-                                          &ctx->launches));
+  CUDA_TRY(ctx, assemble_skeleton(pb));
   CUDA_TRY(ctx, cudaEventRecord(ev[3], ctx->stream));
   std::vector<int> hinfo(nc);
   CUDA_TRY(ctx, cudaMemcpyAsync(hinfo.data(), pb->d_info.ptr, sizeof(int) * nc, cudaMemcpyDeviceToHost, ctx->stream));
@@ -690,7 +721,6 @@ int hdg_assemble(hdg_problem *pb, int precision, int *info) {
   pb->timings[0] = elapsed(ev[0], ev[1]);
   pb->timings[1] = elapsed(ev[1], ev[2]);
   pb->timings[2] = elapsed(ev[2], ev[3]);
-  pb->precision = precision;
   bool bad = false;
   for (size_t c = 0; c < nc; ++c) bad |= hinfo[c] != 0;
   if (info) memcpy(info, hinfo.data(), sizeof(int) * nc);
@@ -1166,6 +1196,302 @@ int hdg_time_kernel(hdg_problem *pb, int which, int reps, double *ms_per_launch)
   CUDA_TRY(ctx, cudaEventRecord(ctx->ev[1], ctx->stream));
   CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   *ms_per_launch = elapsed(ctx->ev[0], ctx->ev[1]) / reps;
+  return HDG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Size-class batching.
+// ---------------------------------------------------------------------------
+}  // extern "C"
+
+struct hdg_batch {
+  hdg_context *ctx = nullptr;
+  std::vector<hdg_problem *> probs;
+  struct Class {
+    int D = 0, k = 0;
+    std::vector<int> members;  // indices into probs, in batch order
+    long long total = 0;       // cells
+    int tpc[3] = {0, 0, 0};    // tuned threads per cell, by precision
+    double tuned_ms[3] = {0, 0, 0};
+  };
+  std::vector<Class> classes;
+  DBuf d_probs, d_bad, d_scratch;
+  std::vector<BatchProblem> h_probs;
+  // the launch sequence as two CUDA graphs (fused cell work; skeleton
+  // assembly), timed by events recorded between the replays
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  int graph_precision = -1;
+  std::vector<const void *> graph_key;  // buffer addresses the graphs were captured with
+  long long graph_launches[2] = {0, 0}; // kernels one replay launches
+  double timings[3] = {0, 0, 0};        // fused integrate+condense, skeleton assembly, solve+recover (ms)
+  ~hdg_batch() {
+    for (auto &g : graph)
+      if (g) cudaGraphExecDestroy(g);
+  }
+};
+
+namespace {
+
+const int kTpcCandidates[4] = {256, 128, 64, 32};
+
+int prec_slot(int precision) { return precision == HDG_PREC_FP64 ? 0 : precision == HDG_PREC_FF_BLOCK ? 1 : 2; }
+
+FusedLaunch fused_launch(hdg_batch *b, size_t ci, int precision, int tpc, size_t prob_off) {
+  hdg_context *ctx = b->ctx;
+  const hdg_batch::Class &cl = b->classes[ci];
+  const RefTables &t = b->probs[(size_t)cl.members[0]]->tab;
+  FusedLaunch L{};
+  L.precision = precision;
+  L.D = cl.D;
+  L.k = cl.k;
+  L.n = t.n;
+  L.ni = t.ni;
+  L.nf = t.nf;
+  L.nqv = t.nqv;
+  L.tpc = tpc;
+  L.probs = b->d_probs.as<BatchProblem>() + prob_off;
+  L.nprob = (int)cl.members.size();
+  L.total = cl.total;
+  L.scratch = b->d_scratch.as<float>();
+  L.scratch_bytes = b->d_scratch.bytes;
+  L.bad = b->d_bad.as<int>() + prob_off;
+  L.num_sms = ctx->num_sms;
+  L.smem_optin = ctx->smem_optin;
+  return L;
+}
+
+}  // namespace
+
+extern "C" {
+
+int hdg_batch_create(hdg_context *ctx, int nproblems, hdg_problem *const *problems, hdg_batch **out) {
+  if (!ctx || !out || nproblems < 1 || !problems) return ctx ? ctx->fail(HDG_ERR_INVALID, "bad arguments") : 1;
+  *out = nullptr;
+  hdg_batch *b = new (std::nothrow) hdg_batch();
+  if (!b) return ctx->fail(HDG_ERR_NOMEM, "host allocation failed");
+  b->ctx = ctx;
+  for (int i = 0; i < nproblems; ++i) {
+    hdg_problem *pb = problems[i];
+    if (!pb || pb->ctx != ctx) {
+      delete b;
+      return ctx->fail(HDG_ERR_INVALID, "problem %d is null or belongs to another context", i);
+    }
+    b->probs.push_back(pb);
+    size_t ci = 0;
+    for (; ci < b->classes.size(); ++ci)
+      if (b->classes[ci].D == pb->mesh.D && b->classes[ci].k == pb->mesh.k) break;
+    if (ci == b->classes.size()) {
+      b->classes.emplace_back();
+      b->classes.back().D = pb->mesh.D;
+      b->classes.back().k = pb->mesh.k;
+    }
+    b->classes[ci].members.push_back(i);
+    b->classes[ci].total += pb->mesh.ncells;
+  }
+  *out = b;
+  return HDG_OK;
+}
+
+int hdg_batch_destroy(hdg_batch *b) {
+  if (!b) return HDG_OK;
+  cudaSetDevice(b->ctx->device);
+  cudaStreamSynchronize(b->ctx->stream);
+  for (DBuf *d : {&b->d_probs, &b->d_bad, &b->d_scratch}) d->stream = b->ctx->stream;
+  delete b;
+  return HDG_OK;
+}
+
+int hdg_batch_assemble(hdg_batch *b, int precision, int *bad) {
+  if (!b) return HDG_ERR_INVALID;
+  hdg_context *ctx = b->ctx;
+  if (precision != HDG_PREC_FP64 && precision != HDG_PREC_FF_BLOCK)
+    return ctx->fail(HDG_ERR_INVALID, "batched kernels exist for HDG_PREC_FP64 and HDG_PREC_FF_BLOCK");
+  cudaSetDevice(ctx->device);
+  for (const auto &cl : b->classes)
+    if (!fused_batch_supported(cl.D, cl.k, precision))
+      return ctx->fail(HDG_ERR_INVALID, "no fused batch kernel for D=%d k=%d at this precision", cl.D, cl.k);
+  int rc;
+  for (hdg_problem *pb : b->probs)
+    if ((rc = assemble_prepare(pb, precision, false))) return rc;
+  for (DBuf *d : {&b->d_probs, &b->d_bad, &b->d_scratch}) d->stream = ctx->stream;
+  // per-problem descriptors, class by class
+  const size_t np = b->probs.size();
+  b->h_probs.assign(np, BatchProblem{});
+  std::vector<size_t> class_off(b->classes.size());
+  {
+    size_t k = 0;
+    for (size_t ci = 0; ci < b->classes.size(); ++ci) {
+      class_off[ci] = k;
+      long long first = 0;
+      for (int m : b->classes[ci].members) {
+        hdg_problem *pb = b->probs[(size_t)m];
+        BatchProblem &P = b->h_probs[k++];
+        const size_t nc = pb->mesh.ncells, ni = pb->tab.ni, nf = pb->tab.nf;
+        P.a = cell_args(pb);
+        P.T = mixed_tables(pb);
+        P.Mh = pb->d_minv.as<float>();
+        P.Ml = P.Mh + (size_t)pb->tab.nk * pb->tab.nk;
+        P.S = pb->d_S.as<double>();
+        P.g = pb->d_g.as<double>();
+        P.Xh = pb->d_fact.as<float>();
+        P.Xl = P.Xh + nc * ni * (nf + 1);
+        P.fact = pb->d_fact.as<double>();
+        P.info = pb->d_info.as<int>();
+        P.first = first;
+        first += (long long)nc;
+      }
+    }
+  }
+  CUDA_TRY(ctx, b->d_probs.reserve(sizeof(BatchProblem) * np));
+  CUDA_TRY(ctx, b->d_bad.reserve(sizeof(int) * np));
+  CUDA_TRY(ctx, cudaMemcpyAsync(b->d_probs.ptr, b->h_probs.data(), sizeof(BatchProblem) * np, cudaMemcpyHostToDevice,
+                                ctx->stream));
+  const int slot = prec_slot(precision);
+  // scratch for every candidate tile (block elimination keeps cells in L2 slots)
+  size_t scratch = 16;
+  for (size_t ci = 0; ci < b->classes.size(); ++ci)
+    for (int tpc : kTpcCandidates) {
+      FusedLaunch L = fused_launch(b, ci, precision, tpc, class_off[ci]);
+      size_t need = 0;
+      L.dry_run = true;
+      L.scratch_bytes_out = &need;
+      if (launch_fused_batch(L, ctx->stream, &ctx->launches) == cudaSuccess) scratch = std::max(scratch, need);
+      cudaGetLastError();
+    }
+  CUDA_TRY(ctx, b->d_scratch.reserve(scratch));
+  // autotune: threads per cell (cells per CTA) for each class, timed on this batch
+  cudaEvent_t *ev = ctx->ev;
+  for (size_t ci = 0; ci < b->classes.size(); ++ci) {
+    hdg_batch::Class &cl = b->classes[ci];
+    if (cl.tpc[slot]) continue;
+    double best = 1e300;
+    for (int tpc : kTpcCandidates) {
+      FusedLaunch L = fused_launch(b, ci, precision, tpc, class_off[ci]);
+      if (launch_fused_batch(L, ctx->stream, &ctx->launches) != cudaSuccess) {  // infeasible tile
+        cudaGetLastError();
+        continue;
+      }
+      CUDA_TRY(ctx, cudaEventRecord(ev[0], ctx->stream));
+      CUDA_TRY(ctx, launch_fused_batch(L, ctx->stream, &ctx->launches));
+      CUDA_TRY(ctx, cudaEventRecord(ev[1], ctx->stream));
+      CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+      const double ms = elapsed(ev[0], ev[1]);
+      if (ms < best) {
+        best = ms;
+        cl.tpc[slot] = tpc;
+      }
+    }
+    if (!cl.tpc[slot]) return ctx->fail(HDG_ERR_INVALID, "no feasible tile for class D=%d k=%d", cl.D, cl.k);
+    cl.tuned_ms[slot] = best;
+  }
+  // the batch's launch sequence as one CUDA graph (re-captured when buffers move)
+  std::vector<const void *> key{b->d_probs.ptr, b->d_bad.ptr, b->d_scratch.ptr};
+  for (hdg_problem *pb : b->probs)
+    for (const DBuf *d : pb->device_buffers()) key.push_back(d->ptr);
+  auto enqueue_cells = [&]() -> cudaError_t {
+    cudaError_t e = cudaMemsetAsync(b->d_bad.ptr, 0, sizeof(int) * np, ctx->stream);
+    for (size_t ci = 0; ci < b->classes.size() && e == cudaSuccess; ++ci)
+      e = launch_fused_batch(fused_launch(b, ci, precision, b->classes[ci].tpc[slot], class_off[ci]), ctx->stream,
+                             &ctx->launches);
+    return e;
+  };
+  auto enqueue_skeleton = [&]() -> cudaError_t {
+    cudaError_t e = cudaSuccess;
+    for (hdg_problem *pb : b->probs)
+      if (e == cudaSuccess) e = assemble_skeleton(pb);
+    return e;
+  };
+  if (!b->graph[0] || b->graph_precision != precision || b->graph_key != key) {
+    for (int gi = 0; gi < 2; ++gi) {
+      if (b->graph[gi]) cudaGraphExecDestroy(b->graph[gi]);
+      b->graph[gi] = nullptr;
+      cudaGraph_t g;
+      const long long l0 = ctx->launches;
+      CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+      cudaError_t e = gi == 0 ? enqueue_cells() : enqueue_skeleton();
+      cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &g);
+      b->graph_launches[gi] = ctx->launches - l0;
+      ctx->launches = l0;
+      CUDA_TRY(ctx, e);
+      CUDA_TRY(ctx, e2);
+      e = cudaGraphInstantiate(&b->graph[gi], g, 0);
+      cudaGraphDestroy(g);
+      CUDA_TRY(ctx, e);
+    }
+    b->graph_precision = precision;
+    b->graph_key = key;
+  }
+  CUDA_TRY(ctx, cudaEventRecord(ev[4], ctx->stream));
+  CUDA_TRY(ctx, cudaGraphLaunch(b->graph[0], ctx->stream));
+  CUDA_TRY(ctx, cudaEventRecord(ev[5], ctx->stream));
+  CUDA_TRY(ctx, cudaGraphLaunch(b->graph[1], ctx->stream));
+  CUDA_TRY(ctx, cudaEventRecord(ev[6], ctx->stream));
+  ctx->launches += b->graph_launches[0] + b->graph_launches[1];
+  std::vector<int> hbad(np);
+  CUDA_TRY(ctx, cudaMemcpyAsync(hbad.data(), b->d_bad.ptr, sizeof(int) * np, cudaMemcpyDeviceToHost, ctx->stream));
+  CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  b->timings[0] = elapsed(ev[4], ev[5]);
+  b->timings[1] = elapsed(ev[5], ev[6]);
+  // descriptors are in class order; report per problem in batch order
+  std::vector<int> bad_by_problem(np, 0);
+  {
+    size_t k = 0;
+    for (const auto &cl : b->classes)
+      for (int m : cl.members) bad_by_problem[(size_t)m] = hbad[k++];
+  }
+  bool any = false;
+  for (size_t i = 0; i < np; ++i) {
+    any |= bad_by_problem[i] != 0;
+    hdg_problem *pb = b->probs[i];
+    pb->timings[0] = 0.0;
+    pb->timings[1] = b->timings[0];
+    pb->timings[2] = b->timings[1];
+    pb->assembled = bad_by_problem[i] == 0;
+  }
+  if (bad) memcpy(bad, bad_by_problem.data(), sizeof(int) * np);
+  if (any) return ctx->fail(HDG_ERR_SINGULAR, "zero pivot in an interior block of a batched problem (see bad)");
+  return HDG_OK;
+}
+
+int hdg_batch_solve(hdg_batch *b, int solver, double rtol, int maxit, int *iters, double *relres) {
+  if (!b) return HDG_ERR_INVALID;
+  hdg_context *ctx = b->ctx;
+  cudaSetDevice(ctx->device);
+  const auto h0 = std::chrono::steady_clock::now();
+  for (size_t i = 0; i < b->probs.size(); ++i) {
+    int it = 0;
+    double rel = 0.0;
+    int rc = hdg_solve_skeleton(b->probs[i], solver, rtol, maxit, &it, &rel);
+    if (iters) iters[i] = it;
+    if (relres) relres[i] = rel;
+    if (rc) return rc;
+    if ((rc = hdg_recover(b->probs[i]))) return rc;
+  }
+  CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  b->timings[2] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - h0).count();
+  return HDG_OK;
+}
+
+int hdg_batch_timings(const hdg_batch *b, double *ms) {
+  if (!b || !ms) return HDG_ERR_INVALID;
+  for (int i = 0; i < 3; ++i) ms[i] = b->timings[i];
+  return HDG_OK;
+}
+
+int hdg_batch_tuning(const hdg_batch *b, int precision, int max_classes, int *D, int *k, int *tpc, double *ms,
+                     long long *cells, int *nclasses) {
+  if (!b || !nclasses) return HDG_ERR_INVALID;
+  const int slot = prec_slot(precision);
+  const int nc = (int)b->classes.size();
+  *nclasses = nc;
+  for (int i = 0; i < nc && i < max_classes; ++i) {
+    const auto &cl = b->classes[(size_t)i];
+    if (D) D[i] = cl.D;
+    if (k) k[i] = cl.k;
+    if (tpc) tpc[i] = cl.tpc[slot];
+    if (ms) ms[i] = cl.tuned_ms[slot];
+    if (cells) cells[i] = cl.total;
+  }
   return HDG_OK;
 }
 

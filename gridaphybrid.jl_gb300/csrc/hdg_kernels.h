@@ -209,6 +209,35 @@ cudaError_t launch_pcg32_spmv(const Pcg32Args &a, cudaStream_t s, long long *lau
 cudaError_t launch_outer_init(const OuterArgs &a, cudaStream_t s, long long *launches);
 // x += e, then r = c - M x and |r|^2
 cudaError_t launch_outer_update(const OuterArgs &a, const float *e, cudaStream_t s, long long *launches);
+// Size-class batching: one persistent fused integrate -> condense launch over
+// the cells of several problems of one (D, k) class.
+struct BatchProblem {
+  CellArgs a;
+  MixedTables T;
+  const float *Mh, *Ml;  // M_ref^{-1} (hi, lo), block elimination
+  double *S, *g;         // condensed blocks and vectors
+  float *Xh, *Xl;        // float-float recovery pairs, block elimination
+  double *fact;          // FP64 recovery factors [U11 | U12 | y]
+  int *info;             // per cell
+  long long first;       // first item (cell) of this problem in the class
+};
+struct FusedLaunch {
+  int precision, D, k, n, ni, nf, nqv;
+  int tpc;                     // threads per cell: 32, 64, 128 or 256 (256/tpc cells per CTA)
+  const BatchProblem *probs;   // device array, ordered by `first`
+  int nprob;
+  long long total;             // cells in the class
+  float *scratch;              // block elimination: per-group cell slots
+  size_t scratch_bytes;
+  size_t *scratch_bytes_out;   // receives the slots' size for this configuration (may be null)
+  bool dry_run;                // size the launch only
+  int *bad;                    // per problem: largest zero-pivot index (0 = ok)
+  int num_sms;
+  size_t smem_optin;
+};
+bool fused_batch_supported(int D, int k, int precision);
+cudaError_t launch_fused_batch(const FusedLaunch &L, cudaStream_t s, long long *launches);
+
 // dense LU solve of a CSR system (small n), one CTA
 cudaError_t launch_dense_solve(int n, const int64_t *rowptr, const int *colind,
                                const double *val, const double *rhs, double *work,

@@ -17,83 +17,11 @@
 #include <cuda_runtime.h>
 
 #include "hdg_kernels.h"
+#include "k_ff_cell.cuh"
+#include "k_ffblock_cell.cuh"
 
 namespace hdg {
 namespace ffb {
-
-__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
-  s = a + b;
-  const float bb = s - a;
-  e = (a - (s - bb)) + (b - bb);
-}
-
-__device__ __forceinline__ void fast_two_sum(float a, float b, float &s, float &e) {
-  s = a + b;
-  e = b - (s - a);
-}
-
-// (h, l) += (ah + al) * (bh + bl)
-__device__ __forceinline__ void mac(float &h, float &l, float ah, float al, float bh, float bl) {
-  const float p = ah * bh;
-  float pe = fmaf(ah, bh, -p);
-  pe = fmaf(al, bh, pe);
-  pe = fmaf(ah, bl, pe);
-  float s, e;
-  two_sum(h, p, s, e);
-  h = s;
-  l += e + pe;
-}
-
-// normalised product (ah + al) * (bh + bl)
-__device__ __forceinline__ void mul(float ah, float al, float bh, float bl, float &h, float &l) {
-  const float p = ah * bh;
-  float pe = fmaf(ah, bh, -p);
-  pe = fmaf(al, bh, pe);
-  pe = fmaf(ah, bl, pe);
-  fast_two_sum(p, pe, h, l);
-}
-
-// normalised (ah + al) - (bh + bl)
-__device__ __forceinline__ void sub(float ah, float al, float bh, float bl, float &h, float &l) {
-  float s, e;
-  two_sum(ah, -bh, s, e);
-  e += al - bl;
-  fast_two_sum(s, e, h, l);
-}
-
-// normalised (ah + al) / (bh + bl)
-__device__ __forceinline__ void div(float ah, float al, float bh, float bl, float &h, float &l) {
-  const float q1 = ah / bh;
-  float ph, pl;
-  mul(q1, 0.0f, bh, bl, ph, pl);
-  float rh, rl;
-  sub(ah, al, ph, pl, rh, rl);
-  const float q2 = rh / bh;
-  fast_two_sum(q1, q2, h, l);
-}
-
-__device__ __forceinline__ void normalise(float &h, float &l) {
-  float s, e;
-  fast_two_sum(h, l, s, e);
-  h = s;
-  l = e;
-}
-
-template <int D_, int NK_, int NFD_>
-struct Cfg {
-  static constexpr int D = D_, NK = NK_, NFD = NFD_;
-  static constexpr int NU = D * NK, NI = (D + 1) * NK, NF = 2 * D * NFD, N = NI + NF, NC = NF + 1;
-  static constexpr int NT = 256;
-  // shared memory (floats): Y (D NK NK), P (NK NK; holds M^{-1} until P is
-  // formed), Z (D NK NC), Q (NK NC), each hi + lo -- 71 KB for 3D k=2, three
-  // CTAs per SM
-  static constexpr size_t smem_floats = 2 * ((size_t)D * NK * NK + NK * NK + (size_t)D * NK * NC + NK * NC);
-  static constexpr size_t smem_bytes = smem_floats * 4 + 64 * 4;
-};
-
-// A entry (row r, column c) of cell matrix in column-major n x n (hi, lo)
-#define AH(r, c) __ldg(Ah + (size_t)(r) + (size_t)N * (c))
-#define AL(r, c) __ldg(Al + (size_t)(r) + (size_t)N * (c))
 
 template <class C>
 __global__ void __launch_bounds__(C::NT, 3)
@@ -102,229 +30,16 @@ __global__ void __launch_bounds__(C::NT, 3)
                             const float *__restrict__ Minv_h, const float *__restrict__ Minv_l,
                             const double *__restrict__ inv_m, double *S, double *g, float *Xhi, float *Xlo,
                             int *info) {
-  constexpr int D = C::D, NK = C::NK, NU = C::NU, NI = C::NI, NF = C::NF, N = C::N, NC = C::NC, NT = C::NT;
+  constexpr int N = C::N, NF = C::NF, NI = C::NI, NC = C::NC;
   extern __shared__ float smem[];
-  float *Yh = smem, *Yl = Yh + D * NK * NK;       // [d][a][b]
-  float *Ph = Yl + D * NK * NK, *Pl = Ph + NK * NK;  // [a][b]
-  float *Zh = Pl + NK * NK, *Zl = Zh + D * NK * NC;  // [d][a][c]
-  float *Qh = Zl + D * NK * NC, *Ql = Qh + NK * NC;  // [a][c]
-  const float *Mh = Ph, *Ml = Pl;                      // M^{-1} [a][k], until P is formed
-  int *sflag = reinterpret_cast<int *>(Ql + NK * NC);  // [0] pivot row, [1] info
-  const int t = threadIdx.x;
-  // Threads run fastest over the row index of each output, so the
-  // column-major A entries they read are broadcast (one column entry per
-  // warp) or contiguous (consecutive rows of one column).
-  for (int cell = blockIdx.x; cell < ncells; cell += gridDim.x) {
-    const float *Ah = Ahi + (size_t)cell * N * N, *Al = Alo + (size_t)cell * N * N;
-    const float *bh = bhi + (size_t)cell * N, *bl = blo + (size_t)cell * N;
-    float imh, iml;  // 1/m as float-float
-    {
-      const double v = inv_m[cell];
-      imh = (float)v;
-      iml = (float)(v - (double)imh);
-    }
-    // Y_d = (1/m) M^{-1} G_d  and  Z_d = (1/m) M^{-1} R_{u_d}
-    for (int e = t; e < NK * NK; e += NT) {
-      Ph[e] = __ldg(Minv_h + e);
-      Pl[e] = __ldg(Minv_l + e);
-    }
-    __syncthreads();
-    for (int o = t; o < D * NK * (NK + NC); o += NT) {
-      const int a = o % NK, rest = o / NK;
-      const int c = rest % (NK + NC), d = rest / (NK + NC);
-      float h = 0.0f, l = 0.0f;
-      if (c < NK) {  // G_d column c (pressure DOF c)
-        for (int k = 0; k < NK; ++k)
-          mac(h, l, Mh[a * NK + k], Ml[a * NK + k], AH(d * NK + k, NU + c), AL(d * NK + k, NU + c));
-      } else {
-        const int cc = c - NK;  // right-hand-side column (skeleton DOF or b)
-        for (int k = 0; k < NK; ++k) {
-          const float rh = cc < NF ? AH(d * NK + k, NI + cc) : bh[d * NK + k];
-          const float rl = cc < NF ? AL(d * NK + k, NI + cc) : bl[d * NK + k];
-          mac(h, l, Mh[a * NK + k], Ml[a * NK + k], rh, rl);
-        }
-      }
-      float ph, pl;
-      normalise(h, l);
-      mul(h, l, imh, iml, ph, pl);
-      if (c < NK) {
-        Yh[(d * NK + a) * NK + c] = ph;
-        Yl[(d * NK + a) * NK + c] = pl;
-      } else {
-        Zh[(d * NK + a) * NC + (c - NK)] = ph;
-        Zl[(d * NK + a) * NC + (c - NK)] = pl;
-      }
-    }
-    __syncthreads();
-    // P = T - sum_d G'_d Y_d ;  Q = R_p - sum_d G'_d Z_d
-    for (int o = t; o < NK * (NK + NC); o += NT) {
-      const int a = o % NK, c = o / NK;
-      float h = 0.0f, l = 0.0f;
-      if (c < NK) {
-        for (int d = 0; d < D; ++d)
-          for (int k = 0; k < NK; ++k)
-            mac(h, l, AH(NU + a, d * NK + k), AL(NU + a, d * NK + k), Yh[(d * NK + k) * NK + c],
-                Yl[(d * NK + k) * NK + c]);
-        float rh, rl;
-        sub(AH(NU + a, NU + c), AL(NU + a, NU + c), h, l, rh, rl);
-        Ph[a * NK + c] = rh;
-        Pl[a * NK + c] = rl;
-      } else {
-        const int cc = c - NK;
-        for (int d = 0; d < D; ++d)
-          for (int k = 0; k < NK; ++k)
-            mac(h, l, AH(NU + a, d * NK + k), AL(NU + a, d * NK + k), Zh[(d * NK + k) * NC + cc],
-                Zl[(d * NK + k) * NC + cc]);
-        const float rh0 = cc < NF ? AH(NU + a, NI + cc) : bh[NU + a];
-        const float rl0 = cc < NF ? AL(NU + a, NI + cc) : bl[NU + a];
-        float rh, rl;
-        sub(rh0, rl0, h, l, rh, rl);
-        Qh[a * NC + cc] = rh;
-        Ql[a * NC + cc] = rl;
-      }
-    }
-    if (t == 0) sflag[1] = 0;
-    __syncthreads();
-    // LU with partial pivoting of [P | Q] (pivot search by warp 0), then X_p = U^{-1} Q
-    for (int j = 0; j < NK; ++j) {
-      if (t < 32) {
-        float best = -1.0f;
-        int bi = j;
-        for (int i = j + t; i < NK; i += 32) {
-          const float v = fabsf(Ph[i * NK + j]);
-          if (v > best) {
-            best = v;
-            bi = i;
-          }
-        }
-        for (int off = 16; off > 0; off >>= 1) {
-          const float ob = __shfl_down_sync(0xffffffffu, best, off);
-          const int oi = __shfl_down_sync(0xffffffffu, bi, off);
-          if (ob > best || (ob == best && oi < bi)) {
-            best = ob;
-            bi = oi;
-          }
-        }
-        if (t == 0) {
-          sflag[0] = bi;
-          if (best == 0.0f && sflag[1] == 0) sflag[1] = j + 1;
-        }
-      }
-      __syncthreads();
-      const int p = sflag[0];
-      if (p != j) {
-        for (int c = t; c < NK + NC; c += NT) {
-          float *rh = c < NK ? Ph : Qh, *rl = c < NK ? Pl : Ql;
-          const int ld = c < NK ? NK : NC, cc = c < NK ? c : c - NK;
-          float th = rh[j * ld + cc], tl = rl[j * ld + cc];
-          rh[j * ld + cc] = rh[p * ld + cc];
-          rl[j * ld + cc] = rl[p * ld + cc];
-          rh[p * ld + cc] = th;
-          rl[p * ld + cc] = tl;
-        }
-      }
-      __syncthreads();
-      const float pvh = Ph[j * NK + j], pvl = Pl[j * NK + j];
-      const int rows = NK - j - 1, cols = NK - j - 1 + NC;
-      // multipliers (column j below the diagonal)
-      for (int i = j + 1 + t; i < NK; i += NT) {
-        if (pvh != 0.0f) {
-          float qh, ql;
-          div(Ph[i * NK + j], Pl[i * NK + j], pvh, pvl, qh, ql);
-          Ph[i * NK + j] = qh;
-          Pl[i * NK + j] = ql;
-        }
-      }
-      __syncthreads();
-      for (int e = t; e < rows * cols; e += NT) {
-        const int i = j + 1 + e / cols, c = e % cols;
-        const float lh = Ph[i * NK + j], ll = Pl[i * NK + j];
-        float uh, ul, *th, *tl;
-        if (c < NK - j - 1) {
-          const int cc = j + 1 + c;
-          uh = Ph[j * NK + cc];
-          ul = Pl[j * NK + cc];
-          th = Ph + i * NK + cc;
-          tl = Pl + i * NK + cc;
-        } else {
-          const int cc = c - (NK - j - 1);
-          uh = Qh[j * NC + cc];
-          ul = Ql[j * NC + cc];
-          th = Qh + i * NC + cc;
-          tl = Ql + i * NC + cc;
-        }
-        float ph, pl, rh, rl;
-        mul(lh, ll, uh, ul, ph, pl);
-        sub(*th, *tl, ph, pl, rh, rl);
-        *th = rh;
-        *tl = rl;
-      }
-      __syncthreads();
-    }
-    for (int j = NK - 1; j >= 0; --j) {  // back substitution on Q (NC columns)
-      const float pvh = Ph[j * NK + j], pvl = Pl[j * NK + j];
-      for (int c = t; c < NC; c += NT) {
-        float qh = 0.0f, ql = 0.0f;
-        if (pvh != 0.0f) div(Qh[j * NC + c], Ql[j * NC + c], pvh, pvl, qh, ql);
-        Qh[j * NC + c] = qh;
-        Ql[j * NC + c] = ql;
-      }
-      __syncthreads();
-      for (int e = t; e < j * NC; e += NT) {
-        const int i = e / NC, c = e % NC;
-        float ph, pl, rh, rl;
-        mul(Ph[i * NK + j], Pl[i * NK + j], Qh[j * NC + c], Ql[j * NC + c], ph, pl);
-        sub(Qh[i * NC + c], Ql[i * NC + c], ph, pl, rh, rl);
-        Qh[i * NC + c] = rh;
-        Ql[i * NC + c] = rl;
-      }
-      __syncthreads();
-    }
-    // X_{u_d} = Z_d - Y_d X_p (in place in Z)
-    for (int o = t; o < D * NK * NC; o += NT) {
-      const int d = o / (NK * NC), rem = o - d * NK * NC, a = rem / NC, c = rem - a * NC;
-      float h = 0.0f, l = 0.0f;
-      for (int k = 0; k < NK; ++k)
-        mac(h, l, Yh[(d * NK + a) * NK + k], Yl[(d * NK + a) * NK + k], Qh[k * NC + c], Ql[k * NC + c]);
-      float rh, rl;
-      sub(Zh[(d * NK + a) * NC + c], Zl[(d * NK + a) * NC + c], h, l, rh, rl);
-      Zh[(d * NK + a) * NC + c] = rh;
-      Zl[(d * NK + a) * NC + c] = rl;
-    }
-    __syncthreads();
-    // S = A_ff - A_fi X, g = b_f - A_fi y
-    for (int o = t; o < NF * NC; o += NT) {
-      const int f = o % NF, c = o / NF;
-      float h = 0.0f, l = 0.0f;
-      for (int k = 0; k < NU; ++k)
-        mac(h, l, AH(NI + f, k), AL(NI + f, k), Zh[k * NC + c], Zl[k * NC + c]);
-      for (int k = 0; k < NK; ++k)
-        mac(h, l, AH(NI + f, NU + k), AL(NI + f, NU + k), Qh[k * NC + c], Ql[k * NC + c]);
-      const double rhs = c < NF ? (double)AH(NI + f, NI + c) + (double)AL(NI + f, NI + c)
-                                : (double)bh[NI + f] + (double)bl[NI + f];
-      const double v = rhs - ((double)h + (double)l);
-      if (c < NF)
-        S[(size_t)cell * NF * NF + f + (size_t)NF * c] = v;
-      else
-        g[(size_t)cell * NF + f] = v;
-    }
-    // X = [X_u; X_p] (ni x nc, column-major) as float-float pairs for the recovery
-    if (Xhi) {
-      float *xh = Xhi + (size_t)cell * NI * NC, *xl = Xlo + (size_t)cell * NI * NC;
-      for (int e = t; e < NI * NC; e += NT) {
-        const int c = e / NI, m = e - c * NI;
-        const bool u = m < NU;
-        xh[e] = u ? Zh[m * NC + c] : Qh[(m - NU) * NC + c];
-        xl[e] = u ? Zl[m * NC + c] : Ql[(m - NU) * NC + c];
-      }
-    }
-    if (t == 0 && info) info[cell] = sflag[1];
-    __syncthreads();
-  }
+  for (int cell = blockIdx.x; cell < ncells; cell += gridDim.x)
+    ffblock_cell<C, C::NT, true>(true, Ahi + (size_t)cell * N * N, Alo + (size_t)cell * N * N, bhi + (size_t)cell * N,
+                                 blo + (size_t)cell * N, Minv_h, Minv_l, inv_m[cell], smem, S + (size_t)cell * NF * NF,
+                                 g + (size_t)cell * NF, Xhi ? Xhi + (size_t)cell * NI * NC : nullptr,
+                                 Xlo ? Xlo + (size_t)cell * NI * NC : nullptr, info ? info + cell : nullptr,
+                                 threadIdx.x);
 }
 
-#undef AH
-#undef AL
 
 template <class C>
 static cudaError_t launch_cfg(int ncells, const float *Ahi, const float *Alo, const float *bhi, const float *blo,
@@ -376,19 +91,8 @@ cudaError_t launch_condense_ffblock(int D, int k, int ncells, const float *Ahi, 
 
 // 1/m = kappa / |det J| per cell, in FP64 (a handful of FP64 operations per cell)
 __global__ void inv_mass_scale_kernel(CellArgs a, double *inv_m) {
-  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < a.ncells; c += gridDim.x * blockDim.x) {
-    const int D = a.D;
-    const double *J = a.jac + (size_t)c * D * D;
-    double det;
-    if (D == 2) {
-      det = J[0] * J[3] - J[2] * J[1];
-    } else {
-      det = J[0] * (J[4] * J[8] - J[7] * J[5]) - J[3] * (J[1] * J[8] - J[7] * J[2]) +
-            J[6] * (J[1] * J[5] - J[4] * J[2]);
-    }
-    const double kap = a.kappa ? a.kappa[c] : 1.0;
-    inv_m[c] = kap / fabs(det);
-  }
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < a.ncells; c += gridDim.x * blockDim.x)
+    inv_m[c] = cell_inv_mass(a, c);
 }
 
 cudaError_t launch_inv_mass_scale(const CellArgs &a, double *inv_m, cudaStream_t s, long long *launches) {

@@ -74,6 +74,12 @@ SIGNATURES = {
     "hdg_time_kernel": (_i, [_vp, _i, _i, _vp]),
     "hdg_problem_device_bytes": (_i, [_vp, _vp]),
     "hdg_footprint": (_i, [_i, _i, _i, _i, _i, _vp]),
+    "hdg_batch_create": (_i, [_vp, _i, _vp, ctypes.POINTER(_vp)]),
+    "hdg_batch_destroy": (_i, [_vp]),
+    "hdg_batch_assemble": (_i, [_vp, _i, _vp]),
+    "hdg_batch_solve": (_i, [_vp, _i, _d, _i, _vp, _vp]),
+    "hdg_batch_timings": (_i, [_vp, _vp]),
+    "hdg_batch_tuning": (_i, [_vp, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp]),
     "hdg_server_create": (_i, [_i, _i, _d, ctypes.POINTER(_vp)]),
     "hdg_server_destroy": (_i, [_vp]),
     "hdg_server_submit": (_i, [_vp, _vp, _vp]),

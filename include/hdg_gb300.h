@@ -240,6 +240,40 @@ int hdg_time_kernel(hdg_problem *pb, int which, int reps, double *ms_per_launch)
 int hdg_problem_device_bytes(const hdg_problem *pb, double *bytes);
 
 /* ------------------------------------------------------------------------
+ * Size-class batching (no reference counterpart: the reference assembles one
+ * problem per HybridAffineFEOperator).  The problems of a batch share one
+ * context and are grouped by (D, k); each class is integrated and condensed
+ * by ONE persistent fused launch over the cells of all its problems, the cell
+ * blocks staying on chip (FP64: in shared memory) or in L2 (float-float block
+ * elimination), and the condensed blocks are then assembled into each
+ * problem's skeleton system.  The first assemble of a class times the tile
+ * choices (threads per cell = 32, 64, 128, 256, i.e. 8..1 cells per CTA) and
+ * keeps the fastest; the whole launch sequence is captured in a CUDA graph
+ * and replayed while the problems' buffers stay put.  After
+ * hdg_batch_assemble every problem is assembled exactly as hdg_assemble would
+ * leave it (same state, same values), so hdg_solve_skeleton / hdg_recover /
+ * hdg_get_* work per problem.
+ * ------------------------------------------------------------------------ */
+typedef struct hdg_batch hdg_batch;
+int hdg_batch_create(hdg_context *ctx, int nproblems, hdg_problem *const *problems,
+                     hdg_batch **out);
+int hdg_batch_destroy(hdg_batch *b);
+/* precision: HDG_PREC_FP64 or HDG_PREC_FF_BLOCK.  bad (may be NULL, nproblems
+ * values, batch order) receives each problem's first zero pivot (0 = ok). */
+int hdg_batch_assemble(hdg_batch *b, int precision, int *bad);
+/* Skeleton solve + recovery of every problem; iters/relres may be NULL. */
+int hdg_batch_solve(hdg_batch *b, int solver, double rtol, int maxit, int *iters,
+                    double *relres);
+/* ms of the last calls: [fused integrate+condense (all classes),
+ * skeleton assembly (all problems), solve + recover (all problems)]. */
+int hdg_batch_timings(const hdg_batch *b, double *ms);
+/* The tuned tile per class for a precision: D, k, threads per cell, the
+ * fused launch's ms at tuning time and the class's cells (arrays of
+ * max_classes); nclasses receives the number of classes. */
+int hdg_batch_tuning(const hdg_batch *b, int precision, int max_classes, int *D, int *k,
+                     int *tpc, double *ms, long long *cells, int *nclasses);
+
+/* ------------------------------------------------------------------------
  * Serving (no reference counterpart: the reference solves one problem per
  * `solve(op)` call).  A server owns `slots` worker threads; each runs one
  * request at a time on its own stream, so admitted requests overlap on the

@@ -53,3 +53,12 @@ def test_footprint_rejects_bad_shapes():
     assert lib.hdg_footprint(4, 8, 1, 0, 0, ctypes.byref(b)) == _lib.HDG_ERR_INVALID
     assert lib.hdg_footprint(2, 0, 1, 0, 0, ctypes.byref(b)) == _lib.HDG_ERR_INVALID
     assert lib.hdg_footprint(2, 8, 5, 0, 0, ctypes.byref(b)) == _lib.HDG_ERR_INVALID
+
+
+def test_batching_workload_is_seeded():
+    from gridaphybrid_gb300.batching import batching_workload
+    a, b = batching_workload(seed=4), batching_workload(seed=4)
+    assert len(a) == 64
+    assert all(x["n"] == y["n"] and x["k"] == y["k"] and np.array_equal(x["kappa"], y["kappa"]) for x, y in zip(a, b))
+    assert {x["k"] for x in a} == {1, 2, 3} and all(16 <= x["n"] <= 128 for x in a)
+    assert abs(np.log(a[0]["kappa"]).std() - 1.5) < 0.3
