@@ -879,25 +879,38 @@ static int solve_pcg_refined(hdg_problem *pb, double rtol, int maxit, int *it_ou
   double rr = ho[1];
   int total = 0, outer = 0;
   int status = HDG_OK;
+  int base = 0;         // iterations counted before the last init (SC_ITERS restarts there)
+  int cycle_start = 0;  // iterations counted when the graph last started from ia.p
+  bool restart = true;  // next cycle starts a fresh Krylov space
   while (cc > 0.0 && rr > rtol * rtol * cc) {
-    if (total >= maxit || outer >= 30) {
+    if (total >= maxit || outer >= 60) {
       status = ctx->fail(HDG_ERR_NOT_CONVERGED, "refined PCG: relative residual %.3e after %d iterations",
                          std::sqrt(rr / cc), total);
       break;
     }
-    // ask the inner solve for the reduction still missing (FP32 cannot go much below 1e-5)
-    const double eta = std::max(1e-5, 0.3 * rtol * std::sqrt(cc / rr));
-    CUDA_TRY(ctx, launch_pcg32_init(ia, eta, ctx->stream, &ctx->launches));
-    int inner = 0;
+    // the reduction the inner solve is asked for before the next FP64
+    // residual: refine_delta, or just what is still missing at the end
+    const double eta = std::max(pb->refine_delta, 0.3 * rtol * std::sqrt(cc / rr));
+    const double rr_before = rr;
+    if (restart || !pb->refine_keep) {
+      CUDA_TRY(ctx, launch_pcg32_init(ia, eta, ctx->stream, &ctx->launches));
+      base = total;
+    } else {
+      // the graph's first SpMV reads p_old from ia.p; after an odd number of
+      // iterations since it last started, the current p is in ia.p2
+      if ((total - cycle_start) & 1)
+        CUDA_TRY(ctx, cudaMemcpyAsync(ia.p, ia.p2, sizeof(float) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+      CUDA_TRY(ctx, launch_pcg32_replace(ia, eta, ctx->stream, &ctx->launches));
+    }
+    cycle_start = total;
     for (;;) {
       CUDA_TRY(ctx, cudaGraphLaunch(pb->pcg32_graph, ctx->stream));
       ctx->launches += 4LL * pairs;
       CUDA_TRY(ctx, cudaMemcpyAsync(h, ia.scal, sizeof(double) * 16, cudaMemcpyDeviceToHost, ctx->stream));
       CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-      inner = (int)h[8];
-      if (h[7] != 0.0 || total + inner >= maxit || !std::isfinite(h[4])) break;
+      total = base + (int)h[8];
+      if (h[7] != 0.0 || total >= maxit || !std::isfinite(h[4])) break;
     }
-    total += inner;
     ++outer;
     CUDA_TRY(ctx, launch_outer_update(oa, ia.x, ctx->stream, &ctx->launches));
     CUDA_TRY(ctx, cudaMemcpyAsync(ho, oa.scal, sizeof(double) * 2, cudaMemcpyDeviceToHost, ctx->stream));
@@ -907,6 +920,9 @@ static int solve_pcg_refined(hdg_problem *pb, double rtol, int maxit, int *it_ou
       status = ctx->fail(HDG_ERR_NOT_CONVERGED, "refined PCG breakdown (non-finite residual)");
       break;
     }
+    // a kept direction that no longer cuts the true residual (the FP32
+    // recurrence drifted) is dropped: the next cycle restarts
+    restart = rr > 0.0625 * rr_before;
   }
   {
     unsigned int herr = 0;
@@ -1133,6 +1149,14 @@ int hdg_problem_device_bytes(const hdg_problem *pb, double *bytes) {
   double s = 0.0;
   for (const DBuf *b : const_cast<hdg_problem *>(pb)->device_buffers()) s += (double)b->bytes;
   *bytes = s;
+  return HDG_OK;
+}
+
+int hdg_set_refinement(hdg_problem *pb, double delta, int keep_direction) {
+  if (!pb) return HDG_ERR_INVALID;
+  if (!(delta >= 1e-8 && delta < 1.0)) return pb->ctx->fail(HDG_ERR_INVALID, "delta must lie in [1e-8, 1)");
+  pb->refine_delta = delta;
+  pb->refine_keep = keep_direction ? 1 : 0;
   return HDG_OK;
 }
 

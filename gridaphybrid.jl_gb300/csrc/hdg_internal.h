@@ -199,6 +199,10 @@ struct hdg_problem {
   hdg::DBuf d_minv, d_invm;
   cudaGraphExec_t pcg32_graph = nullptr;
   int cellop_nstage = 0, cellop_ctas = 0;  // streaming-kernel pipeline depth and grid
+  // FP64 residual refinement of the FP32 skeleton solve: the inner reduction
+  // between FP64 residuals, and whether the search direction survives them
+  double refine_delta = 3e-2;
+  int refine_keep = 1;
   int last_outer = 0;
   hdg::DBuf d_uint, d_errs;
   hdg::DBuf h_pinned;  // host staging

@@ -204,6 +204,8 @@ cudaError_t launch_binv_to_f32(size_t count, const double *Binv, float *Binv32, 
                                long long *launches);
 cudaError_t launch_pcg32_init(const Pcg32Args &a, double eta, cudaStream_t s, long long *launches);
 cudaError_t launch_pcg32_iteration_pair(const Pcg32Args &a, cudaStream_t s, long long *launches);
+// residual replacement keeping the search direction (reliable update)
+cudaError_t launch_pcg32_replace(const Pcg32Args &a, double eta, cudaStream_t s, long long *launches);
 // one unassembled SpMV (+ its dot product) as launched inside the inner PCG
 cudaError_t launch_pcg32_spmv(const Pcg32Args &a, cudaStream_t s, long long *launches);
 cudaError_t launch_outer_init(const OuterArgs &a, cudaStream_t s, long long *launches);

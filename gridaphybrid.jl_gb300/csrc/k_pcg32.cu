@@ -85,6 +85,53 @@ __global__ void __launch_bounds__(kPcgThreads) pcg32_init_kernel(Pcg32Args a, do
   }
 }
 
+// reliable update: the inner residual is replaced by the FP64 outer residual
+// (x = 0 again: the correction so far went into the FP64 iterate) and the
+// search direction p is kept, so the Krylov space is not thrown away:
+// z = Binv r, beta = (r,z)_new / (r,z) of the iteration before, and the next
+// SpMV forms p = z + beta p as in any other iteration.
+__global__ void __launch_bounds__(kPcgThreads) pcg32_replace_kernel(Pcg32Args a, double eta) {
+  __shared__ float rs[kPcgThreads];
+  __shared__ double red[32];
+  const int tile = (kPcgThreads / a.nfd) * a.nfd;
+  double rz = 0.0, rr = 0.0;
+  for (int base = blockIdx.x * tile; base < a.n; base += gridDim.x * tile) {
+    const int row = base + (int)threadIdx.x;
+    const bool act = threadIdx.x < (unsigned)tile && row < a.n;
+    float r = 0.0f;
+    if (act) {
+      r = (float)a.rhs[row];
+      a.x[row] = 0.0f;
+      a.r[row] = r;
+      rr += (double)r * r;
+    }
+    const float z = apply_binv32(a, act ? row : a.n, r, rs);
+    if (act) {
+      a.z[row] = z;
+      rz += (double)r * z;
+    }
+  }
+  double s = block_sum(rz, red);
+  if (threadIdx.x == 0) a.partials[blockIdx.x] = s;
+  s = block_sum(rr, red);
+  if (threadIdx.x == 0) a.partials[a.nparts + blockIdx.x] = s;
+  if (last_cta(a.counter)) {
+    const double vrz = sum_partials(a.partials, a.nparts, 0, red);
+    const double vrr = sum_partials(a.partials, a.nparts, 1, red);
+    if (threadIdx.x == 0) {
+      // the update that ended the cycle stored beta = (r,z)_N / (r,z)_{N-1}
+      // and (r,z)_N; with r_N replaced, beta = (r,z)_new / (r,z)_{N-1}
+      const double old = a.scal[SC_RZ];
+      a.scal[SC_BETA] = old != 0.0 ? a.scal[SC_BETA] * (vrz / old) : 0.0;
+      a.scal[SC_RZ] = vrz;
+      a.scal[SC_RR] = vrr;
+      a.scal[SC_TOL2] = eta * eta * vrr;
+      a.scal[SC_DONE] = (vrr == 0.0) ? 1.0 : 0.0;
+      *a.counter = 0u;
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // The unassembled FP32 operator.
 //
@@ -409,6 +456,12 @@ cudaError_t launch_binv_to_f32(size_t count, const double *Binv, float *Binv32, 
 
 cudaError_t launch_pcg32_init(const Pcg32Args &a, double eta, cudaStream_t s, long long *launches) {
   pcg32_init_kernel<<<a.nparts, kPcgThreads, 0, s>>>(a, eta);
+  ++*launches;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pcg32_replace(const Pcg32Args &a, double eta, cudaStream_t s, long long *launches) {
+  pcg32_replace_kernel<<<a.nparts, kPcgThreads, 0, s>>>(a, eta);
   ++*launches;
   return cudaGetLastError();
 }

@@ -73,6 +73,7 @@ SIGNATURES = {
     "hdg_get_timings": (_i, [_vp, _vp]),
     "hdg_time_kernel": (_i, [_vp, _i, _i, _vp]),
     "hdg_problem_device_bytes": (_i, [_vp, _vp]),
+    "hdg_set_refinement": (_i, [_vp, _d, _i]),
     "hdg_footprint": (_i, [_i, _i, _i, _i, _i, _vp]),
     "hdg_batch_create": (_i, [_vp, _i, _vp, ctypes.POINTER(_vp)]),
     "hdg_batch_destroy": (_i, [_vp]),

@@ -198,6 +198,14 @@ int hdg_get_skeleton_system(hdg_problem *pb, long long *rowptr, int *colind,
 int hdg_solve_skeleton(hdg_problem *pb, int solver, double rtol, int maxit,
                        int *iters, double *relres);
 
+/* Options of the fast precisions' skeleton solve (an FP32 PCG inside FP64
+ * residual refinement; no reference counterpart).  delta: the relative
+ * residual reduction the FP32 iterations make between two FP64 residuals
+ * (default 3e-2); keep_direction: 1 (default) replaces the FP32 residual by
+ * the FP64 one and keeps the search direction (reliable updates), 0 restarts
+ * the FP32 PCG at every FP64 residual. */
+int hdg_set_refinement(hdg_problem *pb, double delta, int keep_direction);
+
 /* Interior recovery _compute_hybridizable_from_skeleton_free_dof_values
  * (src/HybridAffineFEOperators.jl:102-150) with the stored factors. */
 int hdg_recover(hdg_problem *pb);
