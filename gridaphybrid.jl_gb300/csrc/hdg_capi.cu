@@ -136,7 +136,7 @@ cudaError_t run_integrate(hdg_problem *pb) {
                                  &ctx->launches);
   float *Ahi = pb->d_A.as<float>(), *bhi = pb->d_b.as<float>();
   return launch_integrate_mixed(a, mixed_tables(pb), Ahi, Ahi + nc * n * n, bhi, bhi + nc * n, ctx->stream,
-                                ctx->num_sms, &ctx->launches);
+                                ctx->num_sms, &ctx->launches, pb->precision == HDG_PREC_FF_BLOCK);
 }
 
 cudaError_t run_condense(hdg_problem *pb) {
@@ -162,15 +162,21 @@ cudaError_t run_condense(hdg_problem *pb) {
                                pb->d_info.as<int>(), ctx->stream, ctx->num_sms, &ctx->launches);
 }
 
+// The Dirichlet data the lift and the recovery use: the problem's values, or
+// zeros while the Newton path solves for a correction.
+const double *dirichlet_values(const hdg_problem *pb) {
+  return pb->zero_dirichlet ? pb->d_dirzero.as<double>() : pb->d_dirvals.as<double>();
+}
+
 cudaError_t run_recover(hdg_problem *pb) {
   hdg_context *ctx = pb->ctx;
   CellArgs a = cell_args(pb);
   const size_t nc = pb->mesh.ncells, ni = pb->tab.ni, nf = pb->tab.nf;
   if (pb->precision == HDG_PREC_FP64)
-    return launch_recover_fp64(a, pb->d_fact.as<double>(), pb->d_x.as<double>(), pb->d_dirvals.as<double>(),
+    return launch_recover_fp64(a, pb->d_fact.as<double>(), pb->d_x.as<double>(), dirichlet_values(pb),
                                pb->d_uint.as<double>(), ctx->stream, ctx->num_sms, &ctx->launches);
   const float *Xhi = pb->d_fact.as<float>();
-  return launch_recover_mixed(a, Xhi, Xhi + nc * ni * (nf + 1), pb->d_x.as<double>(), pb->d_dirvals.as<double>(),
+  return launch_recover_mixed(a, Xhi, Xhi + nc * ni * (nf + 1), pb->d_x.as<double>(), dirichlet_values(pb),
                               pb->d_uint.as<double>(), ctx->stream, ctx->num_sms, &ctx->launches);
 }
 
@@ -192,7 +198,7 @@ AssembleArgs assemble_args(hdg_problem *pb) {
   as.ndir_cells = (int)pb->pat.dir_cells.size();
   as.cell_facets = pb->d_cell_facets.as<int>();
   as.facet_dofs = pb->d_facet_dofs.as<int>();
-  as.dirvals = pb->d_dirvals.as<double>();
+  as.dirvals = dirichlet_values(pb);
   return as;
 }
 
@@ -1142,6 +1148,93 @@ int hdg_solve(hdg_problem *pb, int precision, int solver, double rtol, int maxit
     stats[6] = pb->timings[0] + pb->timings[1] + pb->timings[2] + pb->timings[3] + pb->timings[4];
   }
   return HDG_OK;
+}
+
+int hdg_newton_solve(hdg_problem *pb, int solver, double lin_rtol, int lin_maxit, double ftol, int max_iters,
+                     const double *x0, double *res_norms, int *iters) {
+  if (!pb) return HDG_ERR_INVALID;
+  hdg_context *ctx = pb->ctx;
+  if (!pb->form_set) return ctx->fail(HDG_ERR_STATE, "set the weak form first (hdg_set_darcy)");
+  if (!(ftol > 0.0) || max_iters < 0) return ctx->fail(HDG_ERR_INVALID, "ftol must be > 0 and max_iters >= 0");
+  cudaSetDevice(ctx->device);
+  int rc = assemble_prepare(pb, HDG_PREC_FP64, true);
+  if (rc) return rc;
+  const size_t nc = pb->mesh.ncells, ni = pb->tab.ni, nk = pb->tab.nk, D = pb->tab.D;
+  const size_t nfree = pb->mesh.nfree, nint = nc * ni, ndir = pb->mesh.ndir;
+  CUDA_TRY(ctx, pb->d_newton.reserve(sizeof(double) * (nint + nfree + 1)));
+  CUDA_TRY(ctx, pb->d_rmax.reserve(sizeof(double) * 2));
+  CUDA_TRY(ctx, pb->d_dirzero.reserve(sizeof(double) * (ndir ? ndir : 1)));
+  CUDA_TRY(ctx, cudaMemsetAsync(pb->d_dirzero.ptr, 0, sizeof(double) * (ndir ? ndir : 1), ctx->stream));
+  CUDA_TRY(ctx, pb->d_uint.reserve(sizeof(double) * nint));
+  CUDA_TRY(ctx, pb->d_x.reserve(sizeof(double) * (nfree ? nfree : 1)));
+  double *xint = pb->d_newton.as<double>(), *xskel = xint + nint;
+  if (x0) {
+    // Gridap layout [flux of all cells | pressure of all cells | free skeleton] -> cell-major
+    CUDA_TRY(ctx, cudaMemcpy2DAsync(xint, ni * sizeof(double), x0, D * nk * sizeof(double), D * nk * sizeof(double),
+                                    nc, cudaMemcpyDefault, ctx->stream));
+    CUDA_TRY(ctx, cudaMemcpy2DAsync(xint + D * nk, ni * sizeof(double), x0 + nc * D * nk, nk * sizeof(double),
+                                    nk * sizeof(double), nc, cudaMemcpyDefault, ctx->stream));
+    if (nfree)
+      CUDA_TRY(ctx, cudaMemcpyAsync(xskel, x0 + nint, sizeof(double) * nfree, cudaMemcpyDefault, ctx->stream));
+  } else {
+    CUDA_TRY(ctx, cudaMemsetAsync(xint, 0, sizeof(double) * (nint + nfree), ctx->stream));
+  }
+  CellArgs a = cell_args(pb);
+  int it = 0;
+  int status = HDG_OK;
+  double hr[2];
+  for (;; ++it) {
+    // Jacobian (the cell matrices) and residual r_c = A_c x_c - b_c
+    CUDA_TRY(ctx, run_integrate(pb));
+    AssembleArgs as = assemble_args(pb);
+    CUDA_TRY(ctx, launch_newton_residual(a, as, pb->d_A.as<double>(), pb->d_b.as<double>(), xint, xskel,
+                                         pb->d_dirvals.as<double>(), pb->d_rmax.as<double>(), ctx->stream,
+                                         ctx->num_sms, &ctx->launches));
+    CUDA_TRY(ctx, cudaMemcpyAsync(hr, pb->d_rmax.ptr, sizeof(hr), cudaMemcpyDeviceToHost, ctx->stream));
+    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    const double norm = std::max(hr[0], hr[1]);
+    if (res_norms) res_norms[it] = norm;
+    if (!std::isfinite(norm)) {
+      status = ctx->fail(HDG_ERR_NOT_CONVERGED, "Newton: non-finite residual");
+      break;
+    }
+    if (norm <= ftol) break;
+    if (it == max_iters) {
+      status = ctx->fail(HDG_ERR_NOT_CONVERGED, "Newton: residual %.3e after %d iterations", norm, it);
+      break;
+    }
+    // the hybridized linear solve of J dx = r with zero Dirichlet data
+    // (src/HybridLinearSolvers.jl:22-59)
+    CUDA_TRY(ctx, run_condense(pb));
+    pb->zero_dirichlet = true;
+    cudaError_t e = assemble_skeleton(pb);
+    pb->zero_dirichlet = false;
+    CUDA_TRY(ctx, e);
+    pb->assembled = true;
+    int lit = 0;
+    double lrel = 0.0;
+    pb->zero_dirichlet = true;
+    rc = hdg_solve_skeleton(pb, solver, lin_rtol, lin_maxit, &lit, &lrel);
+    if (rc == HDG_OK) rc = run_recover(pb) == cudaSuccess ? HDG_OK : HDG_ERR_CUDA;
+    pb->zero_dirichlet = false;
+    if (rc) {
+      status = rc == HDG_ERR_CUDA ? ctx->fail(HDG_ERR_CUDA, "Newton: correction recovery failed") : rc;
+      break;
+    }
+    // x <- x - dx
+    CUDA_TRY(ctx, launch_newton_update(nint, xint, pb->d_uint.as<double>(), ctx->stream, ctx->num_sms,
+                                       &ctx->launches));
+    CUDA_TRY(ctx, launch_newton_update(nfree, xskel, pb->d_x.as<double>(), ctx->stream, ctx->num_sms,
+                                       &ctx->launches));
+  }
+  if (iters) *iters = it;
+  // the iterate becomes the problem's solution (free DOF values, L2 errors)
+  CUDA_TRY(ctx, cudaMemcpyAsync(pb->d_uint.ptr, xint, sizeof(double) * nint, cudaMemcpyDeviceToDevice, ctx->stream));
+  if (nfree)
+    CUDA_TRY(ctx, cudaMemcpyAsync(pb->d_x.ptr, xskel, sizeof(double) * nfree, cudaMemcpyDeviceToDevice, ctx->stream));
+  CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  pb->solved = pb->recovered = status == HDG_OK;
+  return status;
 }
 
 int hdg_problem_device_bytes(const hdg_problem *pb, double *bytes) {

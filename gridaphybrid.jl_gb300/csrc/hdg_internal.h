@@ -205,6 +205,10 @@ struct hdg_problem {
   int refine_keep = 1;
   int last_outer = 0;
   hdg::DBuf d_uint, d_errs;
+  // Newton path: the iterate [interior cell-major | free skeleton], the
+  // residual norms, and zero Dirichlet data for the corrections
+  hdg::DBuf d_newton, d_rmax, d_dirzero;
+  bool zero_dirichlet = false;
   hdg::DBuf h_pinned;  // host staging
   cudaGraphExec_t pcg_graph = nullptr;
   int pcg_graph_chunk = 0;
@@ -214,7 +218,8 @@ struct hdg_problem {
             &d_dirvals, &d_A, &d_b, &d_S, &d_g, &d_fact, &d_info, &d_aux, &d_rowptr, &d_colind, &d_val,
             &d_rhs, &d_br_row0, &d_br_src, &d_blk_off, &d_blk_rowlen, &d_blk_src, &d_diag_blk, &d_dir_cells,
             &d_Binv, &d_x, &d_r, &d_z, &d_p, &d_p2, &d_q, &d_partials, &d_scal, &d_counter, &d_cellop,
-            &d_cell_blk, &d_qc, &d_Binv32, &d_v32, &d_scal2, &d_minv, &d_invm, &d_uint, &d_errs};
+            &d_cell_blk, &d_qc, &d_Binv32, &d_v32, &d_scal2, &d_minv, &d_invm, &d_uint, &d_errs,
+            &d_newton, &d_rmax, &d_dirzero};
   }
   ~hdg_problem();
 };

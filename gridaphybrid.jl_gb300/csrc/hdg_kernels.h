@@ -92,9 +92,10 @@ struct MixedTables {
   const float *Mh, *Ml, *Gh, *Gl, *Fh, *Fl, *Hh, *Hl, *Lh, *Ll;
 };
 // Mixed precision: float-float integration -> (A_hi, A_lo), (b_hi, b_lo)
+// skip_uu: leave the flux-flux block unwritten (block elimination does not read it)
 cudaError_t launch_integrate_mixed(const CellArgs &a, const MixedTables &T, float *Ahi, float *Alo,
                                    float *bhi, float *blo, cudaStream_t s, int num_sms,
-                                   long long *launches);
+                                   long long *launches, bool skip_uu = false);
 cudaError_t launch_split_fp64(size_t count, const double *x, float *hi, float *lo, cudaStream_t s,
                               int num_sms, long long *launches);
 // FP32 LU + one float-float refinement step; Xhi/Xlo (ncells x ni x (nf+1)) may be null
@@ -239,6 +240,15 @@ struct FusedLaunch {
 };
 bool fused_batch_supported(int D, int k, int precision);
 cudaError_t launch_fused_batch(const FusedLaunch &L, cudaStream_t s, long long *launches);
+
+// Newton path: b_c <- A_c x_c - b_c for the iterate (interior values cell-major,
+// free skeleton values), rmax[0] / rmax[1] = max |r| over interior rows / the
+// assembled free skeleton rows; and x <- x - dx.
+cudaError_t launch_newton_residual(const CellArgs &a, const AssembleArgs &as, const double *A, double *b,
+                                   const double *xint, const double *xskel, const double *dirvals, double *rmax,
+                                   cudaStream_t s, int num_sms, long long *launches);
+cudaError_t launch_newton_update(size_t count, double *x, const double *dx, cudaStream_t s, int num_sms,
+                                 long long *launches);
 
 // dense LU solve of a CSR system (small n), one CTA
 cudaError_t launch_dense_solve(int n, const int64_t *rowptr, const int *colind,

@@ -68,7 +68,7 @@ __global__ void __launch_bounds__(kBatchThreads) fused_ffblock_kernel(const Batc
     const int p = active ? find_problem(probs, nprob, item) : 0;
     const BatchProblem &P = probs[p];
     const int c = active ? (int)(item - P.first) : 0;
-    integrate_cell_ff(P.a, P.T, c, active, f, fq, Ah, Al, bh, bl, t, TPC);
+    integrate_cell_ff(P.a, P.T, c, active, f, fq, Ah, Al, bh, bl, t, TPC, true);
     const double invm = active ? cell_inv_mass(P.a, c) : 1.0;
     int *infoc = active ? P.info + c : nullptr;
     ffb::ffblock_cell<C, TPC, false>(active, Ah, Al, bh, bl, P.Mh, P.Ml, invm, fsm, P.S + (size_t)c * NF * NF,

@@ -21,20 +21,20 @@
 namespace hdg {
 
 __global__ void __launch_bounds__(256) integrate_mixed_kernel(CellArgs a, MixedTables T, float *Ahi, float *Alo,
-                                                              float *bhi, float *blo) {
+                                                              float *bhi, float *blo, bool skip_uu) {
   __shared__ CellFactorsFF f;
   __shared__ double fq[512 * 4];
   const int n = a.n;
   for (int c = blockIdx.x; c < a.ncells; c += gridDim.x)
     integrate_cell_ff(a, T, c, true, f, fq, Ahi + (size_t)c * n * n, Alo + (size_t)c * n * n, bhi + (size_t)c * n,
-                      blo + (size_t)c * n, threadIdx.x, blockDim.x);
+                      blo + (size_t)c * n, threadIdx.x, blockDim.x, skip_uu);
 }
 
 cudaError_t launch_integrate_mixed(const CellArgs &a, const MixedTables &T, float *Ahi, float *Alo, float *bhi,
-                                   float *blo, cudaStream_t s, int num_sms, long long *launches) {
+                                   float *blo, cudaStream_t s, int num_sms, long long *launches, bool skip_uu) {
   if (a.nqv > 512) return cudaErrorInvalidValue;
   int grid = a.ncells < num_sms * 8 ? a.ncells : num_sms * 8;
-  integrate_mixed_kernel<<<grid, 256, 0, s>>>(a, T, Ahi, Alo, bhi, blo);
+  integrate_mixed_kernel<<<grid, 256, 0, s>>>(a, T, Ahi, Alo, bhi, blo, skip_uu);
   ++*launches;
   return cudaGetLastError();
 }

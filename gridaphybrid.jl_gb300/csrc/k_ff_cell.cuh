@@ -193,9 +193,11 @@ __device__ __forceinline__ void cell_entry_ff(const CellArgs &a, const MixedTabl
 // the group's shared scratch.  Every thread of the CTA must call it (it
 // contains CTA barriers); threads of groups without a cell pass active=false
 // and still reach the barriers.
+// skip_uu: the flux-flux block (rows and columns < D*nk) is not written (the
+// block elimination uses (|J|/kappa) M_ref^{-1} instead of reading it).
 __device__ __forceinline__ void integrate_cell_ff(const CellArgs &a, const MixedTables &T, int c, bool active,
                                                   CellFactorsFF &f, double *fq, float *Ah, float *Al, float *bh,
-                                                  float *bl, int t, int nt) {
+                                                  float *bl, int t, int nt, bool skip_uu = false) {
   const int n = a.n, D = a.D;
   if (t == 0 && active) cell_factors_ff(a, c, f);
   __syncthreads();
@@ -216,8 +218,10 @@ __device__ __forceinline__ void integrate_cell_ff(const CellArgs &a, const Mixed
   }
   __syncthreads();
   if (active) {
+    const int nu = skip_uu ? D * a.nk : 0;
     for (int e = t; e < n * n; e += nt) {
       const int j = e / n, i = e - j * n;
+      if (i < nu && j < nu) continue;
       int ti, si, ii, tj, sj, jj;
       decode_row(i, D, a.nk, a.ni, a.nfd, ti, si, ii);
       decode_row(j, D, a.nk, a.ni, a.nfd, tj, sj, jj);

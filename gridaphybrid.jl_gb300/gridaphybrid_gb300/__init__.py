@@ -9,17 +9,18 @@ from ._lib import Context, HdgError, default_context
 from .maps import (ArrayBlock, BackwardStaticCondensationMap, MatrixBlock,
                    StaticCondensationMap, SumFacetsMap, VectorBlock, densify,
                    evaluate, lazy_map, return_cache)
-from .operators import (CartesianDiscreteModel, DarcyHDG, HybridAffineFEOperator,
-                        MultiFieldFESpace, ReferenceFE, Skeleton, TestFESpace,
-                        TrialFESpace, Triangulation, darcy_spaces,
-                        get_cell_normal_vector, get_cell_owner_normal_vector,
-                        solve)
+from .operators import (CartesianDiscreteModel, DarcyHDG, FEFunction, FESolver,
+                        HybridAffineFEOperator, HybridFEOperator, MultiFieldFESpace,
+                        NLSolver, ReferenceFE, Skeleton, TestFESpace, TrialFESpace,
+                        Triangulation, darcy_spaces, get_cell_normal_vector,
+                        get_cell_owner_normal_vector, solve, solve_)
 
 __all__ = [
     "ArrayBlock", "BackwardStaticCondensationMap", "CartesianDiscreteModel", "Context",
-    "DarcyHDG", "HdgError", "HybridAffineFEOperator", "MatrixBlock", "MultiFieldFESpace",
+    "DarcyHDG", "FEFunction", "FESolver", "HdgError", "HybridAffineFEOperator", "HybridFEOperator",
+    "NLSolver", "MatrixBlock", "MultiFieldFESpace",
     "ReferenceFE", "Skeleton", "StaticCondensationMap", "SumFacetsMap", "TestFESpace",
     "TrialFESpace", "Triangulation", "VectorBlock", "darcy_spaces", "default_context",
     "densify", "evaluate", "get_cell_normal_vector", "get_cell_owner_normal_vector",
-    "lazy_map", "return_cache", "solve",
+    "lazy_map", "return_cache", "solve", "solve_",
 ]

@@ -74,6 +74,7 @@ SIGNATURES = {
     "hdg_time_kernel": (_i, [_vp, _i, _i, _vp]),
     "hdg_problem_device_bytes": (_i, [_vp, _vp]),
     "hdg_set_refinement": (_i, [_vp, _d, _i]),
+    "hdg_newton_solve": (_i, [_vp, _i, _d, _i, _d, _i, _vp, _vp, _vp]),
     "hdg_footprint": (_i, [_i, _i, _i, _i, _i, _vp]),
     "hdg_batch_create": (_i, [_vp, _i, _vp, ctypes.POINTER(_vp)]),
     "hdg_batch_destroy": (_i, [_vp]),

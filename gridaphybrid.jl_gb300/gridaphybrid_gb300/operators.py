@@ -266,6 +266,84 @@ def solve(op, solver="pcg", rtol=1e-10, maxit=20000):
     return HybridFEFunction(op, it.value, rel.value)
 
 
+class HybridFEOperator:
+    """HybridFEOperator(residual, X, Y, bulk_fields, skeleton_fields)
+    (src/HybridFEOperators.jl:68-145): the nonlinear-operator form, solved by
+    Newton's method; its Jacobian is the hybridizable cell matrix, so every
+    Newton step runs the whole hybridization path (integrate, condense,
+    assemble, skeleton solve, recover) on the residual."""
+
+    def __init__(self, weakform, trial, test, bulk_fields, skeleton_fields, context=None):
+        if list(bulk_fields) != [1, 2] or list(skeleton_fields) != [3]:
+            raise ValueError("the Darcy HDG operator expects bulk_fields=[1,2] (flux, pressure) "
+                             "and skeleton_fields=[3] (trace)")
+        self.weakform, self.trial, self.test = weakform, trial, test
+        orders = {s.reffe.order for s in trial.spaces}
+        if len(orders) != 1:
+            raise ValueError("flux, pressure and trace must share the order k (Q_k / Q_k / Q_k)")
+        self.k = orders.pop()
+        self.model = trial[0].trian.model
+        self.ctx = context or _lib.default_context()
+        self.pb = _Problem(self.ctx, self.model, self.k)
+        c = self.ctx
+        c.check(c.lib.hdg_set_darcy(self.pb.h, weakform.stab, weakform.tau, weakform.problem))
+        c.check(c.lib.hdg_set_permeability(self.pb.h, _lib.ptr(weakform.kappa)))
+
+    def num_free_dofs(self):
+        return self.pb.ncells * self.pb.ni + self.pb.nfree
+
+
+class NLSolver:
+    """NLSolver(method=:newton, ftol=1e-8, iterations=1000) (NLsolve.jl's Newton
+    without line search, as used by test/DarcyHDGTests.jl:151,160); the linear
+    solve of each step is the hybridized one (src/HybridLinearSolvers.jl)."""
+
+    def __init__(self, method="newton", ftol=1e-8, iterations=1000, linear_solver="direct", rtol=1e-12,
+                 maxit=20000, show_trace=False):
+        if method != "newton":
+            raise ValueError("only method='newton' is provided")
+        self.ftol, self.iterations = float(ftol), int(iterations)
+        self.linear_solver = {"pcg": _lib.HDG_SOLVER_PCG, "direct": _lib.HDG_SOLVER_DIRECT}[linear_solver]
+        self.rtol, self.maxit = float(rtol), int(maxit)
+        self.show_trace = show_trace
+
+
+class FESolver:
+    def __init__(self, nls):
+        self.nls = nls
+
+
+class FEFunction:
+    """FEFunction(X, free_values): an initial guess for solve_."""
+
+    def __init__(self, space, free_values):
+        self.space = space
+        self.free_dof_values = np.ascontiguousarray(free_values, dtype=np.float64)
+
+
+def solve_(xh0, solver, op):
+    """solve!(xh0, solver, op) for a HybridFEOperator
+    (src/HybridLinearSolvers.jl:15-59 inside NLsolve's Newton loop): returns
+    (xh, cache) with the converged HybridFEFunction and the Newton history."""
+    nls = solver.nls
+    x0 = None
+    if xh0 is not None:
+        if xh0.free_dof_values.size != op.num_free_dofs():
+            raise ValueError("the initial guess has %d values, the space %d" % (xh0.free_dof_values.size,
+                                                                               op.num_free_dofs()))
+        x0 = xh0.free_dof_values
+    norms = np.zeros(nls.iterations + 1)
+    it = ctypes.c_int()
+    c = op.ctx
+    c.check(c.lib.hdg_newton_solve(op.pb.h, nls.linear_solver, nls.rtol, nls.maxit, nls.ftol, nls.iterations,
+                                   _lib.ptr(x0), _lib.ptr(norms), ctypes.byref(it)))
+    hist = norms[:it.value + 1].copy()
+    if nls.show_trace:
+        for i, r in enumerate(hist):
+            print("Newton %3d  residual %.3e" % (i, r))
+    return HybridFEFunction(op, it.value, float(hist[-1])), {"iterations": it.value, "residual_norms": hist}
+
+
 def darcy_spaces(model, k):
     """The spaces of the Darcy HDG test: Q_k flux, Q_k pressure, Q_k trace with
     Dirichlet facets on the whole boundary (test/DarcyHDGTests.jl:32-52)."""

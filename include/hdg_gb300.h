@@ -198,6 +198,23 @@ int hdg_get_skeleton_system(hdg_problem *pb, long long *rowptr, int *colind,
 int hdg_solve_skeleton(hdg_problem *pb, int solver, double rtol, int maxit,
                        int *iters, double *relres);
 
+/* HybridFEOperator(res, X, Y, bulk, skel) + solve!(xh0, FESolver(NLSolver(
+ * method=:newton)), op) (src/HybridFEOperators.jl:68-239,
+ * src/HybridLinearSolvers.jl:15-59, test/DarcyHDGTests.jl:157-165).  Newton
+ * iterations x <- x - dx: each step integrates the Jacobian (the cell
+ * matrices A_c) and the residual r_c = A_c x_c - b_c of the iterate,
+ * condenses [A_c | r_c], solves the skeleton system for dx with zero
+ * Dirichlet data (the correction vanishes there, :49-50) and recovers the
+ * interior corrections.  Stops when the max norm of the assembled residual
+ * is <= ftol (NLsolve's default 1e-8) or returns HDG_ERR_NOT_CONVERGED after
+ * max_iters steps.  x0: the initial free DOF values (hdg_get_free_dof_values
+ * layout), or NULL for zeros (FEFunction(X, zeros(num_free_dofs(X))));
+ * res_norms (max_iters + 1 values, may be NULL) receives the residual norm
+ * before each step; iters the number of steps.  FP64 arithmetic.  The
+ * result is the problem's solution (hdg_get_free_dof_values, hdg_l2_errors). */
+int hdg_newton_solve(hdg_problem *pb, int solver, double lin_rtol, int lin_maxit, double ftol,
+                     int max_iters, const double *x0, double *res_norms, int *iters);
+
 /* Options of the fast precisions' skeleton solve (an FP32 PCG inside FP64
  * residual refinement; no reference counterpart).  delta: the relative
  * residual reduction the FP32 iterations make between two FP64 residuals
