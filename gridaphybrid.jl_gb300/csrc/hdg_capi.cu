@@ -4,7 +4,9 @@
 // the kernels on the context's stream.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <chrono>
+#include <thread>
 
 #include <algorithm>
 #include <cmath>
@@ -943,6 +945,31 @@ static int solve_pcg_refined(hdg_problem *pb, double rtol, int maxit, int *it_ou
   return status;
 }
 
+// Every buffer a PCG solve and the recovery use, reserved up front (so that a
+// solve run on another stream allocates nothing).
+static int solve_reserve(hdg_problem *pb) {
+  hdg_context *ctx = pb->ctx;
+  const size_t n = pb->mesh.nfree ? pb->mesh.nfree : 1, nfd = pb->mesh.nfd, nbr = pb->pat.nblockrows;
+  CUDA_TRY(ctx, pb->d_x.reserve(sizeof(double) * n));
+  CUDA_TRY(ctx, pb->d_Binv.reserve(sizeof(double) * nbr * nfd * nfd));
+  for (DBuf *b : {&pb->d_r, &pb->d_z, &pb->d_p, &pb->d_p2, &pb->d_q}) CUDA_TRY(ctx, b->reserve(sizeof(double) * n));
+  CUDA_TRY(ctx, pb->d_partials.reserve(sizeof(double) * 3 * ctx->num_sms * 4));
+  CUDA_TRY(ctx, pb->d_scal.reserve(sizeof(double) * 16));
+  CUDA_TRY(ctx, pb->d_counter.reserve(sizeof(unsigned int) * 4));
+  if (!pb->h_pinned.ptr) {
+    CUDA_TRY(ctx, cudaMallocHost(&pb->h_pinned.ptr, 4096));
+    pb->h_pinned.bytes = 4096;
+  }
+  if (pb->precision != HDG_PREC_FP64) {
+    CUDA_TRY(ctx, pb->d_Binv32.reserve(sizeof(float) * nbr * nfd * nfd));
+    CUDA_TRY(ctx, pb->d_v32.reserve(sizeof(float) * 5 * n));
+    CUDA_TRY(ctx, pb->d_qc.reserve(sizeof(float) * pb->mesh.ncells * 2 * pb->mesh.D * nfd));
+    CUDA_TRY(ctx, pb->d_scal2.reserve(sizeof(double) * 16));
+  }
+  CUDA_TRY(ctx, pb->d_uint.reserve(sizeof(double) * pb->mesh.ncells * pb->tab.ni));
+  return HDG_OK;
+}
+
 int hdg_solve_skeleton(hdg_problem *pb, int solver, double rtol, int maxit, int *iters,
                        double *relres) {
   if (!pb) return HDG_ERR_INVALID;
@@ -1340,16 +1367,19 @@ struct hdg_batch {
   int graph_precision = -1;
   std::vector<const void *> graph_key;  // buffer addresses the graphs were captured with
   long long graph_launches[2] = {0, 0}; // kernels one replay launches
+  std::vector<hdg_context *> workers;   // streams of the concurrent skeleton solves
   double timings[3] = {0, 0, 0};        // fused integrate+condense, skeleton assembly, solve+recover (ms)
   ~hdg_batch() {
     for (auto &g : graph)
       if (g) cudaGraphExecDestroy(g);
+    for (hdg_context *w : workers) hdg_context_destroy(w);
   }
 };
 
 namespace {
 
 const int kTpcCandidates[4] = {256, 128, 64, 32};
+constexpr size_t kBatchSolveStreams = 8;
 
 int prec_slot(int precision) { return precision == HDG_PREC_FP64 ? 0 : precision == HDG_PREC_FF_BLOCK ? 1 : 2; }
 
@@ -1575,14 +1605,64 @@ int hdg_batch_solve(hdg_batch *b, int solver, double rtol, int maxit, int *iters
   hdg_context *ctx = b->ctx;
   cudaSetDevice(ctx->device);
   const auto h0 = std::chrono::steady_clock::now();
-  for (size_t i = 0; i < b->probs.size(); ++i) {
-    int it = 0;
-    double rel = 0.0;
-    int rc = hdg_solve_skeleton(b->probs[i], solver, rtol, maxit, &it, &rel);
-    if (iters) iters[i] = it;
-    if (relres) relres[i] = rel;
-    if (rc) return rc;
-    if ((rc = hdg_recover(b->probs[i]))) return rc;
+  const size_t np = b->probs.size();
+  for (hdg_problem *pb : b->probs)
+    if (!pb->assembled) return ctx->fail(HDG_ERR_STATE, "assemble the batch first");
+  const int nworkers = solver == HDG_SOLVER_PCG ? (int)std::min<size_t>(np, kBatchSolveStreams) : 1;
+  if (nworkers <= 1) {
+    for (size_t i = 0; i < np; ++i) {
+      int it = 0;
+      double rel = 0.0;
+      int rc = hdg_solve_skeleton(b->probs[i], solver, rtol, maxit, &it, &rel);
+      if (iters) iters[i] = it;
+      if (relres) relres[i] = rel;
+      if (rc) return rc;
+      if ((rc = hdg_recover(b->probs[i]))) return rc;
+    }
+  } else {
+    // The problems' skeleton solves are independent: worker threads run them
+    // concurrently, each on its own stream.  Everything a solve touches is
+    // reserved first on the batch stream, so the workers allocate nothing.
+    int rc;
+    for (hdg_problem *pb : b->probs)
+      if ((rc = solve_reserve(pb))) return rc;
+    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    while ((int)b->workers.size() < nworkers) {
+      hdg_context *w = nullptr;
+      if ((rc = hdg_context_create(ctx->device, &w))) return ctx->fail(rc, "worker stream creation failed");
+      b->workers.push_back(w);
+    }
+    std::atomic<size_t> next(0);
+    std::vector<int> rcs(np, HDG_OK);
+    std::vector<std::string> msgs(np);
+    std::vector<std::thread> threads;
+    for (int t = 0; t < nworkers; ++t)
+      threads.emplace_back([&, t] {
+        hdg_context *w = b->workers[(size_t)t];
+        cudaSetDevice(w->device);
+        for (size_t i = next++; i < np; i = next++) {
+          hdg_problem *pb = b->probs[i];
+          hdg_context *own = pb->ctx;
+          pb->ctx = w;  // this solve runs on the worker's stream
+          int it = 0;
+          double rel = 0.0;
+          int r = hdg_solve_skeleton(pb, solver, rtol, maxit, &it, &rel);
+          if (r == HDG_OK) r = hdg_recover(pb);
+          cudaStreamSynchronize(w->stream);
+          if (r != HDG_OK) msgs[i] = w->err;
+          pb->ctx = own;
+          rcs[i] = r;
+          if (iters) iters[i] = it;
+          if (relres) relres[i] = rel;
+        }
+      });
+    for (auto &th : threads) th.join();
+    for (hdg_context *w : b->workers) {
+      ctx->launches += w->launches;
+      w->launches = 0;
+    }
+    for (size_t i = 0; i < np; ++i)
+      if (rcs[i] != HDG_OK) return ctx->fail(rcs[i], "problem %zu: %s", i, msgs[i].c_str());
   }
   CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   b->timings[2] = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - h0).count();
