@@ -255,7 +255,13 @@ int orc_cart_topology(int D, const int *n, int *cell_facets, int *facet_cells,
  * consecutive, free and Dirichlet DOFs numbered separately. */
 int orc_facet_dofs(int D, int k, int nfacets, const int *facet_is_boundary,
                    int *facet_dofs, int *nfree, int *ndir) {
-  int nfd = ipow(k + 1, D - 1);
+  return orc_facet_dofs_n(ipow(k + 1, D - 1), nfacets, facet_is_boundary, facet_dofs, nfree, ndir);
+}
+
+/* The same with nfd DOFs per facet (a vector-valued facet space has
+ * D * (k+1)^(D-1), component-major within the facet). */
+int orc_facet_dofs_n(int nfd, int nfacets, const int *facet_is_boundary, int *facet_dofs, int *nfree,
+                     int *ndir) {
   int fr = 0, di = 0;
   for (int f = 0; f < nfacets; ++f)
     for (int a = 0; a < nfd; ++a)
@@ -813,7 +819,13 @@ static int cmp_int(const void *a, const void *b) {
 int orc_csr_pattern(int D, int k, int ncells, int nfacets,
                     const int *cell_facets, const int *facet_dofs, int nfree,
                     int64_t *rowptr, int32_t *colind, int64_t *nnz) {
-  int nfd = ipow(k + 1, D - 1), nl = 2 * D;
+  return orc_csr_pattern_n(D, ipow(k + 1, D - 1), ncells, nfacets, cell_facets, facet_dofs, nfree, rowptr, colind,
+                           nnz);
+}
+
+int orc_csr_pattern_n(int D, int nfd, int ncells, int nfacets, const int *cell_facets, const int *facet_dofs,
+                      int nfree, int64_t *rowptr, int32_t *colind, int64_t *nnz) {
+  int nl = 2 * D;
   /* facet -> cells */
   int *fc = malloc(sizeof(int) * 2 * nfacets);
   for (int f = 0; f < 2 * nfacets; ++f) fc[f] = -1;
@@ -886,11 +898,19 @@ int orc_assemble(int D, int k, int ncells, const int *cell_facets,
                  const int *facet_dofs, int nfree, const double *dir_vals,
                  const double *S, const double *g, const int64_t *rowptr,
                  const int32_t *colind, double *val, double *rhs) {
-  int nfd = ipow(k + 1, D - 1), nl = 2 * D, nf = nl * nfd;
+  return orc_assemble_n(D, ipow(k + 1, D - 1), ncells, cell_facets, facet_dofs, nfree, dir_vals, S, g, rowptr,
+                        colind, val, rhs);
+}
+
+int orc_assemble_n(int D, int nfd, int ncells, const int *cell_facets, const int *facet_dofs, int nfree,
+                   const double *dir_vals, const double *S, const double *g, const int64_t *rowptr,
+                   const int32_t *colind, double *val, double *rhs) {
+  int nl = 2 * D, nf = nl * nfd;
+  if (nf > 512) return -1;
   memset(val, 0, sizeof(double) * rowptr[nfree]);
   memset(rhs, 0, sizeof(double) * nfree);
-  int ids[64];
-  double gl[64];
+  int ids[512];
+  double gl[512];
   for (int c = 0; c < ncells; ++c) {
     const double *Sc = S + (size_t)c * nf * nf;
     for (int lf = 0; lf < nl; ++lf)
@@ -1043,7 +1063,12 @@ int orc_pcg(int n, int bs, const int64_t *rowptr, const int32_t *colind,
 int orc_cell_skeleton_values(int D, int k, int ncells, const int *cell_facets,
                              const int *facet_dofs, const double *xfree,
                              const double *dir_vals, double *xcell) {
-  int nfd = ipow(k + 1, D - 1), nl = 2 * D, nf = nl * nfd;
+  return orc_cell_skeleton_values_n(D, ipow(k + 1, D - 1), ncells, cell_facets, facet_dofs, xfree, dir_vals, xcell);
+}
+
+int orc_cell_skeleton_values_n(int D, int nfd, int ncells, const int *cell_facets, const int *facet_dofs,
+                               const double *xfree, const double *dir_vals, double *xcell) {
+  int nl = 2 * D, nf = nl * nfd;
 #pragma omp parallel for schedule(static)
   for (int c = 0; c < ncells; ++c)
     for (int lf = 0; lf < nl; ++lf)
@@ -1195,3 +1220,393 @@ int orc_solve_darcy(int D, int k, const int *n, const double *domain,
   if (bad) return 2;
   return rc;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Linear elasticity HDG (test/LinearElasticityHDGTests.jl:140-150 with the  */
+/* compliance of :15-38), without the P_m bulk-to-skeleton projection (the    */
+/* reference's bulk_to_skeleton_projection=false).  Spaces: symmetric stress */
+/* Q_k (D(D+1)/2 components), displacement Q_k (D components), displacement  */
+/* trace Q_k on facets (D components, Dirichlet on the boundary); per-cell   */
+/* Poisson ratio nu, Young's modulus E.  Vector/tensor DOFs are component-   */
+/* major, tensor components in upper-triangle order                          */
+/* (src/tmp_fixes_symmetric_valued_lagrangian_reffes.jl:104-125).            */
+/* ------------------------------------------------------------------------ */
+
+enum { EPROB_LINEAR = 0, EPROB_SMOOTH = 1 };
+
+static int sym_ncomp(int D) { return D * (D + 1) / 2; }
+
+static void sym_pair(int D, int c, int *i, int *j) {
+  static const int p2[3][2] = {{0, 0}, {0, 1}, {1, 1}};
+  static const int p3[6][2] = {{0, 0}, {0, 1}, {0, 2}, {1, 1}, {1, 2}, {2, 2}};
+  *i = D == 2 ? p2[c][0] : p3[c][0];
+  *j = D == 2 ? p2[c][1] : p3[c][1];
+}
+
+/* entry (r, s) of the symmetric unit tensor of component c */
+static double sym_unit(int D, int c, int r, int s) {
+  int i, j;
+  sym_pair(D, c, &i, &j);
+  return ((r == i && s == j) || (r == j && s == i)) ? 1.0 : 0.0;
+}
+
+/* Displacement u, gradient gu[i][j] = du_i/dx_j and Hessian hu[i][j][k].
+ * EPROB_LINEAR: u = (x+2y, 2x+y) (test/LinearElasticityHDGTests.jl:48-50) and
+ * (x+2y, 2x+y+z, y+3z) in 3D; EPROB_SMOOTH: u = (10 sin(pi x)(1-x)(y-y^2)(1-y/2), 0)
+ * (:52-57) in 2D and (sin pi x, cos pi y, xyz) in 3D. */
+static void elast_exact(int problem, int D, const double *x, double *u, double gu[3][3], double hu[3][3][3]) {
+  const double pi = 3.14159265358979323846;
+  memset(u, 0, sizeof(double) * 3);
+  memset(gu, 0, sizeof(double) * 9);
+  memset(hu, 0, sizeof(double) * 27);
+  if (problem == EPROB_LINEAR) {
+    if (D == 2) {
+      u[0] = x[0] + 2 * x[1];
+      u[1] = 2 * x[0] + x[1];
+      gu[0][0] = 1; gu[0][1] = 2; gu[1][0] = 2; gu[1][1] = 1;
+    } else {
+      u[0] = x[0] + 2 * x[1];
+      u[1] = 2 * x[0] + x[1] + x[2];
+      u[2] = x[1] + 3 * x[2];
+      gu[0][0] = 1; gu[0][1] = 2; gu[1][0] = 2; gu[1][1] = 1; gu[1][2] = 1; gu[2][1] = 1; gu[2][2] = 3;
+    }
+  } else if (D == 2) {
+    const double X = x[0], Y = x[1];
+    const double A = sin(pi * X) * (1 - X), dA = pi * cos(pi * X) * (1 - X) - sin(pi * X),
+                 ddA = -pi * pi * sin(pi * X) * (1 - X) - 2 * pi * cos(pi * X);
+    const double B = Y - 1.5 * Y * Y + 0.5 * Y * Y * Y, dB = 1 - 3 * Y + 1.5 * Y * Y, ddB = -3 + 3 * Y;
+    u[0] = 10 * A * B;
+    gu[0][0] = 10 * dA * B;
+    gu[0][1] = 10 * A * dB;
+    hu[0][0][0] = 10 * ddA * B;
+    hu[0][0][1] = hu[0][1][0] = 10 * dA * dB;
+    hu[0][1][1] = 10 * A * ddB;
+  } else {
+    const double X = x[0], Y = x[1], Z = x[2];
+    u[0] = sin(pi * X);
+    u[1] = cos(pi * Y);
+    u[2] = X * Y * Z;
+    gu[0][0] = pi * cos(pi * X);
+    gu[1][1] = -pi * sin(pi * Y);
+    gu[2][0] = Y * Z; gu[2][1] = X * Z; gu[2][2] = X * Y;
+    hu[0][0][0] = -pi * pi * sin(pi * X);
+    hu[1][1][1] = -pi * pi * cos(pi * Y);
+    hu[2][0][1] = hu[2][1][0] = Z;
+    hu[2][0][2] = hu[2][2][0] = Y;
+    hu[2][1][2] = hu[2][2][1] = X;
+  }
+}
+
+/* sigma = A^{-1} eps for A(s) = (1+nu)/E s - nu/E tr(s) I (:15-38):
+ * sigma = 2 mu eps + lam tr(eps) I, mu = E/(2(1+nu)), lam = nu E/((1+nu)(1+nu-D nu)) */
+static void elast_lame(int D, double E, double nu, double *mu, double *lam) {
+  *mu = E / (2.0 * (1.0 + nu));
+  *lam = nu * E / ((1.0 + nu) * (1.0 + nu - D * nu));
+}
+
+static void elast_sigma(int D, double E, double nu, double gu[3][3], double sig[3][3]) {
+  double mu, lam, tr = 0.0;
+  elast_lame(D, E, nu, &mu, &lam);
+  for (int d = 0; d < D; ++d) tr += gu[d][d];
+  for (int i = 0; i < D; ++i)
+    for (int j = 0; j < D; ++j) sig[i][j] = mu * (gu[i][j] + gu[j][i]) + (i == j ? lam * tr : 0.0);
+}
+
+/* f = div sigma_exact */
+static void elast_force(int D, double E, double nu, double hu[3][3][3], double *f) {
+  double mu, lam;
+  elast_lame(D, E, nu, &mu, &lam);
+  for (int i = 0; i < D; ++i) {
+    double v = 0.0;
+    for (int j = 0; j < D; ++j) v += mu * (hu[i][j][j] + hu[j][i][j]);
+    for (int k2 = 0; k2 < D; ++k2) v += lam * hu[k2][i][k2];
+    f[i] = v;
+  }
+}
+
+int orc_elasticity_sizes(int D, int k, int *ni, int *nf, int *nfd) {
+  if (D < 2 || D > 3 || k < 1 || k > MAXK) return -1;
+  int nk = ipow(k + 1, D);
+  *nfd = D * ipow(k + 1, D - 1);
+  *ni = (sym_ncomp(D) + D) * nk;
+  *nf = 2 * D * *nfd;
+  return 0;
+}
+
+/* Cell block of
+ *   int( v (.) A(sigma) + (div v).u - w.(div sigma) )dOmega - int((v.n).uhat)d(dK)
+ *   + int(tau w.u) - int(tau w.uhat) + int(mu.(sigma.n)) - int(tau mu.u) + int(tau mu.uhat) on dK,
+ *   l = int(-w.f)dOmega,
+ * DOFs [sigma (nsym x nk) | u (D x nk) | uhat per local facet (D x nfs)],
+ * integrated point by point; A column-major. */
+static void integrate_cell_elast(const reftab *t, int c, const int *n, const double *domain, double tau, double E,
+                                 double nu, int problem, double *A, double *b) {
+  const int D = t->D, nk = t->nk, nfs = t->nfd, ns = sym_ncomp(D);
+  const int ni = (ns + D) * nk, nfd = D * nfs, N = ni + 2 * D * nfd;
+  const int ou = ns * nk;  /* first displacement DOF */
+  double x0[MAXD], h[MAXD];
+  cell_geom(D, n, domain, c, x0, h);
+  double detJ = 1.0;
+  for (int d = 0; d < D; ++d) detJ *= h[d];
+  memset(A, 0, sizeof(double) * (size_t)N * N);
+  memset(b, 0, sizeof(double) * N);
+#define AIJ(i, j) A[(size_t)(i) + (size_t)N * (j)]
+  double Cm[6][6];  /* E_c (.) A(E_d) */
+  for (int ca = 0; ca < ns; ++ca)
+    for (int cb = 0; cb < ns; ++cb) {
+      double dd = 0.0, trc = 0.0, trd = 0.0;
+      for (int r = 0; r < D; ++r) {
+        trc += sym_unit(D, ca, r, r);
+        trd += sym_unit(D, cb, r, r);
+        for (int s2 = 0; s2 < D; ++s2) dd += sym_unit(D, ca, r, s2) * sym_unit(D, cb, r, s2);
+      }
+      Cm[ca][cb] = (1.0 + nu) / E * dd - nu / E * trc * trd;
+    }
+  for (int q = 0; q < t->nqv; ++q) {
+    const double *ph = &t->phi[q * nk];
+    const double *dph = &t->dphi[q * nk * D];
+    const double wq = t->qv_w[q] * detJ;
+    double x[MAXD], u[3], gu[3][3], hu[3][3][3], f[3];
+    for (int d = 0; d < D; ++d) x[d] = x0[d] + h[d] * t->qv_xi[q * D + d];
+    elast_exact(problem, D, x, u, gu, hu);
+    elast_force(D, E, nu, hu, f);
+    for (int a = 0; a < nk; ++a) {
+      for (int bb = 0; bb < nk; ++bb) {
+        const double mm = wq * ph[a] * ph[bb];
+        for (int ca = 0; ca < ns; ++ca)
+          for (int cb = 0; cb < ns; ++cb) AIJ(ca * nk + a, cb * nk + bb) += Cm[ca][cb] * mm;
+        for (int ca = 0; ca < ns; ++ca)
+          for (int kk = 0; kk < D; ++kk) {
+            double dv = 0.0;  /* ((div (phi_a E_ca)) . e_kk) */
+            for (int j = 0; j < D; ++j) dv += sym_unit(D, ca, kk, j) * dph[a * D + j] / h[j];
+            /* (div v).u */
+            AIJ(ca * nk + a, ou + kk * nk + bb) += wq * dv * ph[bb];
+            /* -w.(div sigma): test (kk, bb), trial (ca, a) */
+            AIJ(ou + kk * nk + bb, ca * nk + a) -= wq * ph[bb] * dv;
+          }
+      }
+      for (int kk = 0; kk < D; ++kk) b[ou + kk * nk + a] -= wq * ph[a] * f[kk];
+    }
+  }
+  for (int lf = 0; lf < 2 * D; ++lf) {
+    const int dn = D - 1 - lf / 2, side = lf % 2;
+    double nrm[MAXD] = {0, 0, 0};
+    nrm[dn] = side ? 1.0 : -1.0;
+    double detF = 1.0;
+    for (int d = 0; d < D; ++d)
+      if (d != dn) detF *= h[d];
+    const int off = ni + lf * nfd;
+    for (int q = 0; q < t->nqf; ++q) {
+      const double *ph = &t->fphi[(lf * t->nqf + q) * nk];
+      const double *mu = &t->mu[q * nfs];
+      const double wq = t->qf_w[q] * detF;
+      for (int a = 0; a < nk; ++a) {
+        for (int m = 0; m < nfs; ++m)
+          for (int kk = 0; kk < D; ++kk) {
+            const int hu_i = off + kk * nfs + m;
+            for (int ca = 0; ca < ns; ++ca) {
+              double en = 0.0;  /* ((E_ca) n) . e_kk */
+              for (int j = 0; j < D; ++j) en += sym_unit(D, ca, kk, j) * nrm[j];
+              if (en == 0.0) continue;
+              AIJ(ca * nk + a, hu_i) -= wq * en * ph[a] * mu[m];  /* -(v.n).uhat */
+              AIJ(hu_i, ca * nk + a) += wq * en * mu[m] * ph[a];  /* mu.(sigma.n) */
+            }
+            AIJ(ou + kk * nk + a, hu_i) -= wq * tau * ph[a] * mu[m];  /* -tau w.uhat */
+            AIJ(hu_i, ou + kk * nk + a) -= wq * tau * mu[m] * ph[a];  /* -tau mu.u */
+          }
+        for (int bb = 0; bb < nk; ++bb)
+          for (int kk = 0; kk < D; ++kk) AIJ(ou + kk * nk + a, ou + kk * nk + bb) += wq * tau * ph[a] * ph[bb];
+      }
+      for (int m = 0; m < nfs; ++m)
+        for (int m2 = 0; m2 < nfs; ++m2)
+          for (int kk = 0; kk < D; ++kk) AIJ(off + kk * nfs + m, off + kk * nfs + m2) += wq * tau * mu[m] * mu[m2];
+    }
+  }
+#undef AIJ
+}
+
+int orc_integrate_elasticity(int D, int k, const int *n, const double *domain, double tau, double E,
+                             const double *nu, int problem, double *A, double *b) {
+  reftab t;
+  if (reftab_init(&t, D, k)) return -1;
+  int ncells, nfacets, ni, nf, nfd;
+  orc_cart_counts(D, n, &ncells, &nfacets);
+  orc_elasticity_sizes(D, k, &ni, &nf, &nfd);
+  const size_t N = (size_t)ni + nf;
+#pragma omp parallel for schedule(static)
+  for (int c = 0; c < ncells; ++c)
+    integrate_cell_elast(&t, c, n, domain, tau, E, nu ? nu[c] : 0.3, problem, A + (size_t)c * N * N, b + (size_t)c * N);
+  reftab_free(&t);
+  return 0;
+}
+
+/* TrialFESpace(M, u_exact) (:96-98): nodal interpolation of u at the facet
+ * nodes, component-major per facet. */
+int orc_dirichlet_values_elasticity(int D, int k, const int *n, const double *domain, int problem, int nfacets,
+                                    const int *facet_is_boundary, const int *facet_dofs, int ndir, double *vals) {
+  int ncells, nf2;
+  orc_cart_counts(D, n, &ncells, &nf2);
+  int *cell_facets = malloc(sizeof(int) * ncells * 2 * D);
+  int *facet_cells = malloc(sizeof(int) * nfacets * 2);
+  int *isb = malloc(sizeof(int) * nfacets);
+  orc_cart_topology(D, n, cell_facets, facet_cells, isb);
+  int flat[36 * 2];
+  orc_lagrange_lattice(D - 1, k, flat);
+  const int nfs = ipow(k + 1, D - 1), nfd = D * nfs;
+  for (int c = 0; c < ncells; ++c) {
+    double x0[MAXD], h[MAXD];
+    cell_geom(D, n, domain, c, x0, h);
+    for (int lf = 0; lf < 2 * D; ++lf) {
+      int f = cell_facets[c * 2 * D + lf];
+      if (!facet_is_boundary[f]) continue;
+      int dn = D - 1 - lf / 2, side = lf % 2;
+      for (int a = 0; a < nfs; ++a) {
+        double x[MAXD];
+        int j = 0;
+        for (int d = 0; d < D; ++d) {
+          double xi = (d == dn) ? (double)side : (double)flat[a * (D - 1) + j++] / k;
+          x[d] = x0[d] + h[d] * xi;
+        }
+        double u[3], gu[3][3], hu[3][3][3];
+        elast_exact(problem, D, x, u, gu, hu);
+        for (int kk = 0; kk < D; ++kk) {
+          int id = facet_dofs[f * nfd + kk * nfs + a];
+          if (id < 0 && -1 - id < ndir) vals[-1 - id] = u[kk];
+        }
+      }
+    }
+  }
+  free(cell_facets);
+  free(facet_cells);
+  free(isb);
+  return 0;
+}
+
+/* sqrt(sum(int(e_sigma (.) e_sigma))) and sqrt(sum(int(e_u . e_u))) (:153-157) */
+int orc_l2_errors_elasticity(int D, int k, const int *n, const double *domain, double E, const double *nu,
+                             int problem, const double *uint, double *err_sigma, double *err_u) {
+  reftab t;
+  if (reftab_init(&t, D, k)) return -1;
+  int ncells, nfacets, ni, nf, nfd;
+  orc_cart_counts(D, n, &ncells, &nfacets);
+  orc_elasticity_sizes(D, k, &ni, &nf, &nfd);
+  const int nk = t.nk, ns = sym_ncomp(D), ou = ns * nk;
+  double es = 0.0, eu = 0.0;
+#pragma omp parallel for reduction(+ : es, eu) schedule(static)
+  for (int c = 0; c < ncells; ++c) {
+    double x0[MAXD], h[MAXD], detJ = 1.0;
+    cell_geom(D, n, domain, c, x0, h);
+    for (int d = 0; d < D; ++d) detJ *= h[d];
+    const double *v = uint + (size_t)c * ni;
+    const double nuc = nu ? nu[c] : 0.3;
+    for (int q = 0; q < t.nqv; ++q) {
+      double x[MAXD], u[3], gu[3][3], hu[3][3][3], sig[3][3];
+      for (int d = 0; d < D; ++d) x[d] = x0[d] + h[d] * t.qv_xi[q * D + d];
+      elast_exact(problem, D, x, u, gu, hu);
+      elast_sigma(D, E, nuc, gu, sig);
+      double sh[6] = {0, 0, 0, 0, 0, 0}, uh[3] = {0, 0, 0};
+      for (int a = 0; a < nk; ++a) {
+        const double ph = t.phi[q * nk + a];
+        for (int cc = 0; cc < ns; ++cc) sh[cc] += v[cc * nk + a] * ph;
+        for (int kk = 0; kk < D; ++kk) uh[kk] += v[ou + kk * nk + a] * ph;
+      }
+      double e2 = 0.0, u2 = 0.0;
+      for (int cc = 0; cc < ns; ++cc) {
+        int i, j;
+        sym_pair(D, cc, &i, &j);
+        const double d = sig[i][j] - sh[cc];
+        e2 += (i == j ? 1.0 : 2.0) * d * d;
+      }
+      for (int kk = 0; kk < D; ++kk) u2 += (u[kk] - uh[kk]) * (u[kk] - uh[kk]);
+      const double w = t.qv_w[q] * detJ;
+      es += w * e2;
+      eu += w * u2;
+    }
+  }
+  *err_sigma = sqrt(es);
+  *err_u = sqrt(eu);
+  reftab_free(&t);
+  return 0;
+}
+
+/* Whole path as for Darcy (integrate + condense per cell, assemble, skeleton
+ * solve: 0 dense LU, 1 block-Jacobi PCG on sign*S; re-integrate + backward map
+ * per cell).  sign: the sign that makes the skeleton operator SPD for PCG. */
+int orc_solve_elasticity(int D, int k, const int *n, const double *domain, double tau, double E, const double *nu,
+                         int problem, int solver, double sign, double rtol, int maxit, double *uint_out,
+                         double *lambda_out, int *iters, double *relres, double *err_sigma, double *err_u) {
+  reftab t;
+  if (reftab_init(&t, D, k)) return -1;
+  int ncells, nfacets, nfree, ndir, ni, nf, nfd;
+  orc_cart_counts(D, n, &ncells, &nfacets);
+  orc_elasticity_sizes(D, k, &ni, &nf, &nfd);
+  const int nl = 2 * D, N = ni + nf;
+  int *cell_facets = malloc(sizeof(int) * ncells * nl);
+  int *facet_cells = malloc(sizeof(int) * nfacets * 2);
+  int *isb = malloc(sizeof(int) * nfacets);
+  int *fdofs = malloc(sizeof(int) * nfacets * nfd);
+  orc_cart_topology(D, n, cell_facets, facet_cells, isb);
+  orc_facet_dofs_n(nfd, nfacets, isb, fdofs, &nfree, &ndir);
+  double *dvals = malloc(sizeof(double) * (ndir > 0 ? ndir : 1));
+  orc_dirichlet_values_elasticity(D, k, n, domain, problem, nfacets, isb, fdofs, ndir, dvals);
+  double *S = malloc(sizeof(double) * (size_t)ncells * nf * nf);
+  double *g = malloc(sizeof(double) * (size_t)ncells * nf);
+  int bad = 0;
+#pragma omp parallel reduction(+ : bad)
+  {
+    double *A = malloc(sizeof(double) * (size_t)N * N), *b = malloc(sizeof(double) * N);
+    double *work = malloc(sizeof(double) * ((size_t)ni * ni + 2 * (size_t)ni * nf + ni));
+    int *ipiv = malloc(sizeof(int) * ni);
+#pragma omp for schedule(static)
+    for (int c = 0; c < ncells; ++c) {
+      integrate_cell_elast(&t, c, n, domain, tau, E, nu ? nu[c] : 0.3, problem, A, b);
+      if (static_condensation_cell(ni, nf, A, b, S + (size_t)c * nf * nf, g + (size_t)c * nf, work, ipiv)) ++bad;
+    }
+    free(A); free(b); free(work); free(ipiv);
+  }
+  int64_t nnz;
+  int64_t *rowptr = malloc(sizeof(int64_t) * (nfree + 1));
+  orc_csr_pattern_n(D, nfd, ncells, nfacets, cell_facets, fdofs, nfree, NULL, NULL, &nnz);
+  int32_t *colind = malloc(sizeof(int32_t) * (nnz > 0 ? nnz : 1));
+  double *val = malloc(sizeof(double) * (nnz > 0 ? nnz : 1));
+  double *rhs = malloc(sizeof(double) * (nfree > 0 ? nfree : 1));
+  double *lam = malloc(sizeof(double) * (nfree > 0 ? nfree : 1));
+  orc_csr_pattern_n(D, nfd, ncells, nfacets, cell_facets, fdofs, nfree, rowptr, colind, &nnz);
+  int rc = orc_assemble_n(D, nfd, ncells, cell_facets, fdofs, nfree, dvals, S, g, rowptr, colind, val, rhs);
+  int it = 0;
+  double rel = 0.0;
+  if (!rc) {
+    if (solver == 0) rc = orc_dense_solve(nfree, rowptr, colind, val, rhs, lam);
+    else rc = orc_pcg(nfree, nfd, rowptr, colind, val, rhs, lam, sign, rtol, maxit, &it, &rel);
+  }
+  double *ucells = uint_out ? uint_out : malloc(sizeof(double) * (size_t)ncells * ni);
+#pragma omp parallel reduction(+ : bad)
+  {
+    double *A = malloc(sizeof(double) * (size_t)N * N), *b = malloc(sizeof(double) * N);
+    double *work = malloc(sizeof(double) * ((size_t)ni * ni + (size_t)ni * nf));
+    double *xc = malloc(sizeof(double) * nf);
+    int *ipiv = malloc(sizeof(int) * ni);
+#pragma omp for schedule(static)
+    for (int c = 0; c < ncells; ++c) {
+      for (int lf = 0; lf < nl; ++lf)
+        for (int a = 0; a < nfd; ++a) {
+          int id = fdofs[cell_facets[c * nl + lf] * nfd + a];
+          xc[lf * nfd + a] = id >= 0 ? lam[id] : dvals[-1 - id];
+        }
+      integrate_cell_elast(&t, c, n, domain, tau, E, nu ? nu[c] : 0.3, problem, A, b);
+      if (backward_cell(ni, nf, A, b, xc, ucells + (size_t)c * ni, work, ipiv)) ++bad;
+    }
+    free(A); free(b); free(work); free(xc); free(ipiv);
+  }
+  if (iters) *iters = it;
+  if (relres) *relres = rel;
+  if (err_sigma && err_u) orc_l2_errors_elasticity(D, k, n, domain, E, nu, problem, ucells, err_sigma, err_u);
+  if (lambda_out) memcpy(lambda_out, lam, sizeof(double) * nfree);
+  if (!uint_out) free(ucells);
+  free(cell_facets); free(facet_cells); free(isb); free(fdofs); free(dvals);
+  free(S); free(g); free(rowptr); free(colind); free(val); free(rhs); free(lam);
+  reftab_free(&t);
+  if (bad) return 2;
+  return rc;
+}
+

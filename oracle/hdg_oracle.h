@@ -43,6 +43,8 @@ int orc_cart_topology(int D, const int *n, int *cell_facets, int *facet_cells,
                       int *facet_is_boundary);
 int orc_facet_dofs(int D, int k, int nfacets, const int *facet_is_boundary,
                    int *facet_dofs, int *nfree, int *ndir);
+int orc_facet_dofs_n(int nfd, int nfacets, const int *facet_is_boundary, int *facet_dofs, int *nfree,
+                     int *ndir);
 
 /* Integration of the Darcy HDG forms -------------------------------------- */
 int orc_cell_sizes(int D, int k, int *ni, int *nf);
@@ -75,6 +77,14 @@ int orc_assemble(int D, int k, int ncells, const int *cell_facets,
                  const int *facet_dofs, int nfree, const double *dir_vals,
                  const double *S, const double *g, const int64_t *rowptr,
                  const int32_t *colind, double *val, double *rhs);
+/* the same with nfd DOFs per facet */
+int orc_csr_pattern_n(int D, int nfd, int ncells, int nfacets, const int *cell_facets, const int *facet_dofs,
+                      int nfree, int64_t *rowptr, int32_t *colind, int64_t *nnz);
+int orc_assemble_n(int D, int nfd, int ncells, const int *cell_facets, const int *facet_dofs, int nfree,
+                   const double *dir_vals, const double *S, const double *g, const int64_t *rowptr,
+                   const int32_t *colind, double *val, double *rhs);
+int orc_cell_skeleton_values_n(int D, int nfd, int ncells, const int *cell_facets, const int *facet_dofs,
+                               const double *xfree, const double *dir_vals, double *xcell);
 int orc_dense_solve(int n, const int64_t *rowptr, const int32_t *colind,
                     const double *val, const double *rhs, double *x);
 int orc_pcg(int n, int bs, const int64_t *rowptr, const int32_t *colind,
@@ -93,6 +103,17 @@ int orc_solve_darcy(int D, int k, const int *n, const double *domain,
                     int solver, double rtol, int maxit, double *uint_out,
                     double *lambda_out, double *times_out, int *iters,
                     double *relres, double *err_flux, double *err_pres);
+/* Linear elasticity HDG (test/LinearElasticityHDGTests.jl) --------------- */
+int orc_elasticity_sizes(int D, int k, int *ni, int *nf, int *nfd);
+int orc_integrate_elasticity(int D, int k, const int *n, const double *domain, double tau, double E,
+                             const double *nu, int problem, double *A, double *b);
+int orc_dirichlet_values_elasticity(int D, int k, const int *n, const double *domain, int problem, int nfacets,
+                                    const int *facet_is_boundary, const int *facet_dofs, int ndir, double *vals);
+int orc_l2_errors_elasticity(int D, int k, const int *n, const double *domain, double E, const double *nu,
+                             int problem, const double *uint, double *err_sigma, double *err_u);
+int orc_solve_elasticity(int D, int k, const int *n, const double *domain, double tau, double E, const double *nu,
+                         int problem, int solver, double sign, double rtol, int maxit, double *uint_out,
+                         double *lambda_out, int *iters, double *relres, double *err_sigma, double *err_u);
 int orc_max_threads(void);
 void orc_set_threads(int nthreads);
 

@@ -212,6 +212,100 @@ def solve_darcy(D, k, n, tau=1.0, stab=STAB_TEXTBOOK, problem=PROBLEM_LINEAR, ka
                 relres=rel.value, err_flux=ef.value, err_pres=ep.value, mesh=m)
 
 
+EPROBLEM_LINEAR = 0
+EPROBLEM_SMOOTH = 1
+
+
+class ElasticityMesh(Mesh):
+    """The linear elasticity HDG spaces on the same Cartesian mesh: symmetric
+    stress Q_k, displacement Q_k, displacement trace Q_k (D components per
+    facet node, component-major) with Dirichlet data on the boundary."""
+
+    def __init__(self, D, n, k, domain=None):
+        super().__init__(D, n, k, domain)
+        L = lib()
+        ni, nf, nfd = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        L.orc_elasticity_sizes(D, k, ctypes.byref(ni), ctypes.byref(nf), ctypes.byref(nfd))
+        self.ni, self.nf, self.nfd = ni.value, nf.value, nfd.value
+        self.facet_dofs = np.zeros((self.nfacets, self.nfd), dtype=np.int32)
+        nfree, ndir = ctypes.c_int(), ctypes.c_int()
+        L.orc_facet_dofs_n(self.nfd, self.nfacets, P(self.facet_is_boundary), P(self.facet_dofs),
+                           ctypes.byref(nfree), ctypes.byref(ndir))
+        self.nfree, self.ndir = nfree.value, ndir.value
+
+    def integrate(self, tau=1.0, E=1.0, nu=None, problem=EPROBLEM_SMOOTH):
+        n = self.ni + self.nf
+        A = np.zeros((self.ncells, n, n))  # A[c, j, i] = A_c(i, j)
+        b = np.zeros((self.ncells, n))
+        v = None if nu is None else np.ascontiguousarray(nu, dtype=np.float64)
+        rc = lib().orc_integrate_elasticity(self.D, self.k, P(self.n), P(self.domain), ctypes.c_double(tau),
+                                            ctypes.c_double(E), P(v), problem, P(A), P(b))
+        assert rc == 0
+        return A, b
+
+    def dirichlet_values(self, problem):
+        vals = np.zeros(max(self.ndir, 1))
+        lib().orc_dirichlet_values_elasticity(self.D, self.k, P(self.n), P(self.domain), problem, self.nfacets,
+                                              P(self.facet_is_boundary), P(self.facet_dofs), self.ndir, P(vals))
+        return vals[:self.ndir] if self.ndir else vals[:0]
+
+    def csr_pattern(self):
+        nnz = ctypes.c_int64()
+        L = lib()
+        L.orc_csr_pattern_n(self.D, self.nfd, self.ncells, self.nfacets, P(self.cell_facets), P(self.facet_dofs),
+                            self.nfree, None, None, ctypes.byref(nnz))
+        rowptr = np.zeros(self.nfree + 1, dtype=np.int64)
+        colind = np.zeros(nnz.value, dtype=np.int32)
+        L.orc_csr_pattern_n(self.D, self.nfd, self.ncells, self.nfacets, P(self.cell_facets), P(self.facet_dofs),
+                            self.nfree, P(rowptr), P(colind), ctypes.byref(nnz))
+        return rowptr, colind
+
+    def assemble(self, S, g, dirvals):
+        rowptr, colind = self.csr_pattern()
+        val = np.zeros(len(colind))
+        rhs = np.zeros(self.nfree)
+        dv = np.ascontiguousarray(dirvals if len(dirvals) else np.zeros(1))
+        rc = lib().orc_assemble_n(self.D, self.nfd, self.ncells, P(self.cell_facets), P(self.facet_dofs),
+                                  self.nfree, P(dv), P(np.ascontiguousarray(S)), P(np.ascontiguousarray(g)),
+                                  P(rowptr), P(colind), P(val), P(rhs))
+        assert rc == 0
+        return rowptr, colind, val, rhs
+
+    def cell_skeleton_values(self, lam, dirvals):
+        x = np.zeros((self.ncells, self.nf))
+        dv = np.ascontiguousarray(dirvals if len(dirvals) else np.zeros(1))
+        lib().orc_cell_skeleton_values_n(self.D, self.nfd, self.ncells, P(self.cell_facets), P(self.facet_dofs),
+                                         P(np.ascontiguousarray(lam)), P(dv), P(x))
+        return x
+
+    def l2_errors(self, problem, uint, E=1.0, nu=None):
+        es, eu = ctypes.c_double(), ctypes.c_double()
+        v = None if nu is None else np.ascontiguousarray(nu, dtype=np.float64)
+        lib().orc_l2_errors_elasticity(self.D, self.k, P(self.n), P(self.domain), ctypes.c_double(E), P(v), problem,
+                                       P(np.ascontiguousarray(uint)), ctypes.byref(es), ctypes.byref(eu))
+        return es.value, eu.value
+
+
+def solve_elasticity(D, k, n, tau=None, E=1.0, nu=None, problem=EPROBLEM_SMOOTH, solver=0, sign=1.0,
+                     rtol=1e-12, maxit=100000, domain=None):
+    """The elasticity path on the CPU (solver 0: dense LU, 1: block-Jacobi PCG on
+    sign * S); tau defaults to the reference's 1/h (cells per side)."""
+    L = lib()
+    n = np.array(n, dtype=np.int32)
+    dom = np.array(domain if domain is not None else [0.0, 1.0] * D, dtype=np.float64)
+    m = ElasticityMesh(D, n, k, dom)
+    tau = float(n[0]) if tau is None else float(tau)
+    uint = np.zeros((m.ncells, m.ni))
+    lam = np.zeros(max(m.nfree, 1))
+    it, rel, es, eu = ctypes.c_int(), ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    v = None if nu is None else np.ascontiguousarray(nu, dtype=np.float64)
+    rc = L.orc_solve_elasticity(D, k, P(n), P(dom), ctypes.c_double(tau), ctypes.c_double(E), P(v), problem, solver,
+                                ctypes.c_double(sign), ctypes.c_double(rtol), maxit, P(uint), P(lam),
+                                ctypes.byref(it), ctypes.byref(rel), ctypes.byref(es), ctypes.byref(eu))
+    return dict(rc=rc, uint=uint, lam=lam[:m.nfree], iters=it.value, relres=rel.value, err_sigma=es.value,
+                err_u=eu.value, mesh=m, tau=tau)
+
+
 def set_threads(n):
     lib().orc_set_threads(int(n))
 

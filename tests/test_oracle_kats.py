@@ -153,3 +153,56 @@ def test_pcg_matches_dense():
     r1 = oracle.solve_darcy(3, 1, (3, 3, 3), problem=oracle.PROBLEM_SIN, kappa=kappa, solver=1, rtol=1e-14)
     assert np.abs(r0["lam"] - r1["lam"]).max() < 1e-11 * np.abs(r0["lam"]).max()
     assert np.abs(r0["uint"] - r1["uint"]).max() < 1e-11 * np.abs(r0["uint"]).max()
+
+
+# ---------------------------------------------------------------------------
+# Linear elasticity HDG (test/LinearElasticityHDGTests.jl)
+# ---------------------------------------------------------------------------
+
+@pytest.mark.parametrize("D,n,k", [(2, (2, 2), 1), (2, (3, 2), 2), (3, (2, 2, 2), 1)])
+def test_elasticity_linear_displacement_is_exact(D, n, k):
+    """A linear displacement (constant stress, f = 0) is in the discrete
+    spaces: the HDG solution reproduces it (the reference's linear u_exact,
+    test/LinearElasticityHDGTests.jl:48-50)."""
+    r = oracle.solve_elasticity(D, k, n, problem=oracle.EPROBLEM_LINEAR,
+                                nu=np.random.default_rng(1).uniform(0.2, 0.45, size=int(np.prod(n))))
+    assert r["rc"] == 0
+    assert r["err_sigma"] < 1e-12 and r["err_u"] < 1e-12
+
+
+def test_elasticity_convergence_rates():
+    """Smooth 2D displacement of the reference test (:52-57), k = 1: stress
+    error ~ h^k, displacement error ~ h^(k+1)."""
+    es, eu = [], []
+    for nn in (4, 8, 16):
+        r = oracle.solve_elasticity(2, 1, (nn, nn), problem=oracle.EPROBLEM_SMOOTH)
+        es.append(r["err_sigma"])
+        eu.append(r["err_u"])
+    rs = np.log2(es[1] / es[2])
+    ru = np.log2(eu[1] / eu[2])
+    assert 0.9 < rs < 1.6 and 1.8 < ru < 2.4
+
+
+def test_elasticity_skeleton_operator_is_spd():
+    m = oracle.ElasticityMesh(2, (3, 3), 1)
+    nu = np.random.default_rng(0).uniform(0.2, 0.45, size=m.ncells)
+    A, b = m.integrate(tau=3.0, nu=nu)
+    S, g, info = oracle.static_condensation(A, b, m.ni)
+    assert (info == 0).all()
+    rowptr, colind, val, rhs = m.assemble(S, g, m.dirichlet_values(oracle.EPROBLEM_SMOOTH))
+    K = np.zeros((m.nfree, m.nfree))
+    for r in range(m.nfree):
+        K[r, colind[rowptr[r]:rowptr[r + 1]]] = val[rowptr[r]:rowptr[r + 1]]
+    assert np.abs(K - K.T).max() < 1e-12 * np.abs(K).max()
+    assert np.linalg.eigvalsh(K).min() > 0.0
+    # PCG on +S agrees with the dense solve
+    d = oracle.solve_elasticity(2, 1, (3, 3), nu=nu, solver=0)
+    p = oracle.solve_elasticity(2, 1, (3, 3), nu=nu, solver=1, sign=1.0, rtol=1e-13)
+    assert np.abs(d["lam"] - p["lam"]).max() < 1e-9 * np.abs(d["lam"]).max()
+
+
+def test_elasticity_sym_tensor_layout_sizes():
+    for D, k, ni, nf in [(2, 1, (3 + 2) * 4, 4 * 2 * 2), (3, 1, (6 + 3) * 8, 6 * 3 * 4), (3, 2, (6 + 3) * 27, 6 * 3 * 9)]:
+        m = oracle.ElasticityMesh(D, (2,) * D, k)
+        assert (m.ni, m.nf) == (ni, nf)
+        assert m.nfd == D * (k + 1) ** (D - 1)
