@@ -108,6 +108,10 @@ CellArgs cell_args(hdg_problem *pb) {
   a.tau = pb->tau;
   a.stab_mode = pb->stab_mode;
   a.problem = pb->problem;
+  a.phys = t.phys;
+  a.nsym = t.nsym;
+  a.nfs = t.nfs;
+  a.young = pb->young;
   return a;
 }
 
@@ -133,6 +137,14 @@ cudaError_t run_integrate(hdg_problem *pb) {
   hdg_context *ctx = pb->ctx;
   CellArgs a = cell_args(pb);
   const size_t nc = pb->mesh.ncells, n = pb->tab.n;
+  if (pb->physics == HDG_PHYSICS_ELASTICITY) {
+    if (pb->precision == HDG_PREC_FP64)
+      return launch_integrate_elasticity(a, pb->d_A.as<double>(), pb->d_b.as<double>(), nullptr, nullptr, nullptr,
+                                         nullptr, ctx->stream, ctx->num_sms, &ctx->launches);
+    float *Ahi = pb->d_A.as<float>(), *bhi = pb->d_b.as<float>();
+    return launch_integrate_elasticity(a, nullptr, nullptr, Ahi, Ahi + nc * n * n, bhi, bhi + nc * n, ctx->stream,
+                                       ctx->num_sms, &ctx->launches);
+  }
   if (pb->precision == HDG_PREC_FP64)
     return launch_integrate_fp64(a, pb->d_A.as<double>(), pb->d_b.as<double>(), ctx->stream, ctx->num_sms,
                                  &ctx->launches);
@@ -166,6 +178,16 @@ cudaError_t run_condense(hdg_problem *pb) {
 
 // The Dirichlet data the lift and the recovery use: the problem's values, or
 // zeros while the Newton path solves for a correction.
+// The sign that makes the condensed skeleton operator SPD: the Darcy forms'
+// is negative definite, the elasticity form's positive definite.
+// DOFs per cell of the first bulk field (Darcy flux: D nk; elasticity stress: nsym nk)
+size_t first_field_width(const hdg_problem *pb) {
+  const RefTables &t = pb->tab;
+  return (size_t)(pb->physics == HDG_PHYSICS_ELASTICITY ? t.nsym : t.D) * t.nk;
+}
+
+double skeleton_sign(const hdg_problem *pb) { return pb->physics == HDG_PHYSICS_ELASTICITY ? 1.0 : -1.0; }
+
 const double *dirichlet_values(const hdg_problem *pb) {
   return pb->zero_dirichlet ? pb->d_dirzero.as<double>() : pb->d_dirvals.as<double>();
 }
@@ -219,14 +241,20 @@ void interpolate_dirichlet(const hdg_problem *pb, std::vector<double> &vals) {
       const int id = m.facet_dofs[(size_t)f * nfd + b];
       double xi[3], x[3];
       for (int d = 0, j = 0; d < D; ++d)
-        xi[d] = (d == dn) ? double(side) : double(t.flat[b * (D - 1) + j++]) / k;
+        xi[d] = (d == dn) ? double(side) : double(t.flat[(b % t.nfs) * (D - 1) + j++]) / k;
       for (int d = 0; d < D; ++d) {
         x[d] = m.origin[(size_t)c * D + d];
         for (int e = 0; e < D; ++e) x[d] += m.jac[(size_t)c * D * D + e * D + d] * xi[e];
       }
-      double p, q[3], fu[3], g;
-      exact_solution(pb->problem, D, x, 1.0, p, q, fu, g);
-      vals[-1 - id] = p;
+      if (pb->physics == HDG_PHYSICS_ELASTICITY) {
+        double u[3], gu[3][3], hu[3][3][3];
+        elasticity_exact(pb->problem, D, x, u, gu, hu);
+        vals[-1 - id] = u[b / t.nfs];  // component-major within the facet
+      } else {
+        double p, q[3], fu[3], g;
+        exact_solution(pb->problem, D, x, 1.0, p, q, fu, g);
+        vals[-1 - id] = p;
+      }
     }
   }
 }
@@ -240,7 +268,8 @@ int upload_dirichlet(hdg_problem *pb) {
 int setup_problem(hdg_problem *pb) {
   hdg_context *ctx = pb->ctx;
   std::string err;
-  if (build_ref_tables(pb->mesh.D, pb->mesh.k, pb->tab)) return ctx->fail(HDG_ERR_INVALID, "unsupported D/k");
+  if (build_ref_tables(pb->mesh.D, pb->mesh.k, pb->tab, pb->physics))
+    return ctx->fail(HDG_ERR_INVALID, "unsupported D/k");
   int rc = build_pattern(pb->mesh, pb->pat, err);
   if (rc) return ctx->fail(rc, "%s", err.c_str());
   std::vector<double> packed;
@@ -500,16 +529,24 @@ int hdg_sum_facets(hdg_context *ctx, int nitems, int nfacets, int len, const dou
 // ---------------------------------------------------------------------------
 int hdg_problem_create_cartesian(hdg_context *ctx, int D, const int *cells, const double *domain,
                                  int k, hdg_problem **out) {
+  return hdg_problem_create_cartesian_physics(ctx, D, cells, domain, k, HDG_PHYSICS_DARCY, out);
+}
+
+int hdg_problem_create_cartesian_physics(hdg_context *ctx, int D, const int *cells, const double *domain, int k,
+                                         int physics, hdg_problem **out) {
   if (!ctx) return HDG_ERR_INVALID;
   if (!cells || !domain || !out) return ctx->fail(HDG_ERR_INVALID, "null argument");
+  if (physics != HDG_PHYSICS_DARCY && physics != HDG_PHYSICS_ELASTICITY)
+    return ctx->fail(HDG_ERR_INVALID, "unknown physics %d", physics);
   *out = nullptr;
   cudaSetDevice(ctx->device);
   hdg_problem *pb = new (std::nothrow) hdg_problem();
   if (!pb) return ctx->fail(HDG_ERR_NOMEM, "host allocation failed");
   pb->ctx = ctx;
+  pb->physics = physics;
   for (DBuf *b : pb->device_buffers()) b->stream = ctx->stream;
   std::string err;
-  int rc = build_cartesian_mesh(D, cells, domain, k, pb->mesh, err);
+  int rc = build_cartesian_mesh(D, cells, domain, k, pb->mesh, err, physics == HDG_PHYSICS_ELASTICITY ? D : 1);
   if (rc) {
     delete pb;
     return ctx->fail(rc, "%s", err.c_str());
@@ -593,9 +630,32 @@ int hdg_get_topology(const hdg_problem *pb, int *cell_facets, int *facet_cells, 
   return HDG_OK;
 }
 
+int hdg_set_elasticity(hdg_problem *pb, double tau, double young, int problem) {
+  if (!pb) return HDG_ERR_INVALID;
+  hdg_context *ctx = pb->ctx;
+  if (pb->physics != HDG_PHYSICS_ELASTICITY)
+    return ctx->fail(HDG_ERR_INVALID, "the problem was not created for elasticity");
+  if (!(tau > 0.0) || !std::isfinite(tau)) return ctx->fail(HDG_ERR_INVALID, "tau must be > 0");
+  if (!(young > 0.0) || !std::isfinite(young)) return ctx->fail(HDG_ERR_INVALID, "Young's modulus must be > 0");
+  if (problem != HDG_EPROBLEM_LINEAR && problem != HDG_EPROBLEM_SMOOTH)
+    return ctx->fail(HDG_ERR_INVALID, "unknown problem %d", problem);
+  cudaSetDevice(ctx->device);
+  pb->stab_mode = HDG_STAB_TEXTBOOK;
+  pb->tau = tau;
+  pb->young = young;
+  pb->problem = problem;
+  pb->form_set = true;
+  pb->assembled = pb->solved = pb->recovered = false;
+  int rc = upload_dirichlet(pb);
+  if (rc) return rc;
+  CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return HDG_OK;
+}
+
 int hdg_set_darcy(hdg_problem *pb, int stab_mode, double tau, int problem) {
   if (!pb) return HDG_ERR_INVALID;
   hdg_context *ctx = pb->ctx;
+  if (pb->physics != HDG_PHYSICS_DARCY) return ctx->fail(HDG_ERR_INVALID, "the problem was not created for Darcy");
   if (stab_mode != HDG_STAB_TEXTBOOK && stab_mode != HDG_STAB_OWNER_SIGN)
     return ctx->fail(HDG_ERR_INVALID, "unknown stabilisation %d", stab_mode);
   if (!(tau > 0.0) || !std::isfinite(tau)) return ctx->fail(HDG_ERR_INVALID, "tau must be > 0");
@@ -660,6 +720,8 @@ static int assemble_prepare(hdg_problem *pb, int precision, bool cell_blocks) {
   const RefTables &t = pb->tab;
   const size_t nc = pb->mesh.ncells, n = t.n, ni = t.ni, nf = t.nf;
   const bool mixed = precision != HDG_PREC_FP64;
+  if (precision == HDG_PREC_FF_BLOCK && pb->physics != HDG_PHYSICS_DARCY)
+    return ctx->fail(HDG_ERR_INVALID, "block elimination is built for the Darcy form");
   if (precision == HDG_PREC_FF_BLOCK && !ffblock_supported(t.D, t.k))
     return ctx->fail(HDG_ERR_INVALID, "block elimination is built for D=2, k<=3 and D=3, k<=2");
   const size_t need = precision == HDG_PREC_FP32_REFINED ? condense_mixed_smem((int)ni, (int)nf)
@@ -701,7 +763,7 @@ static cudaError_t assemble_skeleton(hdg_problem *pb) {
                                   &ctx->launches);
   if (e != cudaSuccess || pb->precision == HDG_PREC_FP64) return e;
   // the operator in the SPD frame
-  return launch_pack_cell_blocks(pb->mesh.ncells, 2 * t.D, t.nfd, -1.0, pb->d_S.as<double>(),
+  return launch_pack_cell_blocks(pb->mesh.ncells, 2 * t.D, t.nfd, skeleton_sign(pb), pb->d_S.as<double>(),
                                  pb->d_cellop.as<float>(), ctx->smem_optin, ctx->stream, ctx->num_sms,
                                  &ctx->launches);
 }
@@ -792,7 +854,7 @@ static PcgArgs pcg_args(hdg_problem *pb) {
   a.diag_blk = pb->d_diag_blk.as<int>();
   a.blk_off = pb->d_blk_off.as<int64_t>();
   a.blk_rowlen = pb->d_blk_rowlen.as<int>();
-  a.sign = -1.0;  // the condensed skeleton operator of these forms is negative definite
+  a.sign = skeleton_sign(pb);
   return a;
 }
 
@@ -866,7 +928,7 @@ static int solve_pcg_refined(hdg_problem *pb, double rtol, int maxit, int *it_ou
   oa.scal = pb->d_scal2.as<double>();
   oa.counter = ia.counter;
   oa.nparts = ia.nparts;
-  oa.sign = -1.0;
+  oa.sign = skeleton_sign(pb);
   const int pairs = 8;
   if (!pb->pcg32_graph) {
     cudaGraph_t g;
@@ -1116,13 +1178,14 @@ int hdg_get_free_dof_values(hdg_problem *pb, double *out) {
   if (!pb->recovered) return ctx->fail(HDG_ERR_STATE, "recover first");
   if (!out) return ctx->fail(HDG_ERR_INVALID, "null output");
   cudaSetDevice(ctx->device);
-  const size_t nc = pb->mesh.ncells, ni = pb->tab.ni, nk = pb->tab.nk, D = pb->tab.D;
+  const size_t nc = pb->mesh.ncells, ni = pb->tab.ni;
+  const size_t w1 = first_field_width(pb), w2 = ni - w1;
   const double *u = pb->d_uint.as<double>();
-  // [flux of all cells | pressure of all cells | free skeleton values]
-  CUDA_TRY(ctx, cudaMemcpy2DAsync(out, D * nk * sizeof(double), u, ni * sizeof(double), D * nk * sizeof(double),
-                                  nc, cudaMemcpyDefault, ctx->stream));
-  CUDA_TRY(ctx, cudaMemcpy2DAsync(out + nc * D * nk, nk * sizeof(double), u + D * nk, ni * sizeof(double),
-                                  nk * sizeof(double), nc, cudaMemcpyDefault, ctx->stream));
+  // [first bulk field of all cells | second bulk field of all cells | free skeleton values]
+  CUDA_TRY(ctx, cudaMemcpy2DAsync(out, w1 * sizeof(double), u, ni * sizeof(double), w1 * sizeof(double), nc,
+                                  cudaMemcpyDefault, ctx->stream));
+  CUDA_TRY(ctx, cudaMemcpy2DAsync(out + nc * w1, w2 * sizeof(double), u + w1, ni * sizeof(double),
+                                  w2 * sizeof(double), nc, cudaMemcpyDefault, ctx->stream));
   if (pb->mesh.nfree)
     CUDA_TRY(ctx, cudaMemcpyAsync(out + nc * ni, pb->d_x.ptr, sizeof(double) * pb->mesh.nfree, cudaMemcpyDefault,
                                   ctx->stream));
@@ -1138,8 +1201,12 @@ int hdg_l2_errors(hdg_problem *pb, double *err_flux, double *err_pres) {
   const size_t nc = pb->mesh.ncells;
   CUDA_TRY(ctx, pb->d_errs.reserve(sizeof(double) * 2 * nc));
   CellArgs a = cell_args(pb);
-  CUDA_TRY(ctx, launch_l2_errors(a, pb->d_uint.as<double>(), pb->d_errs.as<double>(), ctx->stream, ctx->num_sms,
-                                 &ctx->launches));
+  if (pb->physics == HDG_PHYSICS_ELASTICITY)
+    CUDA_TRY(ctx, launch_l2_errors_elasticity(a, pb->d_uint.as<double>(), pb->d_errs.as<double>(), ctx->stream,
+                                              ctx->num_sms, &ctx->launches));
+  else
+    CUDA_TRY(ctx, launch_l2_errors(a, pb->d_uint.as<double>(), pb->d_errs.as<double>(), ctx->stream, ctx->num_sms,
+                                   &ctx->launches));
   std::vector<double> h(2 * nc);
   CUDA_TRY(ctx, cudaMemcpyAsync(h.data(), pb->d_errs.ptr, sizeof(double) * 2 * nc, cudaMemcpyDeviceToHost,
                                 ctx->stream));
@@ -1186,7 +1253,8 @@ int hdg_newton_solve(hdg_problem *pb, int solver, double lin_rtol, int lin_maxit
   cudaSetDevice(ctx->device);
   int rc = assemble_prepare(pb, HDG_PREC_FP64, true);
   if (rc) return rc;
-  const size_t nc = pb->mesh.ncells, ni = pb->tab.ni, nk = pb->tab.nk, D = pb->tab.D;
+  const size_t nc = pb->mesh.ncells, ni = pb->tab.ni;
+  const size_t w1 = first_field_width(pb), w2 = ni - w1;
   const size_t nfree = pb->mesh.nfree, nint = nc * ni, ndir = pb->mesh.ndir;
   CUDA_TRY(ctx, pb->d_newton.reserve(sizeof(double) * (nint + nfree + 1)));
   CUDA_TRY(ctx, pb->d_rmax.reserve(sizeof(double) * 2));
@@ -1196,11 +1264,11 @@ int hdg_newton_solve(hdg_problem *pb, int solver, double lin_rtol, int lin_maxit
   CUDA_TRY(ctx, pb->d_x.reserve(sizeof(double) * (nfree ? nfree : 1)));
   double *xint = pb->d_newton.as<double>(), *xskel = xint + nint;
   if (x0) {
-    // Gridap layout [flux of all cells | pressure of all cells | free skeleton] -> cell-major
-    CUDA_TRY(ctx, cudaMemcpy2DAsync(xint, ni * sizeof(double), x0, D * nk * sizeof(double), D * nk * sizeof(double),
-                                    nc, cudaMemcpyDefault, ctx->stream));
-    CUDA_TRY(ctx, cudaMemcpy2DAsync(xint + D * nk, ni * sizeof(double), x0 + nc * D * nk, nk * sizeof(double),
-                                    nk * sizeof(double), nc, cudaMemcpyDefault, ctx->stream));
+    // Gridap layout [first bulk field of all cells | second | free skeleton] -> cell-major
+    CUDA_TRY(ctx, cudaMemcpy2DAsync(xint, ni * sizeof(double), x0, w1 * sizeof(double), w1 * sizeof(double), nc,
+                                    cudaMemcpyDefault, ctx->stream));
+    CUDA_TRY(ctx, cudaMemcpy2DAsync(xint + w1, ni * sizeof(double), x0 + nc * w1, w2 * sizeof(double),
+                                    w2 * sizeof(double), nc, cudaMemcpyDefault, ctx->stream));
     if (nfree)
       CUDA_TRY(ctx, cudaMemcpyAsync(xskel, x0 + nint, sizeof(double) * nfree, cudaMemcpyDefault, ctx->stream));
   } else {

@@ -109,13 +109,24 @@ static void gauss01(int np, std::vector<double> &x, std::vector<double> &w) {
   }
 }
 
-int build_ref_tables(int D, int k, RefTables &t) {
+int build_ref_tables(int D, int k, RefTables &t, int phys) {
   if (D < 2 || D > kMaxD || k < 1 || k > kMaxK) return -1;
   t.D = D;
   t.k = k;
+  t.phys = phys;
   t.nk = ipow(k + 1, D);
-  t.nfd = ipow(k + 1, D - 1);
-  t.ni = (D + 1) * t.nk;
+  t.nfs = ipow(k + 1, D - 1);
+  if (phys == HDG_PHYSICS_ELASTICITY) {
+    // [symmetric stress | displacement] inside, displacement trace on facets
+    t.nsym = D * (D + 1) / 2;
+    t.ni = (t.nsym + D) * t.nk;
+    t.nfd = D * t.nfs;
+  } else {
+    // [flux | pressure] inside, scalar trace on facets
+    t.nsym = 0;
+    t.ni = (D + 1) * t.nk;
+    t.nfd = t.nfs;
+  }
   t.nf = 2 * D * t.nfd;
   t.n = t.ni + t.nf;
   // quadrature degree 2(k+1) as the reference's Measure(., 2*(order+1))
@@ -126,7 +137,7 @@ int build_ref_tables(int D, int k, RefTables &t) {
   if (D - 1 == 0) t.flat.clear();
   std::vector<double> x1, w1;
   gauss01(t.n1, x1, w1);
-  const int nk = t.nk, nfd = t.nfd;
+  const int nk = t.nk, nfd = t.nfs;  // scalar facet basis for the tables
 
   auto eval_cell = [&](const double *xi, double *val, double *grad) {
     for (int a = 0; a < nk; ++a) {
@@ -283,7 +294,7 @@ TableOffsetsF pack_tables_ff(const RefTables &t, std::vector<float> &packed) {
 // facets Dirichlet.
 // ---------------------------------------------------------------------------
 int build_cartesian_mesh(int D, const int *cells, const double *domain, int k,
-                         HostMesh &m, std::string &err) {
+                         HostMesh &m, std::string &err, int ncomp) {
   if (D < 2 || D > kMaxD) {
     err = "D must be 2 or 3";
     return HDG_ERR_INVALID;
@@ -309,7 +320,7 @@ int build_cartesian_mesh(int D, const int *cells, const double *domain, int k,
   m.k = k;
   m.cartesian = true;
   m.ncells = (int)nc;
-  m.nfd = ipow(k + 1, D - 1);
+  m.nfd = ncomp * ipow(k + 1, D - 1);
   for (int d = 0; d < D; ++d) {
     m.cells[d] = cells[d];
     m.domain[2 * d] = domain[2 * d];

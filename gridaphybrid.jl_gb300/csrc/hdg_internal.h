@@ -67,19 +67,22 @@ struct DBuf {
 // ---------------------------------------------------------------------------
 struct RefTables {
   int D = 0, k = 0, nk = 0, nfd = 0, ni = 0, nf = 0, n = 0, n1 = 0, nqv = 0;
+  // physics (HDG_PHYSICS_*), symmetric-tensor components (elasticity), scalar
+  // facet nodes; nfd = DOFs per facet = (facet components) x nfs
+  int phys = 0, nsym = 0, nfs = 0;
   std::vector<int> lat;    // nk x D cell node lattice (Gridap node order)
   std::vector<int> flat;   // nfd x (D-1) facet node lattice
   std::vector<double> M;   // nk x nk      int phi_a phi_b
   std::vector<double> G;   // D x nk x nk  int d_e phi_a phi_b
   std::vector<double> F;   // 2D x nk x nk int_F phi_a phi_b (unit facet measure)
-  std::vector<double> H;   // 2D x nk x nfd int_F phi_a mu_b
-  std::vector<double> L;   // nfd x nfd    int_F mu_a mu_b
+  std::vector<double> H;   // 2D x nk x nfs int_F phi_a mu_b
+  std::vector<double> L;   // nfs x nfs    int_F mu_a mu_b
   std::vector<double> qxi; // nqv x D volume points
   std::vector<double> qw;  // nqv
   std::vector<double> qphi;// nqv x nk
   std::vector<double> Minv;// nk x nk inverse of M (block elimination path)
 };
-int build_ref_tables(int D, int k, RefTables &t);
+int build_ref_tables(int D, int k, RefTables &t, int phys = 0);
 
 // Offsets (in doubles) of each table inside the packed device table buffer.
 struct TableOffsets {
@@ -109,8 +112,9 @@ struct HostMesh {
   std::vector<int> facet_lface;   // nfacets x 2 : local facet index in that cell
   std::vector<int> facet_first_dof; // nfacets: first free DOF or -1
 };
+// ncomp: components of the facet field (1 scalar trace, D displacement trace)
 int build_cartesian_mesh(int D, const int *cells, const double *domain, int k,
-                         HostMesh &m, std::string &err);
+                         HostMesh &m, std::string &err, int ncomp = 1);
 int finish_mesh(HostMesh &m, std::string &err);  // derives facet_cell etc.
 
 // Skeleton CSR pattern and the block maps used by the deterministic gather.
@@ -178,6 +182,8 @@ struct hdg_problem {
   int stab_mode = HDG_STAB_TEXTBOOK;
   int problem = HDG_PROBLEM_LINEAR;
   double tau = 1.0;
+  int physics = HDG_PHYSICS_DARCY;
+  double young = 1.0;  // elasticity: Young's modulus (the per-cell coefficient is the Poisson ratio)
   bool form_set = false, assembled = false, solved = false, recovered = false;
   int precision = HDG_PREC_FP64;
   double timings[5] = {0, 0, 0, 0, 0};

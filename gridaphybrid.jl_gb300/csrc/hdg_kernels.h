@@ -50,9 +50,97 @@ HDG_HD void exact_solution(int problem, int D, const double *x, double kappa,
   }
 }
 
+// Linear elasticity manufactured solutions (test/LinearElasticityHDGTests.jl):
+// displacement u, gradient gu[i][j] = du_i/dx_j, Hessian hu[i][j][k].
+HDG_HD void elasticity_exact(int problem, int D, const double *x, double *u, double (*gu)[3],
+                             double (*hu)[3][3]) {
+  const double pi = 3.14159265358979323846;
+  for (int i = 0; i < 3; ++i) {
+    u[i] = 0.0;
+    for (int j = 0; j < 3; ++j) {
+      gu[i][j] = 0.0;
+      for (int k = 0; k < 3; ++k) hu[i][j][k] = 0.0;
+    }
+  }
+  if (problem == 0) {  // linear: u = (x+2y, 2x+y) (:48-50); 3D (x+2y, 2x+y+z, y+3z)
+    u[0] = x[0] + 2 * x[1];
+    u[1] = 2 * x[0] + x[1];
+    gu[0][0] = 1; gu[0][1] = 2; gu[1][0] = 2; gu[1][1] = 1;
+    if (D == 3) {
+      u[1] += x[2];
+      u[2] = x[1] + 3 * x[2];
+      gu[1][2] = 1; gu[2][1] = 1; gu[2][2] = 3;
+    }
+  } else if (D == 2) {  // (:52-57)
+    const double X = x[0], Y = x[1];
+    const double A = sin(pi * X) * (1 - X), dA = pi * cos(pi * X) * (1 - X) - sin(pi * X),
+                 ddA = -pi * pi * sin(pi * X) * (1 - X) - 2 * pi * cos(pi * X);
+    const double B = Y - 1.5 * Y * Y + 0.5 * Y * Y * Y, dB = 1 - 3 * Y + 1.5 * Y * Y, ddB = -3 + 3 * Y;
+    u[0] = 10 * A * B;
+    gu[0][0] = 10 * dA * B;
+    gu[0][1] = 10 * A * dB;
+    hu[0][0][0] = 10 * ddA * B;
+    hu[0][0][1] = hu[0][1][0] = 10 * dA * dB;
+    hu[0][1][1] = 10 * A * ddB;
+  } else {  // (sin pi x, cos pi y, xyz)
+    const double X = x[0], Y = x[1], Z = x[2];
+    u[0] = sin(pi * X);
+    u[1] = cos(pi * Y);
+    u[2] = X * Y * Z;
+    gu[0][0] = pi * cos(pi * X);
+    gu[1][1] = -pi * sin(pi * Y);
+    gu[2][0] = Y * Z; gu[2][1] = X * Z; gu[2][2] = X * Y;
+    hu[0][0][0] = -pi * pi * sin(pi * X);
+    hu[1][1][1] = -pi * pi * cos(pi * Y);
+    hu[2][0][1] = hu[2][1][0] = Z;
+    hu[2][0][2] = hu[2][2][0] = Y;
+    hu[2][1][2] = hu[2][2][1] = X;
+  }
+}
+
+// sigma = A^{-1}(eps) for A(s) = (1+nu)/E s - nu/E tr(s) I (:15-38):
+// 2 mu eps + lam tr(eps) I with mu = E/(2(1+nu)), lam = nu E/((1+nu)(1+nu-D nu))
+HDG_HD void elasticity_lame(int D, double E, double nu, double &mu, double &lam) {
+  mu = E / (2.0 * (1.0 + nu));
+  lam = nu * E / ((1.0 + nu) * (1.0 + nu - D * nu));
+}
+
+// f = div sigma_exact
+HDG_HD void elasticity_force(int D, double E, double nu, const double (*hu)[3][3], double *f) {
+  double mu, lam;
+  elasticity_lame(D, E, nu, mu, lam);
+  for (int i = 0; i < D; ++i) {
+    double v = 0.0;
+    for (int j = 0; j < D; ++j) v += mu * (hu[i][j][j] + hu[j][i][j]);
+    for (int k = 0; k < D; ++k) v += lam * hu[k][i][k];
+    f[i] = v;
+  }
+}
+
+// the (i, j) pair of symmetric-tensor component c (upper triangle, row by row)
+HDG_HD void sym_pair(int D, int c, int &i, int &j) {
+  if (D == 2) {
+    i = c == 2 ? 1 : 0;
+    j = c == 0 ? 0 : 1;
+  } else {
+    const int ii[6] = {0, 0, 0, 1, 1, 2}, jj[6] = {0, 1, 2, 1, 2, 2};
+    i = ii[c];
+    j = jj[c];
+  }
+}
+
+// entry (r, s) of the symmetric unit tensor of component c
+HDG_HD double sym_unit(int D, int c, int r, int s) {
+  int i, j;
+  sym_pair(D, c, i, j);
+  return ((r == i && s == j) || (r == j && s == i)) ? 1.0 : 0.0;
+}
+
 // Everything the cell kernels read, as plain device pointers.
 struct CellArgs {
   int D, k, nk, nfd, ni, nf, n, nqv, ncells;
+  int phys, nsym, nfs;  // physics, symmetric-tensor components, scalar facet nodes
+  double young;         // elasticity: Young's modulus (kappa holds the Poisson ratio)
   const double *M, *G, *F, *H, *L, *qxi, *qw, *qphi;  // reference tables
   const double *origin, *jac, *kappa;                // per cell
   const int *cell_facets, *facet_cell;               // topology
@@ -249,6 +337,14 @@ cudaError_t launch_newton_residual(const CellArgs &a, const AssembleArgs &as, co
                                    cudaStream_t s, int num_sms, long long *launches);
 cudaError_t launch_newton_update(size_t count, double *x, const double *dx, cudaStream_t s, int num_sms,
                                  long long *launches);
+
+// Linear elasticity HDG cells: blocks in FP64 (A, b) or as float-float pairs
+// (the entries computed in FP64 and split), and the stress / displacement L2
+// error contributions per cell (errs: 2 per cell).
+cudaError_t launch_integrate_elasticity(const CellArgs &a, double *A, double *b, float *Ahi, float *Alo, float *bhi,
+                                        float *blo, cudaStream_t s, int num_sms, long long *launches);
+cudaError_t launch_l2_errors_elasticity(const CellArgs &a, const double *uint, double *errs, cudaStream_t s,
+                                        int num_sms, long long *launches);
 
 // dense LU solve of a CSR system (small n), one CTA
 cudaError_t launch_dense_solve(int n, const int64_t *rowptr, const int *colind,

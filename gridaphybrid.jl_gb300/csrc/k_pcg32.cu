@@ -473,7 +473,7 @@ static size_t cellop_dyn_smem(int nstage) {
 }
 
 #define HDG_CELLOP_CASES(X) \
-  X(4, 2) X(4, 3) X(4, 4) X(4, 5) X(6, 4) X(6, 9) X(6, 16) X(6, 25)
+  X(4, 2) X(4, 3) X(4, 4) X(4, 5) X(4, 6) X(4, 8) X(6, 4) X(6, 9) X(6, 12) X(6, 16) X(6, 25)
 
 bool cellop_supported(int nl, int nfd) {
 #define X(L, F) \
@@ -581,7 +581,10 @@ cudaError_t launch_outer_update(const OuterArgs &a, const float *e, cudaStream_t
     case 3: outer_residual_kernel<3><<<a.nparts, kPcgThreads, 0, s>>>(a); break;
     case 4: outer_residual_kernel<4><<<a.nparts, kPcgThreads, 0, s>>>(a); break;
     case 5: outer_residual_kernel<5><<<a.nparts, kPcgThreads, 0, s>>>(a); break;
+    case 6: outer_residual_kernel<6><<<a.nparts, kPcgThreads, 0, s>>>(a); break;
+    case 8: outer_residual_kernel<8><<<a.nparts, kPcgThreads, 0, s>>>(a); break;
     case 9: outer_residual_kernel<9><<<a.nparts, kPcgThreads, 0, s>>>(a); break;
+    case 12: outer_residual_kernel<12><<<a.nparts, kPcgThreads, 0, s>>>(a); break;
     case 16: outer_residual_kernel<16><<<a.nparts, kPcgThreads, 0, s>>>(a); break;
     case 25: outer_residual_kernel<25><<<a.nparts, kPcgThreads, 0, s>>>(a); break;
     default: return cudaErrorInvalidValue;

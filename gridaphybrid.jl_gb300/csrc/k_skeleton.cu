@@ -126,7 +126,7 @@ cudaError_t launch_assemble(const AssembleArgs &a, const double *S, const double
     if (false) {
     }
     HDG_ASM(4, 2) HDG_ASM(4, 3) HDG_ASM(4, 4) HDG_ASM(4, 5) HDG_ASM(6, 1) HDG_ASM(6, 4) HDG_ASM(6, 9)
-    HDG_ASM(6, 16) HDG_ASM(6, 25) HDG_ASM(4, 1)
+    HDG_ASM(6, 16) HDG_ASM(6, 25) HDG_ASM(4, 1) HDG_ASM(4, 6) HDG_ASM(4, 8) HDG_ASM(6, 12)
     else return cudaErrorInvalidValue;
 #undef HDG_ASM
     ++*launches;
@@ -400,7 +400,10 @@ static cudaError_t spmv_dispatch(const PcgArgs &a, const V *val, const double *p
     HDG_SPMV_CASE(3)
     HDG_SPMV_CASE(4)
     HDG_SPMV_CASE(5)
+    HDG_SPMV_CASE(6)
+    HDG_SPMV_CASE(8)
     HDG_SPMV_CASE(9)
+    HDG_SPMV_CASE(12)
     HDG_SPMV_CASE(16)
     HDG_SPMV_CASE(25)
 #undef HDG_SPMV_CASE
@@ -415,7 +418,9 @@ static cudaError_t spmv_any(const PcgArgs &a, const double *po, double *pn, cuda
 }
 
 bool pcg_supports_nfd(int nfd) {
-  return nfd == 2 || nfd == 3 || nfd == 4 || nfd == 5 || nfd == 9 || nfd == 16 || nfd == 25;
+  // scalar traces (k+1)^(D-1); displacement traces D (k+1)^(D-1): 4, 6, 8 (2D), 12 (3D k=1)
+  return nfd == 2 || nfd == 3 || nfd == 4 || nfd == 5 || nfd == 6 || nfd == 8 || nfd == 9 || nfd == 12 ||
+         nfd == 16 || nfd == 25;
 }
 
 cudaError_t launch_spmv(const PcgArgs &a, cudaStream_t s, long long *launches) {

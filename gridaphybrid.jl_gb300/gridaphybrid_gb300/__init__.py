@@ -9,18 +9,18 @@ from ._lib import Context, HdgError, default_context
 from .maps import (ArrayBlock, BackwardStaticCondensationMap, MatrixBlock,
                    StaticCondensationMap, SumFacetsMap, VectorBlock, densify,
                    evaluate, lazy_map, return_cache)
-from .operators import (CartesianDiscreteModel, DarcyHDG, FEFunction, FESolver,
+from .operators import (CartesianDiscreteModel, DarcyHDG, ElasticityHDG, FEFunction, FESolver,
                         HybridAffineFEOperator, HybridFEOperator, MultiFieldFESpace,
                         NLSolver, ReferenceFE, Skeleton, TestFESpace, TrialFESpace,
-                        Triangulation, darcy_spaces, get_cell_normal_vector,
+                        Triangulation, darcy_spaces, elasticity_spaces, get_cell_normal_vector,
                         get_cell_owner_normal_vector, solve, solve_)
 
 __all__ = [
     "ArrayBlock", "BackwardStaticCondensationMap", "CartesianDiscreteModel", "Context",
-    "DarcyHDG", "FEFunction", "FESolver", "HdgError", "HybridAffineFEOperator", "HybridFEOperator",
+    "DarcyHDG", "ElasticityHDG", "FEFunction", "FESolver", "HdgError", "HybridAffineFEOperator", "HybridFEOperator",
     "NLSolver", "MatrixBlock", "MultiFieldFESpace",
     "ReferenceFE", "Skeleton", "StaticCondensationMap", "SumFacetsMap", "TestFESpace",
     "TrialFESpace", "Triangulation", "VectorBlock", "darcy_spaces", "default_context",
-    "densify", "evaluate", "get_cell_normal_vector", "get_cell_owner_normal_vector",
+    "densify", "elasticity_spaces", "evaluate", "get_cell_normal_vector", "get_cell_owner_normal_vector",
     "lazy_map", "return_cache", "solve", "solve_",
 ]

@@ -5,6 +5,7 @@ present, every call raises.
 """
 import ctypes
 import os
+import weakref
 
 import numpy as np
 
@@ -27,6 +28,10 @@ HDG_STAB_OWNER_SIGN = 1
 HDG_PROBLEM_REF_LINEAR = 0
 HDG_PROBLEM_LINEAR = 1
 HDG_PROBLEM_SIN = 2
+HDG_PHYSICS_DARCY = 0
+HDG_PHYSICS_ELASTICITY = 1
+HDG_EPROBLEM_LINEAR = 0
+HDG_EPROBLEM_SMOOTH = 1
 HDG_SOLVER_PCG = 0
 HDG_SOLVER_DIRECT = 1
 
@@ -55,6 +60,8 @@ SIGNATURES = {
     "hdg_static_condensation_noalloc": (_i, [_vp, _i, _i, _i, _vp, _vp, _vp, _vp, _vp]),
     "hdg_problem_create_cartesian": (_i, [_vp, _i, _vp, _vp, _i, ctypes.POINTER(_vp)]),
     "hdg_problem_create": (_i, [_vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp, ctypes.POINTER(_vp)]),
+    "hdg_problem_create_cartesian_physics": (_i, [_vp, _i, _vp, _vp, _i, _i, ctypes.POINTER(_vp)]),
+    "hdg_set_elasticity": (_i, [_vp, _d, _d, _i]),
     "hdg_problem_destroy": (_i, [_vp]),
     "hdg_problem_info": (_i, [_vp, _vp]),
     "hdg_get_topology": (_i, [_vp, _vp, _vp, _vp]),
@@ -152,15 +159,26 @@ def ptr(a):
 
 
 class Context:
-    """One GPU + stream (hdg_context)."""
+    """One GPU + stream (hdg_context).  Objects that live on the context
+    (problems, batches) register themselves and are released before it, so
+    the context is never destroyed under them (e.g. when the interpreter
+    tears down its objects in arbitrary order)."""
 
     def __init__(self, device=0):
         self.lib = load()
+        self._children = weakref.WeakSet()
         h = ctypes.c_void_p()
         rc = self.lib.hdg_context_create(device, ctypes.byref(h))
         if rc != HDG_OK:
             raise HdgError(rc, "hdg_context_create(device=%d) failed: no usable sm_103a GPU" % device)
         self.handle = h
+
+    def register(self, obj):
+        self._children.add(obj)
+
+    @property
+    def alive(self):
+        return getattr(self, "handle", None) is not None
 
     def check(self, rc):
         if rc != HDG_OK:
@@ -176,6 +194,11 @@ class Context:
 
     def close(self):
         if getattr(self, "handle", None):
+            for child in list(getattr(self, "_children", ())):
+                try:
+                    child.close()
+                except Exception:
+                    pass
             self.lib.hdg_context_destroy(self.handle)
             self.handle = None
 

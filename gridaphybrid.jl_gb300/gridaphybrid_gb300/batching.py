@@ -35,6 +35,7 @@ class Batch:
         h = ctypes.c_void_p()
         c.check(c.lib.hdg_batch_create(c.handle, len(self.pbs), handles, ctypes.byref(h)))
         self.h = h
+        c.register(self)
 
     @property
     def cells(self):
@@ -84,7 +85,8 @@ class Batch:
 
     def close(self):
         if getattr(self, "h", None):
-            self.ctx.lib.hdg_batch_destroy(self.h)
+            if self.ctx.alive:
+                self.ctx.lib.hdg_batch_destroy(self.h)
             self.h = None
         for pb in getattr(self, "pbs", []):
             pb.close()

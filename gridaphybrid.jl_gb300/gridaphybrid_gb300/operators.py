@@ -24,6 +24,7 @@ from . import _lib
 
 lagrangian = "lagrangian"
 VectorValue = "VectorValue"
+SymTensorValue = "SymTensorValue"
 Float64 = "Float64"
 
 
@@ -157,17 +158,54 @@ class DarcyHDG:
         self.kappa = None if kappa is None else np.ascontiguousarray(kappa, dtype=np.float64)
 
 
+class ElasticityHDG:
+    """The linear elasticity HDG form of test/LinearElasticityHDGTests.jl:140-150
+    (without the P_m projection, bulk_to_skeleton_projection=false):
+      v (.) A(sigma) + (div v).u - w.(div sigma) on Omega,
+      -(v.n).uhat + tau w.(u - uhat) + mu.(sigma.n) - tau mu.(u - uhat) on dK,
+    compliance A(s) = (1+nu)/E s - nu/E tr(s) I (:15-38) with a per-cell
+    Poisson ratio nu; `problem` selects the manufactured displacement
+    ("linear" :48-50 or "smooth" :52-57) giving f = div sigma_exact and the
+    Dirichlet data.  tau defaults to the reference's 1/h (cells per side)."""
+
+    PROBLEMS = {"linear": _lib.HDG_EPROBLEM_LINEAR, "smooth": _lib.HDG_EPROBLEM_SMOOTH}
+    physics = _lib.HDG_PHYSICS_ELASTICITY
+
+    def __init__(self, tau=None, E=1.0, nu=None, problem="smooth"):
+        self.tau = None if tau is None else float(tau)
+        self.E = float(E)
+        self.problem = self.PROBLEMS[problem]
+        self.nu = None if nu is None else np.ascontiguousarray(nu, dtype=np.float64)
+
+    def apply(self, c, pb, model):
+        tau = float(model.partition[0]) if self.tau is None else self.tau
+        c.check(c.lib.hdg_set_elasticity(pb.h, tau, self.E, self.problem))
+        c.check(c.lib.hdg_set_permeability(pb.h, _lib.ptr(self.nu)))
+
+
+DarcyHDG.physics = _lib.HDG_PHYSICS_DARCY
+
+
+def _darcy_apply(self, c, pb, model):
+    c.check(c.lib.hdg_set_darcy(pb.h, self.stab, self.tau, self.problem))
+    c.check(c.lib.hdg_set_permeability(pb.h, _lib.ptr(self.kappa)))
+
+
+DarcyHDG.apply = _darcy_apply
+
+
 class _Problem:
     """Owns an hdg_problem handle."""
 
-    def __init__(self, ctx, model, k):
+    def __init__(self, ctx, model, k, physics=_lib.HDG_PHYSICS_DARCY):
         self.ctx = ctx
         h = ctypes.c_void_p()
         cells = np.array(model.partition, dtype=np.int32)
         dom = np.array(model.domain, dtype=np.float64)
-        ctx.check(ctx.lib.hdg_problem_create_cartesian(ctx.handle, model.D, _lib.ptr(cells),
-                                                       _lib.ptr(dom), k, ctypes.byref(h)))
+        ctx.check(ctx.lib.hdg_problem_create_cartesian_physics(ctx.handle, model.D, _lib.ptr(cells),
+                                                               _lib.ptr(dom), k, physics, ctypes.byref(h)))
         self.h = h
+        ctx.register(self)
         info = np.zeros(8, dtype=np.int64)
         ctx.check(ctx.lib.hdg_problem_info(h, _lib.ptr(info)))
         (self.ncells, self.nfacets, self.ni, self.nf, self.nfree, self.ndir, self.nnz,
@@ -183,7 +221,8 @@ class _Problem:
 
     def close(self):
         if self.h:
-            self.ctx.lib.hdg_problem_destroy(self.h)
+            if self.ctx.alive:  # a destroyed context took its device memory with it
+                self.ctx.lib.hdg_problem_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -201,7 +240,7 @@ class HybridAffineFEOperator:
     def __init__(self, weakform, trial, test, bulk_fields, skeleton_fields,
                  precision=_lib.HDG_PREC_FP64, context=None):
         if list(bulk_fields) != [1, 2] or list(skeleton_fields) != [3]:
-            raise ValueError("the Darcy HDG operator expects bulk_fields=[1,2] (flux, pressure) "
+            raise ValueError("the HDG operators expect bulk_fields=[1,2] (flux/stress, pressure/displacement) "
                              "and skeleton_fields=[3] (trace)")
         self.weakform, self.trial, self.test = weakform, trial, test
         self.bulk_fields, self.skeleton_fields = list(bulk_fields), list(skeleton_fields)
@@ -213,10 +252,9 @@ class HybridAffineFEOperator:
         self.k = orders.pop()
         self.model = model
         self.ctx = context or _lib.default_context()
-        self.pb = _Problem(self.ctx, model, self.k)
+        self.pb = _Problem(self.ctx, model, self.k, weakform.physics)
         c = self.ctx
-        c.check(c.lib.hdg_set_darcy(self.pb.h, weakform.stab, weakform.tau, weakform.problem))
-        c.check(c.lib.hdg_set_permeability(self.pb.h, _lib.ptr(weakform.kappa)))
+        weakform.apply(c, self.pb, model)
         self.info = np.zeros(self.pb.ncells, dtype=np.int32)
         c.check(c.lib.hdg_assemble(self.pb.h, precision, _lib.ptr(self.info)))
 
@@ -284,10 +322,8 @@ class HybridFEOperator:
         self.k = orders.pop()
         self.model = trial[0].trian.model
         self.ctx = context or _lib.default_context()
-        self.pb = _Problem(self.ctx, self.model, self.k)
-        c = self.ctx
-        c.check(c.lib.hdg_set_darcy(self.pb.h, weakform.stab, weakform.tau, weakform.problem))
-        c.check(c.lib.hdg_set_permeability(self.pb.h, _lib.ptr(weakform.kappa)))
+        self.pb = _Problem(self.ctx, self.model, self.k, weakform.physics)
+        weakform.apply(self.ctx, self.pb, self.model)
 
     def num_free_dofs(self):
         return self.pb.ncells * self.pb.ni + self.pb.nfree
@@ -342,6 +378,21 @@ def solve_(xh0, solver, op):
         for i, r in enumerate(hist):
             print("Newton %3d  residual %.3e" % (i, r))
     return HybridFEFunction(op, it.value, float(hist[-1])), {"iterations": it.value, "residual_norms": hist}
+
+
+def elasticity_spaces(model, k):
+    """The spaces of the elasticity HDG test with matching orders: symmetric
+    stress Q_k, displacement Q_k, displacement trace Q_k with Dirichlet facets
+    on the whole boundary (test/LinearElasticityHDGTests.jl:79-110; the
+    reference uses P spaces and a k+1 displacement with the P_m projection)."""
+    Omega = Triangulation(model)
+    Gamma = Triangulation(model, model.D - 1)
+    V = TestFESpace(Omega, ReferenceFE(lagrangian, SymTensorValue, k), conformity="L2")
+    W = TestFESpace(Omega, ReferenceFE(lagrangian, VectorValue, k), conformity="L2")
+    M = TestFESpace(Gamma, ReferenceFE(lagrangian, VectorValue, k), conformity="L2", dirichlet_tags="boundary")
+    Y = MultiFieldFESpace([V, W, M])
+    X = MultiFieldFESpace([TrialFESpace(V), TrialFESpace(W), TrialFESpace(M, "u_exact")])
+    return X, Y
 
 
 def darcy_spaces(model, k):

@@ -58,6 +58,15 @@ extern "C" {
 #define HDG_PROBLEM_LINEAR 1     /* p = x+y[+z], q = -kappa grad p, f = 0 */
 #define HDG_PROBLEM_SIN 2        /* p = prod sin(pi x_d), q = -kappa grad p, f = div q */
 
+/* Physics of a problem (fixes the field layout at creation). */
+#define HDG_PHYSICS_DARCY 0      /* flux (D comps) + pressure inside, scalar trace (test/DarcyHDGTests.jl) */
+#define HDG_PHYSICS_ELASTICITY 1 /* symmetric stress + displacement inside, displacement trace
+                                    (test/LinearElasticityHDGTests.jl) */
+
+/* Built-in manufactured elasticity problems. */
+#define HDG_EPROBLEM_LINEAR 0 /* u = (x+2y, 2x+y) (:48-50); 3D (x+2y, 2x+y+z, y+3z) */
+#define HDG_EPROBLEM_SMOOTH 1 /* u = (10 sin(pi x)(1-x)(y-y^2)(1-y/2), 0) (:52-57); 3D (sin pi x, cos pi y, xyz) */
+
 /* Skeleton solvers. */
 #define HDG_SOLVER_PCG 0        /* facet-block-Jacobi PCG on -S (SPD forms) */
 #define HDG_SOLVER_DIRECT 1     /* dense LU with partial pivoting (small systems, any form) */
@@ -156,6 +165,13 @@ int hdg_problem_create(hdg_context *ctx, int D, int k, int ncells, int nfacets,
                        const double *cell_origin, const double *cell_jacobian,
                        const int *cell_facets, const int *facet_dofs,
                        hdg_problem **out);
+/* The same Cartesian mesh for a given physics (HDG_PHYSICS_*): the facet
+ * space has one (Darcy) or D (elasticity) components per facet node,
+ * component-major within a facet as Gridap's vector-valued Lagrangian spaces
+ * (src/tmp_fixes_symmetric_valued_lagrangian_reffes.jl:104-125). */
+int hdg_problem_create_cartesian_physics(hdg_context *ctx, int D, const int *cells,
+                                         const double *domain, int k, int physics,
+                                         hdg_problem **out);
 int hdg_problem_destroy(hdg_problem *pb);
 
 /* info[0..7] = ncells, nfacets, ni, nf, nfree, ndirichlet, nnz, nfacet_dofs */
@@ -174,6 +190,9 @@ int hdg_get_topology(const hdg_problem *pb, int *cell_facets, int *facet_cells,
  * in the flux mass term): stab_mode HDG_STAB_*, tau > 0, problem HDG_PROBLEM_*
  * (sources + Dirichlet data).  kappa: ncells values (NULL = 1). */
 int hdg_set_darcy(hdg_problem *pb, int stab_mode, double tau, int problem);
+/* The per-cell coefficient (ncells values): the permeability kappa of the
+ * Darcy form (NULL = 1), or the Poisson ratio nu of the elasticity form
+ * (NULL = 0.3). */
 int hdg_set_permeability(hdg_problem *pb, const double *kappa);
 /* Dirichlet values of the trial skeleton space, ndirichlet values
  * (TrialFESpace(M, p), test/DarcyHDGTests.jl:52).  hdg_set_darcy interpolates
@@ -215,6 +234,17 @@ int hdg_solve_skeleton(hdg_problem *pb, int solver, double rtol, int maxit,
 int hdg_newton_solve(hdg_problem *pb, int solver, double lin_rtol, int lin_maxit, double ftol,
                      int max_iters, const double *x0, double *res_norms, int *iters);
 
+/* The linear elasticity HDG form of test/LinearElasticityHDGTests.jl:140-150
+ * without the P_m projection (bulk_to_skeleton_projection=false):
+ *   v (.) A(sigma) + (div v).u - w.(div sigma) on Omega,
+ *   -(v.n).uhat + tau w.(u - uhat) + mu.(sigma.n) - tau mu.(u - uhat) on dK,
+ * compliance A(s) = (1+nu)/E s - nu/E tr(s) I (:15-38) with the per-cell
+ * Poisson ratio given by hdg_set_permeability (the per-cell coefficient),
+ * f = div sigma_exact and Dirichlet data u_exact (problem: HDG_EPROBLEM_*).
+ * The problem must have been created with HDG_PHYSICS_ELASTICITY.
+ * hdg_l2_errors then returns the stress and displacement errors. */
+int hdg_set_elasticity(hdg_problem *pb, double tau, double young, int problem);
+
 /* Options of the fast precisions' skeleton solve (an FP32 PCG inside FP64
  * residual refinement; no reference counterpart).  delta: the relative
  * residual reduction the FP32 iterations make between two FP64 residuals
@@ -228,9 +258,10 @@ int hdg_set_refinement(hdg_problem *pb, double delta, int keep_direction);
 int hdg_recover(hdg_problem *pb);
 
 /* Free DOF values of the multi-field trial space in Gridap's consecutive
- * layout [flux of all cells | pressure of all cells | free skeleton DOFs]
- * (FEFunction(op.trial, free_dof_values), :99).  Length
- * ncells*ni + nfree. */
+ * layout [first bulk field of all cells | second bulk field of all cells |
+ * free skeleton DOFs] (FEFunction(op.trial, free_dof_values), :99): Darcy
+ * [flux | pressure | trace], elasticity [stress | displacement | trace].
+ * Length ncells*ni + nfree. */
 int hdg_get_free_dof_values(hdg_problem *pb, double *out);
 /* Interior values per cell (ncells x ni) and free skeleton values (nfree). */
 int hdg_get_cell_interior_values(hdg_problem *pb, double *out);
