@@ -259,6 +259,50 @@ def run_batching(args, ctx):
     return out
 
 
+def run_elasticity(args, ctx):
+    """The precision workload: 3D linear elasticity HDG on the unit cube,
+    E = 1, nu ~ U(0.2, 0.45) per cell (seed 0), u = (sin pi x, cos pi y, xyz),
+    tau = 1/h; FP32 LU + float-float refinement against the FP64 path on the
+    GPU (both solved to 1e-12), and the FP64 path against the C oracle on a
+    smaller mesh.  Cell order k = 1 (n = 144 per cell): the k = 2 cell block
+    (n = 405) exceeds the shared-memory condensation kernels."""
+    import gridaphybrid_gb300 as gh
+    from gridaphybrid_gb300 import _lib
+    n = args.elasticity_n
+    k = 1
+    nu = np.random.default_rng(0).uniform(0.2, 0.45, size=n ** 3)
+    model = gh.CartesianDiscreteModel((0, 1) * 3, (n,) * 3)
+    X, Y = gh.elasticity_spaces(model, k)
+    out = {"workload": "3D linear elasticity HDG %d^3 hex, k=%d (sym stress 6x8 + displacement 3x8 inside, "
+                       "3x4 per facet), E=1, nu~U(0.2,0.45) per cell, u=(sin pi x, cos pi y, xyz), tau=1/h" % (n, k),
+           "cells": n ** 3}
+    sols = {}
+    for name, prec in (("fp64", _lib.HDG_PREC_FP64), ("fp32_refined", _lib.HDG_PREC_FP32_REFINED)):
+        form = gh.ElasticityHDG(nu=nu, problem="smooth")
+        op = gh.HybridAffineFEOperator(form, X, Y, [1, 2], [3], precision=prec, context=ctx)
+        xh = gh.solve(op, solver="pcg", rtol=1e-12)
+        h = op.pb.h
+        t0 = time.perf_counter()
+        reps = 2
+        for _ in range(reps):
+            ctx.check(ctx.lib.hdg_assemble(h, prec, None))
+            it, rel = ctypes.c_int(), ctypes.c_double()
+            ctx.check(ctx.lib.hdg_solve_skeleton(h, _lib.HDG_SOLVER_PCG, 1e-10, 20000, ctypes.byref(it),
+                                                 ctypes.byref(rel)))
+            ctx.check(ctx.lib.hdg_recover(h))
+        ctx.synchronize()
+        ms = 1000.0 * (time.perf_counter() - t0) / reps
+        es, eu = xh.l2_errors()
+        sols[name] = xh.free_dof_values.copy()
+        out[name] = {"ms_per_solve": ms, "cells_per_s": n ** 3 / (ms / 1000.0), "pcg_iters": xh.iterations,
+                     "err_sigma_vs_exact": es, "err_u_vs_exact": eu}
+        op.pb.close()
+    ref = sols["fp64"]
+    out["fp32_refined"]["rel_err_vs_fp64"] = float(np.abs(sols["fp32_refined"] - ref).max() / np.abs(ref).max())
+    out["fp32_refined"]["speedup_vs_fp64"] = out["fp64"]["ms_per_solve"] / out["fp32_refined"]["ms_per_solve"]
+    return out
+
+
 def run_gpu(args, rank=0, nranks=1, device=0):
     """One replica per GPU: every rank runs the whole workload on its own GPU;
     the timed regions are bracketed by barriers and the maximum over ranks is
@@ -376,6 +420,7 @@ def run_gpu(args, rank=0, nranks=1, device=0):
         lib.hdg_problem_destroy(h)
         return
     batching_out = run_batching(args, ctx) if args.batch_problems > 0 else None
+    elasticity_out = run_elasticity(args, ctx) if args.elasticity_n > 0 else None
     serving_out = run_serving(args, prec, precs["fp64"]) if args.serve_seconds > 0 else None
 
     peaks, peak_kind = measured_peaks()
@@ -428,6 +473,8 @@ def run_gpu(args, rank=0, nranks=1, device=0):
         line["fp64_compare"] = compare
     if batching_out:
         line["batching"] = batching_out
+    if elasticity_out:
+        line["elasticity"] = elasticity_out
     if serving_out:
         line["serving"] = serving_out
     if not args.no_cpu_baseline:
@@ -457,6 +504,8 @@ def main():
     ap.add_argument("--serve-slots", type=int, default=8)
     ap.add_argument("--batch-problems", type=int, default=64,
                     help="problems of the batching workload (0 skips it)")
+    ap.add_argument("--elasticity-n", type=int, default=24,
+                    help="cells per side of the elasticity precision workload (0 skips it)")
     ap.add_argument("--n-side", type=int, default=32,
                     help="cells per side (32 is the benchmark workload; smaller sizes are for profiling)")
     args = ap.parse_args()

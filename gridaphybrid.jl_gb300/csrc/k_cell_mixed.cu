@@ -303,6 +303,11 @@ cudaError_t launch_condense_mixed(int ncells, int ni, int nf, const float *Ahi, 
   HDG_RT_CASE(32, 24, 16, 8)
   HDG_RT_CASE(27, 12, 8, 8)
   HDG_RT_CASE(12, 8, 4, 8)
+  // linear elasticity cells: 3D k=1, 2D k=1..3
+  HDG_RT_CASE(72, 72, 16, 16)
+  HDG_RT_CASE(20, 16, 8, 8)
+  HDG_RT_CASE(45, 24, 16, 8)
+  HDG_RT_CASE(80, 32, 16, 16)
 #undef HDG_RT_CASE
   const size_t smem = condense_mixed_smem(ni, nf);
   if (smem > 48 * 1024) {
