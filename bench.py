@@ -262,44 +262,57 @@ def run_batching(args, ctx):
 def run_elasticity(args, ctx):
     """The precision workload: 3D linear elasticity HDG on the unit cube,
     E = 1, nu ~ U(0.2, 0.45) per cell (seed 0), u = (sin pi x, cos pi y, xyz),
-    tau = 1/h; FP32 LU + float-float refinement against the FP64 path on the
-    GPU (both solved to 1e-12), and the FP64 path against the C oracle on a
-    smaller mesh.  Cell order k = 1 (n = 144 per cell): the k = 2 cell block
-    (n = 405) exceeds the shared-memory condensation kernels."""
+    tau = 1/h, cell order k (default 2: n = 405 DOFs per cell).  The fast path
+    (float-float block elimination on the FP32 pipes + FP32 skeleton PCG with
+    FP64 residual refinement; at k = 1 also the FP32 LU + refinement path)
+    against the plain FP64 path on the GPU (FP64 block elimination at k = 2,
+    where the cell block exceeds the shared-memory LU), all solved to 1e-12."""
     import gridaphybrid_gb300 as gh
     from gridaphybrid_gb300 import _lib
-    n = args.elasticity_n
-    k = 1
+    n, k = args.elasticity_n, args.elasticity_k
+    nk, nfs = (k + 1) ** 3, (k + 1) ** 2
     nu = np.random.default_rng(0).uniform(0.2, 0.45, size=n ** 3)
     model = gh.CartesianDiscreteModel((0, 1) * 3, (n,) * 3)
     X, Y = gh.elasticity_spaces(model, k)
-    out = {"workload": "3D linear elasticity HDG %d^3 hex, k=%d (sym stress 6x8 + displacement 3x8 inside, "
-                       "3x4 per facet), E=1, nu~U(0.2,0.45) per cell, u=(sin pi x, cos pi y, xyz), tau=1/h" % (n, k),
+    out = {"workload": "3D linear elasticity HDG %d^3 hex, k=%d (sym stress 6x%d + displacement 3x%d inside, "
+                       "3x%d per facet, n=%d per cell), E=1, nu~U(0.2,0.45) per cell, u=(sin pi x, cos pi y, xyz), "
+                       "tau=1/h" % (n, k, nk, nk, nfs, 9 * nk + 18 * nfs),
            "cells": n ** 3}
+    paths = [("fp64", _lib.HDG_PREC_FP64), ("ffblock", _lib.HDG_PREC_FF_BLOCK)]
+    if k == 1:
+        paths.append(("fp32_refined", _lib.HDG_PREC_FP32_REFINED))
     sols = {}
-    for name, prec in (("fp64", _lib.HDG_PREC_FP64), ("fp32_refined", _lib.HDG_PREC_FP32_REFINED)):
+    for name, prec in paths:
         form = gh.ElasticityHDG(nu=nu, problem="smooth")
         op = gh.HybridAffineFEOperator(form, X, Y, [1, 2], [3], precision=prec, context=ctx)
         xh = gh.solve(op, solver="pcg", rtol=1e-12)
         h = op.pb.h
-        t0 = time.perf_counter()
         reps = 2
+        phases = np.zeros(5)
+        t0 = time.perf_counter()
         for _ in range(reps):
             ctx.check(ctx.lib.hdg_assemble(h, prec, None))
             it, rel = ctypes.c_int(), ctypes.c_double()
             ctx.check(ctx.lib.hdg_solve_skeleton(h, _lib.HDG_SOLVER_PCG, 1e-10, 20000, ctypes.byref(it),
                                                  ctypes.byref(rel)))
             ctx.check(ctx.lib.hdg_recover(h))
+            ms5 = np.zeros(5)
+            ctx.check(ctx.lib.hdg_get_timings(h, _lib.ptr(ms5)))
+            phases += ms5
         ctx.synchronize()
         ms = 1000.0 * (time.perf_counter() - t0) / reps
+        phases /= reps
         es, eu = xh.l2_errors()
         sols[name] = xh.free_dof_values.copy()
         out[name] = {"ms_per_solve": ms, "cells_per_s": n ** 3 / (ms / 1000.0), "pcg_iters": xh.iterations,
+                     "phase_ms": {"integrate": phases[0], "condense": phases[1], "assemble": phases[2],
+                                  "solve": phases[3], "recover": phases[4]},
                      "err_sigma_vs_exact": es, "err_u_vs_exact": eu}
         op.pb.close()
     ref = sols["fp64"]
-    out["fp32_refined"]["rel_err_vs_fp64"] = float(np.abs(sols["fp32_refined"] - ref).max() / np.abs(ref).max())
-    out["fp32_refined"]["speedup_vs_fp64"] = out["fp64"]["ms_per_solve"] / out["fp32_refined"]["ms_per_solve"]
+    for name, _ in paths[1:]:
+        out[name]["rel_err_vs_fp64"] = float(np.abs(sols[name] - ref).max() / np.abs(ref).max())
+        out[name]["speedup_vs_fp64"] = out["fp64"]["ms_per_solve"] / out[name]["ms_per_solve"]
     return out
 
 
@@ -506,6 +519,8 @@ def main():
                     help="problems of the batching workload (0 skips it)")
     ap.add_argument("--elasticity-n", type=int, default=24,
                     help="cells per side of the elasticity precision workload (0 skips it)")
+    ap.add_argument("--elasticity-k", type=int, default=2, choices=(1, 2),
+                    help="cell order of the elasticity precision workload")
     ap.add_argument("--n-side", type=int, default=32,
                     help="cells per side (32 is the benchmark workload; smaller sizes are for profiling)")
     args = ap.parse_args()

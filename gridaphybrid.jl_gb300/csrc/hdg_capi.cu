@@ -143,7 +143,7 @@ cudaError_t run_integrate(hdg_problem *pb) {
                                          nullptr, ctx->stream, ctx->num_sms, &ctx->launches);
     float *Ahi = pb->d_A.as<float>(), *bhi = pb->d_b.as<float>();
     return launch_integrate_elasticity(a, nullptr, nullptr, Ahi, Ahi + nc * n * n, bhi, bhi + nc * n, ctx->stream,
-                                       ctx->num_sms, &ctx->launches);
+                                       ctx->num_sms, &ctx->launches, pb->precision == HDG_PREC_FF_BLOCK);
   }
   if (pb->precision == HDG_PREC_FP64)
     return launch_integrate_fp64(a, pb->d_A.as<double>(), pb->d_b.as<double>(), ctx->stream, ctx->num_sms,
@@ -153,9 +153,56 @@ cudaError_t run_integrate(hdg_problem *pb) {
                                 ctx->num_sms, &ctx->launches, pb->precision == HDG_PREC_FF_BLOCK);
 }
 
+// The L2-panel block elimination's launch description (dry_run: size only).
+L2BlockLaunch l2block_launch(const hdg_problem *pb, size_t *need, bool dry_run) {
+  L2BlockLaunch L{};
+  L.elasticity = pb->physics == HDG_PHYSICS_ELASTICITY;
+  L.D = pb->tab.D;
+  L.k = pb->tab.k;
+  L.fp64 = pb->precision == HDG_PREC_FP64;
+  L.smem_optin = pb->ctx->smem_optin;
+  L.num_sms = pb->ctx->num_sms;
+  L.scratch_bytes = pb->d_escratch.bytes;
+  L.scratch_bytes_out = need;
+  L.dry_run = dry_run;
+  return L;
+}
+
+cudaError_t run_condense_l2block(hdg_problem *pb) {
+  hdg_context *ctx = pb->ctx;
+  const size_t nc = pb->mesh.ncells, n = pb->tab.n, ni = pb->tab.ni, nf = pb->tab.nf, nk = pb->tab.nk;
+  L2BlockArgs A{};
+  A.ncells = (int)nc;
+  A.cell = cell_args(pb);
+  A.S = pb->d_S.as<double>();
+  A.g = pb->d_g.as<double>();
+  A.info = pb->d_info.as<int>();
+  A.scratch = pb->d_escratch.ptr;
+  const float *Mf = pb->d_minv.as<float>();
+  if (pb->precision == HDG_PREC_FP64) {
+    A.A0 = pb->d_A.ptr;
+    A.b0 = pb->d_b.ptr;
+    A.Minv0 = Mf + 2 * nk * nk;
+    A.X0 = pb->d_fact.ptr;
+  } else {
+    const float *Ahi = pb->d_A.as<float>(), *bhi = pb->d_b.as<float>();
+    float *Xhi = pb->d_fact.as<float>();
+    A.A0 = Ahi;
+    A.A1 = Ahi + nc * n * n;
+    A.b0 = bhi;
+    A.b1 = bhi + nc * n;
+    A.Minv0 = Mf;
+    A.Minv1 = Mf + nk * nk;
+    A.X0 = Xhi;
+    A.X1 = Xhi + nc * ni * (nf + 1);
+  }
+  return launch_condense_l2block(A, l2block_launch(pb, nullptr, false), ctx->stream, &ctx->launches);
+}
+
 cudaError_t run_condense(hdg_problem *pb) {
   hdg_context *ctx = pb->ctx;
   const size_t nc = pb->mesh.ncells, n = pb->tab.n, ni = pb->tab.ni, nf = pb->tab.nf;
+  if (pb->eblock) return run_condense_l2block(pb);
   if (pb->precision == HDG_PREC_FP64)
     return launch_condense_fp64((int)nc, (int)ni, (int)nf, pb->d_A.as<double>(), pb->d_b.as<double>(),
                                 pb->d_S.as<double>(), pb->d_g.as<double>(), pb->d_fact.as<double>(),
@@ -196,6 +243,9 @@ cudaError_t run_recover(hdg_problem *pb) {
   hdg_context *ctx = pb->ctx;
   CellArgs a = cell_args(pb);
   const size_t nc = pb->mesh.ncells, ni = pb->tab.ni, nf = pb->tab.nf;
+  if (pb->precision == HDG_PREC_FP64 && pb->eblock)
+    return launch_recover_x64(a, pb->d_fact.as<double>(), pb->d_x.as<double>(), dirichlet_values(pb),
+                              pb->d_uint.as<double>(), ctx->stream, ctx->num_sms, &ctx->launches);
   if (pb->precision == HDG_PREC_FP64)
     return launch_recover_fp64(a, pb->d_fact.as<double>(), pb->d_x.as<double>(), dirichlet_values(pb),
                                pb->d_uint.as<double>(), ctx->stream, ctx->num_sms, &ctx->launches);
@@ -278,13 +328,14 @@ int setup_problem(hdg_problem *pb) {
   std::vector<float> packed_f;
   pb->toff_f = pack_tables_ff(pb->tab, packed_f);
   if ((rc = upload(ctx, pb->d_tabf, packed_f))) return rc;
-  {  // M_ref^{-1} as (hi, lo) floats for the block-elimination path
+  {  // M_ref^{-1} for the block-elimination paths: (hi, lo) floats, then FP64
     const std::vector<double> &Mi = pb->tab.Minv;
-    std::vector<float> mf(2 * Mi.size());
+    std::vector<float> mf(4 * Mi.size());
     for (size_t i = 0; i < Mi.size(); ++i) {
       mf[i] = (float)Mi[i];
       mf[Mi.size() + i] = (float)(Mi[i] - (double)mf[i]);
     }
+    memcpy(mf.data() + 2 * Mi.size(), Mi.data(), sizeof(double) * Mi.size());
     if ((rc = upload(ctx, pb->d_minv, mf))) return rc;
   }
   if ((rc = upload(ctx, pb->d_origin, pb->mesh.origin))) return rc;
@@ -720,19 +771,35 @@ static int assemble_prepare(hdg_problem *pb, int precision, bool cell_blocks) {
   const RefTables &t = pb->tab;
   const size_t nc = pb->mesh.ncells, n = t.n, ni = t.ni, nf = t.nf;
   const bool mixed = precision != HDG_PREC_FP64;
-  if (precision == HDG_PREC_FF_BLOCK && pb->physics != HDG_PHYSICS_DARCY)
-    return ctx->fail(HDG_ERR_INVALID, "block elimination is built for the Darcy form");
-  if (precision == HDG_PREC_FF_BLOCK && !ffblock_supported(t.D, t.k))
-    return ctx->fail(HDG_ERR_INVALID, "block elimination is built for D=2, k<=3 and D=3, k<=2");
-  const size_t need = precision == HDG_PREC_FP32_REFINED ? condense_mixed_smem((int)ni, (int)nf)
-                      : precision == HDG_PREC_FP64       ? n * (n + 1) * sizeof(double)
-                                                         : 0;
+  const bool elast = pb->physics == HDG_PHYSICS_ELASTICITY;
+  const bool l2ok = l2block_supported(elast, t.D, t.k);
+  if (precision == HDG_PREC_FF_BLOCK && !(l2ok || (!elast && ffblock_supported(t.D, t.k))))
+    return ctx->fail(HDG_ERR_INVALID, "block elimination is built for D=2, k<=3 and D=3, k<=2 (Darcy: k<=3)");
+  // the L2-panel block elimination: every elasticity FF_BLOCK assembly, Darcy
+  // beyond the shared-memory one, and FP64 cell blocks beyond the shared-memory LU
+  const bool dense64_fits = n * (n + 1) * sizeof(double) <= ctx->smem_optin - 1024;
+  const bool eblock = l2ok && ((precision == HDG_PREC_FF_BLOCK && (elast || !ffblock_supported(t.D, t.k))) ||
+                               (precision == HDG_PREC_FP64 && !dense64_fits));
+  const size_t need = precision == HDG_PREC_FP32_REFINED          ? condense_mixed_smem((int)ni, (int)nf)
+                      : (precision == HDG_PREC_FP64 && !eblock)  ? n * (n + 1) * sizeof(double)
+                                                                 : 0;
   if (need > ctx->smem_optin - 1024)
     return ctx->fail(HDG_ERR_INVALID, "cell block %zu exceeds the shared-memory condensation kernel", n);
   const int nl = 2 * t.D;
   if (mixed && !cellop_supported(nl, (int)t.nfd))
     return ctx->fail(HDG_ERR_INVALID, "no unassembled FP32 operator for %d facets of %zu DOFs", nl, t.nfd);
-  if (precision == HDG_PREC_FF_BLOCK && cell_blocks) CUDA_TRY(ctx, pb->d_invm.reserve(sizeof(double) * nc));
+  if (precision == HDG_PREC_FF_BLOCK && cell_blocks && !eblock)
+    CUDA_TRY(ctx, pb->d_invm.reserve(sizeof(double) * nc));
+  pb->precision = precision;
+  pb->eblock = eblock;
+  if (eblock) {
+    size_t scratch = 0;
+    L2BlockArgs sizing{};
+    sizing.ncells = (int)nc;
+    CUDA_TRY(ctx, launch_condense_l2block(sizing, l2block_launch(pb, &scratch, true), ctx->stream,
+                                          &ctx->launches));
+    CUDA_TRY(ctx, pb->d_escratch.reserve(scratch));
+  }
   if (cell_blocks) {
     // cell blocks: FP64, or (hi, lo) float pairs in the same bytes
     CUDA_TRY(ctx, pb->d_A.reserve(sizeof(double) * nc * n * n));
@@ -742,7 +809,8 @@ static int assemble_prepare(hdg_problem *pb, int precision, bool cell_blocks) {
   CUDA_TRY(ctx, pb->d_g.reserve(sizeof(double) * nc * nf));
   CUDA_TRY(ctx, pb->d_aux.reserve(sizeof(double) * nc * nf));
   // recovery factors: FP64 [U11 | U12 | y], or the float-float pair X1 = (X0, delta)
-  CUDA_TRY(ctx, pb->d_fact.reserve(mixed ? sizeof(float) * 2 * nc * ni * (nf + 1) : sizeof(double) * nc * ni * (n + 1)));
+  CUDA_TRY(ctx, pb->d_fact.reserve(mixed || eblock ? sizeof(float) * 2 * nc * ni * (nf + 1)
+                                                   : sizeof(double) * nc * ni * (n + 1)));
   CUDA_TRY(ctx, pb->d_info.reserve(sizeof(int) * nc));
   CUDA_TRY(ctx, pb->d_val.reserve(sizeof(double) * (pb->pat.nnz ? pb->pat.nnz : 1)));
   CUDA_TRY(ctx, pb->d_rhs.reserve(sizeof(double) * (pb->mesh.nfree ? pb->mesh.nfree : 1)));
@@ -886,6 +954,12 @@ static Pcg32Args pcg32_args(hdg_problem *pb) {
   ia.nstage = pb->cellop_nstage;
   ia.ctas = pb->cellop_ctas;
   ia.error = pb->d_counter.as<unsigned int>() + 1;
+  {  // update kernel: about two tiles of block rows per CTA, at most eight CTAs per SM
+    const long long tiles = (pb->pat.nblockrows + kPcgThreadsHost / ia.nfd - 1) / (kPcgThreadsHost / ia.nfd);
+    long long g = (tiles + 1) / 2;
+    const long long cap = (long long)pb->ctx->num_sms * 8;
+    ia.uctas = g > cap ? (int)cap : g < 1 ? 1 : (int)g;
+  }
   return ia;
 }
 
@@ -1015,7 +1089,7 @@ static int solve_reserve(hdg_problem *pb) {
   CUDA_TRY(ctx, pb->d_x.reserve(sizeof(double) * n));
   CUDA_TRY(ctx, pb->d_Binv.reserve(sizeof(double) * nbr * nfd * nfd));
   for (DBuf *b : {&pb->d_r, &pb->d_z, &pb->d_p, &pb->d_p2, &pb->d_q}) CUDA_TRY(ctx, b->reserve(sizeof(double) * n));
-  CUDA_TRY(ctx, pb->d_partials.reserve(sizeof(double) * 3 * ctx->num_sms * 4));
+  CUDA_TRY(ctx, pb->d_partials.reserve(sizeof(double) * 3 * ctx->num_sms * 8));
   CUDA_TRY(ctx, pb->d_scal.reserve(sizeof(double) * 16));
   CUDA_TRY(ctx, pb->d_counter.reserve(sizeof(unsigned int) * 4));
   if (!pb->h_pinned.ptr) {
@@ -1064,8 +1138,9 @@ int hdg_solve_skeleton(hdg_problem *pb, int solver, double rtol, int maxit, int 
     if (hinfo) status = ctx->fail(HDG_ERR_SINGULAR, "singular skeleton system (pivot %d)", hinfo);
     pb->d_z.release();
   } else {
-    if (pb->pat.max_rowlen > 288)
-      return ctx->fail(HDG_ERR_INVALID, "skeleton rows of %d entries exceed the SpMV kernel's 288", pb->pat.max_rowlen);
+    if (pb->pat.max_rowlen > kMaxSkeletonRowLen)
+      return ctx->fail(HDG_ERR_INVALID, "skeleton rows of %d entries exceed the SpMV kernel's %d", pb->pat.max_rowlen,
+                       kMaxSkeletonRowLen);
     if (!pcg_supports_nfd((int)nfd))
       return ctx->fail(HDG_ERR_INVALID, "PCG has no kernel for %zu DOFs per facet", nfd);
     CUDA_TRY(ctx, pb->d_Binv.reserve(sizeof(double) * pb->pat.nblockrows * nfd * nfd));
@@ -1074,7 +1149,7 @@ int hdg_solve_skeleton(hdg_problem *pb, int solver, double rtol, int maxit, int 
     CUDA_TRY(ctx, pb->d_p.reserve(sizeof(double) * n));
     CUDA_TRY(ctx, pb->d_p2.reserve(sizeof(double) * n));
     CUDA_TRY(ctx, pb->d_q.reserve(sizeof(double) * n));
-    CUDA_TRY(ctx, pb->d_partials.reserve(sizeof(double) * 3 * ctx->num_sms * 4));
+    CUDA_TRY(ctx, pb->d_partials.reserve(sizeof(double) * 3 * ctx->num_sms * 8));
     CUDA_TRY(ctx, pb->d_scal.reserve(sizeof(double) * 16));
     CUDA_TRY(ctx, pb->d_counter.reserve(sizeof(unsigned int) * 4));
     if (!pb->h_pinned.ptr) {

@@ -201,8 +201,12 @@ struct hdg_problem {
   // blocks, its cell map and per-cell products, FP32 block inverses, inner
   // vectors (x, r, z, p, p2), outer scalars
   hdg::DBuf d_cellop, d_cell_blk, d_qc, d_Binv32, d_v32, d_scal2;
-  // block-elimination path: M_ref^{-1} as (hi, lo) floats, 1/m per cell
-  hdg::DBuf d_minv, d_invm;
+  // block-elimination path: M_ref^{-1} as (hi, lo) floats then FP64, 1/m per
+  // cell, the elasticity kernel's per-CTA scratch panels
+  hdg::DBuf d_minv, d_invm, d_escratch;
+  // the elasticity cell blocks of this assembly are condensed by block
+  // elimination (float-float, or FP64 when the dense block exceeds shared memory)
+  bool eblock = false;
   cudaGraphExec_t pcg32_graph = nullptr;
   int cellop_nstage = 0, cellop_ctas = 0;  // streaming-kernel pipeline depth and grid
   // FP64 residual refinement of the FP32 skeleton solve: the inner reduction
@@ -224,7 +228,7 @@ struct hdg_problem {
             &d_dirvals, &d_A, &d_b, &d_S, &d_g, &d_fact, &d_info, &d_aux, &d_rowptr, &d_colind, &d_val,
             &d_rhs, &d_br_row0, &d_br_src, &d_blk_off, &d_blk_rowlen, &d_blk_src, &d_diag_blk, &d_dir_cells,
             &d_Binv, &d_x, &d_r, &d_z, &d_p, &d_p2, &d_q, &d_partials, &d_scal, &d_counter, &d_cellop,
-            &d_cell_blk, &d_qc, &d_Binv32, &d_v32, &d_scal2, &d_minv, &d_invm, &d_uint, &d_errs,
+            &d_cell_blk, &d_qc, &d_Binv32, &d_v32, &d_scal2, &d_minv, &d_invm, &d_escratch, &d_uint, &d_errs,
             &d_newton, &d_rmax, &d_dirzero};
   }
   ~hdg_problem();

@@ -200,6 +200,35 @@ cudaError_t launch_condense_ffblock(int D, int k, int ncells, const float *Ahi, 
                                     const float *Minv_l, const double *inv_m, double *S, double *g,
                                     float *Xhi, float *Xlo, int *info, cudaStream_t s, int num_sms,
                                     long long *launches);
+// Two-field block elimination with L2 panels (k_condense_l2block.cu):
+// elasticity (all built orders) and Darcy cells beyond the shared-memory
+// block elimination; float-float or FP64
+struct L2BlockArgs {
+  int ncells;
+  const void *A0, *A1, *b0, *b1;  // cell blocks: FP64 in A0/b0, or (hi, lo) float arrays
+  const void *Minv0, *Minv1;      // reference mass inverse, the same way
+  CellArgs cell;
+  double *S, *g;
+  void *X0, *X1;  // recovery X = A_ii^{-1} [A_if | b_i] (ni x (nf+1)), the same way; may be null
+  int *info;
+  void *scratch;  // per-CTA panels
+};
+struct L2BlockLaunch {
+  bool elasticity;
+  int D, k;
+  bool fp64;
+  size_t smem_optin;
+  int num_sms;
+  size_t scratch_bytes;        // bytes at args.scratch
+  size_t *scratch_bytes_out;   // receives the bytes the launch needs (may be null)
+  bool dry_run;                // only size the scratch
+};
+bool l2block_supported(bool elasticity, int D, int k);
+cudaError_t launch_condense_l2block(const L2BlockArgs &args, const L2BlockLaunch &L, cudaStream_t s,
+                                    long long *launches);
+// u = y - X_f x_f from an FP64 X of the block elimination
+cudaError_t launch_recover_x64(const CellArgs &a, const double *X, const double *lambda, const double *dirvals,
+                               double *uint, cudaStream_t s, int num_sms, long long *launches);
 cudaError_t launch_recover_mixed(const CellArgs &a, const float *Xhi, const float *Xlo,
                                  const double *lambda, const double *dirvals, double *uint,
                                  cudaStream_t s, int num_sms, long long *launches);
@@ -265,7 +294,12 @@ struct Pcg32Args {
   float *qc;              // ncells x nl*nfd per-cell products
   int nstage, ctas;       // pipeline depth and grid of the streaming kernel
   unsigned int *error;    // set to 1 when a bulk copy never completed
+  int uctas;              // grid of the update kernel (partials: 2 x uctas)
 };
+// threads per CTA of the PCG vector kernels (kPcgThreads on the device side)
+// and the longest skeleton row their FP64 SpMV stages (kMaxRowLen)
+constexpr int kPcgThreadsHost = 256;
+constexpr int kMaxSkeletonRowLen = 304;
 // Cell-operator layout: threads per cell, cells per CTA stage, floats per record.
 HDG_HD constexpr int cellop_tpc(int nf) { return nf <= 8 ? 8 : nf <= 16 ? 16 : ((nf + 31) / 32) * 32; }
 HDG_HD constexpr int cellop_cps(int nf) { return cellop_tpc(nf) >= 256 ? 1 : 256 / cellop_tpc(nf); }
@@ -340,9 +374,11 @@ cudaError_t launch_newton_update(size_t count, double *x, const double *dx, cuda
 
 // Linear elasticity HDG cells: blocks in FP64 (A, b) or as float-float pairs
 // (the entries computed in FP64 and split), and the stress / displacement L2
-// error contributions per cell (errs: 2 per cell).
+// error contributions per cell (errs: 2 per cell).  skip_ss: the stress-stress
+// block is not written (the block elimination never reads it).
 cudaError_t launch_integrate_elasticity(const CellArgs &a, double *A, double *b, float *Ahi, float *Alo, float *bhi,
-                                        float *blo, cudaStream_t s, int num_sms, long long *launches);
+                                        float *blo, cudaStream_t s, int num_sms, long long *launches,
+                                        bool skip_ss = false);
 cudaError_t launch_l2_errors_elasticity(const CellArgs &a, const double *uint, double *errs, cudaStream_t s,
                                         int num_sms, long long *launches);
 

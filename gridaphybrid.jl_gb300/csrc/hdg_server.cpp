@@ -56,7 +56,7 @@ bool shape_supported(int D, int k, int precision, int solver, size_t smem_optin,
   const size_t avail = smem_optin > 1024 ? smem_optin - 1024 : 0;
   switch (precision) {
     case HDG_PREC_FP64:
-      if ((size_t)s.n * (s.n + 1) * sizeof(double) > avail) {
+      if ((size_t)s.n * (s.n + 1) * sizeof(double) > avail && !l2block_supported(false, D, k)) {
         why = "the FP64 cell block exceeds shared memory";
         return false;
       }
@@ -68,8 +68,8 @@ bool shape_supported(int D, int k, int precision, int solver, size_t smem_optin,
       }
       break;
     case HDG_PREC_FF_BLOCK:
-      if (!ffblock_supported(D, k)) {
-        why = "block elimination is built for D=2, k<=3 and D=3, k<=2";
+      if (!ffblock_supported(D, k) && !l2block_supported(false, D, k)) {
+        why = "block elimination is built for D=2, k<=3 and D=3, k<=3";
         return false;
       }
       break;
@@ -104,6 +104,10 @@ double footprint_bound(int D, int n, int k, int precision, int solver) {
   const double nblocks = nbr * (2 * nl - 1);
   const double nnz = nblocks * s.nfd * s.nfd;
   const bool fast = precision != HDG_PREC_FP64;
+  // cell blocks condensed by the L2-panel block elimination (FP64 too large
+  // for the shared-memory LU, or float-float beyond the shared-memory kernel)
+  const bool l2block = l2block_supported(false, D, k) &&
+                       (fast ? !ffblock_supported(D, k) : (double)s.n * (s.n + 1) * 8.0 > 227.0 * 1024 - 1024);
   double b = 0.0;
   // mesh and Dirichlet data
   b += ncells * (D + D * D) * 8.0 + ncells * nl * 4.0 + nfacets * s.nfd * 4.0 + nfacets * 2 * 4.0 + ncells * 8.0 +
@@ -113,8 +117,9 @@ double footprint_bound(int D, int n, int k, int precision, int solver) {
   // cell blocks, condensed blocks, recovery factors, CSR values and rhs
   b += ncells * ((double)s.n * s.n * 8 + s.n * 8 + (double)s.nf * s.nf * 8 + 2.0 * s.nf * 8 + 4) + nnz * 8 +
        nfree * 8;
-  b += fast ? 8.0 * ncells * s.ni * (s.nf + 1) : 8.0 * ncells * s.ni * (s.n + 1);
+  b += fast || l2block ? 8.0 * ncells * s.ni * (s.nf + 1) : 8.0 * ncells * s.ni * (s.n + 1);
   if (precision == HDG_PREC_FF_BLOCK) b += ncells * 8.0;
+  if (l2block) b += 64.0 * (1 << 20);  // per-CTA panels (one CTA per SM)
   if (fast) b += ncells * cellop_rec(nl, s.nfd) * 4.0;
   // skeleton solve
   if (solver == HDG_SOLVER_DIRECT) {

@@ -1,0 +1,494 @@
+// k_condense_l2block.cu -- static condensation by two-field block
+// elimination with the panels in L2 (sm_103a), in float-float on the FP32
+// pipes or in plain FP64 (the same algorithm: the FP64 path for cell blocks
+// too large for the shared-memory LU).
+//
+// Cell DOFs: [field 1 s (NC1 comps x NK) | field 2 u (NC2 x NK) | trace f
+// (2D facets x NC2 x NFS)], component-major.  Field 1's block is a reference
+// mass matrix times a per-cell factor:
+//   elasticity (s = symmetric stress, u = displacement, NC1 = D(D+1)/2,
+//     NC2 = D): A_ss = |J| (C_nu (x) M_ref), C_nu[c][d] = E_c : A(E_d);
+//   Darcy (s = flux, u = pressure, NC1 = D, NC2 = 1):
+//     A_ss = (|J|/kappa) (I_D (x) M_ref);
+// so A_ss^{-1} = (C^{-1} (x) M_ref^{-1}) with a small per-cell C^{-1} (6x6 at
+// most) and the reference mass inverse; A_ss itself is never read.  With
+// R = [A_sf | b_s] and R_u = [A_uf | b_u]:
+//   Y = A_ss^{-1} A_su,  Z = A_ss^{-1} R      NS x NU, NS x NC (per-CTA scratch, L2)
+//   P = A_uu - A_us Y,   Q = R_u - A_us Z    NU x NU, NU x NC (shared memory)
+//   X_u = P^{-1} Q   (LU with partial pivoting of field 2's Schur complement)
+//   X_s = Z - Y X_u
+//   S = A_ff - A_fs X_s - A_fu X_u,   g = b_f - A_fs y_s - A_fu y_u
+// Structural zeros that hold on every affine cell are skipped:
+//   - elasticity: A_us / A_su couple displacement component k only to the
+//     stress components whose index pair contains k;
+//   - A_fs / A_fu / A_sf couple a trace row of facet F only to the volume
+//     nodes on F (Lagrange nodes off F vanish on F), found from the H table.
+#include <cuda_runtime.h>
+
+#include "hdg_kernels.h"
+#include "k_ffblock_cell.cuh"
+
+namespace hdg {
+namespace be {
+
+// float-float values (hi, lo) on the FP32 pipes
+struct ArFF {
+  struct __align__(8) V {
+    float h, l;
+  };
+  static __device__ __forceinline__ V zero() { return V{0.0f, 0.0f}; }
+  static __device__ __forceinline__ void mac(V &c, V a, V b) { ffb::mac(c.h, c.l, a.h, a.l, b.h, b.l); }
+  static __device__ __forceinline__ V fin(V a) {
+    ffb::normalise(a.h, a.l);
+    return a;
+  }
+  static __device__ __forceinline__ V sub(V a, V b) {
+    V r;
+    ffb::sub(a.h, a.l, b.h, b.l, r.h, r.l);
+    return r;
+  }
+  static __device__ __forceinline__ V mul(V a, V b) {
+    V r;
+    ffb::mul(a.h, a.l, b.h, b.l, r.h, r.l);
+    return r;
+  }
+  static __device__ __forceinline__ V div(V a, V b) {
+    V r;
+    ffb::div(a.h, a.l, b.h, b.l, r.h, r.l);
+    return r;
+  }
+  static __device__ __forceinline__ float mag(V a) { return fabsf(a.h); }
+  static __device__ __forceinline__ bool nonzero(V a) { return a.h != 0.0f; }
+  static __device__ __forceinline__ double dbl(V a) { return (double)a.h + (double)a.l; }
+  static __device__ __forceinline__ V of(double x) {
+    V r;
+    r.h = (float)x;
+    r.l = (float)(x - (double)r.h);
+    return r;
+  }
+  // element i of a (hi array, lo array) pair
+  static __device__ __forceinline__ V ld(const void *p0, const void *p1, size_t i) {
+    return V{__ldg(static_cast<const float *>(p0) + i), __ldg(static_cast<const float *>(p1) + i)};
+  }
+  static __device__ __forceinline__ void st(void *p0, void *p1, size_t i, V v) {
+    static_cast<float *>(p0)[i] = v.h;
+    static_cast<float *>(p1)[i] = v.l;
+  }
+};
+
+// plain FP64
+struct Ar64 {
+  using V = double;
+  static __device__ __forceinline__ V zero() { return 0.0; }
+  static __device__ __forceinline__ void mac(V &c, V a, V b) { c = fma(a, b, c); }
+  static __device__ __forceinline__ V fin(V a) { return a; }
+  static __device__ __forceinline__ V sub(V a, V b) { return a - b; }
+  static __device__ __forceinline__ V mul(V a, V b) { return a * b; }
+  static __device__ __forceinline__ V div(V a, V b) { return a / b; }
+  static __device__ __forceinline__ double mag(V a) { return fabs(a); }
+  static __device__ __forceinline__ bool nonzero(V a) { return a != 0.0; }
+  static __device__ __forceinline__ double dbl(V a) { return a; }
+  static __device__ __forceinline__ V of(double x) { return x; }
+  static __device__ __forceinline__ V ld(const void *p0, const void *, size_t i) {
+    return __ldg(static_cast<const double *>(p0) + i);
+  }
+  static __device__ __forceinline__ void st(void *p0, void *, size_t i, V v) { static_cast<double *>(p0)[i] = v; }
+};
+
+__host__ __device__ constexpr int ipow_c(int b, int e) { return e == 0 ? 1 : b * ipow_c(b, e - 1); }
+
+template <int D_, int K_, bool ELAST_>
+struct ECfg {
+  static constexpr int D = D_, K = K_;
+  static constexpr bool ELAST = ELAST_;
+  static constexpr int NK = ipow_c(K + 1, D), NC1 = ELAST ? D * (D + 1) / 2 : D, NC2 = ELAST ? D : 1;
+  static constexpr int NS = NC1 * NK, NU = NC2 * NK;
+  static constexpr int NI = NS + NU, NFS = ipow_c(K + 1, D - 1), NFD = NC2 * NFS, NL = 2 * D, NF = NL * NFD;
+  static constexpr int N = NI + NF, NC = NF + 1;
+  static constexpr int NT = NU * NC >= 8192 ? 512 : 256;
+  // shared: P (NU x NU), Q (NU x NC), M^{-1} (NK x NK), C^{-1}/|J| (6 x 6), as values
+  static constexpr size_t smem_values = (size_t)NU * NU + (size_t)NU * NC + (size_t)NK * NK + 36;
+  // per-CTA scratch: Y (NS x NU), Z (NS x NC), column-major, as values
+  static constexpr size_t slot_values = (size_t)NS * NU + (size_t)NS * NC;
+};
+
+// shared-memory bookkeeping beside the value arrays
+template <class C>
+struct Lists {
+  int fn_cnt[C::NL];          // volume nodes on local facet lf ...
+  int fn_node[C::NL][C::NK];  // ... and their indices
+  int kmask[3];               // bit c: field-1 component c couples to field-2 component k
+  int kc_cnt[3], kc_comp[3][6];
+  int piv, info;
+};
+
+template <class C, class Ar>
+constexpr size_t smem_bytes() {
+  return C::smem_values * sizeof(typename Ar::V) + sizeof(Lists<C>) + 16;
+}
+
+// C_nu^{-1} / |J| in FP64: Gauss-Jordan with partial pivoting on the compliance
+__device__ void compliance_inverse(int D, int nsym, double E, double nu, double detJ, double (*Ci)[6]) {
+  double Cm[6][6], I[6][6];
+  for (int c = 0; c < nsym; ++c)
+    for (int d = 0; d < nsym; ++d) {
+      double dd = 0.0, trc = 0.0, trd = 0.0;
+      for (int r = 0; r < D; ++r) {
+        trc += sym_unit(D, c, r, r);
+        trd += sym_unit(D, d, r, r);
+        for (int s = 0; s < D; ++s) dd += sym_unit(D, c, r, s) * sym_unit(D, d, r, s);
+      }
+      Cm[c][d] = (1.0 + nu) / E * dd - nu / E * trc * trd;
+      I[c][d] = c == d ? 1.0 : 0.0;
+    }
+  for (int col = 0; col < nsym; ++col) {
+    int pr = col;
+    for (int i = col + 1; i < nsym; ++i)
+      if (fabs(Cm[i][col]) > fabs(Cm[pr][col])) pr = i;
+    for (int j = 0; j < nsym; ++j) {
+      double t = Cm[col][j];
+      Cm[col][j] = Cm[pr][j];
+      Cm[pr][j] = t;
+      t = I[col][j];
+      I[col][j] = I[pr][j];
+      I[pr][j] = t;
+    }
+    const double piv = 1.0 / Cm[col][col];
+    for (int j = 0; j < nsym; ++j) {
+      Cm[col][j] *= piv;
+      I[col][j] *= piv;
+    }
+    for (int i = 0; i < nsym; ++i) {
+      if (i == col) continue;
+      const double f = Cm[i][col];
+      for (int j = 0; j < nsym; ++j) {
+        Cm[i][j] -= f * Cm[col][j];
+        I[i][j] -= f * I[col][j];
+      }
+    }
+  }
+  for (int c = 0; c < nsym; ++c)
+    for (int d = 0; d < nsym; ++d) Ci[c][d] = I[c][d] / detJ;
+}
+
+template <class C, class Ar>
+__global__ void __launch_bounds__(C::NT, 1) condense_l2block_kernel(L2BlockArgs a) {
+  using V = typename Ar::V;
+  constexpr int D = C::D, NK = C::NK, NSYM = C::NC1, NC2 = C::NC2, NS = C::NS, NU = C::NU, NI = C::NI, NF = C::NF, N = C::N,
+                NC = C::NC, NT = C::NT, NFD = C::NFD, NL = C::NL, NFS = C::NFS;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  V *P = reinterpret_cast<V *>(smem_raw);  // [r][j]
+  V *Q = P + NU * NU;                      // [r][c]
+  V *Mi = Q + (size_t)NU * NC;             // [a][k]
+  V *Ci = Mi + NK * NK;                    // [c][d]
+  Lists<C> &L = *reinterpret_cast<Lists<C> *>(Ci + 36);
+  V *Y = static_cast<V *>(a.scratch) + (size_t)blockIdx.x * C::slot_values;  // [m + NS j]
+  V *Z = Y + (size_t)NS * NU;                                                // [m + NS c]
+  const CellArgs &ca = a.cell;
+  const int t = threadIdx.x;
+  for (int e = t; e < NK * NK; e += NT) Mi[e] = Ar::ld(a.Minv0, a.Minv1, e);
+  if (t < NL) {  // volume nodes with a nonzero trace coupling on facet t
+    int cnt = 0;
+    for (int node = 0; node < NK; ++node) {
+      bool nz = false;
+      for (int b = 0; b < NFS; ++b) nz |= ca.H[((size_t)t * NK + node) * NFS + b] != 0.0;
+      if (nz) L.fn_node[t][cnt++] = node;
+    }
+    L.fn_cnt[t] = cnt;
+  }
+  if (t == 0) {
+    for (int k = 0; k < NC2; ++k) {
+      int m = 0, cnt = 0;
+      for (int c = 0; c < NSYM; ++c) {
+        bool couples = true;  // Darcy: the pressure couples to every flux component
+        if (C::ELAST) {
+          int i, j;
+          sym_pair(D, c, i, j);
+          couples = i == k || j == k;
+        }
+        if (couples) {
+          m |= 1 << c;
+          L.kc_comp[k][cnt++] = c;
+        }
+      }
+      L.kmask[k] = m;
+      L.kc_cnt[k] = cnt;
+    }
+  }
+  for (int cell = blockIdx.x; cell < a.ncells; cell += gridDim.x) {
+    const size_t A0 = (size_t)cell * N * N, b0 = (size_t)cell * N;
+    auto A = [&](int r, int c) { return Ar::ld(a.A0, a.A1, A0 + (size_t)r + (size_t)N * c); };
+    auto B = [&](int r) { return Ar::ld(a.b0, a.b1, b0 + r); };
+    __syncthreads();  // the previous cell's readers of the lists / Ci are done
+    if (t == 0) {
+      const double *J = ca.jac + (size_t)cell * D * D;
+      const double det = D == 2 ? J[0] * J[3] - J[2] * J[1]
+                                : J[0] * (J[4] * J[8] - J[7] * J[5]) - J[3] * (J[1] * J[8] - J[7] * J[2]) +
+                                      J[6] * (J[1] * J[5] - J[4] * J[2]);
+      double Cinv[6][6];
+      if (C::ELAST) {
+        compliance_inverse(D, NSYM, ca.young, ca.kappa ? ca.kappa[cell] : 0.3, fabs(det), Cinv);
+      } else {  // kappa / |J| on the diagonal
+        const double s = (ca.kappa ? ca.kappa[cell] : 1.0) / fabs(det);
+        for (int c = 0; c < NSYM; ++c)
+          for (int d = 0; d < NSYM; ++d) Cinv[c][d] = c == d ? s : 0.0;
+      }
+      for (int c = 0; c < NSYM; ++c)
+        for (int d = 0; d < NSYM; ++d) Ci[c * 6 + d] = Ar::of(Cinv[c][d]);
+      L.info = 0;
+    }
+    __syncthreads();
+    // 1. Y = A_ss^{-1} A_su and Z = A_ss^{-1} [A_sf | b_s]: M^{-1} on each
+    //    stress component of the column, then the components mixed by C^{-1}/|J|
+    for (int o = t; o < NK * (NU + NC); o += NT) {
+      const int an = o % NK, col = o / NK;
+      V T[NSYM];
+#pragma unroll
+      for (int cp = 0; cp < NSYM; ++cp) T[cp] = Ar::zero();
+      if (col < NU) {
+        const int msk = L.kmask[col / NK];
+#pragma unroll
+        for (int cp = 0; cp < NSYM; ++cp)
+          if (msk >> cp & 1)
+            for (int k = 0; k < NK; ++k) Ar::mac(T[cp], Mi[an * NK + k], A(cp * NK + k, NS + col));
+      } else if (col < NU + NF) {
+        const int f = col - NU, lf = f / NFD, cnt = L.fn_cnt[lf];
+#pragma unroll
+        for (int cp = 0; cp < NSYM; ++cp)
+          for (int q = 0; q < cnt; ++q) {
+            const int k = L.fn_node[lf][q];
+            Ar::mac(T[cp], Mi[an * NK + k], A(cp * NK + k, NI + f));
+          }
+      } else {
+#pragma unroll
+        for (int cp = 0; cp < NSYM; ++cp)
+          for (int k = 0; k < NK; ++k) Ar::mac(T[cp], Mi[an * NK + k], B(cp * NK + k));
+      }
+#pragma unroll
+      for (int cp = 0; cp < NSYM; ++cp) T[cp] = Ar::fin(T[cp]);
+#pragma unroll
+      for (int c = 0; c < NSYM; ++c) {
+        V v = Ar::zero();
+#pragma unroll
+        for (int cp = 0; cp < NSYM; ++cp) Ar::mac(v, Ci[c * 6 + cp], T[cp]);
+        v = Ar::fin(v);
+        const int m = c * NK + an;
+        if (col < NU)
+          Y[m + (size_t)NS * col] = v;
+        else
+          Z[m + (size_t)NS * (col - NU)] = v;
+      }
+    }
+    __syncthreads();
+    // 2. P = A_uu - A_us Y,  Q = [A_uf | b_u] - A_us Z
+    for (int o = t; o < NU * (NU + NC); o += NT) {
+      const int r = o % NU, col = o / NU, kd = r / NK;
+      const bool isP = col < NU;
+      const V *x = isP ? Y + (size_t)NS * col : Z + (size_t)NS * (col - NU);
+      V acc = Ar::zero();
+      const int cnt = L.kc_cnt[kd];
+      for (int q = 0; q < cnt; ++q) {
+        const int m0 = L.kc_comp[kd][q] * NK;
+        for (int k = 0; k < NK; ++k) Ar::mac(acc, A(NS + r, m0 + k), x[m0 + k]);
+      }
+      acc = Ar::fin(acc);
+      const V r0 = isP ? A(NS + r, NS + col) : col - NU < NF ? A(NS + r, NI + col - NU) : B(NS + r);
+      const V v = Ar::sub(r0, acc);
+      if (isP)
+        P[r * NU + col] = v;
+      else
+        Q[r * NC + col - NU] = v;
+    }
+    __syncthreads();
+    // 3. LU with partial pivoting of [P | Q]; the pivot search is warp 0's
+    for (int j = 0; j < NU; ++j) {
+      if (t < 32) {
+        auto best = Ar::mag(Ar::zero()) - 1;
+        int bi = j;
+        for (int i = j + t; i < NU; i += 32) {
+          const auto v = Ar::mag(P[i * NU + j]);
+          if (v > best) {
+            best = v;
+            bi = i;
+          }
+        }
+        for (int off = 16; off > 0; off >>= 1) {
+          const auto ob = __shfl_down_sync(0xffffffffu, best, off);
+          const int oi = __shfl_down_sync(0xffffffffu, bi, off);
+          if (ob > best || (ob == best && oi < bi)) {
+            best = ob;
+            bi = oi;
+          }
+        }
+        if (t == 0) {
+          L.piv = bi;
+          if (!(best > 0) && L.info == 0) L.info = j + 1;
+        }
+      }
+      __syncthreads();
+      const int p = L.piv;
+      if (p != j)
+        for (int c = t; c < NU + NC; c += NT) {
+          V *row_j = c < NU ? P + j * NU + c : Q + j * NC + (c - NU);
+          V *row_p = c < NU ? P + p * NU + c : Q + p * NC + (c - NU);
+          const V tmp = *row_j;
+          *row_j = *row_p;
+          *row_p = tmp;
+        }
+      __syncthreads();
+      const V pv = P[j * NU + j];
+      if (Ar::nonzero(pv))
+        for (int i = j + 1 + t; i < NU; i += NT) P[i * NU + j] = Ar::div(P[i * NU + j], pv);
+      __syncthreads();
+      const int rows = NU - j - 1, w = NU - j - 1, cols = w + NC;
+      for (int e = t; e < rows * cols; e += NT) {
+        const int i = j + 1 + e / cols, c = e % cols;
+        const V l = P[i * NU + j];
+        V *tg;
+        V u;
+        if (c < w) {
+          u = P[j * NU + j + 1 + c];
+          tg = P + i * NU + j + 1 + c;
+        } else {
+          u = Q[j * NC + c - w];
+          tg = Q + i * NC + c - w;
+        }
+        *tg = Ar::sub(*tg, Ar::mul(l, u));
+      }
+      __syncthreads();
+    }
+    // 4. back substitution: X_u = U^{-1} Q, in Q
+    for (int j = NU - 1; j >= 0; --j) {
+      const V pv = P[j * NU + j];
+      for (int c = t; c < NC; c += NT) Q[j * NC + c] = Ar::nonzero(pv) ? Ar::div(Q[j * NC + c], pv) : Ar::zero();
+      __syncthreads();
+      for (int e = t; e < j * NC; e += NT) {
+        const int i = e / NC, c = e - i * NC;
+        Q[i * NC + c] = Ar::sub(Q[i * NC + c], Ar::mul(P[i * NU + j], Q[j * NC + c]));
+      }
+      __syncthreads();
+    }
+    // 5. X_s = Z - Y X_u, in Z
+    for (int o = t; o < NS * NC; o += NT) {
+      const int m = o % NS, c = o / NS;
+      V acc = Ar::zero();
+      for (int k = 0; k < NU; ++k) Ar::mac(acc, Y[m + (size_t)NS * k], Q[k * NC + c]);
+      Z[m + (size_t)NS * c] = Ar::sub(Z[m + (size_t)NS * c], Ar::fin(acc));
+    }
+    __syncthreads();
+    // 6. S = A_ff - A_fs X_s - A_fu X_u and g, over the volume nodes on the row's facet
+    for (int o = t; o < NF * NC; o += NT) {
+      const int f = o % NF, c = o / NF, lf = f / NFD, cnt = L.fn_cnt[lf];
+      V acc = Ar::zero();
+      for (int q = 0; q < cnt; ++q) {
+        const int node = L.fn_node[lf][q];
+#pragma unroll
+        for (int cc = 0; cc < NSYM; ++cc) {
+          const int m = cc * NK + node;
+          Ar::mac(acc, A(NI + f, m), Z[m + (size_t)NS * c]);
+        }
+#pragma unroll
+        for (int kd = 0; kd < NC2; ++kd) {
+          const int u = kd * NK + node;
+          Ar::mac(acc, A(NI + f, NS + u), Q[u * NC + c]);
+        }
+      }
+      const V rhs = c < NF ? A(NI + f, NI + c) : B(NI + f);
+      const double v = Ar::dbl(rhs) - Ar::dbl(Ar::fin(acc));
+      if (c < NF)
+        a.S[(size_t)cell * NF * NF + f + (size_t)NF * c] = v;
+      else
+        a.g[(size_t)cell * NF + f] = v;
+    }
+    // 7. X = [X_s; X_u] (NI x NC, column-major) for the recovery
+    if (a.X0) {
+      const size_t x0 = (size_t)cell * NI * NC;
+      for (int e = t; e < NI * NC; e += NT) {
+        const int c = e / NI, m = e - c * NI;
+        Ar::st(a.X0, a.X1, x0 + e, m < NS ? Z[m + (size_t)NS * c] : Q[(m - NS) * NC + c]);
+      }
+    }
+    if (t == 0 && a.info) a.info[cell] = L.info;
+  }
+}
+
+template <class C, class Ar>
+cudaError_t launch_cfg(const L2BlockArgs &args, const L2BlockLaunch &L, cudaStream_t s, long long *launches) {
+  auto kern = condense_l2block_kernel<C, Ar>;
+  const size_t smem = smem_bytes<C, Ar>();
+  if (smem > L.smem_optin) return cudaErrorInvalidConfiguration;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, C::NT, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  long long grid = (long long)per_sm * L.num_sms;
+  if (grid > args.ncells) grid = args.ncells;
+  if (grid < 1) grid = 1;
+  const size_t need = (size_t)grid * C::slot_values * sizeof(typename Ar::V);
+  if (L.scratch_bytes_out) *L.scratch_bytes_out = need;
+  if (L.dry_run) return cudaSuccess;
+  if (need > L.scratch_bytes || !args.scratch) return cudaErrorMemoryAllocation;
+  kern<<<(int)grid, C::NT, smem, s>>>(args);
+  ++*launches;
+  return cudaGetLastError();
+}
+
+}  // namespace be
+
+bool l2block_supported(bool elasticity, int D, int k) {
+  if (elasticity) return (D == 2 && k >= 1 && k <= 3) || (D == 3 && k >= 1 && k <= 2);
+  return D == 3 && k == 3;  // Darcy: the shared-memory block elimination covers D=2, k<=3 and D=3, k<=2
+}
+
+cudaError_t launch_condense_l2block(const L2BlockArgs &args, const L2BlockLaunch &L, cudaStream_t s,
+                                    long long *launches) {
+#define HDG_L2B(EL, DD, KK)                                                                    \
+  if (L.elasticity == EL && L.D == DD && L.k == KK)                                            \
+    return L.fp64 ? be::launch_cfg<be::ECfg<DD, KK, EL>, be::Ar64>(args, L, s, launches)       \
+                  : be::launch_cfg<be::ECfg<DD, KK, EL>, be::ArFF>(args, L, s, launches);
+  HDG_L2B(true, 2, 1)
+  HDG_L2B(true, 2, 2)
+  HDG_L2B(true, 2, 3)
+  HDG_L2B(true, 3, 1)
+  HDG_L2B(true, 3, 2)
+  HDG_L2B(false, 3, 3)
+#undef HDG_L2B
+  return cudaErrorInvalidValue;
+}
+
+// u = y - X_f x_f per cell, X = [X_f | y] (ni x (nf+1), column-major, FP64)
+__global__ void __launch_bounds__(128) recover_x64_kernel(CellArgs a, const double *__restrict__ X,
+                                                          const double *__restrict__ lambda,
+                                                          const double *__restrict__ dirvals, double *uint) {
+  __shared__ double xf[6 * 64];
+  const int ni = a.ni, nf = a.nf, nfd = a.nfd, nl = 2 * a.D, nc = nf + 1;
+  for (int c = blockIdx.x; c < a.ncells; c += gridDim.x) {
+    for (int e = threadIdx.x; e < nf; e += blockDim.x) {
+      const int lf = e / nfd, j = e - lf * nfd;
+      const int id = a.facet_dofs[(size_t)a.cell_facets[(size_t)c * nl + lf] * nfd + j];
+      xf[e] = id >= 0 ? lambda[id] : dirvals[-1 - id];
+    }
+    __syncthreads();
+    const double *x = X + (size_t)c * ni * nc;
+    for (int i = threadIdx.x; i < ni; i += blockDim.x) {
+      double v = x[i + (size_t)ni * nf];
+      for (int j = 0; j < nf; ++j) v -= x[i + (size_t)ni * j] * xf[j];
+      uint[(size_t)c * ni + i] = v;
+    }
+    __syncthreads();
+  }
+}
+
+cudaError_t launch_recover_x64(const CellArgs &a, const double *X, const double *lambda, const double *dirvals,
+                               double *uint, cudaStream_t s, int num_sms, long long *launches) {
+  if (a.nf > 6 * 64) return cudaErrorInvalidValue;
+  int grid = a.ncells < num_sms * 8 ? a.ncells : num_sms * 8;
+  if (grid < 1) grid = 1;
+  recover_x64_kernel<<<grid, 128, 0, s>>>(a, X, lambda, dirvals, uint);
+  ++*launches;
+  return cudaGetLastError();
+}
+
+}  // namespace hdg

@@ -107,7 +107,7 @@ __device__ void compliance(int D, int nsym, double E, double nu, double (*Cm)[6]
 }
 
 __global__ void __launch_bounds__(256) integrate_elasticity_kernel(CellArgs a, double *A, double *b, float *Ahi,
-                                                                   float *Alo, float *bhi, float *blo) {
+                                                                   float *Alo, float *bhi, float *blo, bool skip_ss) {
   __shared__ CellFactors f;
   __shared__ double Cm[6][6];
   __shared__ double fq[512 * 3];
@@ -133,8 +133,10 @@ __global__ void __launch_bounds__(256) integrate_elasticity_kernel(CellArgs a, d
     }
     __syncthreads();
     const size_t base = (size_t)c * n * n;
+    const int ns = a.nsym * a.nk;
     for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
       const int j = e / n, i = e - j * n;
+      if (skip_ss && i < ns && j < ns) continue;
       const double v = elast_entry(a, f, Cm, f.detJ, i, j);
       if (A) {
         A[base + e] = v;
@@ -224,11 +226,11 @@ __global__ void __launch_bounds__(128) l2_errors_elasticity_kernel(CellArgs a, c
 }  // namespace
 
 cudaError_t launch_integrate_elasticity(const CellArgs &a, double *A, double *b, float *Ahi, float *Alo, float *bhi,
-                                        float *blo, cudaStream_t s, int num_sms, long long *launches) {
+                                        float *blo, cudaStream_t s, int num_sms, long long *launches, bool skip_ss) {
   if (a.nqv > 512 || a.nsym > 6) return cudaErrorInvalidValue;
   int grid = a.ncells < num_sms * 8 ? a.ncells : num_sms * 8;
   if (grid < 1) grid = 1;
-  integrate_elasticity_kernel<<<grid, 256, 0, s>>>(a, A, b, Ahi, Alo, bhi, blo);
+  integrate_elasticity_kernel<<<grid, 256, 0, s>>>(a, A, b, Ahi, Alo, bhi, blo, skip_ss);
   ++*launches;
   return cudaGetLastError();
 }

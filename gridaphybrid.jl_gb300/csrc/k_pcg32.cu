@@ -307,7 +307,13 @@ __global__ void __launch_bounds__(CellOp<NL, NFD>::THREADS)
 
 // q = qc(owner) + qc(other) per free row; x += alpha p; r -= alpha q;
 // z = Binv r with the tile's block inverses staged in shared memory; beta;
-// convergence against eta |rhs|
+// convergence against eta |rhs|.  The row's loads (source cells, p, x, r)
+// are issued together, so a tile costs two dependent memory round trips
+// (source cells, then their products); the grid (a.uctas, up to eight CTAs
+// per SM) keeps enough tiles in flight to hide them.
+static_assert(kPcgThreads == kPcgThreadsHost, "host and device PCG block sizes differ");
+static_assert(kMaxRowLen == kMaxSkeletonRowLen, "host and device skeleton row limits differ");
+
 template <int NFD>
 __global__ void __launch_bounds__(kPcgThreads) pcg32_update_cells_kernel(Pcg32Args a, const float *__restrict__ p) {
   constexpr int BPT = kPcgThreads / NFD;  // block rows per tile
@@ -317,21 +323,31 @@ __global__ void __launch_bounds__(kPcgThreads) pcg32_update_cells_kernel(Pcg32Ar
   if (a.scal[SC_DONE] != 0.0) return;
   const float alpha = (float)a.scal[SC_ALPHA];
   const int lb = threadIdx.x / NFD, i = threadIdx.x - lb * NFD;
+  const float *__restrict__ qc = a.qc;
+  float *__restrict__ xg = a.x;
+  float *__restrict__ rg = a.r;
   double rz = 0.0, rr = 0.0;
   for (int br0 = blockIdx.x * BPT; br0 < a.nblockrows; br0 += gridDim.x * BPT) {
     const int nb = min(BPT, a.nblockrows - br0);
-    const float *Bg = a.Binv32 + (size_t)br0 * NFD * NFD;
-    for (int e = threadIdx.x; e < nb * NFD * NFD; e += blockDim.x) Bs[e] = Bg[e];
     const bool act = lb < nb;
     const int br = br0 + lb, row = br * NFD + i;
+    int2 src = make_int2(0, -1);
+    float pv = 0.0f, xv = 0.0f, r0 = 0.0f;
+    if (act) {
+      src = __ldg(reinterpret_cast<const int2 *>(a.br_src) + br);
+      pv = p[row];
+      xv = xg[row];
+      r0 = rg[row];
+    }
+    const float *Bg = a.Binv32 + (size_t)br0 * NFD * NFD;
+    for (int e = threadIdx.x; e < nb * NFD * NFD; e += blockDim.x) Bs[e] = __ldg(Bg + e);
     float rv = 0.0f;
     if (act) {
-      const int s0 = a.br_src[2 * br], s1 = a.br_src[2 * br + 1];
-      float q = a.qc[(size_t)s0 * NFD + i];
-      if (s1 >= 0) q += a.qc[(size_t)s1 * NFD + i];
-      a.x[row] = fmaf(alpha, p[row], a.x[row]);
-      rv = fmaf(-alpha, q, a.r[row]);
-      a.r[row] = rv;
+      float q = qc[(size_t)src.x * NFD + i];
+      if (src.y >= 0) q += qc[(size_t)src.y * NFD + i];
+      xg[row] = fmaf(alpha, pv, xv);
+      rv = fmaf(-alpha, q, r0);
+      rg[row] = rv;
       rr += (double)rv * rv;
     }
     rs[threadIdx.x] = rv;
@@ -347,13 +363,14 @@ __global__ void __launch_bounds__(kPcgThreads) pcg32_update_cells_kernel(Pcg32Ar
     }
     __syncthreads();
   }
+  const int np = (int)gridDim.x;
   double s = block_sum(rz, red);
   if (threadIdx.x == 0) a.partials[blockIdx.x] = s;
   s = block_sum(rr, red);
-  if (threadIdx.x == 0) a.partials[a.nparts + blockIdx.x] = s;
+  if (threadIdx.x == 0) a.partials[np + blockIdx.x] = s;
   if (last_cta(a.counter)) {
-    const double vrz = sum_partials(a.partials, a.nparts, 0, red);
-    const double vrr = sum_partials(a.partials, a.nparts, 1, red);
+    const double vrz = sum_partials(a.partials, np, 0, red);
+    const double vrr = sum_partials(a.partials, np, 1, red);
     if (threadIdx.x == 0) {
       a.scal[SC_BETA] = vrz / a.scal[SC_RZ];
       a.scal[SC_RZ] = vrz;
@@ -473,7 +490,7 @@ static size_t cellop_dyn_smem(int nstage) {
 }
 
 #define HDG_CELLOP_CASES(X) \
-  X(4, 2) X(4, 3) X(4, 4) X(4, 5) X(4, 6) X(4, 8) X(6, 4) X(6, 9) X(6, 12) X(6, 16) X(6, 25)
+  X(4, 2) X(4, 3) X(4, 4) X(4, 5) X(4, 6) X(4, 8) X(6, 4) X(6, 9) X(6, 12) X(6, 16) X(6, 25) X(6, 27)
 
 bool cellop_supported(int nl, int nfd) {
 #define X(L, F) \
@@ -536,9 +553,9 @@ static void cell_spmv(const Pcg32Args &a, const float *po, float *pn, cudaStream
 template <int NL, int NFD>
 static void pcg32_pair(const Pcg32Args &a, cudaStream_t s) {
   cell_spmv<NL, NFD>(a, a.p, a.p2, s);
-  pcg32_update_cells_kernel<NFD><<<a.nparts, kPcgThreads, 0, s>>>(a, a.p2);
+  pcg32_update_cells_kernel<NFD><<<a.uctas, kPcgThreads, 0, s>>>(a, a.p2);
   cell_spmv<NL, NFD>(a, a.p2, a.p, s);
-  pcg32_update_cells_kernel<NFD><<<a.nparts, kPcgThreads, 0, s>>>(a, a.p);
+  pcg32_update_cells_kernel<NFD><<<a.uctas, kPcgThreads, 0, s>>>(a, a.p);
 }
 
 cudaError_t launch_pcg32_iteration_pair(const Pcg32Args &a, cudaStream_t s, long long *launches) {
@@ -587,6 +604,7 @@ cudaError_t launch_outer_update(const OuterArgs &a, const float *e, cudaStream_t
     case 12: outer_residual_kernel<12><<<a.nparts, kPcgThreads, 0, s>>>(a); break;
     case 16: outer_residual_kernel<16><<<a.nparts, kPcgThreads, 0, s>>>(a); break;
     case 25: outer_residual_kernel<25><<<a.nparts, kPcgThreads, 0, s>>>(a); break;
+    case 27: outer_residual_kernel<27><<<a.nparts, kPcgThreads, 0, s>>>(a); break;
     default: return cudaErrorInvalidValue;
   }
   *launches += 2;

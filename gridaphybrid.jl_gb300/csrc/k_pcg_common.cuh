@@ -19,7 +19,7 @@ enum {
 };
 
 constexpr int kPcgThreads = 256;
-constexpr int kMaxRowLen = 288;  // 11 neighbour facets x 25 DOFs (3D, k=4) fits
+constexpr int kMaxRowLen = 304;  // 11 neighbour facets x 27 DOFs (3D elasticity, k=2) fits
 
 __device__ __forceinline__ double block_sum(double v, double *red) {
   for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);

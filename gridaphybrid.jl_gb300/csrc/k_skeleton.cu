@@ -126,7 +126,7 @@ cudaError_t launch_assemble(const AssembleArgs &a, const double *S, const double
     if (false) {
     }
     HDG_ASM(4, 2) HDG_ASM(4, 3) HDG_ASM(4, 4) HDG_ASM(4, 5) HDG_ASM(6, 1) HDG_ASM(6, 4) HDG_ASM(6, 9)
-    HDG_ASM(6, 16) HDG_ASM(6, 25) HDG_ASM(4, 1) HDG_ASM(4, 6) HDG_ASM(4, 8) HDG_ASM(6, 12)
+    HDG_ASM(6, 16) HDG_ASM(6, 25) HDG_ASM(4, 1) HDG_ASM(4, 6) HDG_ASM(4, 8) HDG_ASM(6, 12) HDG_ASM(6, 27)
     else return cudaErrorInvalidValue;
 #undef HDG_ASM
     ++*launches;
@@ -156,7 +156,7 @@ cudaError_t launch_assemble(const AssembleArgs &a, const double *S, const double
 // Inverse of each facet's diagonal block of sign*A (Gauss-Jordan, partial pivoting).
 __global__ void binv_kernel(PcgArgs a) {
   const int nfd = a.nfd;
-  double M[25 * 25], I[25 * 25];
+  double M[27 * 27], I[27 * 27];
   for (int br = blockIdx.x * blockDim.x + threadIdx.x; br < a.nblockrows;
        br += gridDim.x * blockDim.x) {
     const int blk = a.diag_blk[br];
@@ -378,7 +378,7 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_update_kernel(PcgArgs a, cons
 
 cudaError_t launch_pcg_setup(const PcgArgs &a, double rtol, cudaStream_t s, int num_sms,
                              long long *launches) {
-  if (a.nfd > 25) return cudaErrorInvalidValue;
+  if (a.nfd > 27) return cudaErrorInvalidValue;
   int g = (a.nblockrows + 127) / 128;
   if (g < 1) g = 1;
   cudaError_t e = cudaMemsetAsync(a.counter, 0, sizeof(unsigned int), s);
@@ -406,6 +406,7 @@ static cudaError_t spmv_dispatch(const PcgArgs &a, const V *val, const double *p
     HDG_SPMV_CASE(12)
     HDG_SPMV_CASE(16)
     HDG_SPMV_CASE(25)
+    HDG_SPMV_CASE(27)
 #undef HDG_SPMV_CASE
     default:
       return cudaErrorInvalidValue;
@@ -418,9 +419,9 @@ static cudaError_t spmv_any(const PcgArgs &a, const double *po, double *pn, cuda
 }
 
 bool pcg_supports_nfd(int nfd) {
-  // scalar traces (k+1)^(D-1); displacement traces D (k+1)^(D-1): 4, 6, 8 (2D), 12 (3D k=1)
+  // scalar traces (k+1)^(D-1); displacement traces D (k+1)^(D-1): 4, 6, 8 (2D), 12, 27 (3D k=1, 2)
   return nfd == 2 || nfd == 3 || nfd == 4 || nfd == 5 || nfd == 6 || nfd == 8 || nfd == 9 || nfd == 12 ||
-         nfd == 16 || nfd == 25;
+         nfd == 16 || nfd == 25 || nfd == 27;
 }
 
 cudaError_t launch_spmv(const PcgArgs &a, cudaStream_t s, long long *launches) {

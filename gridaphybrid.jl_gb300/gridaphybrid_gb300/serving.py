@@ -108,7 +108,7 @@ P_2D = 0.75
 N2D_MU, N2D_SIGMA, N2D_RANGE = 32.0, 0.7, (8, 256)
 N3D_MU, N3D_SIGMA, N3D_RANGE = 12.0, 0.45, (4, 48)
 K2D = (1, 2, 3)
-K3D = (1, 2)  # 3D k=3 cell blocks (n = 352) exceed one CTA's shared memory
+K3D = (1, 2, 3)
 
 
 def poisson_trace(rate=200.0, seconds=60.0, seed=0):

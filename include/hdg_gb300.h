@@ -43,10 +43,14 @@ extern "C" {
 /* Arithmetic of the cell-local work. */
 #define HDG_PREC_FP64 0          /* FP64 integration, LU and Schur complement */
 #define HDG_PREC_FP32_REFINED 1  /* FP32 LU, refined with high-precision residuals */
-/* Operator path only (hdg_assemble): the Darcy cell matrix's flux block is
- * (|J|/kappa)(I (x) M_ref), so the condensation is done by block elimination
- * (a small pressure-Schur LU and dense products) entirely in float-float on
- * the FP32 pipes; skeleton solve and recovery as for HDG_PREC_FP32_REFINED. */
+/* Operator path only (hdg_assemble): the first bulk block of the cell matrix
+ * is a reference mass matrix times a per-cell factor -- Darcy flux:
+ * (|J|/kappa)(I (x) M_ref); elasticity stress: |J| (C_nu (x) M_ref) -- so the
+ * condensation is done by block elimination (an LU of the second field's Schur
+ * complement and dense products) entirely in float-float on the FP32 pipes;
+ * skeleton solve and recovery as for HDG_PREC_FP32_REFINED.  D=2, k<=3 and
+ * D=3, k<=2.  FP64 elasticity cell blocks too large for the shared-memory LU
+ * (D=3, k=2) are condensed by the same block elimination in FP64. */
 #define HDG_PREC_FF_BLOCK 2
 
 /* Stabilisation of the Darcy HDG form. */

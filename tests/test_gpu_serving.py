@@ -111,16 +111,32 @@ def test_mesh_reuse_gives_the_fresh_result():
 def test_unsupported_shape_rejected_at_submit():
     with Server(slots=1) as srv:
         with pytest.raises(_lib.HdgError):
-            srv.submit(3, 4, 3, precision=_lib.HDG_PREC_FF_BLOCK)
+            srv.submit(3, 4, 4, precision=_lib.HDG_PREC_FF_BLOCK)
+        with pytest.raises(_lib.HdgError):
+            srv.submit(3, 4, 3, precision=_lib.HDG_PREC_FP32_REFINED)
         with pytest.raises(_lib.HdgError):
             srv.submit(2, 0, 1)
+
+
+@pytest.mark.parametrize("precision", [_lib.HDG_PREC_FF_BLOCK, _lib.HDG_PREC_FP64])
+def test_3d_k3_request_served(precision):
+    """3D k=3 (cell block n = 352, condensed by the L2-panel block
+    elimination) through the serving loop: the single-problem API's bits."""
+    kap = kappa_for(3, 4, 5)
+    with Server(slots=2) as srv:
+        t = srv.submit(3, 4, 3, kappa=kap, precision=precision, want_solution=True)
+        srv.drain()
+        res = {r["ticket"]: r for r in srv.poll(max_items=4)}
+    assert res[t]["status"] == 0
+    assert np.array_equal(res[t]["solution"], _solve_direct_api(3, 4, 3, kap, precision))
 
 
 def test_footprint_bounds_the_reserved_bytes():
     lib = _lib.load()
     for (D, n, k, prec) in [(2, 32, 1, _lib.HDG_PREC_FP64), (2, 24, 3, _lib.HDG_PREC_FF_BLOCK),
                             (3, 8, 2, _lib.HDG_PREC_FF_BLOCK), (3, 8, 2, _lib.HDG_PREC_FP64),
-                            (3, 6, 1, _lib.HDG_PREC_FP32_REFINED)]:
+                            (3, 6, 1, _lib.HDG_PREC_FP32_REFINED), (3, 5, 3, _lib.HDG_PREC_FF_BLOCK),
+                            (3, 5, 3, _lib.HDG_PREC_FP64)]:
         model = gh.CartesianDiscreteModel((0, 1) * D, (n,) * D)
         X, Y = gh.darcy_spaces(model, k)
         op = gh.HybridAffineFEOperator(gh.DarcyHDG(tau=1.0, problem="sin"), X, Y, [1, 2], [3], precision=prec)
