@@ -195,10 +195,12 @@ def run_serving(args, prec, prec64):
     if args.precision != "fp64" and args.serve_fp64_seconds > 0:
         runs.append(("fp64", prec64, args.serve_fp64_seconds))
     for name, p, limit in runs:
+        rejected = []
         with serving.Server(slots=args.serve_slots) as srv:
-            resp, wall = serving.run_trace(srv, trace, p, max_seconds=limit)
+            resp, wall = serving.run_trace(srv, trace, p, max_seconds=limit, rejected=rejected)
             st = srv.stats()
         summ = serving.latency_summary(resp, wall)
+        summ["rejected_over_budget"] = [list(r[:3]) for r in rejected]
         summ.update({"seconds_of_trace": limit or args.serve_seconds, "peak_hbm_gb": st["peak_bytes"] / 1e9,
                      "max_concurrent": int(st["max_concurrent"]), "mesh_hits": int(st["mesh_hits"]),
                      "evictions": int(st["evictions"])})

@@ -135,6 +135,7 @@ MixedTables mixed_tables(hdg_problem *pb) {
 // Phase launches on the problem's buffers, for the precision of the last assemble.
 cudaError_t run_integrate(hdg_problem *pb) {
   hdg_context *ctx = pb->ctx;
+  if (pb->eblock && pb->l2_fused) return cudaSuccess;  // integrated inside the condensation kernel
   CellArgs a = cell_args(pb);
   const size_t nc = pb->mesh.ncells, n = pb->tab.n;
   if (pb->physics == HDG_PHYSICS_ELASTICITY) {
@@ -142,8 +143,11 @@ cudaError_t run_integrate(hdg_problem *pb) {
       return launch_integrate_elasticity(a, pb->d_A.as<double>(), pb->d_b.as<double>(), nullptr, nullptr, nullptr,
                                          nullptr, ctx->stream, ctx->num_sms, &ctx->launches);
     float *Ahi = pb->d_A.as<float>(), *bhi = pb->d_b.as<float>();
+    // float-float entries for the block elimination; FP64 entries split for the FP32 LU + refinement
+    const MixedTables T = mixed_tables(pb);
+    const bool ffb = pb->precision == HDG_PREC_FF_BLOCK;
     return launch_integrate_elasticity(a, nullptr, nullptr, Ahi, Ahi + nc * n * n, bhi, bhi + nc * n, ctx->stream,
-                                       ctx->num_sms, &ctx->launches, pb->precision == HDG_PREC_FF_BLOCK);
+                                       ctx->num_sms, &ctx->launches, ffb, ffb ? &T : nullptr);
   }
   if (pb->precision == HDG_PREC_FP64)
     return launch_integrate_fp64(a, pb->d_A.as<double>(), pb->d_b.as<double>(), ctx->stream, ctx->num_sms,
@@ -157,6 +161,8 @@ cudaError_t run_integrate(hdg_problem *pb) {
 L2BlockLaunch l2block_launch(const hdg_problem *pb, size_t *need, bool dry_run) {
   L2BlockLaunch L{};
   L.elasticity = pb->physics == HDG_PHYSICS_ELASTICITY;
+  L.fused = pb->l2_fused;
+  L.nqv = pb->tab.nqv;
   L.D = pb->tab.D;
   L.k = pb->tab.k;
   L.fp64 = pb->precision == HDG_PREC_FP64;
@@ -178,6 +184,7 @@ cudaError_t run_condense_l2block(hdg_problem *pb) {
   A.g = pb->d_g.as<double>();
   A.info = pb->d_info.as<int>();
   A.scratch = pb->d_escratch.ptr;
+  A.Tb = mixed_tables(pb);
   const float *Mf = pb->d_minv.as<float>();
   if (pb->precision == HDG_PREC_FP64) {
     A.A0 = pb->d_A.ptr;
@@ -764,7 +771,7 @@ static float elapsed(cudaEvent_t a, cudaEvent_t b) {
 // Validates the precision for this problem and reserves the buffers of an
 // assembly.  cell_blocks: the separate integrate / condense kernels keep the
 // cell blocks A, b in HBM (the batched fused kernels do not).
-static int assemble_prepare(hdg_problem *pb, int precision, bool cell_blocks) {
+static int assemble_prepare(hdg_problem *pb, int precision, bool cell_blocks, bool allow_fused) {
   hdg_context *ctx = pb->ctx;
   if (precision != HDG_PREC_FP64 && precision != HDG_PREC_FP32_REFINED && precision != HDG_PREC_FF_BLOCK)
     return ctx->fail(HDG_ERR_INVALID, "unknown precision %d", precision);
@@ -792,6 +799,10 @@ static int assemble_prepare(hdg_problem *pb, int precision, bool cell_blocks) {
     CUDA_TRY(ctx, pb->d_invm.reserve(sizeof(double) * nc));
   pb->precision = precision;
   pb->eblock = eblock;
+  // the L2-panel kernel integrates its cells itself unless the caller needs
+  // the cell blocks (the Newton path's residuals)
+  pb->l2_fused = eblock && allow_fused;
+  if (pb->l2_fused) cell_blocks = false;
   if (eblock) {
     size_t scratch = 0;
     L2BlockArgs sizing{};
@@ -842,7 +853,7 @@ int hdg_assemble(hdg_problem *pb, int precision, int *info) {
   if (!pb) return HDG_ERR_INVALID;
   hdg_context *ctx = pb->ctx;
   cudaSetDevice(ctx->device);
-  int rc = assemble_prepare(pb, precision, true);
+  int rc = assemble_prepare(pb, precision, true, true);
   if (rc) return rc;
   const size_t nc = pb->mesh.ncells;
   cudaEvent_t *ev = ctx->ev;
@@ -1326,7 +1337,7 @@ int hdg_newton_solve(hdg_problem *pb, int solver, double lin_rtol, int lin_maxit
   if (!pb->form_set) return ctx->fail(HDG_ERR_STATE, "set the weak form first (hdg_set_darcy)");
   if (!(ftol > 0.0) || max_iters < 0) return ctx->fail(HDG_ERR_INVALID, "ftol must be > 0 and max_iters >= 0");
   cudaSetDevice(ctx->device);
-  int rc = assemble_prepare(pb, HDG_PREC_FP64, true);
+  int rc = assemble_prepare(pb, HDG_PREC_FP64, true, false);
   if (rc) return rc;
   const size_t nc = pb->mesh.ncells, ni = pb->tab.ni;
   const size_t w1 = first_field_width(pb), w2 = ni - w1;
@@ -1602,7 +1613,7 @@ int hdg_batch_assemble(hdg_batch *b, int precision, int *bad) {
       return ctx->fail(HDG_ERR_INVALID, "no fused batch kernel for D=%d k=%d at this precision", cl.D, cl.k);
   int rc;
   for (hdg_problem *pb : b->probs)
-    if ((rc = assemble_prepare(pb, precision, false))) return rc;
+    if ((rc = assemble_prepare(pb, precision, false, false))) return rc;
   for (DBuf *d : {&b->d_probs, &b->d_bad, &b->d_scratch}) d->stream = ctx->stream;
   // per-problem descriptors, class by class
   const size_t np = b->probs.size();

@@ -207,6 +207,8 @@ struct hdg_problem {
   // the elasticity cell blocks of this assembly are condensed by block
   // elimination (float-float, or FP64 when the dense block exceeds shared memory)
   bool eblock = false;
+  // ... integrating each cell into the kernel's L2 slot (no cell blocks in HBM)
+  bool l2_fused = false;
   cudaGraphExec_t pcg32_graph = nullptr;
   int cellop_nstage = 0, cellop_ctas = 0;  // streaming-kernel pipeline depth and grid
   // FP64 residual refinement of the FP32 skeleton solve: the inner reduction

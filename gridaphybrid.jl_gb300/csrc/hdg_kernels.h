@@ -211,12 +211,15 @@ struct L2BlockArgs {
   double *S, *g;
   void *X0, *X1;  // recovery X = A_ii^{-1} [A_if | b_i] (ni x (nf+1)), the same way; may be null
   int *info;
-  void *scratch;  // per-CTA panels
+  void *scratch;   // per-CTA panels (and the fused kernel's cell block)
+  MixedTables Tb;  // float-float reference tables (fused float-float integration)
 };
 struct L2BlockLaunch {
   bool elasticity;
   int D, k;
   bool fp64;
+  bool fused;  // integrate each cell into its CTA's slot instead of reading A, b from HBM
+  int nqv;     // quadrature points (the fused kernel's shared memory)
   size_t smem_optin;
   int num_sms;
   size_t scratch_bytes;        // bytes at args.scratch
@@ -373,12 +376,13 @@ cudaError_t launch_newton_update(size_t count, double *x, const double *dx, cuda
                                  long long *launches);
 
 // Linear elasticity HDG cells: blocks in FP64 (A, b) or as float-float pairs
-// (the entries computed in FP64 and split), and the stress / displacement L2
-// error contributions per cell (errs: 2 per cell).  skip_ss: the stress-stress
-// block is not written (the block elimination never reads it).
+// (with Tb: every entry computed in float-float from the float-float tables;
+// without: computed in FP64 and split), and the stress / displacement L2 error
+// contributions per cell (errs: 2 per cell).  skip_ss: the stress-stress block
+// is not written (the block elimination never reads it).
 cudaError_t launch_integrate_elasticity(const CellArgs &a, double *A, double *b, float *Ahi, float *Alo, float *bhi,
                                         float *blo, cudaStream_t s, int num_sms, long long *launches,
-                                        bool skip_ss = false);
+                                        bool skip_ss = false, const MixedTables *Tb = nullptr);
 cudaError_t launch_l2_errors_elasticity(const CellArgs &a, const double *uint, double *errs, cudaStream_t s,
                                         int num_sms, long long *launches);
 

@@ -114,12 +114,14 @@ double footprint_bound(int D, int n, int k, int precision, int solver) {
        nbnd * s.nfd * 8.0;
   // pattern and block maps
   b += (nfree + 1) * 8.0 + nnz * 4.0 + nbr * 4 * 4.0 + nblocks * 20.0 + ncells * 4.0 + ncells * nl * 4.0;
-  // cell blocks, condensed blocks, recovery factors, CSR values and rhs
-  b += ncells * ((double)s.n * s.n * 8 + s.n * 8 + (double)s.nf * s.nf * 8 + 2.0 * s.nf * 8 + 4) + nnz * 8 +
-       nfree * 8;
+  // cell blocks (not kept by the L2-panel kernel, which integrates each cell
+  // into its slot), condensed blocks, recovery factors, CSR values and rhs
+  const double blocks = l2block ? 0.0 : (double)s.n * s.n * 8 + s.n * 8;
+  b += ncells * (blocks + (double)s.nf * s.nf * 8 + 2.0 * s.nf * 8 + 4) + nnz * 8 + nfree * 8;
   b += fast || l2block ? 8.0 * ncells * s.ni * (s.nf + 1) : 8.0 * ncells * s.ni * (s.n + 1);
   if (precision == HDG_PREC_FF_BLOCK) b += ncells * 8.0;
-  if (l2block) b += 64.0 * (1 << 20);  // per-CTA panels (one CTA per SM)
+  if (l2block)  // per-CTA slots (one CTA per SM): panels Y, Z and the cell block
+    b += 160.0 * 8.0 * ((double)s.ni * (s.nf + 1) * 2 + (double)s.n * s.n + s.n);
   if (fast) b += ncells * cellop_rec(nl, s.nfd) * 4.0;
   // skeleton solve
   if (solver == HDG_SOLVER_DIRECT) {

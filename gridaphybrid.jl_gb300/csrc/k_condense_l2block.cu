@@ -18,15 +18,29 @@
 //   X_u = P^{-1} Q   (LU with partial pivoting of field 2's Schur complement)
 //   X_s = Z - Y X_u
 //   S = A_ff - A_fs X_s - A_fu X_u,   g = b_f - A_fs y_s - A_fu y_u
-// Structural zeros that hold on every affine cell are skipped:
+// Zeros are skipped (only exact zeros, so the results do not change):
 //   - elasticity: A_us / A_su couple displacement component k only to the
-//     stress components whose index pair contains k;
+//     stress components whose index pair contains k (every affine cell);
 //   - A_fs / A_fu / A_sf couple a trace row of facet F only to the volume
-//     nodes on F (Lagrange nodes off F vanish on F), found from the H table.
+//     nodes on F (Lagrange nodes off F vanish on F), found from the H table;
+//   - per cell, the components a trace row/column of (F, trace component j)
+//     couples to on those nodes, found by scanning the cell's entries (on
+//     an axis-aligned cell: one stress or flux component, one displacement
+//     component).
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "hdg_kernels.h"
+#include "k_elast_cell.cuh"
+#include "k_ff_cell.cuh"
 #include "k_ffblock_cell.cuh"
+#include "k_fp64_cell.cuh"
+
+// threads per CTA for the largest cells (3D elasticity k=2)
+#ifndef HDG_L2BLOCK_BIG_NT
+#define HDG_L2BLOCK_BIG_NT 512
+#endif
 
 namespace hdg {
 namespace be {
@@ -74,6 +88,10 @@ struct ArFF {
     static_cast<float *>(p0)[i] = v.h;
     static_cast<float *>(p1)[i] = v.l;
   }
+  // the same through the coherent path (data written earlier in this kernel)
+  static __device__ __forceinline__ V ldc(const void *p0, const void *p1, size_t i) {
+    return V{static_cast<const float *>(p0)[i], static_cast<const float *>(p1)[i]};
+  }
 };
 
 // plain FP64
@@ -93,6 +111,9 @@ struct Ar64 {
     return __ldg(static_cast<const double *>(p0) + i);
   }
   static __device__ __forceinline__ void st(void *p0, void *, size_t i, V v) { static_cast<double *>(p0)[i] = v; }
+  static __device__ __forceinline__ V ldc(const void *p0, const void *, size_t i) {
+    return static_cast<const double *>(p0)[i];
+  }
 };
 
 __host__ __device__ constexpr int ipow_c(int b, int e) { return e == 0 ? 1 : b * ipow_c(b, e - 1); }
@@ -105,11 +126,17 @@ struct ECfg {
   static constexpr int NS = NC1 * NK, NU = NC2 * NK;
   static constexpr int NI = NS + NU, NFS = ipow_c(K + 1, D - 1), NFD = NC2 * NFS, NL = 2 * D, NF = NL * NFD;
   static constexpr int N = NI + NF, NC = NF + 1;
-  static constexpr int NT = NU * NC >= 8192 ? 512 : 256;
+  // register-tile heights: rows of one field-2 component (phase 2), rows of
+  // one facet and trace component (phase 6)
+  static constexpr int TR = NK % 4 == 0 ? 4 : NK % 3 == 0 ? 3 : NK % 2 == 0 ? 2 : 1;
+  static constexpr int TF = NFS % 4 == 0 ? 4 : NFS % 3 == 0 ? 3 : NFS % 2 == 0 ? 2 : 1;
+  static constexpr int NT = NU * NC >= 8192 ? HDG_L2BLOCK_BIG_NT : 256;
   // shared: P (NU x NU), Q (NU x NC), M^{-1} (NK x NK), C^{-1}/|J| (6 x 6), as values
   static constexpr size_t smem_values = (size_t)NU * NU + (size_t)NU * NC + (size_t)NK * NK + 36;
-  // per-CTA scratch: Y (NS x NU), Z (NS x NC), column-major, as values
+  // per-CTA scratch: Y (NS x NU), Z (NS x NC), column-major, as values; the
+  // fused kernel adds the cell block A (N x N) and b (N)
   static constexpr size_t slot_values = (size_t)NS * NU + (size_t)NS * NC;
+  static constexpr size_t slot_values_fused = slot_values + (size_t)N * N + N;
 };
 
 // shared-memory bookkeeping beside the value arrays
@@ -117,14 +144,109 @@ template <class C>
 struct Lists {
   int fn_cnt[C::NL];          // volume nodes on local facet lf ...
   int fn_node[C::NL][C::NK];  // ... and their indices
+  int fn_max;                 // max over facets of fn_cnt
   int kmask[3];               // bit c: field-1 component c couples to field-2 component k
   int kc_cnt[3], kc_comp[3][6];
+  // this cell: bit c (field-1 component c) / bit NC1 + k (field-2 component k)
+  // is set when a trace row or column of (facet lf, trace component j) has a
+  // nonzero coupling to that component on the facet's nodes
+  int fmask[C::NL][3];
   int piv, info;
 };
 
 template <class C, class Ar>
 constexpr size_t smem_bytes() {
   return C::smem_values * sizeof(typename Ar::V) + sizeof(Lists<C>) + 16;
+}
+
+// the fused kernel's integration scratch: cell factors / terms, per-point
+// source values (nqv x (D+1)), the row decode table (elasticity)
+template <class C>
+size_t integ_bytes(int nqv) {
+  size_t fac = sizeof(ElastScratch);
+  if (sizeof(CellFactors) > fac) fac = sizeof(CellFactors);
+  if (sizeof(CellFactorsFF) > fac) fac = sizeof(CellFactorsFF);
+  fac = (fac + 15) / 16 * 16;
+  return fac + (size_t)nqv * (C::D + 1) * sizeof(double) + (size_t)C::N * sizeof(int) + 16;
+}
+
+// Cell `cell` integrated into the CTA's slot: A (column-major N x N, the
+// field-1 block left unwritten) and b, as (hi, lo) float arrays or FP64.
+template <class C, class Ar>
+__device__ void integrate_into_slot(const L2BlockArgs &a, int cell, void *A0, void *A1, void *b0, void *b1,
+                                    unsigned char *integ, int t) {
+  constexpr int N = C::N, NT = C::NT, NS = C::NS;
+  constexpr bool FF = !std::is_same<Ar, Ar64>::value;
+  const CellArgs &ca = a.cell;
+  size_t fac = sizeof(ElastScratch);
+  if (sizeof(CellFactors) > fac) fac = sizeof(CellFactors);
+  if (sizeof(CellFactorsFF) > fac) fac = sizeof(CellFactorsFF);
+  fac = (fac + 15) / 16 * 16;
+  double *fq = reinterpret_cast<double *>(integ + fac);
+  int *dec = reinterpret_cast<int *>(fq + (size_t)ca.nqv * (C::D + 1));
+  if constexpr (C::ELAST) {
+    ElastScratch &S = *reinterpret_cast<ElastScratch *>(integ);
+    for (int i = t; i < N; i += NT) dec[i] = elast_pack(ca, i);
+    elast_cell_prepare(ca, cell, S, fq, FF, t, NT);  // barriers inside
+    int i = t % N, j = t / N;
+    for (int e = t; e < N * N; e += NT) {
+      if (!(i < NS && j < NS)) {
+        if constexpr (FF) {
+          float h, l;
+          elast_entry_ff(ca, a.Tb, S.TF, dec[i], dec[j], h, l);
+          static_cast<float *>(A0)[e] = h;
+          static_cast<float *>(A1)[e] = l;
+        } else {
+          static_cast<double *>(A0)[e] = elast_entry_t(ca, S.f, S.T, dec[i], dec[j]);
+        }
+      }
+      i += NT % N;
+      j += NT / N;
+      if (i >= N) {
+        i -= N;
+        ++j;
+      }
+    }
+    for (int r = t; r < N; r += NT) {
+      const double v = elast_source_entry(ca, fq, r);
+      if constexpr (FF) {
+        split_double(v, static_cast<float *>(b0)[r], static_cast<float *>(b1)[r]);
+      } else {
+        static_cast<double *>(b0)[r] = v;
+      }
+    }
+    __syncthreads();
+  } else if constexpr (FF) {
+    CellFactorsFF &f = *reinterpret_cast<CellFactorsFF *>(integ);
+    integrate_cell_ff(ca, a.Tb, cell, true, f, fq, static_cast<float *>(A0), static_cast<float *>(A1),
+                      static_cast<float *>(b0), static_cast<float *>(b1), t, NT, true);  // barriers inside
+  } else {
+    CellFactors &f = *reinterpret_cast<CellFactors *>(integ);
+    if (t == 0) cell_factors(ca, cell, f);
+    __syncthreads();
+    source_values(ca, f, cell, fq, t, NT);
+    __syncthreads();
+    double *Ad = static_cast<double *>(A0);
+    for (int e = t; e < N * N; e += NT) {
+      const int j = e / N, i = e - j * N;
+      if (i < NS && j < NS) continue;
+      int ti, si, ii, tj, sj, jj;
+      decode(i, C::D, C::NK, ca.ni, ca.nfd, ti, si, ii);
+      decode(j, C::D, C::NK, ca.ni, ca.nfd, tj, sj, jj);
+      Ad[e] = cell_entry<double>(ca, f, ti, si, ii, tj, sj, jj);
+    }
+    for (int r = t; r < N; r += NT) {
+      int ti, si, ii;
+      decode(r, C::D, C::NK, ca.ni, ca.nfd, ti, si, ii);
+      double v = 0.0;
+      if (ti < 2) {
+        const int comp = ti == 0 ? si : C::D;
+        for (int q = 0; q < ca.nqv; ++q) v += fq[q * (C::D + 1) + comp] * ca.qphi[q * C::NK + ii];
+      }
+      static_cast<double *>(b0)[r] = v;
+    }
+    __syncthreads();
+  }
 }
 
 // C_nu^{-1} / |J| in FP64: Gauss-Jordan with partial pivoting on the compliance
@@ -171,7 +293,7 @@ __device__ void compliance_inverse(int D, int nsym, double E, double nu, double 
     for (int d = 0; d < nsym; ++d) Ci[c][d] = I[c][d] / detJ;
 }
 
-template <class C, class Ar>
+template <class C, class Ar, bool FUSED>
 __global__ void __launch_bounds__(C::NT, 1) condense_l2block_kernel(L2BlockArgs a) {
   using V = typename Ar::V;
   constexpr int D = C::D, NK = C::NK, NSYM = C::NC1, NC2 = C::NC2, NS = C::NS, NU = C::NU, NI = C::NI, NF = C::NF, N = C::N,
@@ -182,8 +304,21 @@ __global__ void __launch_bounds__(C::NT, 1) condense_l2block_kernel(L2BlockArgs 
   V *Mi = Q + (size_t)NU * NC;             // [a][k]
   V *Ci = Mi + NK * NK;                    // [c][d]
   Lists<C> &L = *reinterpret_cast<Lists<C> *>(Ci + 36);
-  V *Y = static_cast<V *>(a.scratch) + (size_t)blockIdx.x * C::slot_values;  // [m + NS j]
-  V *Z = Y + (size_t)NS * NU;                                                // [m + NS c]
+  unsigned char *integ = reinterpret_cast<unsigned char *>(&L + 1);
+  integ += (16 - reinterpret_cast<uintptr_t>(integ) % 16) % 16;
+  constexpr size_t slot = FUSED ? C::slot_values_fused : C::slot_values;
+  V *Y = static_cast<V *>(a.scratch) + (size_t)blockIdx.x * slot;  // [m + NS j]
+  V *Z = Y + (size_t)NS * NU;                                      // [m + NS c]
+  // the fused kernel's cell block in the slot: (hi, lo) float arrays or FP64
+  V *slotA = Z + (size_t)NS * NC;
+  void *sA0 = slotA, *sA1 = nullptr, *sb0 = nullptr, *sb1 = nullptr;
+  if constexpr (sizeof(V) == 8 && !std::is_same<Ar, Ar64>::value) {
+    sA1 = reinterpret_cast<float *>(slotA) + (size_t)N * N;
+    sb0 = reinterpret_cast<float *>(slotA) + 2 * (size_t)N * N;
+    sb1 = reinterpret_cast<float *>(slotA) + 2 * (size_t)N * N + N;
+  } else {
+    sb0 = reinterpret_cast<double *>(slotA) + (size_t)N * N;
+  }
   const CellArgs &ca = a.cell;
   const int t = threadIdx.x;
   for (int e = t; e < NK * NK; e += NT) Mi[e] = Ar::ld(a.Minv0, a.Minv1, e);
@@ -195,6 +330,12 @@ __global__ void __launch_bounds__(C::NT, 1) condense_l2block_kernel(L2BlockArgs 
       if (nz) L.fn_node[t][cnt++] = node;
     }
     L.fn_cnt[t] = cnt;
+  }
+  __syncthreads();
+  if (t == 0) {
+    int mx = 0;
+    for (int lf = 0; lf < NL; ++lf) mx = max(mx, L.fn_cnt[lf]);
+    L.fn_max = mx;
   }
   if (t == 0) {
     for (int k = 0; k < NC2; ++k) {
@@ -216,10 +357,21 @@ __global__ void __launch_bounds__(C::NT, 1) condense_l2block_kernel(L2BlockArgs 
     }
   }
   for (int cell = blockIdx.x; cell < a.ncells; cell += gridDim.x) {
-    const size_t A0 = (size_t)cell * N * N, b0 = (size_t)cell * N;
-    auto A = [&](int r, int c) { return Ar::ld(a.A0, a.A1, A0 + (size_t)r + (size_t)N * c); };
-    auto B = [&](int r) { return Ar::ld(a.b0, a.b1, b0 + r); };
-    __syncthreads();  // the previous cell's readers of the lists / Ci are done
+    const size_t A0 = FUSED ? 0 : (size_t)cell * N * N, b0 = FUSED ? 0 : (size_t)cell * N;
+    auto A = [&](int r, int c) {
+      if constexpr (FUSED)
+        return Ar::ldc(sA0, sA1, (size_t)r + (size_t)N * c);
+      else
+        return Ar::ld(a.A0, a.A1, A0 + (size_t)r + (size_t)N * c);
+    };
+    auto B = [&](int r) {
+      if constexpr (FUSED)
+        return Ar::ldc(sb0, sb1, (size_t)r);
+      else
+        return Ar::ld(a.b0, a.b1, b0 + r);
+    };
+    __syncthreads();  // the previous cell's readers of the lists / Ci / slot are done
+    if constexpr (FUSED) integrate_into_slot<C, Ar>(a, cell, sA0, sA1, sb0, sb1, integ, t);
     if (t == 0) {
       const double *J = ca.jac + (size_t)cell * D * D;
       const double det = D == 2 ? J[0] * J[3] - J[2] * J[1]
@@ -237,6 +389,21 @@ __global__ void __launch_bounds__(C::NT, 1) condense_l2block_kernel(L2BlockArgs 
         for (int d = 0; d < NSYM; ++d) Ci[c * 6 + d] = Ar::of(Cinv[c][d]);
       L.info = 0;
     }
+    if (t < NL * 3) L.fmask[t / 3][t % 3] = 0;
+    __syncthreads();
+    // the cell's trace couplings: entries of A_fi / A_if on the facet's nodes
+    // that are exactly zero are skipped below (they contribute nothing)
+    {
+      const int fm = L.fn_max;
+      for (int e = t; e < NF * (NSYM + NC2) * fm; e += NT) {
+        const int f = e % NF, rest = e / NF, cc = rest % (NSYM + NC2), q = rest / (NSYM + NC2);
+        const int lf = f / NFD, kf = (f - lf * NFD) / NFS;
+        if (q >= L.fn_cnt[lf]) continue;
+        const int node = L.fn_node[lf][q];
+        const int m = cc < NSYM ? cc * NK + node : NS + (cc - NSYM) * NK + node;
+        if (Ar::nonzero(A(NI + f, m)) || Ar::nonzero(A(m, NI + f))) atomicOr(&L.fmask[lf][kf], 1 << cc);
+      }
+    }
     __syncthreads();
     // 1. Y = A_ss^{-1} A_su and Z = A_ss^{-1} [A_sf | b_s]: M^{-1} on each
     //    stress component of the column, then the components mixed by C^{-1}/|J|
@@ -253,12 +420,14 @@ __global__ void __launch_bounds__(C::NT, 1) condense_l2block_kernel(L2BlockArgs 
             for (int k = 0; k < NK; ++k) Ar::mac(T[cp], Mi[an * NK + k], A(cp * NK + k, NS + col));
       } else if (col < NU + NF) {
         const int f = col - NU, lf = f / NFD, cnt = L.fn_cnt[lf];
+        const int msk = L.fmask[lf][(f - lf * NFD) / NFS];
 #pragma unroll
         for (int cp = 0; cp < NSYM; ++cp)
-          for (int q = 0; q < cnt; ++q) {
-            const int k = L.fn_node[lf][q];
-            Ar::mac(T[cp], Mi[an * NK + k], A(cp * NK + k, NI + f));
-          }
+          if (msk >> cp & 1)
+            for (int q = 0; q < cnt; ++q) {
+              const int k = L.fn_node[lf][q];
+              Ar::mac(T[cp], Mi[an * NK + k], A(cp * NK + k, NI + f));
+            }
       } else {
 #pragma unroll
         for (int cp = 0; cp < NSYM; ++cp)
@@ -280,24 +449,55 @@ __global__ void __launch_bounds__(C::NT, 1) condense_l2block_kernel(L2BlockArgs 
       }
     }
     __syncthreads();
-    // 2. P = A_uu - A_us Y,  Q = [A_uf | b_u] - A_us Z
-    for (int o = t; o < NU * (NU + NC); o += NT) {
-      const int r = o % NU, col = o / NU, kd = r / NK;
-      const bool isP = col < NU;
-      const V *x = isP ? Y + (size_t)NS * col : Z + (size_t)NS * (col - NU);
-      V acc = Ar::zero();
-      const int cnt = L.kc_cnt[kd];
-      for (int q = 0; q < cnt; ++q) {
-        const int m0 = L.kc_comp[kd][q] * NK;
-        for (int k = 0; k < NK; ++k) Ar::mac(acc, A(NS + r, m0 + k), x[m0 + k]);
+    // 2. P = A_uu - A_us Y,  Q = [A_uf | b_u] - A_us Z, register tiles of
+    //    TR rows (one field-2 component) x 4 columns
+    {
+      constexpr int TR = C::TR, RT = NU / TR, CT = (NU + NC + 3) / 4;
+      for (int o = t; o < RT * CT; o += NT) {
+        const int r0 = (o % RT) * TR, col0 = (o / RT) * 4, kd = r0 / NK;
+        const V *xp[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int col = min(col0 + j, NU + NC - 1);
+          xp[j] = col < NU ? Y + (size_t)NS * col : Z + (size_t)NS * (col - NU);
+        }
+        V acc[TR][4];
+#pragma unroll
+        for (int i = 0; i < TR; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) acc[i][j] = Ar::zero();
+        const int cnt = L.kc_cnt[kd];
+        for (int q = 0; q < cnt; ++q) {
+          const int m0 = L.kc_comp[kd][q] * NK;
+#pragma unroll 3
+          for (int k = 0; k < NK; ++k) {
+            V av[TR], xv[4];
+#pragma unroll
+            for (int i = 0; i < TR; ++i) av[i] = A(NS + r0 + i, m0 + k);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) xv[j] = xp[j][m0 + k];
+#pragma unroll
+            for (int i = 0; i < TR; ++i)
+#pragma unroll
+              for (int j = 0; j < 4; ++j) Ar::mac(acc[i][j], av[i], xv[j]);
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int col = col0 + j;
+          if (col >= NU + NC) continue;
+#pragma unroll
+          for (int i = 0; i < TR; ++i) {
+            const int r = r0 + i;
+            const V rv = col < NU ? A(NS + r, NS + col) : col - NU < NF ? A(NS + r, NI + col - NU) : B(NS + r);
+            const V v = Ar::sub(rv, Ar::fin(acc[i][j]));
+            if (col < NU)
+              P[r * NU + col] = v;
+            else
+              Q[r * NC + col - NU] = v;
+          }
+        }
       }
-      acc = Ar::fin(acc);
-      const V r0 = isP ? A(NS + r, NS + col) : col - NU < NF ? A(NS + r, NI + col - NU) : B(NS + r);
-      const V v = Ar::sub(r0, acc);
-      if (isP)
-        P[r * NU + col] = v;
-      else
-        Q[r * NC + col - NU] = v;
     }
     __syncthreads();
     // 3. LU with partial pivoting of [P | Q]; the pivot search is warp 0's
@@ -368,37 +568,94 @@ __global__ void __launch_bounds__(C::NT, 1) condense_l2block_kernel(L2BlockArgs 
       }
       __syncthreads();
     }
-    // 5. X_s = Z - Y X_u, in Z
-    for (int o = t; o < NS * NC; o += NT) {
-      const int m = o % NS, c = o / NS;
-      V acc = Ar::zero();
-      for (int k = 0; k < NU; ++k) Ar::mac(acc, Y[m + (size_t)NS * k], Q[k * NC + c]);
-      Z[m + (size_t)NS * c] = Ar::sub(Z[m + (size_t)NS * c], Ar::fin(acc));
+    // 5. X_s = Z - Y X_u, in Z: register tiles of 4 x 4
+    {
+      constexpr int MT = (NS + 3) / 4, CT = (NC + 3) / 4;
+      for (int o = t; o < MT * CT; o += NT) {
+        const int m0 = (o % MT) * 4, c0 = (o / MT) * 4;
+        int mi[4], cj[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          mi[i] = min(m0 + i, NS - 1);
+          cj[i] = min(c0 + i, NC - 1);
+        }
+        V acc[4][4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) acc[i][j] = Ar::zero();
+#pragma unroll 3
+        for (int k = 0; k < NU; ++k) {
+          V yv[4], xv[4];
+#pragma unroll
+          for (int i = 0; i < 4; ++i) yv[i] = Y[mi[i] + (size_t)NS * k];
+#pragma unroll
+          for (int j = 0; j < 4; ++j) xv[j] = Q[k * NC + cj[j]];
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) Ar::mac(acc[i][j], yv[i], xv[j]);
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j)
+            if (m0 + i < NS && c0 + j < NC) {
+              const size_t e = (size_t)(m0 + i) + (size_t)NS * (c0 + j);
+              Z[e] = Ar::sub(Z[e], Ar::fin(acc[i][j]));
+            }
+      }
     }
     __syncthreads();
-    // 6. S = A_ff - A_fs X_s - A_fu X_u and g, over the volume nodes on the row's facet
-    for (int o = t; o < NF * NC; o += NT) {
-      const int f = o % NF, c = o / NF, lf = f / NFD, cnt = L.fn_cnt[lf];
-      V acc = Ar::zero();
-      for (int q = 0; q < cnt; ++q) {
-        const int node = L.fn_node[lf][q];
+    // 6. S = A_ff - A_fs X_s - A_fu X_u and g, over the volume nodes on the
+    //    rows' facet: register tiles of TF rows (one facet) x 4 columns
+    {
+      constexpr int TF = C::TF, FT = NF / TF, CT = (NC + 3) / 4;
+      for (int o = t; o < FT * CT; o += NT) {
+        const int f0 = (o % FT) * TF, c0 = (o / FT) * 4, lf = f0 / NFD, cnt = L.fn_cnt[lf];
+        const int msk = L.fmask[lf][(f0 - lf * NFD) / NFS];  // the tile's rows share (lf, trace component)
+        int cj[4];
 #pragma unroll
-        for (int cc = 0; cc < NSYM; ++cc) {
-          const int m = cc * NK + node;
-          Ar::mac(acc, A(NI + f, m), Z[m + (size_t)NS * c]);
+        for (int j = 0; j < 4; ++j) cj[j] = min(c0 + j, NC - 1);
+        V acc[TF][4];
+#pragma unroll
+        for (int i = 0; i < TF; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) acc[i][j] = Ar::zero();
+        for (int q = 0; q < cnt; ++q) {
+          const int node = L.fn_node[lf][q];
+#pragma unroll
+          for (int cc = 0; cc < NSYM + NC2; ++cc) {
+            if (!(msk >> cc & 1)) continue;
+            const bool s1 = cc < NSYM;
+            const int m = s1 ? cc * NK + node : NS + (cc - NSYM) * NK + node;
+            V av[TF], xv[4];
+#pragma unroll
+            for (int i = 0; i < TF; ++i) av[i] = A(NI + f0 + i, m);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) xv[j] = s1 ? Z[m + (size_t)NS * cj[j]] : Q[(m - NS) * NC + cj[j]];
+#pragma unroll
+            for (int i = 0; i < TF; ++i)
+#pragma unroll
+              for (int j = 0; j < 4; ++j) Ar::mac(acc[i][j], av[i], xv[j]);
+          }
         }
 #pragma unroll
-        for (int kd = 0; kd < NC2; ++kd) {
-          const int u = kd * NK + node;
-          Ar::mac(acc, A(NI + f, NS + u), Q[u * NC + c]);
+        for (int j = 0; j < 4; ++j) {
+          const int c = c0 + j;
+          if (c >= NC) continue;
+#pragma unroll
+          for (int i = 0; i < TF; ++i) {
+            const int f = f0 + i;
+            const V rhs = c < NF ? A(NI + f, NI + c) : B(NI + f);
+            const double v = Ar::dbl(rhs) - Ar::dbl(Ar::fin(acc[i][j]));
+            if (c < NF)
+              a.S[(size_t)cell * NF * NF + f + (size_t)NF * c] = v;
+            else
+              a.g[(size_t)cell * NF + f] = v;
+          }
         }
       }
-      const V rhs = c < NF ? A(NI + f, NI + c) : B(NI + f);
-      const double v = Ar::dbl(rhs) - Ar::dbl(Ar::fin(acc));
-      if (c < NF)
-        a.S[(size_t)cell * NF * NF + f + (size_t)NF * c] = v;
-      else
-        a.g[(size_t)cell * NF + f] = v;
     }
     // 7. X = [X_s; X_u] (NI x NC, column-major) for the recovery
     if (a.X0) {
@@ -412,10 +669,10 @@ __global__ void __launch_bounds__(C::NT, 1) condense_l2block_kernel(L2BlockArgs 
   }
 }
 
-template <class C, class Ar>
+template <class C, class Ar, bool FUSED>
 cudaError_t launch_cfg(const L2BlockArgs &args, const L2BlockLaunch &L, cudaStream_t s, long long *launches) {
-  auto kern = condense_l2block_kernel<C, Ar>;
-  const size_t smem = smem_bytes<C, Ar>();
+  auto kern = condense_l2block_kernel<C, Ar, FUSED>;
+  const size_t smem = smem_bytes<C, Ar>() + (FUSED ? integ_bytes<C>(L.nqv) + 16 : 0);
   if (smem > L.smem_optin) return cudaErrorInvalidConfiguration;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
@@ -426,7 +683,7 @@ cudaError_t launch_cfg(const L2BlockArgs &args, const L2BlockLaunch &L, cudaStre
   long long grid = (long long)per_sm * L.num_sms;
   if (grid > args.ncells) grid = args.ncells;
   if (grid < 1) grid = 1;
-  const size_t need = (size_t)grid * C::slot_values * sizeof(typename Ar::V);
+  const size_t need = (size_t)grid * (FUSED ? C::slot_values_fused : C::slot_values) * sizeof(typename Ar::V);
   if (L.scratch_bytes_out) *L.scratch_bytes_out = need;
   if (L.dry_run) return cudaSuccess;
   if (need > L.scratch_bytes || !args.scratch) return cudaErrorMemoryAllocation;
@@ -444,10 +701,16 @@ bool l2block_supported(bool elasticity, int D, int k) {
 
 cudaError_t launch_condense_l2block(const L2BlockArgs &args, const L2BlockLaunch &L, cudaStream_t s,
                                     long long *launches) {
-#define HDG_L2B(EL, DD, KK)                                                                    \
-  if (L.elasticity == EL && L.D == DD && L.k == KK)                                            \
-    return L.fp64 ? be::launch_cfg<be::ECfg<DD, KK, EL>, be::Ar64>(args, L, s, launches)       \
-                  : be::launch_cfg<be::ECfg<DD, KK, EL>, be::ArFF>(args, L, s, launches);
+  // fused (integration in the slot): float-float and FP64; cell blocks from
+  // HBM: FP64 only (the Newton path keeps them for its residuals)
+  if (!L.fused && !L.fp64) return cudaErrorInvalidValue;
+#define HDG_L2B(EL, DD, KK)                                                                        \
+  if (L.elasticity == EL && L.D == DD && L.k == KK) {                                              \
+    using CF = be::ECfg<DD, KK, EL>;                                                               \
+    if (!L.fused) return be::launch_cfg<CF, be::Ar64, false>(args, L, s, launches);                \
+    return L.fp64 ? be::launch_cfg<CF, be::Ar64, true>(args, L, s, launches)                       \
+                  : be::launch_cfg<CF, be::ArFF, true>(args, L, s, launches);                      \
+  }
   HDG_L2B(true, 2, 1)
   HDG_L2B(true, 2, 2)
   HDG_L2B(true, 2, 3)

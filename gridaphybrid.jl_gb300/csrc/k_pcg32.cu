@@ -168,6 +168,42 @@ __global__ void pack_cell_blocks_kernel(int ncells, int nl, int nfd, int rec, do
   }
 }
 
+// The same records for large cells (the whole S_c does not fit a CTA's
+// shared memory several times over): one work item per (cell, upper block),
+// the block and its transposed partner staged as two nfd x nfd tiles.
+__global__ void pack_cell_blocks_tiled_kernel(int ncells, int nl, int nfd, int rec, double sign,
+                                              const double *__restrict__ S, float *__restrict__ out) {
+  extern __shared__ double T[];  // 2 nfd^2
+  const int nf = nl * nfd, nb = nfd * nfd, nblk = nl * (nl + 1) / 2;
+  double *T1 = T, *T2 = T + nb;
+  const long long items = (long long)ncells * nblk;
+  for (long long it = blockIdx.x; it < items; it += gridDim.x) {
+    const int c = (int)(it / nblk), blk = (int)(it - (long long)c * nblk);
+    int lo = 0, rem = blk;
+    while (rem >= nl - lo) {
+      rem -= nl - lo;
+      ++lo;
+    }
+    const int hi = lo + rem;
+    const double *Sc = S + (size_t)c * nf * nf;
+    // T1[r + nfd s] = S(lo nfd + r, hi nfd + s), T2[r + nfd s] = S(hi nfd + r, lo nfd + s)
+    for (int e = threadIdx.x; e < nb; e += blockDim.x) {
+      const int s = e / nfd, r = e - s * nfd;
+      T1[e] = Sc[(size_t)(lo * nfd + r) + (size_t)nf * (hi * nfd + s)];
+      T2[e] = Sc[(size_t)(hi * nfd + r) + (size_t)nf * (lo * nfd + s)];
+    }
+    __syncthreads();
+    float *o = out + (size_t)c * rec + (size_t)blk * nb;
+    for (int w = threadIdx.x; w < nb; w += blockDim.x) {
+      const int r = w / nfd, s = w - r * nfd;
+      o[w] = (float)(0.5 * sign * (T1[r + nfd * s] + T2[s + nfd * r]));
+    }
+    if (blk == nblk - 1)  // the record's padding
+      for (int e = nblk * nb + threadIdx.x; e < rec; e += blockDim.x) out[(size_t)c * rec + e] = 0.0f;
+    __syncthreads();
+  }
+}
+
 constexpr int kMaxBulkStages = 8;
 
 template <int NL, int NFD>
@@ -312,6 +348,16 @@ __global__ void __launch_bounds__(CellOp<NL, NFD>::THREADS)
 // (source cells, then their products); the grid (a.uctas, up to eight CTAs
 // per SM) keeps enough tiles in flight to hide them.
 static_assert(kPcgThreads == kPcgThreadsHost, "host and device PCG block sizes differ");
+
+// 4-byte global -> shared copy that does not stall the issuing thread
+__device__ __forceinline__ void cp_async4(float *dst, const float *src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  const size_t g = __cvta_generic_to_global(src);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(g) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit_wait_all() {
+  asm volatile("cp.async.commit_group;\ncp.async.wait_all;\n" ::: "memory");
+}
 static_assert(kMaxRowLen == kMaxSkeletonRowLen, "host and device skeleton row limits differ");
 
 template <int NFD>
@@ -339,8 +385,9 @@ __global__ void __launch_bounds__(kPcgThreads) pcg32_update_cells_kernel(Pcg32Ar
       xv = xg[row];
       r0 = rg[row];
     }
+    // the tile's block inverses: asynchronous 4-byte copies, all in flight at once
     const float *Bg = a.Binv32 + (size_t)br0 * NFD * NFD;
-    for (int e = threadIdx.x; e < nb * NFD * NFD; e += blockDim.x) Bs[e] = __ldg(Bg + e);
+    for (int e = threadIdx.x; e < nb * NFD * NFD; e += blockDim.x) cp_async4(Bs + e, Bg + e);
     float rv = 0.0f;
     if (act) {
       float q = qc[(size_t)src.x * NFD + i];
@@ -351,6 +398,7 @@ __global__ void __launch_bounds__(kPcgThreads) pcg32_update_cells_kernel(Pcg32Ar
       rr += (double)rv * rv;
     }
     rs[threadIdx.x] = rv;
+    cp_async_commit_wait_all();
     __syncthreads();
     if (act) {
       const float *B = Bs + lb * NFD * NFD + i * NFD;
@@ -504,10 +552,12 @@ template <int NL, int NFD>
 static cudaError_t cellop_configure_t(size_t smem_optin, int num_sms, int *nstage, int *ctas) {
   using C = CellOp<NL, NFD>;
   const size_t stage = (size_t)C::CPS * C::REC * sizeof(float);
-  // about 108 KB of records in flight per CTA, two CTAs per SM where they fit
+  // about 108 KB of records in flight per CTA, two CTAs per SM where they fit;
+  // large records (one cell of 3D elasticity k=2: 61 KB) get three stages, so
+  // two copies are in flight while one stage is computed
   int ns = (int)((110 * 1024) / stage);
   ns = ns > kMaxBulkStages ? kMaxBulkStages : ns;
-  if (ns < 2) ns = 2;
+  if (ns < 3) ns = 3;
   while (ns > 2 && (size_t)ns * stage + 4096 > smem_optin) --ns;
   if ((size_t)ns * stage + 4096 > smem_optin) return cudaErrorInvalidValue;
   const size_t dyn = cellop_dyn_smem<NL, NFD>(ns);
@@ -535,7 +585,16 @@ cudaError_t launch_pack_cell_blocks(int ncells, int nl, int nfd, double sign, co
                                     size_t smem_optin, cudaStream_t s, int num_sms, long long *launches) {
   const int nf = nl * nfd;
   const size_t smem = sizeof(double) * nf * nf;
-  if (smem > smem_optin) return cudaErrorInvalidValue;
+  if (smem > 64 * 1024) {  // large cells: block-pair tiles
+    const size_t tsmem = 2 * sizeof(double) * nfd * nfd;
+    if (tsmem > 48 * 1024) return cudaErrorInvalidValue;
+    const long long items = (long long)ncells * (nl * (nl + 1) / 2);
+    long long grid = items < (long long)num_sms * 16 ? items : (long long)num_sms * 16;
+    if (grid < 1) grid = 1;
+    pack_cell_blocks_tiled_kernel<<<(int)grid, 256, tsmem, s>>>(ncells, nl, nfd, cellop_rec(nl, nfd), sign, S, out);
+    ++*launches;
+    return cudaGetLastError();
+  }
   cudaError_t e = cudaFuncSetAttribute(pack_cell_blocks_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int grid = ncells < num_sms * 16 ? ncells : num_sms * 16;

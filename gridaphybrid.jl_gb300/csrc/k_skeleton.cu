@@ -154,52 +154,75 @@ cudaError_t launch_assemble(const AssembleArgs &a, const double *S, const double
 // replayed; once SC_DONE is set every kernel returns immediately.
 // ---------------------------------------------------------------------------
 // Inverse of each facet's diagonal block of sign*A (Gauss-Jordan, partial pivoting).
-__global__ void binv_kernel(PcgArgs a) {
-  const int nfd = a.nfd;
-  double M[27 * 27], I[27 * 27];
-  for (int br = blockIdx.x * blockDim.x + threadIdx.x; br < a.nblockrows;
-       br += gridDim.x * blockDim.x) {
+// Facet-block inverses of the block-Jacobi preconditioner: one warp per
+// skeleton block row, Gauss-Jordan with partial pivoting on [sign*D | I] in
+// shared memory (lanes over the 2 nfd columns); a singular block gets the
+// identity.
+constexpr int kBinvWarps = 4;
+__global__ void __launch_bounds__(32 * kBinvWarps) binv_kernel(PcgArgs a) {
+  extern __shared__ double Wsm[];  // kBinvWarps x nfd x 2 nfd
+  const int nfd = a.nfd, w2 = 2 * nfd;
+  const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+  double *W = Wsm + (size_t)wl * nfd * w2;
+  const int nw = gridDim.x * kBinvWarps;
+  for (int br = blockIdx.x * kBinvWarps + wl; br < a.nblockrows; br += nw) {
     const int blk = a.diag_blk[br];
     const int64_t off = a.blk_off[blk];
     const int rl = a.blk_rowlen[blk];
-    for (int i = 0; i < nfd; ++i)
-      for (int j = 0; j < nfd; ++j) {
-        M[i * nfd + j] = a.sign * a.val[off + (int64_t)i * rl + j];
-        I[i * nfd + j] = (i == j) ? 1.0 : 0.0;
-      }
+    for (int e = lane; e < nfd * w2; e += 32) {
+      const int i = e / w2, j = e - i * w2;
+      W[e] = j < nfd ? a.sign * a.val[off + (int64_t)i * rl + j] : (j - nfd == i ? 1.0 : 0.0);
+    }
+    __syncwarp();
+    bool singular = false;
     for (int c = 0; c < nfd; ++c) {
-      int pr = c;
-      for (int i = c + 1; i < nfd; ++i)
-        if (fabs(M[i * nfd + c]) > fabs(M[pr * nfd + c])) pr = i;
-      if (M[pr * nfd + c] == 0.0) {
-        for (int i = 0; i < nfd * nfd; ++i) I[i] = (i % (nfd + 1) == 0) ? 1.0 : 0.0;
+      double best = -1.0;
+      int bi = c;
+      for (int i = c + lane; i < nfd; i += 32) {
+        const double v = fabs(W[i * w2 + c]);
+        if (v > best) {
+          best = v;
+          bi = i;
+        }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ob > best || (ob == best && oi < bi)) {
+          best = ob;
+          bi = oi;
+        }
+      }
+      if (!(best > 0.0)) {
+        singular = true;
         break;
       }
-      if (pr != c)
-        for (int j = 0; j < nfd; ++j) {
-          double t = M[c * nfd + j];
-          M[c * nfd + j] = M[pr * nfd + j];
-          M[pr * nfd + j] = t;
-          t = I[c * nfd + j];
-          I[c * nfd + j] = I[pr * nfd + j];
-          I[pr * nfd + j] = t;
+      if (bi != c)
+        for (int j = lane; j < w2; j += 32) {
+          const double t = W[c * w2 + j];
+          W[c * w2 + j] = W[bi * w2 + j];
+          W[bi * w2 + j] = t;
         }
-      const double piv = 1.0 / M[c * nfd + c];
-      for (int j = 0; j < nfd; ++j) {
-        M[c * nfd + j] *= piv;
-        I[c * nfd + j] *= piv;
-      }
+      __syncwarp();
+      const double piv = 1.0 / W[c * w2 + c];
+      __syncwarp();
+      for (int j = lane; j < w2; j += 32) W[c * w2 + j] *= piv;
+      // column c of every row, held by lane i (nfd <= 32)
+      const double fl = lane < nfd ? W[lane * w2 + c] : 0.0;
+      __syncwarp();
       for (int i = 0; i < nfd; ++i) {
-        if (i == c) continue;
-        const double fct = M[i * nfd + c];
-        if (fct != 0.0)
-          for (int j = 0; j < nfd; ++j) {
-            M[i * nfd + j] -= fct * M[c * nfd + j];
-            I[i * nfd + j] -= fct * I[c * nfd + j];
-          }
+        const double f = __shfl_sync(0xffffffffu, fl, i);
+        if (i == c || f == 0.0) continue;
+        for (int j = lane; j < w2; j += 32) W[i * w2 + j] -= f * W[c * w2 + j];
       }
+      __syncwarp();
     }
-    for (int i = 0; i < nfd * nfd; ++i) a.Binv[(size_t)br * nfd * nfd + i] = I[i];
+    double *out = a.Binv + (size_t)br * nfd * nfd;
+    for (int e = lane; e < nfd * nfd; e += 32) {
+      const int i = e / nfd, j = e - i * nfd;
+      out[e] = singular ? (i == j ? 1.0 : 0.0) : W[i * w2 + nfd + j];
+    }
+    __syncwarp();
   }
 }
 
@@ -379,14 +402,14 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_update_kernel(PcgArgs a, cons
 cudaError_t launch_pcg_setup(const PcgArgs &a, double rtol, cudaStream_t s, int num_sms,
                              long long *launches) {
   if (a.nfd > 27) return cudaErrorInvalidValue;
-  int g = (a.nblockrows + 127) / 128;
+  int g = (a.nblockrows + kBinvWarps - 1) / kBinvWarps;
+  if (g > num_sms * 16) g = num_sms * 16;
   if (g < 1) g = 1;
   cudaError_t e = cudaMemsetAsync(a.counter, 0, sizeof(unsigned int), s);
   if (e != cudaSuccess) return e;
-  binv_kernel<<<g, 128, 0, s>>>(a);
+  binv_kernel<<<g, 32 * kBinvWarps, sizeof(double) * kBinvWarps * a.nfd * 2 * a.nfd, s>>>(a);
   pcg_init_kernel<<<a.nparts, kPcgThreads, 0, s>>>(a, rtol);
   *launches += 2;
-  (void)num_sms;
   return cudaGetLastError();
 }
 

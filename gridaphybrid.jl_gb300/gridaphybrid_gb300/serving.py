@@ -133,8 +133,11 @@ def kappa_for(D, n, seed):
     return np.exp(np.random.default_rng(seed).normal(size=n ** D))
 
 
-def run_trace(server, trace, precision, rtol=1e-10, max_seconds=None):
-    """Submits each request at its arrival time; returns (responses, wall seconds)."""
+def run_trace(server, trace, precision, rtol=1e-10, max_seconds=None, rejected=None):
+    """Submits each request at its arrival time; returns (responses, wall
+    seconds).  A request the server refuses at submit (its footprint exceeds
+    the whole HBM budget) is appended to `rejected` as (D, n, k, message) when
+    a list is given, and re-raised otherwise."""
     t0 = time.perf_counter()
     resp = []
     pending = 0
@@ -147,7 +150,13 @@ def run_trace(server, trace, precision, rtol=1e-10, max_seconds=None):
                 break
             resp += server.poll(timeout_ms=0.0)
             time.sleep(min(ta - now, 0.002))
-        server.submit(D, n, k, kappa=kappa_for(D, n, ks), precision=precision, rtol=rtol)
+        try:
+            server.submit(D, n, k, kappa=kappa_for(D, n, ks), precision=precision, rtol=rtol)
+        except _lib.HdgError as e:
+            if rejected is None:
+                raise
+            rejected.append((D, n, k, str(e)))
+            continue
         pending += 1
     server.drain()
     resp += server.poll(timeout_ms=0.0, max_items=max(256, pending))
