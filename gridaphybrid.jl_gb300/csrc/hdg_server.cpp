@@ -2,9 +2,11 @@
 // and coefficient fields, admitted as worker slots and HBM budget free up and
 // run concurrently, each on its own stream.
 //
-// Threads: `slots` workers share one queue.  A worker takes the first queued
-// request that fits in the budget (a request may be passed by smaller ones at
-// most kMaxBypass times, after which admission waits for it), reuses an idle
+// Threads: `slots` workers share one queue.  A worker takes the first request
+// in priority order that fits in the budget -- requests that have waited
+// kAgeMs in arrival order, then the others shortest estimated work first (the
+// first in that order may be passed by others at most kMaxBypass times when
+// it does not fit, after which admission waits for it) -- reuses an idle
 // resident mesh of the same shape when there is one (connectivity, pattern
 // and every device buffer stay on the GPU between requests), solves through
 // the same entry points as a single-problem caller, and posts the response.
@@ -145,6 +147,9 @@ namespace {
 using Clock = std::chrono::steady_clock;
 
 constexpr int kMaxBypass = 8;
+// admission order: requests that have waited this long first (in arrival
+// order), then the rest shortest estimated work first
+constexpr double kAgeMs = 1000.0;
 // resident meshes that are idle may hold at most this share of the budget
 constexpr double kIdleShare = 0.5;
 
@@ -166,6 +171,7 @@ struct Job {
   hdg_request req{};
   std::vector<double> kappa;
   double footprint = 0.0;
+  double work = 0.0;  // estimated device work: cells x (cell block size)^2
   Clock::time_point t_submit;
   int bypassed = 0;
 };
@@ -215,7 +221,19 @@ struct hdg_server {
   // With mu held: picks the next admissible job; moves it to `job`, and the
   // resident mesh to reuse (or null) to `res`; evicted meshes go to `trash`.
   bool admit(Job &job, std::unique_ptr<Resident> &res, std::vector<std::unique_ptr<Resident>> &trash) {
-    for (size_t qi = 0; qi < queue.size(); ++qi) {
+    // priority order: aged requests in arrival order, then shortest work first
+    const Clock::time_point now = Clock::now();
+    std::vector<size_t> order(queue.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+    auto aged = [&](size_t i) { return ms_between(queue[i].t_submit, now) >= kAgeMs; };
+    std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) {
+      const bool ax = aged(x), ay = aged(y);
+      if (ax != ay) return ax;
+      if (ax) return x < y;
+      return queue[x].work < queue[y].work;
+    });
+    for (size_t oi = 0; oi < order.size(); ++oi) {
+      const size_t qi = order[oi];
       Job &j = queue[qi];
       const hdg_request &q = j.req;
       int match = -1;
@@ -227,7 +245,7 @@ struct hdg_server {
       // a reused mesh is already charged; only growth beyond it is new
       const double need = std::max(0.0, j.footprint - (keep ? keep->bytes : 0.0));
       if (in_use + need > budget && in_use + need - evictable(keep) > budget) {
-        if (qi == 0 && ++j.bypassed > kMaxBypass) return false;  // the head waits for memory
+        if (oi == 0 && ++j.bypassed > kMaxBypass) return false;  // the first in order waits for memory
         continue;
       }
       // evict least-recently-used idle meshes until the job fits
@@ -418,6 +436,10 @@ int hdg_server_submit(hdg_server *s, const hdg_request *req, long long *ticket) 
   if (ncells > 2.0e8) return s->fail(HDG_ERR_INVALID, "mesh too large");
   if (req->kappa) j.kappa.assign(req->kappa, req->kappa + (size_t)ncells);
   j.footprint = footprint_bound(req->D, req->n, req->k, req->precision, req->solver);
+  {
+    const double nb = std::pow(req->k + 1.0, req->D) * (req->D + 1) + 2.0 * req->D * std::pow(req->k + 1.0, req->D - 1);
+    j.work = ncells * nb * nb;
+  }
   if (j.footprint > s->budget) return s->fail(HDG_ERR_INVALID, "request larger than the HBM budget");
   j.t_submit = Clock::now();
   {

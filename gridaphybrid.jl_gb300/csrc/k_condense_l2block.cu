@@ -37,7 +37,7 @@
 #include "k_ffblock_cell.cuh"
 #include "k_fp64_cell.cuh"
 
-// threads per CTA for the largest cells (3D elasticity k=2)
+// threads per CTA for the largest cells (3D elasticity k=2, 3D Darcy k=3)
 #ifndef HDG_L2BLOCK_BIG_NT
 #define HDG_L2BLOCK_BIG_NT 512
 #endif
@@ -130,7 +130,7 @@ struct ECfg {
   // one facet and trace component (phase 6)
   static constexpr int TR = NK % 4 == 0 ? 4 : NK % 3 == 0 ? 3 : NK % 2 == 0 ? 2 : 1;
   static constexpr int TF = NFS % 4 == 0 ? 4 : NFS % 3 == 0 ? 3 : NFS % 2 == 0 ? 2 : 1;
-  static constexpr int NT = NU * NC >= 8192 ? HDG_L2BLOCK_BIG_NT : 256;
+  static constexpr int NT = NU * NC >= 4096 ? HDG_L2BLOCK_BIG_NT : 256;
   // shared: P (NU x NU), Q (NU x NC), M^{-1} (NK x NK), C^{-1}/|J| (6 x 6), as values
   static constexpr size_t smem_values = (size_t)NU * NU + (size_t)NU * NC + (size_t)NK * NK + 36;
   // per-CTA scratch: Y (NS x NU), Z (NS x NC), column-major, as values; the

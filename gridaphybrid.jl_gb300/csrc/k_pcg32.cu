@@ -552,12 +552,14 @@ template <int NL, int NFD>
 static cudaError_t cellop_configure_t(size_t smem_optin, int num_sms, int *nstage, int *ctas) {
   using C = CellOp<NL, NFD>;
   const size_t stage = (size_t)C::CPS * C::REC * sizeof(float);
-  // about 108 KB of records in flight per CTA, two CTAs per SM where they fit;
-  // large records (one cell of 3D elasticity k=2: 61 KB) get three stages, so
-  // two copies are in flight while one stage is computed
+  // about 108 KB of records in flight per CTA, two CTAs per SM where two
+  // stages each fit; otherwise (one cell of 3D elasticity k=2: 61 KB) one CTA
+  // with as many stages as fit
   int ns = (int)((110 * 1024) / stage);
   ns = ns > kMaxBulkStages ? kMaxBulkStages : ns;
-  if (ns < 3) ns = 3;
+  if (2 * (2 * stage + 4096) > smem_optin) ns = (int)((smem_optin - 4096) / stage);
+  ns = ns > kMaxBulkStages ? kMaxBulkStages : ns;
+  if (ns < 2) ns = 2;
   while (ns > 2 && (size_t)ns * stage + 4096 > smem_optin) --ns;
   if ((size_t)ns * stage + 4096 > smem_optin) return cudaErrorInvalidValue;
   const size_t dyn = cellop_dyn_smem<NL, NFD>(ns);

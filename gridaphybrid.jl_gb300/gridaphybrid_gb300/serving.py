@@ -182,4 +182,19 @@ def latency_summary(resp, wall_s):
         "mesh_reuse": float(np.mean([r["reused_mesh"] for r in resp if r["status"] == 0])),
         "queue_p50_ms": float(np.percentile([r["queue_ms"] for r in resp if r["status"] == 0], 50)),
         "run_p50_ms": float(np.percentile([r["run_ms"] for r in resp if r["status"] == 0], 50)),
+        "by_class": _by_class(resp),
     }
+
+
+def _by_class(resp):
+    """Per (D, k): completed requests, cells, latency p50/p99 and run time p50."""
+    out = {}
+    for D, k in sorted({(r["shape"][0], r["shape"][2]) for r in resp if r["status"] == 0}):
+        rs = [r for r in resp if r["status"] == 0 and r["shape"][0] == D and r["shape"][2] == k]
+        lat = np.array([r["latency_ms"] for r in rs])
+        out["%dD_k%d" % (D, k)] = {
+            "completed": len(rs), "cells": int(sum(r["shape"][1] ** D for r in rs)),
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "run_p50_ms": float(np.percentile([r["run_ms"] for r in rs], 50)),
+        }
+    return out

@@ -68,13 +68,13 @@ def test_admission_respects_budget_and_reuses_meshes():
     budget = 1.02 * fp(3, 10, 2)
     assert fp(3, 12, 1) < budget
     with Server(slots=1, budget_bytes=budget) as srv:
-        for i, (D, n, k) in enumerate(shapes):
+        for i, (D, n, k) in enumerate(shapes):  # one at a time: the admission order is the submission order
             srv.submit(D, n, k, kappa=kappa_for(D, n, i), precision=_lib.HDG_PREC_FF_BLOCK)
-        srv.drain()
+            srv.drain()
         res = sorted(srv.poll(max_items=16), key=lambda r: r["ticket"])
         st = srv.stats()
     assert len(res) == len(shapes) and all(r["status"] == 0 for r in res)
-    assert [r["reused_mesh"] for r in res][:2] == [0, 1]
+    assert [r["reused_mesh"] for r in res] == [0, 1, 0, 0]
     assert st["peak_bytes"] <= budget
     assert st["mesh_hits"] >= 1 and st["evictions"] >= 1
 
@@ -94,6 +94,19 @@ def test_requests_overlap_under_a_budget():
     assert len(res) == 12 and all(r["status"] == 0 for r in res)
     assert 2 <= st["max_concurrent"] <= 3
     assert st["peak_bytes"] <= budget
+
+
+def test_shortest_work_first_admission():
+    """With the slot busy, queued small requests are admitted before a queued
+    large one that arrived earlier (none has waited long enough to age)."""
+    with Server(slots=1) as srv:
+        srv.submit(3, 16, 2, kappa=kappa_for(3, 16, 0))  # occupies the slot
+        big = srv.submit(3, 16, 2, kappa=kappa_for(3, 16, 1))
+        small = [srv.submit(2, 8, 1, kappa=kappa_for(2, 8, 2 + i)) for i in range(3)]
+        srv.drain()
+        order = [r["ticket"] for r in srv.poll(max_items=8)]
+    assert len(order) == 5
+    assert order.index(big) > max(order.index(t) for t in small)
 
 
 def test_mesh_reuse_gives_the_fresh_result():
