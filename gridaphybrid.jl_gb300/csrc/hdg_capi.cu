@@ -185,6 +185,23 @@ cudaError_t run_condense_l2block(hdg_problem *pb) {
   A.info = pb->d_info.as<int>();
   A.scratch = pb->d_escratch.ptr;
   A.Tb = mixed_tables(pb);
+  {
+    const L2RefHost &r = pb->l2ref;
+    const size_t nv = r.val.size();
+    const float *vf = pb->d_l2ref_val.as<float>();
+    A.ref_idx = pb->d_l2ref_idx.as<int>();
+    A.ref_v0 = pb->precision == HDG_PREC_FP64 ? (const void *)(vf + 2 * nv) : (const void *)vf;
+    A.ref_v1 = pb->precision == HDG_PREC_FP64 ? nullptr : (const void *)(vf + nv);
+    A.off_cidx = r.off_cidx;
+    A.off_rptr = r.off_rptr;
+    A.off_ridx = r.off_ridx;
+    A.off_hptr = r.off_hptr;
+    A.off_hidx = r.off_hidx;
+    A.voff_c = r.voff_c;
+    A.voff_r = r.voff_r;
+    A.voff_h = r.voff_h;
+    A.voff_hd = r.voff_hd;
+  }
   const float *Mf = pb->d_minv.as<float>();
   if (pb->precision == HDG_PREC_FP64) {
     A.A0 = pb->d_A.ptr;
@@ -344,6 +361,19 @@ int setup_problem(hdg_problem *pb) {
     }
     memcpy(mf.data() + 2 * Mi.size(), Mi.data(), sizeof(double) * Mi.size());
     if ((rc = upload(ctx, pb->d_minv, mf))) return rc;
+  }
+  if (l2block_supported(pb->physics == HDG_PHYSICS_ELASTICITY, pb->mesh.D, pb->mesh.k)) {
+    // sparse M^{-1} G_e, M^{-1} H_F for the L2-panel block elimination
+    build_l2_ref(pb->tab, pb->l2ref);
+    if ((rc = upload(ctx, pb->d_l2ref_idx, pb->l2ref.idx))) return rc;
+    const std::vector<double> &v = pb->l2ref.val;
+    std::vector<float> vf(4 * v.size());
+    for (size_t i = 0; i < v.size(); ++i) {
+      vf[i] = (float)v[i];
+      vf[v.size() + i] = (float)(v[i] - (double)vf[i]);
+    }
+    memcpy(vf.data() + 2 * v.size(), v.data(), sizeof(double) * v.size());
+    if ((rc = upload(ctx, pb->d_l2ref_val, vf))) return rc;
   }
   if ((rc = upload(ctx, pb->d_origin, pb->mesh.origin))) return rc;
   if ((rc = upload(ctx, pb->d_jac, pb->mesh.jac))) return rc;

@@ -209,6 +209,20 @@ int build_ref_tables(int D, int k, RefTables &t, int phys) {
     }
     t.Minv = Iv;
   }
+  // M^{-1} G_e, cleaned of rounding noise
+  t.MG.assign(D * nk * nk, 0.0);
+  for (int e = 0; e < D; ++e) {
+    double mx = 0.0;
+    for (int a = 0; a < nk; ++a)
+      for (int b = 0; b < nk; ++b) {
+        double v = 0.0;
+        for (int j = 0; j < nk; ++j) v += t.Minv[a * nk + j] * t.G[(e * nk + j) * nk + b];
+        t.MG[(e * nk + a) * nk + b] = v;
+        mx = std::max(mx, std::fabs(v));
+      }
+    for (int i = 0; i < nk * nk; ++i)
+      if (std::fabs(t.MG[e * nk * nk + i]) < 1e-12 * mx) t.MG[e * nk * nk + i] = 0.0;
+  }
   // facet tables: facet parameters are the non-normal directions, increasing
   const int nqf = ipow(t.n1, D - 1);
   t.F.assign(2 * D * nk * nk, 0.0);
@@ -243,7 +257,83 @@ int build_ref_tables(int D, int k, RefTables &t, int phys) {
       }
     }
   }
+  // M^{-1} H_lf, cleaned of rounding noise
+  t.MH.assign(2 * D * nk * nfd, 0.0);
+  for (int lf = 0; lf < 2 * D; ++lf) {
+    double mx = 0.0;
+    for (int a = 0; a < nk; ++a)
+      for (int b = 0; b < nfd; ++b) {
+        double v = 0.0;
+        for (int j = 0; j < nk; ++j) v += t.Minv[a * nk + j] * t.H[(lf * nk + j) * nfd + b];
+        t.MH[(lf * nk + a) * nfd + b] = v;
+        mx = std::max(mx, std::fabs(v));
+      }
+    for (int i = 0; i < nk * nfd; ++i)
+      if (std::fabs(t.MH[lf * nk * nfd + i]) < 1e-12 * mx) t.MH[lf * nk * nfd + i] = 0.0;
+  }
   return 0;
+}
+
+void build_l2_ref(const RefTables &t, L2RefHost &r) {
+  const int D = t.D, nk = t.nk, nfs = t.nfs, nl = 2 * D;
+  r.idx.clear();
+  r.val.clear();
+  // MG by column: for (e, b) the rows a
+  for (int e = 0, cnt = 0; e < D; ++e)
+    for (int b = 0; b < nk; ++b) {
+      r.idx.push_back(cnt);
+      for (int a = 0; a < nk; ++a)
+        if (t.MG[(e * nk + a) * nk + b] != 0.0) ++cnt;
+      if (e == D - 1 && b == nk - 1) r.idx.push_back(cnt);
+    }
+  r.off_cidx = (int)r.idx.size();
+  r.voff_c = 0;
+  for (int e = 0; e < D; ++e)
+    for (int b = 0; b < nk; ++b)
+      for (int a = 0; a < nk; ++a)
+        if (t.MG[(e * nk + a) * nk + b] != 0.0) {
+          r.idx.push_back(a);
+          r.val.push_back(t.MG[(e * nk + a) * nk + b]);
+        }
+  // MG by row: for (e, a) the columns b
+  r.off_rptr = (int)r.idx.size();
+  r.voff_r = (int)r.val.size();
+  for (int e = 0, cnt = 0; e < D; ++e)
+    for (int a = 0; a < nk; ++a) {
+      r.idx.push_back(cnt);
+      for (int b = 0; b < nk; ++b)
+        if (t.MG[(e * nk + a) * nk + b] != 0.0) ++cnt;
+      if (e == D - 1 && a == nk - 1) r.idx.push_back(cnt);
+    }
+  r.off_ridx = (int)r.idx.size();
+  for (int e = 0; e < D; ++e)
+    for (int a = 0; a < nk; ++a)
+      for (int b = 0; b < nk; ++b)
+        if (t.MG[(e * nk + a) * nk + b] != 0.0) {
+          r.idx.push_back(b);
+          r.val.push_back(t.MG[(e * nk + a) * nk + b]);
+        }
+  // MH by column: for (lf, fb) the rows a
+  r.off_hptr = (int)r.idx.size();
+  r.voff_h = (int)r.val.size();
+  for (int lf = 0, cnt = 0; lf < nl; ++lf)
+    for (int fb = 0; fb < nfs; ++fb) {
+      r.idx.push_back(cnt);
+      for (int a = 0; a < nk; ++a)
+        if (t.MH[(lf * nk + a) * nfs + fb] != 0.0) ++cnt;
+      if (lf == nl - 1 && fb == nfs - 1) r.idx.push_back(cnt);
+    }
+  r.off_hidx = (int)r.idx.size();
+  for (int lf = 0; lf < nl; ++lf)
+    for (int fb = 0; fb < nfs; ++fb)
+      for (int a = 0; a < nk; ++a)
+        if (t.MH[(lf * nk + a) * nfs + fb] != 0.0) {
+          r.idx.push_back(a);
+          r.val.push_back(t.MH[(lf * nk + a) * nfs + fb]);
+        }
+  // MH dense
+  r.voff_hd = (int)r.val.size();
+  r.val.insert(r.val.end(), t.MH.begin(), t.MH.end());
 }
 
 TableOffsets pack_tables(const RefTables &t, std::vector<double> &packed) {

@@ -81,7 +81,22 @@ struct RefTables {
   std::vector<double> qw;  // nqv
   std::vector<double> qphi;// nqv x nk
   std::vector<double> Minv;// nk x nk inverse of M (block elimination path)
+  // M^{-1} G_e (D x nk x nk) and M^{-1} H_lf (2D x nk x nfs), entries below
+  // 1e-12 of the matrix's largest set to zero: on the tensor-product cell they
+  // vanish exactly (a node couples only along one lattice line / to its facet line)
+  std::vector<double> MG, MH;
 };
+// The sparse reference operators of the L2-panel block elimination as
+// column lists (MG by column b, MG by row a, MH by column): int data
+// [cptr (D nk + 1) | cidx | rptr (D nk + 1) | ridx | hptr (2D nfs + 1) | hidx]
+// and the values in the same order, followed by MH dense (2D x nk x nfs).
+struct L2RefHost {
+  std::vector<int> idx;
+  std::vector<double> val;
+  int off_cidx = 0, off_rptr = 0, off_ridx = 0, off_hptr = 0, off_hidx = 0;   // in idx
+  int voff_c = 0, voff_r = 0, voff_h = 0, voff_hd = 0;                         // in val
+};
+void build_l2_ref(const RefTables &t, L2RefHost &r);
 int build_ref_tables(int D, int k, RefTables &t, int phys = 0);
 
 // Offsets (in doubles) of each table inside the packed device table buffer.
@@ -204,6 +219,10 @@ struct hdg_problem {
   // block-elimination path: M_ref^{-1} as (hi, lo) floats then FP64, 1/m per
   // cell, the elasticity kernel's per-CTA scratch panels
   hdg::DBuf d_minv, d_invm, d_escratch;
+  // the L2-panel kernel's sparse reference products: index lists, values
+  // ((hi, lo) floats then FP64) and their offsets
+  hdg::DBuf d_l2ref_idx, d_l2ref_val;
+  hdg::L2RefHost l2ref;
   // the elasticity cell blocks of this assembly are condensed by block
   // elimination (float-float, or FP64 when the dense block exceeds shared memory)
   bool eblock = false;
@@ -230,7 +249,7 @@ struct hdg_problem {
             &d_dirvals, &d_A, &d_b, &d_S, &d_g, &d_fact, &d_info, &d_aux, &d_rowptr, &d_colind, &d_val,
             &d_rhs, &d_br_row0, &d_br_src, &d_blk_off, &d_blk_rowlen, &d_blk_src, &d_diag_blk, &d_dir_cells,
             &d_Binv, &d_x, &d_r, &d_z, &d_p, &d_p2, &d_q, &d_partials, &d_scal, &d_counter, &d_cellop,
-            &d_cell_blk, &d_qc, &d_Binv32, &d_v32, &d_scal2, &d_minv, &d_invm, &d_escratch, &d_uint, &d_errs,
+            &d_cell_blk, &d_qc, &d_Binv32, &d_v32, &d_scal2, &d_minv, &d_invm, &d_escratch, &d_l2ref_idx, &d_l2ref_val, &d_uint, &d_errs,
             &d_newton, &d_rmax, &d_dirzero};
   }
   ~hdg_problem();

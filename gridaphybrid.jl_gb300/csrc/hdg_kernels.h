@@ -213,6 +213,12 @@ struct L2BlockArgs {
   int *info;
   void *scratch;   // per-CTA panels (and the fused kernel's cell block)
   MixedTables Tb;  // float-float reference tables (fused float-float integration)
+  // sparse reference products M^{-1} G_e, M^{-1} H_F: index lists (ref_idx)
+  // and values (ref_v0/ref_v1: FP64, or (hi, lo) float arrays)
+  const int *ref_idx;
+  const void *ref_v0, *ref_v1;
+  int off_cidx, off_rptr, off_ridx, off_hptr, off_hidx;  // in ref_idx
+  int voff_c, voff_r, voff_h, voff_hd;                   // in the values
 };
 struct L2BlockLaunch {
   bool elasticity;

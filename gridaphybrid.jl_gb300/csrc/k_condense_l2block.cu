@@ -13,11 +13,20 @@
 // so A_ss^{-1} = (C^{-1} (x) M_ref^{-1}) with a small per-cell C^{-1} (6x6 at
 // most) and the reference mass inverse; A_ss itself is never read.  With
 // R = [A_sf | b_s] and R_u = [A_uf | b_u]:
-//   Y = A_ss^{-1} A_su,  Z = A_ss^{-1} R      NS x NU, NS x NC (per-CTA scratch, L2)
+//   Y = A_ss^{-1} A_su,  Z = A_ss^{-1} R      (never formed for A_su, A_sf: below)
 //   P = A_uu - A_us Y,   Q = R_u - A_us Z    NU x NU, NU x NC (shared memory)
 //   X_u = P^{-1} Q   (LU with partial pivoting of field 2's Schur complement)
-//   X_s = Z - Y X_u
+//   X_s = Z - Y X_u                           NS x NC (per-CTA scratch, L2)
 //   S = A_ff - A_fs X_s - A_fu X_u,   g = b_f - A_fs y_s - A_fu y_u
+// The coupling blocks are per-cell coefficients times reference tables,
+//   A_su[(c,a),(k,b)] = sum_e alpha[c][k][e] G_e[a][b],
+//   A_sf[(c,a),(F,j,b)] = delta[c][j][F] H_F[a][b],
+// so with the reference products MG_e = M^{-1} G_e and MH_F = M^{-1} H_F
+//   Y[(c,a),(k,b)] = sum_e W_e[c][k] MG_e[a][b],   W_e = C^{-1} alpha_e,
+//   Z[(c,a),(F,j,b)] = Dh[c][j][F] MH_F[a][b],     Dh = C^{-1} delta.
+// On the tensor-product reference cell MG_e and MH_F have k+1 entries per
+// column (a node couples along one lattice line); the products with Y and Z
+// run over those entries only.
 // Zeros are skipped (only exact zeros, so the results do not change):
 //   - elasticity: A_us / A_su couple displacement component k only to the
 //     stress components whose index pair contains k (every affine cell);
@@ -131,11 +140,13 @@ struct ECfg {
   static constexpr int TR = NK % 4 == 0 ? 4 : NK % 3 == 0 ? 3 : NK % 2 == 0 ? 2 : 1;
   static constexpr int TF = NFS % 4 == 0 ? 4 : NFS % 3 == 0 ? 3 : NFS % 2 == 0 ? 2 : 1;
   static constexpr int NT = NU * NC >= 4096 ? HDG_L2BLOCK_BIG_NT : 256;
-  // shared: P (NU x NU), Q (NU x NC), M^{-1} (NK x NK), C^{-1}/|J| (6 x 6), as values
-  static constexpr size_t smem_values = (size_t)NU * NU + (size_t)NU * NC + (size_t)NK * NK + 36;
-  // per-CTA scratch: Y (NS x NU), Z (NS x NC), column-major, as values; the
-  // fused kernel adds the cell block A (N x N) and b (N)
-  static constexpr size_t slot_values = (size_t)NS * NU + (size_t)NS * NC;
+  // shared: P (NU x NU), Q (NU x NC), M^{-1} (NK x NK), C^{-1}/|J| (6 x 6),
+  // the panel coefficients W (D x NC1 x NC2) and Dh (NC1 x NC2 x NL), as values
+  static constexpr size_t smem_values =
+      (size_t)NU * NU + (size_t)NU * NC + (size_t)NK * NK + 36 + 54 + 108;
+  // per-CTA scratch, column-major, as values: Z / X_s (NS x NC), the products
+  // T (D NU x NC); the fused kernel adds the cell block A (N x N) and b (N)
+  static constexpr size_t slot_values = (size_t)NS * NC + (size_t)D * NU * NC;
   static constexpr size_t slot_values_fused = slot_values + (size_t)N * N + N;
 };
 
@@ -152,6 +163,8 @@ struct Lists {
   // nonzero coupling to that component on the facet's nodes
   int fmask[C::NL][3];
   int piv, info;
+  double cinv[6][6];  // C^{-1} / |J| of the cell (FP64)
+  CellFactors cf;     // the cell's geometric factors (FP64)
 };
 
 template <class C, class Ar>
@@ -303,14 +316,21 @@ __global__ void __launch_bounds__(C::NT, 1) condense_l2block_kernel(L2BlockArgs 
   V *Q = P + NU * NU;                      // [r][c]
   V *Mi = Q + (size_t)NU * NC;             // [a][k]
   V *Ci = Mi + NK * NK;                    // [c][d]
-  Lists<C> &L = *reinterpret_cast<Lists<C> *>(Ci + 36);
+  V *Wc = Ci + 36;                         // [(e NC1 + c) NC2 + k]
+  V *Dh = Wc + 54;                         // [(c NC2 + j) NL + F]
+  Lists<C> &L = *reinterpret_cast<Lists<C> *>(Dh + 108);
   unsigned char *integ = reinterpret_cast<unsigned char *>(&L + 1);
   integ += (16 - reinterpret_cast<uintptr_t>(integ) % 16) % 16;
   constexpr size_t slot = FUSED ? C::slot_values_fused : C::slot_values;
-  V *Y = static_cast<V *>(a.scratch) + (size_t)blockIdx.x * slot;  // [m + NS j]
-  V *Z = Y + (size_t)NS * NU;                                      // [m + NS c]
+  V *Z = static_cast<V *>(a.scratch) + (size_t)blockIdx.x * slot;  // [m + NS c]
+  V *Tp = Z + (size_t)NS * NC;                                     // [(e NU + u) + D NU c]
   // the fused kernel's cell block in the slot: (hi, lo) float arrays or FP64
-  V *slotA = Z + (size_t)NS * NC;
+  V *slotA = Tp + (size_t)D * NU * NC;
+  // sparse reference products
+  const int *rcp = a.ref_idx, *rci = a.ref_idx + a.off_cidx;  // MG by column
+  const int *rrp = a.ref_idx + a.off_rptr, *rri = a.ref_idx + a.off_ridx;  // MG by row
+  const int *rhp = a.ref_idx + a.off_hptr, *rhi = a.ref_idx + a.off_hidx;  // MH by column
+  auto RV = [&](int i) { return Ar::ld(a.ref_v0, a.ref_v1, (size_t)i); };
   void *sA0 = slotA, *sA1 = nullptr, *sb0 = nullptr, *sb1 = nullptr;
   if constexpr (sizeof(V) == 8 && !std::is_same<Ar, Ar64>::value) {
     sA1 = reinterpret_cast<float *>(slotA) + (size_t)N * N;
@@ -386,11 +406,49 @@ __global__ void __launch_bounds__(C::NT, 1) condense_l2block_kernel(L2BlockArgs 
           for (int d = 0; d < NSYM; ++d) Cinv[c][d] = c == d ? s : 0.0;
       }
       for (int c = 0; c < NSYM; ++c)
-        for (int d = 0; d < NSYM; ++d) Ci[c * 6 + d] = Ar::of(Cinv[c][d]);
+        for (int d = 0; d < NSYM; ++d) {
+          Ci[c * 6 + d] = Ar::of(Cinv[c][d]);
+          L.cinv[c][d] = Cinv[c][d];
+        }
+      cell_factors(ca, cell, L.cf);
       L.info = 0;
     }
     if (t < NL * 3) L.fmask[t / 3][t % 3] = 0;
     __syncthreads();
+    // panel coefficients W_e = C^{-1} alpha_e and Dh = C^{-1} delta (FP64,
+    // the integration's own factors: alpha, delta are its coefficients of G, H)
+    for (int o = t; o < D * NSYM * NC2 + NSYM * NC2 * NL; o += NT) {
+      double v = 0.0;
+      if (o < D * NSYM * NC2) {
+        const int e = o / (NSYM * NC2), c = (o / NC2) % NSYM, k = o % NC2;
+        for (int cp = 0; cp < NSYM; ++cp) {
+          double al;
+          if (C::ELAST) {  // -sum_jj E_cp(k, jj) cg[e][jj]  (the (div v).u term)
+            al = 0.0;
+            for (int jj = 0; jj < D; ++jj) al += sym_unit(D, cp, k, jj) * L.cf.cg[e][jj];
+            al = -al;
+          } else {  // cg[e][d] (the -(div v) p term)
+            al = L.cf.cg[e][cp];
+          }
+          v += L.cinv[c][cp] * al;
+        }
+        Wc[o] = Ar::of(v);
+      } else {
+        const int r = o - D * NSYM * NC2, c = r / (NC2 * NL), j = (r / NL) % NC2, F = r % NL;
+        for (int cp = 0; cp < NSYM; ++cp) {
+          double de;
+          if (C::ELAST) {  // -sum_jj E_cp(j, jj) cn[F][jj]  (the -(v.n).uhat term)
+            de = 0.0;
+            for (int jj = 0; jj < D; ++jj) de += sym_unit(D, cp, j, jj) * L.cf.cn[F][jj];
+            de = -de;
+          } else {  // cn[F][d]  (the (v.n) l term)
+            de = L.cf.cn[F][cp];
+          }
+          v += L.cinv[c][cp] * de;
+        }
+        Dh[r] = Ar::of(v);
+      }
+    }
     // the cell's trace couplings: entries of A_fi / A_if on the facet's nodes
     // that are exactly zero are skipped below (they contribute nothing)
     {
@@ -405,97 +463,92 @@ __global__ void __launch_bounds__(C::NT, 1) condense_l2block_kernel(L2BlockArgs 
       }
     }
     __syncthreads();
-    // 1. Y = A_ss^{-1} A_su and Z = A_ss^{-1} [A_sf | b_s]: M^{-1} on each
-    //    stress component of the column, then the components mixed by C^{-1}/|J|
-    for (int o = t; o < NK * (NU + NC); o += NT) {
-      const int an = o % NK, col = o / NK;
+    // 1. the b column of Z: A_ss^{-1} b_s (M^{-1} on each field-1 component,
+    //    then the components mixed by C^{-1})
+    for (int an = t; an < NK; an += NT) {
       V T[NSYM];
 #pragma unroll
-      for (int cp = 0; cp < NSYM; ++cp) T[cp] = Ar::zero();
-      if (col < NU) {
-        const int msk = L.kmask[col / NK];
-#pragma unroll
-        for (int cp = 0; cp < NSYM; ++cp)
-          if (msk >> cp & 1)
-            for (int k = 0; k < NK; ++k) Ar::mac(T[cp], Mi[an * NK + k], A(cp * NK + k, NS + col));
-      } else if (col < NU + NF) {
-        const int f = col - NU, lf = f / NFD, cnt = L.fn_cnt[lf];
-        const int msk = L.fmask[lf][(f - lf * NFD) / NFS];
-#pragma unroll
-        for (int cp = 0; cp < NSYM; ++cp)
-          if (msk >> cp & 1)
-            for (int q = 0; q < cnt; ++q) {
-              const int k = L.fn_node[lf][q];
-              Ar::mac(T[cp], Mi[an * NK + k], A(cp * NK + k, NI + f));
-            }
-      } else {
-#pragma unroll
-        for (int cp = 0; cp < NSYM; ++cp)
-          for (int k = 0; k < NK; ++k) Ar::mac(T[cp], Mi[an * NK + k], B(cp * NK + k));
+      for (int cp = 0; cp < NSYM; ++cp) {
+        T[cp] = Ar::zero();
+        for (int k = 0; k < NK; ++k) Ar::mac(T[cp], Mi[an * NK + k], B(cp * NK + k));
+        T[cp] = Ar::fin(T[cp]);
       }
-#pragma unroll
-      for (int cp = 0; cp < NSYM; ++cp) T[cp] = Ar::fin(T[cp]);
 #pragma unroll
       for (int c = 0; c < NSYM; ++c) {
         V v = Ar::zero();
 #pragma unroll
         for (int cp = 0; cp < NSYM; ++cp) Ar::mac(v, Ci[c * 6 + cp], T[cp]);
-        v = Ar::fin(v);
-        const int m = c * NK + an;
-        if (col < NU)
-          Y[m + (size_t)NS * col] = v;
-        else
-          Z[m + (size_t)NS * (col - NU)] = v;
+        Z[c * NK + an + (size_t)NS * NF] = Ar::fin(v);
       }
     }
     __syncthreads();
-    // 2. P = A_uu - A_us Y,  Q = [A_uf | b_u] - A_us Z, register tiles of
-    //    TR rows (one field-2 component) x 4 columns
+    // 2. P = A_uu - A_us Y,  Q = [A_uf | b_u] - A_us Z, register tiles of TR
+    //    rows (one field-2 component) x one column; Y, Z through their factors
     {
-      constexpr int TR = C::TR, RT = NU / TR, CT = (NU + NC + 3) / 4;
-      for (int o = t; o < RT * CT; o += NT) {
-        const int r0 = (o % RT) * TR, col0 = (o / RT) * 4, kd = r0 / NK;
-        const V *xp[4];
+      constexpr int TR = C::TR, RT = NU / TR;
+      for (int o = t; o < RT * (NU + NC); o += NT) {
+        const int r0 = (o % RT) * TR, col = o / RT, kr = r0 / NK;
+        V acc[TR];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const int col = min(col0 + j, NU + NC - 1);
-          xp[j] = col < NU ? Y + (size_t)NS * col : Z + (size_t)NS * (col - NU);
-        }
-        V acc[TR][4];
+        for (int i = 0; i < TR; ++i) acc[i] = Ar::zero();
+        const int cnt = L.kc_cnt[kr];  // A_us: only these field-1 components couple to row component kr
+        if (col < NU) {  // Y column (k, b): sum_c sum_e W_e[c][k] sum_a A_us[r][(c,a)] MG_e[a][b]
+          const int k = col / NK, b = col - k * NK;
+          for (int q = 0; q < cnt; ++q) {
+            const int c = L.kc_comp[kr][q];
+            for (int e = 0; e < D; ++e) {
+              const V w = Wc[(e * NSYM + c) * NC2 + k];
+              if (!Ar::nonzero(w)) continue;
+              V sm[TR];
 #pragma unroll
-        for (int i = 0; i < TR; ++i)
+              for (int i = 0; i < TR; ++i) sm[i] = Ar::zero();
+              for (int p = rcp[e * NK + b]; p < rcp[e * NK + b + 1]; ++p) {
+                const int am = c * NK + rci[p];
+                const V rv = RV(a.voff_c + p);
 #pragma unroll
-          for (int j = 0; j < 4; ++j) acc[i][j] = Ar::zero();
-        const int cnt = L.kc_cnt[kd];
-        for (int q = 0; q < cnt; ++q) {
-          const int m0 = L.kc_comp[kd][q] * NK;
-#pragma unroll 3
-          for (int k = 0; k < NK; ++k) {
-            V av[TR], xv[4];
+                for (int i = 0; i < TR; ++i) Ar::mac(sm[i], A(NS + r0 + i, am), rv);
+              }
 #pragma unroll
-            for (int i = 0; i < TR; ++i) av[i] = A(NS + r0 + i, m0 + k);
+              for (int i = 0; i < TR; ++i) Ar::mac(acc[i], Ar::fin(sm[i]), w);
+            }
+          }
+        } else if (col < NU + NF) {  // Z facet column (F, j, b): sum_c Dh[c][j][F] sum_a A_us[r][(c,a)] MH_F[a][b]
+          const int f = col - NU, F = f / NFD, j = (f - F * NFD) / NFS, b = f % NFS;
+          for (int q = 0; q < cnt; ++q) {
+            const int c = L.kc_comp[kr][q];
+            const V w = Dh[(c * NC2 + j) * NL + F];
+            if (!Ar::nonzero(w)) continue;
+            V sm[TR];
 #pragma unroll
-            for (int j = 0; j < 4; ++j) xv[j] = xp[j][m0 + k];
+            for (int i = 0; i < TR; ++i) sm[i] = Ar::zero();
+            for (int p = rhp[F * NFS + b]; p < rhp[F * NFS + b + 1]; ++p) {
+              const int am = c * NK + rhi[p];
+              const V rv = RV(a.voff_h + p);
 #pragma unroll
-            for (int i = 0; i < TR; ++i)
+              for (int i = 0; i < TR; ++i) Ar::mac(sm[i], A(NS + r0 + i, am), rv);
+            }
 #pragma unroll
-              for (int j = 0; j < 4; ++j) Ar::mac(acc[i][j], av[i], xv[j]);
+            for (int i = 0; i < TR; ++i) Ar::mac(acc[i], Ar::fin(sm[i]), w);
+          }
+        } else {  // the b column of Z (dense)
+          for (int q = 0; q < cnt; ++q) {
+            const int m0 = L.kc_comp[kr][q] * NK;
+            for (int k = 0; k < NK; ++k) {
+              const V zv = Z[m0 + k + (size_t)NS * NF];
+#pragma unroll
+              for (int i = 0; i < TR; ++i) Ar::mac(acc[i], A(NS + r0 + i, m0 + k), zv);
+            }
           }
         }
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const int col = col0 + j;
-          if (col >= NU + NC) continue;
-#pragma unroll
-          for (int i = 0; i < TR; ++i) {
-            const int r = r0 + i;
-            const V rv = col < NU ? A(NS + r, NS + col) : col - NU < NF ? A(NS + r, NI + col - NU) : B(NS + r);
-            const V v = Ar::sub(rv, Ar::fin(acc[i][j]));
-            if (col < NU)
-              P[r * NU + col] = v;
-            else
-              Q[r * NC + col - NU] = v;
-          }
+        for (int i = 0; i < TR; ++i) {
+          const int r = r0 + i;
+          const V rv = col < NU ? A(NS + r, NS + col) : col - NU < NF ? A(NS + r, NI + col - NU) : B(NS + r);
+          const V v = Ar::sub(rv, Ar::fin(acc[i]));
+          if (col < NU)
+            P[r * NU + col] = v;
+          else
+            Q[r * NC + col - NU] = v;
         }
       }
     }
@@ -568,42 +621,57 @@ __global__ void __launch_bounds__(C::NT, 1) condense_l2block_kernel(L2BlockArgs 
       }
       __syncthreads();
     }
-    // 5. X_s = Z - Y X_u, in Z: register tiles of 4 x 4
+    // 5. X_s = Z - Y X_u = Z - sum_e sum_k W_e[:][k] (MG_e X_u[(k, .)]):
+    //    first T_e[(k,a)][c] = sum_b MG_e[a][b] X_u[(k,b)][c] (4 columns per thread)
     {
-      constexpr int MT = (NS + 3) / 4, CT = (NC + 3) / 4;
-      for (int o = t; o < MT * CT; o += NT) {
-        const int m0 = (o % MT) * 4, c0 = (o / MT) * 4;
-        int mi[4], cj[4];
+      constexpr int CT = (NC + 3) / 4;
+      for (int o = t; o < D * NU * CT; o += NT) {
+        const int c0 = (o % CT) * 4, row = o / CT, e = row / NU, u = row - e * NU, k = u / NK, an = u - k * NK;
+        V acc[4];
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          mi[i] = min(m0 + i, NS - 1);
-          cj[i] = min(c0 + i, NC - 1);
-        }
-        V acc[4][4];
+        for (int j = 0; j < 4; ++j) acc[j] = Ar::zero();
+        for (int p = rrp[e * NK + an]; p < rrp[e * NK + an + 1]; ++p) {
+          const V rv = RV(a.voff_r + p);
+          const V *xq = Q + (k * NK + rri[p]) * NC;
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
-#pragma unroll
-          for (int j = 0; j < 4; ++j) acc[i][j] = Ar::zero();
-#pragma unroll 3
-        for (int k = 0; k < NU; ++k) {
-          V yv[4], xv[4];
-#pragma unroll
-          for (int i = 0; i < 4; ++i) yv[i] = Y[mi[i] + (size_t)NS * k];
-#pragma unroll
-          for (int j = 0; j < 4; ++j) xv[j] = Q[k * NC + cj[j]];
-#pragma unroll
-          for (int i = 0; i < 4; ++i)
-#pragma unroll
-            for (int j = 0; j < 4; ++j) Ar::mac(acc[i][j], yv[i], xv[j]);
+          for (int j = 0; j < 4; ++j) Ar::mac(acc[j], rv, xq[min(c0 + j, NC - 1)]);
         }
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j)
+          if (c0 + j < NC) Tp[(size_t)(e * NU + u) + (size_t)D * NU * (c0 + j)] = Ar::fin(acc[j]);
+      }
+    }
+    __syncthreads();
+    //    then X_s[(c,a)][col] = Z[(c,a)][col] - sum_e sum_k W_e[c][k] T_e[(k,a)][col],
+    //    Z's facet columns from their factors, its b column in place
+    {
+      constexpr int CT = (NC + 3) / 4;
+      for (int o = t; o < NS * CT; o += NT) {
+        const int c0 = (o % CT) * 4, m = o / CT, c = m / NK, an = m - c * NK;
+        V acc[4];
 #pragma unroll
-          for (int j = 0; j < 4; ++j)
-            if (m0 + i < NS && c0 + j < NC) {
-              const size_t e = (size_t)(m0 + i) + (size_t)NS * (c0 + j);
-              Z[e] = Ar::sub(Z[e], Ar::fin(acc[i][j]));
-            }
+        for (int j = 0; j < 4; ++j) acc[j] = Ar::zero();
+        for (int e = 0; e < D; ++e)
+          for (int k = 0; k < NC2; ++k) {
+            const V w = Wc[(e * NSYM + c) * NC2 + k];
+            if (!Ar::nonzero(w)) continue;
+            const V *tp = Tp + (size_t)(e * NU + k * NK + an);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) Ar::mac(acc[j], w, tp[(size_t)D * NU * min(c0 + j, NC - 1)]);
+          }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int col = c0 + j;
+          if (col >= NC) continue;
+          V z;
+          if (col < NF) {
+            const int F = col / NFD, jj = (col - F * NFD) / NFS, b = col % NFS;
+            z = Ar::mul(Dh[(c * NC2 + jj) * NL + F], RV(a.voff_hd + (F * NK + an) * NFS + b));
+          } else {
+            z = Z[m + (size_t)NS * NF];
+          }
+          Z[m + (size_t)NS * col] = Ar::sub(z, Ar::fin(acc[j]));
+        }
       }
     }
     __syncthreads();
