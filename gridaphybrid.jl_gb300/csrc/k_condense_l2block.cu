@@ -139,15 +139,20 @@ struct ECfg {
   // one facet and trace component (phase 6)
   static constexpr int TR = NK % 4 == 0 ? 4 : NK % 3 == 0 ? 3 : NK % 2 == 0 ? 2 : 1;
   static constexpr int TF = NFS % 4 == 0 ? 4 : NFS % 3 == 0 ? 3 : NFS % 2 == 0 ? 2 : 1;
-  static constexpr int NT = NU * NC >= 4096 ? HDG_L2BLOCK_BIG_NT : 256;
+  static constexpr int NT = ELAST && NU * NC >= 4096 ? HDG_L2BLOCK_BIG_NT : 256;
+  // M^{-1} in shared memory, except where leaving it in L1 lets two CTAs share an SM
+  static constexpr bool MI_SHARED = ELAST || NK < 64;
   // shared: P (NU x NU), Q (NU x NC), M^{-1} (NK x NK), C^{-1}/|J| (6 x 6),
   // the panel coefficients W (D x NC1 x NC2) and Dh (NC1 x NC2 x NL), as values
   static constexpr size_t smem_values =
-      (size_t)NU * NU + (size_t)NU * NC + (size_t)NK * NK + 36 + 54 + 108;
+      (size_t)NU * NU + (size_t)NU * NC + (MI_SHARED ? (size_t)NK * NK : 0) + 36 + 54 + 108;
   // per-CTA scratch, column-major, as values: Z / X_s (NS x NC), the products
   // T (D NU x NC); the fused kernel adds the cell block A (N x N) and b (N)
   static constexpr size_t slot_values = (size_t)NS * NC + (size_t)D * NU * NC;
-  static constexpr size_t slot_values_fused = slot_values + (size_t)N * N + N;
+  // the fused kernel stores only rows NS.. of the cell block (the field-1 rows
+  // are never read: A_ss, A_su, A_sf enter through their factors)
+  static constexpr int NR = N - NS;
+  static constexpr size_t slot_values_fused = slot_values + (size_t)NR * N + N;
 };
 
 // shared-memory bookkeeping beside the value arrays
@@ -163,6 +168,7 @@ struct Lists {
   // nonzero coupling to that component on the facet's nodes
   int fmask[C::NL][3];
   int piv, info;
+  int pivs[8];        // the pivot rows of the current LU panel
   double cinv[6][6];  // C^{-1} / |J| of the cell (FP64)
   CellFactors cf;     // the cell's geometric factors (FP64)
 };
@@ -183,12 +189,13 @@ size_t integ_bytes(int nqv) {
   return fac + (size_t)nqv * (C::D + 1) * sizeof(double) + (size_t)C::N * sizeof(int) + 16;
 }
 
-// Cell `cell` integrated into the CTA's slot: A (column-major N x N, the
-// field-1 block left unwritten) and b, as (hi, lo) float arrays or FP64.
+// Cell `cell` integrated into the CTA's slot: rows NS..N-1 of A (column-major,
+// leading dimension NR = N - NS) and the whole b, as (hi, lo) float arrays or
+// FP64.  Row and column decoding divide by compile-time sizes.
 template <class C, class Ar>
 __device__ void integrate_into_slot(const L2BlockArgs &a, int cell, void *A0, void *A1, void *b0, void *b1,
                                     unsigned char *integ, int t) {
-  constexpr int N = C::N, NT = C::NT, NS = C::NS;
+  constexpr int N = C::N, NT = C::NT, NS = C::NS, NR = C::NR, D = C::D, NK = C::NK, NI = C::NI, NFD = C::NFD;
   constexpr bool FF = !std::is_same<Ar, Ar64>::value;
   const CellArgs &ca = a.cell;
   size_t fac = sizeof(ElastScratch);
@@ -201,23 +208,15 @@ __device__ void integrate_into_slot(const L2BlockArgs &a, int cell, void *A0, vo
     ElastScratch &S = *reinterpret_cast<ElastScratch *>(integ);
     for (int i = t; i < N; i += NT) dec[i] = elast_pack(ca, i);
     elast_cell_prepare(ca, cell, S, fq, FF, t, NT);  // barriers inside
-    int i = t % N, j = t / N;
-    for (int e = t; e < N * N; e += NT) {
-      if (!(i < NS && j < NS)) {
-        if constexpr (FF) {
-          float h, l;
-          elast_entry_ff(ca, a.Tb, S.TF, dec[i], dec[j], h, l);
-          static_cast<float *>(A0)[e] = h;
-          static_cast<float *>(A1)[e] = l;
-        } else {
-          static_cast<double *>(A0)[e] = elast_entry_t(ca, S.f, S.T, dec[i], dec[j]);
-        }
-      }
-      i += NT % N;
-      j += NT / N;
-      if (i >= N) {
-        i -= N;
-        ++j;
+    for (int e = t; e < NR * N; e += NT) {
+      const int j = e / NR, i = NS + (e - j * NR);
+      if constexpr (FF) {
+        float h, l;
+        elast_entry_ff(ca, a.Tb, S.TF, dec[i], dec[j], h, l);
+        static_cast<float *>(A0)[e] = h;
+        static_cast<float *>(A1)[e] = l;
+      } else {
+        static_cast<double *>(A0)[e] = elast_entry_t(ca, S.f, S.T, dec[i], dec[j]);
       }
     }
     for (int r = t; r < N; r += NT) {
@@ -229,34 +228,59 @@ __device__ void integrate_into_slot(const L2BlockArgs &a, int cell, void *A0, vo
       }
     }
     __syncthreads();
-  } else if constexpr (FF) {
-    CellFactorsFF &f = *reinterpret_cast<CellFactorsFF *>(integ);
-    integrate_cell_ff(ca, a.Tb, cell, true, f, fq, static_cast<float *>(A0), static_cast<float *>(A1),
-                      static_cast<float *>(b0), static_cast<float *>(b1), t, NT, true);  // barriers inside
   } else {
-    CellFactors &f = *reinterpret_cast<CellFactors *>(integ);
-    if (t == 0) cell_factors(ca, cell, f);
+    // Darcy: the cell factors (float-float or FP64) and the source per point
+    CellFactorsFF &fF = *reinterpret_cast<CellFactorsFF *>(integ);
+    CellFactors &f6 = *reinterpret_cast<CellFactors *>(integ);
+    if (t == 0) {
+      if constexpr (FF)
+        cell_factors_ff(ca, cell, fF);
+      else
+        cell_factors(ca, cell, f6);
+    }
     __syncthreads();
-    source_values(ca, f, cell, fq, t, NT);
+    {
+      const double kap = ca.kappa ? ca.kappa[cell] : 1.0;
+      for (int q = t; q < ca.nqv; q += NT) {
+        double x[3], p, qe[3], fu[3], g;
+        for (int d = 0; d < D; ++d) {
+          x[d] = FF ? fF.x0[d] : f6.x0[d];
+          for (int e = 0; e < D; ++e) x[d] += (FF ? fF.J[d][e] : f6.J[d][e]) * ca.qxi[q * D + e];
+        }
+        exact_solution(ca.problem, D, x, kap, p, qe, fu, g);
+        const double w = ca.qw[q] * (FF ? fF.detJ : f6.detJ);
+        for (int d = 0; d < D; ++d) fq[q * (D + 1) + d] = w * fu[d];
+        fq[q * (D + 1) + D] = w * g;
+      }
+    }
     __syncthreads();
-    double *Ad = static_cast<double *>(A0);
-    for (int e = t; e < N * N; e += NT) {
-      const int j = e / N, i = e - j * N;
-      if (i < NS && j < NS) continue;
+    for (int e = t; e < NR * N; e += NT) {
+      const int j = e / NR, i = NS + (e - j * NR);
       int ti, si, ii, tj, sj, jj;
-      decode(i, C::D, C::NK, ca.ni, ca.nfd, ti, si, ii);
-      decode(j, C::D, C::NK, ca.ni, ca.nfd, tj, sj, jj);
-      Ad[e] = cell_entry<double>(ca, f, ti, si, ii, tj, sj, jj);
+      decode_row(i, D, NK, NI, NFD, ti, si, ii);
+      decode_row(j, D, NK, NI, NFD, tj, sj, jj);
+      if constexpr (FF) {
+        float h, l;
+        cell_entry_ff(ca, a.Tb, fF, ti, si, ii, tj, sj, jj, h, l);
+        static_cast<float *>(A0)[e] = h;
+        static_cast<float *>(A1)[e] = l;
+      } else {
+        static_cast<double *>(A0)[e] = cell_entry<double>(ca, f6, ti, si, ii, tj, sj, jj);
+      }
     }
     for (int r = t; r < N; r += NT) {
       int ti, si, ii;
-      decode(r, C::D, C::NK, ca.ni, ca.nfd, ti, si, ii);
+      decode_row(r, D, NK, NI, NFD, ti, si, ii);
       double v = 0.0;
       if (ti < 2) {
-        const int comp = ti == 0 ? si : C::D;
-        for (int q = 0; q < ca.nqv; ++q) v += fq[q * (C::D + 1) + comp] * ca.qphi[q * C::NK + ii];
+        const int comp = ti == 0 ? si : D;
+        for (int q = 0; q < ca.nqv; ++q) v += fq[q * (D + 1) + comp] * ca.qphi[q * NK + ii];
       }
-      static_cast<double *>(b0)[r] = v;
+      if constexpr (FF) {
+        split_double(v, static_cast<float *>(b0)[r], static_cast<float *>(b1)[r]);
+      } else {
+        static_cast<double *>(b0)[r] = v;
+      }
     }
     __syncthreads();
   }
@@ -307,7 +331,7 @@ __device__ void compliance_inverse(int D, int nsym, double E, double nu, double 
 }
 
 template <class C, class Ar, bool FUSED>
-__global__ void __launch_bounds__(C::NT, 1) condense_l2block_kernel(L2BlockArgs a) {
+__global__ void __launch_bounds__(C::NT, C::MI_SHARED ? 1 : 2) condense_l2block_kernel(L2BlockArgs a) {
   using V = typename Ar::V;
   constexpr int D = C::D, NK = C::NK, NSYM = C::NC1, NC2 = C::NC2, NS = C::NS, NU = C::NU, NI = C::NI, NF = C::NF, N = C::N,
                 NC = C::NC, NT = C::NT, NFD = C::NFD, NL = C::NL, NFS = C::NFS;
@@ -315,7 +339,7 @@ __global__ void __launch_bounds__(C::NT, 1) condense_l2block_kernel(L2BlockArgs 
   V *P = reinterpret_cast<V *>(smem_raw);  // [r][j]
   V *Q = P + NU * NU;                      // [r][c]
   V *Mi = Q + (size_t)NU * NC;             // [a][k]
-  V *Ci = Mi + NK * NK;                    // [c][d]
+  V *Ci = Mi + (C::MI_SHARED ? NK * NK : 0);  // [c][d]
   V *Wc = Ci + 36;                         // [(e NC1 + c) NC2 + k]
   V *Dh = Wc + 54;                         // [(c NC2 + j) NL + F]
   Lists<C> &L = *reinterpret_cast<Lists<C> *>(Dh + 108);
@@ -332,16 +356,24 @@ __global__ void __launch_bounds__(C::NT, 1) condense_l2block_kernel(L2BlockArgs 
   const int *rhp = a.ref_idx + a.off_hptr, *rhi = a.ref_idx + a.off_hidx;  // MH by column
   auto RV = [&](int i) { return Ar::ld(a.ref_v0, a.ref_v1, (size_t)i); };
   void *sA0 = slotA, *sA1 = nullptr, *sb0 = nullptr, *sb1 = nullptr;
+  constexpr int NR = C::NR;
   if constexpr (sizeof(V) == 8 && !std::is_same<Ar, Ar64>::value) {
-    sA1 = reinterpret_cast<float *>(slotA) + (size_t)N * N;
-    sb0 = reinterpret_cast<float *>(slotA) + 2 * (size_t)N * N;
-    sb1 = reinterpret_cast<float *>(slotA) + 2 * (size_t)N * N + N;
+    sA1 = reinterpret_cast<float *>(slotA) + (size_t)NR * N;
+    sb0 = reinterpret_cast<float *>(slotA) + 2 * (size_t)NR * N;
+    sb1 = reinterpret_cast<float *>(slotA) + 2 * (size_t)NR * N + N;
   } else {
-    sb0 = reinterpret_cast<double *>(slotA) + (size_t)N * N;
+    sb0 = reinterpret_cast<double *>(slotA) + (size_t)NR * N;
   }
   const CellArgs &ca = a.cell;
   const int t = threadIdx.x;
-  for (int e = t; e < NK * NK; e += NT) Mi[e] = Ar::ld(a.Minv0, a.Minv1, e);
+  if constexpr (C::MI_SHARED)
+    for (int e = t; e < NK * NK; e += NT) Mi[e] = Ar::ld(a.Minv0, a.Minv1, e);
+  auto MI = [&](int i) {
+    if constexpr (C::MI_SHARED)
+      return Mi[i];
+    else
+      return Ar::ld(a.Minv0, a.Minv1, (size_t)i);
+  };
   if (t < NL) {  // volume nodes with a nonzero trace coupling on facet t
     int cnt = 0;
     for (int node = 0; node < NK; ++node) {
@@ -378,9 +410,9 @@ __global__ void __launch_bounds__(C::NT, 1) condense_l2block_kernel(L2BlockArgs 
   }
   for (int cell = blockIdx.x; cell < a.ncells; cell += gridDim.x) {
     const size_t A0 = FUSED ? 0 : (size_t)cell * N * N, b0 = FUSED ? 0 : (size_t)cell * N;
-    auto A = [&](int r, int c) {
+    auto A = [&](int r, int c) {  // rows r >= NS only
       if constexpr (FUSED)
-        return Ar::ldc(sA0, sA1, (size_t)r + (size_t)N * c);
+        return Ar::ldc(sA0, sA1, (size_t)(r - NS) + (size_t)NR * c);
       else
         return Ar::ld(a.A0, a.A1, A0 + (size_t)r + (size_t)N * c);
     };
@@ -449,8 +481,8 @@ __global__ void __launch_bounds__(C::NT, 1) condense_l2block_kernel(L2BlockArgs 
         Dh[r] = Ar::of(v);
       }
     }
-    // the cell's trace couplings: entries of A_fi / A_if on the facet's nodes
-    // that are exactly zero are skipped below (they contribute nothing)
+    // the cell's trace couplings: entries of A_fi on the facet's nodes that
+    // are exactly zero are skipped below (they contribute nothing)
     {
       const int fm = L.fn_max;
       for (int e = t; e < NF * (NSYM + NC2) * fm; e += NT) {
@@ -459,7 +491,7 @@ __global__ void __launch_bounds__(C::NT, 1) condense_l2block_kernel(L2BlockArgs 
         if (q >= L.fn_cnt[lf]) continue;
         const int node = L.fn_node[lf][q];
         const int m = cc < NSYM ? cc * NK + node : NS + (cc - NSYM) * NK + node;
-        if (Ar::nonzero(A(NI + f, m)) || Ar::nonzero(A(m, NI + f))) atomicOr(&L.fmask[lf][kf], 1 << cc);
+        if (Ar::nonzero(A(NI + f, m))) atomicOr(&L.fmask[lf][kf], 1 << cc);
       }
     }
     __syncthreads();
@@ -470,7 +502,7 @@ __global__ void __launch_bounds__(C::NT, 1) condense_l2block_kernel(L2BlockArgs 
 #pragma unroll
       for (int cp = 0; cp < NSYM; ++cp) {
         T[cp] = Ar::zero();
-        for (int k = 0; k < NK; ++k) Ar::mac(T[cp], Mi[an * NK + k], B(cp * NK + k));
+        for (int k = 0; k < NK; ++k) Ar::mac(T[cp], MI(an * NK + k), B(cp * NK + k));
         T[cp] = Ar::fin(T[cp]);
       }
 #pragma unroll
@@ -553,73 +585,147 @@ __global__ void __launch_bounds__(C::NT, 1) condense_l2block_kernel(L2BlockArgs 
       }
     }
     __syncthreads();
-    // 3. LU with partial pivoting of [P | Q]; the pivot search is warp 0's
-    for (int j = 0; j < NU; ++j) {
-      if (t < 32) {
-        auto best = Ar::mag(Ar::zero()) - 1;
-        int bi = j;
-        for (int i = j + t; i < NU; i += 32) {
-          const auto v = Ar::mag(P[i * NU + j]);
-          if (v > best) {
-            best = v;
-            bi = i;
+    // 3. blocked LU with partial pivoting of [P | Q], panels of NB columns:
+    //    warp 0 factors the panel (pivot search, row swaps and updates inside
+    //    the panel, __syncwarp only); then the CTA applies the panel's swaps to
+    //    the trailing columns, solves the panel's block row and updates the
+    //    trailing matrix with register tiles (rank-NB).  The multipliers of L
+    //    are not swapped (only U and the transformed Q are used later).
+    {
+      constexpr int NB = 8, TCW = NU + NC;  // columns of [P | Q]
+      auto W = [&](int r, int c) -> V & { return c < NU ? P[r * NU + c] : Q[r * NC + (c - NU)]; };
+      for (int j0 = 0; j0 < NU; j0 += NB) {
+        const int nb = min(NB, NU - j0);
+        if (t < 32) {
+          for (int jj = j0; jj < j0 + nb; ++jj) {
+            auto best = Ar::mag(Ar::zero()) - 1;
+            int bi = jj;
+            for (int i = jj + t; i < NU; i += 32) {
+              const auto v = Ar::mag(P[i * NU + jj]);
+              if (v > best) {
+                best = v;
+                bi = i;
+              }
+            }
+            for (int off = 16; off > 0; off >>= 1) {
+              const auto ob = __shfl_xor_sync(0xffffffffu, best, off);
+              const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
+              if (ob > best || (ob == best && oi < bi)) {
+                best = ob;
+                bi = oi;
+              }
+            }
+            if (t == 0) {
+              L.pivs[jj - j0] = bi;
+              if (!(best > 0) && L.info == 0) L.info = jj + 1;
+            }
+            if (bi != jj && t < nb) {  // swap rows jj and bi inside the panel
+              const V tmp = P[jj * NU + j0 + t];
+              P[jj * NU + j0 + t] = P[bi * NU + j0 + t];
+              P[bi * NU + j0 + t] = tmp;
+            }
+            __syncwarp();
+            const V pv = P[jj * NU + jj];
+            for (int i = jj + 1 + t; i < NU; i += 32) {
+              const V l = Ar::nonzero(pv) ? Ar::div(P[i * NU + jj], pv) : Ar::zero();
+              P[i * NU + jj] = l;
+              for (int c = jj + 1; c < j0 + nb; ++c) P[i * NU + c] = Ar::sub(P[i * NU + c], Ar::mul(l, P[jj * NU + c]));
+            }
+            __syncwarp();
           }
         }
-        for (int off = 16; off > 0; off >>= 1) {
-          const auto ob = __shfl_down_sync(0xffffffffu, best, off);
-          const int oi = __shfl_down_sync(0xffffffffu, bi, off);
-          if (ob > best || (ob == best && oi < bi)) {
-            best = ob;
-            bi = oi;
+        __syncthreads();
+        // the panel's swaps on the trailing columns, then its block row U12 = L11^{-1} A12
+        for (int c = j0 + nb + t; c < TCW; c += NT) {
+          for (int q = 0; q < nb; ++q) {
+            const int pr = L.pivs[q];
+            if (pr != j0 + q) {
+              const V tmp = W(j0 + q, c);
+              W(j0 + q, c) = W(pr, c);
+              W(pr, c) = tmp;
+            }
+          }
+          for (int i = 1; i < nb; ++i) {
+            V acc = Ar::zero();
+            for (int m = 0; m < i; ++m) Ar::mac(acc, P[(j0 + i) * NU + j0 + m], W(j0 + m, c));
+            W(j0 + i, c) = Ar::sub(W(j0 + i, c), Ar::fin(acc));
           }
         }
-        if (t == 0) {
-          L.piv = bi;
-          if (!(best > 0) && L.info == 0) L.info = j + 1;
+        __syncthreads();
+        // trailing update: W[i][c] -= L21[i][.] U12[.][c], tiles of 4 rows x 4 columns
+        {
+          const int r0 = j0 + nb, rows = NU - r0, c0s = j0 + nb, cols = TCW - c0s;
+          const int RTt = (rows + 3) / 4, CTt = (cols + 3) / 4;
+          for (int o = t; o < RTt * CTt; o += NT) {  // columns fastest: L broadcast, U rows contiguous
+            const int cb = c0s + (o % CTt) * 4, ib = r0 + (o / CTt) * 4;
+            V acc[4][4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+              for (int j = 0; j < 4; ++j) acc[i][j] = Ar::zero();
+            for (int m = 0; m < nb; ++m) {
+              V lv[4], uv[4];
+#pragma unroll
+              for (int i = 0; i < 4; ++i) lv[i] = P[min(ib + i, NU - 1) * NU + j0 + m];
+#pragma unroll
+              for (int j = 0; j < 4; ++j) uv[j] = W(j0 + m, min(cb + j, TCW - 1));
+#pragma unroll
+              for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) Ar::mac(acc[i][j], lv[i], uv[j]);
+            }
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+              for (int j = 0; j < 4; ++j)
+                if (ib + i < NU && cb + j < TCW) W(ib + i, cb + j) = Ar::sub(W(ib + i, cb + j), Ar::fin(acc[i][j]));
+          }
         }
+        __syncthreads();
       }
-      __syncthreads();
-      const int p = L.piv;
-      if (p != j)
-        for (int c = t; c < NU + NC; c += NT) {
-          V *row_j = c < NU ? P + j * NU + c : Q + j * NC + (c - NU);
-          V *row_p = c < NU ? P + p * NU + c : Q + p * NC + (c - NU);
-          const V tmp = *row_j;
-          *row_j = *row_p;
-          *row_p = tmp;
-        }
-      __syncthreads();
-      const V pv = P[j * NU + j];
-      if (Ar::nonzero(pv))
-        for (int i = j + 1 + t; i < NU; i += NT) P[i * NU + j] = Ar::div(P[i * NU + j], pv);
-      __syncthreads();
-      const int rows = NU - j - 1, w = NU - j - 1, cols = w + NC;
-      for (int e = t; e < rows * cols; e += NT) {
-        const int i = j + 1 + e / cols, c = e % cols;
-        const V l = P[i * NU + j];
-        V *tg;
-        V u;
-        if (c < w) {
-          u = P[j * NU + j + 1 + c];
-          tg = P + i * NU + j + 1 + c;
-        } else {
-          u = Q[j * NC + c - w];
-          tg = Q + i * NC + c - w;
-        }
-        *tg = Ar::sub(*tg, Ar::mul(l, u));
-      }
-      __syncthreads();
     }
-    // 4. back substitution: X_u = U^{-1} Q, in Q
-    for (int j = NU - 1; j >= 0; --j) {
-      const V pv = P[j * NU + j];
-      for (int c = t; c < NC; c += NT) Q[j * NC + c] = Ar::nonzero(pv) ? Ar::div(Q[j * NC + c], pv) : Ar::zero();
-      __syncthreads();
-      for (int e = t; e < j * NC; e += NT) {
-        const int i = e / NC, c = e - i * NC;
-        Q[i * NC + c] = Ar::sub(Q[i * NC + c], Ar::mul(P[i * NU + j], Q[j * NC + c]));
+    // 4. blocked back substitution X_u = U^{-1} Q, in Q: the diagonal block of
+    //    NB rows column by column, then the rows above by register tiles
+    {
+      constexpr int NB = 8;
+      for (int i1 = NU; i1 > 0; i1 -= NB) {
+        const int i0 = max(0, i1 - NB);
+        for (int c = t; c < NC; c += NT)
+          for (int i = i1 - 1; i >= i0; --i) {
+            V acc = Ar::zero();
+            for (int m = i + 1; m < i1; ++m) Ar::mac(acc, P[i * NU + m], Q[m * NC + c]);
+            const V pv = P[i * NU + i];
+            const V r = Ar::sub(Q[i * NC + c], Ar::fin(acc));
+            Q[i * NC + c] = Ar::nonzero(pv) ? Ar::div(r, pv) : Ar::zero();
+          }
+        __syncthreads();
+        const int RTt = (i0 + 3) / 4, CTt = (NC + 3) / 4;
+        for (int o = t; o < RTt * CTt; o += NT) {  // columns fastest
+          const int cb = (o % CTt) * 4, ib = (o / CTt) * 4;
+          V acc[4][4];
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[i][j] = Ar::zero();
+          for (int m = i0; m < i1; ++m) {
+            V lv[4], xv[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) lv[i] = P[min(ib + i, i0 - 1) * NU + m];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) xv[j] = Q[m * NC + min(cb + j, NC - 1)];
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+              for (int j = 0; j < 4; ++j) Ar::mac(acc[i][j], lv[i], xv[j]);
+          }
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+              if (ib + i < i0 && cb + j < NC) Q[(ib + i) * NC + cb + j] = Ar::sub(Q[(ib + i) * NC + cb + j], Ar::fin(acc[i][j]));
+        }
+        __syncthreads();
       }
-      __syncthreads();
     }
     // 5. X_s = Z - Y X_u = Z - sum_e sum_k W_e[:][k] (MG_e X_u[(k, .)]):
     //    first T_e[(k,a)][c] = sum_b MG_e[a][b] X_u[(k,b)][c] (4 columns per thread)
