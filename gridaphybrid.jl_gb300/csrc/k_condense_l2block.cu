@@ -144,8 +144,10 @@ struct ECfg {
   static constexpr bool MI_SHARED = ELAST || NK < 64;
   // shared: P (NU x NU), Q (NU x NC), M^{-1} (NK x NK), C^{-1}/|J| (6 x 6),
   // the panel coefficients W (D x NC1 x NC2) and Dh (NC1 x NC2 x NL), as values
+  // P's row stride
+  static constexpr int LDP = NU;
   static constexpr size_t smem_values =
-      (size_t)NU * NU + (size_t)NU * NC + (MI_SHARED ? (size_t)NK * NK : 0) + 36 + 54 + 108;
+      (size_t)NU * LDP + (size_t)NU * NC + (MI_SHARED ? (size_t)NK * NK : 0) + 36 + 54 + 108;
   // per-CTA scratch, column-major, as values: Z / X_s (NS x NC), the products
   // T (D NU x NC); the fused kernel adds the cell block A (N x N) and b (N)
   static constexpr size_t slot_values = (size_t)NS * NC + (size_t)D * NU * NC;
@@ -337,7 +339,8 @@ __global__ void __launch_bounds__(C::NT, C::MI_SHARED ? 1 : 2) condense_l2block_
                 NC = C::NC, NT = C::NT, NFD = C::NFD, NL = C::NL, NFS = C::NFS;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   V *P = reinterpret_cast<V *>(smem_raw);  // [r][j]
-  V *Q = P + NU * NU;                      // [r][c]
+  constexpr int LDP = C::LDP;
+  V *Q = P + NU * LDP;                     // [r][c]
   V *Mi = Q + (size_t)NU * NC;             // [a][k]
   V *Ci = Mi + (C::MI_SHARED ? NK * NK : 0);  // [c][d]
   V *Wc = Ci + 36;                         // [(e NC1 + c) NC2 + k]
@@ -578,7 +581,7 @@ __global__ void __launch_bounds__(C::NT, C::MI_SHARED ? 1 : 2) condense_l2block_
           const V rv = col < NU ? A(NS + r, NS + col) : col - NU < NF ? A(NS + r, NI + col - NU) : B(NS + r);
           const V v = Ar::sub(rv, Ar::fin(acc[i]));
           if (col < NU)
-            P[r * NU + col] = v;
+            P[r * LDP + col] = v;
           else
             Q[r * NC + col - NU] = v;
         }
@@ -593,7 +596,7 @@ __global__ void __launch_bounds__(C::NT, C::MI_SHARED ? 1 : 2) condense_l2block_
     //    are not swapped (only U and the transformed Q are used later).
     {
       constexpr int NB = 8, TCW = NU + NC;  // columns of [P | Q]
-      auto W = [&](int r, int c) -> V & { return c < NU ? P[r * NU + c] : Q[r * NC + (c - NU)]; };
+      auto W = [&](int r, int c) -> V & { return c < NU ? P[r * LDP + c] : Q[r * NC + (c - NU)]; };
       for (int j0 = 0; j0 < NU; j0 += NB) {
         const int nb = min(NB, NU - j0);
         if (t < 32) {
@@ -601,7 +604,7 @@ __global__ void __launch_bounds__(C::NT, C::MI_SHARED ? 1 : 2) condense_l2block_
             auto best = Ar::mag(Ar::zero()) - 1;
             int bi = jj;
             for (int i = jj + t; i < NU; i += 32) {
-              const auto v = Ar::mag(P[i * NU + jj]);
+              const auto v = Ar::mag(P[i * LDP + jj]);
               if (v > best) {
                 best = v;
                 bi = i;
@@ -620,16 +623,16 @@ __global__ void __launch_bounds__(C::NT, C::MI_SHARED ? 1 : 2) condense_l2block_
               if (!(best > 0) && L.info == 0) L.info = jj + 1;
             }
             if (bi != jj && t < nb) {  // swap rows jj and bi inside the panel
-              const V tmp = P[jj * NU + j0 + t];
-              P[jj * NU + j0 + t] = P[bi * NU + j0 + t];
-              P[bi * NU + j0 + t] = tmp;
+              const V tmp = P[jj * LDP + j0 + t];
+              P[jj * LDP + j0 + t] = P[bi * LDP + j0 + t];
+              P[bi * LDP + j0 + t] = tmp;
             }
             __syncwarp();
-            const V pv = P[jj * NU + jj];
+            const V pv = P[jj * LDP + jj];
             for (int i = jj + 1 + t; i < NU; i += 32) {
-              const V l = Ar::nonzero(pv) ? Ar::div(P[i * NU + jj], pv) : Ar::zero();
-              P[i * NU + jj] = l;
-              for (int c = jj + 1; c < j0 + nb; ++c) P[i * NU + c] = Ar::sub(P[i * NU + c], Ar::mul(l, P[jj * NU + c]));
+              const V l = Ar::nonzero(pv) ? Ar::div(P[i * LDP + jj], pv) : Ar::zero();
+              P[i * LDP + jj] = l;
+              for (int c = jj + 1; c < j0 + nb; ++c) P[i * LDP + c] = Ar::sub(P[i * LDP + c], Ar::mul(l, P[jj * LDP + c]));
             }
             __syncwarp();
           }
@@ -647,7 +650,7 @@ __global__ void __launch_bounds__(C::NT, C::MI_SHARED ? 1 : 2) condense_l2block_
           }
           for (int i = 1; i < nb; ++i) {
             V acc = Ar::zero();
-            for (int m = 0; m < i; ++m) Ar::mac(acc, P[(j0 + i) * NU + j0 + m], W(j0 + m, c));
+            for (int m = 0; m < i; ++m) Ar::mac(acc, P[(j0 + i) * LDP + j0 + m], W(j0 + m, c));
             W(j0 + i, c) = Ar::sub(W(j0 + i, c), Ar::fin(acc));
           }
         }
@@ -657,7 +660,7 @@ __global__ void __launch_bounds__(C::NT, C::MI_SHARED ? 1 : 2) condense_l2block_
           const int r0 = j0 + nb, rows = NU - r0, c0s = j0 + nb, cols = TCW - c0s;
           const int RTt = (rows + 3) / 4, CTt = (cols + 3) / 4;
           for (int o = t; o < RTt * CTt; o += NT) {  // columns fastest: L broadcast, U rows contiguous
-            const int cb = c0s + (o % CTt) * 4, ib = r0 + (o / CTt) * 4;
+            const int cb = c0s + (o % CTt), ib = r0 + (o / CTt) * 4;  // columns cb + j CTt
             V acc[4][4];
 #pragma unroll
             for (int i = 0; i < 4; ++i)
@@ -666,9 +669,9 @@ __global__ void __launch_bounds__(C::NT, C::MI_SHARED ? 1 : 2) condense_l2block_
             for (int m = 0; m < nb; ++m) {
               V lv[4], uv[4];
 #pragma unroll
-              for (int i = 0; i < 4; ++i) lv[i] = P[min(ib + i, NU - 1) * NU + j0 + m];
+              for (int i = 0; i < 4; ++i) lv[i] = P[min(ib + i, NU - 1) * LDP + j0 + m];
 #pragma unroll
-              for (int j = 0; j < 4; ++j) uv[j] = W(j0 + m, min(cb + j, TCW - 1));
+              for (int j = 0; j < 4; ++j) uv[j] = W(j0 + m, min(cb + j * CTt, TCW - 1));
 #pragma unroll
               for (int i = 0; i < 4; ++i)
 #pragma unroll
@@ -678,7 +681,8 @@ __global__ void __launch_bounds__(C::NT, C::MI_SHARED ? 1 : 2) condense_l2block_
             for (int i = 0; i < 4; ++i)
 #pragma unroll
               for (int j = 0; j < 4; ++j)
-                if (ib + i < NU && cb + j < TCW) W(ib + i, cb + j) = Ar::sub(W(ib + i, cb + j), Ar::fin(acc[i][j]));
+                if (ib + i < NU && cb + j * CTt < TCW)
+                  W(ib + i, cb + j * CTt) = Ar::sub(W(ib + i, cb + j * CTt), Ar::fin(acc[i][j]));
           }
         }
         __syncthreads();
@@ -693,15 +697,15 @@ __global__ void __launch_bounds__(C::NT, C::MI_SHARED ? 1 : 2) condense_l2block_
         for (int c = t; c < NC; c += NT)
           for (int i = i1 - 1; i >= i0; --i) {
             V acc = Ar::zero();
-            for (int m = i + 1; m < i1; ++m) Ar::mac(acc, P[i * NU + m], Q[m * NC + c]);
-            const V pv = P[i * NU + i];
+            for (int m = i + 1; m < i1; ++m) Ar::mac(acc, P[i * LDP + m], Q[m * NC + c]);
+            const V pv = P[i * LDP + i];
             const V r = Ar::sub(Q[i * NC + c], Ar::fin(acc));
             Q[i * NC + c] = Ar::nonzero(pv) ? Ar::div(r, pv) : Ar::zero();
           }
         __syncthreads();
         const int RTt = (i0 + 3) / 4, CTt = (NC + 3) / 4;
         for (int o = t; o < RTt * CTt; o += NT) {  // columns fastest
-          const int cb = (o % CTt) * 4, ib = (o / CTt) * 4;
+          const int cb = o % CTt, ib = (o / CTt) * 4;  // columns cb + j CTt
           V acc[4][4];
 #pragma unroll
           for (int i = 0; i < 4; ++i)
@@ -710,9 +714,9 @@ __global__ void __launch_bounds__(C::NT, C::MI_SHARED ? 1 : 2) condense_l2block_
           for (int m = i0; m < i1; ++m) {
             V lv[4], xv[4];
 #pragma unroll
-            for (int i = 0; i < 4; ++i) lv[i] = P[min(ib + i, i0 - 1) * NU + m];
+            for (int i = 0; i < 4; ++i) lv[i] = P[min(ib + i, i0 - 1) * LDP + m];
 #pragma unroll
-            for (int j = 0; j < 4; ++j) xv[j] = Q[m * NC + min(cb + j, NC - 1)];
+            for (int j = 0; j < 4; ++j) xv[j] = Q[m * NC + min(cb + j * CTt, NC - 1)];
 #pragma unroll
             for (int i = 0; i < 4; ++i)
 #pragma unroll
@@ -722,7 +726,8 @@ __global__ void __launch_bounds__(C::NT, C::MI_SHARED ? 1 : 2) condense_l2block_
           for (int i = 0; i < 4; ++i)
 #pragma unroll
             for (int j = 0; j < 4; ++j)
-              if (ib + i < i0 && cb + j < NC) Q[(ib + i) * NC + cb + j] = Ar::sub(Q[(ib + i) * NC + cb + j], Ar::fin(acc[i][j]));
+              if (ib + i < i0 && cb + j * CTt < NC)
+                Q[(ib + i) * NC + cb + j * CTt] = Ar::sub(Q[(ib + i) * NC + cb + j * CTt], Ar::fin(acc[i][j]));
         }
         __syncthreads();
       }
@@ -732,7 +737,7 @@ __global__ void __launch_bounds__(C::NT, C::MI_SHARED ? 1 : 2) condense_l2block_
     {
       constexpr int CT = (NC + 3) / 4;
       for (int o = t; o < D * NU * CT; o += NT) {
-        const int c0 = (o % CT) * 4, row = o / CT, e = row / NU, u = row - e * NU, k = u / NK, an = u - k * NK;
+        const int c0 = o % CT, row = o / CT, e = row / NU, u = row - e * NU, k = u / NK, an = u - k * NK;  // columns c0 + j CT
         V acc[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) acc[j] = Ar::zero();
@@ -740,11 +745,11 @@ __global__ void __launch_bounds__(C::NT, C::MI_SHARED ? 1 : 2) condense_l2block_
           const V rv = RV(a.voff_r + p);
           const V *xq = Q + (k * NK + rri[p]) * NC;
 #pragma unroll
-          for (int j = 0; j < 4; ++j) Ar::mac(acc[j], rv, xq[min(c0 + j, NC - 1)]);
+          for (int j = 0; j < 4; ++j) Ar::mac(acc[j], rv, xq[min(c0 + j * CT, NC - 1)]);
         }
 #pragma unroll
         for (int j = 0; j < 4; ++j)
-          if (c0 + j < NC) Tp[(size_t)(e * NU + u) + (size_t)D * NU * (c0 + j)] = Ar::fin(acc[j]);
+          if (c0 + j * CT < NC) Tp[(size_t)(e * NU + u) + (size_t)D * NU * (c0 + j * CT)] = Ar::fin(acc[j]);
       }
     }
     __syncthreads();
@@ -753,7 +758,7 @@ __global__ void __launch_bounds__(C::NT, C::MI_SHARED ? 1 : 2) condense_l2block_
     {
       constexpr int CT = (NC + 3) / 4;
       for (int o = t; o < NS * CT; o += NT) {
-        const int c0 = (o % CT) * 4, m = o / CT, c = m / NK, an = m - c * NK;
+        const int c0 = o % CT, m = o / CT, c = m / NK, an = m - c * NK;  // columns c0 + j CT
         V acc[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) acc[j] = Ar::zero();
@@ -763,11 +768,11 @@ __global__ void __launch_bounds__(C::NT, C::MI_SHARED ? 1 : 2) condense_l2block_
             if (!Ar::nonzero(w)) continue;
             const V *tp = Tp + (size_t)(e * NU + k * NK + an);
 #pragma unroll
-            for (int j = 0; j < 4; ++j) Ar::mac(acc[j], w, tp[(size_t)D * NU * min(c0 + j, NC - 1)]);
+            for (int j = 0; j < 4; ++j) Ar::mac(acc[j], w, tp[(size_t)D * NU * min(c0 + j * CT, NC - 1)]);
           }
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-          const int col = c0 + j;
+          const int col = c0 + j * CT;
           if (col >= NC) continue;
           V z;
           if (col < NF) {
