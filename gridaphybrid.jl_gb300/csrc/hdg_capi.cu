@@ -431,6 +431,7 @@ int hdg_context_create(int device, hdg_context **out) {
   ctx->device = device;
   ctx->num_sms = prop.multiProcessorCount;
   ctx->smem_optin = prop.sharedMemPerBlockOptin;
+  ctx->coop = prop.cooperativeLaunch != 0;
   if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
     delete ctx;
     return HDG_ERR_CUDA;
@@ -1023,8 +1024,8 @@ static int solve_pcg_refined(hdg_problem *pb, double rtol, int maxit, int *it_ou
   CUDA_TRY(ctx, pb->d_Binv32.reserve(sizeof(float) * nbr * nfd * nfd));
   CUDA_TRY(ctx, pb->d_v32.reserve(sizeof(float) * 5 * n));
   CUDA_TRY(ctx, pb->d_qc.reserve(sizeof(float) * pb->mesh.ncells * nl * nfd));
-  // last-CTA counter and the bulk-copy error flag start at zero
-  CUDA_TRY(ctx, cudaMemsetAsync(pb->d_counter.ptr, 0, sizeof(unsigned int) * 2, ctx->stream));
+  // last-CTA counter, bulk-copy error flag and the grid-barrier count and generation start at zero
+  CUDA_TRY(ctx, cudaMemsetAsync(pb->d_counter.ptr, 0, sizeof(unsigned int) * 4, ctx->stream));
   CUDA_TRY(ctx, pb->d_scal2.reserve(sizeof(double) * 16));
   CUDA_TRY(ctx, launch_binv_to_f32(nbr * nfd * nfd, pb->d_Binv.as<double>(), pb->d_Binv32.as<float>(), ctx->stream,
                                    &ctx->launches));
@@ -1045,7 +1046,18 @@ static int solve_pcg_refined(hdg_problem *pb, double rtol, int maxit, int *it_ou
   oa.nparts = ia.nparts;
   oa.sign = skeleton_sign(pb);
   const int pairs = 8;
-  if (!pb->pcg32_graph) {
+  // the inner iterations as one cooperative launch per chunk where its grid
+  // can be co-resident (about two cell units per CTA on small problems), else
+  // replays of a graph of 8 two-kernel iteration pairs
+  int pgrid = 0, pstage = 0;
+  size_t psmem = 0;
+  if (ctx->coop && ctx->persistent_pcg) {
+    const int cps = cellop_cps(nl * (int)nfd);
+    const long long units = (pb->mesh.ncells + cps - 1) / cps;
+    const long long want = std::min<long long>(std::max<long long>((units + 1) / 2, 1), (long long)ctx->num_sms * 8);
+    pgrid = pcg32_persistent_config(nl, (int)nfd, ctx->smem_optin, ctx->num_sms, (int)want, &pstage, &psmem);
+  }
+  if (!pgrid && !pb->pcg32_graph) {
     cudaGraph_t g;
     long long dummy = 0;
     CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
@@ -1089,8 +1101,16 @@ static int solve_pcg_refined(hdg_problem *pb, double rtol, int maxit, int *it_ou
     }
     cycle_start = total;
     for (;;) {
-      CUDA_TRY(ctx, cudaGraphLaunch(pb->pcg32_graph, ctx->stream));
-      ctx->launches += 4LL * pairs;
+      if (pgrid) {
+        Pcg32Args pa = ia;
+        pa.nstage = pstage;
+        int cap = std::min(maxit - total, 4096) & ~1;  // even: the next launch starts from ia.p
+        if (cap < 2) cap = 2;
+        CUDA_TRY(ctx, launch_pcg32_persistent(pa, pgrid, psmem, cap, ctx->stream, &ctx->launches));
+      } else {
+        CUDA_TRY(ctx, cudaGraphLaunch(pb->pcg32_graph, ctx->stream));
+        ctx->launches += 4LL * pairs;
+      }
       CUDA_TRY(ctx, cudaMemcpyAsync(h, ia.scal, sizeof(double) * 16, cudaMemcpyDeviceToHost, ctx->stream));
       CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
       total = base + (int)h[8];
@@ -1467,6 +1487,13 @@ int hdg_set_refinement(hdg_problem *pb, double delta, int keep_direction) {
 int hdg_footprint(int D, int n, int k, int precision, int solver, double *bytes) {
   if (!bytes || D < 2 || D > 3 || n < 1 || k < 1 || k > kMaxK) return HDG_ERR_INVALID;
   *bytes = footprint_bound(D, n, k, precision, solver);
+  return HDG_OK;
+}
+
+int hdg_context_set_persistent_pcg(hdg_context *ctx, int on) {
+  if (!ctx) return HDG_ERR_INVALID;
+  if (on && !ctx->coop) return ctx->fail(HDG_ERR_INVALID, "the device has no cooperative launches");
+  ctx->persistent_pcg = on ? 1 : 0;
   return HDG_OK;
 }
 

@@ -172,6 +172,8 @@ struct hdg_context {
   long long launches = 0;
   int num_sms = 0;
   size_t smem_optin = 0;
+  bool coop = false;       // cooperative launches (the persistent inner PCG)
+  int persistent_pcg = 0;  // use them when the grid can be co-resident (opt-in)
   hdg::DBuf scratch[6];  // Map-level staging buffers
   cudaEvent_t ev[8] = {nullptr};
   cudaEvent_t user_ev[4] = {nullptr};

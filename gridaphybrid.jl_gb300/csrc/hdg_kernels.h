@@ -305,6 +305,15 @@ struct Pcg32Args {
   unsigned int *error;    // set to 1 when a bulk copy never completed
   int uctas;              // grid of the update kernel (partials: 2 x uctas)
 };
+// The inner FP32 PCG as one cooperative launch (k_pcg32_persistent.cu):
+// grid, ring depth and dynamic shared memory for this shape (grid 0: not
+// available), then the launch of up to iter_cap iterations (stops at
+// SC_DONE; a.nstage must be the configured depth).  Uses counter[2],
+// counter[3] (zeroed before the first launch) for its grid barriers and
+// partials[0 .. 3 grid).
+int pcg32_persistent_config(int nl, int nfd, size_t smem_optin, int num_sms, int want, int *nstage, size_t *smem);
+cudaError_t launch_pcg32_persistent(const Pcg32Args &a, int grid, size_t smem, int iter_cap, cudaStream_t s,
+                                    long long *launches);
 // threads per CTA of the PCG vector kernels (kPcgThreads on the device side)
 // and the longest skeleton row their FP64 SpMV stages (kMaxRowLen)
 constexpr int kPcgThreadsHost = 256;

@@ -255,19 +255,37 @@ __global__ void __launch_bounds__(CellOp<NL, NFD>::THREADS)
   }
   __syncthreads();
   double acc = 0.0;
+  // The gather of p = z + beta p_old is pipelined across stages: the block-row
+  // entry of stage t+2 and the p_old / z values of stage t+1 are loaded while
+  // stage t is computed (two dependent loads, each hidden behind one stage).
+  auto load_ent = [&](int tt) -> int {
+    const int cc = ((int)blockIdx.x + tt * (int)gridDim.x) * C::CPS + g;
+    return (tt < mine && i < C::NF && cc < a.ncells) ? a.cell_blk[(size_t)cc * NL + lf] : -1;
+  };
+  int ent_a = load_ent(0), ent_b = load_ent(1);
+  float po_a = 0.0f, z_a = 0.0f;
+  if (ent_a >= 0) {
+    const int row = (ent_a >> 1) * NFD + r;
+    po_a = p_old[row];
+    z_a = a.z[row];
+  }
   for (int t = 0; t < mine; ++t) {
     const int slot = t % nstage;
     const int c = ((int)blockIdx.x + t * (int)gridDim.x) * C::CPS + g;
     const bool act = i < C::NF && c < a.ncells;
     float pv = 0.0f;
-    if (act) {
-      const int ent = a.cell_blk[(size_t)c * NL + lf];
-      if (ent >= 0) {
-        const int row = (ent >> 1) * NFD + r;
-        pv = fmaf(beta, p_old[row], a.z[row]);
-        if (ent & 1) p_new[row] = pv;
-      }
+    if (ent_a >= 0) {
+      pv = fmaf(beta, po_a, z_a);
+      if (ent_a & 1) p_new[(ent_a >> 1) * NFD + r] = pv;
     }
+    // stage t+1's values, stage t+2's entry
+    ent_a = ent_b;
+    if (ent_a >= 0) {
+      const int row = (ent_a >> 1) * NFD + r;
+      po_a = p_old[row];
+      z_a = a.z[row];
+    }
+    ent_b = load_ent(t + 2);
     ps[g][i] = pv;
     if (!mbar_wait_bounded(&bars[slot], (uint32_t)(t / nstage) & 1u)) abort_flag = 1;
     __syncthreads();

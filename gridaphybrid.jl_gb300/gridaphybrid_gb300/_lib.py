@@ -78,6 +78,7 @@ SIGNATURES = {
     "hdg_l2_errors": (_i, [_vp, _vp, _vp]),
     "hdg_solve": (_i, [_vp, _i, _i, _d, _i, _vp, _vp, _vp]),
     "hdg_get_timings": (_i, [_vp, _vp]),
+    "hdg_context_set_persistent_pcg": (_i, [_vp, ctypes.c_int]),
     "hdg_time_kernel": (_i, [_vp, _i, _i, _vp]),
     "hdg_problem_device_bytes": (_i, [_vp, _vp]),
     "hdg_set_refinement": (_i, [_vp, _d, _i]),

@@ -284,6 +284,13 @@ int hdg_solve(hdg_problem *pb, int precision, int solver, double rtol,
               int maxit, const double *kappa, double *free_dof_values,
               double *stats);
 
+/* Inner FP32 skeleton iterations of the fast paths as one cooperative launch
+ * per chunk (on = 1: every iteration's SpMV and update phases inside one
+ * kernel, separated by bounded grid barriers) instead of replays of a CUDA
+ * graph of two-kernel iterations (on = 0, the default).  Same arithmetic; the
+ * sums run over a different number of CTAs, so the last bits may differ. */
+int hdg_context_set_persistent_pcg(hdg_context *ctx, int on);
+
 /* Device-event timings of the last hdg_assemble/solve_skeleton/recover calls
  * in ms: [integrate, condense, assemble, skeleton solve, recover]. */
 int hdg_get_timings(const hdg_problem *pb, double *ms);

@@ -144,3 +144,30 @@ def test_fast_solve_is_deterministic(ctx, precision):
     assert np.array_equal(runs[0][0], runs[1][0])
     assert np.array_equal(runs[0][1], runs[1][1])
     assert runs[0][2] == runs[1][2]
+
+
+@pytest.mark.parametrize("case", ["darcy-k2", "darcy-k3", "elasticity-k2"])
+def test_persistent_inner_pcg_matches_graph_path(case):
+    """The inner FP32 iterations as one cooperative launch (bounded grid
+    barriers) give the solution of the two-kernel graph path: both solved to
+    1e-12, agreeing to 1e-9."""
+    from gridaphybrid_gb300 import cases
+    sols = []
+    for on in (0, 1):
+        c = gh.Context(0)
+        c.check(c.lib.hdg_context_set_persistent_pcg(c.handle, on))
+        if case == "darcy-k2":
+            kappa = np.exp(np.random.default_rng(31).normal(size=6 * 5 * 4))
+            model = gh.CartesianDiscreteModel((0, 1) * 3, (6, 5, 4))
+            X, Y = gh.darcy_spaces(model, 2)
+            op = gh.HybridAffineFEOperator(gh.DarcyHDG(tau=1.0, problem="sin", kappa=kappa), X, Y, [1, 2], [3],
+                                           precision=_lib.HDG_PREC_FF_BLOCK, context=c)
+        elif case == "darcy-k3":
+            op = cases.darcy(4, 3, context=c)
+        else:
+            op = cases.elasticity(4, 2, context=c)
+        xh = gh.solve(op, solver="pcg", rtol=1e-12)
+        sols.append(xh.free_dof_values.copy())
+        op.pb.close()
+        c.close()
+    assert relmax(sols[1], sols[0]) < 1e-9
