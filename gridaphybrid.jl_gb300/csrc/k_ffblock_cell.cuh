@@ -74,7 +74,9 @@ struct Cfg {
   // formed), Z (D NK NC), Q (NK NC), each hi + lo -- 71 KB for 3D k=2, three
   // CTAs per SM
   static constexpr size_t smem_floats = 2 * ((size_t)D * NK * NK + NK * NK + (size_t)D * NK * NC + NK * NC);
-  static constexpr size_t smem_bytes = smem_floats * 4 + 64 * 4;
+  // + flags (64 ints) + per local facet the interior columns its trace rows couple to (2D x NI ints, counts)
+  static constexpr int NL = 2 * D;
+  static constexpr size_t smem_bytes = smem_floats * 4 + 64 * 4 + ((size_t)NL * NI + 8) * 4;
 };
 
 // A entry (row r, column c) of the column-major N x N cell matrix (hi, lo) and
@@ -110,6 +112,8 @@ __device__ __forceinline__ void ffblock_cell(bool active, const float *__restric
   float *Qh = Zl + D * NK * NC, *Ql = Qh + NK * NC;  // [a][c]
   const float *Mh = Ph, *Ml = Pl;                      // M^{-1} [a][k], until P is formed
   int *sflag = reinterpret_cast<int *>(Ql + NK * NC);  // [0] pivot row, [1] info
+  int *flist = sflag + 64;                             // [lf][q]: interior columns coupled to facet lf
+  int *fcnt = flist + C::NL * NI;                      // [lf]: their count
   // Threads run fastest over the row index of each output, so the
   // column-major A entries they read are broadcast (one column entry per
   // warp) or contiguous (consecutive rows of one column).
@@ -288,14 +292,39 @@ __device__ __forceinline__ void ffblock_cell(bool active, const float *__restric
     Zl[(d * NK + a) * NC + c] = rl;
   }
   __syncthreads();
+  // the interior columns each local facet's trace rows couple to (entries of
+  // A_fi that are exactly zero add nothing to S: skipping them leaves the bits
+  // unchanged), in increasing order: one warp per facet, ballot compaction
+  {
+    constexpr int NFACE = C::NL, NFDc = C::NFD;
+    const int lane = t & 31, warp = t >> 5, nwarps = NT >> 5;
+    for (int lf = warp; lf < NFACE; lf += nwarps) {
+      int base = 0;
+      for (int c0 = 0; c0 < NI; c0 += 32) {
+        const int col = c0 + lane;
+        bool nz = false;
+        if (col < NI)
+          for (int j = 0; j < NFDc; ++j) nz |= AH(NI + lf * NFDc + j, col) != 0.0f;
+        const unsigned bal = __ballot_sync(0xffffffffu, nz);
+        if (nz) flist[lf * NI + base + __popc(bal & ((1u << lane) - 1u))] = col;
+        base += __popc(bal);
+      }
+      if (lane == 0) fcnt[lf] = base;
+    }
+  }
+  __syncthreads();
   // S = A_ff - A_fi X, g = b_f - A_fi y
   for (int o = t; o < NF * NC; o += NT) {
-    const int f = o % NF, c = o / NF;
+    const int f = o % NF, c = o / NF, lf = f / C::NFD;
     float h = 0.0f, l = 0.0f;
-    for (int k = 0; k < NU; ++k)
-      mac(h, l, AH(NI + f, k), AL(NI + f, k), Zh[k * NC + c], Zl[k * NC + c]);
-    for (int k = 0; k < NK; ++k)
-      mac(h, l, AH(NI + f, NU + k), AL(NI + f, NU + k), Qh[k * NC + c], Ql[k * NC + c]);
+    const int cnt = fcnt[lf];
+    for (int q = 0; q < cnt; ++q) {
+      const int k = flist[lf * NI + q];
+      if (k < NU)
+        mac(h, l, AH(NI + f, k), AL(NI + f, k), Zh[k * NC + c], Zl[k * NC + c]);
+      else
+        mac(h, l, AH(NI + f, k), AL(NI + f, k), Qh[(k - NU) * NC + c], Ql[(k - NU) * NC + c]);
+    }
     const double rhs = c < NF ? (double)AH(NI + f, NI + c) + (double)AL(NI + f, NI + c)
                               : (double)LDB(bh, NI + f) + (double)LDB(bl, NI + f);
     const double v = rhs - ((double)h + (double)l);
