@@ -76,7 +76,7 @@ struct Cfg {
   static constexpr size_t smem_floats = 2 * ((size_t)D * NK * NK + NK * NK + (size_t)D * NK * NC + NK * NC);
   // + flags (64 ints) + per local facet the interior columns its trace rows couple to (2D x NI ints, counts)
   static constexpr int NL = 2 * D;
-  static constexpr size_t smem_bytes = smem_floats * 4 + 64 * 4 + ((size_t)NL * NI + 8) * 4;
+  static constexpr size_t smem_bytes = smem_floats * 4 + 64 * 4 + ((size_t)NL * NI + 8 + NL * 4) * 4;
 };
 
 // A entry (row r, column c) of the column-major N x N cell matrix (hi, lo) and
@@ -112,8 +112,35 @@ __device__ __forceinline__ void ffblock_cell(bool active, const float *__restric
   float *Qh = Zl + D * NK * NC, *Ql = Qh + NK * NC;  // [a][c]
   const float *Mh = Ph, *Ml = Pl;                      // M^{-1} [a][k], until P is formed
   int *sflag = reinterpret_cast<int *>(Ql + NK * NC);  // [0] pivot row, [1] info
-  int *flist = sflag + 64;                             // [lf][q]: interior columns coupled to facet lf
+  int *flist = sflag + 64;                             // [lf][q]: interior rows / columns coupled to facet lf
   int *fcnt = flist + C::NL * NI;                      // [lf]: their count
+  int *fseg = fcnt + 8;                                // [lf][d]: start of field d's entries (d <= D)
+  constexpr int NFACE = C::NL, NFDc = C::NFD;
+  const int lane = t & 31, warp = t >> 5, nwarps = NT >> 5;
+  // The interior rows each local facet's trace columns couple to (A_if: its
+  // exactly-zero entries add nothing to Z and Q), in increasing order, with
+  // the start of each field's rows: one warp per facet, ballot compaction.
+  for (int lf = warp; lf < NFACE; lf += nwarps) {
+    int base = 0;
+    for (int r0 = 0; r0 < NI; r0 += 32) {
+      const int row = r0 + lane;
+      bool nz = false;
+      if (row < NI)
+        for (int j = 0; j < NFDc; ++j) nz |= AH(row, NI + lf * NFDc + j) != 0.0f;
+      const unsigned bal = __ballot_sync(0xffffffffu, nz);
+      if (nz) flist[lf * NI + base + __popc(bal & ((1u << lane) - 1u))] = row;
+      base += __popc(bal);
+    }
+    __syncwarp();
+    if (lane == 0) {
+      fcnt[lf] = base;
+      int q = 0;
+      for (int d = 0; d <= D; ++d) {  // fields: D flux components, then the pressure
+        while (q < base && flist[lf * NI + q] < d * NK) ++q;
+        fseg[lf * 4 + d] = q;
+      }
+    }
+  }
   // Threads run fastest over the row index of each output, so the
   // column-major A entries they read are broadcast (one column entry per
   // warp) or contiguous (consecutive rows of one column).
@@ -136,13 +163,15 @@ __device__ __forceinline__ void ffblock_cell(bool active, const float *__restric
     if (c < NK) {  // G_d column c (pressure DOF c)
       for (int k = 0; k < NK; ++k)
         mac(h, l, Mh[a * NK + k], Ml[a * NK + k], AH(d * NK + k, NU + c), AL(d * NK + k, NU + c));
-    } else {
-      const int cc = c - NK;  // right-hand-side column (skeleton DOF or b)
-      for (int k = 0; k < NK; ++k) {
-        const float rh = cc < NF ? AH(d * NK + k, NI + cc) : LDB(bh, d * NK + k);
-        const float rl = cc < NF ? AL(d * NK + k, NI + cc) : LDB(bl, d * NK + k);
-        mac(h, l, Mh[a * NK + k], Ml[a * NK + k], rh, rl);
+    } else if (c - NK < NF) {  // skeleton column: only field d's rows coupled to its facet
+      const int cc = c - NK, lf = cc / NFDc;
+      const int q1 = fseg[lf * 4 + d + 1];
+      for (int q = fseg[lf * 4 + d]; q < q1; ++q) {
+        const int k = flist[lf * NI + q] - d * NK;
+        mac(h, l, Mh[a * NK + k], Ml[a * NK + k], AH(d * NK + k, NI + cc), AL(d * NK + k, NI + cc));
       }
+    } else {  // b
+      for (int k = 0; k < NK; ++k) mac(h, l, Mh[a * NK + k], Ml[a * NK + k], LDB(bh, d * NK + k), LDB(bl, d * NK + k));
     }
     float ph, pl;
     normalise(h, l);
@@ -170,11 +199,14 @@ __device__ __forceinline__ void ffblock_cell(bool active, const float *__restric
       Ph[a * NK + c] = rh;
       Pl[a * NK + c] = rl;
     } else {
-      const int cc = c - NK;
-      for (int d = 0; d < D; ++d)
+      const int cc = c - NK, lf = cc / NFDc;
+      for (int d = 0; d < D; ++d) {
+        // a skeleton column of Z_d is exactly zero when no row of field d couples to its facet
+        if (cc < NF && fseg[lf * 4 + d] == fseg[lf * 4 + d + 1]) continue;
         for (int k = 0; k < NK; ++k)
           mac(h, l, AH(NU + a, d * NK + k), AL(NU + a, d * NK + k), Zh[(d * NK + k) * NC + cc],
               Zl[(d * NK + k) * NC + cc]);
+      }
       const float rh0 = cc < NF ? AH(NU + a, NI + cc) : LDB(bh, NU + a);
       const float rl0 = cc < NF ? AL(NU + a, NI + cc) : LDB(bl, NU + a);
       float rh, rl;
@@ -296,8 +328,6 @@ __device__ __forceinline__ void ffblock_cell(bool active, const float *__restric
   // A_fi that are exactly zero add nothing to S: skipping them leaves the bits
   // unchanged), in increasing order: one warp per facet, ballot compaction
   {
-    constexpr int NFACE = C::NL, NFDc = C::NFD;
-    const int lane = t & 31, warp = t >> 5, nwarps = NT >> 5;
     for (int lf = warp; lf < NFACE; lf += nwarps) {
       int base = 0;
       for (int c0 = 0; c0 < NI; c0 += 32) {
