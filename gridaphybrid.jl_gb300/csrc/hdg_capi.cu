@@ -236,9 +236,11 @@ cudaError_t run_condense(hdg_problem *pb) {
     CellArgs a = cell_args(pb);
     cudaError_t e = launch_inv_mass_scale(a, pb->d_invm.as<double>(), ctx->stream, &ctx->launches);
     if (e != cudaSuccess) return e;
-    const float *Mh = pb->d_minv.as<float>(), *Ml = Mh + (size_t)pb->tab.nk * pb->tab.nk;
+    const size_t nk2 = (size_t)pb->tab.nk * pb->tab.nk;
+    const float *Mh = pb->d_minv.as<float>(), *Ml = Mh + nk2;
+    const float *MGh = Mh + 4 * nk2, *MGl = MGh + pb->tab.D * nk2;
     return launch_condense_ffblock(pb->tab.D, pb->tab.k, (int)nc, Ahi, Ahi + nc * n * n, bhi, bhi + nc * n, Mh, Ml,
-                                   pb->d_invm.as<double>(), pb->d_S.as<double>(), pb->d_g.as<double>(), Xhi,
+                                   MGh, MGl, pb->d_invm.as<double>(), pb->d_S.as<double>(), pb->d_g.as<double>(), Xhi,
                                    Xhi + nc * ni * (nf + 1), pb->d_info.as<int>(), ctx->stream, ctx->num_sms,
                                    &ctx->launches);
   }
@@ -354,12 +356,18 @@ int setup_problem(hdg_problem *pb) {
   if ((rc = upload(ctx, pb->d_tabf, packed_f))) return rc;
   {  // M_ref^{-1} for the block-elimination paths: (hi, lo) floats, then FP64
     const std::vector<double> &Mi = pb->tab.Minv;
-    std::vector<float> mf(4 * Mi.size());
+    // [M^{-1} hi | lo | FP64 | M^{-1} G_e hi | lo]
+    const std::vector<double> &MG = pb->tab.MG;
+    std::vector<float> mf(4 * Mi.size() + 2 * MG.size());
     for (size_t i = 0; i < Mi.size(); ++i) {
       mf[i] = (float)Mi[i];
       mf[Mi.size() + i] = (float)(Mi[i] - (double)mf[i]);
     }
     memcpy(mf.data() + 2 * Mi.size(), Mi.data(), sizeof(double) * Mi.size());
+    for (size_t i = 0; i < MG.size(); ++i) {
+      mf[4 * Mi.size() + i] = (float)MG[i];
+      mf[4 * Mi.size() + MG.size() + i] = (float)(MG[i] - (double)(float)MG[i]);
+    }
     if ((rc = upload(ctx, pb->d_minv, mf))) return rc;
   }
   if (l2block_supported(pb->physics == HDG_PHYSICS_ELASTICITY, pb->mesh.D, pb->mesh.k)) {
@@ -827,7 +835,7 @@ static int assemble_prepare(hdg_problem *pb, int precision, bool cell_blocks, bo
   if (mixed && !cellop_supported(nl, (int)t.nfd))
     return ctx->fail(HDG_ERR_INVALID, "no unassembled FP32 operator for %d facets of %zu DOFs", nl, t.nfd);
   if (precision == HDG_PREC_FF_BLOCK && cell_blocks && !eblock)
-    CUDA_TRY(ctx, pb->d_invm.reserve(sizeof(double) * nc));
+    CUDA_TRY(ctx, pb->d_invm.reserve(sizeof(double) * 10 * nc));
   pb->precision = precision;
   pb->eblock = eblock;
   // the L2-panel kernel integrates its cells itself unless the caller needs
@@ -1689,6 +1697,8 @@ int hdg_batch_assemble(hdg_batch *b, int precision, int *bad) {
         P.T = mixed_tables(pb);
         P.Mh = pb->d_minv.as<float>();
         P.Ml = P.Mh + (size_t)pb->tab.nk * pb->tab.nk;
+        P.MGh = P.Mh + 4 * (size_t)pb->tab.nk * pb->tab.nk;
+        P.MGl = P.MGh + (size_t)pb->tab.D * pb->tab.nk * pb->tab.nk;
         P.S = pb->d_S.as<double>();
         P.g = pb->d_g.as<double>();
         P.Xh = pb->d_fact.as<float>();

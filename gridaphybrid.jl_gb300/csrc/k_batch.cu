@@ -69,9 +69,11 @@ __global__ void __launch_bounds__(kBatchThreads) fused_ffblock_kernel(const Batc
     const BatchProblem &P = probs[p];
     const int c = active ? (int)(item - P.first) : 0;
     integrate_cell_ff(P.a, P.T, c, active, f, fq, Ah, Al, bh, bl, t, TPC, true);
-    const double invm = active ? cell_inv_mass(P.a, c) : 1.0;
+    double coef[10] = {1.0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    if (active) cell_y_coef(P.a, c, coef);
     int *infoc = active ? P.info + c : nullptr;
-    ffb::ffblock_cell<C, TPC, false>(active, Ah, Al, bh, bl, P.Mh, P.Ml, invm, fsm, P.S + (size_t)c * NF * NF,
+    ffb::ffblock_cell<C, TPC, false>(active, Ah, Al, bh, bl, P.Mh, P.Ml, P.MGh, P.MGl, coef, fsm,
+                                     P.S + (size_t)c * NF * NF,
                                      P.g + (size_t)c * NF, P.Xh + (size_t)c * NI * NC, P.Xl + (size_t)c * NI * NC,
                                      infoc, t);
     if (active && t == 0 && *infoc) atomicMax(bad + p, *infoc);

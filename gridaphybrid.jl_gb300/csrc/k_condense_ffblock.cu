@@ -11,14 +11,16 @@
 //   X_p = P^{-1} Q (LU with partial pivoting of the NK x NK pressure Schur)
 //   X_{u_d} = Z_d - Y_d X_p
 //   S = A_ff - A_fi X,   g = b_f - A_fi y
-// The only sequential part is the NK-step LU of P; everything else is small
-// dense products.  Every value is a float-float pair (~48 significant bits),
+// Y_d comes from the reference products M^{-1} G_e (exactly sparse on the
+// tensor-product cell) and per-cell coefficients; P, X_u, Z, Q and S skip the
+// exactly-zero entries.  The only sequential part is the NK-step LU of P.  Every value is a float-float pair (~48 significant bits),
 // so no refinement is needed (S agrees with the FP64 elimination to ~1e-14).
 #include <cuda_runtime.h>
 
 #include "hdg_kernels.h"
 #include "k_ff_cell.cuh"
 #include "k_ffblock_cell.cuh"
+#include "k_fp64_cell.cuh"
 
 namespace hdg {
 namespace ffb {
@@ -28,13 +30,15 @@ __global__ void __launch_bounds__(C::NT, 3)
     condense_ffblock_kernel(int ncells, const float *__restrict__ Ahi, const float *__restrict__ Alo,
                             const float *__restrict__ bhi, const float *__restrict__ blo,
                             const float *__restrict__ Minv_h, const float *__restrict__ Minv_l,
-                            const double *__restrict__ inv_m, double *S, double *g, float *Xhi, float *Xlo,
+                            const float *__restrict__ MG_h, const float *__restrict__ MG_l,
+                            const double *__restrict__ coef, double *S, double *g, float *Xhi, float *Xlo,
                             int *info) {
   constexpr int N = C::N, NF = C::NF, NI = C::NI, NC = C::NC;
   extern __shared__ float smem[];
   for (int cell = blockIdx.x; cell < ncells; cell += gridDim.x)
     ffblock_cell<C, C::NT, true>(true, Ahi + (size_t)cell * N * N, Alo + (size_t)cell * N * N, bhi + (size_t)cell * N,
-                                 blo + (size_t)cell * N, Minv_h, Minv_l, inv_m[cell], smem, S + (size_t)cell * NF * NF,
+                                 blo + (size_t)cell * N, Minv_h, Minv_l, MG_h, MG_l, coef + 10 * (size_t)cell, smem,
+                                 S + (size_t)cell * NF * NF,
                                  g + (size_t)cell * NF, Xhi ? Xhi + (size_t)cell * NI * NC : nullptr,
                                  Xlo ? Xlo + (size_t)cell * NI * NC : nullptr, info ? info + cell : nullptr,
                                  threadIdx.x);
@@ -43,8 +47,9 @@ __global__ void __launch_bounds__(C::NT, 3)
 
 template <class C>
 static cudaError_t launch_cfg(int ncells, const float *Ahi, const float *Alo, const float *bhi, const float *blo,
-                              const float *Mh, const float *Ml, const double *inv_m, double *S, double *g,
-                              float *Xhi, float *Xlo, int *info, cudaStream_t s, int num_sms) {
+                              const float *Mh, const float *Ml, const float *MGh, const float *MGl,
+                              const double *coef, double *S, double *g, float *Xhi, float *Xlo, int *info,
+                              cudaStream_t s, int num_sms) {
   const size_t smem = C::smem_bytes;
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(condense_ffblock_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -58,8 +63,8 @@ static cudaError_t launch_cfg(int ncells, const float *Ahi, const float *Alo, co
   int grid = num_sms * per_sm;
   if (grid > ncells) grid = ncells;
   if (grid < 1) grid = 1;
-  condense_ffblock_kernel<C><<<grid, C::NT, smem, s>>>(ncells, Ahi, Alo, bhi, blo, Mh, Ml, inv_m, S, g, Xhi, Xlo,
-                                                       info);
+  condense_ffblock_kernel<C><<<grid, C::NT, smem, s>>>(ncells, Ahi, Alo, bhi, blo, Mh, Ml, MGh, MGl, coef, S, g,
+                                                       Xhi, Xlo, info);
   return cudaGetLastError();
 }
 
@@ -70,15 +75,15 @@ bool ffblock_supported(int D, int k) {
 }
 
 cudaError_t launch_condense_ffblock(int D, int k, int ncells, const float *Ahi, const float *Alo, const float *bhi,
-                                    const float *blo, const float *Minv_h, const float *Minv_l,
-                                    const double *inv_m, double *S, double *g, float *Xhi, float *Xlo, int *info,
-                                    cudaStream_t s, int num_sms, long long *launches) {
+                                    const float *blo, const float *Minv_h, const float *Minv_l, const float *MG_h,
+                                    const float *MG_l, const double *coef, double *S, double *g, float *Xhi,
+                                    float *Xlo, int *info, cudaStream_t s, int num_sms, long long *launches) {
   ++*launches;
 #define HDG_FFB(DD, KK)                                                                                   \
   if (D == DD && k == KK)                                                                                 \
     return ffb::launch_cfg<ffb::Cfg<DD, (KK + 1) * (KK + 1) * (DD == 3 ? (KK + 1) : 1),                    \
                                     (DD == 3 ? (KK + 1) * (KK + 1) : (KK + 1))>>(                          \
-        ncells, Ahi, Alo, bhi, blo, Minv_h, Minv_l, inv_m, S, g, Xhi, Xlo, info, s, num_sms);
+        ncells, Ahi, Alo, bhi, blo, Minv_h, Minv_l, MG_h, MG_l, coef, S, g, Xhi, Xlo, info, s, num_sms);
   HDG_FFB(2, 1)
   HDG_FFB(2, 2)
   HDG_FFB(2, 3)
@@ -89,10 +94,11 @@ cudaError_t launch_condense_ffblock(int D, int k, int ncells, const float *Ahi, 
   return cudaErrorInvalidValue;
 }
 
-// 1/m = kappa / |det J| per cell, in FP64 (a handful of FP64 operations per cell)
-__global__ void inv_mass_scale_kernel(CellArgs a, double *inv_m) {
+// per cell: 1/m = kappa / |det J| and the panel coefficients cg[e][d] / m
+// (10 doubles, cell_y_coef), in FP64
+__global__ void inv_mass_scale_kernel(CellArgs a, double *coef) {
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < a.ncells; c += gridDim.x * blockDim.x)
-    inv_m[c] = cell_inv_mass(a, c);
+    cell_y_coef(a, c, coef + 10 * (size_t)c);
 }
 
 cudaError_t launch_inv_mass_scale(const CellArgs &a, double *inv_m, cudaStream_t s, long long *launches) {

@@ -76,7 +76,7 @@ struct Cfg {
   static constexpr size_t smem_floats = 2 * ((size_t)D * NK * NK + NK * NK + (size_t)D * NK * NC + NK * NC);
   // + flags (64 ints) + per local facet the interior columns its trace rows couple to (2D x NI ints, counts)
   static constexpr int NL = 2 * D;
-  static constexpr size_t smem_bytes = smem_floats * 4 + 64 * 4 + ((size_t)NL * NI + 8 + NL * 4) * 4;
+  static constexpr size_t smem_bytes = smem_floats * 4 + 64 * 4 + ((size_t)NL * NI + 8 + NL * 4 + 2 * D * NK) * 4;
 };
 
 // A entry (row r, column c) of the column-major N x N cell matrix (hi, lo) and
@@ -103,8 +103,9 @@ template <class C, int NT, bool RO>
 __device__ __forceinline__ void ffblock_cell(bool active, const float *__restrict__ Ah, const float *__restrict__ Al,
                                              const float *__restrict__ bh, const float *__restrict__ bl,
                                              const float *__restrict__ Minv_h, const float *__restrict__ Minv_l,
-                                             double invm, float *smem, double *Sc, double *gc, float *xh, float *xl,
-                                             int *infoc, int t) {
+                                             const float *__restrict__ MG_h, const float *__restrict__ MG_l,
+                                             const double *coef, float *smem, double *Sc, double *gc, float *xh,
+                                             float *xl, int *infoc, int t) {
   constexpr int D = C::D, NK = C::NK, NU = C::NU, NI = C::NI, NF = C::NF, N = C::N, NC = C::NC;
   float *Yh = smem, *Yl = Yh + D * NK * NK;          // [d][a][b]
   float *Ph = Yl + D * NK * NK, *Pl = Ph + NK * NK;  // [a][b]
@@ -115,6 +116,8 @@ __device__ __forceinline__ void ffblock_cell(bool active, const float *__restric
   int *flist = sflag + 64;                             // [lf][q]: interior rows / columns coupled to facet lf
   int *fcnt = flist + C::NL * NI;                      // [lf]: their count
   int *fseg = fcnt + 8;                                // [lf][d]: start of field d's entries (d <= D)
+  unsigned *ycol = reinterpret_cast<unsigned *>(fseg + C::NL * 4);  // [d][c]: rows a with Y_d[a][c] != 0
+  unsigned *yrow = ycol + D * NK;                                    // [d][a]: columns c with Y_d[a][c] != 0
   constexpr int NFACE = C::NL, NFDc = C::NFD;
   const int lane = t & 31, warp = t >> 5, nwarps = NT >> 5;
   // The interior rows each local facet's trace columns couple to (A_if: its
@@ -146,11 +149,13 @@ __device__ __forceinline__ void ffblock_cell(bool active, const float *__restric
   // warp) or contiguous (consecutive rows of one column).
   float imh, iml;  // 1/m as float-float
   {
-    const double v = invm;
+    const double v = coef[0];
     imh = (float)v;
     iml = (float)(v - (double)imh);
   }
-  // Y_d = (1/m) M^{-1} G_d  and  Z_d = (1/m) M^{-1} R_{u_d}
+  // Y_d = (1/m) M^{-1} G_d = sum_e w_ed MG_e from the reference products
+  // (MG_e = M^{-1} G_e, exactly sparse on the tensor-product cell), and
+  // Z_d = (1/m) M^{-1} R_{u_d}
   for (int e = t; e < NK * NK; e += NT) {
     Ph[e] = __ldg(Minv_h + e);
     Pl[e] = __ldg(Minv_l + e);
@@ -160,9 +165,17 @@ __device__ __forceinline__ void ffblock_cell(bool active, const float *__restric
     const int a = o % NK, rest = o / NK;
     const int c = rest % (NK + NC), d = rest / (NK + NC);
     float h = 0.0f, l = 0.0f;
-    if (c < NK) {  // G_d column c (pressure DOF c)
-      for (int k = 0; k < NK; ++k)
-        mac(h, l, Mh[a * NK + k], Ml[a * NK + k], AH(d * NK + k, NU + c), AL(d * NK + k, NU + c));
+    if (c < NK) {  // Y_d column c (pressure DOF c)
+      for (int e = 0; e < D; ++e) {
+        const double w = coef[1 + 3 * e + d];
+        if (w == 0.0) continue;
+        const float wh = (float)w, wl = (float)(w - (double)wh);
+        mac(h, l, __ldg(MG_h + (e * NK + a) * NK + c), __ldg(MG_l + (e * NK + a) * NK + c), wh, wl);
+      }
+      normalise(h, l);
+      Yh[(d * NK + a) * NK + c] = h;
+      Yl[(d * NK + a) * NK + c] = l;
+      continue;
     } else if (c - NK < NF) {  // skeleton column: only field d's rows coupled to its facet
       const int cc = c - NK, lf = cc / NFDc;
       const int q1 = fseg[lf * 4 + d + 1];
@@ -176,13 +189,17 @@ __device__ __forceinline__ void ffblock_cell(bool active, const float *__restric
     float ph, pl;
     normalise(h, l);
     mul(h, l, imh, iml, ph, pl);
-    if (c < NK) {
-      Yh[(d * NK + a) * NK + c] = ph;
-      Yl[(d * NK + a) * NK + c] = pl;
-    } else {
-      Zh[(d * NK + a) * NC + (c - NK)] = ph;
-      Zl[(d * NK + a) * NC + (c - NK)] = pl;
-    }
+    Zh[(d * NK + a) * NC + (c - NK)] = ph;
+    Zl[(d * NK + a) * NC + (c - NK)] = pl;
+  }
+  __syncthreads();
+  // Y's zero pattern by columns and by rows (NK <= 32: one ballot each)
+  for (int idx = warp; idx < 2 * D * NK; idx += nwarps) {
+    const bool bycol = idx < D * NK;
+    const int dx = bycol ? idx : idx - D * NK, dd = dx / NK, x = dx - dd * NK;
+    const bool nz = lane < NK && (bycol ? Yh[(dd * NK + lane) * NK + x] : Yh[(dd * NK + x) * NK + lane]) != 0.0f;
+    const unsigned bal = __ballot_sync(0xffffffffu, nz);
+    if (lane == 0) (bycol ? ycol : yrow)[dx] = bal;
   }
   __syncthreads();
   // P = T - sum_d G'_d Y_d ;  Q = R_p - sum_d G'_d Z_d
@@ -191,9 +208,11 @@ __device__ __forceinline__ void ffblock_cell(bool active, const float *__restric
     float h = 0.0f, l = 0.0f;
     if (c < NK) {
       for (int d = 0; d < D; ++d)
-        for (int k = 0; k < NK; ++k)
+        for (unsigned m = ycol[d * NK + c]; m; m &= m - 1) {
+          const int k = __ffs(m) - 1;
           mac(h, l, AH(NU + a, d * NK + k), AL(NU + a, d * NK + k), Yh[(d * NK + k) * NK + c],
               Yl[(d * NK + k) * NK + c]);
+        }
       float rh, rl;
       sub(AH(NU + a, NU + c), AL(NU + a, NU + c), h, l, rh, rl);
       Ph[a * NK + c] = rh;
@@ -316,8 +335,10 @@ __device__ __forceinline__ void ffblock_cell(bool active, const float *__restric
   for (int o = t; o < D * NK * NC; o += NT) {
     const int d = o / (NK * NC), rem = o - d * NK * NC, a = rem / NC, c = rem - a * NC;
     float h = 0.0f, l = 0.0f;
-    for (int k = 0; k < NK; ++k)
+    for (unsigned m = yrow[d * NK + a]; m; m &= m - 1) {
+      const int k = __ffs(m) - 1;
       mac(h, l, Yh[(d * NK + a) * NK + k], Yl[(d * NK + a) * NK + k], Qh[k * NC + c], Ql[k * NC + c]);
+    }
     float rh, rl;
     sub(Zh[(d * NK + a) * NC + c], Zl[(d * NK + a) * NC + c], h, l, rh, rl);
     Zh[(d * NK + a) * NC + c] = rh;

@@ -76,6 +76,18 @@ __device__ __forceinline__ void cell_factors(const CellArgs &a, int c, CellFacto
   }
 }
 
+// The Darcy block elimination's per-cell coefficients: w[0] = 1/m =
+// kappa/|det J| and w[1 + 3e + d] = cg[e][d] / m, so that the flux panel
+// Y_d = (1/m) M^{-1} A_{u_d p} = sum_e w[1 + 3e + d] M^{-1} G_e.
+__device__ __forceinline__ void cell_y_coef(const CellArgs &a, int c, double *w) {
+  CellFactors f;
+  cell_factors(a, c, f);
+  const double im = (a.kappa ? a.kappa[c] : 1.0) / f.detJ;
+  w[0] = im;
+  for (int e = 0; e < 3; ++e)
+    for (int d = 0; d < 3; ++d) w[1 + 3 * e + d] = (e < a.D && d < a.D) ? f.cg[e][d] * im : 0.0;
+}
+
 // Row decode: type 0 = flux (sub = component), 1 = pressure, 2 = skeleton (sub = lf)
 __device__ __forceinline__ void decode(int i, int D, int nk, int ni, int nfd,
                                        int &type, int &sub, int &idx) {
