@@ -154,6 +154,61 @@ cudaError_t launch_assemble(const AssembleArgs &a, const double *S, const double
 // replayed; once SC_DONE is set every kernel returns immediately.
 // ---------------------------------------------------------------------------
 // Inverse of each facet's diagonal block of sign*A (Gauss-Jordan, partial pivoting).
+// Facet-block inverses for small blocks (nfd <= NMAX): one thread per skeleton
+// block row, Gauss-Jordan with partial pivoting on [sign*D | I] in registers
+// and local memory; a singular block gets the identity.
+template <int NMAX>
+__global__ void __launch_bounds__(128) binv_thread_kernel(PcgArgs a) {
+  const int nfd = a.nfd;
+  double M[NMAX * NMAX], I[NMAX * NMAX];
+  for (int br = blockIdx.x * blockDim.x + threadIdx.x; br < a.nblockrows; br += gridDim.x * blockDim.x) {
+    const int blk = a.diag_blk[br];
+    const int64_t off = a.blk_off[blk];
+    const int rl = a.blk_rowlen[blk];
+    for (int i = 0; i < nfd; ++i)
+      for (int j = 0; j < nfd; ++j) {
+        M[i * nfd + j] = a.sign * a.val[off + (int64_t)i * rl + j];
+        I[i * nfd + j] = (i == j) ? 1.0 : 0.0;
+      }
+    bool singular = false;
+    for (int c = 0; c < nfd && !singular; ++c) {
+      int pr = c;
+      for (int i = c + 1; i < nfd; ++i)
+        if (fabs(M[i * nfd + c]) > fabs(M[pr * nfd + c])) pr = i;
+      if (!(fabs(M[pr * nfd + c]) > 0.0)) {
+        singular = true;
+        break;
+      }
+      if (pr != c)
+        for (int j = 0; j < nfd; ++j) {
+          double t = M[c * nfd + j];
+          M[c * nfd + j] = M[pr * nfd + j];
+          M[pr * nfd + j] = t;
+          t = I[c * nfd + j];
+          I[c * nfd + j] = I[pr * nfd + j];
+          I[pr * nfd + j] = t;
+        }
+      const double piv = 1.0 / M[c * nfd + c];
+      for (int j = 0; j < nfd; ++j) {
+        M[c * nfd + j] *= piv;
+        I[c * nfd + j] *= piv;
+      }
+      for (int i = 0; i < nfd; ++i) {
+        if (i == c) continue;
+        const double f = M[i * nfd + c];
+        if (f != 0.0)
+          for (int j = 0; j < nfd; ++j) {
+            M[i * nfd + j] -= f * M[c * nfd + j];
+            I[i * nfd + j] -= f * I[c * nfd + j];
+          }
+      }
+    }
+    double *out = a.Binv + (size_t)br * nfd * nfd;
+    for (int i = 0; i < nfd; ++i)
+      for (int j = 0; j < nfd; ++j) out[i * nfd + j] = singular ? (i == j ? 1.0 : 0.0) : I[i * nfd + j];
+  }
+}
+
 // Facet-block inverses of the block-Jacobi preconditioner: one warp per
 // skeleton block row, Gauss-Jordan with partial pivoting on [sign*D | I] in
 // shared memory (lanes over the 2 nfd columns); a singular block gets the
@@ -402,12 +457,18 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_update_kernel(PcgArgs a, cons
 cudaError_t launch_pcg_setup(const PcgArgs &a, double rtol, cudaStream_t s, int num_sms,
                              long long *launches) {
   if (a.nfd > 27) return cudaErrorInvalidValue;
-  int g = (a.nblockrows + kBinvWarps - 1) / kBinvWarps;
-  if (g > num_sms * 16) g = num_sms * 16;
-  if (g < 1) g = 1;
   cudaError_t e = cudaMemsetAsync(a.counter, 0, sizeof(unsigned int), s);
   if (e != cudaSuccess) return e;
-  binv_kernel<<<g, 32 * kBinvWarps, sizeof(double) * kBinvWarps * a.nfd * 2 * a.nfd, s>>>(a);
+  if (a.nfd <= 12) {  // small blocks: one thread per block row
+    int g = (a.nblockrows + 127) / 128;
+    if (g < 1) g = 1;
+    binv_thread_kernel<12><<<g, 128, 0, s>>>(a);
+  } else {
+    int g = (a.nblockrows + kBinvWarps - 1) / kBinvWarps;
+    if (g > num_sms * 16) g = num_sms * 16;
+    if (g < 1) g = 1;
+    binv_kernel<<<g, 32 * kBinvWarps, sizeof(double) * kBinvWarps * a.nfd * 2 * a.nfd, s>>>(a);
+  }
   pcg_init_kernel<<<a.nparts, kPcgThreads, 0, s>>>(a, rtol);
   *launches += 2;
   return cudaGetLastError();
