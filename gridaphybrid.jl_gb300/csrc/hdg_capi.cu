@@ -101,6 +101,7 @@ CellArgs cell_args(hdg_problem *pb) {
   a.qphi = tb + pb->toff.qphi;
   a.origin = pb->d_origin.as<double>();
   a.jac = pb->d_jac.as<double>();
+  a.axis = pb->mesh.axis ? 1 : 0;
   a.kappa = pb->d_kappa.ptr ? pb->d_kappa.as<double>() : nullptr;
   a.cell_facets = pb->d_cell_facets.as<int>();
   a.facet_cell = pb->d_facet_cell.as<int>();
@@ -153,8 +154,13 @@ cudaError_t run_integrate(hdg_problem *pb) {
     return launch_integrate_fp64(a, pb->d_A.as<double>(), pb->d_b.as<double>(), ctx->stream, ctx->num_sms,
                                  &ctx->launches);
   float *Ahi = pb->d_A.as<float>(), *bhi = pb->d_b.as<float>();
+  // FF_BLOCK on the shared-memory elimination: the float-float cell
+  // coefficients go after the panel coefficients (10 doubles per cell)
+  const bool ffb = pb->precision == HDG_PREC_FF_BLOCK;
+  const bool have = ffb && !pb->eblock && pb->d_invm.bytes >= sizeof(double) * 11 * nc + sizeof(float) * 2 * 34 * nc;
+  float2 *coef = have ? reinterpret_cast<float2 *>(pb->d_invm.as<double>() + 10 * nc) : nullptr;
   return launch_integrate_mixed(a, mixed_tables(pb), Ahi, Ahi + nc * n * n, bhi, bhi + nc * n, ctx->stream,
-                                ctx->num_sms, &ctx->launches, pb->precision == HDG_PREC_FF_BLOCK);
+                                ctx->num_sms, &ctx->launches, ffb, coef);
 }
 
 // The L2-panel block elimination's launch description (dry_run: size only).
@@ -384,6 +390,14 @@ int setup_problem(hdg_problem *pb) {
     if ((rc = upload(ctx, pb->d_l2ref_val, vf))) return rc;
   }
   if ((rc = upload(ctx, pb->d_origin, pb->mesh.origin))) return rc;
+  {
+    HostMesh &m = pb->mesh;
+    m.axis = true;
+    for (size_t c = 0; c < (size_t)m.ncells && m.axis; ++c)
+      for (int col = 0; col < m.D; ++col)
+        for (int row = 0; row < m.D; ++row)
+          if (row != col && m.jac[c * m.D * m.D + col * m.D + row] != 0.0) m.axis = false;
+  }
   if ((rc = upload(ctx, pb->d_jac, pb->mesh.jac))) return rc;
   if ((rc = upload(ctx, pb->d_cell_facets, pb->mesh.cell_facets))) return rc;
   if ((rc = upload(ctx, pb->d_facet_dofs, pb->mesh.facet_dofs))) return rc;
@@ -835,7 +849,7 @@ static int assemble_prepare(hdg_problem *pb, int precision, bool cell_blocks, bo
   if (mixed && !cellop_supported(nl, (int)t.nfd))
     return ctx->fail(HDG_ERR_INVALID, "no unassembled FP32 operator for %d facets of %zu DOFs", nl, t.nfd);
   if (precision == HDG_PREC_FF_BLOCK && cell_blocks && !eblock)
-    CUDA_TRY(ctx, pb->d_invm.reserve(sizeof(double) * 10 * nc));
+    CUDA_TRY(ctx, pb->d_invm.reserve(sizeof(double) * 11 * nc + sizeof(float) * 2 * 34 * nc));
   pb->precision = precision;
   pb->eblock = eblock;
   // the L2-panel kernel integrates its cells itself unless the caller needs

@@ -121,6 +121,7 @@ struct HostMesh {
   double domain[2 * kMaxD] = {0, 0, 0, 0, 0, 0};
   std::vector<double> origin;     // ncells x D
   std::vector<double> jac;        // ncells x D x D (column-major per cell)
+  bool axis = false;              // every jac is diagonal
   std::vector<int> cell_facets;   // ncells x 2D
   std::vector<int> facet_dofs;    // nfacets x nfd
   std::vector<int> facet_cell;    // nfacets x 2 : cells around (first = owner), -1

@@ -34,8 +34,12 @@ HDG_HD void exact_solution(int problem, int D, const double *x, double kappa,
   } else {
     double s[3], c[3], prod = 1.0;
     for (int d = 0; d < D; ++d) {
+#ifdef __CUDA_ARCH__
+      sincospi(x[d], &s[d], &c[d]);  // sin(pi x), cos(pi x) without rounding pi x first
+#else
       s[d] = sin(pi * x[d]);
       c[d] = cos(pi * x[d]);
+#endif
       prod *= s[d];
     }
     p = prod;
@@ -147,6 +151,7 @@ struct CellArgs {
   const int *facet_dofs;
   double tau;
   int stab_mode, problem;
+  int axis;  // every cell Jacobian is diagonal (axis-aligned cells)
 };
 
 // FP64 integration of the cell matrices/vectors (column-major n x n, n).
@@ -180,10 +185,13 @@ struct MixedTables {
   const float *Mh, *Ml, *Gh, *Gl, *Fh, *Fl, *Hh, *Hl, *Lh, *Ll;
 };
 // Mixed precision: float-float integration -> (A_hi, A_lo), (b_hi, b_lo)
-// skip_uu: leave the flux-flux block unwritten (block elimination does not read it)
+// skip_uu: leave the flux-flux block unwritten (block elimination does not
+// read it); with coef (34 float2 + 1 double per cell of scratch) and D <= 3, k <= 2 (3D)
+// or k <= 3 (2D) the flux rows' pressure columns are left unwritten as well
+// and the entries are formed by the per-entry kernels
 cudaError_t launch_integrate_mixed(const CellArgs &a, const MixedTables &T, float *Ahi, float *Alo,
                                    float *bhi, float *blo, cudaStream_t s, int num_sms,
-                                   long long *launches, bool skip_uu = false);
+                                   long long *launches, bool skip_uu = false, float2 *coef = nullptr);
 cudaError_t launch_split_fp64(size_t count, const double *x, float *hi, float *lo, cudaStream_t s,
                               int num_sms, long long *launches);
 // FP32 LU + one float-float refinement step; Xhi/Xlo (ncells x ni x (nf+1)) may be null

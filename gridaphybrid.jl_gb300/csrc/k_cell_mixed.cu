@@ -30,10 +30,274 @@ __global__ void __launch_bounds__(256) integrate_mixed_kernel(CellArgs a, MixedT
                       blo + (size_t)c * n, threadIdx.x, blockDim.x, skip_uu);
 }
 
+// ---------------------------------------------------------------------------
+// Darcy integration for the block elimination (HDG_PREC_FF_BLOCK), sizes
+// fixed at compile time.  Every entry of a cell block is a sum of at most
+// D + 2D terms (cell coefficient) x (reference table value), so the entry's
+// decode and its table values are the same for every cell: one thread owns an
+// entry and sweeps a group of cells, reading the cells' coefficients from
+// shared memory.  The flux rows' flux and pressure columns (A_uu, A_up) are
+// not written: the elimination takes A_uu from (|J|/kappa) M_ref and the flux
+// panel from M^{-1} G_e, and reads neither.
+// ---------------------------------------------------------------------------
+constexpr int kFFCoef = 34;  // float-float pairs per cell: m, cg[3][3], cn[6][3], ct[6]
+constexpr int kFFCells = 64;  // cells per entry-kernel CTA
+
+template <int D, int K>
+struct DarcyShape {
+  static constexpr int K1 = K + 1, NK = D == 2 ? K1 * K1 : K1 * K1 * K1, NFD = D == 2 ? K1 : K1 * K1;
+  static constexpr int NL = 2 * D, NU = D * NK, NI = (D + 1) * NK, NF = NL * NFD, N = NI + NF;
+  static constexpr int R0 = N - NU;              // rows written in a column j < NI
+  static constexpr int NE = NI * R0 + NF * N;    // entries written per cell
+};
+
+// per cell: the coefficients of cell_entry_ff as float-float pairs, slots
+// [0] m = |det J|/kappa, [1 + 3e + d] cg[e][d], [10 + 3lf + d] cn[lf][d], [28 + lf] ct[lf]
+__global__ void ff_cell_coef_kernel(CellArgs a, float2 *coef, double *detj) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < a.ncells; c += gridDim.x * blockDim.x) {
+    CellFactorsFF f{};
+    cell_factors_ff(a, c, f);
+    float2 *o = coef + (size_t)c * kFFCoef;
+    detj[c] = f.detJ;
+    o[0] = make_float2(f.cm[0], f.cm[1]);
+    for (int e = 0; e < 3; ++e)
+      for (int d = 0; d < 3; ++d) o[1 + 3 * e + d] = make_float2(f.cg[e][d][0], f.cg[e][d][1]);
+    for (int lf = 0; lf < 6; ++lf) {
+      for (int d = 0; d < 3; ++d) o[10 + 3 * lf + d] = make_float2(f.cn[lf][d][0], f.cn[lf][d][1]);
+      o[28 + lf] = make_float2(f.ct[lf][0], f.ct[lf][1]);
+    }
+  }
+}
+
+// entry = sum over the kept terms t (bit t of keep) of coef[slot_t] *
+// (th_t + tl_t) over the group's cells, in the term order of cell_entry_ff;
+// wkeep (the warp's union of keep) skips the terms no lane keeps
+template <int NT, size_t CS>
+__device__ __forceinline__ void ff_entry_cells(const float2 *cs, int ncg, unsigned keep, unsigned wkeep,
+                                               const int *sl, const float *th, const float *tl, float *ah,
+                                               float *al) {
+#pragma unroll 4
+  for (int cl = 0; cl < ncg; ++cl) {
+    const float2 *cf = cs + cl * kFFCoef;
+    float h = 0.0f, l = 0.0f;
+#pragma unroll
+    for (int t = 0; t < NT; ++t)
+      if ((wkeep >> t) & 1u)
+        if ((keep >> t) & 1u) {
+          const float2 v = cf[sl[t]];
+          ff_mac2(h, l, th[t], tl[t], v.x, v.y);
+        }
+    float s, e;
+    two_sum(h, l, s, e);
+    ah[(size_t)cl * CS] = s;
+    al[(size_t)cl * CS] = e;
+  }
+}
+
+// axis: every cell's Jacobian is diagonal, so cg[e][d] = 0 for e != d and
+// cn[lf][d] = 0 unless d is the axis normal to facet lf; those terms (and
+// terms whose table value is zero) are skipped -- they add exact zeros, as
+// cell_entry_ff's zero-coefficient test does.
+template <int D, int K>
+__global__ void __launch_bounds__(256, 3) integrate_ffentries_kernel(int ncells, MixedTables T, bool axis,
+                                                                  const float2 *__restrict__ coef, float *Ahi,
+                                                                  float *Alo) {
+  using S = DarcyShape<D, K>;
+  constexpr int N = S::N, NK = S::NK, NFD = S::NFD, NU = S::NU, NI = S::NI, NL = S::NL, R0 = S::R0;
+  constexpr size_t CS = (size_t)N * N;
+  __shared__ float2 cs[kFFCells * kFFCoef];
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool active = e < S::NE;
+  int i = 0, j = 0;
+  if (active) {
+    if (e < NI * R0) {
+      j = e / R0;
+      i = NU + (e - j * R0);
+    } else {
+      const int r = e - NI * R0, jf = r / N;
+      j = NI + jf;
+      i = r - jf * N;
+    }
+  }
+  // row / column types: 0 flux (component s, node x), 1 pressure (node x), 2 facet (s, node x)
+  const int ti = i < NU ? 0 : (i < NI ? 1 : 2), tj = j < NU ? 0 : (j < NI ? 1 : 2);
+  const int si = ti == 0 ? i / NK : (ti == 2 ? (i - NI) / NFD : 0);
+  const int ii = ti == 0 ? i - si * NK : (ti == 1 ? i - NU : i - NI - si * NFD);
+  const int sj = tj == 0 ? j / NK : (tj == 2 ? (j - NI) / NFD : 0);
+  const int jj = tj == 0 ? j - sj * NK : (tj == 1 ? j - NU : j - NI - sj * NFD);
+  auto normal_axis = [](int lf) { return D - 1 - lf / 2; };
+  constexpr int NTM = D + NL;
+  int sl[NTM];
+  float th[NTM], tl[NTM];
+  bool keep[NTM];
+#pragma unroll
+  for (int t = 0; t < NTM; ++t) {
+    sl[t] = 0;
+    th[t] = 0.0f;
+    tl[t] = 0.0f;
+    keep[t] = false;
+  }
+  if (active) {
+    int k = -1, slot = 0;
+    const float *Th = nullptr, *Tl = nullptr;
+    bool neg = false, zc = false;
+    if (ti == 1 && tj == 0) {  // G terms, then F terms
+#pragma unroll
+      for (int t = 0; t < D; ++t) {
+        sl[t] = 1 + 3 * t + sj;
+        th[t] = __ldg(T.Gh + (t * NK + ii) * NK + jj);
+        tl[t] = __ldg(T.Gl + (t * NK + ii) * NK + jj);
+        keep[t] = !(axis && t != sj);
+      }
+#pragma unroll
+      for (int lf = 0; lf < NL; ++lf) {
+        sl[D + lf] = 10 + 3 * lf + sj;
+        th[D + lf] = __ldg(T.Fh + (lf * NK + ii) * NK + jj);
+        tl[D + lf] = __ldg(T.Fl + (lf * NK + ii) * NK + jj);
+        keep[D + lf] = !(axis && normal_axis(lf) != sj);
+      }
+    } else if (ti == 1 && tj == 1) {
+#pragma unroll
+      for (int lf = 0; lf < NL; ++lf) {
+        sl[lf] = 28 + lf;
+        th[lf] = __ldg(T.Fh + (lf * NK + ii) * NK + jj);
+        tl[lf] = __ldg(T.Fl + (lf * NK + ii) * NK + jj);
+        keep[lf] = true;
+      }
+    } else if (ti == 0) {  // tj == 2
+      slot = 10 + 3 * sj + si, Th = T.Hh, Tl = T.Hl, k = (sj * NK + ii) * NFD + jj;
+      zc = axis && normal_axis(sj) != si;
+    } else if (ti == 1) {  // tj == 2
+      slot = 28 + sj, Th = T.Hh, Tl = T.Hl, k = (sj * NK + ii) * NFD + jj, neg = true;
+    } else if (tj == 0) {
+      slot = 10 + 3 * si + sj, Th = T.Hh, Tl = T.Hl, k = (si * NK + jj) * NFD + ii;
+      zc = axis && normal_axis(si) != sj;
+    } else if (tj == 1) {
+      slot = 28 + si, Th = T.Hh, Tl = T.Hl, k = (si * NK + jj) * NFD + ii;
+    } else if (si == sj) {
+      slot = 28 + si, Th = T.Lh, Tl = T.Ll, k = ii * NFD + jj, neg = true;
+    }
+    if (k >= 0 && !zc) {
+      const float h = __ldg(Th + k), l = __ldg(Tl + k);
+      sl[0] = slot;
+      th[0] = neg ? -h : h;
+      tl[0] = neg ? -l : l;
+      keep[0] = true;
+    }
+  }
+  unsigned km = 0;
+#pragma unroll
+  for (int t = 0; t < NTM; ++t)
+    if (keep[t] && (th[t] != 0.0f || tl[t] != 0.0f)) km |= 1u << t;
+  const unsigned wkm = __reduce_or_sync(0xffffffffu, km);
+  const int ngroups = (ncells + kFFCells - 1) / kFFCells;
+  for (int grp = blockIdx.y; grp < ngroups; grp += gridDim.y) {
+    const int c0 = grp * kFFCells, ncg = min(kFFCells, ncells - c0);
+    __syncthreads();
+    for (int o = threadIdx.x; o < ncg * kFFCoef; o += blockDim.x) cs[o] = coef[(size_t)c0 * kFFCoef + o];
+    __syncthreads();
+    if (!active) continue;
+    float *ah = Ahi + (size_t)c0 * CS + (size_t)j * N + i, *al = Alo + (size_t)c0 * CS + (size_t)j * N + i;
+    if (wkm == 0)
+      for (int cl = 0; cl < ncg; ++cl) {
+        ah[(size_t)cl * CS] = 0.0f;
+        al[(size_t)cl * CS] = 0.0f;
+      }
+    else
+      ff_entry_cells<NTM, CS>(cs, ncg, km, wkm, sl, th, tl, ah, al);
+  }
+}
+
+// b = [int f_u . v ; int g w ; 0] per cell: one warp per cell, in FP64 and
+// in the operation order of integrate_cell_ff (the batched assembly gives
+// the same bits).  |det J| comes from ff_cell_coef_kernel.
+template <int D, int K>
+__global__ void __launch_bounds__(256) ff_cell_rhs_kernel(CellArgs a, const double *__restrict__ detj, float *bhi,
+                                                          float *blo) {
+  using S = DarcyShape<D, K>;
+  constexpr int NK = S::NK, NU = S::NU, NI = S::NI, N = S::N, NW = 8;
+  extern __shared__ double rs[];
+  const int nq = a.nqv, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  double *phi = rs, *fq = phi + nq * NK + warp * nq * (D + 1);
+  for (int o = threadIdx.x; o < nq * NK; o += blockDim.x) phi[o] = a.qphi[o];
+  __syncthreads();
+  for (int c = blockIdx.x * NW + warp; c < a.ncells; c += gridDim.x * NW) {
+    double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, x0[3] = {0, 0, 0};
+    for (int col = 0; col < D; ++col) {
+      x0[col] = a.origin[(size_t)c * D + col];
+      for (int row = 0; row < D; ++row) J[row][col] = a.jac[(size_t)c * D * D + col * D + row];
+    }
+    const double adet = detj[c], kap = a.kappa ? a.kappa[c] : 1.0;
+    for (int q = lane; q < nq; q += 32) {
+      double x[3], p, qe[3], fu[3], g;
+      for (int d = 0; d < D; ++d) {
+        x[d] = x0[d];
+        for (int e = 0; e < D; ++e) x[d] += J[d][e] * a.qxi[q * D + e];
+      }
+      exact_solution(a.problem, D, x, kap, p, qe, fu, g);
+      const double w = a.qw[q] * adet;
+      for (int d = 0; d < D; ++d) fq[q * (D + 1) + d] = w * fu[d];
+      fq[q * (D + 1) + D] = w * g;
+    }
+    __syncwarp();
+    for (int i = lane; i < N; i += 32) {
+      double v = 0.0;
+      if (i < NI) {
+        const int comp = i < NU ? i / NK : D, ii = i < NU ? i - comp * NK : i - NU;
+        for (int q = 0; q < nq; ++q) v += fq[q * (D + 1) + comp] * phi[q * NK + ii];
+      }
+      float h, l;
+      split_double(v, h, l);
+      bhi[(size_t)c * N + i] = h;
+      blo[(size_t)c * N + i] = l;
+    }
+    __syncwarp();
+  }
+}
+
+template <int D, int K>
+static cudaError_t launch_integrate_ffblock(const CellArgs &a, const MixedTables &T, float *Ahi, float *Alo,
+                                            float *bhi, float *blo, float2 *coef, cudaStream_t s, int num_sms,
+                                            long long *launches) {
+  using S = DarcyShape<D, K>;
+  double *detj = reinterpret_cast<double *>(coef + (size_t)kFFCoef * a.ncells);
+  int g0 = (a.ncells + 255) / 256;
+  if (g0 > 8 * num_sms) g0 = 8 * num_sms;
+  if (g0 < 1) g0 = 1;
+  ff_cell_coef_kernel<<<g0, 256, 0, s>>>(a, coef, detj);
+  ++*launches;
+  const size_t rsmem = sizeof(double) * ((size_t)a.nqv * S::NK + 8 * (size_t)a.nqv * (D + 1));
+  if (rsmem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(ff_cell_rhs_kernel<D, K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)rsmem);
+    if (e != cudaSuccess) return e;
+  }
+  int g1 = (a.ncells + 7) / 8;
+  if (g1 > 4 * num_sms) g1 = 4 * num_sms;
+  if (g1 < 1) g1 = 1;
+  ff_cell_rhs_kernel<D, K><<<g1, 256, rsmem, s>>>(a, detj, bhi, blo);
+  ++*launches;
+  const int ngroups = (a.ncells + kFFCells - 1) / kFFCells;
+  dim3 grid((S::NE + 255) / 256, ngroups < 65535 ? ngroups : 65535);
+  integrate_ffentries_kernel<D, K><<<grid, 256, 0, s>>>(a.ncells, T, a.axis != 0, coef, Ahi, Alo);
+  ++*launches;
+  return cudaGetLastError();
+}
+
 cudaError_t launch_integrate_mixed(const CellArgs &a, const MixedTables &T, float *Ahi, float *Alo, float *bhi,
-                                   float *blo, cudaStream_t s, int num_sms, long long *launches, bool skip_uu) {
+                                   float *blo, cudaStream_t s, int num_sms, long long *launches, bool skip_uu,
+                                   float2 *coef) {
   if (a.nqv > 512) return cudaErrorInvalidValue;
   int grid = a.ncells < num_sms * 8 ? a.ncells : num_sms * 8;
+#define HDG_IFB(DD, KK)                                                                                     \
+  if (skip_uu && coef && a.D == DD && a.k == KK)                                                            \
+    return launch_integrate_ffblock<DD, KK>(a, T, Ahi, Alo, bhi, blo, coef, s, num_sms, launches);
+  HDG_IFB(2, 1)
+  HDG_IFB(2, 2)
+  HDG_IFB(2, 3)
+  HDG_IFB(3, 1)
+  HDG_IFB(3, 2)
+#undef HDG_IFB
   integrate_mixed_kernel<<<grid, 256, 0, s>>>(a, T, Ahi, Alo, bhi, blo, skip_uu);
   ++*launches;
   return cudaGetLastError();
