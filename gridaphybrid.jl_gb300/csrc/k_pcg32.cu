@@ -221,13 +221,13 @@ struct CellOp {
 // keeps `nstage` stages of cell records in flight with bulk copies (L2
 // evict-first: the records are read once per iteration, the vectors stay).
 template <int NL, int NFD>
-__global__ void __launch_bounds__(CellOp<NL, NFD>::THREADS)
+__global__ void __launch_bounds__(CellOp<NL, NFD>::THREADS, 2)
     cell_spmv32_kernel(Pcg32Args a, const float *__restrict__ p_old, float *__restrict__ p_new) {
   using C = CellOp<NL, NFD>;
   extern __shared__ __align__(128) float ring[];
   __shared__ __align__(8) uint64_t bars[kMaxBulkStages];
   __shared__ __align__(16) float ps[C::CPS][C::TPC];
-  __shared__ double red[32];
+  __shared__ float2 redf[32];
   __shared__ int abort_flag;
   if (a.scal[SC_DONE] != 0.0) return;
   const float beta = (float)a.scal[SC_BETA];
@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(CellOp<NL, NFD>::THREADS)
     for (; issued < min(nstage, mine); ++issued) issue(issued);
   }
   __syncthreads();
-  double acc = 0.0;
+  FFSum acc;  // (p, qc) over this thread's rows, float-float
   // The gather of p = z + beta p_old is pipelined across stages: the block-row
   // entry of stage t+2 and the p_old / z values of stage t+1 are loaded while
   // stage t is computed (two dependent loads, each hidden behind one stage).
@@ -338,7 +338,7 @@ __global__ void __launch_bounds__(CellOp<NL, NFD>::THREADS)
         }
       }
       a.qc[(size_t)c * C::NF + i] = q;
-      acc += (double)pv * q;
+      acc.add_prod(pv, q);
     }
     __syncthreads();  // the slot and ps are free again
     if (threadIdx.x == 0 && issued < mine) {
@@ -347,10 +347,10 @@ __global__ void __launch_bounds__(CellOp<NL, NFD>::THREADS)
       ++issued;
     }
   }
-  const double tsum = block_sum(acc, red);
-  if (threadIdx.x == 0) a.partials[blockIdx.x] = tsum;
+  const float2 tsum = block_sum_ff(acc.hi, acc.lo, redf);
+  if (threadIdx.x == 0) store_partial_ff(a.partials, (int)gridDim.x, 0, tsum);
   if (last_cta(a.counter)) {
-    const double pq = sum_partials(a.partials, (int)gridDim.x, 0, red);
+    const double pq = sum_partials_ff(a.partials, (int)gridDim.x, 0, redf);
     if (threadIdx.x == 0) {
       a.scal[SC_PAP] = pq;
       a.scal[SC_ALPHA] = a.scal[SC_RZ] / pq;
@@ -383,14 +383,14 @@ __global__ void __launch_bounds__(kPcgThreads) pcg32_update_cells_kernel(Pcg32Ar
   constexpr int BPT = kPcgThreads / NFD;  // block rows per tile
   __shared__ float rs[kPcgThreads];
   __shared__ float Bs[BPT * NFD * NFD];
-  __shared__ double red[32];
+  __shared__ float2 redf[32];
   if (a.scal[SC_DONE] != 0.0) return;
   const float alpha = (float)a.scal[SC_ALPHA];
   const int lb = threadIdx.x / NFD, i = threadIdx.x - lb * NFD;
   const float *__restrict__ qc = a.qc;
   float *__restrict__ xg = a.x;
   float *__restrict__ rg = a.r;
-  double rz = 0.0, rr = 0.0;
+  FFSum rz, rr;  // float-float: no FP64 in the per-row or per-CTA sums
   for (int br0 = blockIdx.x * BPT; br0 < a.nblockrows; br0 += gridDim.x * BPT) {
     const int nb = min(BPT, a.nblockrows - br0);
     const bool act = lb < nb;
@@ -413,7 +413,7 @@ __global__ void __launch_bounds__(kPcgThreads) pcg32_update_cells_kernel(Pcg32Ar
       xg[row] = fmaf(alpha, pv, xv);
       rv = fmaf(-alpha, q, r0);
       rg[row] = rv;
-      rr += (double)rv * rv;
+      rr.add_prod(rv, rv);
     }
     rs[threadIdx.x] = rv;
     cp_async_commit_wait_all();
@@ -425,18 +425,18 @@ __global__ void __launch_bounds__(kPcgThreads) pcg32_update_cells_kernel(Pcg32Ar
 #pragma unroll
       for (int j = 0; j < NFD; ++j) z = fmaf(B[j], rl[j], z);
       a.z[row] = z;
-      rz += (double)rv * z;
+      rz.add_prod(rv, z);
     }
     __syncthreads();
   }
   const int np = (int)gridDim.x;
-  double s = block_sum(rz, red);
-  if (threadIdx.x == 0) a.partials[blockIdx.x] = s;
-  s = block_sum(rr, red);
-  if (threadIdx.x == 0) a.partials[np + blockIdx.x] = s;
+  float2 s = block_sum_ff(rz.hi, rz.lo, redf);
+  if (threadIdx.x == 0) store_partial_ff(a.partials, np, 0, s);
+  s = block_sum_ff(rr.hi, rr.lo, redf);
+  if (threadIdx.x == 0) store_partial_ff(a.partials, np, 1, s);
   if (last_cta(a.counter)) {
-    const double vrz = sum_partials(a.partials, np, 0, red);
-    const double vrr = sum_partials(a.partials, np, 1, red);
+    const double vrz = sum_partials_ff(a.partials, np, 0, redf);
+    const double vrr = sum_partials_ff(a.partials, np, 1, redf);
     if (threadIdx.x == 0) {
       a.scal[SC_BETA] = vrz / a.scal[SC_RZ];
       a.scal[SC_RZ] = vrz;

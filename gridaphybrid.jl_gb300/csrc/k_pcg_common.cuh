@@ -50,6 +50,72 @@ __device__ __forceinline__ double sum_partials(const double *partials, int npart
   return block_sum(s, red);
 }
 
+// ---------------------------------------------------------------------------
+// Dot products on the FP32 pipes.  GB300 issues FP64 at a small fraction of
+// its FP32 rate, and reductions that every CTA runs at the same moment (the
+// end of a one-wave launch) serialise on that pipe; float-float pairs
+// (unevaluated hi + lo, ~48 significant bits) carry the same sums on the
+// FP32 pipes.  FP64 remains for the final scalars only.
+// ---------------------------------------------------------------------------
+// (ah, al) += (bh, bl): Knuth two-sum of the high parts, then renormalised
+__device__ __forceinline__ void ff_add(float &ah, float &al, float bh, float bl) {
+  const float s = ah + bh;
+  const float bb = s - ah;
+  float e = (ah - (s - bb)) + (bh - bb);
+  e += al + bl;
+  ah = s + e;
+  al = e - (ah - s);
+}
+
+// running sum of FP32 products: fma gives each product's rounding error exactly
+struct FFSum {
+  float hi = 0.0f, lo = 0.0f;
+  __device__ __forceinline__ void add_prod(float a, float b) {
+    const float p = a * b;
+    const float pe = fmaf(a, b, -p);
+    const float s = hi + p;
+    const float bb = s - hi;
+    const float e = (hi - (s - bb)) + (p - bb);
+    hi = s;
+    lo += e + pe;
+  }
+};
+
+// block sum of float-float pairs, in a fixed order; valid in thread 0
+__device__ __forceinline__ float2 block_sum_ff(float hi, float lo, float2 *redf) {
+  for (int off = 16; off > 0; off >>= 1) {
+    const float bh = __shfl_down_sync(0xffffffffu, hi, off), bl = __shfl_down_sync(0xffffffffu, lo, off);
+    ff_add(hi, lo, bh, bl);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) redf[w] = make_float2(hi, lo);
+  __syncthreads();
+  float2 s = make_float2(0.0f, 0.0f);
+  if (threadIdx.x == 0)
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) ff_add(s.x, s.y, redf[i].x, redf[i].y);
+  return s;
+}
+
+// A CTA's float-float partial k, stored as a float2 in the double-sized slot
+// k*nparts + blockIdx.x of the partials array.
+__device__ __forceinline__ void store_partial_ff(double *partials, int nparts, int k, float2 v) {
+  reinterpret_cast<float2 *>(partials)[(size_t)k * nparts + blockIdx.x] = v;
+}
+
+// sum of the float-float partials k*nparts + 0..nparts in a fixed order (the
+// last CTA), returned in FP64; valid in thread 0
+__device__ __forceinline__ double sum_partials_ff(const double *partials, int nparts, int k, float2 *redf) {
+  const float2 *p = reinterpret_cast<const float2 *>(partials) + (size_t)k * nparts;
+  float hi = 0.0f, lo = 0.0f;
+  for (int i = threadIdx.x; i < nparts; i += blockDim.x) {
+    const float2 v = __ldcg(p + i);
+    ff_add(hi, lo, v.x, v.y);
+  }
+  const float2 s = block_sum_ff(hi, lo, redf);
+  return (double)s.x + (double)s.y;
+}
+
 template <int N>
 struct Pow2Ceil {
   static constexpr int v = N <= 1 ? 1 : N <= 2 ? 2 : N <= 4 ? 4 : N <= 8 ? 8 : N <= 16 ? 16 : 32;
