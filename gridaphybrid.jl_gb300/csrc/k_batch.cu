@@ -38,11 +38,77 @@ __device__ __forceinline__ int find_problem(const BatchProblem *probs, int nprob
 
 __host__ __device__ constexpr size_t align16(size_t b) { return (b + 15) / 16 * 16; }
 
+// integrate_cell_ff with the class's sizes fixed at compile time (constant
+// divisors in the row decode) and only the entries the block elimination
+// reads: the flux rows' flux and pressure columns are skipped.  Each entry
+// and b come from the same cell_entry_ff / source loop, so the values equal
+// the single-problem kernels' bit for bit.
+template <class C>
+__device__ __forceinline__ void integrate_cell_ffc(const CellArgs &a, const MixedTables &T, int c, bool active,
+                                                   CellFactorsFF &f, double *fq, float *Ah, float *Al, float *bh,
+                                                   float *bl, int t, int nt) {
+  constexpr int D = C::D, NK = C::NK, NFD = C::NFD, NU = C::NU, NI = C::NI, N = C::N;
+  constexpr int R0 = N - NU, NE = NI * R0 + (N - NI) * N;  // written entries
+  if (t == 0 && active) cell_factors_ff(a, c, f);
+  __syncthreads();
+  if (active) {
+    const double kap = a.kappa ? a.kappa[c] : 1.0;
+    for (int q = t; q < a.nqv; q += nt) {
+      double x[3], p, qe[3], fu[3], g;
+      for (int d = 0; d < D; ++d) {
+        x[d] = f.x0[d];
+        for (int e = 0; e < D; ++e) x[d] += f.J[d][e] * a.qxi[q * D + e];
+      }
+      exact_solution(a.problem, D, x, kap, p, qe, fu, g);
+      const double w = a.qw[q] * f.detJ;
+      for (int d = 0; d < D; ++d) fq[q * (D + 1) + d] = w * fu[d];
+      fq[q * (D + 1) + D] = w * g;
+    }
+  }
+  __syncthreads();
+  if (active) {
+    for (int e = t; e < NE; e += nt) {
+      int i, j;
+      if (e < NI * R0) {
+        j = e / R0;
+        i = NU + (e - j * R0);
+      } else {
+        const int r = e - NI * R0, jf = r / N;
+        j = NI + jf;
+        i = r - jf * N;
+      }
+      int ti, si, ii, tj, sj, jj;
+      decode_row(i, D, NK, NI, NFD, ti, si, ii);
+      decode_row(j, D, NK, NI, NFD, tj, sj, jj);
+      float h, l;
+      cell_entry_ff(a, T, f, ti, si, ii, tj, sj, jj, h, l);
+      Ah[j * N + i] = h;
+      Al[j * N + i] = l;
+    }
+    for (int i = t; i < N; i += nt) {
+      int ti, si, ii;
+      decode_row(i, D, NK, NI, NFD, ti, si, ii);
+      double v = 0.0;
+      if (ti < 2) {
+        const int comp = ti == 0 ? si : D;
+        for (int q = 0; q < a.nqv; ++q) v += fq[q * (D + 1) + comp] * a.qphi[q * NK + ii];
+      }
+      float h, l;
+      split_double(v, h, l);
+      bh[i] = h;
+      bl[i] = l;
+    }
+  }
+  __syncthreads();
+}
+
 template <class C>
 struct FfbLayout {
   static constexpr size_t ffb = align16(C::smem_bytes);
   static constexpr size_t fac = align16(sizeof(CellFactorsFF));
-  static constexpr size_t group(int nqv) { return ffb + fac + align16((size_t)nqv * (C::D + 1) * sizeof(double)); }
+  static constexpr size_t fqb(int nqv) { return align16((size_t)nqv * (C::D + 1) * sizeof(double)); }
+  // + the cell's 10 panel coefficients (cell_y_coef)
+  static constexpr size_t group(int nqv) { return ffb + fac + fqb(nqv) + align16(10 * sizeof(double)); }
   static constexpr size_t slot_floats = 2 * ((size_t)C::N * C::N + C::N);
 };
 
@@ -58,6 +124,7 @@ __global__ void __launch_bounds__(kBatchThreads) fused_ffblock_kernel(const Batc
   float *fsm = reinterpret_cast<float *>(base);
   CellFactorsFF &f = *reinterpret_cast<CellFactorsFF *>(base + L::ffb);
   double *fq = reinterpret_cast<double *>(base + L::ffb + L::fac);
+  double *coef = reinterpret_cast<double *>(base + group_bytes - align16(10 * sizeof(double)));
   float *Ah = scratch + ((size_t)blockIdx.x * CPC + grp) * L::slot_floats;
   float *Al = Ah + (size_t)N * N, *bh = Al + (size_t)N * N, *bl = bh + N;
   const long long per_wave = (long long)gridDim.x * CPC;
@@ -68,9 +135,19 @@ __global__ void __launch_bounds__(kBatchThreads) fused_ffblock_kernel(const Batc
     const int p = active ? find_problem(probs, nprob, item) : 0;
     const BatchProblem &P = probs[p];
     const int c = active ? (int)(item - P.first) : 0;
-    integrate_cell_ff(P.a, P.T, c, active, f, fq, Ah, Al, bh, bl, t, TPC, true);
-    double coef[10] = {1.0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-    if (active) cell_y_coef(P.a, c, coef);
+    // the cell's panel coefficients, once per cell (FP64 divisions: one
+    // thread, not the whole group); integrate_cell_ffc's first barrier
+    // publishes them, the barrier here retires the previous cell's readers
+    __syncthreads();
+    if (t == 0) {
+      if (active) {
+        cell_y_coef(P.a, c, coef);
+      } else {
+        coef[0] = 1.0;
+        for (int q = 1; q < 10; ++q) coef[q] = 0.0;
+      }
+    }
+    integrate_cell_ffc<C>(P.a, P.T, c, active, f, fq, Ah, Al, bh, bl, t, TPC);
     int *infoc = active ? P.info + c : nullptr;
     ffb::ffblock_cell<C, TPC, false>(active, Ah, Al, bh, bl, P.Mh, P.Ml, P.MGh, P.MGl, coef, fsm,
                                      P.S + (size_t)c * NF * NF,
