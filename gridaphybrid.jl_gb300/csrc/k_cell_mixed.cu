@@ -203,6 +203,8 @@ __global__ void __launch_bounds__(256, 3) integrate_ffentries_kernel(int ncells,
         ah[(size_t)cl * CS] = 0.0f;
         al[(size_t)cl * CS] = 0.0f;
       }
+    else if (wkm == 1u)  // single-term entries (the facet couplings): no per-term tests
+      ff_entry_cells<1, CS>(cs, ncg, km, wkm, sl, th, tl, ah, al);
     else
       ff_entry_cells<NTM, CS>(cs, ncg, km, wkm, sl, th, tl, ah, al);
   }
