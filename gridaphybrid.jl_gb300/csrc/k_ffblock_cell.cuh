@@ -113,6 +113,9 @@ __device__ __forceinline__ void ffblock_cell(bool active, const float *__restric
   float *Qh = Zl + D * NK * NC, *Ql = Qh + NK * NC;  // [a][c]
   const float *Mh = Ph, *Ml = Pl;                      // M^{-1} [a][k], until P is formed
   int *sflag = reinterpret_cast<int *>(Ql + NK * NC);  // [0] pivot row, [1] info
+  // [32..49]: the panel coefficients coef[1 + 3e + d] as float-float pairs,
+  // split once per cell (FP64 is a narrow pipe on GB300)
+  float *wsp = reinterpret_cast<float *>(sflag + 32);
   int *flist = sflag + 64;                             // [lf][q]: interior rows / columns coupled to facet lf
   int *fcnt = flist + C::NL * NI;                      // [lf]: their count
   int *fseg = fcnt + 8;                                // [lf][d]: start of field d's entries (d <= D)
@@ -160,6 +163,12 @@ __device__ __forceinline__ void ffblock_cell(bool active, const float *__restric
     Ph[e] = __ldg(Minv_h + e);
     Pl[e] = __ldg(Minv_l + e);
   }
+  if (t < 9) {
+    const double w = coef[1 + t];
+    const float wh = (float)w;
+    wsp[2 * t] = wh;
+    wsp[2 * t + 1] = (float)(w - (double)wh);
+  }
   __syncthreads();
   for (int o = t; o < D * NK * (NK + NC); o += NT) {
     const int a = o % NK, rest = o / NK;
@@ -167,9 +176,8 @@ __device__ __forceinline__ void ffblock_cell(bool active, const float *__restric
     float h = 0.0f, l = 0.0f;
     if (c < NK) {  // Y_d column c (pressure DOF c)
       for (int e = 0; e < D; ++e) {
-        const double w = coef[1 + 3 * e + d];
-        if (w == 0.0) continue;
-        const float wh = (float)w, wl = (float)(w - (double)wh);
+        const float wh = wsp[2 * (3 * e + d)], wl = wsp[2 * (3 * e + d) + 1];
+        if (wh == 0.0f && wl == 0.0f) continue;
         mac(h, l, __ldg(MG_h + (e * NK + a) * NK + c), __ldg(MG_l + (e * NK + a) * NK + c), wh, wl);
       }
       normalise(h, l);
@@ -376,9 +384,12 @@ __device__ __forceinline__ void ffblock_cell(bool active, const float *__restric
       else
         mac(h, l, AH(NI + f, k), AL(NI + f, k), Qh[(k - NU) * NC + c], Ql[(k - NU) * NC + c]);
     }
-    const double rhs = c < NF ? (double)AH(NI + f, NI + c) + (double)AL(NI + f, NI + c)
-                              : (double)LDB(bh, NI + f) + (double)LDB(bl, NI + f);
-    const double v = rhs - ((double)h + (double)l);
+    // the difference in float-float, one conversion to FP64
+    const float rh = c < NF ? AH(NI + f, NI + c) : LDB(bh, NI + f);
+    const float rl = c < NF ? AL(NI + f, NI + c) : LDB(bl, NI + f);
+    float vh, vl;
+    sub(rh, rl, h, l, vh, vl);
+    const double v = (double)vh + (double)vl;
     if (!active) continue;
     if (c < NF)
       Sc[f + (size_t)NF * c] = v;
