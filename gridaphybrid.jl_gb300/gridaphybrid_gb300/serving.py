@@ -140,6 +140,7 @@ def run_trace(server, trace, precision, rtol=1e-10, max_seconds=None, rejected=N
     a list is given, and re-raised otherwise."""
     t0 = time.perf_counter()
     resp = []
+    requests = {}  # ticket -> (D, n, k, kappa seed)
     pending = 0
     for (ta, D, n, k, ks) in trace:
         if max_seconds is not None and ta > max_seconds:
@@ -151,12 +152,13 @@ def run_trace(server, trace, precision, rtol=1e-10, max_seconds=None, rejected=N
             resp += server.poll(timeout_ms=0.0)
             time.sleep(min(ta - now, 0.002))
         try:
-            server.submit(D, n, k, kappa=kappa_for(D, n, ks), precision=precision, rtol=rtol)
+            ticket = server.submit(D, n, k, kappa=kappa_for(D, n, ks), precision=precision, rtol=rtol)
         except _lib.HdgError as e:
             if rejected is None:
                 raise
             rejected.append((D, n, k, str(e)))
             continue
+        requests[ticket] = (D, n, k, ks)
         pending += 1
     server.drain()
     resp += server.poll(timeout_ms=0.0, max_items=max(256, pending))
@@ -165,14 +167,19 @@ def run_trace(server, trace, precision, rtol=1e-10, max_seconds=None, rejected=N
         if not got:
             break
         resp += got
+    for r in resp:
+        r["request"] = requests.get(r["ticket"])
     return resp, time.perf_counter() - t0
 
 
 def latency_summary(resp, wall_s):
     lat = np.array([r["latency_ms"] for r in resp if r["status"] == 0])
     ok = int(lat.size)
+    # each failed request: its shape and kappa seed (to replay it), the status and where the solve stopped
+    failures = [{"request": r.get("request"), "status": int(r["status"]), "iters": int(r["iters"]),
+                 "relres": float(r["relres"])} for r in resp if r["status"] != 0][:20]
     if ok == 0:
-        return {"completed": 0, "failed": len(resp)}
+        return {"completed": 0, "failed": len(resp), "failures": failures}
     cells = sum(r["shape"][1] ** r["shape"][0] for r in resp if r["status"] == 0)
     return {
         "completed": ok, "failed": len(resp) - ok,
@@ -183,6 +190,7 @@ def latency_summary(resp, wall_s):
         "queue_p50_ms": float(np.percentile([r["queue_ms"] for r in resp if r["status"] == 0], 50)),
         "run_p50_ms": float(np.percentile([r["run_ms"] for r in resp if r["status"] == 0], 50)),
         "by_class": _by_class(resp),
+        "failures": failures,
     }
 
 
