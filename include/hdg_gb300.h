@@ -252,7 +252,7 @@ int hdg_set_elasticity(hdg_problem *pb, double tau, double young, int problem);
 /* Options of the fast precisions' skeleton solve (an FP32 PCG inside FP64
  * residual refinement; no reference counterpart).  delta: the relative
  * residual reduction the FP32 iterations make between two FP64 residuals
- * (default 3e-2); keep_direction: 1 (default) replaces the FP32 residual by
+ * (default 1e-2 for D = 3, 3e-2 for D = 2); keep_direction: 1 (default) replaces the FP32 residual by
  * the FP64 one and keeps the search direction (reliable updates), 0 restarts
  * the FP32 PCG at every FP64 residual. */
 int hdg_set_refinement(hdg_problem *pb, double delta, int keep_direction);
