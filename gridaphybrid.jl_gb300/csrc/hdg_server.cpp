@@ -309,6 +309,10 @@ struct hdg_server {
       int rc = run(job, res, r);
       const Clock::time_point t_end = Clock::now();
       r.status = rc;
+      if (rc != HDG_OK && res && res->ctx) {  // before a failed request's mesh (and context) goes
+        std::strncpy(r.message, hdg_last_error(res->ctx), sizeof(r.message) - 1);
+        r.message[sizeof(r.message) - 1] = '\0';
+      }
       r.run_ms = ms_between(t_start, t_end);
       r.latency_ms = ms_between(job.t_submit, t_end);
       {

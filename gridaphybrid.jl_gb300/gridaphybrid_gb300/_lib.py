@@ -110,7 +110,7 @@ class Response(ctypes.Structure):
     """struct hdg_response."""
     _fields_ = [("ticket", _ll), ("status", _i), ("iters", _i), ("relres", _d), ("err_flux", _d),
                 ("err_pressure", _d), ("queue_ms", _d), ("run_ms", _d), ("latency_ms", _d),
-                ("footprint_bytes", _d), ("reused_mesh", _i), ("slot", _i)]
+                ("footprint_bytes", _d), ("reused_mesh", _i), ("slot", _i), ("message", ctypes.c_char * 160)]
 
 
 class HdgError(RuntimeError):

@@ -177,7 +177,9 @@ def latency_summary(resp, wall_s):
     ok = int(lat.size)
     # each failed request: its shape and kappa seed (to replay it), the status and where the solve stopped
     failures = [{"request": r.get("request"), "status": int(r["status"]), "iters": int(r["iters"]),
-                 "relres": float(r["relres"])} for r in resp if r["status"] != 0][:20]
+                 "relres": float(r["relres"]),
+                 "message": r["message"].decode(errors="replace") if isinstance(r.get("message"), bytes) else ""}
+                for r in resp if r["status"] != 0][:20]
     if ok == 0:
         return {"completed": 0, "failed": len(resp), "failures": failures}
     cells = sum(r["shape"][1] ** r["shape"][0] for r in resp if r["status"] == 0)

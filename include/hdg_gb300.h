@@ -380,6 +380,7 @@ typedef struct hdg_response {
   double footprint_bytes;/* reserved at admission */
   int reused_mesh;       /* 1 if the mesh was already resident */
   int slot;              /* worker that ran it */
+  char message[160];     /* the failing call's hdg_last_error text ("" on success) */
 } hdg_response;
 
 /* Upper bound of the device bytes one request of this shape needs. */
