@@ -62,3 +62,29 @@ def test_batching_workload_is_seeded():
     assert all(x["n"] == y["n"] and x["k"] == y["k"] and np.array_equal(x["kappa"], y["kappa"]) for x, y in zip(a, b))
     assert {x["k"] for x in a} == {1, 2, 3} and all(16 <= x["n"] <= 128 for x in a)
     assert abs(np.log(a[0]["kappa"]).std() - 1.5) < 0.3
+
+
+def _resp(ticket, status, shape, request, message=b""):
+    return {"ticket": ticket, "status": status, "iters": 7, "relres": 1e-3, "latency_ms": 10.0 + ticket,
+            "queue_ms": 1.0, "run_ms": 9.0, "reused_mesh": 0, "shape": shape, "request": request,
+            "message": message}
+
+
+def test_latency_summary_lists_failures_with_their_requests():
+    resp = [_resp(i, 0, (2, 8, 1), (2, 8, 1, i)) for i in range(9)]
+    resp.append(_resp(9, _lib.HDG_ERR_NOT_CONVERGED, (2, 16, 3), (2, 16, 3, 42), b"refined PCG: stalled"))
+    s = serving.latency_summary(resp, wall_s=1.0)
+    assert s["completed"] == 9 and s["failed"] == 1
+    (f,) = s["failures"]
+    assert f["request"] == (2, 16, 3, 42)
+    assert f["status"] == _lib.HDG_ERR_NOT_CONVERGED and f["iters"] == 7
+    assert f["message"] == "refined PCG: stalled"
+    # a failed request counts in no latency figure
+    assert s["max_ms"] == 18.0
+
+
+def test_response_struct_matches_the_c_layout():
+    """hdg_response: an 8-byte ticket, two ints, seven doubles, two ints, then the 160-byte message."""
+    fields = dict(_lib.Response._fields_)
+    assert "message" in fields
+    assert ctypes.sizeof(_lib.Response) == 8 + 4 + 4 + 8 * 7 + 4 + 4 + 160
