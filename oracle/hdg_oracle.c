@@ -535,6 +535,125 @@ static void integrate_cell(const reftab *t, int c, const int *n,
 #undef AIJ
 }
 
+/* The same cell block for a general affine cell x = x0 + J xi (J[row][col],
+ * from cell_jacobian column-major per cell), as Gridap integrates on any
+ * affine map: physical gradients through J^{-T}, the outward unit normal of
+ * facet lf as J^{-T} n_ref / |J^{-T} n_ref| (src/Skeleton.jl:524-585,
+ * push_normal), the facet measure |det J| |J^{-T} n_ref|.  For a diagonal J
+ * it computes what integrate_cell computes (checked by a KAT). */
+static void integrate_cell_affine(const reftab *t, int c, const double *x0, const double *jac, double tau,
+                                  int stab_mode, int problem, double kappa, const int *facet_cells,
+                                  const int *cell_facets, double *A, double *b) {
+  int D = t->D, nk = t->nk, nfd = t->nfd, ni = t->ni, N = t->n;
+  double J[MAXD][MAXD] = {{0}}, Ji[MAXD][MAXD] = {{0}}, det;
+  for (int col = 0; col < D; ++col)
+    for (int row = 0; row < D; ++row) J[row][col] = jac[col * D + row];
+  if (D == 2) {
+    det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+    Ji[0][0] = J[1][1] / det;
+    Ji[0][1] = -J[0][1] / det;
+    Ji[1][0] = -J[1][0] / det;
+    Ji[1][1] = J[0][0] / det;
+  } else {
+    for (int r = 0; r < 3; ++r)
+      for (int q = 0; q < 3; ++q) {  /* cofactor of J[q][r] -> Ji[r][q] */
+        const int r1 = (q + 1) % 3, r2 = (q + 2) % 3, c1 = (r + 1) % 3, c2 = (r + 2) % 3;
+        Ji[r][q] = J[r1][c1] * J[r2][c2] - J[r1][c2] * J[r2][c1];
+      }
+    det = J[0][0] * Ji[0][0] + J[0][1] * Ji[1][0] + J[0][2] * Ji[2][0];
+    for (int r = 0; r < 3; ++r)
+      for (int q = 0; q < 3; ++q) Ji[r][q] /= det;
+  }
+  const double detJ = fabs(det);
+  memset(A, 0, sizeof(double) * N * N);
+  memset(b, 0, sizeof(double) * N);
+#define AIJ(i, j) A[(size_t)(i) + (size_t)N * (j)]
+  for (int q = 0; q < t->nqv; ++q) {
+    const double *ph = &t->phi[q * nk];
+    const double *dph = &t->dphi[q * nk * D];
+    double wq = t->qv_w[q] * detJ;
+    double x[MAXD], pe, qe[MAXD], fu[MAXD], g;
+    for (int d = 0; d < D; ++d) {
+      x[d] = x0[d];
+      for (int e = 0; e < D; ++e) x[d] += J[d][e] * t->qv_xi[q * D + e];
+    }
+    exact(problem, D, x, kappa, &pe, qe, fu, &g);
+    for (int a = 0; a < nk; ++a) {
+      double gx[MAXD];  /* physical gradient of basis a: d/dx_d = sum_e Ji[e][d] d/dxi_e */
+      for (int d = 0; d < D; ++d) {
+        gx[d] = 0.0;
+        for (int e = 0; e < D; ++e) gx[d] += Ji[e][d] * dph[a * D + e];
+      }
+      for (int bb = 0; bb < nk; ++bb) {
+        double m = wq * ph[a] * ph[bb] / kappa;
+        for (int d = 0; d < D; ++d) AIJ(d * nk + a, d * nk + bb) += m;
+        for (int d = 0; d < D; ++d) {
+          AIJ(d * nk + a, D * nk + bb) -= wq * gx[d] * ph[bb];
+          AIJ(D * nk + a, d * nk + bb) -= wq * gx[d] * ph[bb];
+        }
+      }
+      for (int d = 0; d < D; ++d) b[d * nk + a] += wq * ph[a] * fu[d];
+      b[D * nk + a] += wq * ph[a] * g;
+    }
+  }
+  for (int lf = 0; lf < 2 * D; ++lf) {
+    int dn = D - 1 - lf / 2, side = lf % 2;
+    double v[MAXD] = {0, 0, 0}, nv = 0.0;
+    for (int d = 0; d < D; ++d) {
+      v[d] = (side ? 1.0 : -1.0) * Ji[dn][d];
+      nv += v[d] * v[d];
+    }
+    nv = sqrt(nv);
+    double nrm[MAXD] = {0, 0, 0};
+    for (int d = 0; d < D; ++d) nrm[d] = v[d] / nv;
+    const double detF = detJ * nv;
+    int f = cell_facets[c * 2 * D + lf];
+    double s = 1.0;
+    if (stab_mode == 1) s = (facet_cells[2 * f] == c) ? 1.0 : -1.0;
+    int off = ni + lf * nfd;
+    for (int q = 0; q < t->nqf; ++q) {
+      const double *ph = &t->fphi[(lf * t->nqf + q) * nk];
+      const double *mu = &t->mu[q * nfd];
+      double wq = t->qf_w[q] * detF;
+      for (int a = 0; a < nk; ++a) {
+        for (int bb = 0; bb < nfd; ++bb) {
+          for (int d = 0; d < D; ++d) {
+            double w = wq * ph[a] * nrm[d] * mu[bb];
+            AIJ(d * nk + a, off + bb) += w;
+            AIJ(off + bb, d * nk + a) += w;
+          }
+          AIJ(D * nk + a, off + bb) -= wq * tau * s * ph[a] * mu[bb];
+          AIJ(off + bb, D * nk + a) += wq * tau * s * mu[bb] * ph[a];
+        }
+        for (int bb = 0; bb < nk; ++bb) {
+          for (int d = 0; d < D; ++d)
+            AIJ(D * nk + a, d * nk + bb) += wq * ph[a] * ph[bb] * nrm[d];
+          AIJ(D * nk + a, D * nk + bb) += wq * tau * s * ph[a] * ph[bb];
+        }
+      }
+      for (int a = 0; a < nfd; ++a)
+        for (int bb = 0; bb < nfd; ++bb)
+          AIJ(off + a, off + bb) -= wq * tau * s * mu[a] * mu[bb];
+    }
+  }
+#undef AIJ
+}
+
+int orc_integrate_darcy_affine(int D, int k, int ncells, const double *origin, const double *jacobian,
+                               double tau, int stab_mode, int problem, const double *kappa,
+                               const int *facet_cells, const int *cell_facets, double *A, double *b) {
+  reftab t;
+  if (reftab_init(&t, D, k)) return -1;
+  size_t N = t.n;
+#pragma omp parallel for schedule(static)
+  for (int c = 0; c < ncells; ++c)
+    integrate_cell_affine(&t, c, origin + (size_t)c * D, jacobian + (size_t)c * D * D, tau, stab_mode, problem,
+                          kappa ? kappa[c] : 1.0, facet_cells, cell_facets, A + (size_t)c * N * N,
+                          b + (size_t)c * N);
+  reftab_free(&t);
+  return 0;
+}
+
 int orc_integrate_darcy(int D, int k, const int *n, const double *domain,
                         double tau, int stab_mode, int problem,
                         const double *kappa, const int *facet_cells,

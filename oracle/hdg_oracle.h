@@ -52,6 +52,11 @@ int orc_integrate_darcy(int D, int k, const int *n, const double *domain,
                         double tau, int stab_mode, int problem,
                         const double *kappa, const int *facet_cells,
                         const int *cell_facets, double *A, double *b);
+/* General affine cells: origin (ncells x D), jacobian (ncells x D x D,
+ * column-major per cell), topology as above. */
+int orc_integrate_darcy_affine(int D, int k, int ncells, const double *origin, const double *jacobian,
+                               double tau, int stab_mode, int problem, const double *kappa,
+                               const int *facet_cells, const int *cell_facets, double *A, double *b);
 int orc_integrate_darcy_cells(int D, int k, const int *n, const double *domain,
                               double tau, int stab_mode, int problem,
                               const double *kappa, const int *facet_cells,

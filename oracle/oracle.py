@@ -92,6 +92,33 @@ class Mesh:
         assert rc == 0
         return A, b
 
+    def geometry(self):
+        """Per-cell origin (ncells x D) and Jacobian (ncells x D x D, [cell][col][row]) of the box cells."""
+        D = self.D
+        h = (self.domain[1::2] - self.domain[0::2]) / self.n
+        origin = np.zeros((self.ncells, D))
+        jac = np.zeros((self.ncells, D, D))
+        for c in range(self.ncells):
+            r = c
+            for d in range(D):  # first direction fastest
+                origin[c, d] = self.domain[2 * d] + (r % self.n[d]) * h[d]
+                r //= self.n[d]
+            jac[c] = np.diag(h)
+        return origin, jac
+
+    def integrate_affine(self, origin, jac, tau=1.0, stab=STAB_TEXTBOOK, problem=PROBLEM_LINEAR, kappa=None):
+        """The cell blocks of this topology with every cell an affine map x = origin_c + J_c xi
+        (jac[c] column-major, [cell][col][row]) (orc_integrate_darcy_affine)."""
+        n = self.ni + self.nf
+        A = np.zeros((self.ncells, n, n))
+        b = np.zeros((self.ncells, n))
+        kap = None if kappa is None else np.ascontiguousarray(kappa, dtype=np.float64)
+        rc = lib().orc_integrate_darcy_affine(self.D, self.k, self.ncells, P(np.ascontiguousarray(origin)),
+                                              P(np.ascontiguousarray(jac)), ctypes.c_double(tau), stab, problem,
+                                              P(kap), P(self.facet_cells), P(self.cell_facets), P(A), P(b))
+        assert rc == 0
+        return A, b
+
     def integrate_cells(self, cells, tau=1.0, stab=STAB_TEXTBOOK, problem=PROBLEM_LINEAR, kappa=None):
         cells = np.ascontiguousarray(cells, dtype=np.int32)
         n = self.ni + self.nf
