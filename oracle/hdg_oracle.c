@@ -654,6 +654,74 @@ int orc_integrate_darcy_affine(int D, int k, int ncells, const double *origin, c
   return 0;
 }
 
+/* Bulk-to-skeleton L2 projection P_m on local facet lf of the reference cell
+ * (test/P_m.jl:4-22; compute_bulk_to_skeleton_l2_projection_dofs,
+ * src/GridapAPIExtensions.jl:453-500): with the order-k facet basis mu and
+ * the order-kb cell basis phi,
+ *   A = int_F mu mu^T (nfd x nfd),  B = int_F mu phi^T (nfd x nkb),  P = A \ B,
+ * the coefficients in the facet basis of the projected trace of every cell
+ * basis function (P column-major, nfd x nkb).  On an affine cell the facet
+ * measure scales A and B alike, so P is the same on every cell.  The facet
+ * quadrature is the order-k table's (k + 2 points per direction: exact for
+ * the degree 2k + 1 of mu phi when kb = k + 1). */
+static int getrf(int n, double *A, int lda, int *ipiv);
+static void getrs(int n, int nrhs, const double *LU, int lda, const int *ipiv, double *B, int ldb);
+
+int orc_pm_projection(int D, int k, int kb, int lf, double *P) {
+  if (kb < 1 || kb > MAXK || lf < 0 || lf >= 2 * D) return -1;
+  reftab t, tb;
+  if (reftab_init(&t, D, k)) return -1;
+  if (reftab_init(&tb, D, kb)) {
+    reftab_free(&t);
+    return -1;
+  }
+  const int nfd = t.nfd, nkb = tb.nk;
+  double *A = (double *)calloc((size_t)nfd * nfd, sizeof(double));
+  double *phi = (double *)malloc(sizeof(double) * nkb);
+  int *ipiv = (int *)malloc(sizeof(int) * nfd);
+  memset(P, 0, sizeof(double) * (size_t)nfd * nkb);
+  for (int q = 0; q < t.nqf; ++q) {
+    const double *mu = &t.mu[q * nfd];
+    const double w = t.qf_w[q];
+    basis_eval(&tb, &t.fxi[(lf * t.nqf + q) * D], phi, NULL);
+    for (int a = 0; a < nfd; ++a) {
+      for (int b = 0; b < nfd; ++b) A[a + (size_t)nfd * b] += w * mu[a] * mu[b];
+      for (int j = 0; j < nkb; ++j) P[a + (size_t)nfd * j] += w * mu[a] * phi[j];
+    }
+  }
+  int rc = getrf(nfd, A, nfd, ipiv);
+  if (rc == 0) getrs(nfd, nkb, A, nfd, ipiv, P, nfd);
+  free(A);
+  free(phi);
+  free(ipiv);
+  reftab_free(&t);
+  reftab_free(&tb);
+  return rc;
+}
+
+/* The facet quadrature of the order-k table on local facet lf (for checks of
+ * P_m): cell-local points xi (nqf x D), weights w (nqf), facet basis mu
+ * (nqf x nfd); returns nqf. */
+int orc_facet_quadrature(int D, int k, int lf, double *xi, double *w, double *mu) {
+  reftab t;
+  if (lf < 0 || lf >= 2 * D || reftab_init(&t, D, k)) return -1;
+  const int nq = t.nqf;
+  if (xi) memcpy(xi, &t.fxi[(size_t)lf * nq * D], sizeof(double) * nq * D);
+  if (w) memcpy(w, t.qf_w, sizeof(double) * nq);
+  if (mu) memcpy(mu, t.mu, sizeof(double) * nq * t.nfd);
+  reftab_free(&t);
+  return nq;
+}
+
+/* Cell basis of order k at cell-local points xi (npts x D) -> val (npts x nk). */
+int orc_cell_basis(int D, int k, int npts, const double *xi, double *val) {
+  reftab t;
+  if (reftab_init(&t, D, k)) return -1;
+  for (int p = 0; p < npts; ++p) basis_eval(&t, &xi[(size_t)p * D], &val[(size_t)p * t.nk], NULL);
+  reftab_free(&t);
+  return 0;
+}
+
 int orc_integrate_darcy(int D, int k, const int *n, const double *domain,
                         double tau, int stab_mode, int problem,
                         const double *kappa, const int *facet_cells,

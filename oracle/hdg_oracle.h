@@ -52,6 +52,14 @@ int orc_integrate_darcy(int D, int k, const int *n, const double *domain,
                         double tau, int stab_mode, int problem,
                         const double *kappa, const int *facet_cells,
                         const int *cell_facets, double *A, double *b);
+/* Bulk-to-skeleton L2 projection P_m (facet order k, cell order kb) on local
+ * facet lf of the reference cell: P = (int mu mu^T) \ (int mu phi^T), column-major
+ * nfd x (kb+1)^D.  Returns getrf's info. */
+int orc_pm_projection(int D, int k, int kb, int lf, double *P);
+/* facet quadrature of the order-k tables on local facet lf; returns nqf */
+int orc_facet_quadrature(int D, int k, int lf, double *xi, double *w, double *mu);
+/* order-k cell basis at cell-local points (npts x D) -> (npts x (k+1)^D) */
+int orc_cell_basis(int D, int k, int npts, const double *xi, double *val);
 /* General affine cells: origin (ncells x D), jacobian (ncells x D x D,
  * column-major per cell), topology as above. */
 int orc_integrate_darcy_affine(int D, int k, int ncells, const double *origin, const double *jacobian,

@@ -174,6 +174,32 @@ class Mesh:
         return ef.value, ep.value
 
 
+def pm_projection(D, k, kb, lf):
+    """P_m on local facet lf: (nfd x (kb+1)^D) coefficients in the order-k facet
+    basis of the projected trace of each order-kb cell basis function."""
+    nfd, nkb = (k + 1) ** (D - 1), (kb + 1) ** D
+    pm = np.zeros((nkb, nfd))  # column-major nfd x nkb
+    rc = lib().orc_pm_projection(D, k, kb, lf, P(pm))
+    assert rc == 0
+    return pm.T.copy()
+
+
+def facet_quadrature(D, k, lf):
+    """(xi (nqf x D), w (nqf), mu (nqf x nfd)) of the order-k tables on local facet lf."""
+    n1 = k + 2
+    nq = n1 ** (D - 1)
+    xi, w, mu = np.zeros((nq, D)), np.zeros(nq), np.zeros((nq, (k + 1) ** (D - 1)))
+    assert lib().orc_facet_quadrature(D, k, lf, P(xi), P(w), P(mu)) == nq
+    return xi, w, mu
+
+
+def cell_basis(D, k, xi):
+    xi = np.ascontiguousarray(xi, dtype=np.float64)
+    val = np.zeros((xi.shape[0], (k + 1) ** D))
+    assert lib().orc_cell_basis(D, k, xi.shape[0], P(xi), P(val)) == 0
+    return val
+
+
 def static_condensation(A, b, ni):
     """A: (ncells, n, n) column-major per cell (A[c, j, i]); returns S (column-major), g, info."""
     ncells, n, _ = A.shape

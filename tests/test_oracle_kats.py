@@ -221,3 +221,22 @@ def test_affine_cell_integration_equals_the_box_cells(D, n, k, stab):
     A2, b2 = m.integrate_affine(origin, jac, problem=oracle.PROBLEM_SIN, stab=stab, kappa=kappa)
     assert np.abs(A2 - A).max() <= 1e-14 * np.abs(A).max()
     assert np.abs(b2 - b).max() <= 1e-14 * np.abs(b).max()
+
+
+@pytest.mark.parametrize("D", [2, 3])
+@pytest.mark.parametrize("k", [1, 2, 3])
+def test_pm_projection_kats(D, k):
+    """P_m (test/P_m.jl; src/GridapAPIExtensions.jl:453-500) on every local facet:
+    * bulk order k: the projected trace equals the trace (P_m is the identity on
+      traces when the orders match), so P is a 0/1 selection;
+    * bulk order k + 1: the residual is orthogonal to the facet space, the
+      reference's own check (test/LinearElasticityHDGTests.jl:136-139, < 1e-14)."""
+    for lf in range(2 * D):
+        xi, w, mu = oracle.facet_quadrature(D, k, lf)
+        Pk = oracle.pm_projection(D, k, k, lf)
+        assert np.abs(oracle.cell_basis(D, k, xi) - mu @ Pk).max() < 1e-13
+        assert np.abs(Pk - np.round(Pk)).max() < 1e-12
+        assert set((np.round(Pk) == 1).sum(axis=1).tolist()) == {1}
+        Pb = oracle.pm_projection(D, k, k + 1, lf)
+        res = oracle.cell_basis(D, k + 1, xi) - mu @ Pb
+        assert np.abs(mu.T @ (w[:, None] * res)).max() < 1e-14
