@@ -7,8 +7,8 @@ this package is the host-side mirror of the reference interface.
 from . import _lib
 from ._lib import Context, HdgError, default_context
 from .maps import (ArrayBlock, BackwardStaticCondensationMap, MatrixBlock,
-                   StaticCondensationMap, SumFacetsMap, VectorBlock, densify,
-                   evaluate, lazy_map, return_cache)
+                   Scalar2ArrayBlockMap, StaticCondensationMap, SumFacetsMap, VectorBlock,
+                   densify, evaluate, lazy_map, return_cache)
 from .operators import (CartesianDiscreteModel, DarcyHDG, ElasticityHDG, FEFunction, FESolver,
                         HybridAffineFEOperator, HybridFEOperator, MultiFieldFESpace,
                         NLSolver, ReferenceFE, Skeleton, TestFESpace, TrialFESpace,
@@ -19,7 +19,7 @@ __all__ = [
     "ArrayBlock", "BackwardStaticCondensationMap", "CartesianDiscreteModel", "Context",
     "DarcyHDG", "ElasticityHDG", "FEFunction", "FESolver", "HdgError", "HybridAffineFEOperator", "HybridFEOperator",
     "NLSolver", "MatrixBlock", "MultiFieldFESpace",
-    "ReferenceFE", "Skeleton", "StaticCondensationMap", "SumFacetsMap", "TestFESpace",
+    "ReferenceFE", "Scalar2ArrayBlockMap", "Skeleton", "StaticCondensationMap", "SumFacetsMap", "TestFESpace",
     "TrialFESpace", "Triangulation", "VectorBlock", "darcy_spaces", "default_context",
     "densify", "elasticity_spaces", "evaluate", "get_cell_normal_vector", "get_cell_owner_normal_vector",
     "lazy_map", "return_cache", "solve", "solve_",

@@ -8,8 +8,9 @@ Mirrors the Gridap.Fields.Map protocol the reference uses:
   instead of the reference's per-cell iteration.
 
 Maps: StaticCondensationMap (src/StaticCondensationMap.jl),
-BackwardStaticCondensationMap (src/BackwardStaticCondensationMap.jl) and
-SumFacetsMap (src/SumFacetsMap.jl).  ArrayBlock mirrors
+BackwardStaticCondensationMap (src/BackwardStaticCondensationMap.jl),
+SumFacetsMap (src/SumFacetsMap.jl) and Scalar2ArrayBlockMap
+(src/Scalar2ArrayBlockMap.jl).  ArrayBlock mirrors
 Gridap.Fields.ArrayBlock (a nested array of blocks plus a ``touched`` mask).
 Block bookkeeping (which blocks exist, densification into one dense array)
 is host-side layout work; every arithmetic operation runs in
@@ -269,6 +270,49 @@ class SumFacetsMap:
         if paths == [()]:
             return out[()]
         return _build_nested([(p, out[p]) for p in paths])
+
+
+class Scalar2ArrayBlockMap:
+    """Scalar2ArrayBlockMap (src/Scalar2ArrayBlockMap.jl:1-69): a dense cell
+    matrix A and vector b split into an ArrayBlock of bs[i] x bs[j] blocks and a
+    vector ArrayBlock of bs[i] blocks, every block touched -- the re-blocking of
+    a cell system by field (src/HybridAffineFEOperators.jl:343-356).  Layout
+    work only: the blocks are copies of A's and b's sub-ranges.  Called as the
+    reference calls it, with (A, b), bs or with A, b, bs."""
+
+    @staticmethod
+    def _args(args):
+        if len(args) == 2:
+            (A, b), bs = args
+        else:
+            A, b, bs = args
+        return np.asarray(A), np.asarray(b), [int(x) for x in bs]
+
+    def return_cache(self, *args):
+        A, b, bs = self._args(args)
+        n = len(bs)
+        Ab = np.empty((n, n), dtype=object)
+        bb = np.empty(n, dtype=object)
+        for i in range(n):
+            bb[i] = np.empty(bs[i], dtype=b.dtype)
+            for j in range(n):
+                Ab[i, j] = np.empty((bs[i], bs[j]), dtype=A.dtype)
+        return ArrayBlock(Ab, np.ones((n, n), dtype=bool)), ArrayBlock(bb, np.ones(n, dtype=bool))
+
+    def evaluate(self, cache, *args):
+        A, b, bs = self._args(args)
+        if A.shape != (sum(bs), sum(bs)) or b.shape != (sum(bs),):
+            raise ValueError("A and b must be sum(bs) x sum(bs) and sum(bs)")
+        Ab, bb = cache
+        off = np.concatenate([[0], np.cumsum(bs)])
+        for j in range(len(bs)):
+            for i in range(len(bs)):
+                if Ab.array[i, j].shape != (bs[i], bs[j]):
+                    raise ValueError("cache blocks do not match bs")
+                Ab.array[i, j][...] = A[off[i]:off[i + 1], off[j]:off[j + 1]]
+        for i in range(len(bs)):
+            bb.array[i][...] = b[off[i]:off[i + 1]]
+        return Ab, bb
 
 
 def densify(ab):
