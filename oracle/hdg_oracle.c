@@ -803,6 +803,45 @@ int orc_dirichlet_values(int D, int k, const int *n, const double *domain,
   return 0;
 }
 
+/* Nodal values of the manufactured pressure at every facet DOF of a mesh of
+ * affine cells (x = origin_c + J_c xi; jacobian column-major per cell), at
+ * the facet Lagrange nodes seen from the facet's first cell: free DOF id >= 0
+ * -> free_vals[id], Dirichlet DOF id < 0 -> dir_vals[-1 - id] (the values of
+ * TrialFESpace(M, p), test/DarcyHDGTests.jl:52, on any affine mesh). */
+int orc_facet_node_values_affine(int D, int k, int ncells, const double *origin, const double *jacobian,
+                                 const int *cell_facets, const int *facet_cells, int problem, int nfacets,
+                                 const int *facet_dofs, double *free_vals, double *dir_vals) {
+  int flat[36 * 2];
+  orc_lagrange_lattice(D - 1, k, flat);
+  int nfd = ipow(k + 1, D - 1);
+  for (int c = 0; c < ncells; ++c) {
+    const double *x0 = origin + (size_t)c * D, *J = jacobian + (size_t)c * D * D;
+    for (int lf = 0; lf < 2 * D; ++lf) {
+      int f = cell_facets[c * 2 * D + lf];
+      if (f < 0 || f >= nfacets || facet_cells[2 * f] != c) continue;  /* the facet's first cell */
+      int dn = D - 1 - lf / 2, side = lf % 2;
+      for (int a = 0; a < nfd; ++a) {
+        double xi[MAXD], x[MAXD];
+        int j = 0;
+        for (int d = 0; d < D; ++d) xi[d] = (d == dn) ? (double)side : (double)flat[a * (D - 1) + j++] / k;
+        for (int d = 0; d < D; ++d) {
+          x[d] = x0[d];
+          for (int e = 0; e < D; ++e) x[d] += J[e * D + d] * xi[e];
+        }
+        double p, q[MAXD], fu[MAXD], g;
+        exact(problem, D, x, 1.0, &p, q, fu, &g);
+        int id = facet_dofs[f * nfd + a];
+        if (id >= 0) {
+          if (free_vals) free_vals[id] = p;
+        } else if (dir_vals) {
+          dir_vals[-1 - id] = p;
+        }
+      }
+    }
+  }
+  return 0;
+}
+
 /* ------------------------------------------------------------------------ */
 /* LAPACK/BLAS restatements used by the maps.                                */
 /* ------------------------------------------------------------------------ */

@@ -52,6 +52,11 @@ int orc_integrate_darcy(int D, int k, const int *n, const double *domain,
                         double tau, int stab_mode, int problem,
                         const double *kappa, const int *facet_cells,
                         const int *cell_facets, double *A, double *b);
+/* Manufactured pressure at every facet DOF of a mesh of affine cells (free
+ * ids -> free_vals, Dirichlet ids -> dir_vals; either may be NULL). */
+int orc_facet_node_values_affine(int D, int k, int ncells, const double *origin, const double *jacobian,
+                                 const int *cell_facets, const int *facet_cells, int problem, int nfacets,
+                                 const int *facet_dofs, double *free_vals, double *dir_vals);
 /* Bulk-to-skeleton L2 projection P_m (facet order k, cell order kb) on local
  * facet lf of the reference cell: P = (int mu mu^T) \ (int mu phi^T), column-major
  * nfd x (kb+1)^D.  Returns getrf's info. */

@@ -119,6 +119,18 @@ class Mesh:
         assert rc == 0
         return A, b
 
+    def facet_node_values_affine(self, origin, jac, problem):
+        """(free, dirichlet) nodal values of the manufactured pressure at the facet DOFs
+        of this topology with affine cells (orc_facet_node_values_affine)."""
+        free = np.zeros(max(self.nfree, 1))
+        dirv = np.zeros(max(self.ndir, 1))
+        rc = lib().orc_facet_node_values_affine(self.D, self.k, self.ncells, P(np.ascontiguousarray(origin)),
+                                                P(np.ascontiguousarray(jac)), P(self.cell_facets),
+                                                P(self.facet_cells), problem, self.nfacets, P(self.facet_dofs),
+                                                P(free), P(dirv))
+        assert rc == 0
+        return free[:self.nfree], dirv[:self.ndir]
+
     def integrate_cells(self, cells, tau=1.0, stab=STAB_TEXTBOOK, problem=PROBLEM_LINEAR, kappa=None):
         cells = np.ascontiguousarray(cells, dtype=np.int32)
         n = self.ni + self.nf

@@ -240,3 +240,27 @@ def test_pm_projection_kats(D, k):
         Pb = oracle.pm_projection(D, k, k + 1, lf)
         res = oracle.cell_basis(D, k + 1, xi) - mu @ Pb
         assert np.abs(mu.T @ (w[:, None] * res)).max() < 1e-14
+
+
+SKEW = {2: np.array([[1.0, 0.3], [0.2, 1.0]]),
+        3: np.array([[1.0, 0.3, 0.1], [0.1, 1.0, 0.2], [0.05, 0.1, 1.0]])}
+
+
+@pytest.mark.parametrize("D,n,k", [(2, (4, 3), 1), (2, (3, 3), 2), (2, (3, 2), 3), (3, (2, 2, 2), 1),
+                                   (3, (2, 2, 2), 2)])
+def test_affine_cells_reproduce_a_linear_pressure(D, n, k):
+    """The reference's exactness check (test/DarcyHDGTests.jl:142) on a mesh whose
+    cells are all mapped by one skew: the oracle's affine-cell integration,
+    condensation, assembly and dense solve give the skeleton values of the
+    linear pressure at the free facet nodes."""
+    m = oracle.Mesh(D, n, k)
+    origin, jac = m.geometry()
+    B = SKEW[D]
+    origin = origin @ B.T
+    jac = np.einsum("rd,cjd->cjr", B, jac)  # J' = B J, stored [cell][col][row]
+    A, b = m.integrate_affine(origin, jac, stab=oracle.STAB_TEXTBOOK, problem=oracle.PROBLEM_LINEAR)
+    S, g, info = oracle.static_condensation(A, b, m.ni)
+    free, dirv = m.facet_node_values_affine(origin, jac, oracle.PROBLEM_LINEAR)
+    rowptr, colind, val, rhs = m.assemble(S, g, dirv)
+    lam = oracle.dense_solve(rowptr, colind, val, rhs)
+    assert np.abs(lam - free).max() < 1e-10 * max(1.0, np.abs(free).max())
