@@ -21,6 +21,7 @@ const LIB = joinpath(@__DIR__, "..", "libgridaphybrid_gb300.so")
 const HDG_OK = Cint(0)
 const HDG_PREC_FP64 = Cint(0)
 const HDG_PREC_FP32_REFINED = Cint(1)
+const HDG_PREC_FF_BLOCK = Cint(2)      # float-float block elimination: the fastest path (Darcy, elasticity)
 const HDG_SOLVER_PCG = Cint(0)
 const HDG_SOLVER_DIRECT = Cint(1)
 
@@ -108,6 +109,7 @@ end
 struct GPUHybridOperator
   ctx::Context
   problem::Ptr{Cvoid}
+  D::Int
   ncells::Int
   ni::Int
   nfree::Int
@@ -158,7 +160,7 @@ function GPUHybridOperator(model::CartesianDiscreteModel, order::Integer;
   info = Vector{Clonglong}(undef, 8)
   check(ctx, ccall((:hdg_problem_info, LIB), Cint, (Ptr{Cvoid}, Ptr{Clonglong}), h[], info))
   check(ctx, ccall((:hdg_assemble, LIB), Cint, (Ptr{Cvoid}, Cint, Ptr{Cint}), h[], precision, C_NULL))
-  GPUHybridOperator(ctx, h[], info[1], info[3], info[5])
+  GPUHybridOperator(ctx, h[], D, info[1], info[3], info[5])
 end
 
 function solve_gpu(op::GPUHybridOperator; solver=HDG_SOLVER_PCG, rtol=1e-10, maxit=20000)
@@ -171,6 +173,38 @@ function solve_gpu(op::GPUHybridOperator; solver=HDG_SOLVER_PCG, rtol=1e-10, max
   free = Vector{Float64}(undef, op.ncells * op.ni + op.nfree)
   check(op.ctx, ccall((:hdg_get_free_dof_values, LIB), Cint, (Ptr{Cvoid}, Ptr{Float64}), op.problem, free))
   free                                                               # FEFunction(op.trial, free)
+end
+
+# solve(op) in one call with a new permeability field (src/HybridAffineFEOperators.jl:67-100):
+# sets kappa (one value per cell), assembles in `precision`, solves the skeleton, recovers
+# and returns the free DOF values; `stats` = [iterations, relative residual, ms integrate +
+# condense, ms assemble, ms solve, ms recover, ms total].
+function solve_gpu!(op::GPUHybridOperator, kappa::Vector{Float64}; precision=HDG_PREC_FP64,
+                    solver=HDG_SOLVER_PCG, rtol=1e-10, maxit=20000)
+  length(kappa) == op.ncells || error("kappa needs one value per cell")
+  free = Vector{Float64}(undef, op.ncells * op.ni + op.nfree)
+  stats = Vector{Float64}(undef, 7)
+  check(op.ctx, ccall((:hdg_solve, LIB), Cint,
+                      (Ptr{Cvoid}, Cint, Cint, Cdouble, Cint, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
+                      op.problem, precision, solver, rtol, maxit, kappa, free, stats))
+  free, stats
+end
+
+# sqrt(sum(∫(e⋅e)dΩ)) for the flux and the pressure (test/DarcyHDGTests.jl:141-142)
+function l2_errors(op::GPUHybridOperator)
+  ef = Ref{Cdouble}(0)
+  ep = Ref{Cdouble}(0)
+  check(op.ctx, ccall((:hdg_l2_errors, LIB), Cint, (Ptr{Cvoid}, Ptr{Cdouble}, Ptr{Cdouble}),
+                      op.problem, ef, ep))
+  ef[], ep[]
+end
+
+# refinement of the fast precisions' skeleton solve: the residual reduction between two
+# FP64 residuals (default 1e-2 in 3D, 3e-2 in 2D) and reliable updates on/off
+function set_refinement!(op::GPUHybridOperator; delta=(op.D == 3 ? 1e-2 : 3e-2), keep_direction=true)
+  check(op.ctx, ccall((:hdg_set_refinement, LIB), Cint, (Ptr{Cvoid}, Cdouble, Cint),
+                      op.problem, Float64(delta), keep_direction ? Cint(1) : Cint(0)))
+  op
 end
 
 end # module
