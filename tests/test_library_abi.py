@@ -68,3 +68,16 @@ def test_no_device_means_error_not_fallback():
     assert rc == _lib.HDG_ERR_NODEVICE
     with pytest.raises(_lib.HdgError):
         _lib.Context(0)
+
+
+def test_julia_shim_binds_only_declared_exported_entry_points(libpath):
+    """The Julia binding is shipped as source (no Julia here): every entry point
+    it ccalls must exist in the header and in the library."""
+    shim = os.path.join(ROOT, "gridaphybrid.jl_gb300", "julia", "GridapHybridGB300.jl")
+    called = set(re.findall(r"ccall\(\(:(hdg_[a-z0-9_]+),", open(shim).read()))
+    assert len(called) >= 10
+    out = subprocess.run(["nm", "-D", "--defined-only", libpath], capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\sT\s(hdg_\w+)", out))
+    decl = set(declared_functions())
+    assert not (called - decl), sorted(called - decl)
+    assert not (called - exported), sorted(called - exported)
