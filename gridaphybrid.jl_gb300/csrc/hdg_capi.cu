@@ -18,6 +18,8 @@
 
 using namespace hdg;
 
+std::atomic<long long> hdg::g_device_allocs(0);
+
 #define CUDA_TRY(ctx, call)                                                          \
   do {                                                                               \
     cudaError_t e_ = (call);                                                         \
@@ -28,21 +30,25 @@ using namespace hdg;
 
 namespace {
 
-bool is_device_ptr(const void *p) {
-  if (!p) return false;
-  cudaPointerAttributes at;
-  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
-    cudaGetLastError();
-    return false;
-  }
-  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+bool is_device_ptr(const hdg_context *ctx, const void *p) {
+  return p && ptr_place(p, ctx->device) == PtrPlace::Device;
+}
+
+// HDG_ERR_INVALID when p is device memory of another GPU than the context's.
+int check_ptr_device(hdg_context *ctx, const void *p) {
+  int dev = -1;
+  if (p && ptr_place(p, ctx->device, &dev) == PtrPlace::OtherDevice)
+    return ctx->fail(HDG_ERR_INVALID, "a pointer argument is device memory of GPU %d; the context is on GPU %d",
+                     dev, ctx->device);
+  return HDG_OK;
 }
 
 // Device view of a caller buffer: the pointer itself when it is device memory,
 // else a staging buffer (filled from host when `in`).
 template <typename T>
 int stage_in(hdg_context *ctx, DBuf &buf, const T *src, size_t count, const T **out) {
-  if (is_device_ptr(src)) {
+  if (int rc = check_ptr_device(ctx, src)) return rc;
+  if (is_device_ptr(ctx, src)) {
     *out = src;
     return HDG_OK;
   }
@@ -54,7 +60,8 @@ int stage_in(hdg_context *ctx, DBuf &buf, const T *src, size_t count, const T **
 
 template <typename T>
 int stage_out(hdg_context *ctx, DBuf &buf, T *dst, size_t count, T **out) {
-  if (is_device_ptr(dst)) {
+  if (int rc = check_ptr_device(ctx, dst)) return rc;
+  if (is_device_ptr(ctx, dst)) {
     *out = dst;
     return HDG_OK;
   }
@@ -438,6 +445,21 @@ extern "C" {
 
 int hdg_version(void) { return 100; }
 
+int hdg_device_allocations(long long *count) {
+  if (!count) return HDG_ERR_INVALID;
+  *count = g_device_allocs.load(std::memory_order_relaxed);
+  return HDG_OK;
+}
+
+int hdg_pointer_placement(int memory_type, int pointer_device, int context_device, int *place) {
+  if (!place) return HDG_ERR_INVALID;
+  switch (ptr_place_rule(memory_type, pointer_device, context_device)) {
+    case PtrPlace::Host: *place = 0; return HDG_OK;
+    case PtrPlace::Device: *place = 1; return HDG_OK;
+    default: *place = 2; return HDG_ERR_INVALID;
+  }
+}
+
 int hdg_context_create(int device, hdg_context **out) {
   if (!out) return HDG_ERR_INVALID;
   *out = nullptr;
@@ -574,7 +596,8 @@ int hdg_static_condensation(hdg_context *ctx, int precision, int ncells, int ni,
   bool bad = false;
   for (int c = 0; c < ncells; ++c) bad |= hinfo[c] != 0;
   if (info) {
-    if (is_device_ptr(info))
+    if ((rc = check_ptr_device(ctx, info))) return rc;
+    if (is_device_ptr(ctx, info))
     {
       CUDA_TRY(ctx, cudaMemcpyAsync(info, dinfo, sizeof(int) * ncells, cudaMemcpyDeviceToDevice, ctx->stream));
       CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
@@ -882,7 +905,10 @@ static int assemble_prepare(hdg_problem *pb, int precision, bool cell_blocks, bo
   CUDA_TRY(ctx, pb->d_info.reserve(sizeof(int) * nc));
   CUDA_TRY(ctx, pb->d_val.reserve(sizeof(double) * (pb->pat.nnz ? pb->pat.nnz : 1)));
   CUDA_TRY(ctx, pb->d_rhs.reserve(sizeof(double) * (pb->mesh.nfree ? pb->mesh.nfree : 1)));
-  if (mixed) CUDA_TRY(ctx, pb->d_cellop.reserve(sizeof(float) * nc * cellop_rec(nl, (int)t.nfd)));
+  if (mixed) {
+    CUDA_TRY(ctx, pb->d_cellop.reserve(sizeof(float) * nc * cellop_rec(nl, (int)t.nfd)));
+    CUDA_TRY(ctx, pb->d_W.reserve(sizeof(double) * std::max<size_t>(pb->pat.nblockrows, 1) * t.nfd * t.nfd));
+  }
   pb->precision = precision;
   pb->assembled = pb->solved = pb->recovered = false;
   return HDG_OK;
@@ -898,10 +924,22 @@ static cudaError_t assemble_skeleton(hdg_problem *pb) {
                                   pb->d_val.as<double>(), pb->d_rhs.as<double>(), ctx->stream, ctx->num_sms,
                                   &ctx->launches);
   if (e != cudaSuccess || pb->precision == HDG_PREC_FP64) return e;
-  // the operator in the SPD frame
+  // the scaling of the inner frame, W = blockdiag(L_f^{-1}) with sign*D_f = L_f L_f^T
+  // from the assembled diagonal blocks, then the scaled operator in the SPD frame
+  PcgArgs da{};
+  da.n = pb->mesh.nfree;
+  da.nfd = t.nfd;
+  da.nblockrows = pb->pat.nblockrows;
+  da.val = pb->d_val.as<double>();
+  da.diag_blk = pb->d_diag_blk.as<int>();
+  da.blk_off = pb->d_blk_off.as<int64_t>();
+  da.blk_rowlen = pb->d_blk_rowlen.as<int>();
+  da.sign = skeleton_sign(pb);
+  e = launch_block_chol_inv(da, pb->d_W.as<double>(), ctx->stream, ctx->num_sms, &ctx->launches);
+  if (e != cudaSuccess) return e;
   return launch_pack_cell_blocks(pb->mesh.ncells, 2 * t.D, t.nfd, skeleton_sign(pb), pb->d_S.as<double>(),
-                                 pb->d_cellop.as<float>(), ctx->smem_optin, ctx->stream, ctx->num_sms,
-                                 &ctx->launches);
+                                 pb->d_cell_blk.as<int>(), pb->d_W.as<double>(), pb->d_cellop.as<float>(),
+                                 ctx->smem_optin, ctx->stream, ctx->num_sms, &ctx->launches);
 }
 
 extern "C" {
@@ -1001,11 +1039,11 @@ static Pcg32Args pcg32_args(hdg_problem *pb) {
   ia.n = (int)n;
   ia.nfd = pb->mesh.nfd;
   ia.nblockrows = pb->pat.nblockrows;
-  ia.Binv32 = pb->d_Binv32.as<float>();
+  ia.W = pb->d_W.as<double>();
   ia.rhs = pb->d_r.as<double>();  // the outer residual
   ia.x = v;
   ia.r = v + n;
-  ia.z = v + 2 * n;
+  ia.z = ia.r;  // identity preconditioner in the scaled frame
   ia.p = v + 3 * n;
   ia.p2 = v + 4 * n;
   ia.partials = pb->d_partials.as<double>();
@@ -1017,18 +1055,84 @@ static Pcg32Args pcg32_args(hdg_problem *pb) {
   ia.rec = cellop_rec(ia.nl, ia.nfd);
   ia.blocks = pb->d_cellop.as<float>();
   ia.cell_blk = pb->d_cell_blk.as<int>();
-  ia.br_src = pb->d_br_src.as<int>();
   ia.qc = pb->d_qc.as<float>();
   ia.nstage = pb->cellop_nstage;
   ia.ctas = pb->cellop_ctas;
   ia.error = pb->d_counter.as<unsigned int>() + 1;
-  {  // update kernel: about two tiles of block rows per CTA, at most eight CTAs per SM
-    const long long tiles = (pb->pat.nblockrows + kPcgThreadsHost / ia.nfd - 1) / (kPcgThreadsHost / ia.nfd);
-    long long g = (tiles + 1) / 2;
+  {  // update kernel: about two rows per thread, at most eight CTAs per SM
+    long long g = ((long long)n + 2 * kPcgThreadsHost - 1) / (2 * kPcgThreadsHost);
     const long long cap = (long long)pb->ctx->num_sms * 8;
     ia.uctas = g > cap ? (int)cap : g < 1 ? 1 : (int)g;
   }
   return ia;
+}
+
+// FP64 PCG iterations from the state launch_pcg_setup left (x = 0, r = the
+// right-hand side), as replays of a CUDA graph of 16 iterations, until the
+// device-side done flag or maxit.
+static int run_pcg64(hdg_problem *pb, const PcgArgs &a, int maxit, int *it_out, double *rel_out) {
+  hdg_context *ctx = pb->ctx;
+  const int pairs = 8;  // 16 iterations per graph replay
+  if (!pb->pcg_graph) {
+    cudaGraph_t g;
+    long long dummy = 0;
+    CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    for (int i = 0; i < pairs; ++i) launch_pcg_iteration_pair(a, ctx->stream, ctx->num_sms, &dummy);
+    CUDA_TRY(ctx, cudaStreamEndCapture(ctx->stream, &g));
+    cudaError_t e = cudaGraphInstantiate(&pb->pcg_graph, g, 0);
+    cudaGraphDestroy(g);
+    CUDA_TRY(ctx, e);
+    pb->pcg_graph_chunk = 2 * pairs;
+  }
+  double *h = static_cast<double *>(pb->h_pinned.ptr);
+  int it = 0;
+  double rel = 0.0;
+  int status = HDG_OK;
+  for (;;) {
+    CUDA_TRY(ctx, cudaGraphLaunch(pb->pcg_graph, ctx->stream));
+    ctx->launches += 2LL * pb->pcg_graph_chunk;
+    CUDA_TRY(ctx, cudaMemcpyAsync(h, pb->d_scal.ptr, sizeof(double) * 16, cudaMemcpyDeviceToHost, ctx->stream));
+    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    it = (int)h[8];
+    rel = h[5] > 0 ? std::sqrt(h[4] / h[5]) : 0.0;
+    if (h[7] != 0.0) break;
+    if (it >= maxit) {
+      status = ctx->fail(HDG_ERR_NOT_CONVERGED, "PCG: relative residual %.3e after %d iterations", rel, it);
+      break;
+    }
+    if (!std::isfinite(rel)) {
+      status = ctx->fail(HDG_ERR_NOT_CONVERGED, "PCG breakdown (non-finite residual)");
+      break;
+    }
+  }
+  *it_out = it;
+  *rel_out = rel;
+  return status;
+}
+
+// Correction solve in FP64 for a refined solve whose FP32 cycles stall (the
+// FP32 operator's rounding, about 6e-8 of each entry, times the system's
+// condition number approaches one): with the outer residual r = sign (c - A x)
+// as right-hand side, FP64 PCG solves A e = r from zero, and x <- x + sign e.
+// The outer residual is then recomputed in FP64.  Uses the FP32 inner
+// vectors (no longer needed) to hold the saved iterate.
+static int refine_fp64_correction(hdg_problem *pb, const OuterArgs &oa, double rtol_corr, int maxit, int *its) {
+  hdg_context *ctx = pb->ctx;
+  const size_t n = pb->mesh.nfree;
+  double *xsaved = pb->d_v32.as<double>();             // 5n floats hold n doubles ...
+  float *zero = pb->d_v32.as<float>() + 2 * n;          // ... and n zero floats after them
+  CUDA_TRY(ctx, cudaMemcpyAsync(xsaved, oa.x, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+  CUDA_TRY(ctx, cudaMemsetAsync(zero, 0, sizeof(float) * n, ctx->stream));
+  PcgArgs a = pcg_args(pb);
+  a.rhs = oa.r;  // read once by the init kernel, row by row, before r is overwritten
+  CUDA_TRY(ctx, launch_pcg_setup(a, rtol_corr, ctx->stream, ctx->num_sms, &ctx->launches));
+  double rel = 0.0;
+  int status = run_pcg64(pb, a, maxit, its, &rel);
+  if (status == HDG_ERR_CUDA) return status;
+  // x = xsaved + sign * e (e is in a.x == oa.x), then the FP64 residual
+  CUDA_TRY(ctx, launch_outer_combine(oa, xsaved, ctx->stream, &ctx->launches));
+  CUDA_TRY(ctx, launch_outer_update(oa, zero, ctx->stream, &ctx->launches));
+  return status;
 }
 
 // Mixed-precision skeleton solve: FP32 inner PCG inside an FP64 residual loop.
@@ -1047,14 +1151,14 @@ static int solve_pcg_refined(hdg_problem *pb, double rtol, int maxit, int *it_ou
   }
   if (pb->cellop_ctas > ctx->num_sms * 4)
     return ctx->fail(HDG_ERR_INVALID, "cell operator grid exceeds the partials buffer");
-  CUDA_TRY(ctx, pb->d_Binv32.reserve(sizeof(float) * nbr * nfd * nfd));
+  if (!pb->d_W.ptr) return ctx->fail(HDG_ERR_STATE, "the inner frame's scaling is missing (assemble in a fast precision)");
   CUDA_TRY(ctx, pb->d_v32.reserve(sizeof(float) * 5 * n));
-  CUDA_TRY(ctx, pb->d_qc.reserve(sizeof(float) * pb->mesh.ncells * nl * nfd));
+  CUDA_TRY(ctx, pb->d_qc.reserve(sizeof(float) * nbr * 2 * nfd));
+  // the other-cell half of a facet with one cell is never written: zero
+  CUDA_TRY(ctx, cudaMemsetAsync(pb->d_qc.ptr, 0, sizeof(float) * nbr * 2 * nfd, ctx->stream));
   // last-CTA counter, bulk-copy error flag and the grid-barrier count and generation start at zero
   CUDA_TRY(ctx, cudaMemsetAsync(pb->d_counter.ptr, 0, sizeof(unsigned int) * 4, ctx->stream));
   CUDA_TRY(ctx, pb->d_scal2.reserve(sizeof(double) * 16));
-  CUDA_TRY(ctx, launch_binv_to_f32(nbr * nfd * nfd, pb->d_Binv.as<double>(), pb->d_Binv32.as<float>(), ctx->stream,
-                                   &ctx->launches));
   Pcg32Args ia = pcg32_args(pb);
   OuterArgs oa{};
   oa.n = (int)n;
@@ -1071,6 +1175,7 @@ static int solve_pcg_refined(hdg_problem *pb, double rtol, int maxit, int *it_ou
   oa.counter = ia.counter;
   oa.nparts = ia.nparts;
   oa.sign = skeleton_sign(pb);
+  oa.W = pb->d_W.as<double>();
   const int pairs = 8;
   // the inner iterations as one cooperative launch per chunk where its grid
   // can be co-resident (about two cell units per CTA on small problems), else
@@ -1104,9 +1209,16 @@ static int solve_pcg_refined(hdg_problem *pb, double rtol, int maxit, int *it_ou
   int status = HDG_OK;
   int base = 0;         // iterations counted before the last init (SC_ITERS restarts there)
   int cycle_start = 0;  // iterations counted when the graph last started from ia.p
+  pb->last_fp64_iters = 0;
   bool restart = true;  // next cycle starts a fresh Krylov space
+  int slow = 0;         // consecutive cycles that cut the FP64 residual less than 2x
+  bool stalled = false;
   while (cc > 0.0 && rr > rtol * rtol * cc) {
-    if (total >= maxit || outer >= 60) {
+    if (total < maxit && (slow >= 3 || outer >= 60)) {
+      stalled = true;  // finished below by an FP64 correction solve
+      break;
+    }
+    if (total >= maxit) {
       status = ctx->fail(HDG_ERR_NOT_CONVERGED, "refined PCG: relative residual %.3e after %d iterations",
                          std::sqrt(rr / cc), total);
       break;
@@ -1154,6 +1266,22 @@ static int solve_pcg_refined(hdg_problem *pb, double rtol, int maxit, int *it_ou
     // a kept direction that no longer cuts the true residual (the FP32
     // recurrence drifted) is dropped: the next cycle restarts
     restart = rr > 0.0625 * rr_before;
+    slow = rr > 0.25 * rr_before ? slow + 1 : 0;
+  }
+  if (stalled && status == HDG_OK) {
+    int extra = 0;
+    const double rtol_corr = 0.5 * rtol * std::sqrt(cc / rr);
+    status = refine_fp64_correction(pb, oa, rtol_corr, maxit - total, &extra);
+    if (status == HDG_ERR_CUDA) return status;
+    total += extra;
+    ++outer;
+    pb->last_fp64_iters = extra;
+    CUDA_TRY(ctx, cudaMemcpyAsync(ho, oa.scal, sizeof(double) * 2, cudaMemcpyDeviceToHost, ctx->stream));
+    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    rr = ho[1];
+    if (status == HDG_OK && !(rr <= rtol * rtol * cc))
+      status = ctx->fail(HDG_ERR_NOT_CONVERGED, "refined PCG with FP64 correction: relative residual %.3e after %d "
+                         "iterations", std::sqrt(rr / cc), total);
   }
   {
     unsigned int herr = 0;
@@ -1184,9 +1312,8 @@ static int solve_reserve(hdg_problem *pb) {
     pb->h_pinned.bytes = 4096;
   }
   if (pb->precision != HDG_PREC_FP64) {
-    CUDA_TRY(ctx, pb->d_Binv32.reserve(sizeof(float) * nbr * nfd * nfd));
     CUDA_TRY(ctx, pb->d_v32.reserve(sizeof(float) * 5 * n));
-    CUDA_TRY(ctx, pb->d_qc.reserve(sizeof(float) * pb->mesh.ncells * 2 * pb->mesh.D * nfd));
+    CUDA_TRY(ctx, pb->d_qc.reserve(sizeof(float) * std::max<size_t>(nbr, 1) * 2 * nfd));
     CUDA_TRY(ctx, pb->d_scal2.reserve(sizeof(double) * 16));
   }
   CUDA_TRY(ctx, pb->d_uint.reserve(sizeof(double) * pb->mesh.ncells * pb->tab.ni));
@@ -1210,6 +1337,8 @@ int hdg_solve_skeleton(hdg_problem *pb, int solver, double rtol, int maxit, int 
   int it = 0;
   double rel = 0.0;
   int status = HDG_OK;
+  pb->last_outer = 0;
+  pb->last_fp64_iters = 0;
   if (n == 0) {
     // nothing to solve
   } else if (solver == HDG_SOLVER_DIRECT) {
@@ -1245,40 +1374,12 @@ int hdg_solve_skeleton(hdg_problem *pb, int solver, double rtol, int maxit, int 
     }
     PcgArgs a = pcg_args(pb);
     CUDA_TRY(ctx, launch_pcg_setup(a, rtol, ctx->stream, ctx->num_sms, &ctx->launches));
-    const int pairs = 8;  // 16 iterations per graph replay
     if (pb->precision != HDG_PREC_FP64) {
       status = solve_pcg_refined(pb, rtol, maxit, &it, &rel);
       if (status == HDG_ERR_CUDA) return status;
     } else {
-    if (!pb->pcg_graph) {
-      cudaGraph_t g;
-      long long dummy = 0;
-      CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-      for (int i = 0; i < pairs; ++i) launch_pcg_iteration_pair(a, ctx->stream, ctx->num_sms, &dummy);
-      CUDA_TRY(ctx, cudaStreamEndCapture(ctx->stream, &g));
-      cudaError_t e = cudaGraphInstantiate(&pb->pcg_graph, g, 0);
-      cudaGraphDestroy(g);
-      CUDA_TRY(ctx, e);
-      pb->pcg_graph_chunk = 2 * pairs;
-    }
-    double *h = static_cast<double *>(pb->h_pinned.ptr);
-    for (;;) {
-      CUDA_TRY(ctx, cudaGraphLaunch(pb->pcg_graph, ctx->stream));
-      ctx->launches += 2LL * pb->pcg_graph_chunk;
-      CUDA_TRY(ctx, cudaMemcpyAsync(h, pb->d_scal.ptr, sizeof(double) * 16, cudaMemcpyDeviceToHost, ctx->stream));
-      CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-      it = (int)h[8];
-      rel = h[5] > 0 ? std::sqrt(h[4] / h[5]) : 0.0;
-      if (h[7] != 0.0) break;
-      if (it >= maxit) {
-        status = ctx->fail(HDG_ERR_NOT_CONVERGED, "PCG: relative residual %.3e after %d iterations", rel, it);
-        break;
-      }
-      if (!std::isfinite(rel)) {
-        status = ctx->fail(HDG_ERR_NOT_CONVERGED, "PCG breakdown (non-finite residual)");
-        break;
-      }
-    }
+      status = run_pcg64(pb, a, maxit, &it, &rel);
+      if (status == HDG_ERR_CUDA) return status;
     }
   }
   CUDA_TRY(ctx, cudaEventRecord(ev[5], ctx->stream));
@@ -1526,6 +1627,15 @@ int hdg_context_set_persistent_pcg(hdg_context *ctx, int on) {
 int hdg_get_timings(const hdg_problem *pb, double *ms) {
   if (!pb || !ms) return HDG_ERR_INVALID;
   for (int i = 0; i < 5; ++i) ms[i] = pb->timings[i];
+  return HDG_OK;
+}
+
+int hdg_get_solve_stats(const hdg_problem *pb, double *stats) {
+  if (!pb || !stats) return HDG_ERR_INVALID;
+  stats[0] = pb->last_iters;
+  stats[1] = pb->last_relres;
+  stats[2] = pb->last_outer;
+  stats[3] = pb->last_fp64_iters;
   return HDG_OK;
 }
 

@@ -42,7 +42,7 @@ static std::vector<CubeFace> cube_face_list(int D) {
   return cur;
 }
 
-static std::vector<int> node_lattice(int D, int k) {
+std::vector<int> node_lattice(int D, int k) {
   std::vector<int> lat;
   if (D == 0) {
     return lat;
@@ -67,7 +67,7 @@ static std::vector<int> node_lattice(int D, int k) {
 }
 
 // 1D Lagrange polynomial through the equispaced nodes j/k, value + derivative.
-static void lagrange1d(int k, int i, double x, double &v, double &dv) {
+void lagrange1d(int k, int i, double x, double &v, double &dv) {
   v = 1.0;
   dv = 0.0;
   const double xi = double(i) / k;
@@ -80,7 +80,7 @@ static void lagrange1d(int k, int i, double x, double &v, double &dv) {
 }
 
 // Gauss-Legendre points/weights on [0,1] by Newton iteration on P_n.
-static void gauss01(int np, std::vector<double> &x, std::vector<double> &w) {
+void gauss01(int np, std::vector<double> &x, std::vector<double> &w) {
   x.assign(np, 0.0);
   w.assign(np, 0.0);
   for (int i = 0; i < np; ++i) {

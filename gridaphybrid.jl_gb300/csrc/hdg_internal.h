@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <cstdarg>
 #include <cstdio>
 #include <string>
@@ -14,6 +15,55 @@ namespace hdg {
 
 constexpr int kMaxD = 3;
 constexpr int kMaxK = 4;
+
+// Device allocations made through DBuf::reserve since the library was loaded
+// (all contexts), reported by hdg_device_allocations.
+extern std::atomic<long long> g_device_allocs;
+
+// ---------------------------------------------------------------------------
+// Where a caller's pointer lives, seen from a context on `ctx_device`.
+// ---------------------------------------------------------------------------
+enum class PtrPlace { Host, Device, OtherDevice };
+// The placement rule on cudaPointerAttributes' (type, device): device memory
+// of the context's GPU and managed memory are used in place, host memory is
+// staged, device memory of another GPU is refused (the kernels would fault on
+// it without peer access).
+inline PtrPlace ptr_place_rule(int memory_type, int ptr_device, int ctx_device) {
+  if (memory_type == cudaMemoryTypeManaged) return PtrPlace::Device;
+  if (memory_type == cudaMemoryTypeDevice)
+    return ptr_device == ctx_device ? PtrPlace::Device : PtrPlace::OtherDevice;
+  return PtrPlace::Host;
+}
+inline PtrPlace ptr_place(const void *p, int ctx_device, int *ptr_device = nullptr) {
+  if (!p) return PtrPlace::Host;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return PtrPlace::Host;
+  }
+  if (ptr_device) *ptr_device = at.device;
+  return ptr_place_rule((int)at.type, at.device, ctx_device);
+}
+
+// Makes `device` current for the scope and gives the caller's current device
+// back on exit (host frameworks track their own current device).
+struct DeviceGuard {
+  int prev = -1;
+  cudaError_t status = cudaSuccess;
+  explicit DeviceGuard(int device) {
+    if (cudaGetDevice(&prev) != cudaSuccess) {
+      cudaGetLastError();
+      prev = -1;
+    }
+    if (prev != device) status = cudaSetDevice(device);
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+  }
+  DeviceGuard(const DeviceGuard &) = delete;
+  DeviceGuard &operator=(const DeviceGuard &) = delete;
+};
 
 // ---------------------------------------------------------------------------
 // Device buffer owned by a context or problem.
@@ -51,6 +101,7 @@ struct DBuf {
       ptr = nullptr;
       return e;
     }
+    g_device_allocs.fetch_add(1, std::memory_order_relaxed);
     bytes = nbytes;
     return cudaSuccess;
   }
@@ -98,6 +149,54 @@ struct L2RefHost {
 };
 void build_l2_ref(const RefTables &t, L2RefHost &r);
 int build_ref_tables(int D, int k, RefTables &t, int phys = 0);
+
+// Lagrange lattice of Q_k on [0,1]^D in Gridap's node order (lattice index i
+// is the coordinate i/k), the 1D Lagrange polynomial of node i, and
+// Gauss-Legendre points on [0,1].
+std::vector<int> node_lattice(int D, int k);
+void lagrange1d(int k, int i, double x, double &v, double &dv);
+void gauss01(int np, std::vector<double> &x, std::vector<double> &w);
+
+// A scalar polynomial basis on the reference cube [0,1]^d: Q_k (tensor
+// Lagrange in Gridap's node order) or P_k (total degree <= k, Lagrange at the
+// simplex lattice points i/k; the constant for k = 0).
+constexpr int kBasisQ = 0;
+constexpr int kBasisP = 1;
+struct ScalarBasis {
+  int d = 0, kind = kBasisQ, k = 0, nb = 0;
+  std::vector<int> lat;       // Q: nb x d lattice indices
+  std::vector<int> mono;      // P: nb x d monomial exponents
+  std::vector<double> coef;   // P: nb x nb, phi_a = sum_m coef[a nb + m] x^mono_m
+  std::vector<double> nodes;  // nb x d nodal points
+  int init(int dim, int basis_kind, int order);
+  // values (nb) and reference gradients (nb x d, may be null) at xi
+  void eval(const double *xi, double *val, double *grad) const;
+};
+
+// Reference tables of a general-space form (fields with their own spaces):
+// A the first bulk field (Darcy flux / elasticity stress), B the second
+// (pressure / displacement), T the trace on facets.  spaces[7] = {kindA, kA,
+// kindB, kB, kindT, kT, pm}; pm: P_m of the displacement in the tau terms.
+// All tables FP64, packed in `packed` at the offsets below (in doubles):
+//   MAA  nA x nA            int phiA_a phiA_b
+//   GAB  D x nA x nB        int d_e phiA_a phiB_b
+//   GBA  D x nB x nA        int d_e phiB_b phiA_a
+//   FBA  2D x nB x nA       int_F phiB_b phiA_a       (unit facet measure)
+//   FBB  2D x nB x nB       int_F phiB_b phiB_c, or with pm H_B L^{-1} H_B^T
+//   HA   2D x nA x nT       int_F phiA_a mu_m
+//   HB   2D x nB x nT       int_F phiB_b mu_m
+//   L    nT x nT            int_F mu_m mu_n
+//   qxi (nqv x D), qw (nqv), qphiA (nqv x nA), qphiB (nqv x nB)
+struct GsTables {
+  int D = 0, phys = 0, pm = 0;
+  int spaces[7] = {0, 0, 0, 0, 0, 0, 0};
+  ScalarBasis A, B, T;
+  int ncA = 0, ncB = 0, ncT = 0, nA = 0, nB = 0, nT = 0, ni = 0, nf = 0, nfd = 0, n = 0, n1 = 0, nqv = 0;
+  std::vector<double> packed;
+  int oMAA = 0, oGAB = 0, oGBA = 0, oFBA = 0, oFBB = 0, oHA = 0, oHB = 0, oL = 0, oqxi = 0, oqw = 0, oqphiA = 0,
+      oqphiB = 0;
+};
+int build_gs_tables(int D, int phys, const int *spaces, GsTables &t, std::string &err);
 
 // Offsets (in doubles) of each table inside the packed device table buffer.
 struct TableOffsets {
@@ -215,10 +314,10 @@ struct hdg_problem {
   hdg::DBuf d_br_row0, d_br_src, d_blk_off, d_blk_rowlen, d_blk_src, d_diag_blk,
       d_dir_cells;
   hdg::DBuf d_Binv, d_x, d_r, d_z, d_p, d_p2, d_q, d_partials, d_scal, d_counter;
-  // mixed-precision skeleton solve: the FP32 operator as symmetric cell
-  // blocks, its cell map and per-cell products, FP32 block inverses, inner
-  // vectors (x, r, z, p, p2), outer scalars
-  hdg::DBuf d_cellop, d_cell_blk, d_qc, d_Binv32, d_v32, d_scal2;
+  // mixed-precision skeleton solve: the scaled FP32 operator as symmetric
+  // cell blocks, its cell map, the products by block row, the scaling
+  // W = blockdiag(L_f^{-1}) (FP64), inner vectors (x, r, p, p2), outer scalars
+  hdg::DBuf d_cellop, d_cell_blk, d_qc, d_W, d_v32, d_scal2;
   // block-elimination path: M_ref^{-1} as (hi, lo) floats then FP64, 1/m per
   // cell, the elasticity kernel's per-CTA scratch panels
   hdg::DBuf d_minv, d_invm, d_escratch;
@@ -238,11 +337,16 @@ struct hdg_problem {
   double refine_delta = 3e-2;
   int refine_keep = 1;
   int last_outer = 0;
+  int last_fp64_iters = 0;  // FP64 correction iterations of the last refined solve (0: none needed)
   hdg::DBuf d_uint, d_errs;
   // Newton path: the iterate [interior cell-major | free skeleton], the
   // residual norms, and zero Dirichlet data for the corrections
   hdg::DBuf d_newton, d_rmax, d_dirzero;
   bool zero_dirichlet = false;
+  // general-space form (fields with their own spaces, hdg_problem_create_cartesian_spaces)
+  bool gs = false;
+  hdg::GsTables gst;
+  hdg::DBuf d_gstab;
   hdg::DBuf h_pinned;  // host staging
   cudaGraphExec_t pcg_graph = nullptr;
   int pcg_graph_chunk = 0;
@@ -252,8 +356,8 @@ struct hdg_problem {
             &d_dirvals, &d_A, &d_b, &d_S, &d_g, &d_fact, &d_info, &d_aux, &d_rowptr, &d_colind, &d_val,
             &d_rhs, &d_br_row0, &d_br_src, &d_blk_off, &d_blk_rowlen, &d_blk_src, &d_diag_blk, &d_dir_cells,
             &d_Binv, &d_x, &d_r, &d_z, &d_p, &d_p2, &d_q, &d_partials, &d_scal, &d_counter, &d_cellop,
-            &d_cell_blk, &d_qc, &d_Binv32, &d_v32, &d_scal2, &d_minv, &d_invm, &d_escratch, &d_l2ref_idx, &d_l2ref_val, &d_uint, &d_errs,
-            &d_newton, &d_rmax, &d_dirzero};
+            &d_cell_blk, &d_qc, &d_W, &d_v32, &d_scal2, &d_minv, &d_invm, &d_escratch, &d_l2ref_idx, &d_l2ref_val, &d_uint, &d_errs,
+            &d_newton, &d_rmax, &d_dirzero, &d_gstab};
   }
   ~hdg_problem();
 };

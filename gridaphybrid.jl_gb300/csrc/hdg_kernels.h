@@ -294,23 +294,28 @@ cudaError_t launch_spmv(const PcgArgs &a, cudaStream_t s, long long *launches);
 bool pcg_supports_nfd(int nfd);
 
 // Inner FP32 PCG of the mixed-precision skeleton solve (solves M e = rhs,
-// M = sign*A, with FP32 values and vectors; dot products in FP64).  M is
-// applied unassembled: per cell the upper triangle of facet blocks of
-// sign*(S_c + S_c^T)/2 in FP32, streamed with bulk async copies; the two
-// cells of a facet are summed in the update kernel.
+// M = sign*A, with FP32 values and vectors; dot products in float-float).
+// The facet-block-Jacobi preconditioner is applied by symmetric scaling: with
+// D_f = L_f L_f^T the Cholesky factor of each free facet's diagonal block and
+// W = blockdiag(L_f^{-1}), CG runs on M^ = W M W^T (unit diagonal blocks) for
+// y = W^{-T} e with right-hand side W rhs -- the same iterates as PCG with
+// the preconditioner D^{-1}, without reading D^{-1} every iteration (z = r).
+// M^ is applied unassembled: per cell the upper triangle of facet blocks of
+// W_a sign*(S_c + S_c^T)/2 W_b^T in FP32, streamed with bulk async copies;
+// the two cells of a facet are summed in the update kernel.
 struct Pcg32Args {
   int n, nfd, nblockrows;
-  const float *Binv32;
-  const double *rhs;  // inner right-hand side, already in the M frame
-  float *x, *r, *z, *p, *p2;
+  const double *W;    // nblockrows x nfd x nfd, row-major lower-triangular L_f^{-1}
+  const double *rhs;  // inner right-hand side (the outer residual, M frame, unscaled)
+  float *x, *r, *z, *p, *p2;  // z aliases r (identity preconditioner in the scaled frame)
   double *partials, *scal;
   unsigned int *counter;
   int nparts;             // grid of the vector kernels
   int ncells, nl, rec;    // rec: floats per cell record
   const float *blocks;    // ncells x rec
   const int *cell_blk;    // ncells x nl: 2*block row + (cell owns the facet), -1 on Dirichlet facets
-  const int *br_src;      // nblockrows x 2: cell*nl + local facet, second -1 on the boundary
-  float *qc;              // ncells x nl*nfd per-cell products
+  float *qc;              // nblockrows x 2 x nfd: the owner cell's product M^_c p_c on the block
+                          // row, then the other cell's (zero where the facet has one cell)
   int nstage, ctas;       // pipeline depth and grid of the streaming kernel
   unsigned int *error;    // set to 1 when a bulk copy never completed
   int uctas;              // grid of the update kernel (partials: 2 x uctas)
@@ -336,8 +341,13 @@ bool cellop_supported(int nl, int nfd);
 // pipeline depth and grid for the streaming kernel (sets its shared-memory limit)
 cudaError_t cellop_configure(int nl, int nfd, size_t smem_optin, int num_sms, int *nstage, int *ctas);
 // packs sign*(S_c + S_c^T)/2 (column-major FP64 cell blocks) into cell records
-cudaError_t launch_pack_cell_blocks(int ncells, int nl, int nfd, double sign, const double *S, float *out,
-                                    size_t smem_optin, cudaStream_t s, int num_sms, long long *launches);
+// W = blockdiag(L_f^{-1}) from the assembled FP64 diagonal blocks sign*D_f = L_f L_f^T (a block
+// that is not positive definite gets the identity)
+cudaError_t launch_block_chol_inv(const PcgArgs &a, double *W, cudaStream_t s, int num_sms, long long *launches);
+// the scaled FP32 cell records: per cell the upper facet blocks of W_a sign*(S_c + S_c^T)/2 W_b^T
+cudaError_t launch_pack_cell_blocks(int ncells, int nl, int nfd, double sign, const double *S, const int *cell_blk,
+                                    const double *W, float *out, size_t smem_optin, cudaStream_t s, int num_sms,
+                                    long long *launches);
 // Outer FP64 refinement: x, r = sign*rhs - M x with the FP64 matrix.
 struct OuterArgs {
   int n, nfd, nblockrows;
@@ -350,9 +360,8 @@ struct OuterArgs {
   unsigned int *counter;
   int nparts;
   double sign;
+  const double *W;  // the inner frame's scaling (x += W^T y), or null (x += y)
 };
-cudaError_t launch_binv_to_f32(size_t count, const double *Binv, float *Binv32, cudaStream_t s,
-                               long long *launches);
 cudaError_t launch_pcg32_init(const Pcg32Args &a, double eta, cudaStream_t s, long long *launches);
 cudaError_t launch_pcg32_iteration_pair(const Pcg32Args &a, cudaStream_t s, long long *launches);
 // residual replacement keeping the search direction (reliable update)
@@ -360,8 +369,10 @@ cudaError_t launch_pcg32_replace(const Pcg32Args &a, double eta, cudaStream_t s,
 // one unassembled SpMV (+ its dot product) as launched inside the inner PCG
 cudaError_t launch_pcg32_spmv(const Pcg32Args &a, cudaStream_t s, long long *launches);
 cudaError_t launch_outer_init(const OuterArgs &a, cudaStream_t s, long long *launches);
-// x += e, then r = c - M x and |r|^2
+// x += W^T e (x += e without W), then r = c - M x and |r|^2
 cudaError_t launch_outer_update(const OuterArgs &a, const float *e, cudaStream_t s, long long *launches);
+// x = xsaved + sign * x (x holds an FP64 correction e with A e = sign (c - A xsaved))
+cudaError_t launch_outer_combine(const OuterArgs &a, const double *xsaved, cudaStream_t s, long long *launches);
 // Size-class batching: one persistent fused integrate -> condense launch over
 // the cells of several problems of one (D, k) class.
 struct BatchProblem {

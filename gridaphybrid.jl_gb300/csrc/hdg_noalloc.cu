@@ -17,6 +17,9 @@
 // names a host-side stand-in).  The device address is looked up once per
 // device with cudaGetSymbolAddress, with that device current, on the first
 // call made on that device; make that first call before any stream capture.
+// Every call waits for its own work to finish (it synchronises the context's
+// stream to read the pivot flag) before it returns, and leaves the caller's
+// current device as it found it.
 // All calls share the one array: calls whose work overlaps on the GPU race
 // with each other and must be serialised by the caller (one stream, or
 // events).  The array keeps the contents of the last call; everything that
@@ -59,13 +62,10 @@ __global__ void noalloc_any_nonzero(int n, const int *__restrict__ info, int *fl
     if (info[i] != 0) atomicOr(flag, 1);
 }
 
-bool on_device(const void *p) {
-  cudaPointerAttributes at;
-  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
-    cudaGetLastError();
-    return false;
-  }
-  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+// Device memory of the context's GPU (or managed memory): the only pointers
+// this entry point takes.  Device memory of another GPU is refused too.
+bool on_ctx_device(const hdg_context *ctx, const void *p) {
+  return hdg::ptr_place(p, ctx->device) == hdg::PtrPlace::Device;
 }
 
 }  // namespace
@@ -89,9 +89,14 @@ extern "C" int hdg_static_condensation_noalloc(hdg_context *ctx, int ncells, int
                      ncells, n, n, need, kNoallocBytes);
   if (hdg::condense_mixed_smem(ni, nf) > ctx->smem_optin - 1024)
     return ctx->fail(HDG_ERR_INVALID, "cell block %zu x %zu exceeds the shared-memory condensation kernel", n, n);
-  if (!on_device(A) || !on_device(b) || !on_device(S) || !on_device(g) || (info && !on_device(info)))
-    return ctx->fail(HDG_ERR_INVALID, "hdg_static_condensation_noalloc takes device pointers only");
-  cudaError_t e = cudaSetDevice(ctx->device);
+  if (!on_ctx_device(ctx, A) || !on_ctx_device(ctx, b) || !on_ctx_device(ctx, S) || !on_ctx_device(ctx, g) ||
+      (info && !on_ctx_device(ctx, info)))
+    return ctx->fail(HDG_ERR_INVALID,
+                     "hdg_static_condensation_noalloc takes device pointers of the context's GPU (%d) only",
+                     ctx->device);
+  // the caller's current device is given back on every return below
+  hdg::DeviceGuard guard(ctx->device);
+  cudaError_t e = guard.status;
   void *base = nullptr;
   if (e == cudaSuccess) e = scratch_address(ctx->device, &base);
   if (e != cudaSuccess)

@@ -130,7 +130,8 @@ double footprint_bound(int D, int n, int k, int precision, int solver) {
     b += nfree * (nfree + 1) * 8.0 + ncells * 4.0 + nfree * 8.0;
   } else {
     b += 6 * nfree * 8.0 + nbr * s.nfd * s.nfd * 8.0;
-    if (fast) b += nbr * s.nfd * s.nfd * 4.0 + 5 * nfree * 4.0 + ncells * s.nf * 4.0;
+    // the inner frame's scaling W (FP64), inner vectors, products by block row
+    if (fast) b += nbr * s.nfd * s.nfd * 8.0 + 5 * nfree * 4.0 + 2 * nfree * 4.0;
   }
   // recovery and error norms
   b += ncells * s.ni * 8.0 + 2 * ncells * 8.0;

@@ -5,8 +5,11 @@
 //                  repeat: solve M e ~= r with the inner PCG; x += e;
 //                          r = c - M x with the FP64 matrix; until |r| <= rtol |c|
 //   inner (FP32):  facet-block-Jacobi PCG with FP32 vectors on the FP32
-//                  operator held as unassembled symmetric cell blocks; its dot
-//                  products accumulate in FP64.
+//                  operator held as unassembled symmetric cell blocks, the
+//                  preconditioner applied as a symmetric scaling of the
+//                  records (CG on W M W^T, W = blockdiag(L_f^{-1}) with
+//                  D_f = L_f L_f^T), so an iteration reads no block inverse;
+//                  its dot products accumulate in float-float.
 // GB300 executes FP64 at 1/62 of its FP32 rate, which makes even an FP64
 // SpMV arithmetic-bound; the inner iterations stay on the FP32 pipes and
 // stream about a quarter of the FP64 CSR bytes (FP32, upper blocks only),
@@ -19,61 +22,48 @@
 
 namespace hdg {
 
-// Binv32 = (float) Binv
-__global__ void binv_to_f32_kernel(size_t count, const double *__restrict__ Binv, float *Binv32) {
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < count; i += (size_t)gridDim.x * blockDim.x)
-    Binv32[i] = (float)Binv[i];
-}
-
-// z = Binv32 r for the rows of this CTA's tile (whole facet blocks, rows in smem)
-__device__ __forceinline__ float apply_binv32(const Pcg32Args &a, int row, float rval, float *rs) {
+// W rhs for the rows of this CTA's tile (whole facet blocks; the tile's rhs
+// values staged in shared memory); W is lower triangular.
+__device__ __forceinline__ double apply_w64(const Pcg32Args &a, int row, double v, double *rs) {
   const int nfd = a.nfd;
-  rs[threadIdx.x] = rval;
+  rs[threadIdx.x] = v;
   __syncthreads();
-  float z = 0.0f;
+  double y = 0.0;
   if (row < a.n) {
     const int br = row / nfd, i = row - br * nfd;
     const int first = (int)threadIdx.x - i;
-    const float *B = a.Binv32 + (size_t)br * nfd * nfd + (size_t)i * nfd;
-    for (int j = 0; j < nfd; ++j) z = fmaf(B[j], rs[first + j], z);
+    const double *Wr = a.W + (size_t)br * nfd * nfd + (size_t)i * nfd;
+    for (int j = 0; j <= i; ++j) y = fma(Wr[j], rs[first + j], y);
   }
   __syncthreads();
-  return z;
+  return y;
 }
 
-// inner start: x = 0, r = (float) rhs, z = Binv r, p = 0; scalars by the last CTA
+// inner start: x = 0, r = z = (float) W rhs, p = 0; scalars by the last CTA
 __global__ void __launch_bounds__(kPcgThreads) pcg32_init_kernel(Pcg32Args a, double eta) {
-  __shared__ float rs[kPcgThreads];
+  __shared__ double rs[kPcgThreads];
   __shared__ double red[32];
   const int tile = (kPcgThreads / a.nfd) * a.nfd;
-  double rz = 0.0, rr = 0.0;
+  double rr = 0.0;
   for (int base = blockIdx.x * tile; base < a.n; base += gridDim.x * tile) {
     const int row = base + (int)threadIdx.x;
     const bool act = threadIdx.x < (unsigned)tile && row < a.n;
-    float r = 0.0f;
+    const double y = apply_w64(a, act ? row : a.n, act ? a.rhs[row] : 0.0, rs);
     if (act) {
-      r = (float)a.rhs[row];
+      const float r = (float)y;
       a.x[row] = 0.0f;
       a.r[row] = r;
       a.p[row] = 0.0f;
       a.p2[row] = 0.0f;
       rr += (double)r * r;
     }
-    const float z = apply_binv32(a, act ? row : a.n, r, rs);
-    if (act) {
-      a.z[row] = z;
-      rz += (double)r * z;
-    }
   }
-  double s = block_sum(rz, red);
+  const double s = block_sum(rr, red);
   if (threadIdx.x == 0) a.partials[blockIdx.x] = s;
-  s = block_sum(rr, red);
-  if (threadIdx.x == 0) a.partials[a.nparts + blockIdx.x] = s;
   if (last_cta(a.counter)) {
-    const double vrz = sum_partials(a.partials, a.nparts, 0, red);
-    const double vrr = sum_partials(a.partials, a.nparts, 1, red);
+    const double vrr = sum_partials(a.partials, a.nparts, 0, red);
     if (threadIdx.x == 0) {
-      a.scal[SC_RZ] = vrz;
+      a.scal[SC_RZ] = vrr;
       a.scal[SC_RR] = vrr;
       a.scal[SC_BB] = vrr;
       a.scal[SC_TOL2] = eta * eta * vrr;
@@ -85,45 +75,37 @@ __global__ void __launch_bounds__(kPcgThreads) pcg32_init_kernel(Pcg32Args a, do
   }
 }
 
-// reliable update: the inner residual is replaced by the FP64 outer residual
-// (x = 0 again: the correction so far went into the FP64 iterate) and the
-// search direction p is kept, so the Krylov space is not thrown away:
-// z = Binv r, beta = (r,z)_new / (r,z) of the iteration before, and the next
-// SpMV forms p = z + beta p as in any other iteration.
+// reliable update: the inner residual is replaced by the (scaled) FP64 outer
+// residual (x = 0 again: the correction so far went into the FP64 iterate)
+// and the search direction p is kept, so the Krylov space is not thrown
+// away: beta = (r,r)_new / (r,r) of the iteration before, and the next SpMV
+// forms p = r + beta p as in any other iteration.
 __global__ void __launch_bounds__(kPcgThreads) pcg32_replace_kernel(Pcg32Args a, double eta) {
-  __shared__ float rs[kPcgThreads];
+  __shared__ double rs[kPcgThreads];
   __shared__ double red[32];
   const int tile = (kPcgThreads / a.nfd) * a.nfd;
-  double rz = 0.0, rr = 0.0;
+  double rr = 0.0;
   for (int base = blockIdx.x * tile; base < a.n; base += gridDim.x * tile) {
     const int row = base + (int)threadIdx.x;
     const bool act = threadIdx.x < (unsigned)tile && row < a.n;
-    float r = 0.0f;
+    const double y = apply_w64(a, act ? row : a.n, act ? a.rhs[row] : 0.0, rs);
     if (act) {
-      r = (float)a.rhs[row];
+      const float r = (float)y;
       a.x[row] = 0.0f;
       a.r[row] = r;
       rr += (double)r * r;
     }
-    const float z = apply_binv32(a, act ? row : a.n, r, rs);
-    if (act) {
-      a.z[row] = z;
-      rz += (double)r * z;
-    }
   }
-  double s = block_sum(rz, red);
+  const double s = block_sum(rr, red);
   if (threadIdx.x == 0) a.partials[blockIdx.x] = s;
-  s = block_sum(rr, red);
-  if (threadIdx.x == 0) a.partials[a.nparts + blockIdx.x] = s;
   if (last_cta(a.counter)) {
-    const double vrz = sum_partials(a.partials, a.nparts, 0, red);
-    const double vrr = sum_partials(a.partials, a.nparts, 1, red);
+    const double vrr = sum_partials(a.partials, a.nparts, 0, red);
     if (threadIdx.x == 0) {
-      // the update that ended the cycle stored beta = (r,z)_N / (r,z)_{N-1}
-      // and (r,z)_N; with r_N replaced, beta = (r,z)_new / (r,z)_{N-1}
+      // the update that ended the cycle stored beta = (r,r)_N / (r,r)_{N-1}
+      // and (r,r)_N; with r_N replaced, beta = (r,r)_new / (r,r)_{N-1}
       const double old = a.scal[SC_RZ];
-      a.scal[SC_BETA] = old != 0.0 ? a.scal[SC_BETA] * (vrz / old) : 0.0;
-      a.scal[SC_RZ] = vrz;
+      a.scal[SC_BETA] = old != 0.0 ? a.scal[SC_BETA] * (vrr / old) : 0.0;
+      a.scal[SC_RZ] = vrr;
       a.scal[SC_RR] = vrr;
       a.scal[SC_TOL2] = eta * eta * vrr;
       a.scal[SC_DONE] = (vrr == 0.0) ? 1.0 : 0.0;
@@ -132,35 +114,134 @@ __global__ void __launch_bounds__(kPcgThreads) pcg32_replace_kernel(Pcg32Args a,
   }
 }
 
+// W = blockdiag(L_f^{-1}): one warp per free facet, right-looking Cholesky of
+// sign*D_f in shared memory, then each lane forms one column of L^{-1} by
+// forward substitution.  A block that is not positive definite gets W = I.
+constexpr int kCholWarps = 4;
+__global__ void __launch_bounds__(32 * kCholWarps) block_chol_inv_kernel(PcgArgs a, double *W) {
+  extern __shared__ double csm[];  // kCholWarps x (L, L^{-1}) x nfd^2
+  const int nfd = a.nfd, nb = nfd * nfd;
+  const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+  double *L = csm + (size_t)wl * 2 * nb, *Li = L + nb;
+  for (int br = blockIdx.x * kCholWarps + wl; br < a.nblockrows; br += gridDim.x * kCholWarps) {
+    const int blk = a.diag_blk[br];
+    const int64_t off = a.blk_off[blk];
+    const int rl = a.blk_rowlen[blk];
+    for (int e = lane; e < nb; e += 32) {
+      const int i = e / nfd, j = e - i * nfd;
+      L[e] = a.sign * a.val[off + (int64_t)i * rl + j];
+    }
+    __syncwarp();
+    bool ok = true;
+    for (int c = 0; c < nfd; ++c) {
+      const double d = L[c * nfd + c];
+      if (!(d > 0.0) || !isfinite(d)) {  // the same value in every lane: a uniform exit
+        ok = false;
+        break;
+      }
+      const double sd = sqrt(d), inv = 1.0 / sd;
+      __syncwarp();
+      for (int i = c + 1 + lane; i < nfd; i += 32) L[i * nfd + c] *= inv;
+      if (lane == 0) L[c * nfd + c] = sd;
+      __syncwarp();
+      const int m = nfd - c - 1;
+      for (int e = lane; e < m * m; e += 32) {
+        const int i = c + 1 + e / m, j = c + 1 + e % m;
+        if (j <= i) L[i * nfd + j] -= L[i * nfd + c] * L[j * nfd + c];
+      }
+      __syncwarp();
+    }
+    if (ok)
+      for (int j = lane; j < nfd; j += 32)
+        for (int i = 0; i < nfd; ++i) {
+          if (i < j) {
+            Li[i * nfd + j] = 0.0;
+            continue;
+          }
+          double v = i == j ? 1.0 : 0.0;
+          for (int k = j; k < i; ++k) v -= L[i * nfd + k] * Li[k * nfd + j];
+          Li[i * nfd + j] = v / L[i * nfd + i];
+        }
+    __syncwarp();
+    double *out = W + (size_t)br * nb;
+    for (int e = lane; e < nb; e += 32) {
+      const int i = e / nfd, j = e - i * nfd;
+      out[e] = ok ? Li[e] : (i == j ? 1.0 : 0.0);
+    }
+    __syncwarp();
+  }
+}
+
 // ---------------------------------------------------------------------------
 // The unassembled FP32 operator.
 //
 // Cell record: the upper triangle of facet blocks (a <= b, row-major order of
-// (a, b)) of sign*(S_c + S_c^T)/2, each block nfd x nfd row-major, padded to a
-// multiple of four floats (16 bytes) so records can be bulk-copied.  The
-// symmetric storage streams 21/36 of the full 3D cell matrix; the lower
-// blocks are read transposed from shared memory.
-// ---------------------------------------------------------------------------
+// (a, b)) of the scaled cell operator W_a sign*(S_c + S_c^T)/2 W_b^T (W_f the
+// facet's L_f^{-1}, the identity on Dirichlet facets, whose rows the SpMV
+// skips), each block nfd x nfd row-major, padded to a multiple of four floats
+// (16 bytes) so records can be bulk-copied.  The symmetric storage streams
+// 21/36 of the full 3D cell matrix; the lower blocks are read transposed from
+// shared memory.  The two triangular products run in FP32 from the FP64
+// symmetric part.
+__device__ __forceinline__ void upper_block(int nl, int blk, int &lo, int &hi) {
+  int l = 0, rem = blk;
+  while (rem >= nl - l) {
+    rem -= nl - l;
+    ++l;
+  }
+  lo = l;
+  hi = l + rem;
+}
+
 __global__ void pack_cell_blocks_kernel(int ncells, int nl, int nfd, int rec, double sign,
-                                        const double *__restrict__ S, float *__restrict__ out) {
-  extern __shared__ double Ss[];
+                                        const double *__restrict__ S, const int *__restrict__ cell_blk,
+                                        const double *__restrict__ W, float *__restrict__ out) {
+  extern __shared__ double Ss[];  // nf^2 doubles, then nl nb + 2 nblk nb floats
   const int nf = nl * nfd, nb = nfd * nfd, nblk = nl * (nl + 1) / 2;
+  float *Ws = reinterpret_cast<float *>(Ss + (size_t)nf * nf);
+  float *Ts = Ws + nl * nb;    // the FP32 symmetric part sign (S + S^T)/2 of every upper block
+  float *Us = Ts + nblk * nb;  // T W_hi^T
   for (int c = blockIdx.x; c < ncells; c += gridDim.x) {
     const double *Sc = S + (size_t)c * nf * nf;
     for (int e = threadIdx.x; e < nf * nf; e += blockDim.x) Ss[e] = Sc[e];
+    for (int e = threadIdx.x; e < nl * nb; e += blockDim.x) {
+      const int lf = e / nb, w = e - lf * nb, r = w / nfd, q = w - r * nfd;
+      const int ent = cell_blk[(size_t)c * nl + lf];
+      Ws[e] = ent >= 0 ? (float)W[(size_t)(ent >> 1) * nb + w] : (r == q ? 1.0f : 0.0f);
+    }
     __syncthreads();
+    // T[blk][p][q] = sign (S(lo p, hi q) + S(hi q, lo p)) / 2
+    for (int e = threadIdx.x; e < nblk * nb; e += blockDim.x) {
+      const int blk = e / nb, w = e - blk * nb, p = w / nfd, q = w - p * nfd;
+      int lo, hi;
+      upper_block(nl, blk, lo, hi);
+      const int i = lo * nfd + p, j = hi * nfd + q;
+      Ts[e] = (float)(0.5 * sign * (Ss[i + (size_t)nf * j] + Ss[j + (size_t)nf * i]));
+    }
+    __syncthreads();
+    // U[blk][p][s] = sum_{q <= s} T[blk][p][q] W_hi[s][q]
+    for (int e = threadIdx.x; e < nblk * nb; e += blockDim.x) {
+      const int blk = e / nb, w = e - blk * nb, p = w / nfd, sc = w - p * nfd;
+      int lo, hi;
+      upper_block(nl, blk, lo, hi);
+      const float *Wh = Ws + hi * nb + sc * nfd;
+      const float *T = Ts + blk * nb + p * nfd;
+      float u = 0.0f;
+      for (int q = 0; q <= sc; ++q) u = fmaf(T[q], Wh[q], u);
+      Us[e] = u;
+    }
+    __syncthreads();
+    // record[blk][r][s] = sum_{p <= r} W_lo[r][p] U[blk][p][s]
     float *o = out + (size_t)c * rec;
     for (int e = threadIdx.x; e < rec; e += blockDim.x) {
       float v = 0.0f;
       if (e < nblk * nb) {
-        const int blk = e / nb, w = e - blk * nb, r = w / nfd, s = w - r * nfd;
-        int lo = 0, rem = blk;
-        while (rem >= nl - lo) {
-          rem -= nl - lo;
-          ++lo;
-        }
-        const int i = lo * nfd + r, j = (lo + rem) * nfd + s;
-        v = (float)(0.5 * sign * (Ss[i + (size_t)nf * j] + Ss[j + (size_t)nf * i]));
+        const int blk = e / nb, w = e - blk * nb, r = w / nfd, sc = w - r * nfd;
+        int lo, hi;
+        upper_block(nl, blk, lo, hi);
+        const float *Wl = Ws + lo * nb + r * nfd;
+        const float *U = Us + blk * nb + sc;
+        for (int p = 0; p <= r; ++p) v = fmaf(Wl[p], U[p * nfd], v);
       }
       o[e] = v;
     }
@@ -172,31 +253,44 @@ __global__ void pack_cell_blocks_kernel(int ncells, int nl, int nfd, int rec, do
 // shared memory several times over): one work item per (cell, upper block),
 // the block and its transposed partner staged as two nfd x nfd tiles.
 __global__ void pack_cell_blocks_tiled_kernel(int ncells, int nl, int nfd, int rec, double sign,
-                                              const double *__restrict__ S, float *__restrict__ out) {
-  extern __shared__ double T[];  // 2 nfd^2
+                                              const double *__restrict__ S, const int *__restrict__ cell_blk,
+                                              const double *__restrict__ W, float *__restrict__ out) {
+  extern __shared__ double T[];  // 2 nb doubles, then 3 nb floats
   const int nf = nl * nfd, nb = nfd * nfd, nblk = nl * (nl + 1) / 2;
   double *T1 = T, *T2 = T + nb;
+  float *Wl = reinterpret_cast<float *>(T + 2 * nb), *Wh = Wl + nb, *U = Wh + nb;
   const long long items = (long long)ncells * nblk;
   for (long long it = blockIdx.x; it < items; it += gridDim.x) {
     const int c = (int)(it / nblk), blk = (int)(it - (long long)c * nblk);
-    int lo = 0, rem = blk;
-    while (rem >= nl - lo) {
-      rem -= nl - lo;
-      ++lo;
-    }
-    const int hi = lo + rem;
+    int lo, hi;
+    upper_block(nl, blk, lo, hi);
     const double *Sc = S + (size_t)c * nf * nf;
+    const int el = cell_blk[(size_t)c * nl + lo], eh = cell_blk[(size_t)c * nl + hi];
     // T1[r + nfd s] = S(lo nfd + r, hi nfd + s), T2[r + nfd s] = S(hi nfd + r, lo nfd + s)
     for (int e = threadIdx.x; e < nb; e += blockDim.x) {
-      const int s = e / nfd, r = e - s * nfd;
-      T1[e] = Sc[(size_t)(lo * nfd + r) + (size_t)nf * (hi * nfd + s)];
-      T2[e] = Sc[(size_t)(hi * nfd + r) + (size_t)nf * (lo * nfd + s)];
+      const int sc = e / nfd, r = e - sc * nfd;
+      T1[e] = Sc[(size_t)(lo * nfd + r) + (size_t)nf * (hi * nfd + sc)];
+      T2[e] = Sc[(size_t)(hi * nfd + r) + (size_t)nf * (lo * nfd + sc)];
+      const int wr = e / nfd, wc = e - wr * nfd;  // row-major W index
+      Wl[e] = el >= 0 ? (float)W[(size_t)(el >> 1) * nb + e] : (wr == wc ? 1.0f : 0.0f);
+      Wh[e] = eh >= 0 ? (float)W[(size_t)(eh >> 1) * nb + e] : (wr == wc ? 1.0f : 0.0f);
+    }
+    __syncthreads();
+    // U[p][s] = sum_{q <= s} sign (S(lo p, hi q) + S(hi q, lo p))/2 W_hi[s][q]
+    for (int e = threadIdx.x; e < nb; e += blockDim.x) {
+      const int p = e / nfd, sc = e - p * nfd;
+      float u = 0.0f;
+      for (int q = 0; q <= sc; ++q)
+        u = fmaf((float)(0.5 * sign * (T1[p + nfd * q] + T2[q + nfd * p])), Wh[sc * nfd + q], u);
+      U[e] = u;
     }
     __syncthreads();
     float *o = out + (size_t)c * rec + (size_t)blk * nb;
     for (int w = threadIdx.x; w < nb; w += blockDim.x) {
-      const int r = w / nfd, s = w - r * nfd;
-      o[w] = (float)(0.5 * sign * (T1[r + nfd * s] + T2[s + nfd * r]));
+      const int r = w / nfd, sc = w - r * nfd;
+      float v = 0.0f;
+      for (int p = 0; p <= r; ++p) v = fmaf(Wl[r * nfd + p], U[p * nfd + sc], v);
+      o[w] = v;
     }
     if (blk == nblk - 1)  // the record's padding
       for (int e = nblk * nb + threadIdx.x; e < rec; e += blockDim.x) out[(size_t)c * rec + e] = 0.0f;
@@ -273,6 +367,7 @@ __global__ void __launch_bounds__(CellOp<NL, NFD>::THREADS, 2)
     const int slot = t % nstage;
     const int c = ((int)blockIdx.x + t * (int)gridDim.x) * C::CPS + g;
     const bool act = i < C::NF && c < a.ncells;
+    const int ent = ent_a;  // this stage's block-row entry (ent_a moves on below)
     float pv = 0.0f;
     if (ent_a >= 0) {
       pv = fmaf(beta, po_a, z_a);
@@ -337,7 +432,8 @@ __global__ void __launch_bounds__(CellOp<NL, NFD>::THREADS, 2)
           for (int s = 0; s < NFD; ++s) q = fmaf(Bb[s * st], ps[g][b * NFD + s], q);
         }
       }
-      a.qc[(size_t)c * C::NF + i] = q;
+      // by block row: the owner's product first, then the other cell's
+      if (ent >= 0) a.qc[(size_t)(ent >> 1) * (2 * NFD) + ((ent & 1) ? 0 : NFD) + r] = q;
       acc.add_prod(pv, q);
     }
     __syncthreads();  // the slot and ps are free again
@@ -359,87 +455,41 @@ __global__ void __launch_bounds__(CellOp<NL, NFD>::THREADS, 2)
   }
 }
 
-// q = qc(owner) + qc(other) per free row; x += alpha p; r -= alpha q;
-// z = Binv r with the tile's block inverses staged in shared memory; beta;
-// convergence against eta |rhs|.  The row's loads (source cells, p, x, r)
-// are issued together, so a tile costs two dependent memory round trips
-// (source cells, then their products); the grid (a.uctas, up to eight CTAs
-// per SM) keeps enough tiles in flight to hide them.
+// q = qc(owner) + qc(other) per free row; x += alpha p; r -= alpha q; z = r
+// (the preconditioner is in the scaled records); beta; convergence against
+// eta |rhs|.  Every load of a row is independent of the others (the products
+// sit by block row), so a row costs one memory round trip; rows are spread
+// over the grid (a.uctas CTAs, up to eight per SM) with a grid-stride loop.
 static_assert(kPcgThreads == kPcgThreadsHost, "host and device PCG block sizes differ");
-
-// 4-byte global -> shared copy that does not stall the issuing thread
-__device__ __forceinline__ void cp_async4(float *dst, const float *src) {
-  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-  const size_t g = __cvta_generic_to_global(src);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(g) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit_wait_all() {
-  asm volatile("cp.async.commit_group;\ncp.async.wait_all;\n" ::: "memory");
-}
 static_assert(kMaxRowLen == kMaxSkeletonRowLen, "host and device skeleton row limits differ");
 
 template <int NFD>
-__global__ void __launch_bounds__(kPcgThreads) pcg32_update_cells_kernel(Pcg32Args a, const float *__restrict__ p) {
-  constexpr int BPT = kPcgThreads / NFD;  // block rows per tile
-  __shared__ float rs[kPcgThreads];
-  __shared__ float Bs[BPT * NFD * NFD];
+__global__ void __launch_bounds__(kPcgThreads) pcg32_update_rows_kernel(Pcg32Args a, const float *__restrict__ p) {
   __shared__ float2 redf[32];
   if (a.scal[SC_DONE] != 0.0) return;
   const float alpha = (float)a.scal[SC_ALPHA];
-  const int lb = threadIdx.x / NFD, i = threadIdx.x - lb * NFD;
   const float *__restrict__ qc = a.qc;
   float *__restrict__ xg = a.x;
   float *__restrict__ rg = a.r;
-  FFSum rz, rr;  // float-float: no FP64 in the per-row or per-CTA sums
-  for (int br0 = blockIdx.x * BPT; br0 < a.nblockrows; br0 += gridDim.x * BPT) {
-    const int nb = min(BPT, a.nblockrows - br0);
-    const bool act = lb < nb;
-    const int br = br0 + lb, row = br * NFD + i;
-    int2 src = make_int2(0, -1);
-    float pv = 0.0f, xv = 0.0f, r0 = 0.0f;
-    if (act) {
-      src = __ldg(reinterpret_cast<const int2 *>(a.br_src) + br);
-      pv = p[row];
-      xv = xg[row];
-      r0 = rg[row];
-    }
-    // the tile's block inverses: asynchronous 4-byte copies, all in flight at once
-    const float *Bg = a.Binv32 + (size_t)br0 * NFD * NFD;
-    for (int e = threadIdx.x; e < nb * NFD * NFD; e += blockDim.x) cp_async4(Bs + e, Bg + e);
-    float rv = 0.0f;
-    if (act) {
-      float q = qc[(size_t)src.x * NFD + i];
-      if (src.y >= 0) q += qc[(size_t)src.y * NFD + i];
-      xg[row] = fmaf(alpha, pv, xv);
-      rv = fmaf(-alpha, q, r0);
-      rg[row] = rv;
-      rr.add_prod(rv, rv);
-    }
-    rs[threadIdx.x] = rv;
-    cp_async_commit_wait_all();
-    __syncthreads();
-    if (act) {
-      const float *B = Bs + lb * NFD * NFD + i * NFD;
-      const float *rl = rs + lb * NFD;
-      float z = 0.0f;
-#pragma unroll
-      for (int j = 0; j < NFD; ++j) z = fmaf(B[j], rl[j], z);
-      a.z[row] = z;
-      rz.add_prod(rv, z);
-    }
-    __syncthreads();
+  FFSum rr;  // float-float: no FP64 in the per-row or per-CTA sums
+  for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < a.n; row += gridDim.x * blockDim.x) {
+    const int br = row / NFD, i = row - br * NFD;
+    const float *qb = qc + (size_t)br * (2 * NFD) + i;
+    const float q0 = qb[0], q1 = qb[NFD];
+    const float pv = p[row], xv = xg[row], r0 = rg[row];
+    xg[row] = fmaf(alpha, pv, xv);
+    const float rv = fmaf(-alpha, q0 + q1, r0);
+    rg[row] = rv;
+    rr.add_prod(rv, rv);
   }
   const int np = (int)gridDim.x;
-  float2 s = block_sum_ff(rz.hi, rz.lo, redf);
+  const float2 s = block_sum_ff(rr.hi, rr.lo, redf);
   if (threadIdx.x == 0) store_partial_ff(a.partials, np, 0, s);
-  s = block_sum_ff(rr.hi, rr.lo, redf);
-  if (threadIdx.x == 0) store_partial_ff(a.partials, np, 1, s);
   if (last_cta(a.counter)) {
-    const double vrz = sum_partials_ff(a.partials, np, 0, redf);
-    const double vrr = sum_partials_ff(a.partials, np, 1, redf);
+    const double vrr = sum_partials_ff(a.partials, np, 0, redf);
     if (threadIdx.x == 0) {
-      a.scal[SC_BETA] = vrz / a.scal[SC_RZ];
-      a.scal[SC_RZ] = vrz;
+      a.scal[SC_BETA] = vrr / a.scal[SC_RZ];
+      a.scal[SC_RZ] = vrr;
       a.scal[SC_RR] = vrr;
       a.scal[SC_ITERS] += 1.0;
       if (vrr <= a.scal[SC_TOL2] || !(vrr == vrr)) a.scal[SC_DONE] = 1.0;
@@ -477,6 +527,24 @@ __global__ void __launch_bounds__(kPcgThreads) outer_init_kernel(OuterArgs a) {
 // x += e (the inner correction)
 __global__ void outer_axpy_kernel(int n, const float *__restrict__ e, double *x) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x[i] += (double)e[i];
+}
+
+// x += W^T y: the inner correction y back from the scaled frame (W lower
+// triangular per facet block: row i of W^T is column i of W, entries j >= i)
+__global__ void outer_axpy_scaled_kernel(int n, int nfd, const double *__restrict__ W, const float *__restrict__ y,
+                                         double *x) {
+  for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < n; row += gridDim.x * blockDim.x) {
+    const int br = row / nfd, i = row - br * nfd;
+    const double *Wb = W + (size_t)br * nfd * nfd;
+    const float *yb = y + (size_t)br * nfd;
+    double e = 0.0;
+    for (int j = i; j < nfd; ++j) e = fma(Wb[j * nfd + i], (double)yb[j], e);
+    x[row] += e;
+  }
+}
+
+__global__ void outer_combine_kernel(int n, const double *__restrict__ xs, double sign, double *x) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x[i] = xs[i] + sign * x[i];
 }
 
 // r = c - M x with the FP64 matrix (block-row gather of x), |r|^2
@@ -527,12 +595,16 @@ __global__ void __launch_bounds__(kPcgThreads) outer_residual_kernel(OuterArgs a
 // ---------------------------------------------------------------------------
 // Launchers
 // ---------------------------------------------------------------------------
-cudaError_t launch_binv_to_f32(size_t count, const double *Binv, float *Binv32, cudaStream_t s,
-                               long long *launches) {
-  size_t g = (count + 255) / 256;
-  if (g > 4096) g = 4096;
-  if (g < 1) g = 1;
-  binv_to_f32_kernel<<<(int)g, 256, 0, s>>>(count, Binv, Binv32);
+cudaError_t launch_block_chol_inv(const PcgArgs &a, double *W, cudaStream_t s, int num_sms, long long *launches) {
+  if (a.nfd > 32 || a.nblockrows < 1) return a.nblockrows < 1 ? cudaSuccess : cudaErrorInvalidValue;
+  const size_t smem = sizeof(double) * kCholWarps * 2 * a.nfd * a.nfd;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(block_chol_inv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  int g = (a.nblockrows + kCholWarps - 1) / kCholWarps;
+  if (g > num_sms * 16) g = num_sms * 16;
+  block_chol_inv_kernel<<<g, 32 * kCholWarps, smem, s>>>(a, W);
   ++*launches;
   return cudaGetLastError();
 }
@@ -604,17 +676,19 @@ cudaError_t cellop_configure(int nl, int nfd, size_t smem_optin, int num_sms, in
   return cudaErrorInvalidValue;
 }
 
-cudaError_t launch_pack_cell_blocks(int ncells, int nl, int nfd, double sign, const double *S, float *out,
-                                    size_t smem_optin, cudaStream_t s, int num_sms, long long *launches) {
-  const int nf = nl * nfd;
-  const size_t smem = sizeof(double) * nf * nf;
+cudaError_t launch_pack_cell_blocks(int ncells, int nl, int nfd, double sign, const double *S, const int *cell_blk,
+                                    const double *W, float *out, size_t smem_optin, cudaStream_t s, int num_sms,
+                                    long long *launches) {
+  const int nf = nl * nfd, nb = nfd * nfd, nblk = nl * (nl + 1) / 2;
+  const size_t smem = sizeof(double) * nf * nf + sizeof(float) * (size_t)(nl + 2 * nblk) * nb;
   if (smem > 64 * 1024) {  // large cells: block-pair tiles
-    const size_t tsmem = 2 * sizeof(double) * nfd * nfd;
+    const size_t tsmem = 2 * sizeof(double) * nb + 3 * sizeof(float) * nb;
     if (tsmem > 48 * 1024) return cudaErrorInvalidValue;
-    const long long items = (long long)ncells * (nl * (nl + 1) / 2);
+    const long long items = (long long)ncells * nblk;
     long long grid = items < (long long)num_sms * 16 ? items : (long long)num_sms * 16;
     if (grid < 1) grid = 1;
-    pack_cell_blocks_tiled_kernel<<<(int)grid, 256, tsmem, s>>>(ncells, nl, nfd, cellop_rec(nl, nfd), sign, S, out);
+    pack_cell_blocks_tiled_kernel<<<(int)grid, 256, tsmem, s>>>(ncells, nl, nfd, cellop_rec(nl, nfd), sign, S,
+                                                                 cell_blk, W, out);
     ++*launches;
     return cudaGetLastError();
   }
@@ -622,7 +696,7 @@ cudaError_t launch_pack_cell_blocks(int ncells, int nl, int nfd, double sign, co
   if (e != cudaSuccess) return e;
   int grid = ncells < num_sms * 16 ? ncells : num_sms * 16;
   if (grid < 1) grid = 1;
-  pack_cell_blocks_kernel<<<grid, 256, smem, s>>>(ncells, nl, nfd, cellop_rec(nl, nfd), sign, S, out);
+  pack_cell_blocks_kernel<<<grid, 256, smem, s>>>(ncells, nl, nfd, cellop_rec(nl, nfd), sign, S, cell_blk, W, out);
   ++*launches;
   return cudaGetLastError();
 }
@@ -635,9 +709,9 @@ static void cell_spmv(const Pcg32Args &a, const float *po, float *pn, cudaStream
 template <int NL, int NFD>
 static void pcg32_pair(const Pcg32Args &a, cudaStream_t s) {
   cell_spmv<NL, NFD>(a, a.p, a.p2, s);
-  pcg32_update_cells_kernel<NFD><<<a.uctas, kPcgThreads, 0, s>>>(a, a.p2);
+  pcg32_update_rows_kernel<NFD><<<a.uctas, kPcgThreads, 0, s>>>(a, a.p2);
   cell_spmv<NL, NFD>(a, a.p2, a.p, s);
-  pcg32_update_cells_kernel<NFD><<<a.uctas, kPcgThreads, 0, s>>>(a, a.p);
+  pcg32_update_rows_kernel<NFD><<<a.uctas, kPcgThreads, 0, s>>>(a, a.p);
 }
 
 cudaError_t launch_pcg32_iteration_pair(const Pcg32Args &a, cudaStream_t s, long long *launches) {
@@ -670,11 +744,23 @@ cudaError_t launch_outer_init(const OuterArgs &a, cudaStream_t s, long long *lau
   return cudaGetLastError();
 }
 
+cudaError_t launch_outer_combine(const OuterArgs &a, const double *xsaved, cudaStream_t s, long long *launches) {
+  int g = (a.n + 255) / 256;
+  if (g > 4096) g = 4096;
+  if (g < 1) g = 1;
+  outer_combine_kernel<<<g, 256, 0, s>>>(a.n, xsaved, a.sign, a.x);
+  ++*launches;
+  return cudaGetLastError();
+}
+
 cudaError_t launch_outer_update(const OuterArgs &a, const float *e, cudaStream_t s, long long *launches) {
   int g = (a.n + 255) / 256;
   if (g > 4096) g = 4096;
   if (g < 1) g = 1;
-  outer_axpy_kernel<<<g, 256, 0, s>>>(a.n, e, a.x);
+  if (a.W)
+    outer_axpy_scaled_kernel<<<g, 256, 0, s>>>(a.n, a.nfd, a.W, e, a.x);
+  else
+    outer_axpy_kernel<<<g, 256, 0, s>>>(a.n, e, a.x);
   switch (a.nfd) {
     case 2: outer_residual_kernel<2><<<a.nparts, kPcgThreads, 0, s>>>(a); break;
     case 3: outer_residual_kernel<3><<<a.nparts, kPcgThreads, 0, s>>>(a); break;

@@ -3,9 +3,10 @@
 // barrier, the update phase, a grid barrier -- no kernel boundaries, no
 // pipeline refills.  The same arithmetic as the two-kernel iteration
 // (cell_spmv32_kernel + pcg32_update_cells_kernel):
-//   SpMV:   p = z + beta p_old (owner writes), qc_c = M_c p_c, partial (p, Ap)
-//   update: q = qc(owner) + qc(other), x += alpha p, r -= alpha q, z = Binv r,
-//           partial (r, z), (r, r)
+//   SpMV:   p = r + beta p_old (owner writes), qc = M^_c p_c by block row,
+//           partial (p, Ap)
+//   update: q = qc(owner) + qc(other), x += alpha p, r -= alpha q (z = r: the
+//           preconditioner is a scaling of the records), partial (r, r)
 // Every CTA sums the per-CTA partials itself in one fixed order after each
 // barrier (so all CTAs hold the same alpha, beta and convergence decision,
 // and the result does not depend on timing).  The cell records of a CTA are
@@ -33,15 +34,6 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
   unsigned v;
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
-}
-
-__device__ __forceinline__ void cp_async4p(float *dst, const float *src) {
-  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-  const size_t g = __cvta_generic_to_global(src);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(g) : "memory");
-}
-__device__ __forceinline__ void cp_async_wait_allp() {
-  asm volatile("cp.async.commit_group;\ncp.async.wait_all;\n" ::: "memory");
 }
 
 // Grid-wide barrier of a co-resident grid: arrive on count; the last arriver
@@ -94,12 +86,9 @@ template <int NL, int NFD>
 __global__ void __launch_bounds__(kPcgThreads) pcg32_persistent_kernel(Pcg32Args a, int iter_cap) {
   constexpr int NF = NL * NFD;
   constexpr int TPC = cellop_tpc(NF), CPS = cellop_cps(NF), REC = cellop_rec(NL, NFD);
-  constexpr int BPT = kPcgThreads / NFD;  // block rows per update tile
   extern __shared__ __align__(128) float ring[];
   __shared__ __align__(8) uint64_t bars[kPersistStagesMax];
   __shared__ __align__(16) float ps[CPS][TPC];
-  __shared__ float rs[kPcgThreads];
-  __shared__ float Bs[BPT * NFD * NFD];
   __shared__ double red[32];
   __shared__ int flag, abort_flag;
   if (a.scal[SC_DONE] != 0.0) return;
@@ -113,9 +102,6 @@ __global__ void __launch_bounds__(kPcgThreads) pcg32_persistent_kernel(Pcg32Args
   const bool spmv_thread = threadIdx.x < CPS * TPC;
   const int nunits = (a.ncells + CPS - 1) / CPS;
   const int mine = (int)blockIdx.x < nunits ? (nunits - 1 - (int)blockIdx.x) / G + 1 : 0;
-  // update work: tiles of BPT block rows, round-robin
-  const int ntiles = (a.nblockrows + BPT - 1) / BPT;
-  const int lb = threadIdx.x / NFD, ri = threadIdx.x - lb * NFD;
   uint64_t pol = 0;
   long long issued = 0;  // stages issued (thread 0); stage s holds the records of unit s % mine
   auto issue = [&](long long s) {
@@ -164,8 +150,9 @@ __global__ void __launch_bounds__(kPcgThreads) pcg32_persistent_kernel(Pcg32Args
       const int c = ((int)blockIdx.x + s * G) * CPS + g;
       const bool act = spmv_thread && i < NF && c < a.ncells;
       float pv = 0.0f;
+      int ent = -1;
       if (act) {
-        const int ent = a.cell_blk[(size_t)c * NL + lf];
+        ent = a.cell_blk[(size_t)c * NL + lf];
         if (ent >= 0) {  // p_old and z were written by other CTAs: read through L2
           const int row = (ent >> 1) * NFD + r;
           pv = fmaf(fbeta, __ldcg(p_old + row), __ldcg(a.z + row));
@@ -216,7 +203,7 @@ __global__ void __launch_bounds__(kPcgThreads) pcg32_persistent_kernel(Pcg32Args
             for (int k = 0; k < NFD; ++k) q = fmaf(Bb[k * st], ps[g][b * NFD + k], q);
           }
         }
-        a.qc[(size_t)c * NF + i] = q;
+        if (ent >= 0) a.qc[(size_t)(ent >> 1) * (2 * NFD) + ((ent & 1) ? 0 : NFD) + r] = q;
         acc += (double)pv * q;
       }
       __syncthreads();  // the slot and ps are free again: refill with a later stage's records
@@ -235,46 +222,20 @@ __global__ void __launch_bounds__(kPcgThreads) pcg32_persistent_kernel(Pcg32Args
     const double pq = sum_all(a.partials, G, red);
     const double alpha_d = rz / pq;
     const float alpha = (float)alpha_d;
-    // ---- update phase
-    double rzn = 0.0, rr = 0.0;
-    for (int tile = blockIdx.x; tile < ntiles; tile += G) {
-      const int br0 = tile * BPT;
-      const int nb = min(BPT, a.nblockrows - br0);
-      const bool act = lb < nb;
-      const int br = br0 + lb, row = br * NFD + ri;
-      int2 src = make_int2(0, -1);
-      float pv = 0.0f, xv = 0.0f, r0 = 0.0f;
-      if (act) {  // p_new comes from other CTAs (L2); x and r only ever from this CTA's tiles
-        src = __ldg(reinterpret_cast<const int2 *>(a.br_src) + br);
-        pv = __ldcg(p_new + row);
-        xv = a.x[row];
-        r0 = a.r[row];
-      }
-      const float *Bg = a.Binv32 + (size_t)br0 * NFD * NFD;
-      for (int e = threadIdx.x; e < nb * NFD * NFD; e += blockDim.x) cp_async4p(Bs + e, Bg + e);
-      float rv = 0.0f;
-      if (act) {
-        float q = __ldcg(a.qc + (size_t)src.x * NFD + ri);
-        if (src.y >= 0) q += __ldcg(a.qc + (size_t)src.y * NFD + ri);
-        a.x[row] = fmaf(alpha, pv, xv);
-        rv = fmaf(-alpha, q, r0);
-        a.r[row] = rv;
-        rr += (double)rv * rv;
-      }
-      rs[threadIdx.x] = rv;
-      cp_async_wait_allp();
-      __syncthreads();
-      if (act) {
-        const float *Bm = Bs + lb * NFD * NFD + ri * NFD;
-        const float *rl = rs + lb * NFD;
-        float z = 0.0f;
-#pragma unroll
-        for (int j = 0; j < NFD; ++j) z = fmaf(Bm[j], rl[j], z);
-        a.z[row] = z;
-        rzn += (double)rv * z;
-      }
-      __syncthreads();
+    // ---- update phase: rows round-robin over the grid (the same rows every
+    // iteration, so x and r are only ever touched by this CTA)
+    double rr = 0.0;
+    for (int row = blockIdx.x * kPcgThreads + threadIdx.x; row < a.n; row += G * kPcgThreads) {
+      const int br = row / NFD, ri = row - br * NFD;
+      const float *qb = a.qc + (size_t)br * (2 * NFD) + ri;
+      const float q = __ldcg(qb) + __ldcg(qb + NFD);  // written by other CTAs: read through L2
+      const float pv = __ldcg(p_new + row);
+      a.x[row] = fmaf(alpha, pv, a.x[row]);
+      const float rv = fmaf(-alpha, q, a.r[row]);
+      a.r[row] = rv;
+      rr += (double)rv * rv;
     }
+    const double rzn = rr;
     double s1 = block_sum(rzn, red);
     if (threadIdx.x == 0) a.partials[G + blockIdx.x] = s1;
     s1 = block_sum(rr, red);

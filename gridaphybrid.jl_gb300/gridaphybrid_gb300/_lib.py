@@ -5,6 +5,7 @@ present, every call raises.
 """
 import ctypes
 import os
+import re
 import weakref
 
 import numpy as np
@@ -35,6 +36,23 @@ HDG_EPROBLEM_SMOOTH = 1
 HDG_SOLVER_PCG = 0
 HDG_SOLVER_DIRECT = 1
 
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))),
+                      "include", "hdg_gb300.h")
+
+
+def _header_bytes_constant(name):
+    """A byte-size macro of the C header, e.g. `#define NAME (32u * 1024u * 1024u)`."""
+    with open(HEADER) as f:
+        m = re.search(r"#define\s+%s\s+\(([^)]*)\)" % name, f.read())
+    val = 1
+    for factor in m.group(1).split("*"):
+        val *= int(factor.strip().rstrip("uU"))
+    return val
+
+
+# Size of the fixed scratch array of hdg_static_condensation_noalloc.
+HDG_NOALLOC_SCRATCH_BYTES = _header_bytes_constant("HDG_NOALLOC_SCRATCH_BYTES")
+
 _ERR_NAMES = {
     1: "HDG_ERR_INVALID", 2: "HDG_ERR_CUDA", 3: "HDG_ERR_NOMEM", 4: "HDG_ERR_SINGULAR",
     5: "HDG_ERR_NOT_CONVERGED", 6: "HDG_ERR_STATE", 7: "HDG_ERR_NODEVICE",
@@ -47,6 +65,8 @@ _d = ctypes.c_double
 _ll = ctypes.c_longlong
 SIGNATURES = {
     "hdg_version": (_i, []),
+    "hdg_device_allocations": (_i, [ctypes.POINTER(_ll)]),
+    "hdg_pointer_placement": (_i, [_i, _i, _i, ctypes.POINTER(_i)]),
     "hdg_context_create": (_i, [_i, ctypes.POINTER(_vp)]),
     "hdg_context_destroy": (_i, [_vp]),
     "hdg_last_error": (ctypes.c_char_p, [_vp]),
@@ -78,8 +98,10 @@ SIGNATURES = {
     "hdg_l2_errors": (_i, [_vp, _vp, _vp]),
     "hdg_solve": (_i, [_vp, _i, _i, _d, _i, _vp, _vp, _vp]),
     "hdg_get_timings": (_i, [_vp, _vp]),
+    "hdg_get_solve_stats": (_i, [_vp, _vp]),
     "hdg_context_set_persistent_pcg": (_i, [_vp, ctypes.c_int]),
     "hdg_time_kernel": (_i, [_vp, _i, _i, _vp]),
+    "hdg_measure_pipe_peaks": (_i, [_vp, _vp, _vp]),
     "hdg_problem_device_bytes": (_i, [_vp, _vp]),
     "hdg_set_refinement": (_i, [_vp, _d, _i]),
     "hdg_newton_solve": (_i, [_vp, _i, _d, _i, _d, _i, _vp, _vp, _vp]),

@@ -81,6 +81,20 @@ typedef struct hdg_problem hdg_problem;
 /* Library version (major*10000 + minor*100 + patch). */
 int hdg_version(void);
 
+/* Number of device allocations the library has made since it was loaded (all
+ * contexts and problems; every device buffer is allocated through one routine
+ * that counts).  No reference counterpart. */
+int hdg_device_allocations(long long *count);
+
+/* The rule every entry point applies to a caller's pointer, from the
+ * (memory_type, device) that cudaPointerGetAttributes reports for it and the
+ * context's GPU: *place = 0 host memory (staged through the context's
+ * buffers), 1 usable in place (device memory of the context's GPU, or managed
+ * memory), 2 refused: device memory of another GPU, which the kernels could
+ * not read without peer access; the entry points then return HDG_ERR_INVALID
+ * and so does this query.  No reference counterpart. */
+int hdg_pointer_placement(int memory_type, int pointer_device, int context_device, int *place);
+
 /* Context: one GPU, one stream, a device memory pool.  One context per host
  * thread.  No reference counterpart (the reference is single-threaded Julia). */
 int hdg_context_create(int device, hdg_context **out);
@@ -138,6 +152,10 @@ int hdg_sum_facets(hdg_context *ctx, int nitems, int nfacets, int len,
  *    HDG_ERR_INVALID (split it).
  *  - The first call on a device looks the array's address up
  *    (cudaGetSymbolAddress); make that first call before any stream capture.
+ *  - Each call waits for its own work (it synchronises the context's stream
+ *    to read the pivot flag) and gives the caller's current device back.
+ *  - Pointers must be device memory of the context's GPU (or managed);
+ *    host memory and other GPUs' memory are refused with HDG_ERR_INVALID.
  *  - Every call uses the same array: calls that overlap on the GPU race, so
  *    issue them on one stream (the context's) or order them with events.
  * Results equal hdg_static_condensation(ctx, HDG_PREC_FP32_REFINED, ...). */
@@ -295,6 +313,12 @@ int hdg_context_set_persistent_pcg(hdg_context *ctx, int on);
  * in ms: [integrate, condense, assemble, skeleton solve, recover]. */
 int hdg_get_timings(const hdg_problem *pb, double *ms);
 
+/* The last skeleton solve: [iterations, relative residual, FP64 residual
+ * refinements (fast precisions; 0 for FP64), iterations of the FP64
+ * correction solve that finishes a refined solve whose FP32 cycles stalled
+ * (0 when none was needed)].  No reference counterpart. */
+int hdg_get_solve_stats(const hdg_problem *pb, double *stats);
+
 /* Benchmark support (no reference counterpart): relaunches one kernel of the
  * path `reps` times between CUDA events on the library's stream and returns
  * the mean device time per launch in ms.  which: 0 integrate, 1 condense,
@@ -302,6 +326,12 @@ int hdg_get_timings(const hdg_problem *pb, double *ms);
  * have been assembled (and solved for 3, 4); state is recomputed, not
  * changed. */
 int hdg_time_kernel(hdg_problem *pb, int which, int reps, double *ms_per_launch);
+
+/* Benchmark support (no reference counterpart): the device's measured FMA
+ * pipe peaks in TFLOP/s (an FMA counts 2 flops), from a few-ms kernel of
+ * independent FMA chains at full occupancy timed by CUDA events: FP32 (the
+ * pipes of the float-float paths) and FP64 (the plain FP64 path). */
+int hdg_measure_pipe_peaks(hdg_context *ctx, double *fp32_tflops, double *fp64_tflops);
 
 /* Device bytes currently reserved by the problem (all its buffers). */
 int hdg_problem_device_bytes(const hdg_problem *pb, double *bytes);

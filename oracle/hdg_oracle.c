@@ -1344,33 +1344,87 @@ int orc_l2_errors(int D, int k, const int *n, const double *domain,
   return 0;
 }
 
-/* Whole path as the reference runs it (src/HybridAffineFEOperators.jl:10-50 and
- * :72-150): integrate + condense per cell, assemble, solve the skeleton
- * system (solver 0: dense LU, 1: block-Jacobi PCG on -S), then re-integrate
- * and run BackwardStaticCondensationMap per cell (the reference re-evaluates
- * the weak form and refactorises A_ii in solve!).  Cell matrices are never
- * stored for the whole mesh (one per thread).  uint_out: ncells x ni or NULL;
- * lambda_out: nfree or NULL; times_out[5]: integrate+condense, assemble,
- * solve, recover, total (s). */
-int orc_solve_darcy(int D, int k, const int *n, const double *domain,
-                    double tau, int stab_mode, int problem, const double *kappa,
-                    int solver, double rtol, int maxit, double *uint_out,
-                    double *lambda_out, double *times_out, int *iters,
-                    double *relres, double *err_flux, double *err_pres) {
+/* What the reference builds once per mesh and space (Skeleton(model), the
+ * facet space M with its Dirichlet values, and the sparsity pattern of the
+ * skeleton system: src/Skeleton.jl:113-147, src/HybridAffineFEOperators.jl:
+ * 152-162,358-439, Gridap's assembler's symbolic pass).  A step
+ * (orc_darcy_step) then integrates, condenses, assembles the values, solves
+ * and recovers on it. */
+struct orc_darcy {
+  int D, k, n[MAXD];
+  double domain[2 * MAXD];
+  int problem;
+  int ncells, nfacets, nfree, ndir;
+  int *cell_facets, *facet_cells, *isb, *fdofs;
+  double *dvals;
+  int64_t nnz;
+  int64_t *rowptr;
+  int32_t *colind;
+};
+
+void orc_darcy_free(orc_darcy *h) {
+  if (!h) return;
+  free(h->cell_facets); free(h->facet_cells); free(h->isb); free(h->fdofs); free(h->dvals);
+  free(h->rowptr); free(h->colind);
+  free(h);
+}
+
+int orc_darcy_setup(int D, int k, const int *n, const double *domain, int problem, orc_darcy **out,
+                    int64_t *nnz_out, int *nfree_out) {
   reftab t;
   if (reftab_init(&t, D, k)) return -1;
+  orc_darcy *h = calloc(1, sizeof(orc_darcy));
+  h->D = D;
+  h->k = k;
+  h->problem = problem;
+  for (int d = 0; d < D; ++d) {
+    h->n[d] = n[d];
+    h->domain[2 * d] = domain[2 * d];
+    h->domain[2 * d + 1] = domain[2 * d + 1];
+  }
+  orc_cart_counts(D, n, &h->ncells, &h->nfacets);
+  int nl = 2 * D, nfd = t.nfd;
+  h->cell_facets = malloc(sizeof(int) * h->ncells * nl);
+  h->facet_cells = malloc(sizeof(int) * h->nfacets * 2);
+  h->isb = malloc(sizeof(int) * h->nfacets);
+  h->fdofs = malloc(sizeof(int) * h->nfacets * nfd);
+  orc_cart_topology(D, n, h->cell_facets, h->facet_cells, h->isb);
+  orc_facet_dofs(D, k, h->nfacets, h->isb, h->fdofs, &h->nfree, &h->ndir);
+  h->dvals = malloc(sizeof(double) * (h->ndir > 0 ? h->ndir : 1));
+  orc_dirichlet_values(D, k, n, domain, problem, h->nfacets, h->isb, h->fdofs, h->ndir, h->dvals);
+  h->rowptr = malloc(sizeof(int64_t) * (h->nfree + 1));
+  orc_csr_pattern(D, k, h->ncells, h->nfacets, h->cell_facets, h->fdofs, h->nfree, NULL, NULL, &h->nnz);
+  h->colind = malloc(sizeof(int32_t) * (h->nnz > 0 ? h->nnz : 1));
+  orc_csr_pattern(D, k, h->ncells, h->nfacets, h->cell_facets, h->fdofs, h->nfree, h->rowptr, h->colind, &h->nnz);
+  reftab_free(&t);
+  if (nnz_out) *nnz_out = h->nnz;
+  if (nfree_out) *nfree_out = h->nfree;
+  *out = h;
+  return 0;
+}
+
+/* One solve on a set-up mesh (src/HybridAffineFEOperators.jl:10-50 and
+ * :72-150): integrate + condense per cell, assemble the values into the
+ * pattern, solve the skeleton system (solver 0: dense LU, 1: block-Jacobi PCG
+ * on -S), then re-integrate and run BackwardStaticCondensationMap per cell
+ * (the reference re-evaluates the weak form and refactorises A_ii in
+ * solve!).  Cell matrices are never stored for the whole mesh (one per
+ * thread).  uint_out: ncells x ni or NULL; lambda_out: nfree or NULL;
+ * val_out (nnz), rhs_out (nfree): the assembled skeleton system or NULL;
+ * times_out[5]: integrate+condense, assemble, solve, recover, total (s). */
+int orc_darcy_step(orc_darcy *h, double tau, int stab_mode, const double *kappa, int solver, double rtol,
+                   int maxit, double *uint_out, double *lambda_out, double *val_out, double *rhs_out,
+                   double *times_out, int *iters, double *relres, double *err_flux, double *err_pres) {
+  reftab t;
+  const int D = h->D, k = h->k, problem = h->problem;
+  const int *n = h->n;
+  const double *domain = h->domain;
+  if (reftab_init(&t, D, k)) return -1;
   double t0 = wtime();
-  int ncells, nfacets, nfree, ndir;
-  orc_cart_counts(D, n, &ncells, &nfacets);
-  int nl = 2 * D, nfd = t.nfd, ni = t.ni, nf = t.nf, N = t.n;
-  int *cell_facets = malloc(sizeof(int) * ncells * nl);
-  int *facet_cells = malloc(sizeof(int) * nfacets * 2);
-  int *isb = malloc(sizeof(int) * nfacets);
-  int *fdofs = malloc(sizeof(int) * nfacets * nfd);
-  orc_cart_topology(D, n, cell_facets, facet_cells, isb);
-  orc_facet_dofs(D, k, nfacets, isb, fdofs, &nfree, &ndir);
-  double *dvals = malloc(sizeof(double) * (ndir > 0 ? ndir : 1));
-  orc_dirichlet_values(D, k, n, domain, problem, nfacets, isb, fdofs, ndir, dvals);
+  const int ncells = h->ncells, nfree = h->nfree;
+  const int nl = 2 * D, nfd = t.nfd, ni = t.ni, nf = t.nf, N = t.n;
+  const int *cell_facets = h->cell_facets, *facet_cells = h->facet_cells, *fdofs = h->fdofs;
+  const double *dvals = h->dvals;
   double *S = malloc(sizeof(double) * (size_t)ncells * nf * nf);
   double *g = malloc(sizeof(double) * (size_t)ncells * nf);
   int bad = 0;
@@ -1390,21 +1444,17 @@ int orc_solve_darcy(int D, int k, const int *n, const double *domain,
     free(A); free(b); free(work); free(ipiv);
   }
   double t2 = wtime();
-  int64_t nnz;
-  int64_t *rowptr = malloc(sizeof(int64_t) * (nfree + 1));
-  orc_csr_pattern(D, k, ncells, nfacets, cell_facets, fdofs, nfree, NULL, NULL, &nnz);
-  int32_t *colind = malloc(sizeof(int32_t) * (nnz > 0 ? nnz : 1));
-  double *val = malloc(sizeof(double) * (nnz > 0 ? nnz : 1));
-  double *rhs = malloc(sizeof(double) * (nfree > 0 ? nfree : 1));
+  const int64_t nnz = h->nnz;
+  double *val = val_out ? val_out : malloc(sizeof(double) * (nnz > 0 ? nnz : 1));
+  double *rhs = rhs_out ? rhs_out : malloc(sizeof(double) * (nfree > 0 ? nfree : 1));
   double *lam = malloc(sizeof(double) * (nfree > 0 ? nfree : 1));
-  orc_csr_pattern(D, k, ncells, nfacets, cell_facets, fdofs, nfree, rowptr, colind, &nnz);
-  int rc = orc_assemble(D, k, ncells, cell_facets, fdofs, nfree, dvals, S, g, rowptr, colind, val, rhs);
+  int rc = orc_assemble(D, k, ncells, cell_facets, fdofs, nfree, dvals, S, g, h->rowptr, h->colind, val, rhs);
   double t3 = wtime();
   int it = 0;
   double rel = 0.0;
   if (!rc) {
-    if (solver == 0) rc = orc_dense_solve(nfree, rowptr, colind, val, rhs, lam);
-    else rc = orc_pcg(nfree, nfd, rowptr, colind, val, rhs, lam, -1.0, rtol, maxit, &it, &rel);
+    if (solver == 0) rc = orc_dense_solve(nfree, h->rowptr, h->colind, val, rhs, lam);
+    else rc = orc_pcg(nfree, nfd, h->rowptr, h->colind, val, rhs, lam, -1.0, rtol, maxit, &it, &rel);
   }
   double t4 = wtime();
   double *ucells = uint_out ? uint_out : malloc(sizeof(double) * (size_t)ncells * ni);
@@ -1440,10 +1490,28 @@ int orc_solve_darcy(int D, int k, const int *n, const double *domain,
   if (err_flux && err_pres) orc_l2_errors(D, k, n, domain, problem, kappa, ucells, err_flux, err_pres);
   if (lambda_out) memcpy(lambda_out, lam, sizeof(double) * nfree);
   if (!uint_out) free(ucells);
-  free(cell_facets); free(facet_cells); free(isb); free(fdofs); free(dvals);
-  free(S); free(g); free(rowptr); free(colind); free(val); free(rhs); free(lam);
+  if (!val_out) free(val);
+  if (!rhs_out) free(rhs);
+  free(S); free(g); free(lam);
   reftab_free(&t);
   if (bad) return 2;
+  return rc;
+}
+
+/* Whole path as the reference runs it: orc_darcy_setup + orc_darcy_step;
+ * times_out[4] (total) includes the set-up. */
+int orc_solve_darcy(int D, int k, const int *n, const double *domain,
+                    double tau, int stab_mode, int problem, const double *kappa,
+                    int solver, double rtol, int maxit, double *uint_out,
+                    double *lambda_out, double *times_out, int *iters,
+                    double *relres, double *err_flux, double *err_pres) {
+  double t0 = wtime();
+  orc_darcy *h = NULL;
+  if (orc_darcy_setup(D, k, n, domain, problem, &h, NULL, NULL)) return -1;
+  int rc = orc_darcy_step(h, tau, stab_mode, kappa, solver, rtol, maxit, uint_out, lambda_out, NULL, NULL,
+                          times_out, iters, relres, err_flux, err_pres);
+  if (times_out) times_out[4] = wtime() - t0;
+  orc_darcy_free(h);
   return rc;
 }
 
@@ -1836,3 +1904,587 @@ int orc_solve_elasticity(int D, int k, const int *n, const double *domain, doubl
   return rc;
 }
 
+
+/* ------------------------------------------------------------------------ */
+/* General spaces.  Each field has its own polynomial space and order, as    */
+/* the reference's tests choose them with ReferenceFE(lagrangian, T, order;  */
+/* space=:P) (test/DarcyHDGTests.jl:34-36 flux P_k, pressure P_{k-1}, trace   */
+/* P_k; test/LinearElasticityHDGTests.jl:88-93 stress P_k, displacement      */
+/* P_{k+1}, trace P_k).  space Q: tensor Lagrange of order k in Gridap's node */
+/* order; space P: total degree <= k, Lagrange at the simplex lattice points */
+/* x = i/k (the constant for k = 0).  The interior bases only change the     */
+/* interior DOF values, not the skeleton system (a Schur complement does not */
+/* depend on the interior basis) nor the L2 errors the reference's tests     */
+/* check.  Box cells of a Cartesian mesh; everything integrated point by     */
+/* point.  spaces[7] = {kindA, kA, kindB, kB, kindT, kT, pm}: A the first    */
+/* bulk field (Darcy flux / elasticity stress), B the second (pressure /     */
+/* displacement), T the trace; pm = 1 projects the displacement onto the     */
+/* trace space in the tau terms (P_m, src/GridapAPIExtensions.jl:453-500,    */
+/* test/P_m.jl:4-22, used at test/LinearElasticityHDGTests.jl:134-150).      */
+/* ------------------------------------------------------------------------ */
+
+enum { GS_PHYS_DARCY = 0, GS_PHYS_ELAST = 1, GS_Q = 0, GS_P = 1 };
+
+typedef struct {
+  int d, kind, k, nb;
+  int *lat;      /* Q: nb x d lattice indices */
+  int *mono;     /* P: nb x d exponents */
+  double *coef;  /* P: nb x nb, phi_a = sum_m coef[a nb + m] x^mono_m */
+  double *nodes; /* nb x d */
+} obasis;
+
+static void obasis_free(obasis *b) {
+  free(b->lat);
+  free(b->mono);
+  free(b->coef);
+  free(b->nodes);
+  memset(b, 0, sizeof(*b));
+}
+
+/* dense inverse (row-major, in place) by Gauss-Jordan with partial pivoting */
+static int dense_inverse(int n, double *A) {
+  double *I = calloc((size_t)n * n, sizeof(double));
+  for (int i = 0; i < n; ++i) I[i * n + i] = 1.0;
+  for (int c = 0; c < n; ++c) {
+    int pr = c;
+    for (int i = c + 1; i < n; ++i)
+      if (fabs(A[i * n + c]) > fabs(A[pr * n + c])) pr = i;
+    if (!(fabs(A[pr * n + c]) > 0.0)) {
+      free(I);
+      return -1;
+    }
+    for (int j = 0; j < n; ++j) {
+      double t = A[c * n + j]; A[c * n + j] = A[pr * n + j]; A[pr * n + j] = t;
+      t = I[c * n + j]; I[c * n + j] = I[pr * n + j]; I[pr * n + j] = t;
+    }
+    const double piv = A[c * n + c];
+    for (int j = 0; j < n; ++j) {
+      A[c * n + j] /= piv;
+      I[c * n + j] /= piv;
+    }
+    for (int i = 0; i < n; ++i) {
+      if (i == c) continue;
+      const double f = A[i * n + c];
+      if (f != 0.0)
+        for (int j = 0; j < n; ++j) {
+          A[i * n + j] -= f * A[c * n + j];
+          I[i * n + j] -= f * I[c * n + j];
+        }
+    }
+  }
+  memcpy(A, I, sizeof(double) * n * n);
+  free(I);
+  return 0;
+}
+
+static int obasis_init(obasis *b, int d, int kind, int k) {
+  memset(b, 0, sizeof(*b));
+  b->d = d;
+  b->kind = kind;
+  b->k = k;
+  if (d < 1 || d > 3 || k < 0 || k > 4) return -1;
+  if (kind == GS_Q) {
+    if (k < 1) return -1;
+    b->nb = ipow(k + 1, d);
+    b->lat = malloc(sizeof(int) * b->nb * d);
+    orc_lagrange_lattice(d, k, b->lat);
+    b->nodes = malloc(sizeof(double) * b->nb * d);
+    for (int i = 0; i < b->nb * d; ++i) b->nodes[i] = (double)b->lat[i] / k;
+    return 0;
+  }
+  if (kind != GS_P) return -1;
+  int cnt = 0, tot = ipow(k + 1, d);
+  b->mono = malloc(sizeof(int) * tot * d);
+  for (int a = 0; a < tot; ++a) {
+    int e[3], s = 0, r = a;
+    for (int j = 0; j < d; ++j) {
+      e[j] = r % (k + 1);
+      r /= (k + 1);
+      s += e[j];
+    }
+    if (s <= k) {
+      for (int j = 0; j < d; ++j) b->mono[cnt * d + j] = e[j];
+      ++cnt;
+    }
+  }
+  b->nb = cnt;
+  b->nodes = malloc(sizeof(double) * cnt * d);
+  for (int a = 0; a < cnt; ++a)
+    for (int j = 0; j < d; ++j) b->nodes[a * d + j] = k == 0 ? 0.5 : (double)b->mono[a * d + j] / k;
+  double *V = malloc(sizeof(double) * cnt * cnt);
+  for (int r = 0; r < cnt; ++r)
+    for (int m = 0; m < cnt; ++m) {
+      double v = 1.0;
+      for (int j = 0; j < d; ++j) v *= pow(b->nodes[r * d + j], b->mono[m * d + j]);
+      V[r * cnt + m] = v;
+    }
+  if (dense_inverse(cnt, V)) {
+    free(V);
+    return -1;
+  }
+  b->coef = malloc(sizeof(double) * cnt * cnt);
+  for (int a = 0; a < cnt; ++a)
+    for (int m = 0; m < cnt; ++m) b->coef[a * cnt + m] = V[m * cnt + a]; /* V^{-T} */
+  free(V);
+  return 0;
+}
+
+static void obasis_eval(const obasis *b, const double *xi, double *val, double *grad) {
+  const int d = b->d, nb = b->nb;
+  if (b->kind == GS_Q) {
+    for (int a = 0; a < nb; ++a) {
+      double l[3], dl[3];
+      for (int e = 0; e < d; ++e) lag1d(b->k, b->lat[a * d + e], xi[e], &l[e], &dl[e]);
+      double v = 1.0;
+      for (int e = 0; e < d; ++e) v *= l[e];
+      val[a] = v;
+      if (grad)
+        for (int e = 0; e < d; ++e) {
+          double g = dl[e];
+          for (int j = 0; j < d; ++j)
+            if (j != e) g *= l[j];
+          grad[a * d + e] = g;
+        }
+    }
+    return;
+  }
+  for (int a = 0; a < nb; ++a) {
+    val[a] = 0.0;
+    if (grad)
+      for (int e = 0; e < d; ++e) grad[a * d + e] = 0.0;
+  }
+  for (int m = 0; m < nb; ++m) {
+    double mv = 1.0, md[3];
+    for (int j = 0; j < d; ++j) mv *= pow(xi[j], b->mono[m * d + j]);
+    for (int e = 0; e < d; ++e) {
+      const int pe = b->mono[m * d + e];
+      double g = pe == 0 ? 0.0 : pe * pow(xi[e], pe - 1);
+      for (int j = 0; j < d; ++j)
+        if (j != e) g *= pow(xi[j], b->mono[m * d + j]);
+      md[e] = g;
+    }
+    for (int a = 0; a < nb; ++a) {
+      const double c = b->coef[a * nb + m];
+      val[a] += c * mv;
+      if (grad)
+        for (int e = 0; e < d; ++e) grad[a * d + e] += c * md[e];
+    }
+  }
+}
+
+int orc_gs_basis_eval(int d, int kind, int k, int npts, const double *xi, double *val, double *grad) {
+  obasis b;
+  if (obasis_init(&b, d, kind, k)) return -1;
+  for (int p = 0; p < npts; ++p)
+    obasis_eval(&b, xi + p * d, val + (size_t)p * b.nb, grad ? grad + (size_t)p * b.nb * d : NULL);
+  const int nb = b.nb;
+  obasis_free(&b);
+  return nb;
+}
+
+typedef struct {
+  int D, phys, pm;
+  obasis A, B, T;
+  int ncA, ncB, ncT, nA, nB, nT, ni, nf, nfd, n;
+  int n1, nqv, nqf;
+  double *qv_xi, *qv_w, *qf_w, *qf_s; /* volume points, facet points (nqf x (D-1) parameters) */
+} gstab;
+
+static void gstab_free(gstab *g) {
+  obasis_free(&g->A);
+  obasis_free(&g->B);
+  obasis_free(&g->T);
+  free(g->qv_xi);
+  free(g->qv_w);
+  free(g->qf_w);
+  free(g->qf_s);
+}
+
+static int gstab_init(gstab *g, int D, int phys, const int *sp) {
+  memset(g, 0, sizeof(*g));
+  if (D < 2 || D > 3 || (phys != GS_PHYS_DARCY && phys != GS_PHYS_ELAST)) return -1;
+  g->D = D;
+  g->phys = phys;
+  g->pm = sp[6];
+  if (obasis_init(&g->A, D, sp[0], sp[1]) || obasis_init(&g->B, D, sp[2], sp[3]) ||
+      obasis_init(&g->T, D - 1, sp[4], sp[5])) {
+    gstab_free(g);
+    return -1;
+  }
+  const int ns = D * (D + 1) / 2;
+  g->ncA = phys == GS_PHYS_DARCY ? D : ns;
+  g->ncB = phys == GS_PHYS_DARCY ? 1 : D;
+  g->ncT = phys == GS_PHYS_DARCY ? 1 : D;
+  g->nA = g->A.nb;
+  g->nB = g->B.nb;
+  g->nT = g->T.nb;
+  g->ni = g->ncA * g->nA + g->ncB * g->nB;
+  g->nfd = g->ncT * g->nT;
+  g->nf = 2 * D * g->nfd;
+  g->n = g->ni + g->nf;
+  int kmax = sp[1] > sp[3] ? sp[1] : sp[3];
+  if (sp[5] > kmax) kmax = sp[5];
+  g->n1 = kmax + 2;
+  g->nqv = ipow(g->n1, D);
+  g->nqf = ipow(g->n1, D - 1);
+  double x1[16], w1[16];
+  orc_gauss_legendre01(g->n1, x1, w1);
+  g->qv_xi = malloc(sizeof(double) * g->nqv * D);
+  g->qv_w = malloc(sizeof(double) * g->nqv);
+  for (int q = 0; q < g->nqv; ++q) {
+    double w = 1.0;
+    for (int d = 0, r = q; d < D; ++d, r /= g->n1) {
+      g->qv_xi[q * D + d] = x1[r % g->n1];
+      w *= w1[r % g->n1];
+    }
+    g->qv_w[q] = w;
+  }
+  g->qf_w = malloc(sizeof(double) * g->nqf);
+  g->qf_s = malloc(sizeof(double) * g->nqf * (D - 1));
+  for (int q = 0; q < g->nqf; ++q) {
+    double w = 1.0;
+    for (int d = 0, r = q; d < D - 1; ++d, r /= g->n1) {
+      g->qf_s[q * (D - 1) + d] = x1[r % g->n1];
+      w *= w1[r % g->n1];
+    }
+    g->qf_w[q] = w;
+  }
+  return 0;
+}
+
+int orc_gs_sizes(int D, int phys, const int *spaces, int *sizes /* ni, nf, nfd, nA, nB, nT, nqv */) {
+  gstab g;
+  if (gstab_init(&g, D, phys, spaces)) return -1;
+  sizes[0] = g.ni;
+  sizes[1] = g.nf;
+  sizes[2] = g.nfd;
+  sizes[3] = g.nA;
+  sizes[4] = g.nB;
+  sizes[5] = g.nT;
+  sizes[6] = g.nqv;
+  gstab_free(&g);
+  return 0;
+}
+
+/* cell-local coordinates of facet lf's point with parameters s (the
+ * non-normal dimensions in increasing order) */
+static void facet_point(int D, int lf, const double *s, double *xi) {
+  const int dn = D - 1 - lf / 2, side = lf % 2;
+  for (int d = 0, j = 0; d < D; ++d) xi[d] = (d == dn) ? (double)side : s[j++];
+}
+
+/* P_m on local facet lf: P = (int mu mu^T) \ (int mu phiB^T), nT x nB row-major */
+static int gs_pm_matrix(const gstab *g, int lf, double *P) {
+  const int D = g->D, nT = g->nT, nB = g->nB;
+  double *L = calloc((size_t)nT * nT, sizeof(double)), *mu = malloc(sizeof(double) * nT),
+         *ph = malloc(sizeof(double) * nB);
+  memset(P, 0, sizeof(double) * nT * nB);
+  for (int q = 0; q < g->nqf; ++q) {
+    double xi[3];
+    facet_point(D, lf, &g->qf_s[q * (D - 1)], xi);
+    obasis_eval(&g->T, &g->qf_s[q * (D - 1)], mu, NULL);
+    obasis_eval(&g->B, xi, ph, NULL);
+    for (int m = 0; m < nT; ++m) {
+      for (int m2 = 0; m2 < nT; ++m2) L[m * nT + m2] += g->qf_w[q] * mu[m] * mu[m2];
+      for (int b = 0; b < nB; ++b) P[m * nB + b] += g->qf_w[q] * mu[m] * ph[b];
+    }
+  }
+  int rc = dense_inverse(nT, L);
+  if (!rc) {
+    double *tmp = malloc(sizeof(double) * nT * nB);
+    for (int m = 0; m < nT; ++m)
+      for (int b = 0; b < nB; ++b) {
+        double v = 0.0;
+        for (int m2 = 0; m2 < nT; ++m2) v += L[m * nT + m2] * P[m2 * nB + b];
+        tmp[m * nB + b] = v;
+      }
+    memcpy(P, tmp, sizeof(double) * nT * nB);
+    free(tmp);
+  }
+  free(L);
+  free(mu);
+  free(ph);
+  return rc;
+}
+
+/* The Darcy HDG form of test/DarcyHDGTests.jl:125-135 (stab 1: tau (n.n_o)
+ * terms as written there, 0: tau (p - l)) with flux in A, pressure in B,
+ * trace in T; DOFs [flux (D x nA, component-major) | pressure (nB) | trace
+ * per local facet (nT)].  The elasticity form of
+ * test/LinearElasticityHDGTests.jl:140-150 (compliance :15-38) with stress in
+ * A (upper-triangle components), displacement in B, trace in T (D comps),
+ * and, when pm, P_m(u) in the tau w.u and tau mu.u terms.  A column-major. */
+static void gs_integrate_cell(const gstab *g, int c, const int *n, const double *domain, double tau, int stab,
+                              int problem, double coef, double E, const int *facet_cells, const int *cell_facets,
+                              double *A, double *b) {
+  const int D = g->D, nA = g->nA, nB = g->nB, nT = g->nT, ncA = g->ncA, N = g->n, ni = g->ni;
+  const int oB = ncA * nA;
+  double x0[MAXD], h[MAXD];
+  cell_geom(D, n, domain, c, x0, h);
+  double detJ = 1.0;
+  for (int d = 0; d < D; ++d) detJ *= h[d];
+  memset(A, 0, sizeof(double) * (size_t)N * N);
+  memset(b, 0, sizeof(double) * N);
+  double *pA = malloc(sizeof(double) * nA), *dA = malloc(sizeof(double) * nA * D), *pB = malloc(sizeof(double) * nB),
+         *dB = malloc(sizeof(double) * nB * D), *mu = malloc(sizeof(double) * nT), *pm = malloc(sizeof(double) * nB),
+         *P = malloc(sizeof(double) * nT * nB);
+#define AIJ(i, j) A[(size_t)(i) + (size_t)N * (j)]
+  const int ns = D * (D + 1) / 2;
+  double Cm[6][6];
+  if (g->phys == GS_PHYS_ELAST)
+    for (int ca = 0; ca < ns; ++ca)
+      for (int cb = 0; cb < ns; ++cb) {
+        double dd = 0.0, trc = 0.0, trd = 0.0;
+        for (int r = 0; r < D; ++r) {
+          trc += sym_unit(D, ca, r, r);
+          trd += sym_unit(D, cb, r, r);
+          for (int s2 = 0; s2 < D; ++s2) dd += sym_unit(D, ca, r, s2) * sym_unit(D, cb, r, s2);
+        }
+        Cm[ca][cb] = (1.0 + coef) / E * dd - coef / E * trc * trd;
+      }
+  for (int q = 0; q < g->nqv; ++q) {
+    const double *xi = &g->qv_xi[q * D];
+    obasis_eval(&g->A, xi, pA, dA);
+    obasis_eval(&g->B, xi, pB, dB);
+    const double wq = g->qv_w[q] * detJ;
+    double x[MAXD];
+    for (int d = 0; d < D; ++d) x[d] = x0[d] + h[d] * xi[d];
+    if (g->phys == GS_PHYS_DARCY) {
+      double pe, qe[MAXD], fu[MAXD], gg;
+      exact(problem, D, x, coef, &pe, qe, fu, &gg);
+      for (int a = 0; a < nA; ++a) {
+        for (int a2 = 0; a2 < nA; ++a2)
+          for (int d = 0; d < D; ++d) AIJ(d * nA + a, d * nA + a2) += wq * pA[a] * pA[a2] / coef;
+        for (int bb = 0; bb < nB; ++bb)
+          for (int d = 0; d < D; ++d) {
+            AIJ(d * nA + a, oB + bb) -= wq * (dA[a * D + d] / h[d]) * pB[bb]; /* -(div v) p */
+            AIJ(oB + bb, d * nA + a) -= wq * (dB[bb * D + d] / h[d]) * pA[a]; /* -grad(q).u */
+          }
+        for (int d = 0; d < D; ++d) b[d * nA + a] += wq * pA[a] * fu[d];
+      }
+      for (int bb = 0; bb < nB; ++bb) b[oB + bb] += wq * pB[bb] * gg;
+    } else {
+      double u[3], gu[3][3], hu[3][3][3], f[3];
+      elast_exact(problem, D, x, u, gu, hu);
+      elast_force(D, E, coef, hu, f);
+      for (int a = 0; a < nA; ++a) {
+        for (int a2 = 0; a2 < nA; ++a2)
+          for (int ca = 0; ca < ns; ++ca)
+            for (int cb = 0; cb < ns; ++cb) AIJ(ca * nA + a, cb * nA + a2) += Cm[ca][cb] * wq * pA[a] * pA[a2];
+        for (int bb = 0; bb < nB; ++bb)
+          for (int ca = 0; ca < ns; ++ca)
+            for (int kk = 0; kk < D; ++kk) {
+              double dv = 0.0; /* (div (phiA_a E_ca)) . e_kk */
+              for (int j = 0; j < D; ++j) dv += sym_unit(D, ca, kk, j) * dA[a * D + j] / h[j];
+              AIJ(ca * nA + a, oB + kk * nB + bb) += wq * dv * pB[bb]; /* (div v).u */
+              AIJ(oB + kk * nB + bb, ca * nA + a) -= wq * pB[bb] * dv; /* -w.(div sigma) */
+            }
+      }
+      for (int bb = 0; bb < nB; ++bb)
+        for (int kk = 0; kk < D; ++kk) b[oB + kk * nB + bb] -= wq * pB[bb] * f[kk];
+    }
+  }
+  for (int lf = 0; lf < 2 * D; ++lf) {
+    const int dn = D - 1 - lf / 2, side = lf % 2;
+    double nrm[MAXD] = {0, 0, 0};
+    nrm[dn] = side ? 1.0 : -1.0;
+    double detF = 1.0;
+    for (int d = 0; d < D; ++d)
+      if (d != dn) detF *= h[d];
+    const int f = cell_facets[c * 2 * D + lf];
+    double s = 1.0;
+    if (g->phys == GS_PHYS_DARCY && stab == 1) s = (facet_cells[2 * f] == c) ? 1.0 : -1.0;
+    const int off = ni + lf * g->nfd;
+    if (g->phys == GS_PHYS_ELAST && g->pm) gs_pm_matrix(g, lf, P);
+    for (int q = 0; q < g->nqf; ++q) {
+      double xi[3];
+      facet_point(D, lf, &g->qf_s[q * (D - 1)], xi);
+      obasis_eval(&g->A, xi, pA, NULL);
+      obasis_eval(&g->B, xi, pB, NULL);
+      obasis_eval(&g->T, &g->qf_s[q * (D - 1)], mu, NULL);
+      const double wq = g->qf_w[q] * detF;
+      if (g->phys == GS_PHYS_DARCY) {
+        for (int a = 0; a < nA; ++a)
+          for (int m = 0; m < nT; ++m)
+            for (int d = 0; d < D; ++d) {
+              const double v = wq * pA[a] * nrm[d] * mu[m];
+              AIJ(d * nA + a, off + m) += v; /* (v.n) l */
+              AIJ(off + m, d * nA + a) += v; /* m (u.n) */
+            }
+        for (int bb = 0; bb < nB; ++bb) {
+          for (int m = 0; m < nT; ++m) {
+            AIJ(oB + bb, off + m) -= wq * tau * s * pB[bb] * mu[m]; /* -tau q l (n.no) */
+            AIJ(off + m, oB + bb) += wq * tau * s * mu[m] * pB[bb]; /* tau m p (n.no) */
+          }
+          for (int a = 0; a < nA; ++a)
+            for (int d = 0; d < D; ++d) AIJ(oB + bb, d * nA + a) += wq * pB[bb] * pA[a] * nrm[d]; /* q (u.n) */
+          for (int b2 = 0; b2 < nB; ++b2) AIJ(oB + bb, oB + b2) += wq * tau * s * pB[bb] * pB[b2];
+        }
+        for (int m = 0; m < nT; ++m)
+          for (int m2 = 0; m2 < nT; ++m2) AIJ(off + m, off + m2) -= wq * tau * s * mu[m] * mu[m2];
+      } else {
+        /* the trial displacement on the facet: u, or P_m(u) = sum_m P[m][b] mu_m */
+        for (int bb = 0; bb < nB; ++bb) {
+          if (g->pm) {
+            double v = 0.0;
+            for (int m = 0; m < nT; ++m) v += P[m * nB + bb] * mu[m];
+            pm[bb] = v;
+          } else {
+            pm[bb] = pB[bb];
+          }
+        }
+        for (int m = 0; m < nT; ++m)
+          for (int kk = 0; kk < D; ++kk) {
+            const int hu_i = off + kk * nT + m;
+            for (int a = 0; a < nA; ++a)
+              for (int ca = 0; ca < ns; ++ca) {
+                double en = 0.0; /* ((E_ca) n) . e_kk */
+                for (int j = 0; j < D; ++j) en += sym_unit(D, ca, kk, j) * nrm[j];
+                if (en == 0.0) continue;
+                AIJ(ca * nA + a, hu_i) -= wq * en * pA[a] * mu[m]; /* -(v.n).uhat */
+                AIJ(hu_i, ca * nA + a) += wq * en * mu[m] * pA[a]; /* mu.(sigma.n) */
+              }
+            for (int bb = 0; bb < nB; ++bb) {
+              AIJ(oB + kk * nB + bb, hu_i) -= wq * tau * pB[bb] * mu[m]; /* -tau w.uhat */
+              AIJ(hu_i, oB + kk * nB + bb) -= wq * tau * mu[m] * pm[bb]; /* -tau mu.P(u) */
+            }
+            for (int m2 = 0; m2 < nT; ++m2) AIJ(hu_i, off + kk * nT + m2) += wq * tau * mu[m] * mu[m2]; /* tau mu.uhat */
+          }
+        for (int bb = 0; bb < nB; ++bb)
+          for (int b2 = 0; b2 < nB; ++b2)
+            for (int kk = 0; kk < D; ++kk) AIJ(oB + kk * nB + bb, oB + kk * nB + b2) += wq * tau * pB[bb] * pm[b2]; /* tau w.P(u) */
+      }
+    }
+  }
+#undef AIJ
+  free(pA); free(dA); free(pB); free(dB); free(mu); free(pm); free(P);
+}
+
+int orc_gs_integrate(int D, int phys, const int *spaces, const int *n, const double *domain, double tau, int stab,
+                     int problem, const double *coef, double E, double *A, double *b) {
+  gstab g;
+  if (gstab_init(&g, D, phys, spaces)) return -1;
+  int ncells, nfacets;
+  orc_cart_counts(D, n, &ncells, &nfacets);
+  int *cell_facets = malloc(sizeof(int) * ncells * 2 * D), *facet_cells = malloc(sizeof(int) * nfacets * 2),
+      *isb = malloc(sizeof(int) * nfacets);
+  orc_cart_topology(D, n, cell_facets, facet_cells, isb);
+  const size_t N = (size_t)g.n;
+  const double dflt = phys == GS_PHYS_DARCY ? 1.0 : 0.3;
+#pragma omp parallel for schedule(static)
+  for (int c = 0; c < ncells; ++c)
+    gs_integrate_cell(&g, c, n, domain, tau, stab, problem, coef ? coef[c] : dflt, E, facet_cells, cell_facets,
+                      A + (size_t)c * N * N, b + (size_t)c * N);
+  free(cell_facets); free(facet_cells); free(isb);
+  gstab_free(&g);
+  return 0;
+}
+
+/* TrialFESpace(M, p) / TrialFESpace(M, u_exact): the exact trace at the
+ * trace basis' nodes on every Dirichlet facet, component-major per facet. */
+int orc_gs_dirichlet_values(int D, int phys, const int *spaces, const int *n, const double *domain, int problem,
+                            const int *facet_dofs, int ndir, double *vals) {
+  gstab g;
+  if (gstab_init(&g, D, phys, spaces)) return -1;
+  int ncells, nfacets;
+  orc_cart_counts(D, n, &ncells, &nfacets);
+  int *cell_facets = malloc(sizeof(int) * ncells * 2 * D), *facet_cells = malloc(sizeof(int) * nfacets * 2),
+      *isb = malloc(sizeof(int) * nfacets);
+  orc_cart_topology(D, n, cell_facets, facet_cells, isb);
+  for (int c = 0; c < ncells; ++c) {
+    double x0[MAXD], h[MAXD];
+    cell_geom(D, n, domain, c, x0, h);
+    for (int lf = 0; lf < 2 * D; ++lf) {
+      const int f = cell_facets[c * 2 * D + lf];
+      if (!isb[f]) continue;
+      for (int m = 0; m < g.nT; ++m) {
+        double xi[3], x[3];
+        facet_point(D, lf, &g.T.nodes[m * (D - 1)], xi);
+        for (int d = 0; d < D; ++d) x[d] = x0[d] + h[d] * xi[d];
+        for (int kk = 0; kk < g.ncT; ++kk) {
+          double v;
+          if (phys == GS_PHYS_DARCY) {
+            double p, qv[3], fu[3], gg;
+            exact(problem, D, x, 1.0, &p, qv, fu, &gg);
+            v = p;
+          } else {
+            double u[3], gu[3][3], hu[3][3][3];
+            elast_exact(problem, D, x, u, gu, hu);
+            v = u[kk];
+          }
+          const int id = facet_dofs[f * g.nfd + kk * g.nT + m];
+          if (id < 0 && -1 - id < ndir) vals[-1 - id] = v;
+        }
+      }
+    }
+  }
+  free(cell_facets); free(facet_cells); free(isb);
+  gstab_free(&g);
+  return 0;
+}
+
+/* L2 errors of the two bulk fields against the exact solution:
+ * Darcy (flux, pressure), elasticity (stress, displacement). */
+int orc_gs_l2_errors(int D, int phys, const int *spaces, const int *n, const double *domain, int problem,
+                     const double *coef, double E, const double *uint, double *err1, double *err2) {
+  gstab g;
+  if (gstab_init(&g, D, phys, spaces)) return -1;
+  int ncells, nfacets;
+  orc_cart_counts(D, n, &ncells, &nfacets);
+  const int nA = g.nA, nB = g.nB, ns = D * (D + 1) / 2, oB = g.ncA * nA;
+  double e1 = 0.0, e2 = 0.0;
+#pragma omp parallel for reduction(+ : e1, e2) schedule(static)
+  for (int c = 0; c < ncells; ++c) {
+    double x0[MAXD], h[MAXD], detJ = 1.0;
+    cell_geom(D, n, domain, c, x0, h);
+    for (int d = 0; d < D; ++d) detJ *= h[d];
+    const double *u = uint + (size_t)c * g.ni;
+    const double cf = coef ? coef[c] : (phys == GS_PHYS_DARCY ? 1.0 : 0.3);
+    double pA[216], pB[216];
+    for (int q = 0; q < g.nqv; ++q) {
+      const double *xi = &g.qv_xi[q * D];
+      obasis_eval(&g.A, xi, pA, NULL);
+      obasis_eval(&g.B, xi, pB, NULL);
+      double x[MAXD];
+      for (int d = 0; d < D; ++d) x[d] = x0[d] + h[d] * xi[d];
+      const double w = g.qv_w[q] * detJ;
+      if (phys == GS_PHYS_DARCY) {
+        double p, qe[MAXD], fu[MAXD], gg;
+        exact(problem, D, x, cf, &p, qe, fu, &gg);
+        double s1 = 0.0, ph = 0.0;
+        for (int d = 0; d < D; ++d) {
+          double qh = 0.0;
+          for (int a = 0; a < nA; ++a) qh += u[d * nA + a] * pA[a];
+          s1 += (qe[d] - qh) * (qe[d] - qh);
+        }
+        for (int bb = 0; bb < nB; ++bb) ph += u[oB + bb] * pB[bb];
+        e1 += w * s1;
+        e2 += w * (p - ph) * (p - ph);
+      } else {
+        double ue[3], gu[3][3], hu[3][3][3], sig[3][3];
+        elast_exact(problem, D, x, ue, gu, hu);
+        elast_sigma(D, E, cf, gu, sig);
+        double s1 = 0.0, s2 = 0.0;
+        for (int ca = 0; ca < ns; ++ca) {
+          int i, j;
+          sym_pair(D, ca, &i, &j);
+          double sh = 0.0;
+          for (int a = 0; a < nA; ++a) sh += u[ca * nA + a] * pA[a];
+          const double e = sig[i][j] - sh;
+          s1 += (i == j ? 1.0 : 2.0) * e * e;
+        }
+        for (int kk = 0; kk < D; ++kk) {
+          double uh = 0.0;
+          for (int bb = 0; bb < nB; ++bb) uh += u[oB + kk * nB + bb] * pB[bb];
+          s2 += (ue[kk] - uh) * (ue[kk] - uh);
+        }
+        e1 += w * s1;
+        e2 += w * s2;
+      }
+    }
+  }
+  *err1 = sqrt(e1);
+  *err2 = sqrt(e2);
+  gstab_free(&g);
+  return 0;
+}

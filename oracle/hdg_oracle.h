@@ -116,6 +116,15 @@ int orc_cell_skeleton_values(int D, int k, int ncells, const int *cell_facets,
 int orc_l2_errors(int D, int k, const int *n, const double *domain,
                   int problem, const double *kappa, const double *uint,
                   double *err_flux, double *err_pres);
+/* Set-up of a Cartesian Darcy mesh once (topology, facet DOFs, Dirichlet
+ * values, CSR pattern), then solves on it; orc_solve_darcy = both. */
+typedef struct orc_darcy orc_darcy;
+int orc_darcy_setup(int D, int k, const int *n, const double *domain, int problem, orc_darcy **out,
+                    int64_t *nnz, int *nfree);
+int orc_darcy_step(orc_darcy *h, double tau, int stab_mode, const double *kappa, int solver, double rtol,
+                   int maxit, double *uint_out, double *lambda_out, double *val_out, double *rhs_out,
+                   double *times_out, int *iters, double *relres, double *err_flux, double *err_pres);
+void orc_darcy_free(orc_darcy *h);
 int orc_solve_darcy(int D, int k, const int *n, const double *domain,
                     double tau, int stab_mode, int problem, const double *kappa,
                     int solver, double rtol, int maxit, double *uint_out,

@@ -277,8 +277,124 @@ def solve_darcy(D, k, n, tau=1.0, stab=STAB_TEXTBOOK, problem=PROBLEM_LINEAR, ka
                 relres=rel.value, err_flux=ef.value, err_pres=ep.value, mesh=m)
 
 
+class DarcySetup:
+    """A Cartesian Darcy mesh set up once (topology, facet DOFs, Dirichlet
+    values, CSR pattern: orc_darcy_setup), then solved any number of times
+    (orc_darcy_step).  The split lets a timing compare the per-solve work alone."""
+
+    def __init__(self, D, k, n, problem=PROBLEM_LINEAR, domain=None):
+        L = lib()
+        self.D, self.k = D, k
+        self.n = np.array(n, dtype=np.int32)
+        self.domain = np.array(domain if domain is not None else [0.0, 1.0] * D, dtype=np.float64)
+        self.ni, self.nf = cell_sizes(D, k)
+        self.ncells = int(np.prod(self.n))
+        self.h = ctypes.c_void_p()
+        nnz, nfree = ctypes.c_int64(), ctypes.c_int()
+        rc = L.orc_darcy_setup(D, k, P(self.n), P(self.domain), problem, ctypes.byref(self.h), ctypes.byref(nnz),
+                               ctypes.byref(nfree))
+        assert rc == 0
+        self.nnz, self.nfree = nnz.value, nfree.value
+
+    def step(self, tau=1.0, stab=STAB_TEXTBOOK, kappa=None, solver=1, rtol=1e-12, maxit=100000,
+             want_solution=True, want_system=False):
+        uint = np.zeros((self.ncells, self.ni)) if want_solution else None
+        lam = np.zeros(max(self.nfree, 1)) if want_solution else None
+        val = np.zeros(max(self.nnz, 1)) if want_system else None
+        rhs = np.zeros(max(self.nfree, 1)) if want_system else None
+        times = np.zeros(5)
+        it, rel, ef, ep = ctypes.c_int(), ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        kap = None if kappa is None else np.ascontiguousarray(kappa, dtype=np.float64)
+        rc = lib().orc_darcy_step(self.h, ctypes.c_double(tau), stab, P(kap), solver, ctypes.c_double(rtol), maxit,
+                                  P(uint), P(lam), P(val), P(rhs), P(times), ctypes.byref(it), ctypes.byref(rel),
+                                  ctypes.byref(ef), ctypes.byref(ep))
+        return dict(rc=rc, uint=uint, lam=None if lam is None else lam[:self.nfree],
+                    val=None if val is None else val[:self.nnz], rhs=None if rhs is None else rhs[:self.nfree],
+                    times=times, iters=it.value, relres=rel.value, err_flux=ef.value, err_pres=ep.value)
+
+    def close(self):
+        if self.h:
+            lib().orc_darcy_free(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 EPROBLEM_LINEAR = 0
 EPROBLEM_SMOOTH = 1
+
+# General spaces: a polynomial space per field (Q_k tensor product or P_k
+# total degree), as ReferenceFE(lagrangian, T, order; space=...) chooses them.
+SPACE_Q, SPACE_P = 0, 1
+PHYS_DARCY, PHYS_ELASTICITY = 0, 1
+
+
+def gs_spaces(kindA, kA, kindB, kB, kindT, kT, pm=False):
+    """spaces[7] of the general-space functions: first bulk field (Darcy flux /
+    stress), second (pressure / displacement), trace; pm projects the
+    displacement onto the trace space in the tau terms (P_m)."""
+    return np.array([kindA, kA, kindB, kB, kindT, kT, 1 if pm else 0], dtype=np.int32)
+
+
+def gs_basis_eval(d, kind, k, xi, grad=False):
+    xi = np.ascontiguousarray(np.atleast_2d(xi), dtype=np.float64)
+    npts = xi.shape[0]
+    nb = lib().orc_gs_basis_eval(d, kind, k, 0, P(xi), None, None)
+    assert nb > 0
+    val = np.zeros((npts, nb))
+    gr = np.zeros((npts, nb, d)) if grad else None
+    lib().orc_gs_basis_eval(d, kind, k, npts, P(xi), P(val), P(gr))
+    return (val, gr) if grad else val
+
+
+class GsMesh(Mesh):
+    """A Cartesian mesh with general-space Darcy or elasticity HDG forms: its
+    facet space has nfd = (trace components) x (trace basis size) DOFs per
+    facet, numbered as Gridap numbers an L2 facet space with Dirichlet
+    boundary."""
+
+    def __init__(self, D, n, phys, spaces, domain=None):
+        super().__init__(D, n, 1, domain)
+        L = lib()
+        self.phys = phys
+        self.spaces = np.ascontiguousarray(spaces, dtype=np.int32)
+        sz = np.zeros(7, dtype=np.int32)
+        rc = L.orc_gs_sizes(D, phys, P(self.spaces), P(sz))
+        assert rc == 0, "unsupported spaces"
+        self.ni, self.nf, self.nfd, self.nA, self.nB, self.nT, self.nqv = (int(v) for v in sz)
+        self.facet_dofs = np.zeros((self.nfacets, self.nfd), dtype=np.int32)
+        nfree, ndir = ctypes.c_int(), ctypes.c_int()
+        L.orc_facet_dofs_n(self.nfd, self.nfacets, P(self.facet_is_boundary), P(self.facet_dofs),
+                           ctypes.byref(nfree), ctypes.byref(ndir))
+        self.nfree, self.ndir = nfree.value, ndir.value
+
+    def integrate(self, tau=1.0, stab=STAB_TEXTBOOK, problem=PROBLEM_LINEAR, coef=None, E=1.0):
+        n = self.ni + self.nf
+        A = np.zeros((self.ncells, n, n))
+        b = np.zeros((self.ncells, n))
+        cf = None if coef is None else np.ascontiguousarray(coef, dtype=np.float64)
+        rc = lib().orc_gs_integrate(self.D, self.phys, P(self.spaces), P(self.n), P(self.domain),
+                                    ctypes.c_double(tau), stab, problem, P(cf), ctypes.c_double(E), P(A), P(b))
+        assert rc == 0
+        return A, b
+
+    def dirichlet_values(self, problem):
+        vals = np.zeros(max(self.ndir, 1))
+        lib().orc_gs_dirichlet_values(self.D, self.phys, P(self.spaces), P(self.n), P(self.domain), problem,
+                                      P(self.facet_dofs), self.ndir, P(vals))
+        return vals[:self.ndir] if self.ndir else vals[:0]
+
+    def l2_errors(self, problem, uint, coef=None, E=1.0):
+        e1, e2 = ctypes.c_double(), ctypes.c_double()
+        cf = None if coef is None else np.ascontiguousarray(coef, dtype=np.float64)
+        lib().orc_gs_l2_errors(self.D, self.phys, P(self.spaces), P(self.n), P(self.domain), problem, P(cf),
+                               ctypes.c_double(E), P(np.ascontiguousarray(uint)), ctypes.byref(e1),
+                               ctypes.byref(e2))
+        return e1.value, e2.value
 
 
 class ElasticityMesh(Mesh):
@@ -377,3 +493,40 @@ def set_threads(n):
 
 def max_threads():
     return int(lib().orc_max_threads())
+
+
+GsMesh.csr_pattern = ElasticityMesh.csr_pattern
+GsMesh.assemble = ElasticityMesh.assemble
+GsMesh.cell_skeleton_values = ElasticityMesh.cell_skeleton_values
+
+
+def solve_gs(D, n, phys, spaces, tau=1.0, stab=STAB_TEXTBOOK, problem=PROBLEM_LINEAR, coef=None, E=1.0, solver=0,
+             sign=None, rtol=1e-13, maxit=100000, domain=None):
+    """The general-space path on the CPU: integrate, StaticCondensationMap,
+    assemble, skeleton solve (0: dense LU, 1: block-Jacobi PCG on sign*S; sign
+    defaults to -1 for Darcy, +1 for elasticity), BackwardStaticCondensationMap,
+    L2 errors of the two bulk fields."""
+    m = GsMesh(D, n, phys, spaces, domain)
+    A, b = m.integrate(tau=tau, stab=stab, problem=problem, coef=coef, E=E)
+    S, g, info = static_condensation(A, b, m.ni)
+    assert (info == 0).all()
+    dv = m.dirichlet_values(problem)
+    rowptr, colind, val, rhs = m.assemble(S, g, dv)
+    if solver == 0:
+        lam = dense_solve(rowptr, colind, val, rhs)
+        it, rel = 0, 0.0
+    else:
+        if sign is None:
+            sign = -1.0 if phys == PHYS_DARCY else 1.0
+        lam = np.zeros(len(rhs))
+        itc, relc = ctypes.c_int(), ctypes.c_double()
+        rc = lib().orc_pcg(len(rhs), m.nfd, P(rowptr), P(colind), P(val), P(rhs), P(lam), ctypes.c_double(sign),
+                           ctypes.c_double(rtol), maxit, ctypes.byref(itc), ctypes.byref(relc))
+        assert rc == 0
+        it, rel = itc.value, relc.value
+    xc = m.cell_skeleton_values(lam, dv)
+    uint, _ = backward_static_condensation(A, b, xc, m.ni)
+    e1, e2 = m.l2_errors(problem, uint, coef=coef, E=E)
+    return dict(uint=uint, lam=lam, err1=e1, err2=e2, mesh=m, A=A, b=b, S=S, g=g, val=val, rhs=rhs,
+                rowptr=rowptr, colind=colind, iters=it, relres=rel)
+

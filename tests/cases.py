@@ -1,20 +1,22 @@
-"""Named problem cases: the workloads the benchmark and the kernel profiles
-run, as one-call solves.  `python -m gridaphybrid_gb300.cases <case> [n]`
-solves each problem of the case once and prints its iteration counts; the
-profiling commands run it under ncu.
+"""Named problem cases of the tests and of the kernel profiles, as one-call
+solves.  `python tests/cases.py <case> [n]` solves each problem of the case
+once and prints its iteration counts; the profiling commands run it under ncu.
 
   l2block   3D elasticity HDG k=2 and 3D Darcy HDG k=3 on n^3 cells, float-float
             block elimination (the two-field L2-panel kernel), PCG to 1e-10
   elasticity  3D elasticity HDG k=2 on n^3 cells, float-float path
   darcy-k3  3D Darcy HDG k=3 on n^3 cells, float-float path
 """
+import os
 import sys
 
 import numpy as np
 
-from . import _lib
-from .operators import (CartesianDiscreteModel, DarcyHDG, ElasticityHDG, HybridAffineFEOperator, darcy_spaces,
-                        elasticity_spaces, solve)
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "gridaphybrid.jl_gb300"))
+
+from gridaphybrid_gb300 import _lib  # noqa: E402
+from gridaphybrid_gb300.operators import (CartesianDiscreteModel, DarcyHDG, ElasticityHDG,  # noqa: E402
+                                          HybridAffineFEOperator, darcy_spaces, elasticity_spaces, solve)
 
 
 def elasticity(n, k=2, precision=_lib.HDG_PREC_FF_BLOCK, seed=0, context=None):

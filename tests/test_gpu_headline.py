@@ -1,0 +1,146 @@
+"""Parity of the benchmark workloads against the CPU oracle, at their full size
+where the oracle finishes in seconds, and one smaller case each for the
+elasticity and batching workloads.
+
+Headline (the metric's workload): 3D Darcy HDG, [0,1]^3, 32x32x32 hexes,
+k = 2, tau = 1, textbook stabilisation, kappa = exp(N(0,1)) per cell from seed
+0, p = sin(pi x) sin(pi y) sin(pi z).  The oracle (C, FP64, OpenMP) runs the
+reference's path: per-cell integration, StaticCondensationMap
+(src/StaticCondensationMap.jl:146-196), assembly
+(src/HybridAffineFEOperators.jl:38-48), block-Jacobi PCG on the skeleton
+system to 1e-13, and BackwardStaticCondensationMap
+(src/BackwardStaticCondensationMap.jl:61-102).
+
+Tolerances (relative to the largest entry):
+  - FP64 assembled skeleton values and right-hand side: 1e-12;
+  - FP64 GPU solution (PCG to 1e-12): 1e-10;
+  - float-float block elimination + FP32 PCG in FP64 refinement
+    (HDG_PREC_FF_BLOCK, the bench default) solved to 1e-12: 1e-8;
+  - L2 errors against the manufactured solution: within 1 % of the oracle's.
+"""
+import numpy as np
+import pytest
+
+import gridaphybrid_gb300 as gh
+from gridaphybrid_gb300 import _lib
+from gridaphybrid_gb300.batching import Batch
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+RTOL_SYSTEM = 1e-12
+RTOL_FP64 = 1e-10
+RTOL_FAST = 1e-8
+
+
+def relmax(a, b):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+@pytest.fixture(scope="module")
+def headline_oracle():
+    n = (32, 32, 32)
+    kappa = np.exp(np.random.default_rng(0).normal(0.0, 1.0, 32 ** 3))
+    setup = oracle.DarcySetup(3, 2, n, problem=oracle.PROBLEM_SIN)
+    ref = setup.step(tau=1.0, stab=oracle.STAB_TEXTBOOK, kappa=kappa, solver=1, rtol=1e-13, want_system=True)
+    setup.close()
+    assert ref["rc"] == 0 and ref["relres"] <= 1e-13
+    return n, kappa, ref
+
+
+def _headline_op(n, kappa, precision):
+    model = gh.CartesianDiscreteModel((0, 1) * 3, n)
+    X, Y = gh.darcy_spaces(model, 2)
+    return gh.HybridAffineFEOperator(gh.DarcyHDG(tau=1.0, problem="sin", kappa=kappa), X, Y, [1, 2], [3],
+                                     precision=precision)
+
+
+def test_headline_fp64_system_and_solution(headline_oracle):
+    n, kappa, ref = headline_oracle
+    op = _headline_op(n, kappa, _lib.HDG_PREC_FP64)
+    rowptr, colind, val, rhs = op.skeleton_system()
+    assert len(val) == len(ref["val"]) == 82_425_600
+    assert relmax(val, ref["val"]) < RTOL_SYSTEM
+    assert relmax(rhs, ref["rhs"]) < RTOL_SYSTEM
+    xh = gh.solve(op, solver="pcg", rtol=1e-12, maxit=20000)
+    assert relmax(xh.skeleton, ref["lam"]) < RTOL_FP64
+    assert relmax(xh.cell_interior, ref["uint"]) < RTOL_FP64
+    ef, ep = xh.l2_errors()
+    assert abs(ef - ref["err_flux"]) <= 0.01 * ref["err_flux"]
+    assert abs(ep - ref["err_pres"]) <= 0.01 * ref["err_pres"]
+    op.pb.close()
+
+
+@pytest.mark.parametrize("precision", [_lib.HDG_PREC_FF_BLOCK, _lib.HDG_PREC_FP32_REFINED])
+def test_headline_fast_paths_solution(headline_oracle, precision):
+    n, kappa, ref = headline_oracle
+    op = _headline_op(n, kappa, precision)
+    xh = gh.solve(op, solver="pcg", rtol=1e-12, maxit=20000)
+    assert relmax(xh.skeleton, ref["lam"]) < RTOL_FAST
+    assert relmax(xh.cell_interior, ref["uint"]) < RTOL_FAST
+    ef, ep = xh.l2_errors()
+    assert abs(ef - ref["err_flux"]) <= 0.01 * ref["err_flux"]
+    assert abs(ep - ref["err_pres"]) <= 0.01 * ref["err_pres"]
+    op.pb.close()
+
+
+def test_elasticity_12cube_k2_fast_path_matches_oracle():
+    """The elasticity workload's form and order (3D, k = 2, n = 405 DOFs per
+    cell, E = 1, nu ~ U(0.2, 0.45) per cell, u = (sin pi x, cos pi y, xyz),
+    tau = 1/h) on 12^3 cells: HDG_PREC_FF_BLOCK solved to 1e-12 against the
+    oracle's block-Jacobi PCG to 1e-13."""
+    n = (12, 12, 12)
+    nu = np.random.default_rng(0).uniform(0.2, 0.45, size=12 ** 3)
+    model = gh.CartesianDiscreteModel((0, 1) * 3, n)
+    X, Y = gh.elasticity_spaces(model, 2)
+    op = gh.HybridAffineFEOperator(gh.ElasticityHDG(nu=nu, problem="smooth"), X, Y, [1, 2], [3],
+                                   precision=_lib.HDG_PREC_FF_BLOCK)
+    xh = gh.solve(op, solver="pcg", rtol=1e-12, maxit=20000)
+    ref = oracle.solve_elasticity(3, 2, n, nu=nu, problem=oracle.EPROBLEM_SMOOTH, solver=1, sign=1.0, rtol=1e-13)
+    assert ref["rc"] == 0
+    assert relmax(xh.skeleton, ref["lam"]) < RTOL_FAST
+    assert relmax(xh.cell_interior, ref["uint"]) < RTOL_FAST
+    es, eu = xh.l2_errors()
+    assert abs(es - ref["err_sigma"]) <= 0.01 * ref["err_sigma"]
+    assert abs(eu - ref["err_u"]) <= 0.01 * ref["err_u"]
+    op.pb.close()
+
+
+def test_batch_with_largest_problem_matches_oracle():
+    """The batching workload's extremes in one batch: 2D n = 128 with k = 3
+    (48 interior + 16 facet DOFs per cell), n = 16 with k = 1 and n = 64
+    with k = 2, kappa = exp(N(0, 1.5^2)) per cell, through the fused
+    float-float launches (solved to 1e-11) and FP64 (to 1e-12); each
+    problem's solution against the oracle's."""
+    rng = np.random.default_rng(3)
+    specs = [{"D": 2, "n": n, "k": k, "kappa": np.exp(1.5 * rng.normal(size=n * n))}
+             for n, k in ((128, 3), (16, 1), (64, 2))]
+    refs = []
+    for s in specs:
+        r = oracle.solve_darcy(2, s["k"], (s["n"], s["n"]), problem=oracle.PROBLEM_SIN, kappa=s["kappa"], solver=1,
+                               rtol=1e-13)
+        assert r["rc"] == 0
+        refs.append(r)
+    # The n = 128, k = 3 system is ill-conditioned: its true FP64 residual
+    # cannot be computed below about 1e-11 of the right-hand side (the fast
+    # path tests the true residual, so it is solved to 1e-11), and two FP64
+    # solutions of it, ours and the oracle's, agree to about 1.5e-10 whatever
+    # the tolerance (rounding times the condition number), so the FP64 path is
+    # held to 1e-9 here.
+    for precision, tol, rtol in ((_lib.HDG_PREC_FF_BLOCK, RTOL_FAST, 1e-11), (_lib.HDG_PREC_FP64, 1e-9, 1e-12)):
+        with Batch(specs) as b:
+            assert (b.assemble(precision) == 0).all()
+            its, rel = b.solve(rtol=rtol)
+            assert (rel <= rtol).all()
+            for i, (s, r) in enumerate(zip(specs, refs)):
+                ni = r["uint"].shape[1]
+                fd = b.free_dof_values(i)
+                ncells = s["n"] ** 2
+                D, nk = 2, (s["k"] + 1) ** 2
+                # Gridap's layout [flux of all cells | pressure of all cells | skeleton]
+                flux = fd[:ncells * D * nk].reshape(ncells, D * nk)
+                pres = fd[ncells * D * nk:ncells * ni].reshape(ncells, nk)
+                assert relmax(np.hstack([flux, pres]), r["uint"]) < tol, (i, precision)
+                assert relmax(fd[ncells * ni:], r["lam"]) < tol, (i, precision)

@@ -151,7 +151,7 @@ def test_persistent_inner_pcg_matches_graph_path(case):
     """The inner FP32 iterations as one cooperative launch (bounded grid
     barriers) give the solution of the two-kernel graph path: both solved to
     1e-12, agreeing to 1e-9."""
-    from gridaphybrid_gb300 import cases
+    import cases
     sols = []
     for on in (0, 1):
         c = gh.Context(0)
@@ -171,3 +171,28 @@ def test_persistent_inner_pcg_matches_graph_path(case):
         op.pb.close()
         c.close()
     assert relmax(sols[1], sols[0]) < 1e-9
+
+
+def test_refined_solve_finishes_in_fp64_when_fp32_cycles_stall():
+    """When three FP32 cycles in a row cut the true FP64 residual less than
+    2x, the refined solve finishes with an FP64 correction solve.  Asking the
+    inner iterations for a 10 % reduction per cycle (delta = 0.9) makes every
+    cycle slow, so the correction runs; the solve still reaches 1e-12 and
+    equals the oracle's solution."""
+    n = 24
+    kappa = np.exp(np.random.default_rng(8).normal(size=n * n))
+    model = gh.CartesianDiscreteModel((0, 1, 0, 1), (n, n))
+    X, Y = gh.darcy_spaces(model, 2)
+    op = gh.HybridAffineFEOperator(gh.DarcyHDG(tau=1.0, problem="sin", kappa=kappa), X, Y, [1, 2], [3],
+                                   precision=_lib.HDG_PREC_FF_BLOCK)
+    c = op.pb.ctx
+    c.check(c.lib.hdg_set_refinement(op.pb.h, 0.9, 1))
+    xh = gh.solve(op, solver="pcg", rtol=1e-12, maxit=20000)
+    st = np.zeros(4)
+    c.check(c.lib.hdg_get_solve_stats(op.pb.h, _lib.ptr(st)))
+    assert st[1] <= 1e-12 and st[3] > 0, st  # converged, with FP64 correction iterations
+    ref = oracle.solve_darcy(2, 2, (n, n), problem=oracle.PROBLEM_SIN, kappa=kappa, solver=1, rtol=1e-13)
+    assert ref["rc"] == 0
+    assert relmax(xh.skeleton, ref["lam"]) < 1e-9
+    assert relmax(xh.cell_interior, ref["uint"]) < 1e-9
+    op.pb.close()

@@ -9,6 +9,8 @@ finds the shared scratch array holding the first call's contents).  This file
 is collected last so that a stop-at-first-failure run has run every other test
 first; it also passes on its own in a fresh process.
 """
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -36,6 +38,12 @@ def _reference(ctx, A, b, ni):
     return S, g
 
 
+def _allocations(ctx):
+    n = ctypes.c_longlong()
+    ctx.check(ctx.lib.hdg_device_allocations(ctypes.byref(n)))
+    return n.value
+
+
 @pytest.mark.parametrize("D,k,n", [(3, 2, (2, 2, 2)), (2, 3, (4, 3))])
 def test_noalloc_matches_allocating_entry_point(D, k, n):
     torch = pytest.importorskip("torch")
@@ -48,14 +56,26 @@ def test_noalloc_matches_allocating_entry_point(D, k, n):
     S_ref, g_ref = _reference(ctx, A, b, m.ni)
     dA = torch.from_numpy(A).cuda()
     db = torch.from_numpy(b).cuda()
+    outs = []
     for call in range(2):
-        dS = torch.full((m.ncells, m.nf, m.nf), float("nan"), dtype=torch.float64, device="cuda")
-        dg = torch.full((m.ncells, m.nf), float("nan"), dtype=torch.float64, device="cuda")
-        dinfo = torch.full((m.ncells,), -7, dtype=torch.int32, device="cuda")
-        torch.cuda.synchronize()
+        outs.append((torch.full((m.ncells, m.nf, m.nf), float("nan"), dtype=torch.float64, device="cuda"),
+                     torch.full((m.ncells, m.nf), float("nan"), dtype=torch.float64, device="cuda"),
+                     torch.full((m.ncells,), -7, dtype=torch.int32, device="cuda")))
+    torch.cuda.synchronize()
+    allocs0 = _allocations(ctx)
+    free_after_first = None
+    for call, (dS, dg, dinfo) in enumerate(outs):
+        dev0 = torch.cuda.current_device()
         rc = ctx.lib.hdg_static_condensation_noalloc(ctx.handle, m.ncells, m.ni, m.nf, _lib.ptr(dA),
                                                      _lib.ptr(db), _lib.ptr(dS), _lib.ptr(dg), _lib.ptr(dinfo))
         assert rc == _lib.HDG_OK, ctx.lib.hdg_last_error(ctx.handle)
+        assert torch.cuda.current_device() == dev0
+        if call == 0:
+            # the first call may load the library's code (and with it the
+            # fixed array) onto the device; from then on free memory must not move
+            free_after_first = torch.cuda.mem_get_info()[0]
+        else:
+            assert torch.cuda.mem_get_info()[0] == free_after_first
         S = dS.cpu().numpy()
         g = dg.cpu().numpy()
         assert (dinfo.cpu().numpy() == 0).all()
@@ -65,10 +85,66 @@ def test_noalloc_matches_allocating_entry_point(D, k, n):
         S0, g0, _ = oracle.static_condensation(A, b, m.ni)
         assert relmax(S, S0) < RTOL_MIXED_CELL and relmax(g, g0) < RTOL_MIXED_CELL
     # info may be NULL
+    dS, dg, _ = outs[0]
     rc = ctx.lib.hdg_static_condensation_noalloc(ctx.handle, m.ncells, m.ni, m.nf, _lib.ptr(dA), _lib.ptr(db),
                                                  _lib.ptr(dS), _lib.ptr(dg), None)
     assert rc == _lib.HDG_OK
     assert relmax(dS.cpu().numpy(), S_ref) < RTOL_MIXED_CELL
+    # the library allocated nothing in any of the three calls
+    assert _allocations(ctx) == allocs0
+    assert torch.cuda.mem_get_info()[0] == free_after_first
+    ctx.close()
+
+
+def _max_cells(n, with_info):
+    """Largest batch of n x n cells the fixed array takes: the FP32 hi/lo
+    staging of A and b, rounded up to 256 bytes, one 256-byte flag slot, and
+    the per-cell info ints when the caller passes info = NULL."""
+    scratch = _lib.HDG_NOALLOC_SCRATCH_BYTES
+    per_cell = 2 * (n * n + n) * 4
+
+    def need(c):
+        return (c * per_cell + 255) // 256 * 256 + 256 + (0 if with_info else 4 * c)
+
+    c = scratch // per_cell
+    while need(c) > scratch:
+        c -= 1
+    assert need(c + 1) > scratch
+    return c
+
+
+@pytest.mark.parametrize("with_info", [True, False])
+def test_noalloc_batch_at_the_limit(with_info):
+    """A batch exactly at the fixed array's capacity runs and equals the
+    allocating path; one cell more is refused before anything runs."""
+    torch = pytest.importorskip("torch")
+    ctx = _lib.Context(0)
+    ni, nf = 12, 8
+    n = ni + nf
+    ncells = _max_cells(n, with_info)
+    rng = np.random.default_rng(5)
+    base = rng.normal(size=(16, n, n))
+    base[:, np.arange(ni), np.arange(ni)] += 2.0 * np.sqrt(n)
+    A = np.ascontiguousarray(base[np.arange(ncells) % 16])
+    b = rng.normal(size=(ncells, n))
+    S_ref, g_ref = _reference(ctx, A, b, ni)
+    dA = torch.from_numpy(A).cuda()
+    db = torch.from_numpy(b).cuda()
+    dS = torch.full((ncells, nf, nf), float("nan"), dtype=torch.float64, device="cuda")
+    dg = torch.full((ncells, nf), float("nan"), dtype=torch.float64, device="cuda")
+    dinfo = torch.full((ncells,), -7, dtype=torch.int32, device="cuda") if with_info else None
+    torch.cuda.synchronize()
+    allocs0 = _allocations(ctx)
+    rc = ctx.lib.hdg_static_condensation_noalloc(ctx.handle, ncells, ni, nf, _lib.ptr(dA), _lib.ptr(db),
+                                                 _lib.ptr(dS), _lib.ptr(dg), _lib.ptr(dinfo))
+    assert rc == _lib.HDG_OK, ctx.lib.hdg_last_error(ctx.handle)
+    assert relmax(dS.cpu().numpy(), S_ref) < RTOL_MIXED_CELL
+    assert relmax(dg.cpu().numpy(), g_ref) < RTOL_MIXED_CELL
+    rc = ctx.lib.hdg_static_condensation_noalloc(ctx.handle, ncells + 1, ni, nf, _lib.ptr(dA), _lib.ptr(db),
+                                                 _lib.ptr(dS), _lib.ptr(dg), _lib.ptr(dinfo))
+    assert rc == _lib.HDG_ERR_INVALID
+    assert b"scratch" in ctx.lib.hdg_last_error(ctx.handle)
+    assert _allocations(ctx) == allocs0
     ctx.close()
 
 
@@ -77,7 +153,7 @@ def test_noalloc_rejects_oversized_batches_and_host_pointers():
     ctx = _lib.Context(0)
     ni, nf = 108, 54
     n = ni + nf
-    too_many = _lib_max_cells(n) + 1
+    too_many = _max_cells(n, False) + 1
     # the size check comes before any pointer is touched
     dummy = torch.zeros(1, dtype=torch.float64, device="cuda")
     rc = ctx.lib.hdg_static_condensation_noalloc(ctx.handle, too_many, ni, nf, _lib.ptr(dummy), _lib.ptr(dummy),
@@ -91,9 +167,5 @@ def test_noalloc_rejects_oversized_batches_and_host_pointers():
     rc = ctx.lib.hdg_static_condensation_noalloc(ctx.handle, 1, ni, nf, _lib.ptr(A), _lib.ptr(b), _lib.ptr(S),
                                                  _lib.ptr(g), None)
     assert rc == _lib.HDG_ERR_INVALID
+    assert b"device pointers" in ctx.lib.hdg_last_error(ctx.handle)
     ctx.close()
-
-
-def _lib_max_cells(n):
-    scratch = 32 * 1024 * 1024  # HDG_NOALLOC_SCRATCH_BYTES
-    return scratch // (8 * (n * n + n))
