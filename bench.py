@@ -224,7 +224,7 @@ def run_serving(args, prec, prec64):
         summ["rejected_over_budget"] = [list(r[:3]) for r in rejected]
         summ.update({"seconds_of_trace": limit or args.serve_seconds, "peak_hbm_gb": st["peak_bytes"] / 1e9,
                      "max_concurrent": int(st["max_concurrent"]), "mesh_hits": int(st["mesh_hits"]),
-                     "evictions": int(st["evictions"])})
+                     "evictions": int(st["evictions"]), "retries_after_nomem": int(st["retries_after_nomem"])})
         out[name] = summ
     return out
 

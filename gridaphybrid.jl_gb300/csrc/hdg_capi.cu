@@ -123,6 +123,43 @@ CellArgs cell_args(hdg_problem *pb) {
   return a;
 }
 
+// The general-space form's tables and sizes; the cell part carries the
+// geometry, coefficients and form parameters with the form's own quadrature.
+GsArgs gs_args(hdg_problem *pb) {
+  const GsTables &t = pb->gst;
+  const double *T = pb->d_gstab.as<double>();
+  GsArgs g{};
+  g.cell = cell_args(pb);
+  g.cell.qxi = T + t.oqxi;
+  g.cell.qw = T + t.oqw;
+  g.cell.nqv = t.nqv;
+  g.phys = t.phys;
+  g.nA = t.nA;
+  g.nB = t.nB;
+  g.nT = t.nT;
+  g.ncA = t.ncA;
+  g.ncB = t.ncB;
+  g.copies = t.copies;
+  g.ni1 = t.ni1;
+  g.nfd1 = t.nfd1;
+  g.ni = t.ni;
+  g.nf = t.nf;
+  g.nfd = t.nfd;
+  g.n = t.n;
+  g.nqv = t.nqv;
+  g.MAA = T + t.oMAA;
+  g.GAB = T + t.oGAB;
+  g.GBA = T + t.oGBA;
+  g.FBA = T + t.oFBA;
+  g.FBB = T + t.oFBB;
+  g.HA = T + t.oHA;
+  g.HB = T + t.oHB;
+  g.L = T + t.oL;
+  g.qphiA = T + t.oqphiA;
+  g.qphiB = T + t.oqphiB;
+  return g;
+}
+
 MixedTables mixed_tables(hdg_problem *pb) {
   const float *t = pb->d_tabf.as<float>();
   const TableOffsetsF &o = pb->toff_f;
@@ -141,8 +178,28 @@ MixedTables mixed_tables(hdg_problem *pb) {
 }
 
 // Phase launches on the problem's buffers, for the precision of the last assemble.
+// General-space forms: FP64 cell blocks; for the FP32 LU + refinement they
+// are integrated into the scratch and split into the (hi, lo) float pairs.
+cudaError_t run_integrate_gs(hdg_problem *pb) {
+  hdg_context *ctx = pb->ctx;
+  const GsArgs g = gs_args(pb);
+  const size_t nc = pb->mesh.ncells, n = pb->gst.n;
+  if (pb->precision == HDG_PREC_FP64)
+    return launch_integrate_gs(g, pb->d_A.as<double>(), pb->d_b.as<double>(), ctx->stream, ctx->num_sms,
+                               &ctx->launches);
+  double *A64 = pb->d_escratch.as<double>(), *b64 = A64 + nc * n * n;
+  float *Ahi = pb->d_A.as<float>(), *bhi = pb->d_b.as<float>();
+  cudaError_t e = launch_integrate_gs(g, A64, b64, ctx->stream, ctx->num_sms, &ctx->launches);
+  if (e == cudaSuccess)
+    e = launch_split_fp64(nc * n * n, A64, Ahi, Ahi + nc * n * n, ctx->stream, ctx->num_sms, &ctx->launches);
+  if (e == cudaSuccess)
+    e = launch_split_fp64(nc * n, b64, bhi, bhi + nc * n, ctx->stream, ctx->num_sms, &ctx->launches);
+  return e;
+}
+
 cudaError_t run_integrate(hdg_problem *pb) {
   hdg_context *ctx = pb->ctx;
+  if (pb->gs) return run_integrate_gs(pb);
   if (pb->eblock && pb->l2_fused) return cudaSuccess;  // integrated inside the condensation kernel
   CellArgs a = cell_args(pb);
   const size_t nc = pb->mesh.ncells, n = pb->tab.n;
@@ -267,7 +324,24 @@ cudaError_t run_condense(hdg_problem *pb) {
 // The sign that makes the condensed skeleton operator SPD: the Darcy forms'
 // is negative definite, the elasticity form's positive definite.
 // DOFs per cell of the first bulk field (Darcy flux: D nk; elasticity stress: nsym nk)
+// Free skeleton DOF r of a problem with several copies of its form: the
+// library numbers the DOFs of a facet together ([copy 0 | copy 1 | ..] inside
+// each facet block row); the multi-field space numbers each copy's skeleton
+// field on its own, one after the other (MultiFieldFESpace([M1, M2, ..])).
+int gs_skeleton_copy(const hdg_problem *pb, size_t r) {
+  const GsTables &g = pb->gst;
+  return (int)((r % (size_t)g.nfd) / (size_t)g.nfd1);
+}
+size_t gs_skeleton_id(const hdg_problem *pb, size_t r) {
+  const GsTables &g = pb->gst;
+  const size_t nfd = g.nfd, nfd1 = g.nfd1;
+  const size_t br = r / nfd, j = r % nfd, cp = j / nfd1, a = j % nfd1;
+  const size_t per_copy = pb->mesh.nfree / (size_t)g.copies;
+  return cp * per_copy + br * nfd1 + a;
+}
+
 size_t first_field_width(const hdg_problem *pb) {
+  if (pb->gs) return (size_t)pb->gst.ncA * pb->gst.nA;
   const RefTables &t = pb->tab;
   return (size_t)(pb->physics == HDG_PHYSICS_ELASTICITY ? t.nsym : t.D) * t.nk;
 }
@@ -322,6 +396,37 @@ void interpolate_dirichlet(const hdg_problem *pb, std::vector<double> &vals) {
   const RefTables &t = pb->tab;
   const int D = m.D, nfd = m.nfd, k = m.k;
   vals.assign(m.ndir > 0 ? m.ndir : 1, 0.0);
+  if (pb->gs) {
+    // the exact trace at the nodes of the trace basis, component-major per
+    // facet, the same data for every copy of the form
+    const GsTables &g = pb->gst;
+    for (int f = 0; f < m.nfacets; ++f) {
+      if (m.facet_first_dof[f] >= 0) continue;
+      const int c = m.facet_cell[2 * (size_t)f], lf = m.facet_lface[2 * (size_t)f];
+      const int dn = D - 1 - lf / 2, side = lf % 2;
+      for (int b = 0; b < nfd; ++b) {
+        const int id = m.facet_dofs[(size_t)f * nfd + b];
+        const int bb = b % g.nfd1, comp = bb / g.nT, node = bb - comp * g.nT;
+        double xi[3], x[3];
+        for (int d = 0, j = 0; d < D; ++d)
+          xi[d] = (d == dn) ? double(side) : g.T.nodes[(size_t)node * (D - 1) + j++];
+        for (int d = 0; d < D; ++d) {
+          x[d] = m.origin[(size_t)c * D + d];
+          for (int e = 0; e < D; ++e) x[d] += m.jac[(size_t)c * D * D + e * D + d] * xi[e];
+        }
+        if (pb->physics == HDG_PHYSICS_ELASTICITY) {
+          double u[3], gu[3][3], hu[3][3][3];
+          elasticity_exact(pb->problem, D, x, u, gu, hu);
+          vals[-1 - id] = u[comp];
+        } else {
+          double p, q[3], fu[3], gg;
+          exact_solution(pb->problem, D, x, 1.0, p, q, fu, gg);
+          vals[-1 - id] = p;
+        }
+      }
+    }
+    return;
+  }
   for (int f = 0; f < m.nfacets; ++f) {
     if (m.facet_first_dof[f] >= 0) continue;
     const int c = m.facet_cell[2 * (size_t)f], lf = m.facet_lface[2 * (size_t)f];
@@ -697,6 +802,57 @@ int hdg_problem_create_cartesian_physics(hdg_context *ctx, int D, const int *cel
   return HDG_OK;
 }
 
+int hdg_problem_create_cartesian_spaces(hdg_context *ctx, int D, const int *cells, const double *domain,
+                                        int physics, const int *spaces, int copies, hdg_problem **out) {
+  if (!ctx) return HDG_ERR_INVALID;
+  if (!cells || !domain || !spaces || !out) return ctx->fail(HDG_ERR_INVALID, "null argument");
+  if (physics != HDG_PHYSICS_DARCY && physics != HDG_PHYSICS_ELASTICITY)
+    return ctx->fail(HDG_ERR_INVALID, "unknown physics %d", physics);
+  *out = nullptr;
+  DeviceGuard guard(ctx->device);
+  hdg_problem *pb = new (std::nothrow) hdg_problem();
+  if (!pb) return ctx->fail(HDG_ERR_NOMEM, "host allocation failed");
+  pb->ctx = ctx;
+  pb->physics = physics;
+  pb->gs = true;
+  for (DBuf *b : pb->device_buffers()) b->stream = ctx->stream;
+  std::string err;
+  int rc = build_gs_tables(D, physics, spaces, copies, pb->gst, err);
+  if (!rc) {
+    const GsTables &g = pb->gst;
+    if (g.n * (g.n + 1) * sizeof(double) > ctx->smem_optin - 1024) {
+      err = "the cell block exceeds the shared-memory condensation kernel";
+      rc = HDG_ERR_INVALID;
+    } else if (!assemble_supports(2 * D, g.nfd)) {
+      err = "no skeleton assembly kernel for this many DOFs per facet";
+      rc = HDG_ERR_INVALID;
+    }
+  }
+  // the mesh's facet space: every copy's trace DOFs on every facet
+  if (!rc) rc = build_cartesian_mesh(D, cells, domain, std::max(1, spaces[5]), pb->mesh, err, 1, pb->gst.nfd);
+  if (rc) {
+    delete pb;
+    return ctx->fail(rc, "%s", err.c_str());
+  }
+  if ((rc = setup_problem(pb))) {
+    delete pb;
+    return rc;
+  }
+  // the sizes every later stage reads
+  RefTables &t = pb->tab;
+  t.ni = pb->gst.ni;
+  t.nf = pb->gst.nf;
+  t.n = pb->gst.n;
+  t.nfd = pb->gst.nfd;
+  t.nfs = pb->gst.nT;
+  if ((rc = upload(ctx, pb->d_gstab, pb->gst.packed))) {
+    delete pb;
+    return rc;
+  }
+  *out = pb;
+  return HDG_OK;
+}
+
 int hdg_problem_create(hdg_context *ctx, int D, int k, int ncells, int nfacets,
                        const double *cell_origin, const double *cell_jacobian,
                        const int *cell_facets, const int *facet_dofs, hdg_problem **out) {
@@ -796,7 +952,9 @@ int hdg_set_darcy(hdg_problem *pb, int stab_mode, double tau, int problem) {
   if (pb->physics != HDG_PHYSICS_DARCY) return ctx->fail(HDG_ERR_INVALID, "the problem was not created for Darcy");
   if (stab_mode != HDG_STAB_TEXTBOOK && stab_mode != HDG_STAB_OWNER_SIGN)
     return ctx->fail(HDG_ERR_INVALID, "unknown stabilisation %d", stab_mode);
-  if (!(tau > 0.0) || !std::isfinite(tau)) return ctx->fail(HDG_ERR_INVALID, "tau must be > 0");
+  // tau = 0: the hybridized mixed form without stabilisation (general-space problems, e.g. an RT_k flux)
+  if (!(tau > 0.0 || (pb->gs && tau == 0.0)) || !std::isfinite(tau))
+    return ctx->fail(HDG_ERR_INVALID, pb->gs ? "tau must be >= 0" : "tau must be > 0");
   if (problem < 0 || problem > 2) return ctx->fail(HDG_ERR_INVALID, "unknown problem %d", problem);
   cudaSetDevice(ctx->device);
   pb->stab_mode = stab_mode;
@@ -859,7 +1017,9 @@ static int assemble_prepare(hdg_problem *pb, int precision, bool cell_blocks, bo
   const size_t nc = pb->mesh.ncells, n = t.n, ni = t.ni, nf = t.nf;
   const bool mixed = precision != HDG_PREC_FP64;
   const bool elast = pb->physics == HDG_PHYSICS_ELASTICITY;
-  const bool l2ok = l2block_supported(elast, t.D, t.k);
+  if (pb->gs && precision == HDG_PREC_FF_BLOCK)
+    return ctx->fail(HDG_ERR_INVALID, "general-space forms are condensed in FP64 or FP32 + refinement");
+  const bool l2ok = !pb->gs && l2block_supported(elast, t.D, t.k);
   if (precision == HDG_PREC_FF_BLOCK && !(l2ok || (!elast && ffblock_supported(t.D, t.k))))
     return ctx->fail(HDG_ERR_INVALID, "block elimination is built for D=2, k<=3 and D=3, k<=2 (Darcy: k<=3)");
   // the L2-panel block elimination: every elasticity FF_BLOCK assembly, Darcy
@@ -896,6 +1056,8 @@ static int assemble_prepare(hdg_problem *pb, int precision, bool cell_blocks, bo
     CUDA_TRY(ctx, pb->d_A.reserve(sizeof(double) * nc * n * n));
     CUDA_TRY(ctx, pb->d_b.reserve(sizeof(double) * nc * n));
   }
+  if (pb->gs && mixed)  // the FP64 cell blocks before their float-float split
+    CUDA_TRY(ctx, pb->d_escratch.reserve(sizeof(double) * nc * (n * n + n)));
   CUDA_TRY(ctx, pb->d_S.reserve(sizeof(double) * nc * nf * nf));
   CUDA_TRY(ctx, pb->d_g.reserve(sizeof(double) * nc * nf));
   CUDA_TRY(ctx, pb->d_aux.reserve(sizeof(double) * nc * nf));
@@ -981,6 +1143,42 @@ int hdg_get_skeleton_system(hdg_problem *pb, long long *rowptr, int *colind, dou
   if (!pb->assembled) return ctx->fail(HDG_ERR_STATE, "assemble first");
   cudaSetDevice(ctx->device);
   const HostPattern &p = pb->pat;
+  if (pb->gs && pb->gst.copies > 1) {
+    // the multi-field numbering [skeleton field of copy 0 | copy 1 | ..], and
+    // only the blocks of each field with itself (the copies do not couple)
+    const size_t n = pb->mesh.nfree;
+    std::vector<double> v(p.nnz), b(n);
+    if (p.nnz)
+      CUDA_TRY(ctx, cudaMemcpyAsync(v.data(), pb->d_val.ptr, sizeof(double) * p.nnz, cudaMemcpyDeviceToHost,
+                                    ctx->stream));
+    if (n) CUDA_TRY(ctx, cudaMemcpyAsync(b.data(), pb->d_rhs.ptr, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    std::vector<size_t> inv(n);
+    for (size_t r = 0; r < n; ++r) inv[gs_skeleton_id(pb, r)] = r;
+    std::vector<long long> rp(n + 1, 0);
+    std::vector<std::pair<int, double>> row;
+    std::vector<int> ci;
+    std::vector<double> cv;
+    for (size_t r2 = 0; r2 < n; ++r2) {
+      const size_t r = inv[r2];
+      const int cr = gs_skeleton_copy(pb, r);
+      row.clear();
+      for (int64_t e = p.rowptr[r]; e < p.rowptr[r + 1]; ++e)
+        if (gs_skeleton_copy(pb, p.colind[e]) == cr) row.emplace_back((int)gs_skeleton_id(pb, p.colind[e]), v[e]);
+      std::sort(row.begin(), row.end());
+      for (auto &x : row) {
+        ci.push_back(x.first);
+        cv.push_back(x.second);
+      }
+      rp[r2 + 1] = (long long)ci.size();
+    }
+    if (rowptr) memcpy(rowptr, rp.data(), sizeof(long long) * (n + 1));
+    if (colind && !ci.empty()) memcpy(colind, ci.data(), sizeof(int) * ci.size());
+    if (val && !cv.empty()) memcpy(val, cv.data(), sizeof(double) * cv.size());
+    if (rhs)
+      for (size_t r = 0; r < n; ++r) rhs[gs_skeleton_id(pb, r)] = b[r];
+    return HDG_OK;
+  }
   if (rowptr)
     CUDA_TRY(ctx, cudaMemcpyAsync(rowptr, p.rowptr.data(), sizeof(long long) * p.rowptr.size(), cudaMemcpyDefault, ctx->stream));
   if (colind && p.nnz)
@@ -1136,7 +1334,6 @@ static int refine_fp64_correction(hdg_problem *pb, const OuterArgs &oa, double r
 }
 
 // Mixed-precision skeleton solve: FP32 inner PCG inside an FP64 residual loop.
-// Requires launch_pcg_setup to have produced the FP64 block inverses.
 static int solve_pcg_refined(hdg_problem *pb, double rtol, int maxit, int *it_out, double *rel_out) {
   hdg_context *ctx = pb->ctx;
   const size_t n = pb->mesh.nfree, nfd = pb->mesh.nfd, nbr = pb->pat.nblockrows;
@@ -1373,11 +1570,12 @@ int hdg_solve_skeleton(hdg_problem *pb, int solver, double rtol, int maxit, int 
       pb->h_pinned.bytes = 4096;
     }
     PcgArgs a = pcg_args(pb);
-    CUDA_TRY(ctx, launch_pcg_setup(a, rtol, ctx->stream, ctx->num_sms, &ctx->launches));
     if (pb->precision != HDG_PREC_FP64) {
+      // the FP64 block inverses are needed only if an FP64 correction solve runs
       status = solve_pcg_refined(pb, rtol, maxit, &it, &rel);
       if (status == HDG_ERR_CUDA) return status;
     } else {
+      CUDA_TRY(ctx, launch_pcg_setup(a, rtol, ctx->stream, ctx->num_sms, &ctx->launches));
       status = run_pcg64(pb, a, maxit, &it, &rel);
       if (status == HDG_ERR_CUDA) return status;
     }
@@ -1429,8 +1627,17 @@ int hdg_get_skeleton_values(hdg_problem *pb, double *out) {
   if (!pb->solved) return ctx->fail(HDG_ERR_STATE, "solve first");
   if (!out) return ctx->fail(HDG_ERR_INVALID, "null output");
   cudaSetDevice(ctx->device);
-  if (pb->mesh.nfree)
-    CUDA_TRY(ctx, cudaMemcpyAsync(out, pb->d_x.ptr, sizeof(double) * pb->mesh.nfree, cudaMemcpyDefault, ctx->stream));
+  const size_t nfree = pb->mesh.nfree;
+  if (nfree && pb->gs && pb->gst.copies > 1) {
+    std::vector<double> x(nfree), y(nfree);
+    CUDA_TRY(ctx, cudaMemcpyAsync(x.data(), pb->d_x.ptr, sizeof(double) * nfree, cudaMemcpyDeviceToHost,
+                                  ctx->stream));
+    CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    for (size_t r = 0; r < nfree; ++r) y[gs_skeleton_id(pb, r)] = x[r];
+    CUDA_TRY(ctx, cudaMemcpyAsync(out, y.data(), sizeof(double) * nfree, cudaMemcpyDefault, ctx->stream));
+  } else if (nfree) {
+    CUDA_TRY(ctx, cudaMemcpyAsync(out, pb->d_x.ptr, sizeof(double) * nfree, cudaMemcpyDefault, ctx->stream));
+  }
   CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   return HDG_OK;
 }
@@ -1442,17 +1649,28 @@ int hdg_get_free_dof_values(hdg_problem *pb, double *out) {
   if (!out) return ctx->fail(HDG_ERR_INVALID, "null output");
   cudaSetDevice(ctx->device);
   const size_t nc = pb->mesh.ncells, ni = pb->tab.ni;
-  const size_t w1 = first_field_width(pb), w2 = ni - w1;
   const double *u = pb->d_uint.as<double>();
-  // [first bulk field of all cells | second bulk field of all cells | free skeleton values]
-  CUDA_TRY(ctx, cudaMemcpy2DAsync(out, w1 * sizeof(double), u, ni * sizeof(double), w1 * sizeof(double), nc,
-                                  cudaMemcpyDefault, ctx->stream));
-  CUDA_TRY(ctx, cudaMemcpy2DAsync(out + nc * w1, w2 * sizeof(double), u + w1, ni * sizeof(double),
-                                  w2 * sizeof(double), nc, cudaMemcpyDefault, ctx->stream));
-  if (pb->mesh.nfree)
-    CUDA_TRY(ctx, cudaMemcpyAsync(out + nc * ni, pb->d_x.ptr, sizeof(double) * pb->mesh.nfree, cudaMemcpyDefault,
-                                  ctx->stream));
+  // [each bulk field of all cells, in the multi-field order | free skeleton values]
+  std::vector<size_t> widths;
+  if (pb->gs) {
+    for (int c = 0; c < pb->gst.copies; ++c) widths.push_back((size_t)pb->gst.ncA * pb->gst.nA);
+    for (int c = 0; c < pb->gst.copies; ++c) widths.push_back((size_t)pb->gst.ncB * pb->gst.nB);
+  } else {
+    widths.push_back(first_field_width(pb));
+    widths.push_back(ni - widths[0]);
+  }
+  size_t col = 0, off = 0;
+  for (size_t w : widths) {
+    CUDA_TRY(ctx, cudaMemcpy2DAsync(out + off, w * sizeof(double), u + col, ni * sizeof(double), w * sizeof(double),
+                                    nc, cudaMemcpyDefault, ctx->stream));
+    col += w;
+    off += nc * w;
+  }
   CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  if (pb->mesh.nfree) {
+    int rc = hdg_get_skeleton_values(pb, out + nc * ni);
+    if (rc) return rc;
+  }
   return HDG_OK;
 }
 
@@ -1464,7 +1682,10 @@ int hdg_l2_errors(hdg_problem *pb, double *err_flux, double *err_pres) {
   const size_t nc = pb->mesh.ncells;
   CUDA_TRY(ctx, pb->d_errs.reserve(sizeof(double) * 2 * nc));
   CellArgs a = cell_args(pb);
-  if (pb->physics == HDG_PHYSICS_ELASTICITY)
+  if (pb->gs)
+    CUDA_TRY(ctx, launch_l2_errors_gs(gs_args(pb), pb->d_uint.as<double>(), pb->d_errs.as<double>(), ctx->stream,
+                                      ctx->num_sms, &ctx->launches));
+  else if (pb->physics == HDG_PHYSICS_ELASTICITY)
     CUDA_TRY(ctx, launch_l2_errors_elasticity(a, pb->d_uint.as<double>(), pb->d_errs.as<double>(), ctx->stream,
                                               ctx->num_sms, &ctx->launches));
   else

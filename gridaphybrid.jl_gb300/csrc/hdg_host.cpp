@@ -384,7 +384,7 @@ TableOffsetsF pack_tables_ff(const RefTables &t, std::vector<float> &packed) {
 // facets Dirichlet.
 // ---------------------------------------------------------------------------
 int build_cartesian_mesh(int D, const int *cells, const double *domain, int k,
-                         HostMesh &m, std::string &err, int ncomp) {
+                         HostMesh &m, std::string &err, int ncomp, int nfd) {
   if (D < 2 || D > kMaxD) {
     err = "D must be 2 or 3";
     return HDG_ERR_INVALID;
@@ -410,7 +410,7 @@ int build_cartesian_mesh(int D, const int *cells, const double *domain, int k,
   m.k = k;
   m.cartesian = true;
   m.ncells = (int)nc;
-  m.nfd = ncomp * ipow(k + 1, D - 1);
+  m.nfd = nfd > 0 ? nfd : ncomp * ipow(k + 1, D - 1);
   for (int d = 0; d < D; ++d) {
     m.cells[d] = cells[d];
     m.domain[2 * d] = domain[2 * d];

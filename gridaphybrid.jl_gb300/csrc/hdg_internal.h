@@ -158,17 +158,26 @@ void lagrange1d(int k, int i, double x, double &v, double &dv);
 void gauss01(int np, std::vector<double> &x, std::vector<double> &w);
 
 // A scalar polynomial basis on the reference cube [0,1]^d: Q_k (tensor
-// Lagrange in Gridap's node order) or P_k (total degree <= k, Lagrange at the
-// simplex lattice points i/k; the constant for k = 0).
+// Lagrange in Gridap's node order; the constant for k = 0) or P_k (total
+// degree <= k, Lagrange at the simplex lattice points i/k; the constant for
+// k = 0), or a tensor Lagrange basis with an order per dimension.
 constexpr int kBasisQ = 0;
 constexpr int kBasisP = 1;
+// first bulk field of the Darcy form only: Raviart-Thomas RT_k on the box,
+// component d in the tensor space of order k+1 along d and k across
+constexpr int kBasisRT = 2;
 struct ScalarBasis {
   int d = 0, kind = kBasisQ, k = 0, nb = 0;
+  bool aniso = false;         // tensor Lagrange with an order per dimension (ko)
+  int ko[kMaxD] = {0, 0, 0};
   std::vector<int> lat;       // Q: nb x d lattice indices
   std::vector<int> mono;      // P: nb x d monomial exponents
   std::vector<double> coef;   // P: nb x nb, phi_a = sum_m coef[a nb + m] x^mono_m
   std::vector<double> nodes;  // nb x d nodal points
   int init(int dim, int basis_kind, int order);
+  // tensor Lagrange of order orders[e] along dimension e (equispaced nodes i/m,
+  // the midpoint for order 0), first dimension fastest
+  int init_aniso(int dim, const int *orders);
   // values (nb) and reference gradients (nb x d, may be null) at xi
   void eval(const double *xi, double *val, double *grad) const;
 };
@@ -177,26 +186,33 @@ struct ScalarBasis {
 // A the first bulk field (Darcy flux / elasticity stress), B the second
 // (pressure / displacement), T the trace on facets.  spaces[7] = {kindA, kA,
 // kindB, kB, kindT, kT, pm}; pm: P_m of the displacement in the tau terms.
-// All tables FP64, packed in `packed` at the offsets below (in doubles):
-//   MAA  nA x nA            int phiA_a phiA_b
-//   GAB  D x nA x nB        int d_e phiA_a phiB_b
-//   GBA  D x nB x nA        int d_e phiB_b phiA_a
-//   FBA  2D x nB x nA       int_F phiB_b phiA_a       (unit facet measure)
-//   FBB  2D x nB x nB       int_F phiB_b phiB_c, or with pm H_B L^{-1} H_B^T
-//   HA   2D x nA x nT       int_F phiA_a mu_m
-//   HB   2D x nB x nT       int_F phiB_b mu_m
-//   L    nT x nT            int_F mu_m mu_n
-//   qxi (nqv x D), qw (nqv), qphiA (nqv x nA), qphiB (nqv x nB)
+// All tables FP64, packed in `packed` at the offsets below (in doubles); the
+// A tables hold one slab per component c of the first field (nA functions
+// each; the slabs are equal unless the field is RT_k):
+//   MAA  ncA x nA x nA          int phiA_a phiA_b
+//   GAB  ncA x D x nA x nB      int d_e phiA_a phiB_b
+//   GBA  ncA x D x nB x nA      int d_e phiB_b phiA_a
+//   FBA  ncA x 2D x nB x nA     int_F phiB_b phiA_a       (unit facet measure)
+//   FBB  2D x nB x nB           int_F phiB_b phiB_c, or with pm H_B L^{-1} H_B^T
+//   HA   ncA x 2D x nA x nT     int_F phiA_a mu_m
+//   HB   2D x nB x nT           int_F phiB_b mu_m
+//   L    nT x nT                int_F mu_m mu_n
+//   qxi (nqv x D), qw (nqv), qphiA (ncA x nqv x nA), qphiB (nqv x nB)
+// copies > 1: that many decoupled copies of the form, each with its own
+// fields and its own skeleton field (a skeleton system of several fields).
+// Cell DOFs [A of copy 0 .. A of copy c-1 | B of copy 0 .. | per local facet:
+// the trace DOFs of copy 0, copy 1, ..].
 struct GsTables {
-  int D = 0, phys = 0, pm = 0;
+  int D = 0, phys = 0, pm = 0, copies = 1;
   int spaces[7] = {0, 0, 0, 0, 0, 0, 0};
-  ScalarBasis A, B, T;
+  ScalarBasis A[kMaxD > 6 ? kMaxD : 6], B, T;  // A: one basis per component
   int ncA = 0, ncB = 0, ncT = 0, nA = 0, nB = 0, nT = 0, ni = 0, nf = 0, nfd = 0, n = 0, n1 = 0, nqv = 0;
+  int ni1 = 0, nfd1 = 0;  // one copy: interior DOFs, DOFs per facet
   std::vector<double> packed;
   int oMAA = 0, oGAB = 0, oGBA = 0, oFBA = 0, oFBB = 0, oHA = 0, oHB = 0, oL = 0, oqxi = 0, oqw = 0, oqphiA = 0,
       oqphiB = 0;
 };
-int build_gs_tables(int D, int phys, const int *spaces, GsTables &t, std::string &err);
+int build_gs_tables(int D, int phys, const int *spaces, int copies, GsTables &t, std::string &err);
 
 // Offsets (in doubles) of each table inside the packed device table buffer.
 struct TableOffsets {
@@ -227,9 +243,10 @@ struct HostMesh {
   std::vector<int> facet_lface;   // nfacets x 2 : local facet index in that cell
   std::vector<int> facet_first_dof; // nfacets: first free DOF or -1
 };
-// ncomp: components of the facet field (1 scalar trace, D displacement trace)
+// ncomp: components of the facet field (1 scalar trace, D displacement trace);
+// nfd > 0 sets the DOFs per facet directly (general-space trace bases)
 int build_cartesian_mesh(int D, const int *cells, const double *domain, int k,
-                         HostMesh &m, std::string &err, int ncomp = 1);
+                         HostMesh &m, std::string &err, int ncomp = 1, int nfd = 0);
 int finish_mesh(HostMesh &m, std::string &err);  // derives facet_cell etc.
 
 // Skeleton CSR pattern and the block maps used by the deterministic gather.

@@ -157,6 +157,22 @@ struct CellArgs {
 // FP64 integration of the cell matrices/vectors (column-major n x n, n).
 cudaError_t launch_integrate_fp64(const CellArgs &a, double *A, double *b,
                                   cudaStream_t s, int num_sms, long long *launches);
+
+// General-space forms (fields with their own spaces; the tables of GsTables on
+// the device).  cell: geometry, coefficients and form parameters, with qxi /
+// qw / nqv the general-space quadrature.  DOFs per cell [A field of each copy
+// (ncA x nA) | B field of each copy (ncB x nB) | per local facet the trace of
+// each copy (ncT x nT)], component-major.
+struct GsArgs {
+  CellArgs cell;
+  int phys, nA, nB, nT, ncA, ncB, copies, ni1, nfd1, ni, nf, nfd, n, nqv;
+  const double *MAA, *GAB, *GBA, *FBA, *FBB, *HA, *HB, *L, *qphiA, *qphiB;
+};
+cudaError_t launch_integrate_gs(const GsArgs &g, double *A, double *b, cudaStream_t s, int num_sms,
+                                long long *launches);
+// per-cell squared L2 errors of the two bulk fields, summed over the copies (errs: ncells x 2)
+cudaError_t launch_l2_errors_gs(const GsArgs &g, const double *uint, double *errs, cudaStream_t s, int num_sms,
+                                long long *launches);
 // FP64 condensation of caller-provided cells.  fact (ncells x ni x (n+1)) may
 // be null; it receives [U11 | U12 | y] for the recovery.
 cudaError_t launch_condense_fp64(int ncells, int ni, int nf, const double *A,
@@ -292,6 +308,8 @@ cudaError_t launch_pcg_iteration_pair(const PcgArgs &a, cudaStream_t s, int num_
 cudaError_t launch_spmv(const PcgArgs &a, cudaStream_t s, long long *launches);
 // facet block sizes the PCG kernels are instantiated for
 bool pcg_supports_nfd(int nfd);
+// (facets per cell, DOFs per facet) the skeleton assembly is instantiated for
+bool assemble_supports(int nl, int nfd);
 
 // Inner FP32 PCG of the mixed-precision skeleton solve (solves M e = rhs,
 // M = sign*A, with FP32 values and vectors; dot products in float-float).

@@ -193,7 +193,7 @@ struct hdg_server {
   long long next_ticket = 1;
   long long submitted = 0, completed = 0, failed = 0;
   int running = 0, max_running = 0;
-  long long mesh_hits = 0, mesh_misses = 0, evictions = 0;
+  long long mesh_hits = 0, mesh_misses = 0, evictions = 0, retries = 0;
   unsigned long long clock = 0;
   bool stop = false;
   std::string err;
@@ -308,6 +308,38 @@ struct hdg_server {
       const Clock::time_point t_start = Clock::now();
       r.queue_ms = ms_between(job.t_submit, t_start);
       int rc = run(job, res, r);
+      if (rc == HDG_ERR_NOMEM) {
+        // The device ran out of memory below the admission budget: freed
+        // blocks that the memory pool keeps, or other users of the GPU.  Give
+        // the memory of the failed attempt and of every idle mesh back, return
+        // the pool's unused memory to the device, and run the request once more.
+        if (res) destroy_resident(res.get());
+        res.reset();
+        {
+          std::lock_guard<std::mutex> g(mu);
+          for (auto &m : idle) {
+            in_use -= m->bytes;
+            trash.push_back(std::move(m));
+            ++evictions;
+          }
+          idle.clear();
+          ++retries;
+        }
+        for (auto &t : trash) destroy_resident(t.get());
+        trash.clear();
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+          cudaDeviceSynchronize();
+          cudaMemPoolTrimTo(pool, 0);
+        }
+        cudaGetLastError();
+        r = hdg_response{};
+        r.ticket = job.ticket;
+        r.slot = slot;
+        r.footprint_bytes = job.footprint;
+        r.queue_ms = ms_between(job.t_submit, t_start);
+        rc = run(job, res, r);
+      }
       const Clock::time_point t_end = Clock::now();
       r.status = rc;
       if (rc != HDG_OK && res && res->ctx) {  // before a failed request's mesh (and context) goes
@@ -498,6 +530,7 @@ int hdg_server_stats(hdg_server *s, double *st) {
   st[10] = (double)s->evictions;
   st[11] = (double)s->max_running;
   st[12] = s->busy_ms;
+  st[13] = (double)s->retries;
   return HDG_OK;
 }
 

@@ -66,9 +66,13 @@ int ScalarBasis::init(int dim, int basis_kind, int order) {
   mono.clear();
   coef.clear();
   nodes.clear();
+  aniso = false;
   if (d < 0 || d > kMaxD || k < 0 || k > kMaxK) return -1;
+  if (kind == kBasisQ && k == 0) {  // Q_0: the constant
+    const int zero[kMaxD] = {0, 0, 0};
+    return init_aniso(dim, zero);
+  }
   if (kind == kBasisQ) {
-    if (k < 1) return -1;
     // Gridap's Lagrangian node order (vertices, then edges, faces, interior)
     nb = ipow_i(k + 1, d);
     lat = node_lattice(d, k);
@@ -111,7 +115,59 @@ int ScalarBasis::init(int dim, int basis_kind, int order) {
   return 0;
 }
 
+int ScalarBasis::init_aniso(int dim, const int *orders) {
+  d = dim;
+  kind = kBasisQ;
+  aniso = true;
+  k = 0;
+  lat.clear();
+  mono.clear();
+  coef.clear();
+  nodes.clear();
+  if (d < 0 || d > kMaxD) return -1;
+  nb = 1;
+  for (int e = 0; e < d; ++e) {
+    if (orders[e] < 0 || orders[e] > kMaxK) return -1;
+    ko[e] = orders[e];
+    k = std::max(k, orders[e]);
+    nb *= orders[e] + 1;
+  }
+  lat.resize((size_t)nb * std::max(d, 1));
+  nodes.resize((size_t)nb * std::max(d, 1));
+  for (int a = 0; a < nb; ++a)
+    for (int e = 0, r = a; e < d; r /= (ko[e] + 1), ++e) {
+      const int i = r % (ko[e] + 1);
+      lat[(size_t)a * d + e] = i;
+      nodes[(size_t)a * d + e] = ko[e] == 0 ? 0.5 : double(i) / ko[e];
+    }
+  return 0;
+}
+
 void ScalarBasis::eval(const double *xi, double *val, double *grad) const {
+  if (aniso) {
+    for (int a = 0; a < nb; ++a) {
+      double l[kMaxD], dl[kMaxD];
+      for (int e = 0; e < d; ++e) {
+        if (ko[e] == 0) {
+          l[e] = 1.0;
+          dl[e] = 0.0;
+        } else {
+          lagrange1d(ko[e], lat[(size_t)a * d + e], xi[e], l[e], dl[e]);
+        }
+      }
+      double v = 1.0;
+      for (int e = 0; e < d; ++e) v *= l[e];
+      val[a] = v;
+      if (grad)
+        for (int e = 0; e < d; ++e) {
+          double g = dl[e];
+          for (int j = 0; j < d; ++j)
+            if (j != e) g *= l[j];
+          grad[(size_t)a * d + e] = g;
+        }
+    }
+    return;
+  }
   if (kind == kBasisQ) {
     for (int a = 0; a < nb; ++a) {
       double l[kMaxD], dl[kMaxD];
@@ -164,7 +220,7 @@ static void facet_point(int D, int lf, const double *sp, double *xi) {
   for (int d = 0, j = 0; d < D; ++d) xi[d] = (d == dn) ? double(side) : sp[j++];
 }
 
-int build_gs_tables(int D, int phys, const int *spaces, GsTables &t, std::string &err) {
+int build_gs_tables(int D, int phys, const int *spaces, int copies, GsTables &t, std::string &err) {
   t = GsTables();
   if (D < 2 || D > kMaxD) {
     err = "D must be 2 or 3";
@@ -174,54 +230,72 @@ int build_gs_tables(int D, int phys, const int *spaces, GsTables &t, std::string
     err = "unknown physics";
     return HDG_ERR_INVALID;
   }
+  if (copies < 1 || copies > 4) {
+    err = "copies must be 1..4";
+    return HDG_ERR_INVALID;
+  }
   for (int i = 0; i < 7; ++i) t.spaces[i] = spaces[i];
-  if (t.A.init(D, spaces[0], spaces[1]) || t.B.init(D, spaces[2], spaces[3]) ||
-      t.T.init(D - 1, spaces[4], spaces[5])) {
-    err = "unsupported space (kind Q needs order 1..4, kind P order 0..4)";
-    return HDG_ERR_INVALID;
-  }
-  if (spaces[4] == kBasisP && spaces[5] < 1) {
-    err = "the trace space needs order >= 1";
-    return HDG_ERR_INVALID;
-  }
-  t.D = D;
-  t.phys = phys;
-  t.pm = spaces[6] != 0 && phys == HDG_PHYSICS_ELASTICITY;
   const int nsym = D * (D + 1) / 2;
   t.ncA = phys == HDG_PHYSICS_DARCY ? D : nsym;
   t.ncB = phys == HDG_PHYSICS_DARCY ? 1 : D;
   t.ncT = phys == HDG_PHYSICS_DARCY ? 1 : D;
-  t.nA = t.A.nb;
+  bool ok = true;
+  if (spaces[0] == kBasisRT) {
+    if (phys != HDG_PHYSICS_DARCY || spaces[1] < 0 || spaces[1] > 3) {
+      err = "RT_k (k = 0..3) is a flux space of the Darcy form";
+      return HDG_ERR_INVALID;
+    }
+    for (int c = 0; c < D; ++c) {
+      int ord[kMaxD];
+      for (int e = 0; e < D; ++e) ord[e] = spaces[1] + (e == c ? 1 : 0);
+      ok = ok && t.A[c].init_aniso(D, ord) == 0;
+    }
+  } else {
+    ok = t.A[0].init(D, spaces[0], spaces[1]) == 0;
+    for (int c = 1; c < t.ncA && ok; ++c) t.A[c] = t.A[0];
+  }
+  ok = ok && t.B.init(D, spaces[2], spaces[3]) == 0 && t.T.init(D - 1, spaces[4], spaces[5]) == 0;
+  if (!ok) {
+    err = "unsupported space (kind Q or P of order 0..4; RT_k, k = 0..3, for the Darcy flux)";
+    return HDG_ERR_INVALID;
+  }
+  t.D = D;
+  t.phys = phys;
+  t.copies = copies;
+  t.pm = spaces[6] != 0 && phys == HDG_PHYSICS_ELASTICITY;
+  t.nA = t.A[0].nb;
   t.nB = t.B.nb;
   t.nT = t.T.nb;
-  t.ni = t.ncA * t.nA + t.ncB * t.nB;
-  t.nfd = t.ncT * t.nT;
+  t.ni1 = t.ncA * t.nA + t.ncB * t.nB;
+  t.nfd1 = t.ncT * t.nT;
+  t.ni = copies * t.ni1;
+  t.nfd = copies * t.nfd1;
   t.nf = 2 * D * t.nfd;
   t.n = t.ni + t.nf;
-  const int kmax = std::max(spaces[1], std::max(spaces[3], spaces[5]));
+  int kmax = std::max(spaces[3], spaces[5]);
+  for (int c = 0; c < t.ncA; ++c) kmax = std::max(kmax, t.A[c].k);
   t.n1 = kmax + 2;  // Gauss points per direction: exact for degree 2 kmax + 3
   t.nqv = ipow_i(t.n1, D);
-  const int nqf = ipow_i(t.n1, D - 1), nl = 2 * D;
+  const int nqf = ipow_i(t.n1, D - 1), nl = 2 * D, ncA = t.ncA;
   const int nA = t.nA, nB = t.nB, nT = t.nT;
   std::vector<double> x1, w1;
   gauss01(t.n1, x1, w1);
-  // layout
   size_t o = 0;
   auto take = [&](int &off, size_t count) {
     off = (int)o;
     o += count;
   };
-  take(t.oMAA, (size_t)nA * nA);
-  take(t.oGAB, (size_t)D * nA * nB);
-  take(t.oGBA, (size_t)D * nB * nA);
-  take(t.oFBA, (size_t)nl * nB * nA);
+  take(t.oMAA, (size_t)ncA * nA * nA);
+  take(t.oGAB, (size_t)ncA * D * nA * nB);
+  take(t.oGBA, (size_t)ncA * D * nB * nA);
+  take(t.oFBA, (size_t)ncA * nl * nB * nA);
   take(t.oFBB, (size_t)nl * nB * nB);
-  take(t.oHA, (size_t)nl * nA * nT);
+  take(t.oHA, (size_t)ncA * nl * nA * nT);
   take(t.oHB, (size_t)nl * nB * nT);
   take(t.oL, (size_t)nT * nT);
   take(t.oqxi, (size_t)t.nqv * D);
   take(t.oqw, (size_t)t.nqv);
-  take(t.oqphiA, (size_t)t.nqv * nA);
+  take(t.oqphiA, (size_t)ncA * t.nqv * nA);
   take(t.oqphiB, (size_t)t.nqv * nB);
   t.packed.assign(o, 0.0);
   double *P = t.packed.data();
@@ -233,19 +307,21 @@ int build_gs_tables(int D, int phys, const int *spaces, GsTables &t, std::string
       xi[d] = x1[r % t.n1];
       wq *= w1[r % t.n1];
     }
-    t.A.eval(xi, pA.data(), dA.data());
     t.B.eval(xi, pB.data(), dB.data());
     for (int d = 0; d < D; ++d) P[t.oqxi + q * D + d] = xi[d];
     P[t.oqw + q] = wq;
-    for (int a = 0; a < nA; ++a) P[t.oqphiA + (size_t)q * nA + a] = pA[a];
     for (int b = 0; b < nB; ++b) P[t.oqphiB + (size_t)q * nB + b] = pB[b];
-    for (int a = 0; a < nA; ++a) {
-      for (int a2 = 0; a2 < nA; ++a2) P[t.oMAA + (size_t)a * nA + a2] += wq * pA[a] * pA[a2];
-      for (int b = 0; b < nB; ++b)
-        for (int e = 0; e < D; ++e) {
-          P[t.oGAB + ((size_t)e * nA + a) * nB + b] += wq * dA[(size_t)a * D + e] * pB[b];
-          P[t.oGBA + ((size_t)e * nB + b) * nA + a] += wq * dB[(size_t)b * D + e] * pA[a];
-        }
+    for (int c = 0; c < ncA; ++c) {
+      t.A[c].eval(xi, pA.data(), dA.data());
+      for (int a = 0; a < nA; ++a) P[t.oqphiA + ((size_t)c * t.nqv + q) * nA + a] = pA[a];
+      for (int a = 0; a < nA; ++a) {
+        for (int a2 = 0; a2 < nA; ++a2) P[t.oMAA + ((size_t)c * nA + a) * nA + a2] += wq * pA[a] * pA[a2];
+        for (int b = 0; b < nB; ++b)
+          for (int e = 0; e < D; ++e) {
+            P[t.oGAB + (((size_t)c * D + e) * nA + a) * nB + b] += wq * dA[(size_t)a * D + e] * pB[b];
+            P[t.oGBA + (((size_t)c * D + e) * nB + b) * nA + a] += wq * dB[(size_t)b * D + e] * pA[a];
+          }
+      }
     }
   }
   // facets (unit facet measure)
@@ -261,15 +337,18 @@ int build_gs_tables(int D, int phys, const int *spaces, GsTables &t, std::string
     for (int lf = 0; lf < nl; ++lf) {
       double xi[kMaxD];
       facet_point(D, lf, sp, xi);
-      t.A.eval(xi, pA.data(), nullptr);
       t.B.eval(xi, pB.data(), nullptr);
       for (int b = 0; b < nB; ++b) {
-        for (int a = 0; a < nA; ++a) P[t.oFBA + ((size_t)lf * nB + b) * nA + a] += wq * pB[b] * pA[a];
         for (int b2 = 0; b2 < nB; ++b2) P[t.oFBB + ((size_t)lf * nB + b) * nB + b2] += wq * pB[b] * pB[b2];
         for (int m = 0; m < nT; ++m) P[t.oHB + ((size_t)lf * nB + b) * nT + m] += wq * pB[b] * mu[m];
       }
-      for (int a = 0; a < nA; ++a)
-        for (int m = 0; m < nT; ++m) P[t.oHA + ((size_t)lf * nA + a) * nT + m] += wq * pA[a] * mu[m];
+      for (int c = 0; c < ncA; ++c) {
+        t.A[c].eval(xi, pA.data(), nullptr);
+        for (int b = 0; b < nB; ++b)
+          for (int a = 0; a < nA; ++a) P[t.oFBA + (((size_t)c * nl + lf) * nB + b) * nA + a] += wq * pB[b] * pA[a];
+        for (int a = 0; a < nA; ++a)
+          for (int m = 0; m < nT; ++m) P[t.oHA + (((size_t)c * nl + lf) * nA + a) * nT + m] += wq * pA[a] * mu[m];
+      }
     }
   }
   if (t.pm) {

@@ -10,7 +10,9 @@
 
 namespace hdg {
 
-constexpr uint32_t kBulkWaitPolls = 1u << 22;
+// One mbarrier try_wait suspends for up to a few microseconds (3.8 us measured on
+// a GB300), so 2^18 polls give up after about one second.
+constexpr uint32_t kBulkWaitPolls = 1u << 18;
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -64,10 +66,31 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   return ok != 0;
 }
 
-// true once phase `parity` of bar has completed; false after kBulkWaitPolls polls
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
-  for (uint32_t i = 0; i < kBulkWaitPolls; ++i)
+// true once phase `parity` of bar has completed; false after `polls` polls
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity,
+                                                  uint32_t polls = kBulkWaitPolls) {
+  for (uint32_t i = 0; i < polls; ++i)
     if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+// Grid barriers of co-resident (cooperative) grids wait on a generation word;
+// a poll takes about 0.2 us, so 2^22 polls give up after about one second.
+constexpr uint32_t kGridWaitPolls = 1u << 22;
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// true once *word differs from `old`; false after `polls` polls (32 ns apart)
+__device__ __forceinline__ bool wait_word_change(const unsigned *word, unsigned old,
+                                                 uint32_t polls = kGridWaitPolls) {
+  for (uint32_t i = 0; i < polls; ++i) {
+    if (ld_acquire_u32(word) != old) return true;
+    __nanosleep(32);
+  }
   return false;
 }
 

@@ -116,57 +116,65 @@ __global__ void __launch_bounds__(kPcgThreads) pcg32_replace_kernel(Pcg32Args a,
 
 // W = blockdiag(L_f^{-1}): one warp per free facet, right-looking Cholesky of
 // sign*D_f in shared memory, then each lane forms one column of L^{-1} by
-// forward substitution.  A block that is not positive definite gets W = I.
-constexpr int kCholWarps = 4;
+// forward substitution.  In FP32 (the FP64 pipe runs at 1/64 of the FP32
+// rate on this part): W is a scaling of the inner frame, and every use of it
+// (the records, the inner right-hand side, the correction back-transform)
+// reads the same values, so its own rounding does not enter the solution.  A
+// block that is not positive definite gets W = I.
+constexpr int kCholWarps = 8;
+template <int NFD>
 __global__ void __launch_bounds__(32 * kCholWarps) block_chol_inv_kernel(PcgArgs a, double *W) {
-  extern __shared__ double csm[];  // kCholWarps x (L, L^{-1}) x nfd^2
-  const int nfd = a.nfd, nb = nfd * nfd;
+  constexpr int NB = NFD * NFD;
+  __shared__ float csm[kCholWarps][2][NB];
+  __shared__ float inv_diag[kCholWarps][NFD];
   const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
-  double *L = csm + (size_t)wl * 2 * nb, *Li = L + nb;
+  float *L = csm[wl][0], *Li = csm[wl][1];
   for (int br = blockIdx.x * kCholWarps + wl; br < a.nblockrows; br += gridDim.x * kCholWarps) {
     const int blk = a.diag_blk[br];
     const int64_t off = a.blk_off[blk];
     const int rl = a.blk_rowlen[blk];
-    for (int e = lane; e < nb; e += 32) {
-      const int i = e / nfd, j = e - i * nfd;
-      L[e] = a.sign * a.val[off + (int64_t)i * rl + j];
+    for (int e = lane; e < NB; e += 32) {
+      const int i = e / NFD, j = e - i * NFD;
+      L[e] = (float)(a.sign * a.val[off + (int64_t)i * rl + j]);
     }
     __syncwarp();
     bool ok = true;
-    for (int c = 0; c < nfd; ++c) {
-      const double d = L[c * nfd + c];
-      if (!(d > 0.0) || !isfinite(d)) {  // the same value in every lane: a uniform exit
+    for (int c = 0; c < NFD; ++c) {
+      const float d = L[c * NFD + c];
+      if (!(d > 0.0f) || !isfinite(d)) {  // the same value in every lane: a uniform exit
         ok = false;
         break;
       }
-      const double sd = sqrt(d), inv = 1.0 / sd;
+      const float sd = sqrtf(d), inv = 1.0f / sd;
       __syncwarp();
-      for (int i = c + 1 + lane; i < nfd; i += 32) L[i * nfd + c] *= inv;
-      if (lane == 0) L[c * nfd + c] = sd;
+      for (int i = c + 1 + lane; i < NFD; i += 32) L[i * NFD + c] *= inv;
+      if (lane == 0) {
+        L[c * NFD + c] = sd;
+        inv_diag[wl][c] = inv;
+      }
       __syncwarp();
-      const int m = nfd - c - 1;
-      for (int e = lane; e < m * m; e += 32) {
-        const int i = c + 1 + e / m, j = c + 1 + e % m;
-        if (j <= i) L[i * nfd + j] -= L[i * nfd + c] * L[j * nfd + c];
+      for (int e = lane; e < NB; e += 32) {
+        const int i = e / NFD, j = e - i * NFD;
+        if (j > c && j <= i) L[i * NFD + j] -= L[i * NFD + c] * L[j * NFD + c];
       }
       __syncwarp();
     }
     if (ok)
-      for (int j = lane; j < nfd; j += 32)
-        for (int i = 0; i < nfd; ++i) {
+      for (int j = lane; j < NFD; j += 32)
+        for (int i = 0; i < NFD; ++i) {
           if (i < j) {
-            Li[i * nfd + j] = 0.0;
+            Li[i * NFD + j] = 0.0f;
             continue;
           }
-          double v = i == j ? 1.0 : 0.0;
-          for (int k = j; k < i; ++k) v -= L[i * nfd + k] * Li[k * nfd + j];
-          Li[i * nfd + j] = v / L[i * nfd + i];
+          float v = i == j ? 1.0f : 0.0f;
+          for (int k = j; k < i; ++k) v = fmaf(-L[i * NFD + k], Li[k * NFD + j], v);
+          Li[i * NFD + j] = v * inv_diag[wl][i];
         }
     __syncwarp();
-    double *out = W + (size_t)br * nb;
-    for (int e = lane; e < nb; e += 32) {
-      const int i = e / nfd, j = e - i * nfd;
-      out[e] = ok ? Li[e] : (i == j ? 1.0 : 0.0);
+    double *out = W + (size_t)br * NB;
+    for (int e = lane; e < NB; e += 32) {
+      const int i = e / NFD, j = e - i * NFD;
+      out[e] = ok ? (double)Li[e] : (i == j ? 1.0 : 0.0);
     }
     __syncwarp();
   }
@@ -249,16 +257,73 @@ __global__ void pack_cell_blocks_kernel(int ncells, int nl, int nfd, int rec, do
   }
 }
 
+// The same kernel with the block shape at compile time (constant divisors,
+// the upper-block decode from a table).
+template <int NL, int NFD>
+__global__ void __launch_bounds__(256) pack_cell_blocks_t(int ncells, int rec, double sign,
+                                                          const double *__restrict__ S, const int *__restrict__ cell_blk,
+                                                          const double *__restrict__ W, float *__restrict__ out) {
+  constexpr int NF = NL * NFD, NB = NFD * NFD, NBLK = NL * (NL + 1) / 2;
+  extern __shared__ double Ss[];
+  float *Ws = reinterpret_cast<float *>(Ss + NF * NF);
+  float *Ts = Ws + NL * NB;
+  float *Us = Ts + NBLK * NB;
+  __shared__ unsigned char blo[NBLK], bhi[NBLK];
+  if (threadIdx.x < NBLK) {
+    int lo, hi;
+    upper_block(NL, threadIdx.x, lo, hi);
+    blo[threadIdx.x] = (unsigned char)lo;
+    bhi[threadIdx.x] = (unsigned char)hi;
+  }
+  for (int c = blockIdx.x; c < ncells; c += gridDim.x) {
+    const double *Sc = S + (size_t)c * NF * NF;
+    for (int e = threadIdx.x; e < NF * NF; e += blockDim.x) Ss[e] = Sc[e];
+    for (int e = threadIdx.x; e < NL * NB; e += blockDim.x) {
+      const int lf = e / NB, w = e - lf * NB, r = w / NFD, q = w - r * NFD;
+      const int ent = cell_blk[(size_t)c * NL + lf];
+      Ws[e] = ent >= 0 ? (float)W[(size_t)(ent >> 1) * NB + w] : (r == q ? 1.0f : 0.0f);
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < NBLK * NB; e += blockDim.x) {
+      const int blk = e / NB, w = e - blk * NB, p = w / NFD, q = w - p * NFD;
+      const int i = blo[blk] * NFD + p, j = bhi[blk] * NFD + q;
+      Ts[e] = (float)(0.5 * sign * (Ss[i + NF * j] + Ss[j + NF * i]));
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < NBLK * NB; e += blockDim.x) {
+      const int blk = e / NB, w = e - blk * NB, p = w / NFD, sc = w - p * NFD;
+      const float *Wh = Ws + bhi[blk] * NB + sc * NFD;
+      const float *T = Ts + blk * NB + p * NFD;
+      float u = 0.0f;
+      for (int q = 0; q <= sc; ++q) u = fmaf(T[q], Wh[q], u);
+      Us[e] = u;
+    }
+    __syncthreads();
+    float *o = out + (size_t)c * rec;
+    for (int e = threadIdx.x; e < rec; e += blockDim.x) {
+      float v = 0.0f;
+      if (e < NBLK * NB) {
+        const int blk = e / NB, w = e - blk * NB, r = w / NFD, sc = w - r * NFD;
+        const float *Wl = Ws + blo[blk] * NB + r * NFD;
+        const float *U = Us + blk * NB + sc;
+        for (int p = 0; p <= r; ++p) v = fmaf(Wl[p], U[p * NFD], v);
+      }
+      o[e] = v;
+    }
+    __syncthreads();
+  }
+}
+
 // The same records for large cells (the whole S_c does not fit a CTA's
 // shared memory several times over): one work item per (cell, upper block),
 // the block and its transposed partner staged as two nfd x nfd tiles.
 __global__ void pack_cell_blocks_tiled_kernel(int ncells, int nl, int nfd, int rec, double sign,
                                               const double *__restrict__ S, const int *__restrict__ cell_blk,
                                               const double *__restrict__ W, float *__restrict__ out) {
-  extern __shared__ double T[];  // 2 nb doubles, then 3 nb floats
+  extern __shared__ double T[];  // 2 nb doubles, then 4 nb floats
   const int nf = nl * nfd, nb = nfd * nfd, nblk = nl * (nl + 1) / 2;
   double *T1 = T, *T2 = T + nb;
-  float *Wl = reinterpret_cast<float *>(T + 2 * nb), *Wh = Wl + nb, *U = Wh + nb;
+  float *Wl = reinterpret_cast<float *>(T + 2 * nb), *Wh = Wl + nb, *U = Wh + nb, *Ts = U + nb;
   const long long items = (long long)ncells * nblk;
   for (long long it = blockIdx.x; it < items; it += gridDim.x) {
     const int c = (int)(it / nblk), blk = (int)(it - (long long)c * nblk);
@@ -276,12 +341,17 @@ __global__ void pack_cell_blocks_tiled_kernel(int ncells, int nl, int nfd, int r
       Wh[e] = eh >= 0 ? (float)W[(size_t)(eh >> 1) * nb + e] : (wr == wc ? 1.0f : 0.0f);
     }
     __syncthreads();
-    // U[p][s] = sum_{q <= s} sign (S(lo p, hi q) + S(hi q, lo p))/2 W_hi[s][q]
+    // Ts[p][q] = sign (S(lo p, hi q) + S(hi q, lo p))/2, one FP64 sum per entry
+    for (int e = threadIdx.x; e < nb; e += blockDim.x) {
+      const int p = e / nfd, q = e - p * nfd;
+      Ts[e] = (float)(0.5 * sign * (T1[p + nfd * q] + T2[q + nfd * p]));
+    }
+    __syncthreads();
+    // U[p][s] = sum_{q <= s} Ts[p][q] W_hi[s][q]
     for (int e = threadIdx.x; e < nb; e += blockDim.x) {
       const int p = e / nfd, sc = e - p * nfd;
       float u = 0.0f;
-      for (int q = 0; q <= sc; ++q)
-        u = fmaf((float)(0.5 * sign * (T1[p + nfd * q] + T2[q + nfd * p])), Wh[sc * nfd + q], u);
+      for (int q = 0; q <= sc; ++q) u = fmaf(Ts[p * nfd + q], Wh[sc * nfd + q], u);
       U[e] = u;
     }
     __syncthreads();
@@ -596,15 +666,29 @@ __global__ void __launch_bounds__(kPcgThreads) outer_residual_kernel(OuterArgs a
 // Launchers
 // ---------------------------------------------------------------------------
 cudaError_t launch_block_chol_inv(const PcgArgs &a, double *W, cudaStream_t s, int num_sms, long long *launches) {
-  if (a.nfd > 32 || a.nblockrows < 1) return a.nblockrows < 1 ? cudaSuccess : cudaErrorInvalidValue;
-  const size_t smem = sizeof(double) * kCholWarps * 2 * a.nfd * a.nfd;
-  if (smem > 48 * 1024) {
-    cudaError_t e = cudaFuncSetAttribute(block_chol_inv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-  }
+  if (a.nblockrows < 1) return cudaSuccess;
   int g = (a.nblockrows + kCholWarps - 1) / kCholWarps;
-  if (g > num_sms * 16) g = num_sms * 16;
-  block_chol_inv_kernel<<<g, 32 * kCholWarps, smem, s>>>(a, W);
+  if (g > num_sms * 8) g = num_sms * 8;
+  switch (a.nfd) {
+#define HDG_CHOL_CASE(N) \
+  case N:                \
+    block_chol_inv_kernel<N><<<g, 32 * kCholWarps, 0, s>>>(a, W); break;
+    HDG_CHOL_CASE(1)
+    HDG_CHOL_CASE(2)
+    HDG_CHOL_CASE(3)
+    HDG_CHOL_CASE(4)
+    HDG_CHOL_CASE(5)
+    HDG_CHOL_CASE(6)
+    HDG_CHOL_CASE(8)
+    HDG_CHOL_CASE(9)
+    HDG_CHOL_CASE(12)
+    HDG_CHOL_CASE(16)
+    HDG_CHOL_CASE(25)
+    HDG_CHOL_CASE(27)
+#undef HDG_CHOL_CASE
+    default:
+      return cudaErrorInvalidValue;
+  }
   ++*launches;
   return cudaGetLastError();
 }
@@ -628,7 +712,7 @@ static size_t cellop_dyn_smem(int nstage) {
 }
 
 #define HDG_CELLOP_CASES(X) \
-  X(4, 2) X(4, 3) X(4, 4) X(4, 5) X(4, 6) X(4, 8) X(6, 4) X(6, 9) X(6, 12) X(6, 16) X(6, 25) X(6, 27)
+  X(4, 1) X(6, 1) X(4, 2) X(4, 3) X(4, 4) X(4, 5) X(4, 6) X(4, 8) X(6, 3) X(6, 4) X(6, 6) X(6, 9) X(6, 12) X(6, 16) X(6, 25) X(6, 27)
 
 bool cellop_supported(int nl, int nfd) {
 #define X(L, F) \
@@ -682,7 +766,7 @@ cudaError_t launch_pack_cell_blocks(int ncells, int nl, int nfd, double sign, co
   const int nf = nl * nfd, nb = nfd * nfd, nblk = nl * (nl + 1) / 2;
   const size_t smem = sizeof(double) * nf * nf + sizeof(float) * (size_t)(nl + 2 * nblk) * nb;
   if (smem > 64 * 1024) {  // large cells: block-pair tiles
-    const size_t tsmem = 2 * sizeof(double) * nb + 3 * sizeof(float) * nb;
+    const size_t tsmem = 2 * sizeof(double) * nb + 4 * sizeof(float) * nb;
     if (tsmem > 48 * 1024) return cudaErrorInvalidValue;
     const long long items = (long long)ncells * nblk;
     long long grid = items < (long long)num_sms * 16 ? items : (long long)num_sms * 16;
@@ -692,11 +776,24 @@ cudaError_t launch_pack_cell_blocks(int ncells, int nl, int nfd, double sign, co
     ++*launches;
     return cudaGetLastError();
   }
-  cudaError_t e = cudaFuncSetAttribute(pack_cell_blocks_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return e;
   int grid = ncells < num_sms * 16 ? ncells : num_sms * 16;
   if (grid < 1) grid = 1;
-  pack_cell_blocks_kernel<<<grid, 256, smem, s>>>(ncells, nl, nfd, cellop_rec(nl, nfd), sign, S, cell_blk, W, out);
+  cudaError_t e = cudaErrorInvalidValue;
+#define X(L, F)                                                                                              \
+  if (nl == L && nfd == F) {                                                                                 \
+    e = cudaFuncSetAttribute(pack_cell_blocks_t<L, F>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+    if (e == cudaSuccess)                                                                                    \
+      pack_cell_blocks_t<L, F><<<grid, 256, smem, s>>>(ncells, cellop_rec(L, F), sign, S, cell_blk, W, out);  \
+  }
+  HDG_CELLOP_CASES(X)
+#undef X
+  if (e == cudaErrorInvalidValue) {  // a shape without an instance: the runtime-sized kernel
+    e = cudaFuncSetAttribute(pack_cell_blocks_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    pack_cell_blocks_kernel<<<grid, 256, smem, s>>>(ncells, nl, nfd, cellop_rec(nl, nfd), sign, S, cell_blk, W, out);
+  } else if (e != cudaSuccess) {
+    return e;
+  }
   ++*launches;
   return cudaGetLastError();
 }
@@ -762,6 +859,7 @@ cudaError_t launch_outer_update(const OuterArgs &a, const float *e, cudaStream_t
   else
     outer_axpy_kernel<<<g, 256, 0, s>>>(a.n, e, a.x);
   switch (a.nfd) {
+    case 1: outer_residual_kernel<1><<<a.nparts, kPcgThreads, 0, s>>>(a); break;
     case 2: outer_residual_kernel<2><<<a.nparts, kPcgThreads, 0, s>>>(a); break;
     case 3: outer_residual_kernel<3><<<a.nparts, kPcgThreads, 0, s>>>(a); break;
     case 4: outer_residual_kernel<4><<<a.nparts, kPcgThreads, 0, s>>>(a); break;

@@ -27,14 +27,7 @@ namespace hdg {
 
 namespace {
 
-constexpr uint32_t kGridWaitPolls = 1u << 24;
 constexpr int kPersistStagesMax = 8;
-
-__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
-  unsigned v;
-  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
 
 // Grid-wide barrier of a co-resident grid: arrive on count; the last arriver
 // resets it and opens the next generation.  Returns false (in every thread of
@@ -50,14 +43,7 @@ __device__ bool grid_barrier(unsigned *count, unsigned *gen, unsigned &my_gen, i
       __threadfence();
       atomicAdd(gen, 1u);
     } else {
-      uint32_t polls = 0;
-      while (ld_acquire_u32(gen) == g) {
-        if (++polls >= kGridWaitPolls) {
-          ok = 0;
-          break;
-        }
-        __nanosleep(32);
-      }
+      ok = wait_word_change(gen, g) ? 1 : 0;
     }
     __threadfence();
     my_gen = g + 1;
@@ -301,7 +287,7 @@ static int persistent_grid(size_t smem_optin, int num_sms, int want, int *nstage
 }
 
 #define HDG_PERSIST_CASES(X) \
-  X(4, 2) X(4, 3) X(4, 4) X(4, 5) X(4, 6) X(4, 8) X(6, 4) X(6, 9) X(6, 12) X(6, 16) X(6, 25) X(6, 27)
+  X(4, 1) X(6, 1) X(4, 2) X(4, 3) X(4, 4) X(4, 5) X(4, 6) X(4, 8) X(6, 3) X(6, 4) X(6, 6) X(6, 9) X(6, 12) X(6, 16) X(6, 25) X(6, 27)
 
 int pcg32_persistent_config(int nl, int nfd, size_t smem_optin, int num_sms, int want, int *nstage, size_t *smem) {
 #define X(L, F) \

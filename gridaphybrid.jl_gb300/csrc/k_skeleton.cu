@@ -127,6 +127,7 @@ cudaError_t launch_assemble(const AssembleArgs &a, const double *S, const double
     }
     HDG_ASM(4, 2) HDG_ASM(4, 3) HDG_ASM(4, 4) HDG_ASM(4, 5) HDG_ASM(6, 1) HDG_ASM(6, 4) HDG_ASM(6, 9)
     HDG_ASM(6, 16) HDG_ASM(6, 25) HDG_ASM(4, 1) HDG_ASM(4, 6) HDG_ASM(4, 8) HDG_ASM(6, 12) HDG_ASM(6, 27)
+    HDG_ASM(6, 3) HDG_ASM(6, 6)
     else return cudaErrorInvalidValue;
 #undef HDG_ASM
     ++*launches;
@@ -480,6 +481,7 @@ static cudaError_t spmv_dispatch(const PcgArgs &a, const V *val, const double *p
 #define HDG_SPMV_CASE(N) \
   case N:                \
     pcg_spmv_kernel<V, N><<<a.nparts, kPcgThreads, 0, s>>>(a, val, po, pn); break;
+    HDG_SPMV_CASE(1)
     HDG_SPMV_CASE(2)
     HDG_SPMV_CASE(3)
     HDG_SPMV_CASE(4)
@@ -502,9 +504,16 @@ static cudaError_t spmv_any(const PcgArgs &a, const double *po, double *pn, cuda
   return a.val32 ? spmv_dispatch<float>(a, a.val32, po, pn, s) : spmv_dispatch<double>(a, a.val, po, pn, s);
 }
 
+bool assemble_supports(int nl, int nfd) {
+  if (nl == 4) return nfd == 1 || nfd == 2 || nfd == 3 || nfd == 4 || nfd == 5 || nfd == 6 || nfd == 8;
+  return nl == 6 && (nfd == 1 || nfd == 3 || nfd == 4 || nfd == 6 || nfd == 9 || nfd == 12 || nfd == 16 ||
+                     nfd == 25 || nfd == 27);
+}
+
 bool pcg_supports_nfd(int nfd) {
-  // scalar traces (k+1)^(D-1); displacement traces D (k+1)^(D-1): 4, 6, 8 (2D), 12, 27 (3D k=1, 2)
-  return nfd == 2 || nfd == 3 || nfd == 4 || nfd == 5 || nfd == 6 || nfd == 8 || nfd == 9 || nfd == 12 ||
+  // scalar traces (k+1)^(D-1) (1: RT_0 / Q_0 multipliers); displacement traces D (k+1)^(D-1): 4, 6, 8
+  // (2D), 12, 27 (3D k=1, 2)
+  return nfd == 1 || nfd == 2 || nfd == 3 || nfd == 4 || nfd == 5 || nfd == 6 || nfd == 8 || nfd == 9 || nfd == 12 ||
          nfd == 16 || nfd == 25 || nfd == 27;
 }
 

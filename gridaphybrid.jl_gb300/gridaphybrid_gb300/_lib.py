@@ -35,6 +35,9 @@ HDG_EPROBLEM_LINEAR = 0
 HDG_EPROBLEM_SMOOTH = 1
 HDG_SOLVER_PCG = 0
 HDG_SOLVER_DIRECT = 1
+HDG_SPACE_Q = 0
+HDG_SPACE_P = 1
+HDG_SPACE_RT = 2
 
 HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))),
                       "include", "hdg_gb300.h")
@@ -81,6 +84,7 @@ SIGNATURES = {
     "hdg_problem_create_cartesian": (_i, [_vp, _i, _vp, _vp, _i, ctypes.POINTER(_vp)]),
     "hdg_problem_create": (_i, [_vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp, ctypes.POINTER(_vp)]),
     "hdg_problem_create_cartesian_physics": (_i, [_vp, _i, _vp, _vp, _i, _i, ctypes.POINTER(_vp)]),
+    "hdg_problem_create_cartesian_spaces": (_i, [_vp, _i, _vp, _vp, _i, _vp, _i, ctypes.POINTER(_vp)]),
     "hdg_set_elasticity": (_i, [_vp, _d, _d, _i]),
     "hdg_problem_destroy": (_i, [_vp]),
     "hdg_problem_info": (_i, [_vp, _vp]),
@@ -102,6 +106,7 @@ SIGNATURES = {
     "hdg_context_set_persistent_pcg": (_i, [_vp, ctypes.c_int]),
     "hdg_time_kernel": (_i, [_vp, _i, _i, _vp]),
     "hdg_measure_pipe_peaks": (_i, [_vp, _vp, _vp]),
+    "hdg_check_bounded_waits": (_i, [_vp, ctypes.c_uint, _vp, _vp]),
     "hdg_problem_device_bytes": (_i, [_vp, _vp]),
     "hdg_set_refinement": (_i, [_vp, _d, _i]),
     "hdg_newton_solve": (_i, [_vp, _i, _d, _i, _d, _i, _vp, _vp, _vp]),

@@ -13,8 +13,15 @@ Mirrors the reference's user API (test/DarcyHDGTests.jl:27-142):
 Python cannot evaluate Gridap weak-form closures, so the weak form is a
 descriptor of the Darcy HDG form the reference's tests write out
 (test/DarcyHDGTests.jl:125-135), with the textbook stabilisation as an option
-and a per-cell permeability.  Integration, condensation, assembly, the
-skeleton solve and the recovery all run in libgridaphybrid_gb300.
+and a per-cell permeability, or of the elasticity HDG form
+(test/LinearElasticityHDGTests.jl:140-150).  Each field takes its own space
+(ReferenceFE(lagrangian, T, k; space=:Q or :P), or raviart_thomas for the
+Darcy flux: the RT-H form of test/DarcyRTHTests.jl is DarcyHDG(tau=0)), and
+a multi-field space of c copies [A_1..A_c, B_1..B_c, T_1..T_c] with
+bulk_fields [1..2c] and skeleton_fields [2c+1..3c] sums the form once per
+copy (test/MultiFieldLagrangeMultipliersTests.jl).  Integration,
+condensation, assembly, the skeleton solve and the recovery all run in
+libgridaphybrid_gb300.
 """
 import ctypes
 
@@ -23,6 +30,7 @@ import numpy as np
 from . import _lib
 
 lagrangian = "lagrangian"
+raviart_thomas = "raviart_thomas"
 VectorValue = "VectorValue"
 SymTensorValue = "SymTensorValue"
 Float64 = "Float64"
@@ -100,11 +108,21 @@ def get_cell_owner_normal_vector(skel, facet_cells=None, cell_facets=None):
 
 
 class ReferenceFE:
+    """ReferenceFE(lagrangian, T, order; space=:Q|:P) or
+    ReferenceFE(raviart_thomas, Float64, order) on the Cartesian cells."""
+
+    KINDS = {"Q": _lib.HDG_SPACE_Q, "P": _lib.HDG_SPACE_P}
+
     def __init__(self, kind, value_type, order, space="Q"):
-        if kind != lagrangian:
-            raise ValueError("only lagrangian reference FEs are supported")
-        if space != "Q":
-            raise ValueError("only Q_k (space='Q') tensor-product Lagrangian spaces are supported")
+        space = str(space).lstrip(":")
+        if kind == raviart_thomas:
+            self.kind = _lib.HDG_SPACE_RT
+        elif kind == lagrangian:
+            if space not in self.KINDS:
+                raise ValueError("lagrangian spaces are space='Q' (tensor product) or space='P' (total degree)")
+            self.kind = self.KINDS[space]
+        else:
+            raise ValueError("reference FEs: lagrangian or raviart_thomas")
         self.value_type = value_type
         self.order = int(order)
 
@@ -144,12 +162,15 @@ class DarcyHDG:
       (v.u/kappa) - (div v) p - grad(q).u  on Omega,
       (v.n) l + q(u.n) + tau s q (p - l) + m(u.n) + tau s m (p - l)  on dK,
     s = n.n_o (stabilization="owner_sign", as the reference test) or 1
-    ("textbook" LDG-H).  `problem` selects the built-in manufactured source,
+    ("textbook" LDG-H).  tau = 0 with a raviart_thomas flux is the RT-H form
+    of test/DarcyRTHTests.jl:69-72 (q div u = -grad(q).u + q(u.n) per cell).  `problem` selects the built-in manufactured source,
     Dirichlet data and exact solution."""
 
     STABS = {"textbook": _lib.HDG_STAB_TEXTBOOK, "owner_sign": _lib.HDG_STAB_OWNER_SIGN}
     PROBLEMS = {"ref_linear": _lib.HDG_PROBLEM_REF_LINEAR, "linear": _lib.HDG_PROBLEM_LINEAR,
                 "sin": _lib.HDG_PROBLEM_SIN}
+
+    pm = False
 
     def __init__(self, tau=1.0, stabilization="textbook", problem="linear", kappa=None):
         self.tau = float(tau)
@@ -159,10 +180,11 @@ class DarcyHDG:
 
 
 class ElasticityHDG:
-    """The linear elasticity HDG form of test/LinearElasticityHDGTests.jl:140-150
-    (without the P_m projection, bulk_to_skeleton_projection=false):
+    """The linear elasticity HDG form of test/LinearElasticityHDGTests.jl:140-150:
       v (.) A(sigma) + (div v).u - w.(div sigma) on Omega,
-      -(v.n).uhat + tau w.(u - uhat) + mu.(sigma.n) - tau mu.(u - uhat) on dK,
+      -(v.n).uhat + tau w.(P_m(u) - uhat) + mu.(sigma.n) - tau mu.(P_m(u) - uhat) on dK,
+    P_m the L2 projection of the displacement onto the trace space
+    (bulk_to_skeleton_projection=True, :134-137) or the identity (False),
     compliance A(s) = (1+nu)/E s - nu/E tr(s) I (:15-38) with a per-cell
     Poisson ratio nu; `problem` selects the manufactured displacement
     ("linear" :48-50 or "smooth" :52-57) giving f = div sigma_exact and the
@@ -171,8 +193,9 @@ class ElasticityHDG:
     PROBLEMS = {"linear": _lib.HDG_EPROBLEM_LINEAR, "smooth": _lib.HDG_EPROBLEM_SMOOTH}
     physics = _lib.HDG_PHYSICS_ELASTICITY
 
-    def __init__(self, tau=None, E=1.0, nu=None, problem="smooth"):
+    def __init__(self, tau=None, E=1.0, nu=None, problem="smooth", bulk_to_skeleton_projection=False):
         self.tau = None if tau is None else float(tau)
+        self.pm = bool(bulk_to_skeleton_projection)
         self.E = float(E)
         self.problem = self.PROBLEMS[problem]
         self.nu = None if nu is None else np.ascontiguousarray(nu, dtype=np.float64)
@@ -195,15 +218,24 @@ DarcyHDG.apply = _darcy_apply
 
 
 class _Problem:
-    """Owns an hdg_problem handle."""
+    """Owns an hdg_problem handle: the equal-order Q_k forms, or (spaces =
+    int32[7] {kindA, kA, kindB, kB, kindT, kT, pm}) the general-space forms
+    with `copies` copies."""
 
-    def __init__(self, ctx, model, k, physics=_lib.HDG_PHYSICS_DARCY):
+    def __init__(self, ctx, model, k, physics=_lib.HDG_PHYSICS_DARCY, spaces=None, copies=1):
         self.ctx = ctx
         h = ctypes.c_void_p()
         cells = np.array(model.partition, dtype=np.int32)
         dom = np.array(model.domain, dtype=np.float64)
-        ctx.check(ctx.lib.hdg_problem_create_cartesian_physics(ctx.handle, model.D, _lib.ptr(cells),
-                                                               _lib.ptr(dom), k, physics, ctypes.byref(h)))
+        if spaces is None:
+            ctx.check(ctx.lib.hdg_problem_create_cartesian_physics(ctx.handle, model.D, _lib.ptr(cells),
+                                                                   _lib.ptr(dom), k, physics, ctypes.byref(h)))
+        else:
+            sp = np.ascontiguousarray(spaces, dtype=np.int32)
+            ctx.check(ctx.lib.hdg_problem_create_cartesian_spaces(ctx.handle, model.D, _lib.ptr(cells),
+                                                                  _lib.ptr(dom), physics, _lib.ptr(sp), copies,
+                                                                  ctypes.byref(h)))
+        self.copies = copies
         self.h = h
         ctx.register(self)
         info = np.zeros(8, dtype=np.int64)
@@ -232,6 +264,31 @@ class _Problem:
             pass
 
 
+def _general_spaces(trial, bulk_fields, skeleton_fields, weakform):
+    """(spaces, copies) of a multi-field trial space [A_1..A_c, B_1..B_c,
+    T_1..T_c] with bulk_fields [1..2c] and skeleton_fields [2c+1..3c]
+    (src/HybridAffineFEOperators.jl:10-36 takes any such split); spaces is
+    None for one copy of equal-order Q_k fields without P_m, the forms with
+    the float-float fast path."""
+    nf = len(trial)
+    c = nf // 3
+    if nf % 3 or c < 1 or bulk_fields != list(range(1, 2 * c + 1)) or \
+            skeleton_fields != list(range(2 * c + 1, 3 * c + 1)):
+        raise ValueError("the HDG operators expect fields [A_1..A_c, B_1..B_c, T_1..T_c] (flux/stress, "
+                         "pressure/displacement, trace) with bulk_fields=[1..2c] and skeleton_fields=[2c+1..3c]")
+    per_copy = []
+    for cp in range(c):
+        fe = [trial[cp].reffe, trial[c + cp].reffe, trial[2 * c + cp].reffe]
+        per_copy.append(tuple(v for r in fe for v in (r.kind, r.order)))
+    if len(set(per_copy)) != 1:
+        raise ValueError("the copies of a multi-field HDG space must use the same spaces")
+    sp = per_copy[0]
+    q = _lib.HDG_SPACE_Q
+    if c == 1 and not weakform.pm and sp[0::2] == (q, q, q) and len(set(sp[1::2])) == 1:
+        return None, 1
+    return np.array(list(sp) + [1 if weakform.pm else 0], dtype=np.int32), c
+
+
 class HybridAffineFEOperator:
     """HybridAffineFEOperator(weakform, trial, test, bulk_fields, skeleton_fields)
     (src/HybridAffineFEOperators.jl:10-50): integrates, condenses every cell
@@ -239,20 +296,15 @@ class HybridAffineFEOperator:
 
     def __init__(self, weakform, trial, test, bulk_fields, skeleton_fields,
                  precision=_lib.HDG_PREC_FP64, context=None):
-        if list(bulk_fields) != [1, 2] or list(skeleton_fields) != [3]:
-            raise ValueError("the HDG operators expect bulk_fields=[1,2] (flux/stress, pressure/displacement) "
-                             "and skeleton_fields=[3] (trace)")
         self.weakform, self.trial, self.test = weakform, trial, test
         self.bulk_fields, self.skeleton_fields = list(bulk_fields), list(skeleton_fields)
         self.precision = precision
         model = trial[0].trian.model
-        orders = {s.reffe.order for s in trial.spaces}
-        if len(orders) != 1:
-            raise ValueError("flux, pressure and trace must share the order k (Q_k / Q_k / Q_k)")
-        self.k = orders.pop()
+        spaces, copies = _general_spaces(trial, self.bulk_fields, self.skeleton_fields, weakform)
+        self.k = trial[0].reffe.order
         self.model = model
         self.ctx = context or _lib.default_context()
-        self.pb = _Problem(self.ctx, model, self.k, weakform.physics)
+        self.pb = _Problem(self.ctx, model, self.k, weakform.physics, spaces, copies)
         c = self.ctx
         weakform.apply(c, self.pb, model)
         self.info = np.zeros(self.pb.ncells, dtype=np.int32)
@@ -380,29 +432,47 @@ def solve_(xh0, solver, op):
     return HybridFEFunction(op, it.value, float(hist[-1])), {"iterations": it.value, "residual_norms": hist}
 
 
-def elasticity_spaces(model, k):
-    """The spaces of the elasticity HDG test with matching orders: symmetric
-    stress Q_k, displacement Q_k, displacement trace Q_k with Dirichlet facets
-    on the whole boundary (test/LinearElasticityHDGTests.jl:79-110; the
-    reference uses P spaces and a k+1 displacement with the P_m projection)."""
-    Omega = Triangulation(model)
-    Gamma = Triangulation(model, model.D - 1)
-    V = TestFESpace(Omega, ReferenceFE(lagrangian, SymTensorValue, k), conformity="L2")
-    W = TestFESpace(Omega, ReferenceFE(lagrangian, VectorValue, k), conformity="L2")
-    M = TestFESpace(Gamma, ReferenceFE(lagrangian, VectorValue, k), conformity="L2", dirichlet_tags="boundary")
-    Y = MultiFieldFESpace([V, W, M])
-    X = MultiFieldFESpace([TrialFESpace(V), TrialFESpace(W), TrialFESpace(M, "u_exact")])
+def _copies(V, Q, M, dirichlet, copies):
+    Y = MultiFieldFESpace([V] * copies + [Q] * copies + [M] * copies)
+    X = MultiFieldFESpace([TrialFESpace(V)] * copies + [TrialFESpace(Q)] * copies +
+                          [TrialFESpace(M, dirichlet)] * copies)
     return X, Y
 
 
-def darcy_spaces(model, k):
-    """The spaces of the Darcy HDG test: Q_k flux, Q_k pressure, Q_k trace with
-    Dirichlet facets on the whole boundary (test/DarcyHDGTests.jl:32-52)."""
+def elasticity_spaces(model, k, space="Q", displacement_order=None, copies=1):
+    """The spaces of the elasticity HDG test: symmetric stress, displacement
+    and displacement trace with Dirichlet facets on the whole boundary
+    (test/LinearElasticityHDGTests.jl:79-110).  space="Q": all Q_k (the
+    equal-order forms); space="P": stress P_k, displacement P_{k+1}, trace P_k
+    as the reference's test; displacement_order overrides the displacement's."""
     Omega = Triangulation(model)
     Gamma = Triangulation(model, model.D - 1)
-    V = TestFESpace(Omega, ReferenceFE(lagrangian, VectorValue, k), conformity="L2")
-    Q = TestFESpace(Omega, ReferenceFE(lagrangian, Float64, k), conformity="L2")
-    M = TestFESpace(Gamma, ReferenceFE(lagrangian, Float64, k), conformity="L2", dirichlet_tags="boundary")
-    Y = MultiFieldFESpace([V, Q, M])
-    X = MultiFieldFESpace([TrialFESpace(V), TrialFESpace(Q), TrialFESpace(M, "exact")])
-    return X, Y
+    ku = displacement_order if displacement_order is not None else (k + 1 if space == "P" else k)
+    V = TestFESpace(Omega, ReferenceFE(lagrangian, SymTensorValue, k, space=space), conformity="L2")
+    W = TestFESpace(Omega, ReferenceFE(lagrangian, VectorValue, ku, space=space), conformity="L2")
+    M = TestFESpace(Gamma, ReferenceFE(lagrangian, VectorValue, k, space=space), conformity="L2",
+                    dirichlet_tags="boundary")
+    return _copies(V, W, M, "u_exact", copies)
+
+
+def darcy_spaces(model, k, space="Q", copies=1):
+    """The spaces of the Darcy tests with Dirichlet facets on the whole
+    boundary: space="Q": Q_k flux, pressure and trace (the equal-order forms);
+    "P": flux P_k, pressure P_{k-1}, trace P_k (test/DarcyHDGTests.jl:32-52);
+    "RT": flux RT_k, pressure Q_k, trace Q_k (test/DarcyRTHTests.jl:32-54).
+    copies > 1 repeats each field (test/MultiFieldLagrangeMultipliersTests.jl:
+    37-62)."""
+    Omega = Triangulation(model)
+    Gamma = Triangulation(model, model.D - 1)
+    if space == "RT":
+        rv = ReferenceFE(raviart_thomas, Float64, k)
+        rq = ReferenceFE(lagrangian, Float64, k)
+        rm = ReferenceFE(lagrangian, Float64, k)
+    else:
+        rv = ReferenceFE(lagrangian, VectorValue, k, space=space)
+        rq = ReferenceFE(lagrangian, Float64, k - 1 if space == "P" else k, space=space)
+        rm = ReferenceFE(lagrangian, Float64, k, space=space)
+    V = TestFESpace(Omega, rv, conformity="L2")
+    Q = TestFESpace(Omega, rq, conformity="L2")
+    M = TestFESpace(Gamma, rm, conformity="L2", dirichlet_tags="boundary")
+    return _copies(V, Q, M, "exact", copies)

@@ -77,10 +77,11 @@ class Server:
         self.check(self.lib.hdg_server_drain(self.h, float(timeout_ms)))
 
     def stats(self):
-        st = np.zeros(13)
+        st = np.zeros(14)
         self.check(self.lib.hdg_server_stats(self.h, _lib.ptr(st)))
         keys = ["submitted", "completed", "failed", "running", "queued", "bytes_in_use", "budget",
-                "peak_bytes", "mesh_hits", "mesh_misses", "evictions", "max_concurrent", "busy_ms"]
+                "peak_bytes", "mesh_hits", "mesh_misses", "evictions", "max_concurrent", "busy_ms",
+                "retries_after_nomem"]
         return dict(zip(keys, st.tolist()))
 
     def close(self):

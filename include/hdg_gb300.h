@@ -194,6 +194,38 @@ int hdg_problem_create(hdg_context *ctx, int D, int k, int ncells, int nfacets,
 int hdg_problem_create_cartesian_physics(hdg_context *ctx, int D, const int *cells,
                                          const double *domain, int k, int physics,
                                          hdg_problem **out);
+/* The same Cartesian mesh with a polynomial space of its own for each field,
+ * as the reference's tests choose them: ReferenceFE(lagrangian, T, order;
+ * space=:P) (test/DarcyHDGTests.jl:34-36: flux P_k, pressure P_{k-1},
+ * multiplier P_k; test/LinearElasticityHDGTests.jl:88-93: stress P_k,
+ * displacement P_{k+1}, displacement trace P_k) and raviart_thomas
+ * (test/DarcyRTHTests.jl:28-30: flux RT_k, pressure Q_k, multiplier Q_k,
+ * no stabilisation: hdg_set_darcy with tau = 0).  spaces[7] = {kindA, kA,
+ * kindB, kB, kindT, kT, pm}: A the first bulk field (Darcy flux /
+ * elasticity stress), B the second (pressure / displacement), T the trace;
+ * kind HDG_SPACE_Q (tensor Lagrange, order 0..4), HDG_SPACE_P (total degree,
+ * order 0..4; Lagrange at the simplex lattice points i/k, the constant for
+ * order 0) or, for the Darcy flux, HDG_SPACE_RT (order 0..3); pm = 1 applies
+ * the bulk-to-skeleton projection P_m to the displacement in the tau terms
+ * (src/GridapAPIExtensions.jl:453-500, test/LinearElasticityHDGTests.jl:
+ * 134-150).  copies > 1 builds that many decoupled copies of the form, each
+ * with its own fields and its own skeleton field: the skeleton system of
+ * several fields of test/MultiFieldLagrangeMultipliersTests.jl (bulk fields
+ * [A_1 .. A_c, B_1 .. B_c], skeleton fields [T_1 .. T_c]); the skeleton
+ * values, free DOF values and hdg_get_skeleton_system use that multi-field
+ * numbering (each copy's skeleton field numbered on its own, one after the
+ * other), hdg_l2_errors sums the copies' squared errors.  The cell blocks are
+ * integrated in FP64 and condensed with HDG_PREC_FP64 or
+ * HDG_PREC_FP32_REFINED; the other calls (hdg_set_darcy /
+ * hdg_set_elasticity, hdg_assemble, hdg_solve_skeleton, hdg_recover,
+ * hdg_get_*, hdg_l2_errors, hdg_solve) work as for the equal-order problems.
+ * Free DOF values keep Gridap's layout [each bulk field of all cells |
+ * skeleton]. */
+#define HDG_SPACE_Q 0
+#define HDG_SPACE_P 1
+#define HDG_SPACE_RT 2
+int hdg_problem_create_cartesian_spaces(hdg_context *ctx, int D, const int *cells, const double *domain,
+                                        int physics, const int *spaces, int copies, hdg_problem **out);
 int hdg_problem_destroy(hdg_problem *pb);
 
 /* info[0..7] = ncells, nfacets, ni, nf, nfree, ndirichlet, nnz, nfacet_dofs */
@@ -333,6 +365,19 @@ int hdg_time_kernel(hdg_problem *pb, int which, int reps, double *ms_per_launch)
  * pipes of the float-float paths) and FP64 (the plain FP64 path). */
 int hdg_measure_pipe_peaks(hdg_context *ctx, double *fp32_tflops, double *fp64_tflops);
 
+/* Diagnostic (no reference counterpart): runs the two bounded wait
+ * primitives the kernels use -- the mbarrier wait of the bulk-copy rings and
+ * the generation wait of the cooperative grid barrier -- against a barrier
+ * phase and a word that nothing completes or writes, each for `polls` polls
+ * (1 .. 2^20), with nothing in flight.  expired[0..1] = 1 when the mbarrier /
+ * generation wait gave up (the expected result); ns_per_poll[0..1] = the
+ * time of one poll at the device's rated clock.  The kernels' own limits are
+ * 2^18 polls (mbarrier) and 2^22 polls (grid barrier), about one second each
+ * on a GB300; on expiry they set an
+ * error flag, wait (bounded) for their own copies in flight and return, and
+ * the call fails with HDG_ERR_CUDA while the context stays usable. */
+int hdg_check_bounded_waits(hdg_context *ctx, unsigned polls, int *expired, double *ns_per_poll);
+
 /* Device bytes currently reserved by the problem (all its buffers). */
 int hdg_problem_device_bytes(const hdg_problem *pb, double *bytes);
 
@@ -431,7 +476,11 @@ int hdg_server_poll(hdg_server *s, hdg_response *out, int max, double timeout_ms
 int hdg_server_drain(hdg_server *s, double timeout_ms);
 /* [submitted, completed, failed, running, queued, bytes in use, budget,
  *  peak bytes in use, mesh hits, mesh misses, evictions, max concurrent,
- *  summed run ms of finished requests] (13 values) */
+ *  summed run ms of finished requests, requests run a second time after a
+ *  device allocation failed] (14 values).  A request whose allocation fails
+ *  below the admission budget (memory the pool keeps, or another user of the
+ *  GPU) is run once more after every idle mesh is evicted and the pool's
+ *  unused memory is returned to the device. */
 int hdg_server_stats(hdg_server *s, double *stats);
 const char *hdg_server_last_error(hdg_server *s);
 

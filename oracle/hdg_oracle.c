@@ -1923,10 +1923,11 @@ int orc_solve_elasticity(int D, int k, const int *n, const double *domain, doubl
 /* test/P_m.jl:4-22, used at test/LinearElasticityHDGTests.jl:134-150).      */
 /* ------------------------------------------------------------------------ */
 
-enum { GS_PHYS_DARCY = 0, GS_PHYS_ELAST = 1, GS_Q = 0, GS_P = 1 };
+enum { GS_PHYS_DARCY = 0, GS_PHYS_ELAST = 1, GS_Q = 0, GS_P = 1, GS_RT = 2 };
 
 typedef struct {
   int d, kind, k, nb;
+  int aniso, ko[3]; /* tensor Lagrange with order ko[e] along dimension e */
   int *lat;      /* Q: nb x d lattice indices */
   int *mono;     /* P: nb x d exponents */
   double *coef;  /* P: nb x nb, phi_a = sum_m coef[a nb + m] x^mono_m */
@@ -1977,14 +1978,46 @@ static int dense_inverse(int n, double *A) {
   return 0;
 }
 
+/* tensor Lagrange of order orders[e] along dimension e (nodes i/m, the
+ * midpoint for order 0), first dimension fastest */
+static int obasis_init_aniso(obasis *b, int d, const int *orders) {
+  memset(b, 0, sizeof(*b));
+  b->d = d;
+  b->kind = GS_Q;
+  b->aniso = 1;
+  if (d < 1 || d > 3) return -1;
+  b->nb = 1;
+  for (int e = 0; e < d; ++e) {
+    if (orders[e] < 0 || orders[e] > 4) return -1;
+    b->ko[e] = orders[e];
+    if (orders[e] > b->k) b->k = orders[e];
+    b->nb *= orders[e] + 1;
+  }
+  b->lat = malloc(sizeof(int) * b->nb * d);
+  b->nodes = malloc(sizeof(double) * b->nb * d);
+  for (int a = 0; a < b->nb; ++a) {
+    int r = a;
+    for (int e = 0; e < d; ++e) {
+      const int i = r % (b->ko[e] + 1);
+      r /= b->ko[e] + 1;
+      b->lat[a * d + e] = i;
+      b->nodes[a * d + e] = b->ko[e] == 0 ? 0.5 : (double)i / b->ko[e];
+    }
+  }
+  return 0;
+}
+
 static int obasis_init(obasis *b, int d, int kind, int k) {
   memset(b, 0, sizeof(*b));
   b->d = d;
   b->kind = kind;
   b->k = k;
   if (d < 1 || d > 3 || k < 0 || k > 4) return -1;
+  if (kind == GS_Q && k == 0) {
+    const int zero[3] = {0, 0, 0};
+    return obasis_init_aniso(b, d, zero);
+  }
   if (kind == GS_Q) {
-    if (k < 1) return -1;
     b->nb = ipow(k + 1, d);
     b->lat = malloc(sizeof(int) * b->nb * d);
     orc_lagrange_lattice(d, k, b->lat);
@@ -2031,6 +2064,30 @@ static int obasis_init(obasis *b, int d, int kind, int k) {
 
 static void obasis_eval(const obasis *b, const double *xi, double *val, double *grad) {
   const int d = b->d, nb = b->nb;
+  if (b->aniso) {
+    for (int a = 0; a < nb; ++a) {
+      double l[3], dl[3];
+      for (int e = 0; e < d; ++e) {
+        if (b->ko[e] == 0) {
+          l[e] = 1.0;
+          dl[e] = 0.0;
+        } else {
+          lag1d(b->ko[e], b->lat[a * d + e], xi[e], &l[e], &dl[e]);
+        }
+      }
+      double v = 1.0;
+      for (int e = 0; e < d; ++e) v *= l[e];
+      val[a] = v;
+      if (grad)
+        for (int e = 0; e < d; ++e) {
+          double g = dl[e];
+          for (int j = 0; j < d; ++j)
+            if (j != e) g *= l[j];
+          grad[a * d + e] = g;
+        }
+    }
+    return;
+  }
   if (b->kind == GS_Q) {
     for (int a = 0; a < nb; ++a) {
       double l[3], dl[3];
@@ -2084,14 +2141,14 @@ int orc_gs_basis_eval(int d, int kind, int k, int npts, const double *xi, double
 
 typedef struct {
   int D, phys, pm;
-  obasis A, B, T;
+  obasis A[6], B, T; /* A: one basis per component of the first field (RT_k: different ones) */
   int ncA, ncB, ncT, nA, nB, nT, ni, nf, nfd, n;
   int n1, nqv, nqf;
   double *qv_xi, *qv_w, *qf_w, *qf_s; /* volume points, facet points (nqf x (D-1) parameters) */
 } gstab;
 
 static void gstab_free(gstab *g) {
-  obasis_free(&g->A);
+  for (int c = 0; c < 6; ++c) obasis_free(&g->A[c]);
   obasis_free(&g->B);
   obasis_free(&g->T);
   free(g->qv_xi);
@@ -2106,24 +2163,34 @@ static int gstab_init(gstab *g, int D, int phys, const int *sp) {
   g->D = D;
   g->phys = phys;
   g->pm = sp[6];
-  if (obasis_init(&g->A, D, sp[0], sp[1]) || obasis_init(&g->B, D, sp[2], sp[3]) ||
-      obasis_init(&g->T, D - 1, sp[4], sp[5])) {
+  const int ns = D * (D + 1) / 2;
+  g->ncA = phys == GS_PHYS_DARCY ? D : ns;
+  int bad = 0;
+  for (int c = 0; c < g->ncA; ++c) {
+    if (sp[0] == GS_RT) { /* RT_k: component c of order k+1 along c and k across */
+      int ord[3];
+      for (int e = 0; e < D; ++e) ord[e] = sp[1] + (e == c ? 1 : 0);
+      bad |= phys != GS_PHYS_DARCY || obasis_init_aniso(&g->A[c], D, ord);
+    } else {
+      bad |= obasis_init(&g->A[c], D, sp[0], sp[1]);
+    }
+  }
+  if (bad || obasis_init(&g->B, D, sp[2], sp[3]) || obasis_init(&g->T, D - 1, sp[4], sp[5])) {
     gstab_free(g);
     return -1;
   }
-  const int ns = D * (D + 1) / 2;
-  g->ncA = phys == GS_PHYS_DARCY ? D : ns;
   g->ncB = phys == GS_PHYS_DARCY ? 1 : D;
   g->ncT = phys == GS_PHYS_DARCY ? 1 : D;
-  g->nA = g->A.nb;
+  g->nA = g->A[0].nb;
   g->nB = g->B.nb;
   g->nT = g->T.nb;
   g->ni = g->ncA * g->nA + g->ncB * g->nB;
   g->nfd = g->ncT * g->nT;
   g->nf = 2 * D * g->nfd;
   g->n = g->ni + g->nf;
-  int kmax = sp[1] > sp[3] ? sp[1] : sp[3];
-  if (sp[5] > kmax) kmax = sp[5];
+  int kmax = sp[3] > sp[5] ? sp[3] : sp[5];
+  for (int c = 0; c < g->ncA; ++c)
+    if (g->A[c].k > kmax) kmax = g->A[c].k;
   g->n1 = kmax + 2;
   g->nqv = ipow(g->n1, D);
   g->nqf = ipow(g->n1, D - 1);
@@ -2225,7 +2292,10 @@ static void gs_integrate_cell(const gstab *g, int c, const int *n, const double 
   for (int d = 0; d < D; ++d) detJ *= h[d];
   memset(A, 0, sizeof(double) * (size_t)N * N);
   memset(b, 0, sizeof(double) * N);
-  double *pA = malloc(sizeof(double) * nA), *dA = malloc(sizeof(double) * nA * D), *pB = malloc(sizeof(double) * nB),
+  /* first-field basis values / gradients per component (RT_k: one basis per
+   * component); pA, dA: component 0, which every elasticity stress component uses */
+  double *pAc = malloc(sizeof(double) * 6 * nA), *dAc = malloc(sizeof(double) * 6 * nA * D);
+  double *pA = pAc, *dA = dAc, *pB = malloc(sizeof(double) * nB),
          *dB = malloc(sizeof(double) * nB * D), *mu = malloc(sizeof(double) * nT), *pm = malloc(sizeof(double) * nB),
          *P = malloc(sizeof(double) * nT * nB);
 #define AIJ(i, j) A[(size_t)(i) + (size_t)N * (j)]
@@ -2244,7 +2314,7 @@ static void gs_integrate_cell(const gstab *g, int c, const int *n, const double 
       }
   for (int q = 0; q < g->nqv; ++q) {
     const double *xi = &g->qv_xi[q * D];
-    obasis_eval(&g->A, xi, pA, dA);
+    for (int c2 = 0; c2 < g->ncA; ++c2) obasis_eval(&g->A[c2], xi, pAc + c2 * nA, dAc + c2 * nA * D);
     obasis_eval(&g->B, xi, pB, dB);
     const double wq = g->qv_w[q] * detJ;
     double x[MAXD];
@@ -2254,13 +2324,13 @@ static void gs_integrate_cell(const gstab *g, int c, const int *n, const double 
       exact(problem, D, x, coef, &pe, qe, fu, &gg);
       for (int a = 0; a < nA; ++a) {
         for (int a2 = 0; a2 < nA; ++a2)
-          for (int d = 0; d < D; ++d) AIJ(d * nA + a, d * nA + a2) += wq * pA[a] * pA[a2] / coef;
+          for (int d = 0; d < D; ++d) AIJ(d * nA + a, d * nA + a2) += wq * pAc[d * nA + a] * pAc[d * nA + a2] / coef;
         for (int bb = 0; bb < nB; ++bb)
           for (int d = 0; d < D; ++d) {
-            AIJ(d * nA + a, oB + bb) -= wq * (dA[a * D + d] / h[d]) * pB[bb]; /* -(div v) p */
-            AIJ(oB + bb, d * nA + a) -= wq * (dB[bb * D + d] / h[d]) * pA[a]; /* -grad(q).u */
+            AIJ(d * nA + a, oB + bb) -= wq * (dAc[(d * nA + a) * D + d] / h[d]) * pB[bb]; /* -(div v) p */
+            AIJ(oB + bb, d * nA + a) -= wq * (dB[bb * D + d] / h[d]) * pAc[d * nA + a];   /* -grad(q).u */
           }
-        for (int d = 0; d < D; ++d) b[d * nA + a] += wq * pA[a] * fu[d];
+        for (int d = 0; d < D; ++d) b[d * nA + a] += wq * pAc[d * nA + a] * fu[d];
       }
       for (int bb = 0; bb < nB; ++bb) b[oB + bb] += wq * pB[bb] * gg;
     } else {
@@ -2299,7 +2369,7 @@ static void gs_integrate_cell(const gstab *g, int c, const int *n, const double 
     for (int q = 0; q < g->nqf; ++q) {
       double xi[3];
       facet_point(D, lf, &g->qf_s[q * (D - 1)], xi);
-      obasis_eval(&g->A, xi, pA, NULL);
+      for (int c2 = 0; c2 < g->ncA; ++c2) obasis_eval(&g->A[c2], xi, pAc + c2 * nA, NULL);
       obasis_eval(&g->B, xi, pB, NULL);
       obasis_eval(&g->T, &g->qf_s[q * (D - 1)], mu, NULL);
       const double wq = g->qf_w[q] * detF;
@@ -2307,7 +2377,7 @@ static void gs_integrate_cell(const gstab *g, int c, const int *n, const double 
         for (int a = 0; a < nA; ++a)
           for (int m = 0; m < nT; ++m)
             for (int d = 0; d < D; ++d) {
-              const double v = wq * pA[a] * nrm[d] * mu[m];
+              const double v = wq * pAc[d * nA + a] * nrm[d] * mu[m];
               AIJ(d * nA + a, off + m) += v; /* (v.n) l */
               AIJ(off + m, d * nA + a) += v; /* m (u.n) */
             }
@@ -2317,7 +2387,7 @@ static void gs_integrate_cell(const gstab *g, int c, const int *n, const double 
             AIJ(off + m, oB + bb) += wq * tau * s * mu[m] * pB[bb]; /* tau m p (n.no) */
           }
           for (int a = 0; a < nA; ++a)
-            for (int d = 0; d < D; ++d) AIJ(oB + bb, d * nA + a) += wq * pB[bb] * pA[a] * nrm[d]; /* q (u.n) */
+            for (int d = 0; d < D; ++d) AIJ(oB + bb, d * nA + a) += wq * pB[bb] * pAc[d * nA + a] * nrm[d]; /* q (u.n) */
           for (int b2 = 0; b2 < nB; ++b2) AIJ(oB + bb, oB + b2) += wq * tau * s * pB[bb] * pB[b2];
         }
         for (int m = 0; m < nT; ++m)
@@ -2357,7 +2427,7 @@ static void gs_integrate_cell(const gstab *g, int c, const int *n, const double 
     }
   }
 #undef AIJ
-  free(pA); free(dA); free(pB); free(dB); free(mu); free(pm); free(P);
+  free(pAc); free(dAc); free(pB); free(dB); free(mu); free(pm); free(P);
 }
 
 int orc_gs_integrate(int D, int phys, const int *spaces, const int *n, const double *domain, double tau, int stab,
@@ -2440,10 +2510,11 @@ int orc_gs_l2_errors(int D, int phys, const int *spaces, const int *n, const dou
     for (int d = 0; d < D; ++d) detJ *= h[d];
     const double *u = uint + (size_t)c * g.ni;
     const double cf = coef ? coef[c] : (phys == GS_PHYS_DARCY ? 1.0 : 0.3);
-    double pA[216], pB[216];
+    double pAc[6 * 216], pB[216];
+    const double *pA = pAc;
     for (int q = 0; q < g.nqv; ++q) {
       const double *xi = &g.qv_xi[q * D];
-      obasis_eval(&g.A, xi, pA, NULL);
+      for (int c2 = 0; c2 < g.ncA; ++c2) obasis_eval(&g.A[c2], xi, pAc + c2 * nA, NULL);
       obasis_eval(&g.B, xi, pB, NULL);
       double x[MAXD];
       for (int d = 0; d < D; ++d) x[d] = x0[d] + h[d] * xi[d];
@@ -2454,7 +2525,7 @@ int orc_gs_l2_errors(int D, int phys, const int *spaces, const int *n, const dou
         double s1 = 0.0, ph = 0.0;
         for (int d = 0; d < D; ++d) {
           double qh = 0.0;
-          for (int a = 0; a < nA; ++a) qh += u[d * nA + a] * pA[a];
+          for (int a = 0; a < nA; ++a) qh += u[d * nA + a] * pAc[d * nA + a];
           s1 += (qe[d] - qh) * (qe[d] - qh);
         }
         for (int bb = 0; bb < nB; ++bb) ph += u[oB + bb] * pB[bb];

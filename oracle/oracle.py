@@ -328,8 +328,10 @@ EPROBLEM_LINEAR = 0
 EPROBLEM_SMOOTH = 1
 
 # General spaces: a polynomial space per field (Q_k tensor product or P_k
-# total degree), as ReferenceFE(lagrangian, T, order; space=...) chooses them.
-SPACE_Q, SPACE_P = 0, 1
+# total degree), as ReferenceFE(lagrangian, T, order; space=...) chooses them,
+# or RT_k (raviart_thomas on a box: flux component c of order k+1 along x_c and
+# k across) for the Darcy flux; Q_0 is the constant.
+SPACE_Q, SPACE_P, SPACE_RT = 0, 1, 2
 PHYS_DARCY, PHYS_ELASTICITY = 0, 1
 
 
@@ -395,6 +397,72 @@ class GsMesh(Mesh):
                                ctypes.c_double(E), P(np.ascontiguousarray(uint)), ctypes.byref(e1),
                                ctypes.byref(e2))
         return e1.value, e2.value
+
+
+class GsCopiesMesh(GsMesh):
+    """`copies` independent copies of one general-space form on one mesh, as a
+    multi-field space [A_1..A_c, B_1..B_c, T_1..T_c] sums the same block form
+    once per copy (test/MultiFieldLagrangeMultipliersTests.jl:40-88).  The
+    cell matrix holds the copies' first fields, then their second fields, then
+    per local facet the copies' trace DOFs one copy after the other
+    (facet-major); `multi_field_order` maps facet-major skeleton values to
+    Gridap's numbering, all DOFs of the first trace field before the second."""
+
+    def __init__(self, D, n, phys, spaces, copies, domain=None):
+        self.one = GsMesh(D, n, phys, spaces, domain)
+        Mesh.__init__(self, D, n, 1, domain)
+        o = self.one
+        self.phys, self.spaces, self.copies = phys, o.spaces, copies
+        self.nA, self.nB, self.nT, self.nqv = o.nA, o.nB, o.nT, o.nqv
+        self.ni, self.nfd = copies * o.ni, copies * o.nfd
+        self.nf = 2 * D * self.nfd
+        self.facet_dofs = np.zeros((self.nfacets, self.nfd), dtype=np.int32)
+        nfree, ndir = ctypes.c_int(), ctypes.c_int()
+        lib().orc_facet_dofs_n(self.nfd, self.nfacets, P(self.facet_is_boundary), P(self.facet_dofs),
+                               ctypes.byref(nfree), ctypes.byref(ndir))
+        self.nfree, self.ndir = nfree.value, ndir.value
+        ncA = D if phys == PHYS_DARCY else D * (D + 1) // 2
+        na = ncA * o.nA  # first-field DOFs of one copy
+        self.maps = []
+        for cp in range(copies):
+            i1 = np.arange(o.ni + o.nf)
+            lf, a = np.divmod(i1 - o.ni, o.nfd)
+            m = np.where(i1 < na, cp * na + i1,
+                         np.where(i1 < o.ni, copies * na + cp * (o.ni - na) + i1 - na,
+                                  self.ni + lf * self.nfd + cp * o.nfd + a))
+            self.maps.append(m)
+
+    def integrate(self, **kw):
+        A1, b1 = self.one.integrate(**kw)
+        n = self.ni + self.nf
+        A = np.zeros((self.ncells, n, n))
+        b = np.zeros((self.ncells, n))
+        for m in self.maps:
+            A[:, m[:, None], m[None, :]] = A1
+            b[:, m] = b1
+        return A, b
+
+    def dirichlet_values(self, problem):
+        dv1 = self.one.dirichlet_values(problem)
+        dv = np.zeros(self.ndir)
+        nfd1 = self.one.nfd
+        for cp in range(self.copies):
+            fd = self.facet_dofs[:, cp * nfd1:(cp + 1) * nfd1]
+            on = fd < 0
+            dv[-1 - fd[on]] = dv1[-1 - self.one.facet_dofs[on]]
+        return dv
+
+    def multi_field_order(self, lam):
+        nfd1 = self.one.nfd
+        per = self.nfree // self.copies
+        return np.asarray(lam).reshape(-1, self.copies, nfd1).transpose(1, 0, 2).reshape(self.copies * per)
+
+    def l2_errors(self, problem, uint, coef=None, E=1.0):
+        s1 = s2 = 0.0
+        for m in self.maps:
+            e1, e2 = self.one.l2_errors(problem, uint[:, m[:self.one.ni]], coef=coef, E=E)
+            s1, s2 = s1 + e1 * e1, s2 + e2 * e2
+        return np.sqrt(s1), np.sqrt(s2)
 
 
 class ElasticityMesh(Mesh):
@@ -501,12 +569,12 @@ GsMesh.cell_skeleton_values = ElasticityMesh.cell_skeleton_values
 
 
 def solve_gs(D, n, phys, spaces, tau=1.0, stab=STAB_TEXTBOOK, problem=PROBLEM_LINEAR, coef=None, E=1.0, solver=0,
-             sign=None, rtol=1e-13, maxit=100000, domain=None):
+             sign=None, rtol=1e-13, maxit=100000, domain=None, copies=1):
     """The general-space path on the CPU: integrate, StaticCondensationMap,
     assemble, skeleton solve (0: dense LU, 1: block-Jacobi PCG on sign*S; sign
     defaults to -1 for Darcy, +1 for elasticity), BackwardStaticCondensationMap,
-    L2 errors of the two bulk fields."""
-    m = GsMesh(D, n, phys, spaces, domain)
+    L2 errors of the two bulk fields (root sum of squares over copies)."""
+    m = GsMesh(D, n, phys, spaces, domain) if copies == 1 else GsCopiesMesh(D, n, phys, spaces, copies, domain)
     A, b = m.integrate(tau=tau, stab=stab, problem=problem, coef=coef, E=E)
     S, g, info = static_condensation(A, b, m.ni)
     assert (info == 0).all()

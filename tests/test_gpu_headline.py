@@ -112,7 +112,7 @@ def test_batch_with_largest_problem_matches_oracle():
     """The batching workload's extremes in one batch: 2D n = 128 with k = 3
     (48 interior + 16 facet DOFs per cell), n = 16 with k = 1 and n = 64
     with k = 2, kappa = exp(N(0, 1.5^2)) per cell, through the fused
-    float-float launches (solved to 1e-11) and FP64 (to 1e-12); each
+    float-float launches (solved to 3e-11) and FP64 (to 1e-12); each
     problem's solution against the oracle's."""
     rng = np.random.default_rng(3)
     specs = [{"D": 2, "n": n, "k": k, "kappa": np.exp(1.5 * rng.normal(size=n * n))}
@@ -124,12 +124,12 @@ def test_batch_with_largest_problem_matches_oracle():
         assert r["rc"] == 0
         refs.append(r)
     # The n = 128, k = 3 system is ill-conditioned: its true FP64 residual
-    # cannot be computed below about 1e-11 of the right-hand side (the fast
-    # path tests the true residual, so it is solved to 1e-11), and two FP64
+    # cannot be computed much below 1e-11 of the right-hand side (the fast
+    # path tests the true residual, so it is solved to 3e-11), and two FP64
     # solutions of it, ours and the oracle's, agree to about 1.5e-10 whatever
     # the tolerance (rounding times the condition number), so the FP64 path is
     # held to 1e-9 here.
-    for precision, tol, rtol in ((_lib.HDG_PREC_FF_BLOCK, RTOL_FAST, 1e-11), (_lib.HDG_PREC_FP64, 1e-9, 1e-12)):
+    for precision, tol, rtol in ((_lib.HDG_PREC_FF_BLOCK, RTOL_FAST, 3e-11), (_lib.HDG_PREC_FP64, 1e-9, 1e-12)):
         with Batch(specs) as b:
             assert (b.assemble(precision) == 0).all()
             its, rel = b.solve(rtol=rtol)

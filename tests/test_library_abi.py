@@ -78,6 +78,8 @@ def _c_kind(decl):
     words = [w for w in decl.replace("const ", " ").split() if w not in ("unsigned",)]
     if words[:2] == ["long", "long"]:
         return "longlong"
+    if decl.split()[0] == "unsigned" and words in ([], ["int"]):
+        return "uint"
     return words[0]
 
 
@@ -94,7 +96,7 @@ def c_prototypes():
     return protos
 
 
-_JULIA_KIND = {"Cint": "int", "Int32": "int", "Cdouble": "double", "Float64": "double", "Clonglong": "longlong",
+_JULIA_KIND = {"Cint": "int", "Int32": "int", "Cuint": "uint", "UInt32": "uint", "Cdouble": "double", "Float64": "double", "Clonglong": "longlong",
                "Int64": "longlong", "Cstring": "ptr"}
 
 
@@ -147,6 +149,7 @@ def test_c_prototype_parser_reads_every_declaration():
     assert protos["hdg_launch_count"] == ("longlong", ["ptr"])
     assert protos["hdg_last_error"] == ("ptr", ["ptr"])
     assert protos["hdg_version"] == ("int", [])
+    assert protos["hdg_check_bounded_waits"] == ("int", ["ptr", "uint", "ptr", "ptr"])
 
 
 def test_python_binding_matches_c_prototypes():
@@ -156,6 +159,8 @@ def test_python_binding_matches_c_prototypes():
             return "void"
         if t in (ctypes.c_int,):
             return "int"
+        if t in (ctypes.c_uint,):
+            return "uint"
         if t in (ctypes.c_double,):
             return "double"
         if t in (ctypes.c_longlong,):

@@ -8,6 +8,13 @@ with ReferenceFE(lagrangian, T, order; space=:P)).
     p = -3.14): ||u - u_h|| < 1e-12;
   - Q spaces everywhere reproduce the oracle's equal-order Q_k forms;
   - the P_k bases are Lagrange bases on their nodes;
+  - the reference's RT-H KAT (test/DarcyRTHTests.jl:26-91: flux RT_0,
+    pressure Q_0, multiplier Q_0, no stabilisation, 2x2 quads, the same
+    u and p): ||u - u_h|| < 1e-12, and RT_k-H converging at k+1 in both
+    fields;
+  - the reference's multi-field KAT (test/MultiFieldLagrangeMultipliersTests.jl:
+    24-88: two RT_0-H copies with skeleton fields [5, 6]): both copies exact,
+    and copies of a form solve as the form does, copy by copy;
   - P_m (test/P_m.jl:4-22) leaves the displacement's trace residual
     mu-orthogonal to < 1e-14 (test/LinearElasticityHDGTests.jl:133-137), and
     with it the reference's elasticity configuration (stress P_k,
@@ -19,7 +26,7 @@ import pytest
 
 from oracle import oracle
 
-P, Q = oracle.SPACE_P, oracle.SPACE_Q
+P, Q, RT = oracle.SPACE_P, oracle.SPACE_Q, oracle.SPACE_RT
 
 
 @pytest.mark.parametrize("D,n", [(2, (2, 2)), (3, (2, 2, 2))])
@@ -114,3 +121,34 @@ def test_elasticity_with_pm_converges_at_k_plus_one_and_k_plus_two():
     rs = np.log2(errs[0][0] / errs[1][0])
     ru = np.log2(errs[0][1] / errs[1][1])
     assert rs > 1.9 and ru > 2.9, (rs, ru)
+
+
+@pytest.mark.parametrize("D,n,copies", [(2, (2, 2), 1), (3, (2, 2, 2), 1), (2, (2, 2), 2)])
+def test_reference_rth_and_multifield_kats(D, n, copies):
+    sp = oracle.gs_spaces(RT, 0, Q, 0, Q, 0)
+    r = oracle.solve_gs(D, n, oracle.PHYS_DARCY, sp, tau=0.0, problem=oracle.PROBLEM_REF_LINEAR, solver=0,
+                        copies=copies)
+    m = r["mesh"]
+    if D == 2:  # RT_0: 4 flux + 1 pressure DOFs per copy, 1 DOF per facet per copy
+        assert (m.ni, m.nfd) == (5 * copies, copies)
+    assert r["err1"] < 1e-12 and r["err2"] < 1e-12
+
+
+@pytest.mark.parametrize("k", [0, 1, 2])
+def test_rth_converges_at_k_plus_one(k):
+    sp = oracle.gs_spaces(RT, k, Q, k, Q, k)
+    errs = [oracle.solve_gs(2, (n, n), oracle.PHYS_DARCY, sp, tau=0.0, problem=oracle.PROBLEM_SIN, solver=0)
+            for n in (4, 8)]
+    for key in ("err1", "err2"):
+        assert np.log2(errs[0][key] / errs[1][key]) > k + 0.9
+
+
+def test_copies_solve_copy_by_copy():
+    sp = oracle.gs_spaces(P, 1, P, 0, P, 1)
+    kw = dict(tau=1.0, problem=oracle.PROBLEM_SIN, solver=0)
+    r1 = oracle.solve_gs(2, (3, 2), oracle.PHYS_DARCY, sp, **kw)
+    r2 = oracle.solve_gs(2, (3, 2), oracle.PHYS_DARCY, sp, copies=2, **kw)
+    lam = r2["mesh"].multi_field_order(r2["lam"]).reshape(2, -1)
+    for cp in range(2):
+        assert np.abs(lam[cp] - r1["lam"]).max() < 1e-13
+        assert np.abs(r2["uint"][:, r2["mesh"].maps[cp][:r1["mesh"].ni]] - r1["uint"]).max() < 1e-13
