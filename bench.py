@@ -367,7 +367,9 @@ def oracle_accuracy(setup, got, ncells, ni):
 # launch of condense_ffblock_kernel<3,27,9> at 24^3, divided by its cells (the
 # kernel does the same work in every cell).  Refreshed with the capture in
 # profiles/condense_ffblock_kernel_24cube_k2.md.
-FFBLOCK_FP32_FLOP_PER_CELL = None
+# FP32 work of condense_ffblock_kernel<3,27,9> per cell, from an ncu capture at
+# 24^3: FADD + FMUL + 2 FFMA thread-instructions per cell (FFMA counts 2 flops)
+FFBLOCK_FP32_FLOP_PER_CELL = 3.14e6
 
 
 def condense_roofline(phase, ncells, peaks):
@@ -381,7 +383,8 @@ def condense_roofline(phase, ncells, peaks):
     alg = 2.0 / 3.0 * ni ** 3 + 2 * ni * ni * nf + 2 * nf * nf * ni + 2 * ni * ni + 2 * ni * nf
     ms = float(phase[1])
     ach = alg * ncells / (ms * 1e-3) / 1e12
-    out = {"bound": "fp32 pipe (float-float)", "kernel": "condense_ffblock_kernel<3,27,9>", "ms_per_launch": ms,
+    out = {"bound": "fp32 pipe (float-float); issue- and latency-limited (ncu: 55 % issue active)",
+           "kernel": "condense_ffblock_kernel<3,27,9>", "ms_per_launch": ms,
            "alg_fp64_flop_per_cell": alg, "achieved_fp64_equiv_tflops": ach,
            "fp64_peak_tflops": peaks["fp64_tflops"], "frac_of_fp64_peak": ach / peaks["fp64_tflops"]}
     if FFBLOCK_FP32_FLOP_PER_CELL:
@@ -547,10 +550,10 @@ def run_gpu(args, rank=0, nranks=1, device=0):
         rec = (nl * (nl + 1) // 2 * nfd * nfd + 3) // 4 * 4
         spmv_bytes = ncells * rec * 4 + ncells * nl * 4 + 3 * nfree * 4 + ncells * nf * 4
         spmv_kernel = "cell_spmv32_kernel<6,9>"
-        # DRAM read + write of one launch from an ncu capture at 24^3 (99.83 MB over
-        # 13,824 cells), scaled by cells: the kernel streams each cell record once,
-        # so traffic grows with the cells
-        spmv_traffic = 99.83e6 / 13824 * ncells
+        # DRAM read + write of one launch from an ncu capture at 24^3 (97.45 + 2.69 MB
+        # over 13,824 cells, the bench configuration), scaled by cells: the kernel
+        # streams each cell record once, so traffic grows with the cells
+        spmv_traffic = 100.14e6 / 13824 * ncells
     spmv_gbs = spmv_bytes / (spmv_ms.value * 1e-3) / 1e9
     # assembly: condensed blocks + vectors read, CSR values + rhs written
     asm_bytes = ncells * (nf * nf + nf) * 8 + nnz * 8 + nfree * 8
