@@ -310,7 +310,8 @@ cudaError_t run_condense(hdg_problem *pb) {
     const float *Mh = pb->d_minv.as<float>(), *Ml = Mh + nk2;
     const float *MGh = Mh + 4 * nk2, *MGl = MGh + pb->tab.D * nk2;
     return launch_condense_ffblock(pb->tab.D, pb->tab.k, (int)nc, Ahi, Ahi + nc * n * n, bhi, bhi + nc * n, Mh, Ml,
-                                   MGh, MGl, pb->d_invm.as<double>(), pb->d_S.as<double>(), pb->d_g.as<double>(), Xhi,
+                                   MGh, MGl, pb->d_ffpat.as<int>(), pb->d_invm.as<double>(), pb->d_S.as<double>(),
+                                   pb->d_g.as<double>(), Xhi,
                                    Xhi + nc * ni * (nf + 1), pb->d_info.as<int>(), ctx->stream, ctx->num_sms,
                                    &ctx->launches);
   }
@@ -515,6 +516,11 @@ int setup_problem(hdg_problem *pb) {
           if (row != col && m.jac[c * m.D * m.D + col * m.D + row] != 0.0) m.axis = false;
   }
   if ((rc = upload(ctx, pb->d_jac, pb->mesh.jac))) return rc;
+  if (pb->physics == HDG_PHYSICS_DARCY && ffblock_supported(pb->mesh.D, pb->mesh.k)) {
+    std::vector<int> pat(ffblock_pattern_ints(pb->mesh.D, pb->mesh.k));
+    ffblock_pattern(pb->mesh.D, pb->mesh.k, pb->tab.lat.data(), pb->mesh.axis, pat.data());
+    if ((rc = upload(ctx, pb->d_ffpat, pat))) return rc;
+  }
   if ((rc = upload(ctx, pb->d_cell_facets, pb->mesh.cell_facets))) return rc;
   if ((rc = upload(ctx, pb->d_facet_dofs, pb->mesh.facet_dofs))) return rc;
   if ((rc = upload(ctx, pb->d_facet_cell, pb->mesh.facet_cell))) return rc;
@@ -2048,6 +2054,7 @@ int hdg_batch_assemble(hdg_batch *b, int precision, int *bad) {
         P.Ml = P.Mh + (size_t)pb->tab.nk * pb->tab.nk;
         P.MGh = P.Mh + 4 * (size_t)pb->tab.nk * pb->tab.nk;
         P.MGl = P.MGh + (size_t)pb->tab.D * pb->tab.nk * pb->tab.nk;
+        P.ffpat = pb->d_ffpat.as<int>();
         P.S = pb->d_S.as<double>();
         P.g = pb->d_g.as<double>();
         P.Xh = pb->d_fact.as<float>();

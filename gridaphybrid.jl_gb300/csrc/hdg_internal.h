@@ -337,7 +337,7 @@ struct hdg_problem {
   hdg::DBuf d_cellop, d_cell_blk, d_qc, d_W, d_v32, d_scal2;
   // block-elimination path: M_ref^{-1} as (hi, lo) floats then FP64, 1/m per
   // cell, the elasticity kernel's per-CTA scratch panels
-  hdg::DBuf d_minv, d_invm, d_escratch;
+  hdg::DBuf d_minv, d_invm, d_escratch, d_ffpat;
   // the L2-panel kernel's sparse reference products: index lists, values
   // ((hi, lo) floats then FP64) and their offsets
   hdg::DBuf d_l2ref_idx, d_l2ref_val;
@@ -373,7 +373,7 @@ struct hdg_problem {
             &d_dirvals, &d_A, &d_b, &d_S, &d_g, &d_fact, &d_info, &d_aux, &d_rowptr, &d_colind, &d_val,
             &d_rhs, &d_br_row0, &d_br_src, &d_blk_off, &d_blk_rowlen, &d_blk_src, &d_diag_blk, &d_dir_cells,
             &d_Binv, &d_x, &d_r, &d_z, &d_p, &d_p2, &d_q, &d_partials, &d_scal, &d_counter, &d_cellop,
-            &d_cell_blk, &d_qc, &d_W, &d_v32, &d_scal2, &d_minv, &d_invm, &d_escratch, &d_l2ref_idx, &d_l2ref_val, &d_uint, &d_errs,
+            &d_cell_blk, &d_qc, &d_W, &d_v32, &d_scal2, &d_minv, &d_invm, &d_escratch, &d_ffpat, &d_l2ref_idx, &d_l2ref_val, &d_uint, &d_errs,
             &d_newton, &d_rmax, &d_dirzero, &d_gstab};
   }
   ~hdg_problem();

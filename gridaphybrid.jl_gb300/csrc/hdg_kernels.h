@@ -218,12 +218,16 @@ cudaError_t launch_condense_mixed(int ncells, int ni, int nf, const float *Ahi, 
                                   long long *launches);
 // Darcy block elimination in float-float (HDG_PREC_FF_BLOCK)
 bool ffblock_supported(int D, int k);
+// the per-facet coupled interior rows the elimination runs over (lat: the
+// Q_k node lattice, nk x D; axis: every cell axis-aligned)
+size_t ffblock_pattern_ints(int D, int k);
+void ffblock_pattern(int D, int k, const int *lat, bool axis, int *out);
 // per cell 10 doubles: 1/m and the panel coefficients cg[e][d]/m (cell_y_coef)
 cudaError_t launch_inv_mass_scale(const CellArgs &a, double *coef, cudaStream_t s, long long *launches);
 // MG_h, MG_l: M^{-1} G_e (D x nk x nk, float-float)
 cudaError_t launch_condense_ffblock(int D, int k, int ncells, const float *Ahi, const float *Alo,
                                     const float *bhi, const float *blo, const float *Minv_h,
-                                    const float *Minv_l, const float *MG_h, const float *MG_l,
+                                    const float *Minv_l, const float *MG_h, const float *MG_l, const int *pat,
                                     const double *coef, double *S, double *g, float *Xhi, float *Xlo, int *info,
                                     cudaStream_t s, int num_sms, long long *launches);
 // Two-field block elimination with L2 panels (k_condense_l2block.cu):
@@ -398,6 +402,7 @@ struct BatchProblem {
   MixedTables T;
   const float *Mh, *Ml;    // M_ref^{-1} (hi, lo), block elimination
   const float *MGh, *MGl;  // M_ref^{-1} G_e (hi, lo)
+  const int *ffpat;        // coupling pattern of the block elimination (ffblock_pattern)
   double *S, *g;         // condensed blocks and vectors
   float *Xh, *Xl;        // float-float recovery pairs, block elimination
   double *fact;          // FP64 recovery factors [U11 | U12 | y]

@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(kBatchThreads) fused_ffblock_kernel(const Batc
     }
     integrate_cell_ffc<C>(P.a, P.T, c, active, f, fq, Ah, Al, bh, bl, t, TPC);
     int *infoc = active ? P.info + c : nullptr;
-    ffb::ffblock_cell<C, TPC, false>(active, Ah, Al, bh, bl, P.Mh, P.Ml, P.MGh, P.MGl, coef, fsm,
+    ffb::ffblock_cell<C, TPC, false>(active, Ah, Al, bh, bl, P.Mh, P.Ml, P.MGh, P.MGl, P.ffpat, coef, fsm,
                                      P.S + (size_t)c * NF * NF,
                                      P.g + (size_t)c * NF, P.Xh + (size_t)c * NI * NC, P.Xl + (size_t)c * NI * NC,
                                      infoc, t);

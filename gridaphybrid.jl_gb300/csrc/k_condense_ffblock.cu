@@ -17,6 +17,8 @@
 // so no refinement is needed (S agrees with the FP64 elimination to ~1e-14).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "hdg_kernels.h"
 #include "k_ff_cell.cuh"
 #include "k_ffblock_cell.cuh"
@@ -31,25 +33,26 @@ __global__ void __launch_bounds__(C::NT, 3)
                             const float *__restrict__ bhi, const float *__restrict__ blo,
                             const float *__restrict__ Minv_h, const float *__restrict__ Minv_l,
                             const float *__restrict__ MG_h, const float *__restrict__ MG_l,
-                            const double *__restrict__ coef, double *S, double *g, float *Xhi, float *Xlo,
-                            int *info) {
+                            const int *__restrict__ pat, const double *__restrict__ coef, double *S, double *g,
+                            float *Xhi, float *Xlo, int *info) {
   constexpr int N = C::N, NF = C::NF, NI = C::NI, NC = C::NC;
   extern __shared__ float smem[];
-  for (int cell = blockIdx.x; cell < ncells; cell += gridDim.x)
+  for (int cell = blockIdx.x; cell < ncells; cell += gridDim.x) {
     ffblock_cell<C, C::NT, true>(true, Ahi + (size_t)cell * N * N, Alo + (size_t)cell * N * N, bhi + (size_t)cell * N,
-                                 blo + (size_t)cell * N, Minv_h, Minv_l, MG_h, MG_l, coef + 10 * (size_t)cell, smem,
+                                 blo + (size_t)cell * N, Minv_h, Minv_l, MG_h, MG_l, pat, coef + 10 * (size_t)cell, smem,
                                  S + (size_t)cell * NF * NF,
                                  g + (size_t)cell * NF, Xhi ? Xhi + (size_t)cell * NI * NC : nullptr,
                                  Xlo ? Xlo + (size_t)cell * NI * NC : nullptr, info ? info + cell : nullptr,
                                  threadIdx.x);
+  }
 }
 
 
 template <class C>
 static cudaError_t launch_cfg(int ncells, const float *Ahi, const float *Alo, const float *bhi, const float *blo,
                               const float *Mh, const float *Ml, const float *MGh, const float *MGl,
-                              const double *coef, double *S, double *g, float *Xhi, float *Xlo, int *info,
-                              cudaStream_t s, int num_sms) {
+                              const int *pat, const double *coef, double *S, double *g, float *Xhi, float *Xlo,
+                              int *info, cudaStream_t s, int num_sms) {
   const size_t smem = C::smem_bytes;
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(condense_ffblock_kernel<C>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -63,8 +66,8 @@ static cudaError_t launch_cfg(int ncells, const float *Ahi, const float *Alo, co
   int grid = num_sms * per_sm;
   if (grid > ncells) grid = ncells;
   if (grid < 1) grid = 1;
-  condense_ffblock_kernel<C><<<grid, C::NT, smem, s>>>(ncells, Ahi, Alo, bhi, blo, Mh, Ml, MGh, MGl, coef, S, g,
-                                                       Xhi, Xlo, info);
+  condense_ffblock_kernel<C><<<grid, C::NT, smem, s>>>(ncells, Ahi, Alo, bhi, blo, Mh, Ml, MGh, MGl, pat, coef, S,
+                                                       g, Xhi, Xlo, info);
   return cudaGetLastError();
 }
 
@@ -74,16 +77,52 @@ bool ffblock_supported(int D, int k) {
   return (D == 2 && k >= 1 && k <= 3) || (D == 3 && k >= 1 && k <= 2);
 }
 
+size_t ffblock_pattern_ints(int D, int k) {
+  int nk = 1;
+  for (int d = 0; d < D; ++d) nk *= k + 1;
+  const int nl = 2 * D, ni = (D + 1) * nk;
+  return (size_t)nl * ni + 8 + (size_t)nl * 4;
+}
+
+// The interior rows of the Darcy cell block that the trace of local facet lf
+// couples to: the cell nodes on the facet (lattice index along the facet's
+// normal dimension dn = D-1-lf/2 equal to k for the upper side lf%2 = 1, 0 for
+// the lower), for the flux components (only the normal one when every cell
+// is axis-aligned: the normal has no other component) and for the pressure;
+// Q_k Lagrange functions of the other nodes vanish on the facet, so the other
+// entries of A_if and A_fi are exactly zero.  Layout (ffblock_pattern_ints):
+// [lf][NI] rows in increasing order, then 8 counts, then [lf][4] the index of
+// each field's first row (flux components 0..D-1, pressure D).
+void ffblock_pattern(int D, int k, const int *lat, bool axis, int *out) {
+  int nk = 1;
+  for (int d = 0; d < D; ++d) nk *= k + 1;
+  const int nl = 2 * D, ni = (D + 1) * nk;
+  std::fill(out, out + ffblock_pattern_ints(D, k), 0);
+  int *cnt = out + (size_t)nl * ni, *seg = cnt + 8;
+  for (int lf = 0; lf < nl; ++lf) {
+    const int dn = D - 1 - lf / 2, side = (lf % 2) * k;
+    int q = 0;
+    for (int fld = 0; fld <= D; ++fld) {
+      seg[lf * 4 + fld] = q;
+      if (fld < D && axis && fld != dn) continue;
+      for (int a = 0; a < nk; ++a)
+        if (lat[a * D + dn] == side) out[lf * ni + q++] = fld * nk + a;
+    }
+    cnt[lf] = q;
+  }
+}
+
 cudaError_t launch_condense_ffblock(int D, int k, int ncells, const float *Ahi, const float *Alo, const float *bhi,
                                     const float *blo, const float *Minv_h, const float *Minv_l, const float *MG_h,
-                                    const float *MG_l, const double *coef, double *S, double *g, float *Xhi,
-                                    float *Xlo, int *info, cudaStream_t s, int num_sms, long long *launches) {
+                                    const float *MG_l, const int *pat, const double *coef, double *S, double *g,
+                                    float *Xhi, float *Xlo, int *info, cudaStream_t s, int num_sms,
+                                    long long *launches) {
   ++*launches;
 #define HDG_FFB(DD, KK)                                                                                   \
   if (D == DD && k == KK)                                                                                 \
     return ffb::launch_cfg<ffb::Cfg<DD, (KK + 1) * (KK + 1) * (DD == 3 ? (KK + 1) : 1),                    \
                                     (DD == 3 ? (KK + 1) * (KK + 1) : (KK + 1))>>(                          \
-        ncells, Ahi, Alo, bhi, blo, Minv_h, Minv_l, MG_h, MG_l, coef, S, g, Xhi, Xlo, info, s, num_sms);
+        ncells, Ahi, Alo, bhi, blo, Minv_h, Minv_l, MG_h, MG_l, pat, coef, S, g, Xhi, Xlo, info, s, num_sms);
   HDG_FFB(2, 1)
   HDG_FFB(2, 2)
   HDG_FFB(2, 3)
