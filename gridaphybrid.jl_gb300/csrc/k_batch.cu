@@ -113,7 +113,7 @@ struct FfbLayout {
 };
 
 template <class C, int TPC>
-__global__ void __launch_bounds__(kBatchThreads) fused_ffblock_kernel(const BatchProblem *__restrict__ probs, int nprob,
+__global__ void __launch_bounds__(kBatchThreads, 4) fused_ffblock_kernel(const BatchProblem *__restrict__ probs, int nprob,
                                                                       long long total, size_t group_bytes,
                                                                       float *scratch, int *bad) {
   constexpr int CPC = kBatchThreads / TPC, N = C::N, NF = C::NF, NI = C::NI, NC = C::NC;

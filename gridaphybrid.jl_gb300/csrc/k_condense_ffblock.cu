@@ -77,11 +77,16 @@ bool ffblock_supported(int D, int k) {
   return (D == 2 && k >= 1 && k <= 3) || (D == 3 && k >= 1 && k <= 2);
 }
 
+// coupled interior rows of one facet at most: the facet's (k+1)^(D-1) nodes
+// of each of the D flux components and of the pressure
+static int ffblock_pattern_stride(int D, int k) {
+  int nfd = 1;
+  for (int d = 0; d < D - 1; ++d) nfd *= k + 1;
+  return (D + 1) * nfd;
+}
+
 size_t ffblock_pattern_ints(int D, int k) {
-  int nk = 1;
-  for (int d = 0; d < D; ++d) nk *= k + 1;
-  const int nl = 2 * D, ni = (D + 1) * nk;
-  return (size_t)nl * ni + 8 + (size_t)nl * 4;
+  return (size_t)2 * D * ffblock_pattern_stride(D, k) + 8 + (size_t)2 * D * 4;
 }
 
 // The interior rows of the Darcy cell block that the trace of local facet lf
@@ -91,14 +96,15 @@ size_t ffblock_pattern_ints(int D, int k) {
 // is axis-aligned: the normal has no other component) and for the pressure;
 // Q_k Lagrange functions of the other nodes vanish on the facet, so the other
 // entries of A_if and A_fi are exactly zero.  Layout (ffblock_pattern_ints):
-// [lf][NI] rows in increasing order, then 8 counts, then [lf][4] the index of
-// each field's first row (flux components 0..D-1, pressure D).
+// [lf][(D+1) (k+1)^(D-1)] rows in increasing order, then 8 counts, then
+// [lf][4] the index of each field's first row (flux components 0..D-1,
+// pressure D).
 void ffblock_pattern(int D, int k, const int *lat, bool axis, int *out) {
   int nk = 1;
   for (int d = 0; d < D; ++d) nk *= k + 1;
-  const int nl = 2 * D, ni = (D + 1) * nk;
+  const int nl = 2 * D, stride = ffblock_pattern_stride(D, k);
   std::fill(out, out + ffblock_pattern_ints(D, k), 0);
-  int *cnt = out + (size_t)nl * ni, *seg = cnt + 8;
+  int *cnt = out + (size_t)nl * stride, *seg = cnt + 8;
   for (int lf = 0; lf < nl; ++lf) {
     const int dn = D - 1 - lf / 2, side = (lf % 2) * k;
     int q = 0;
@@ -106,7 +112,7 @@ void ffblock_pattern(int D, int k, const int *lat, bool axis, int *out) {
       seg[lf * 4 + fld] = q;
       if (fld < D && axis && fld != dn) continue;
       for (int a = 0; a < nk; ++a)
-        if (lat[a * D + dn] == side) out[lf * ni + q++] = fld * nk + a;
+        if (lat[a * D + dn] == side) out[lf * stride + q++] = fld * nk + a;
     }
     cnt[lf] = q;
   }

@@ -81,10 +81,10 @@ struct Cfg {
   // formed), Z (D NK NC), Q (NK NC), each hi + lo -- 71 KB for 3D k=2, three
   // CTAs per SM
   static constexpr size_t smem_floats = 2 * ((size_t)YREG + NK * NK + (size_t)D * NK * NC + NK * NC);
-  // the coupling pattern: per local facet its coupled interior rows (NI
+  // the coupling pattern: per local facet its coupled interior rows (CMAX
   // slots each), the counts (8 slots), the start of each field's rows (4
   // slots per facet)
-  static constexpr int PAT_INTS = NL * NI + 8 + NL * 4;
+  static constexpr int PAT_INTS = NL * CMAX + 8 + NL * 4;
   // + flags (64 ints) + pattern + Y's zero masks (2 D NK) + the pivot rows (32)
   static constexpr size_t smem_bytes = smem_floats * 4 + 64 * 4 + ((size_t)PAT_INTS + 2 * D * NK + 32) * 4;
 };
@@ -105,14 +105,17 @@ __device__ __forceinline__ float ld_cell(const float *p) {
 
 // LU with partial pivoting of the NK x NK pressure Schur complement P (NK <=
 // 32) by one warp, lane i working on row i.  Rows stay in place: perm[j] is
-// the row chosen as pivot of step j (largest |P[.][j]| among the rows not yet
-// chosen, the lowest row on ties); each other free row keeps its multiplier
+// the row chosen as pivot of step j; each other free row keeps its multiplier
 // in column j.  So U's row j is row perm[j] from column j on, and L's row j
-// is row perm[j] left of column j.  Writes the first zero pivot step + 1 (or
-// 0) to *info.
+// is row perm[j] left of column j.  The pivot is the largest |P[.][j]| among
+// the free rows, ties going to the row that a row-swapping LU would hold at
+// the lowest position (pos tracks each row's position under those swaps), so
+// the pivots, multipliers and updates are those of lu_solve_group, bit for
+// bit.  Writes the first zero pivot step + 1 (or 0) to *info.
 template <int NK>
 __device__ __forceinline__ void lu_pivot_warp(float *Ph, float *Pl, int *perm, int *info, int lane) {
   bool free_row = lane < NK;
+  int pos = lane;
   int first_zero = 0;
   for (int j = 0; j < NK; ++j) {
     float v = -1.0f;
@@ -120,20 +123,27 @@ __device__ __forceinline__ void lu_pivot_warp(float *Ph, float *Pl, int *perm, i
       v = fabsf(Ph[lane * NK + j]);
       if (v != v) v = INFINITY;  // a NaN pivot candidate: every lane must pick the same row
     }
-    int bi = lane;
+    int bpos = free_row ? pos : 1 << 20, bi = lane;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
       const float ov = __shfl_xor_sync(0xffffffffu, v, off);
+      const int op = __shfl_xor_sync(0xffffffffu, bpos, off);
       const int oi = __shfl_xor_sync(0xffffffffu, bi, off);
-      if (ov > v || (ov == v && oi < bi)) {
+      if (ov > v || (ov == v && op < bpos)) {
         v = ov;
+        bpos = op;
         bi = oi;
       }
     }
     const int p = bi;  // the same in every lane
     if (v == 0.0f && first_zero == 0) first_zero = j + 1;
     if (lane == 0) perm[j] = p;
-    if (lane == p) free_row = false;
+    // a row-swapping LU exchanges the rows at positions j and bpos
+    if (free_row && pos == j && lane != p) pos = bpos;
+    if (lane == p) {
+      free_row = false;
+      pos = j;
+    }
     const float pvh = Ph[p * NK + j], pvl = Pl[p * NK + j];
     if (free_row && pvh != 0.0f) {
       float lh, ll;
@@ -297,6 +307,109 @@ __device__ __forceinline__ void solve_columns(const float *Ph, const float *Pl, 
   }
 }
 
+// [P | Q] -> [U | X_p] by the whole group: LU with partial pivoting (pivot
+// search by warp 0, rows swapped in place), then back substitution on the NC
+// columns of Q.  For groups of one or two warps (the batched kernels' small
+// cells), where the warp-factorisation path would leave the group's only warp
+// serial.
+template <class C, int NT>
+__device__ __forceinline__ void lu_solve_group(float *Ph, float *Pl, float *Qh, float *Ql, int *sflag, int t) {
+  constexpr int NK = C::NK, NC = C::NC;
+  for (int j = 0; j < NK; ++j) {
+    if (t < 32) {
+      float best = -1.0f;
+      int bi = j;
+      for (int i = j + t; i < NK; i += 32) {
+        const float v = fabsf(Ph[i * NK + j]);
+        if (v > best) {
+          best = v;
+          bi = i;
+        }
+      }
+      for (int off = 16; off > 0; off >>= 1) {
+        const float ob = __shfl_down_sync(0xffffffffu, best, off);
+        const int oi = __shfl_down_sync(0xffffffffu, bi, off);
+        if (ob > best || (ob == best && oi < bi)) {
+          best = ob;
+          bi = oi;
+        }
+      }
+      if (t == 0) {
+        sflag[0] = bi;
+        if (best == 0.0f && sflag[1] == 0) sflag[1] = j + 1;
+      }
+    }
+    __syncthreads();
+    const int p = sflag[0];
+    if (p != j) {
+      for (int c = t; c < NK + NC; c += NT) {
+        float *rh = c < NK ? Ph : Qh, *rl = c < NK ? Pl : Ql;
+        const int ld = c < NK ? NK : NC, cc = c < NK ? c : c - NK;
+        const float th = rh[j * ld + cc], tl = rl[j * ld + cc];
+        rh[j * ld + cc] = rh[p * ld + cc];
+        rl[j * ld + cc] = rl[p * ld + cc];
+        rh[p * ld + cc] = th;
+        rl[p * ld + cc] = tl;
+      }
+    }
+    __syncthreads();
+    const float pvh = Ph[j * NK + j], pvl = Pl[j * NK + j];
+    const int rows = NK - j - 1, cols = NK - j - 1 + NC;
+    for (int i = j + 1 + t; i < NK; i += NT) {
+      if (pvh != 0.0f) {
+        float qh, ql;
+        div(Ph[i * NK + j], Pl[i * NK + j], pvh, pvl, qh, ql);
+        Ph[i * NK + j] = qh;
+        Pl[i * NK + j] = ql;
+      }
+    }
+    __syncthreads();
+    for (int e = t; e < rows * cols; e += NT) {
+      const int i = j + 1 + e / cols, c = e % cols;
+      const float lh = Ph[i * NK + j], ll = Pl[i * NK + j];
+      float uh, ul, *th, *tl;
+      if (c < NK - j - 1) {
+        const int cc = j + 1 + c;
+        uh = Ph[j * NK + cc];
+        ul = Pl[j * NK + cc];
+        th = Ph + i * NK + cc;
+        tl = Pl + i * NK + cc;
+      } else {
+        const int cc = c - (NK - j - 1);
+        uh = Qh[j * NC + cc];
+        ul = Ql[j * NC + cc];
+        th = Qh + i * NC + cc;
+        tl = Ql + i * NC + cc;
+      }
+      float ph, pl, rh, rl;
+      mul(lh, ll, uh, ul, ph, pl);
+      sub(*th, *tl, ph, pl, rh, rl);
+      *th = rh;
+      *tl = rl;
+    }
+    __syncthreads();
+  }
+  for (int j = NK - 1; j >= 0; --j) {
+    const float pvh = Ph[j * NK + j], pvl = Pl[j * NK + j];
+    for (int c = t; c < NC; c += NT) {
+      float qh = 0.0f, ql = 0.0f;
+      if (pvh != 0.0f) div(Qh[j * NC + c], Ql[j * NC + c], pvh, pvl, qh, ql);
+      Qh[j * NC + c] = qh;
+      Ql[j * NC + c] = ql;
+    }
+    __syncthreads();
+    for (int e = t; e < j * NC; e += NT) {
+      const int i = e / NC, c = e % NC;
+      float ph, pl, rh, rl;
+      mul(Ph[i * NK + j], Pl[i * NK + j], Qh[j * NC + c], Ql[j * NC + c], ph, pl);
+      sub(Qh[i * NC + c], Ql[i * NC + c], ph, pl, rh, rl);
+      Qh[i * NC + c] = rh;
+      Ql[i * NC + c] = rl;
+    }
+    __syncthreads();
+  }
+}
+
 // One cell of the block elimination with the NT threads t = 0..NT-1 of the
 // caller's group.  smem: the group's C::smem_bytes of shared memory.  Every
 // thread of the CTA must call it (it contains CTA barriers); a group without a
@@ -323,7 +436,7 @@ __device__ __forceinline__ void ffblock_cell(bool active, const float *__restric
   // split once per cell (FP64 is a narrow pipe on GB300)
   float *wsp = reinterpret_cast<float *>(sflag + 32);
   int *flist = sflag + 64;                             // [lf][q]: interior rows / columns coupled to facet lf
-  int *fcnt = flist + C::NL * NI;                      // [lf]: their count
+  int *fcnt = flist + C::NL * CMAX;                    // [lf]: their count
   int *fseg = fcnt + 8;                                // [lf][d]: start of field d's entries (d <= D)
   unsigned *ycol = reinterpret_cast<unsigned *>(flist + C::PAT_INTS);  // [d][c]: rows a with Y_d[a][c] != 0
   unsigned *yrow = ycol + D * NK;                                       // [d][a]: columns c with Y_d[a][c] != 0
@@ -377,7 +490,7 @@ __device__ __forceinline__ void ffblock_cell(bool active, const float *__restric
       const int cc = c - NK, lf = cc / NFDc;
       const int q1 = fseg[lf * 4 + d + 1];
       for (int q = fseg[lf * 4 + d]; q < q1; ++q) {
-        const int k = flist[lf * NI + q] - d * NK;
+        const int k = flist[lf * CMAX + q] - d * NK;
         mac(h, l, Mh[a * NK + k], Ml[a * NK + k], AH(d * NK + k, NI + cc), AL(d * NK + k, NI + cc));
       }
     } else {  // b
@@ -414,17 +527,20 @@ __device__ __forceinline__ void ffblock_cell(bool active, const float *__restric
     Ph[a * NK + c] = rh;
     Pl[a * NK + c] = rl;
   }
-  __syncthreads();
-  // warp 0 factors P while the other warps form Q (a one-warp group does both)
-  if (warp == 0) lu_pivot_warp<NK>(Ph, Pl, perm, sflag + 1, lane);
-  if constexpr (NT == 32) {
-    form_q<C, 32, RO>(Ah, Al, bh, bl, Zh, Zl, Qh, Ql, fseg, t);
-  } else {
+  if constexpr (NT >= 128) {
+    __syncthreads();
+    // warp 0 factors P while the other warps form Q
+    if (warp == 0) lu_pivot_warp<NK>(Ph, Pl, perm, sflag + 1, lane);
     if (warp > 0) form_q<C, NT - 32, RO>(Ah, Al, bh, bl, Zh, Zl, Qh, Ql, fseg, t - 32);
+    __syncthreads();
+    // X_p = P^{-1} Q (in place in Q)
+    solve_columns<C, NT>(Ph, Pl, Qh, Ql, perm, t);
+  } else {
+    form_q<C, NT, RO>(Ah, Al, bh, bl, Zh, Zl, Qh, Ql, fseg, t);
+    if (t == 0) sflag[1] = 0;
+    __syncthreads();
+    lu_solve_group<C, NT>(Ph, Pl, Qh, Ql, sflag, t);
   }
-  __syncthreads();
-  // X_p = P^{-1} Q (in place in Q)
-  solve_columns<C, NT>(Ph, Pl, Qh, Ql, perm, t);
   __syncthreads();
   // X_{u_d} = Z_d - Y_d X_p (in place in Z)
   for (int o = t; o < D * NK * NC; o += NT) {
@@ -446,7 +562,7 @@ __device__ __forceinline__ void ffblock_cell(bool active, const float *__restric
   for (int e = t; e < NF * CMAX; e += NT) {
     const int q = e / NF, f = e - q * NF, lf = f / NFDc;
     if (q < fcnt[lf]) {
-      const int k = flist[lf * NI + q];
+      const int k = flist[lf * CMAX + q];
       Ash[e] = AH(NI + f, k);
       Asl[e] = AL(NI + f, k);
     }
@@ -472,7 +588,7 @@ __device__ __forceinline__ void ffblock_cell(bool active, const float *__restric
       const int cnt = fcnt[lf];
       const int cl = cb + 1 < NC ? cb + 1 : cb;  // the second column (a duplicate at the ragged end)
       for (int q = 0; q < cnt; ++q) {
-        const int k = flist[lf * NI + q];
+        const int k = flist[lf * CMAX + q];
         const float *xhr = k < NU ? Zh + k * NC : Qh + (k - NU) * NC;
         const float *xlr = k < NU ? Zl + k * NC : Ql + (k - NU) * NC;
         const float x0h = xhr[cb], x0l = xlr[cb], x1h = xhr[cl], x1l = xlr[cl];
