@@ -175,7 +175,7 @@ __device__ __forceinline__ void form_q(const float *__restrict__ Ah, const float
   constexpr int D = C::D, NK = C::NK, NU = C::NU, NI = C::NI, NF = C::NF, N = C::N, NC = C::NC, NFDc = C::NFD;
   constexpr int G = NQ / NK;           // row groups (NK <= 27 < 32 <= NQ)
   constexpr int R = (NC + G - 1) / G;  // columns per group
-  constexpr int RC = 8;                // columns per pass
+  constexpr int RC = NQ >= 128 ? 8 : 4;  // columns per pass (fewer registers in small groups)
   if (tq >= G * NK) return;
   const int a = tq % NK, g = tq / NK;
   const int c_end = (g + 1) * R < NC ? (g + 1) * R : NC;
@@ -527,6 +527,8 @@ __device__ __forceinline__ void ffblock_cell(bool active, const float *__restric
     Ph[a * NK + c] = rh;
     Pl[a * NK + c] = rl;
   }
+  // the warp factorisation pays off where the group has warps to spare (the
+  // whole-group LU measured slower at 256 threads for every cell size)
   if constexpr (NT >= 128) {
     __syncthreads();
     // warp 0 factors P while the other warps form Q
@@ -572,7 +574,11 @@ __device__ __forceinline__ void ffblock_cell(bool active, const float *__restric
   // facet x SC columns: per coupled interior row q a thread loads SR staged
   // A_fi entries and SC entries of X and makes SR x SC products
   {
-    constexpr int SR = NFDc % 3 == 0 ? 3 : (NFDc % 2 == 0 ? 2 : 1), SC = 2;
+    // tiles only where they still give every thread work (small cells keep
+    // one output per thread: the phase is latency-bound there)
+    constexpr int SR0 = NFDc % 3 == 0 ? 3 : (NFDc % 2 == 0 ? 2 : 1);
+    constexpr bool TILE = NF * NC / (SR0 * 2) >= NT;
+    constexpr int SR = TILE ? SR0 : 1, SC = TILE ? 2 : 1;
     constexpr int RT = NFDc / SR, CT = (NC + SC - 1) / SC, TILES = C::NL * RT * CT;
     for (int tile = t; tile < TILES; tile += NT) {
       const int ct = tile % CT, rest = tile / CT, rt = rest % RT, lf = rest / RT;
@@ -586,17 +592,22 @@ __device__ __forceinline__ void ffblock_cell(bool active, const float *__restric
           l[r][j] = 0.0f;
         }
       const int cnt = fcnt[lf];
-      const int cl = cb + 1 < NC ? cb + 1 : cb;  // the second column (a duplicate at the ragged end)
       for (int q = 0; q < cnt; ++q) {
         const int k = flist[lf * CMAX + q];
         const float *xhr = k < NU ? Zh + k * NC : Qh + (k - NU) * NC;
         const float *xlr = k < NU ? Zl + k * NC : Ql + (k - NU) * NC;
-        const float x0h = xhr[cb], x0l = xlr[cb], x1h = xhr[cl], x1l = xlr[cl];
+        float vh[SC], vl[SC];
+#pragma unroll
+        for (int j = 0; j < SC; ++j) {
+          const int c = cb + j < NC ? cb + j : cb;  // a duplicate column at the ragged end
+          vh[j] = xhr[c];
+          vl[j] = xlr[c];
+        }
 #pragma unroll
         for (int r = 0; r < SR; ++r) {
           const float ah = Ash[q * NF + f0 + r], al = Asl[q * NF + f0 + r];
-          mac(h[r][0], l[r][0], ah, al, x0h, x0l);
-          mac(h[r][1], l[r][1], ah, al, x1h, x1l);
+#pragma unroll
+          for (int j = 0; j < SC; ++j) mac(h[r][j], l[r][j], ah, al, vh[j], vl[j]);
         }
       }
 #pragma unroll
