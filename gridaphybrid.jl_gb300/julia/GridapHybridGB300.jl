@@ -392,6 +392,51 @@ function set_refinement!(op::GPUHybridOperator; delta=(op.D == 3 ? 1e-2 : 3e-2),
   op
 end
 
+const HDG_PHYSICS_DARCY = Cint(0)
+const _SPACE_KIND = Dict(:Q => Cint(0), :P => Cint(1), :RT => Cint(2))
+
+"""
+    HybridAffineFEOperator(form::DarcyHDGForm, model::CartesianDiscreteModel, spaces;
+                           copies=1, precision=HDG_PREC_FP64)
+
+The Darcy HDG form on a Cartesian model with a space per field, as the
+reference's tests declare them: `spaces = (kindA, kA, kindB, kB, kindT, kT)`
+with kinds `:Q` (`space=:Q`), `:P` (`space=:P`) or, for the flux, `:RT`
+(`ReferenceFE(raviart_thomas, Float64, k)`): `(:P, 1, :P, 0, :P, 1)` is
+test/DarcyHDGTests.jl:34-36, `(:RT, 0, :Q, 0, :Q, 0)` with `tau = 0` the RT-H
+form of test/DarcyRTHTests.jl:65-72.  `copies = c` builds the multi-field
+space [U_1..U_c, P_1..P_c, L_1..L_c] with bulk fields 1:2c and skeleton fields
+2c+1:3c, the block form repeated per copy
+(test/MultiFieldLagrangeMultipliersTests.jl:40-88); the free DOF values come
+back in that multi-field order.  Condensation in FP64 or FP32 with float-float
+refinement (`HDG_PREC_FF_BLOCK` needs equal-order Q_k fields).
+"""
+function HybridAffineFEOperator(form::DarcyHDGForm, model::CartesianDiscreteModel, spaces::Tuple;
+                                copies::Integer=1, precision=HDG_PREC_FP64, ctx=default_context(),
+                                trial=nothing, test=nothing)
+  desc = get_cartesian_descriptor(model)
+  D = length(desc.partition)
+  cells = Cint[desc.partition...]
+  domain = Float64[]
+  for d in 1:D
+    push!(domain, desc.origin[d], desc.origin[d] + desc.sizes[d] * desc.partition[d])
+  end
+  sp = Cint[_SPACE_KIND[spaces[1]], spaces[2], _SPACE_KIND[spaces[3]], spaces[4], _SPACE_KIND[spaces[5]],
+            spaces[6], 0]
+  h = Ref{Ptr{Cvoid}}(C_NULL)
+  check(ctx, ccall((:hdg_problem_create_cartesian_spaces, LIB), Cint,
+                   (Ptr{Cvoid}, Cint, Ptr{Cint}, Ptr{Float64}, Cint, Ptr{Cint}, Cint, Ptr{Ptr{Cvoid}}),
+                   ctx.handle, D, cells, domain, HDG_PHYSICS_DARCY, sp, copies, h))
+  info = Vector{Clonglong}(undef, 8)
+  check(ctx, ccall((:hdg_problem_info, LIB), Cint, (Ptr{Cvoid}, Ptr{Clonglong}), h[], info))
+  op = GPUHybridOperator(ctx, h[], trial, test, D, info[1], info[3], info[5], Cint(precision))
+  finalizer(_destroy!, op)
+  set_form!(op, form)
+  check(op.ctx, ccall((:hdg_assemble, LIB), Cint, (Ptr{Cvoid}, Cint, Ptr{Cint}), op.problem, op.precision,
+                      Ptr{Cint}(C_NULL)))
+  op
+end
+
 export DarcyHDGForm, GPUHybridOperator, l2_errors, set_refinement!, set_map_precision!
 
 end # module
