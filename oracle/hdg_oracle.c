@@ -1049,9 +1049,18 @@ int orc_csr_pattern(int D, int k, int ncells, int nfacets,
                            nnz);
 }
 
+int orc_csr_pattern_nl(int nl, int nfd, int ncells, int nfacets, const int *cell_facets, const int *facet_dofs,
+                       int nfree, int64_t *rowptr, int32_t *colind, int64_t *nnz);
+
+/* box cells: 2D facets per cell */
 int orc_csr_pattern_n(int D, int nfd, int ncells, int nfacets, const int *cell_facets, const int *facet_dofs,
                       int nfree, int64_t *rowptr, int32_t *colind, int64_t *nnz) {
-  int nl = 2 * D;
+  return orc_csr_pattern_nl(2 * D, nfd, ncells, nfacets, cell_facets, facet_dofs, nfree, rowptr, colind, nnz);
+}
+
+/* nl facets per cell (2D for boxes, D + 1 for simplices) */
+int orc_csr_pattern_nl(int nl, int nfd, int ncells, int nfacets, const int *cell_facets, const int *facet_dofs,
+                       int nfree, int64_t *rowptr, int32_t *colind, int64_t *nnz) {
   /* facet -> cells */
   int *fc = malloc(sizeof(int) * 2 * nfacets);
   for (int f = 0; f < 2 * nfacets; ++f) fc[f] = -1;
@@ -1128,10 +1137,21 @@ int orc_assemble(int D, int k, int ncells, const int *cell_facets,
                         colind, val, rhs);
 }
 
+int orc_assemble_nl(int nl, int nfd, int ncells, const int *cell_facets, const int *facet_dofs, int nfree,
+                    const double *dir_vals, const double *S, const double *g, const int64_t *rowptr,
+                    const int32_t *colind, double *val, double *rhs);
+
 int orc_assemble_n(int D, int nfd, int ncells, const int *cell_facets, const int *facet_dofs, int nfree,
                    const double *dir_vals, const double *S, const double *g, const int64_t *rowptr,
                    const int32_t *colind, double *val, double *rhs) {
-  int nl = 2 * D, nf = nl * nfd;
+  return orc_assemble_nl(2 * D, nfd, ncells, cell_facets, facet_dofs, nfree, dir_vals, S, g, rowptr, colind, val,
+                         rhs);
+}
+
+int orc_assemble_nl(int nl, int nfd, int ncells, const int *cell_facets, const int *facet_dofs, int nfree,
+                    const double *dir_vals, const double *S, const double *g, const int64_t *rowptr,
+                    const int32_t *colind, double *val, double *rhs) {
+  int nf = nl * nfd;
   if (nf > 512) return -1;
   memset(val, 0, sizeof(double) * rowptr[nfree]);
   memset(rhs, 0, sizeof(double) * nfree);
@@ -1292,9 +1312,17 @@ int orc_cell_skeleton_values(int D, int k, int ncells, const int *cell_facets,
   return orc_cell_skeleton_values_n(D, ipow(k + 1, D - 1), ncells, cell_facets, facet_dofs, xfree, dir_vals, xcell);
 }
 
+int orc_cell_skeleton_values_nl(int nl, int nfd, int ncells, const int *cell_facets, const int *facet_dofs,
+                                const double *xfree, const double *dir_vals, double *xcell);
+
 int orc_cell_skeleton_values_n(int D, int nfd, int ncells, const int *cell_facets, const int *facet_dofs,
                                const double *xfree, const double *dir_vals, double *xcell) {
-  int nl = 2 * D, nf = nl * nfd;
+  return orc_cell_skeleton_values_nl(2 * D, nfd, ncells, cell_facets, facet_dofs, xfree, dir_vals, xcell);
+}
+
+int orc_cell_skeleton_values_nl(int nl, int nfd, int ncells, const int *cell_facets, const int *facet_dofs,
+                                const double *xfree, const double *dir_vals, double *xcell) {
+  int nf = nl * nfd;
 #pragma omp parallel for schedule(static)
   for (int c = 0; c < ncells; ++c)
     for (int lf = 0; lf < nl; ++lf)
@@ -2557,5 +2585,320 @@ int orc_gs_l2_errors(int D, int phys, const int *spaces, const int *n, const dou
   *err1 = sqrt(e1);
   *err2 = sqrt(e2);
   gstab_free(&g);
+  return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Simplex meshes: the Darcy HDG form on triangles and tetrahedra with P_k   */
+/* fields, as test/DarcyHDGTests.jl:174-177 runs it on simplexify(...) of    */
+/* the Cartesian model.  The reference simplex has vertices v_0 = 0 and      */
+/* v_j = e_{j-1}; local facet lf is the face opposite vertex D - lf, its     */
+/* vertices in increasing local order (the lexicographic face order of a     */
+/* simplex polytope).  A cell's vertices are listed in increasing global     */
+/* order, so a facet's parametrisation (its vertices in increasing global    */
+/* order) is the same from both of its cells and the trace basis needs no    */
+/* permutation (the reference handles general vertex orders through the     */
+/* face vertex permutations of src/Skeleton.jl:282-342).  Cell geometry is   */
+/* given as x = x0 + J xi; gradients go through J^{-T}, normals are          */
+/* J^{-T} n_ref / |J^{-T} n_ref|, and the facet measure is |det J|           */
+/* |J^{-T} n_ref| times the reference face's measure over the unit           */
+/* (D-1)-simplex (sqrt(D) for the face opposite v_0, 1 for the others).      */
+/* ------------------------------------------------------------------------ */
+
+typedef struct {
+  int D, kA, kB, kT, nA, nB, nT, ni, nfd, nf, n, n1, nqv, nqf;
+  obasis A, B, T;
+  double *qv_xi, *qv_w, *qf_s, *qf_w;
+} sxtab;
+
+static void sxtab_free(sxtab *t) {
+  obasis_free(&t->A);
+  obasis_free(&t->B);
+  obasis_free(&t->T);
+  free(t->qv_xi); free(t->qv_w); free(t->qf_s); free(t->qf_w);
+}
+
+/* collapsed (Duffy) Gauss rule on the unit d-simplex, n1 points per direction:
+ * xi_1 = u_1, xi_2 = u_2 (1 - u_1), xi_3 = u_3 (1 - u_1)(1 - u_2) */
+static int simplex_rule(int d, int n1, double **xi, double **w) {
+  double x1[16], w1[16];
+  orc_gauss_legendre01(n1, x1, w1);
+  const int nq = d == 0 ? 1 : ipow(n1, d);
+  *xi = malloc(sizeof(double) * nq * (d > 0 ? d : 1));
+  *w = malloc(sizeof(double) * nq);
+  for (int q = 0; q < nq; ++q) {
+    double u[3] = {0, 0, 0}, wt = 1.0, scale = 1.0;
+    for (int j = 0, r = q; j < d; ++j, r /= n1) {
+      u[j] = x1[r % n1];
+      wt *= w1[r % n1];
+    }
+    for (int j = 0; j < d; ++j) {
+      (*xi)[q * d + j] = u[j] * scale;
+      if (j + 1 < d) {
+        wt *= pow(1.0 - u[j], d - 1 - j);
+        scale *= 1.0 - u[j];
+      }
+    }
+    (*w)[q] = wt;
+  }
+  return nq;
+}
+
+static int sxtab_init(sxtab *t, int D, const int *sp) {
+  memset(t, 0, sizeof(*t));
+  if (D < 2 || D > 3 || sp[0] != GS_P || sp[2] != GS_P || sp[4] != GS_P) return -1;
+  t->D = D;
+  t->kA = sp[1];
+  t->kB = sp[3];
+  t->kT = sp[5];
+  if (obasis_init(&t->A, D, GS_P, sp[1]) || obasis_init(&t->B, D, GS_P, sp[3]) ||
+      obasis_init(&t->T, D - 1, GS_P, sp[5])) {
+    sxtab_free(t);
+    return -1;
+  }
+  t->nA = t->A.nb;
+  t->nB = t->B.nb;
+  t->nT = t->T.nb;
+  t->ni = D * t->nA + t->nB;
+  t->nfd = t->nT;
+  t->nf = (D + 1) * t->nfd;
+  t->n = t->ni + t->nf;
+  int kmax = t->kA > t->kB ? t->kA : t->kB;
+  if (t->kT > kmax) kmax = t->kT;
+  t->n1 = kmax + 2;
+  t->nqv = simplex_rule(D, t->n1, &t->qv_xi, &t->qv_w);
+  t->nqf = simplex_rule(D - 1, t->n1, &t->qf_s, &t->qf_w);
+  return 0;
+}
+
+static void simplex_face_point(int D, int lf, const double *s, double *xi) {
+  int fv[3], k = 0;
+  const int opp = D - lf;
+  for (int v = 0; v <= D; ++v)
+    if (v != opp) fv[k++] = v;
+  double V[4][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  for (int d = 0; d < D; ++d) {
+    xi[d] = V[fv[0]][d];
+    for (int j = 0; j + 1 < D; ++j) xi[d] += s[j] * (V[fv[j + 1]][d] - V[fv[0]][d]);
+  }
+}
+
+static void simplex_ref_normal(int D, int lf, double *nh, double *ratio) {
+  const int opp = D - lf;
+  for (int d = 0; d < D; ++d) nh[d] = 0.0;
+  if (opp == 0) {
+    for (int d = 0; d < D; ++d) nh[d] = 1.0 / sqrt((double)D);
+    *ratio = sqrt((double)D);
+  } else {
+    nh[opp - 1] = -1.0;
+    *ratio = 1.0;
+  }
+}
+
+/* inverse (row-major Ji[r][c]) and determinant of the D x D column-major J */
+static double sx_inverse(int D, const double *Jc, double Ji[3][3]) {
+  double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  for (int c = 0; c < D; ++c)
+    for (int r = 0; r < D; ++r) J[r][c] = Jc[c * D + r];
+  double det;
+  if (D == 2) {
+    det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+    Ji[0][0] = J[1][1] / det; Ji[0][1] = -J[0][1] / det;
+    Ji[1][0] = -J[1][0] / det; Ji[1][1] = J[0][0] / det;
+  } else {
+    const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1], c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2],
+                 c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+    det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+    Ji[0][0] = c00 / det; Ji[1][0] = c01 / det; Ji[2][0] = c02 / det;
+    Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / det;
+    Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / det;
+    Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / det;
+    Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det;
+    Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / det;
+    Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
+  }
+  return det;
+}
+
+int orc_sx_sizes(int D, const int *spaces, int *sizes /* ni, nf, nfd, nA, nB, nT, nqv */) {
+  sxtab t;
+  if (sxtab_init(&t, D, spaces)) return -1;
+  sizes[0] = t.ni; sizes[1] = t.nf; sizes[2] = t.nfd; sizes[3] = t.nA; sizes[4] = t.nB; sizes[5] = t.nT;
+  sizes[6] = t.nqv;
+  sxtab_free(&t);
+  return 0;
+}
+
+/* The Darcy HDG cell blocks (the form of test/DarcyHDGTests.jl:125-135 with a
+ * per-cell permeability in the flux mass term and the box form's term
+ * layout) on simplex cells: origin (ncells x D), jac (ncells x D x D,
+ * column-major), sgn (ncells x (D+1): n . n_owner of each local facet),
+ * coef (ncells, NULL = 1).  A column-major n x n per cell, b n per cell. */
+int orc_sx_integrate(int D, const int *spaces, int ncells, const double *origin, const double *jac,
+                     const double *sgn, double tau, int stab, int problem, const double *coef, double *A,
+                     double *b) {
+  sxtab t;
+  if (sxtab_init(&t, D, spaces)) return -1;
+  const int nA = t.nA, nB = t.nB, nT = t.nT, N = t.n, ni = t.ni, oB = D * nA;
+  int bad = 0;
+#pragma omp parallel for schedule(dynamic, 8) reduction(| : bad)
+  for (int c = 0; c < ncells; ++c) {
+    double Ji[3][3];
+    const double *Jc = jac + (size_t)c * D * D, *x0 = origin + (size_t)c * D;
+    const double det = sx_inverse(D, Jc, Ji), adet = fabs(det);
+    const double kap = coef ? coef[c] : 1.0;
+    double *Ac = A + (size_t)c * N * N, *bc = b + (size_t)c * N;
+    memset(Ac, 0, sizeof(double) * (size_t)N * N);
+    memset(bc, 0, sizeof(double) * N);
+#define AIJ(i, j) Ac[(size_t)(i) + (size_t)N * (j)]
+    double pA[64], dA[64 * 3], gA[64 * 3], pB[64], dB[64 * 3], gB[64 * 3], mu[64];
+    if (nA > 64 || nB > 64 || nT > 64) {
+      bad |= 1;
+      continue;
+    }
+    for (int q = 0; q < t.nqv; ++q) {
+      const double *xi = &t.qv_xi[q * D];
+      obasis_eval(&t.A, xi, pA, dA);
+      obasis_eval(&t.B, xi, pB, dB);
+      for (int a = 0; a < nA; ++a)
+        for (int d = 0; d < D; ++d) {
+          gA[a * D + d] = 0.0;
+          for (int e = 0; e < D; ++e) gA[a * D + d] += Ji[e][d] * dA[a * D + e];
+        }
+      for (int a = 0; a < nB; ++a)
+        for (int d = 0; d < D; ++d) {
+          gB[a * D + d] = 0.0;
+          for (int e = 0; e < D; ++e) gB[a * D + d] += Ji[e][d] * dB[a * D + e];
+        }
+      const double wq = t.qv_w[q] * adet;
+      double x[3];
+      for (int d = 0; d < D; ++d) {
+        x[d] = x0[d];
+        for (int e = 0; e < D; ++e) x[d] += Jc[e * D + d] * xi[e];
+      }
+      double pe, qe[3], fu[3], gg;
+      exact(problem, D, x, kap, &pe, qe, fu, &gg);
+      for (int a = 0; a < nA; ++a) {
+        for (int a2 = 0; a2 < nA; ++a2)
+          for (int d = 0; d < D; ++d) AIJ(d * nA + a, d * nA + a2) += wq * pA[a] * pA[a2] / kap;
+        for (int bb = 0; bb < nB; ++bb)
+          for (int d = 0; d < D; ++d) {
+            AIJ(d * nA + a, oB + bb) -= wq * gA[a * D + d] * pB[bb]; /* -(div v) p */
+            AIJ(oB + bb, d * nA + a) -= wq * gB[bb * D + d] * pA[a]; /* -grad(q).u */
+          }
+        for (int d = 0; d < D; ++d) bc[d * nA + a] += wq * pA[a] * fu[d];
+      }
+      for (int bb = 0; bb < nB; ++bb) bc[oB + bb] += wq * pB[bb] * gg;
+    }
+    for (int lf = 0; lf <= D; ++lf) {
+      double nh[3], ratio, v[3] = {0, 0, 0}, nv = 0.0, nrm[3];
+      simplex_ref_normal(D, lf, nh, &ratio);
+      for (int d = 0; d < D; ++d) {
+        for (int e = 0; e < D; ++e) v[d] += Ji[e][d] * nh[e];
+        nv += v[d] * v[d];
+      }
+      nv = sqrt(nv);
+      for (int d = 0; d < D; ++d) nrm[d] = v[d] / nv;
+      const double area = adet * nv * ratio;
+      const double s = stab == 1 ? sgn[(size_t)c * (D + 1) + lf] : 1.0;
+      const int off = ni + lf * t.nfd;
+      for (int q = 0; q < t.nqf; ++q) {
+        double xi[3];
+        simplex_face_point(D, lf, &t.qf_s[q * (D - 1)], xi);
+        obasis_eval(&t.A, xi, pA, NULL);
+        obasis_eval(&t.B, xi, pB, NULL);
+        obasis_eval(&t.T, &t.qf_s[q * (D - 1)], mu, NULL);
+        const double wq = t.qf_w[q] * area;
+        for (int a = 0; a < nA; ++a)
+          for (int m = 0; m < nT; ++m)
+            for (int d = 0; d < D; ++d) {
+              const double vv = wq * pA[a] * nrm[d] * mu[m];
+              AIJ(d * nA + a, off + m) += vv; /* (v.n) l */
+              AIJ(off + m, d * nA + a) += vv; /* m (u.n) */
+            }
+        for (int bb = 0; bb < nB; ++bb) {
+          for (int m = 0; m < nT; ++m) {
+            AIJ(oB + bb, off + m) -= wq * tau * s * pB[bb] * mu[m]; /* -tau q l (n.no) */
+            AIJ(off + m, oB + bb) += wq * tau * s * mu[m] * pB[bb]; /* tau m p (n.no) */
+          }
+          for (int a = 0; a < nA; ++a)
+            for (int d = 0; d < D; ++d) AIJ(oB + bb, d * nA + a) += wq * pB[bb] * pA[a] * nrm[d]; /* q (u.n) */
+          for (int b2 = 0; b2 < nB; ++b2) AIJ(oB + bb, oB + b2) += wq * tau * s * pB[bb] * pB[b2];
+        }
+        for (int m = 0; m < nT; ++m)
+          for (int m2 = 0; m2 < nT; ++m2) AIJ(off + m, off + m2) -= wq * tau * s * mu[m] * mu[m2];
+      }
+    }
+#undef AIJ
+  }
+  sxtab_free(&t);
+  return bad ? -1 : 0;
+}
+
+/* Dirichlet values: the exact pressure at the trace basis' nodes of each
+ * boundary facet (its own parametrisation), through the facet's cell
+ * (cell_lf[f] = (c, lf) of a cell around facet f). */
+int orc_sx_dirichlet_values(int D, const int *spaces, int nfacets, const int *facet_cell_lf, const double *origin,
+                            const double *jac, int problem, const int *facet_dofs, int ndir, double *vals) {
+  sxtab t;
+  if (sxtab_init(&t, D, spaces)) return -1;
+  for (int f = 0; f < nfacets; ++f) {
+    const int c = facet_cell_lf[2 * f], lf = facet_cell_lf[2 * f + 1];
+    for (int m = 0; m < t.nT; ++m) {
+      const int id = facet_dofs[f * t.nfd + m];
+      if (id >= 0) continue;
+      double xi[3], x[3];
+      simplex_face_point(D, lf, &t.T.nodes[m * (D - 1)], xi);
+      const double *x0 = origin + (size_t)c * D, *Jc = jac + (size_t)c * D * D;
+      for (int d = 0; d < D; ++d) {
+        x[d] = x0[d];
+        for (int e = 0; e < D; ++e) x[d] += Jc[e * D + d] * xi[e];
+      }
+      double p, qv[3], fu[3], gg;
+      exact(problem, D, x, 1.0, &p, qv, fu, &gg);
+      if (-1 - id < ndir) vals[-1 - id] = p;
+    }
+  }
+  sxtab_free(&t);
+  return 0;
+}
+
+int orc_sx_l2_errors(int D, const int *spaces, int ncells, const double *origin, const double *jac, int problem,
+                     const double *coef, const double *uint, double *e1, double *e2) {
+  sxtab t;
+  if (sxtab_init(&t, D, spaces)) return -1;
+  const int nA = t.nA, nB = t.nB, ni = t.ni;
+  double ef = 0.0, ep = 0.0;
+#pragma omp parallel for reduction(+ : ef, ep) schedule(static)
+  for (int c = 0; c < ncells; ++c) {
+    double Ji[3][3], pA[64], pB[64];
+    const double *Jc = jac + (size_t)c * D * D, *x0 = origin + (size_t)c * D;
+    const double adet = fabs(sx_inverse(D, Jc, Ji)), kap = coef ? coef[c] : 1.0;
+    const double *u = uint + (size_t)c * ni;
+    for (int q = 0; q < t.nqv; ++q) {
+      const double *xi = &t.qv_xi[q * D];
+      obasis_eval(&t.A, xi, pA, NULL);
+      obasis_eval(&t.B, xi, pB, NULL);
+      double x[3];
+      for (int d = 0; d < D; ++d) {
+        x[d] = x0[d];
+        for (int e = 0; e < D; ++e) x[d] += Jc[e * D + d] * xi[e];
+      }
+      double p, qe[3], fu[3], gg;
+      exact(problem, D, x, kap, &p, qe, fu, &gg);
+      const double w = t.qv_w[q] * adet;
+      for (int d = 0; d < D; ++d) {
+        double qh = 0.0;
+        for (int a = 0; a < nA; ++a) qh += u[d * nA + a] * pA[a];
+        ef += w * (qe[d] - qh) * (qe[d] - qh);
+      }
+      double ph = 0.0;
+      for (int a = 0; a < nB; ++a) ph += u[D * nA + a] * pB[a];
+      ep += w * (p - ph) * (p - ph);
+    }
+  }
+  *e1 = sqrt(ef);
+  *e2 = sqrt(ep);
+  sxtab_free(&t);
   return 0;
 }

@@ -568,6 +568,156 @@ GsMesh.assemble = ElasticityMesh.assemble
 GsMesh.cell_skeleton_values = ElasticityMesh.cell_skeleton_values
 
 
+class SimplexMesh:
+    """simplexify(CartesianDiscreteModel(domain, n)): every box cell split into
+    D! simplices around its diagonal from the lowest to the highest vertex
+    (Kuhn: one simplex per order in which the path from that vertex steps along
+    the axes; 2 triangles per square, 6 tetrahedra per cube), in box order then
+    in lexicographic order of the axis permutation.  Vertices are the lattice
+    points numbered with x fastest; a cell lists its vertices in increasing
+    global order; local facet lf is the face opposite local vertex D - lf;
+    facets are numbered in first-met order over (cell, local facet); the owner
+    of a facet is its first cell; facet DOFs are numbered facet by facet, the
+    boundary facets' DOFs Dirichlet (negative ids)."""
+
+    def __init__(self, D, n, spaces, domain=None):
+        import itertools
+        self.D, self.n = D, tuple(int(v) for v in n)
+        self.domain = np.array(domain if domain is not None else [0.0, 1.0] * D, dtype=np.float64)
+        self.spaces = np.ascontiguousarray(spaces, dtype=np.int32)
+        sz = np.zeros(7, dtype=np.int32)
+        assert lib().orc_sx_sizes(D, P(self.spaces), P(sz)) == 0, "unsupported simplex spaces"
+        self.ni, self.nf, self.nfd, self.nA, self.nB, self.nT, self.nqv = (int(v) for v in sz)
+        nv = [v + 1 for v in self.n]
+        h = [(self.domain[2 * d + 1] - self.domain[2 * d]) / self.n[d] for d in range(D)]
+
+        def vid(idx):
+            r, m = 0, 1
+            for d in range(D):
+                r += idx[d] * m
+                m *= nv[d]
+            return r
+
+        cells = []
+        for box in itertools.product(*[range(v) for v in reversed(self.n)]):
+            box = tuple(reversed(box))  # x fastest
+            for perm in itertools.permutations(range(D)):
+                cur = list(box)
+                verts = [vid(cur)]
+                for ax in perm:
+                    cur[ax] += 1
+                    verts.append(vid(cur))
+                cells.append(sorted(verts))
+        self.cells = np.array(cells, dtype=np.int64)
+        self.ncells = len(cells)
+        coords = np.zeros((int(np.prod(nv)), D))
+        for idx in itertools.product(*[range(v) for v in nv]):
+            coords[vid(idx)] = [self.domain[2 * d] + idx[d] * h[d] for d in range(D)]
+        self.coords = coords
+        nl = D + 1
+        self.nl = nl
+        fid = {}
+        cell_facets = np.zeros((self.ncells, nl), dtype=np.int32)
+        fcells = []
+        for c, vs in enumerate(cells):
+            for lf in range(nl):
+                opp = D - lf
+                key = tuple(v for j, v in enumerate(vs) if j != opp)
+                if key not in fid:
+                    fid[key] = len(fcells)
+                    fcells.append([c, lf, -1, -1])
+                else:
+                    fcells[fid[key]][2:] = [c, lf]
+                cell_facets[c, lf] = fid[key]
+        self.cell_facets = cell_facets
+        self.nfacets = len(fcells)
+        fc = np.array(fcells, dtype=np.int32)
+        self.facet_cells = np.ascontiguousarray(fc[:, [0, 2]])
+        self.facet_cell_lf = np.ascontiguousarray(fc[:, [0, 1]])
+        self.facet_is_boundary = (fc[:, 2] < 0).astype(np.int32)
+        self.facet_dofs = np.zeros((self.nfacets, self.nfd), dtype=np.int32)
+        nfree, ndir = ctypes.c_int(), ctypes.c_int()
+        lib().orc_facet_dofs_n(self.nfd, self.nfacets, P(self.facet_is_boundary), P(self.facet_dofs),
+                               ctypes.byref(nfree), ctypes.byref(ndir))
+        self.nfree, self.ndir = nfree.value, ndir.value
+        X = coords[self.cells]  # ncells x (D+1) x D
+        self.origin = np.ascontiguousarray(X[:, 0, :])
+        # column-major J per cell: column j = x_{j+1} - x_0
+        self.jac = np.ascontiguousarray((X[:, 1:, :] - X[:, :1, :]).reshape(self.ncells, D * D))
+        self.sgn = np.where(self.facet_cells[cell_facets, 0] == np.arange(self.ncells)[:, None], 1.0, -1.0)
+
+    def integrate(self, tau=1.0, stab=STAB_TEXTBOOK, problem=PROBLEM_LINEAR, coef=None):
+        n = self.ni + self.nf
+        A = np.zeros((self.ncells, n, n))
+        b = np.zeros((self.ncells, n))
+        cf = None if coef is None else np.ascontiguousarray(coef, dtype=np.float64)
+        rc = lib().orc_sx_integrate(self.D, P(self.spaces), self.ncells, P(self.origin), P(self.jac),
+                                    P(np.ascontiguousarray(self.sgn)), ctypes.c_double(tau), stab, problem, P(cf),
+                                    P(A), P(b))
+        assert rc == 0
+        return A, b
+
+    def dirichlet_values(self, problem):
+        vals = np.zeros(max(self.ndir, 1))
+        lib().orc_sx_dirichlet_values(self.D, P(self.spaces), self.nfacets, P(self.facet_cell_lf), P(self.origin),
+                                      P(self.jac), problem, P(self.facet_dofs), self.ndir, P(vals))
+        return vals[:self.ndir]
+
+    def csr_pattern(self):
+        nnz = ctypes.c_int64()
+        L = lib()
+        L.orc_csr_pattern_nl(self.nl, self.nfd, self.ncells, self.nfacets, P(self.cell_facets), P(self.facet_dofs),
+                             self.nfree, None, None, ctypes.byref(nnz))
+        rowptr = np.zeros(self.nfree + 1, dtype=np.int64)
+        colind = np.zeros(nnz.value, dtype=np.int32)
+        L.orc_csr_pattern_nl(self.nl, self.nfd, self.ncells, self.nfacets, P(self.cell_facets), P(self.facet_dofs),
+                             self.nfree, P(rowptr), P(colind), ctypes.byref(nnz))
+        return rowptr, colind
+
+    def assemble(self, S, g, dirvals):
+        rowptr, colind = self.csr_pattern()
+        val = np.zeros(len(colind))
+        rhs = np.zeros(self.nfree)
+        dv = np.ascontiguousarray(dirvals if len(dirvals) else np.zeros(1))
+        rc = lib().orc_assemble_nl(self.nl, self.nfd, self.ncells, P(self.cell_facets), P(self.facet_dofs),
+                                   self.nfree, P(dv), P(np.ascontiguousarray(S)), P(np.ascontiguousarray(g)),
+                                   P(rowptr), P(colind), P(val), P(rhs))
+        assert rc == 0
+        return rowptr, colind, val, rhs
+
+    def cell_skeleton_values(self, lam, dirvals):
+        x = np.zeros((self.ncells, self.nf))
+        dv = np.ascontiguousarray(dirvals if len(dirvals) else np.zeros(1))
+        lib().orc_cell_skeleton_values_nl(self.nl, self.nfd, self.ncells, P(self.cell_facets), P(self.facet_dofs),
+                                          P(np.ascontiguousarray(lam)), P(dv), P(x))
+        return x
+
+    def l2_errors(self, problem, uint, coef=None):
+        e1, e2 = ctypes.c_double(), ctypes.c_double()
+        cf = None if coef is None else np.ascontiguousarray(coef, dtype=np.float64)
+        lib().orc_sx_l2_errors(self.D, P(self.spaces), self.ncells, P(self.origin), P(self.jac), problem, P(cf),
+                               P(np.ascontiguousarray(uint)), ctypes.byref(e1), ctypes.byref(e2))
+        return e1.value, e2.value
+
+
+def solve_simplex(D, n, spaces, tau=1.0, stab=STAB_TEXTBOOK, problem=PROBLEM_LINEAR, coef=None, domain=None):
+    """The Darcy HDG path on a simplexified Cartesian mesh, on the CPU:
+    integrate, StaticCondensationMap, assemble, dense LU on the skeleton,
+    BackwardStaticCondensationMap, L2 errors of the flux and the pressure."""
+    m = SimplexMesh(D, n, spaces, domain)
+    A, b = m.integrate(tau=tau, stab=stab, problem=problem, coef=coef)
+    S, g, info = static_condensation(A, b, m.ni)
+    assert (info == 0).all()
+    dv = m.dirichlet_values(problem)
+    rowptr, colind, val, rhs = m.assemble(S, g, dv)
+    lam = dense_solve(rowptr, colind, val, rhs)
+    xc = m.cell_skeleton_values(lam, dv)
+    uint, _ = backward_static_condensation(A, b, xc, m.ni)
+    e1, e2 = m.l2_errors(problem, uint, coef=coef)
+    return dict(uint=uint, lam=lam, err1=e1, err2=e2, mesh=m, A=A, b=b, S=S, g=g, val=val, rhs=rhs,
+                rowptr=rowptr, colind=colind)
+
+
 def solve_gs(D, n, phys, spaces, tau=1.0, stab=STAB_TEXTBOOK, problem=PROBLEM_LINEAR, coef=None, E=1.0, solver=0,
              sign=None, rtol=1e-13, maxit=100000, domain=None, copies=1):
     """The general-space path on the CPU: integrate, StaticCondensationMap,

@@ -152,3 +152,44 @@ def test_copies_solve_copy_by_copy():
     for cp in range(2):
         assert np.abs(lam[cp] - r1["lam"]).max() < 1e-13
         assert np.abs(r2["uint"][:, r2["mesh"].maps[cp][:r1["mesh"].ni]] - r1["uint"]).max() < 1e-13
+
+
+@pytest.mark.parametrize("D,n", [(2, (2, 2)), (3, (2, 2, 2))])
+def test_reference_darcy_kat_on_simplexified_mesh(D, n):
+    """test/DarcyHDGTests.jl:174-177: simplexify of the 2x2 quads with the
+    reference's P_1 / P_0 / P_1 spaces and the n.n_o form."""
+    sp = oracle.gs_spaces(P, 1, P, 0, P, 1)
+    r = oracle.solve_simplex(D, n, sp, tau=1.0, stab=oracle.STAB_OWNER_SIGN, problem=oracle.PROBLEM_REF_LINEAR)
+    m = r["mesh"]
+    assert m.ncells == np.prod(n) * (2 if D == 2 else 6)
+    if D == 2:  # 8 triangles, 12 edges of the quads + 4 diagonals
+        assert (m.ncells, m.nfacets, m.ni, m.nf) == (8, 16, 7, 6)
+    assert r["err1"] < 1e-12 and r["err2"] < 1e-12
+
+
+@pytest.mark.parametrize("D,k", [(2, 1), (2, 2), (3, 1)])
+def test_simplex_hdg_converges_at_k_plus_one(D, k):
+    sp = oracle.gs_spaces(P, k, P, k, P, k)
+    ns = (3, 6) if D == 3 else (4, 8)
+    errs = [oracle.solve_simplex(D, (n,) * D, sp, tau=1.0, problem=oracle.PROBLEM_SIN) for n in ns]
+    for key in ("err1", "err2"):
+        assert np.log2(errs[0][key] / errs[1][key]) > k + 0.8, key
+
+
+def test_simplex_mesh_is_conforming_and_owner_signs_pair_up():
+    m = oracle.SimplexMesh(3, (2, 3, 2), oracle.gs_spaces(P, 1, P, 0, P, 1))
+    # every interior facet has exactly two cells, with opposite owner signs
+    interior = m.facet_is_boundary == 0
+    assert (m.facet_cells[interior, 1] >= 0).all() and (m.facet_cells[~interior, 1] < 0).all()
+    c0, c1 = m.facet_cells[interior, 0], m.facet_cells[interior, 1]
+    assert (c0 < c1).all()
+    # boundary facets lie on the domain's boundary: all their vertices share a coordinate at 0 or 1
+    X = m.coords
+    for f in np.flatnonzero(~interior)[:50]:
+        c, lf = m.facet_cell_lf[f]
+        vs = [v for j, v in enumerate(m.cells[c]) if j != 3 - lf]
+        pts = X[vs]
+        assert any(np.allclose(pts[:, d], 0.0) or np.allclose(pts[:, d], 1.0) for d in range(3))
+    # volumes add up to the domain's
+    J = m.jac.reshape(-1, 3, 3)
+    assert abs(np.abs(np.linalg.det(J)).sum() / 6.0 - 1.0) < 1e-12
