@@ -147,6 +147,8 @@ GsArgs gs_args(hdg_problem *pb) {
   g.nfd = t.nfd;
   g.n = t.n;
   g.nqv = t.nqv;
+  g.nl = t.nl;
+  g.simplex = t.simplex ? 1 : 0;
   g.MAA = T + t.oMAA;
   g.GAB = T + t.oGAB;
   g.GBA = T + t.oGBA;
@@ -373,7 +375,7 @@ AssembleArgs assemble_args(hdg_problem *pb) {
   AssembleArgs as{};
   as.nf = t.nf;
   as.nfd = t.nfd;
-  as.nl = 2 * t.D;
+  as.nl = pb->mesh.nl;
   as.nblockrows = pb->pat.nblockrows;
   as.ncells = pb->mesh.ncells;
   as.nblocks = pb->pat.nblocks;
@@ -409,8 +411,21 @@ void interpolate_dirichlet(const hdg_problem *pb, std::vector<double> &vals) {
         const int id = m.facet_dofs[(size_t)f * nfd + b];
         const int bb = b % g.nfd1, comp = bb / g.nT, node = bb - comp * g.nT;
         double xi[3], x[3];
-        for (int d = 0, j = 0; d < D; ++d)
-          xi[d] = (d == dn) ? double(side) : g.T.nodes[(size_t)node * (D - 1) + j++];
+        if (g.simplex) {
+          // the face opposite vertex D - lf of the reference simplex, through
+          // its vertices in increasing order
+          static const double V[4][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+          int fv[3], q = 0;
+          for (int v = 0; v <= D; ++v)
+            if (v != D - lf) fv[q++] = v;
+          for (int d = 0; d < D; ++d) {
+            xi[d] = V[fv[0]][d];
+            for (int j = 0; j + 1 < D; ++j) xi[d] += g.T.nodes[(size_t)node * (D - 1) + j] * (V[fv[j + 1]][d] - V[fv[0]][d]);
+          }
+        } else {
+          for (int d = 0, j = 0; d < D; ++d)
+            xi[d] = (d == dn) ? double(side) : g.T.nodes[(size_t)node * (D - 1) + j++];
+        }
         for (int d = 0; d < D; ++d) {
           x[d] = m.origin[(size_t)c * D + d];
           for (int e = 0; e < D; ++e) x[d] += m.jac[(size_t)c * D * D + e * D + d] * xi[e];
@@ -808,8 +823,8 @@ int hdg_problem_create_cartesian_physics(hdg_context *ctx, int D, const int *cel
   return HDG_OK;
 }
 
-int hdg_problem_create_cartesian_spaces(hdg_context *ctx, int D, const int *cells, const double *domain,
-                                        int physics, const int *spaces, int copies, hdg_problem **out) {
+static int create_spaces_problem(hdg_context *ctx, int D, const int *cells, const double *domain, int physics,
+                                 const int *spaces, int copies, bool simplex, hdg_problem **out) {
   if (!ctx) return HDG_ERR_INVALID;
   if (!cells || !domain || !spaces || !out) return ctx->fail(HDG_ERR_INVALID, "null argument");
   if (physics != HDG_PHYSICS_DARCY && physics != HDG_PHYSICS_ELASTICITY)
@@ -823,19 +838,21 @@ int hdg_problem_create_cartesian_spaces(hdg_context *ctx, int D, const int *cell
   pb->gs = true;
   for (DBuf *b : pb->device_buffers()) b->stream = ctx->stream;
   std::string err;
-  int rc = build_gs_tables(D, physics, spaces, copies, pb->gst, err);
+  int rc = build_gs_tables(D, physics, spaces, copies, pb->gst, err, simplex);
   if (!rc) {
     const GsTables &g = pb->gst;
     if (g.n * (g.n + 1) * sizeof(double) > ctx->smem_optin - 1024) {
       err = "the cell block exceeds the shared-memory condensation kernel";
       rc = HDG_ERR_INVALID;
-    } else if (!assemble_supports(2 * D, g.nfd)) {
+    } else if (!assemble_supports(g.nl, g.nfd)) {
       err = "no skeleton assembly kernel for this many DOFs per facet";
       rc = HDG_ERR_INVALID;
     }
   }
   // the mesh's facet space: every copy's trace DOFs on every facet
-  if (!rc) rc = build_cartesian_mesh(D, cells, domain, std::max(1, spaces[5]), pb->mesh, err, 1, pb->gst.nfd);
+  if (!rc)
+    rc = simplex ? build_simplex_mesh(D, cells, domain, pb->gst.nfd, pb->mesh, err)
+                 : build_cartesian_mesh(D, cells, domain, std::max(1, spaces[5]), pb->mesh, err, 1, pb->gst.nfd);
   if (rc) {
     delete pb;
     return ctx->fail(rc, "%s", err.c_str());
@@ -857,6 +874,16 @@ int hdg_problem_create_cartesian_spaces(hdg_context *ctx, int D, const int *cell
   }
   *out = pb;
   return HDG_OK;
+}
+
+int hdg_problem_create_cartesian_spaces(hdg_context *ctx, int D, const int *cells, const double *domain,
+                                        int physics, const int *spaces, int copies, hdg_problem **out) {
+  return create_spaces_problem(ctx, D, cells, domain, physics, spaces, copies, false, out);
+}
+
+int hdg_problem_create_simplex_spaces(hdg_context *ctx, int D, const int *cells, const double *domain, int physics,
+                                      const int *spaces, int copies, hdg_problem **out) {
+  return create_spaces_problem(ctx, D, cells, domain, physics, spaces, copies, true, out);
 }
 
 int hdg_problem_create(hdg_context *ctx, int D, int k, int ncells, int nfacets,
@@ -1038,7 +1065,7 @@ static int assemble_prepare(hdg_problem *pb, int precision, bool cell_blocks, bo
                                                                  : 0;
   if (need > ctx->smem_optin - 1024)
     return ctx->fail(HDG_ERR_INVALID, "cell block %zu exceeds the shared-memory condensation kernel", n);
-  const int nl = 2 * t.D;
+  const int nl = pb->mesh.nl;
   if (mixed && !cellop_supported(nl, (int)t.nfd))
     return ctx->fail(HDG_ERR_INVALID, "no unassembled FP32 operator for %d facets of %zu DOFs", nl, t.nfd);
   if (precision == HDG_PREC_FF_BLOCK && cell_blocks && !eblock)
@@ -1105,7 +1132,7 @@ static cudaError_t assemble_skeleton(hdg_problem *pb) {
   da.sign = skeleton_sign(pb);
   e = launch_block_chol_inv(da, pb->d_W.as<double>(), ctx->stream, ctx->num_sms, &ctx->launches);
   if (e != cudaSuccess) return e;
-  return launch_pack_cell_blocks(pb->mesh.ncells, 2 * t.D, t.nfd, skeleton_sign(pb), pb->d_S.as<double>(),
+  return launch_pack_cell_blocks(pb->mesh.ncells, pb->mesh.nl, t.nfd, skeleton_sign(pb), pb->d_S.as<double>(),
                                  pb->d_cell_blk.as<int>(), pb->d_W.as<double>(), pb->d_cellop.as<float>(),
                                  ctx->smem_optin, ctx->stream, ctx->num_sms, &ctx->launches);
 }
@@ -1255,7 +1282,7 @@ static Pcg32Args pcg32_args(hdg_problem *pb) {
   ia.counter = pb->d_counter.as<unsigned int>();
   ia.nparts = pcg_grid(pb);
   ia.ncells = pb->mesh.ncells;
-  ia.nl = 2 * pb->mesh.D;
+  ia.nl = pb->mesh.nl;
   ia.rec = cellop_rec(ia.nl, ia.nfd);
   ia.blocks = pb->d_cellop.as<float>();
   ia.cell_blk = pb->d_cell_blk.as<int>();
@@ -1344,7 +1371,7 @@ static int solve_pcg_refined(hdg_problem *pb, double rtol, int maxit, int *it_ou
   hdg_context *ctx = pb->ctx;
   const size_t n = pb->mesh.nfree, nfd = pb->mesh.nfd, nbr = pb->pat.nblockrows;
   if (!pb->d_cellop.ptr) return ctx->fail(HDG_ERR_STATE, "the FP32 cell operator is missing (assemble in a fast precision)");
-  const int nl = 2 * pb->mesh.D;
+  const int nl = pb->mesh.nl;
   CUDA_TRY(ctx, cellop_configure(nl, (int)nfd, ctx->smem_optin, ctx->num_sms, &pb->cellop_nstage, &pb->cellop_ctas));
   {  // at least two stages of cells per CTA on small problems
     const int cps = cellop_cps(nl * (int)nfd);
@@ -1739,6 +1766,7 @@ int hdg_newton_solve(hdg_problem *pb, int solver, double lin_rtol, int lin_maxit
   if (!pb) return HDG_ERR_INVALID;
   hdg_context *ctx = pb->ctx;
   if (!pb->form_set) return ctx->fail(HDG_ERR_STATE, "set the weak form first (hdg_set_darcy)");
+  if (pb->mesh.simplex) return ctx->fail(HDG_ERR_INVALID, "the Newton path takes box cells");
   if (!(ftol > 0.0) || max_iters < 0) return ctx->fail(HDG_ERR_INVALID, "ftol must be > 0 and max_iters >= 0");
   cudaSetDevice(ctx->device);
   int rc = assemble_prepare(pb, HDG_PREC_FP64, true, false);

@@ -2,6 +2,7 @@
 // tables, Cartesian meshes in Gridap numbering, the skeleton CSR pattern and
 // the block maps of the deterministic assembly gather.  Runs once per problem.
 #include <algorithm>
+#include <unordered_map>
 #include <cmath>
 #include <cstring>
 
@@ -417,6 +418,7 @@ int build_cartesian_mesh(int D, const int *cells, const double *domain, int k,
     m.domain[2 * d + 1] = domain[2 * d + 1];
   }
   const int nl = 2 * D;
+  m.nl = nl;
   int stride[kMaxD];
   stride[0] = 1;
   for (int d = 1; d < D; ++d) stride[d] = stride[d - 1] * cells[d - 1];
@@ -459,8 +461,131 @@ int build_cartesian_mesh(int D, const int *cells, const double *domain, int k,
   return finish_mesh(m, err);
 }
 
+// simplexify(CartesianDiscreteModel(domain, cells)): each box (x fastest) is
+// split into D! simplices, one per order (lexicographic over the axis
+// permutations) in which the path from the box's lowest vertex to its highest
+// steps along the axes (Kuhn's triangulation, conforming across boxes).  A
+// cell lists its vertices in increasing global order (lattice points, x
+// fastest); local facet lf is the face opposite local vertex D - lf; facets
+// are numbered in first-met order over (cell, local facet), the first cell is
+// the facet's owner, and the facets' DOFs are numbered facet by facet, the
+// boundary facets' DOFs Dirichlet.  Cell maps x = x_0 + J xi with column j of
+// J the edge from vertex 0 to vertex j+1.
+int build_simplex_mesh(int D, const int *cells, const double *domain, int nfd, HostMesh &m, std::string &err) {
+  if (D < 2 || D > 3) {
+    err = "D must be 2 or 3";
+    return HDG_ERR_INVALID;
+  }
+  long long nbox = 1, nvert = 1;
+  int nv[kMaxD];
+  for (int d = 0; d < D; ++d) {
+    if (cells[d] < 1) {
+      err = "cells must be >= 1";
+      return HDG_ERR_INVALID;
+    }
+    nbox *= cells[d];
+    nv[d] = cells[d] + 1;
+    nvert *= nv[d];
+  }
+  const int nperm = D == 2 ? 2 : 6;
+  if (nbox * nperm > (1LL << 30) || nvert >= (1LL << 21)) {
+    err = "mesh too large";
+    return HDG_ERR_INVALID;
+  }
+  m = HostMesh();
+  m.D = D;
+  m.k = 1;
+  m.nl = D + 1;
+  m.simplex = true;
+  m.cartesian = false;
+  m.nfd = nfd;
+  m.ncells = (int)(nbox * nperm);
+  for (int d = 0; d < D; ++d) {
+    m.cells[d] = cells[d];
+    m.domain[2 * d] = domain[2 * d];
+    m.domain[2 * d + 1] = domain[2 * d + 1];
+  }
+  static const int perms3[6][3] = {{0, 1, 2}, {0, 2, 1}, {1, 0, 2}, {1, 2, 0}, {2, 0, 1}, {2, 1, 0}};
+  static const int perms2[2][3] = {{0, 1, 0}, {1, 0, 0}};
+  const int nl = m.nl;
+  m.origin.resize((size_t)m.ncells * D);
+  m.jac.resize((size_t)m.ncells * D * D);
+  m.cell_facets.resize((size_t)m.ncells * nl);
+  std::unordered_map<unsigned long long, int> fid;
+  fid.reserve((size_t)m.ncells * 3);
+  std::vector<char> boundary;
+  std::vector<int> first_cell;
+  auto vid = [&](const int *idx) {
+    long long r = 0, mul = 1;
+    for (int d = 0; d < D; ++d) {
+      r += idx[d] * mul;
+      mul *= nv[d];
+    }
+    return (int)r;
+  };
+  auto coord = [&](int v, int d) {
+    int r = v;
+    for (int e = 0; e < d; ++e) r /= nv[e];
+    const int i = r % nv[d];
+    return domain[2 * d] + i * (domain[2 * d + 1] - domain[2 * d]) / cells[d];
+  };
+  int c = 0;
+  for (long long b = 0; b < nbox; ++b) {
+    int box[kMaxD];
+    long long r = b;
+    for (int d = 0; d < D; ++d) {
+      box[d] = (int)(r % cells[d]);
+      r /= cells[d];
+    }
+    for (int pi = 0; pi < nperm; ++pi, ++c) {
+      const int *perm = D == 2 ? perms2[pi] : perms3[pi];
+      int cur[kMaxD], verts[kMaxD + 1];
+      for (int d = 0; d < D; ++d) cur[d] = box[d];
+      verts[0] = vid(cur);
+      for (int j = 0; j < D; ++j) {
+        ++cur[perm[j]];
+        verts[j + 1] = vid(cur);
+      }
+      std::sort(verts, verts + D + 1);
+      for (int d = 0; d < D; ++d) {
+        m.origin[(size_t)c * D + d] = coord(verts[0], d);
+        for (int j = 0; j < D; ++j)
+          m.jac[(size_t)c * D * D + j * D + d] = coord(verts[j + 1], d) - coord(verts[0], d);
+      }
+      for (int lf = 0; lf < nl; ++lf) {
+        const int opp = D - lf;
+        unsigned long long key = 0;
+        for (int j = 0, sh = 0; j <= D; ++j)
+          if (j != opp) {
+            key |= (unsigned long long)verts[j] << sh;
+            sh += 21;
+          }
+        auto it = fid.find(key);
+        int f;
+        if (it == fid.end()) {
+          f = (int)first_cell.size();
+          fid.emplace(key, f);
+          first_cell.push_back(c);
+          boundary.push_back(1);
+        } else {
+          f = it->second;
+          boundary[f] = 0;  // a second cell: interior
+        }
+        m.cell_facets[(size_t)c * nl + lf] = f;
+      }
+    }
+  }
+  m.nfacets = (int)first_cell.size();
+  m.facet_dofs.resize((size_t)m.nfacets * m.nfd);
+  int fr = 0, di = 0;
+  for (int f = 0; f < m.nfacets; ++f)
+    for (int a = 0; a < m.nfd; ++a) m.facet_dofs[(size_t)f * m.nfd + a] = boundary[f] ? -1 - (di++) : fr++;
+  return finish_mesh(m, err);
+}
+
 int finish_mesh(HostMesh &m, std::string &err) {
-  const int nl = 2 * m.D, nfd = m.nfd;
+  if (m.nl == 0) m.nl = 2 * m.D;
+  const int nl = m.nl, nfd = m.nfd;
   m.facet_cell.assign((size_t)m.nfacets * 2, -1);
   m.facet_lface.assign((size_t)m.nfacets * 2, -1);
   for (int c = 0; c < m.ncells; ++c)
@@ -518,7 +643,7 @@ int finish_mesh(HostMesh &m, std::string &err) {
 // otherwise), in increasing cell order.
 // ---------------------------------------------------------------------------
 int build_pattern(const HostMesh &m, HostPattern &p, std::string &err) {
-  const int nl = 2 * m.D, nfd = m.nfd;
+  const int nl = m.nl, nfd = m.nfd;
   p = HostPattern();
   p.nrows = m.nfree;
   std::vector<int> free_facets;

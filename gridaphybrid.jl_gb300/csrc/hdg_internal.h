@@ -204,6 +204,8 @@ struct ScalarBasis {
 // the trace DOFs of copy 0, copy 1, ..].
 struct GsTables {
   int D = 0, phys = 0, pm = 0, copies = 1;
+  bool simplex = false;  // cells are simplices (D + 1 facets): the reference simplex's tables and rules
+  int nl = 0;            // facets per cell
   int spaces[7] = {0, 0, 0, 0, 0, 0, 0};
   ScalarBasis A[kMaxD > 6 ? kMaxD : 6], B, T;  // A: one basis per component
   int ncA = 0, ncB = 0, ncT = 0, nA = 0, nB = 0, nT = 0, ni = 0, nf = 0, nfd = 0, n = 0, n1 = 0, nqv = 0;
@@ -212,7 +214,8 @@ struct GsTables {
   int oMAA = 0, oGAB = 0, oGBA = 0, oFBA = 0, oFBB = 0, oHA = 0, oHB = 0, oL = 0, oqxi = 0, oqw = 0, oqphiA = 0,
       oqphiB = 0;
 };
-int build_gs_tables(int D, int phys, const int *spaces, int copies, GsTables &t, std::string &err);
+int build_gs_tables(int D, int phys, const int *spaces, int copies, GsTables &t, std::string &err,
+                    bool simplex = false);
 
 // Offsets (in doubles) of each table inside the packed device table buffer.
 struct TableOffsets {
@@ -231,13 +234,15 @@ TableOffsetsF pack_tables_ff(const RefTables &t, std::vector<float> &packed);
 // ---------------------------------------------------------------------------
 struct HostMesh {
   int D = 0, k = 0, ncells = 0, nfacets = 0, nfd = 0, nfree = 0, ndir = 0;
+  int nl = 0;            // facets per cell: 2 D (boxes) or D + 1 (simplices)
+  bool simplex = false;
   bool cartesian = false;
   int cells[kMaxD] = {0, 0, 0};
   double domain[2 * kMaxD] = {0, 0, 0, 0, 0, 0};
   std::vector<double> origin;     // ncells x D
   std::vector<double> jac;        // ncells x D x D (column-major per cell)
   bool axis = false;              // every jac is diagonal
-  std::vector<int> cell_facets;   // ncells x 2D
+  std::vector<int> cell_facets;   // ncells x nl
   std::vector<int> facet_dofs;    // nfacets x nfd
   std::vector<int> facet_cell;    // nfacets x 2 : cells around (first = owner), -1
   std::vector<int> facet_lface;   // nfacets x 2 : local facet index in that cell
@@ -248,6 +253,9 @@ struct HostMesh {
 int build_cartesian_mesh(int D, const int *cells, const double *domain, int k,
                          HostMesh &m, std::string &err, int ncomp = 1, int nfd = 0);
 int finish_mesh(HostMesh &m, std::string &err);  // derives facet_cell etc.
+// simplexify of the Cartesian mesh: every box split into D! simplices around
+// its diagonal from the lowest to the highest vertex (Kuhn), nfd DOFs per facet
+int build_simplex_mesh(int D, const int *cells, const double *domain, int nfd, HostMesh &m, std::string &err);
 
 // Skeleton CSR pattern and the block maps used by the deterministic gather.
 struct HostPattern {

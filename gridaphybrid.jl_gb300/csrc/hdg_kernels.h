@@ -166,6 +166,7 @@ cudaError_t launch_integrate_fp64(const CellArgs &a, double *A, double *b,
 struct GsArgs {
   CellArgs cell;
   int phys, nA, nB, nT, ncA, ncB, copies, ni1, nfd1, ni, nf, nfd, n, nqv;
+  int nl, simplex;  // facets per cell; simplex cells (cell_factors_simplex)
   const double *MAA, *GAB, *GBA, *FBA, *FBB, *HA, *HB, *L, *qphiA, *qphiB;
 };
 cudaError_t launch_integrate_gs(const GsArgs &g, double *A, double *b, cudaStream_t s, int num_sms,

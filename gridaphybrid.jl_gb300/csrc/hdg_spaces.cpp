@@ -220,7 +220,46 @@ static void facet_point(int D, int lf, const double *sp, double *xi) {
   for (int d = 0, j = 0; d < D; ++d) xi[d] = (d == dn) ? double(side) : sp[j++];
 }
 
-int build_gs_tables(int D, int phys, const int *spaces, int copies, GsTables &t, std::string &err) {
+// Reference simplex: vertices v_0 = 0, v_j = e_{j-1}; local facet lf is the
+// face opposite vertex D - lf, parametrised over the unit (D-1)-simplex by its
+// vertices in increasing order.
+static void simplex_facet_point(int D, int lf, const double *sp, double *xi) {
+  static const double V[4][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  int fv[kMaxD], k = 0;
+  for (int v = 0; v <= D; ++v)
+    if (v != D - lf) fv[k++] = v;
+  for (int d = 0; d < D; ++d) {
+    xi[d] = V[fv[0]][d];
+    for (int j = 0; j + 1 < D; ++j) xi[d] += sp[j] * (V[fv[j + 1]][d] - V[fv[0]][d]);
+  }
+}
+
+// Collapsed (Duffy) Gauss rule on the unit d-simplex from n1 Gauss points per
+// direction: xi_1 = u_1, xi_2 = u_2 (1 - u_1), xi_3 = u_3 (1 - u_1)(1 - u_2);
+// exact for degree 2 n1 - d (the collapse adds d - 1 to the degree in u_1).
+static void simplex_rule(int d, int n1, const std::vector<double> &x1, const std::vector<double> &w1,
+                         std::vector<double> &xi, std::vector<double> &w) {
+  const int nq = d == 0 ? 1 : ipow_i(n1, d);
+  xi.assign((size_t)nq * (d > 0 ? d : 1), 0.0);
+  w.assign(nq, 0.0);
+  for (int q = 0; q < nq; ++q) {
+    double u[kMaxD] = {0, 0, 0}, wt = 1.0, scale = 1.0;
+    for (int j = 0, r = q; j < d; ++j, r /= n1) {
+      u[j] = x1[r % n1];
+      wt *= w1[r % n1];
+    }
+    for (int j = 0; j < d; ++j) {
+      xi[(size_t)q * d + j] = u[j] * scale;
+      if (j + 1 < d) {
+        wt *= std::pow(1.0 - u[j], d - 1 - j);
+        scale *= 1.0 - u[j];
+      }
+    }
+    w[q] = wt;
+  }
+}
+
+int build_gs_tables(int D, int phys, const int *spaces, int copies, GsTables &t, std::string &err, bool simplex) {
   t = GsTables();
   if (D < 2 || D > kMaxD) {
     err = "D must be 2 or 3";
@@ -259,9 +298,16 @@ int build_gs_tables(int D, int phys, const int *spaces, int copies, GsTables &t,
     err = "unsupported space (kind Q or P of order 0..4; RT_k, k = 0..3, for the Darcy flux)";
     return HDG_ERR_INVALID;
   }
+  if (simplex && (phys != HDG_PHYSICS_DARCY || spaces[0] != kBasisP || spaces[2] != kBasisP ||
+                  spaces[4] != kBasisP || spaces[6] != 0)) {
+    err = "simplex cells take the Darcy form with P_k fields";
+    return HDG_ERR_INVALID;
+  }
   t.D = D;
   t.phys = phys;
   t.copies = copies;
+  t.simplex = simplex;
+  t.nl = simplex ? D + 1 : 2 * D;
   t.pm = spaces[6] != 0 && phys == HDG_PHYSICS_ELASTICITY;
   t.nA = t.A[0].nb;
   t.nB = t.B.nb;
@@ -270,16 +316,40 @@ int build_gs_tables(int D, int phys, const int *spaces, int copies, GsTables &t,
   t.nfd1 = t.ncT * t.nT;
   t.ni = copies * t.ni1;
   t.nfd = copies * t.nfd1;
-  t.nf = 2 * D * t.nfd;
+  t.nf = t.nl * t.nfd;
   t.n = t.ni + t.nf;
   int kmax = std::max(spaces[3], spaces[5]);
   for (int c = 0; c < t.ncA; ++c) kmax = std::max(kmax, t.A[c].k);
-  t.n1 = kmax + 2;  // Gauss points per direction: exact for degree 2 kmax + 3
-  t.nqv = ipow_i(t.n1, D);
-  const int nqf = ipow_i(t.n1, D - 1), nl = 2 * D, ncA = t.ncA;
+  t.n1 = kmax + 2;  // Gauss points per direction: exact for degree 2 kmax + 3 (box), 2 kmax + 4 - D (simplex)
+  const int nl = t.nl, ncA = t.ncA;
   const int nA = t.nA, nB = t.nB, nT = t.nT;
   std::vector<double> x1, w1;
   gauss01(t.n1, x1, w1);
+  // volume and facet rules: tensor Gauss on the unit box / cube, or the
+  // collapsed rules on the unit simplices
+  std::vector<double> vxi, vw, fs, fw;
+  if (simplex) {
+    simplex_rule(D, t.n1, x1, w1, vxi, vw);
+    simplex_rule(D - 1, t.n1, x1, w1, fs, fw);
+  } else {
+    const int nv = ipow_i(t.n1, D), nfq = ipow_i(t.n1, D - 1);
+    vxi.assign((size_t)nv * D, 0.0);
+    vw.assign(nv, 1.0);
+    for (int q = 0; q < nv; ++q)
+      for (int d = 0, r = q; d < D; ++d, r /= t.n1) {
+        vxi[(size_t)q * D + d] = x1[r % t.n1];
+        vw[q] *= w1[r % t.n1];
+      }
+    fs.assign((size_t)nfq * (D - 1), 0.0);
+    fw.assign(nfq, 1.0);
+    for (int q = 0; q < nfq; ++q)
+      for (int d = 0, r = q; d < D - 1; ++d, r /= t.n1) {
+        fs[(size_t)q * (D - 1) + d] = x1[r % t.n1];
+        fw[q] *= w1[r % t.n1];
+      }
+  }
+  t.nqv = (int)vw.size();
+  const int nqf = (int)fw.size();
   size_t o = 0;
   auto take = [&](int &off, size_t count) {
     off = (int)o;
@@ -302,11 +372,9 @@ int build_gs_tables(int D, int phys, const int *spaces, int copies, GsTables &t,
   std::vector<double> pA(nA), dA((size_t)nA * D), pB(nB), dB((size_t)nB * D), mu(nT);
   // volume
   for (int q = 0; q < t.nqv; ++q) {
-    double xi[kMaxD], wq = 1.0;
-    for (int d = 0, r = q; d < D; ++d, r /= t.n1) {
-      xi[d] = x1[r % t.n1];
-      wq *= w1[r % t.n1];
-    }
+    double xi[kMaxD];
+    for (int d = 0; d < D; ++d) xi[d] = vxi[(size_t)q * D + d];
+    const double wq = vw[q];
     t.B.eval(xi, pB.data(), dB.data());
     for (int d = 0; d < D; ++d) P[t.oqxi + q * D + d] = xi[d];
     P[t.oqw + q] = wq;
@@ -324,19 +392,20 @@ int build_gs_tables(int D, int phys, const int *spaces, int copies, GsTables &t,
       }
     }
   }
-  // facets (unit facet measure)
+  // facets, over the facet's parameter domain (unit box or unit simplex)
   for (int q = 0; q < nqf; ++q) {
-    double sp[kMaxD] = {0, 0, 0}, wq = 1.0;
-    for (int d = 0, r = q; d < D - 1; ++d, r /= t.n1) {
-      sp[d] = x1[r % t.n1];
-      wq *= w1[r % t.n1];
-    }
+    double sp[kMaxD] = {0, 0, 0};
+    for (int d = 0; d < D - 1; ++d) sp[d] = fs[(size_t)q * (D - 1) + d];
+    const double wq = fw[q];
     t.T.eval(sp, mu.data(), nullptr);
     for (int m = 0; m < nT; ++m)
       for (int m2 = 0; m2 < nT; ++m2) P[t.oL + (size_t)m * nT + m2] += wq * mu[m] * mu[m2];
     for (int lf = 0; lf < nl; ++lf) {
       double xi[kMaxD];
-      facet_point(D, lf, sp, xi);
+      if (simplex)
+        simplex_facet_point(D, lf, sp, xi);
+      else
+        facet_point(D, lf, sp, xi);
       t.B.eval(xi, pB.data(), nullptr);
       for (int b = 0; b < nB; ++b) {
         for (int b2 = 0; b2 < nB; ++b2) P[t.oFBB + ((size_t)lf * nB + b) * nB + b2] += wq * pB[b] * pB[b2];

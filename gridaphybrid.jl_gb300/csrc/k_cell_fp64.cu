@@ -188,7 +188,7 @@ __global__ void __launch_bounds__(128) recover_fp64_kernel(CellArgs a, const dou
                                                            double *uint) {
   __shared__ double xf[6 * 64];
   __shared__ double rhs[4 * 512];
-  const int ni = a.ni, nf = a.nf, n = a.n, nfd = a.nfd, nl = 2 * a.D;
+  const int ni = a.ni, nf = a.nf, n = a.n, nfd = a.nfd, nl = a.nf / a.nfd;  // facets per cell (box or simplex)
   for (int c = blockIdx.x; c < a.ncells; c += gridDim.x) {
     for (int e = threadIdx.x; e < nf; e += blockDim.x) {
       const int lf = e / nfd, j = e - lf * nfd;

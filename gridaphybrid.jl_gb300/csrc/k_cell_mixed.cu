@@ -600,7 +600,7 @@ __global__ void __launch_bounds__(128) recover_mixed_kernel(CellArgs a, const fl
                                                             const double *__restrict__ lambda,
                                                             const double *__restrict__ dirvals, double *uint) {
   __shared__ float xf[2][6 * 64];
-  const int ni = a.ni, nf = a.nf, nfd = a.nfd, nl = 2 * a.D, nc = nf + 1;
+  const int ni = a.ni, nf = a.nf, nfd = a.nfd, nl = a.nf / a.nfd, nc = nf + 1;
   for (int c = blockIdx.x; c < a.ncells; c += gridDim.x) {
     for (int e = threadIdx.x; e < nf; e += blockDim.x) {
       const int lf = e / nfd, j = e - lf * nfd;

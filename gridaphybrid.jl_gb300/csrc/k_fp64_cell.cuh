@@ -19,9 +19,12 @@ struct CellFactors {
   double x0[3], J[3][3];       // affine map x = x0 + J xi
 };
 
-__device__ __forceinline__ void cell_factors(const CellArgs &a, int c, CellFactors &f) {
+// The affine map of cell c (x = x0 + J xi, J column-major in a.jac) and its
+// inverse Ji; returns det J.
+__device__ __forceinline__ double cell_affine(const CellArgs &a, int c, double J[3][3], double Ji[3][3]) {
   const int D = a.D;
-  double J[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, Ji[3][3];
+  for (int r = 0; r < 3; ++r)
+    for (int q = 0; q < 3; ++q) J[r][q] = 0.0;
   for (int col = 0; col < D; ++col)
     for (int row = 0; row < D; ++row) J[row][col] = a.jac[(size_t)c * D * D + col * D + row];
   double det;
@@ -46,7 +49,14 @@ __device__ __forceinline__ void cell_factors(const CellArgs &a, int c, CellFacto
     Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / det;
     Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
   }
-  const double adet = fabs(det);
+  return det;
+}
+
+// The volume factors shared by box and simplex cells.
+__device__ __forceinline__ double cell_volume_factors(const CellArgs &a, int c, CellFactors &f, double Ji[3][3]) {
+  const int D = a.D;
+  double J[3][3];
+  const double adet = fabs(cell_affine(a, c, J, Ji));
   const double kap = a.kappa ? a.kappa[c] : 1.0;
   f.detJ = adet;
   f.cm = adet / kap;
@@ -56,23 +66,64 @@ __device__ __forceinline__ void cell_factors(const CellArgs &a, int c, CellFacto
     f.x0[d] = a.origin[(size_t)c * D + d];
     for (int e = 0; e < D; ++e) f.J[d][e] = J[d][e];
   }
+  return adet;
+}
+
+// Facet factors from the reference normal nh of local facet lf (outward on
+// the reference cell) and the ratio of the reference face's measure to its
+// parameter domain's: n = J^{-T} nh / |J^{-T} nh|, the facet Jacobian |J_F| =
+// |det J| |J^{-T} nh| ratio (Nanson), and tau (n . n_owner) |J_F|.
+__device__ __forceinline__ void facet_factors(const CellArgs &a, int c, int nl, int lf, const double *nh,
+                                              double ratio, double adet, const double Ji[3][3], CellFactors &f) {
+  const int D = a.D;
+  double v[3], nv = 0.0;
+  for (int d = 0; d < D; ++d) {
+    v[d] = 0.0;
+    for (int e = 0; e < D; ++e) v[d] += Ji[e][d] * nh[e];  // J^{-T} n_ref
+    nv += v[d] * v[d];
+  }
+  nv = sqrt(nv);
+  const double area = adet * nv * ratio;
+  for (int d = 0; d < D; ++d) f.cn[lf][d] = area * (v[d] / nv);
+  double s = 1.0;
+  if (a.stab_mode == 1) {
+    const int fct = a.cell_facets[(size_t)c * nl + lf];
+    s = (a.facet_cell[2 * (size_t)fct] == c) ? 1.0 : -1.0;  // n . n_owner
+  }
+  f.ct[lf] = a.tau * s * area;
+}
+
+// Box cells: local facet lf has the reference normal +-e_dn, dn = D-1-lf/2
+// (Gridap's face numbering), and a unit parameter square.
+__device__ __forceinline__ void cell_factors(const CellArgs &a, int c, CellFactors &f) {
+  const int D = a.D;
+  double Ji[3][3];
+  const double adet = cell_volume_factors(a, c, f, Ji);
   for (int lf = 0; lf < 2 * D; ++lf) {
-    const int dn = D - 1 - lf / 2;
-    const double sg = (lf % 2) ? 1.0 : -1.0;
-    double v[3], nv = 0.0;
-    for (int d = 0; d < D; ++d) {
-      v[d] = sg * Ji[dn][d];  // J^{-T} n_ref
-      nv += v[d] * v[d];
+    double nh[3] = {0.0, 0.0, 0.0};
+    nh[D - 1 - lf / 2] = (lf % 2) ? 1.0 : -1.0;
+    facet_factors(a, c, 2 * D, lf, nh, 1.0, adet, Ji, f);
+  }
+}
+
+// Simplex cells (vertices v_0 = 0, v_j = e_{j-1} on the reference cell):
+// local facet lf is the face opposite vertex D - lf, with reference normal
+// (1, .., 1)/sqrt(D) opposite v_0 and -e_{m-1} opposite v_m, parametrised over
+// the unit (D-1)-simplex (measure ratio sqrt(D) opposite v_0, 1 otherwise).
+__device__ __forceinline__ void cell_factors_simplex(const CellArgs &a, int c, CellFactors &f) {
+  const int D = a.D;
+  double Ji[3][3];
+  const double adet = cell_volume_factors(a, c, f, Ji);
+  for (int lf = 0; lf <= D; ++lf) {
+    const int opp = D - lf;
+    double nh[3] = {0.0, 0.0, 0.0}, ratio = 1.0;
+    if (opp == 0) {
+      for (int d = 0; d < D; ++d) nh[d] = 1.0 / sqrt((double)D);
+      ratio = sqrt((double)D);
+    } else {
+      nh[opp - 1] = -1.0;
     }
-    nv = sqrt(nv);
-    const double area = adet * nv;  // Nanson: |J_F| = |det J| |J^{-T} n_ref|
-    for (int d = 0; d < D; ++d) f.cn[lf][d] = area * (v[d] / nv);
-    double s = 1.0;
-    if (a.stab_mode == 1) {
-      const int fct = a.cell_facets[(size_t)c * 2 * D + lf];
-      s = (a.facet_cell[2 * (size_t)fct] == c) ? 1.0 : -1.0;  // n . n_owner
-    }
-    f.ct[lf] = a.tau * s * area;
+    facet_factors(a, c, D + 1, lf, nh, ratio, adet, Ji, f);
   }
 }
 

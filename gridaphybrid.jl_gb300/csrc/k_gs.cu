@@ -11,7 +11,10 @@
 //
 // On an affine cell every entry is a short sum of reference tables (contracted
 // once on the host) times the cell's factors: one CTA per cell, threads over
-// the n^2 entries.  The cell blocks then go through the same condensation,
+// the n^2 entries.  Box cells (2D facets) and, for the Darcy form with P_k
+// fields, simplex cells (D + 1 facets: simplexify of the Cartesian model,
+// test/DarcyHDGTests.jl:174-177) share the kernels; only the reference tables
+// and the facet factors differ.  The cell blocks then go through the same condensation,
 // assembly, skeleton solve and recovery as every other form.
 #include <cuda_runtime.h>
 
@@ -65,7 +68,7 @@ __device__ __forceinline__ GsDof gs_decode(const GsArgs &g, int i) {
 // test/DarcyRTHTests.jl:60-62 (-grad(q).u + q (u.n) = q div u on each cell).
 __device__ __forceinline__ double gs_darcy_entry(const GsArgs &g, const CellFactors &f, const GsDof &r,
                                                  const GsDof &s) {
-  const int D = g.cell.D, nA = g.nA, nB = g.nB, nT = g.nT, nl = 2 * D;
+  const int D = g.cell.D, nA = g.nA, nB = g.nB, nT = g.nT, nl = g.nl;
   double v = 0.0;
   if (r.t == 0) {
     const int c = r.comp;
@@ -105,7 +108,7 @@ __device__ __forceinline__ double gs_darcy_entry(const GsArgs &g, const CellFact
 // table, and tau mu.P_m(u) = tau mu.u).  The stress components share one basis.
 __device__ __forceinline__ double gs_elast_entry(const GsArgs &g, const CellFactors &f, const ElastCellTerms &T,
                                                  const GsDof &r, const GsDof &s) {
-  const int D = g.cell.D, nA = g.nA, nB = g.nB, nT = g.nT, nl = 2 * D;
+  const int D = g.cell.D, nA = g.nA, nB = g.nB, nT = g.nT, nl = g.nl;
   if (r.t == 0) {
     if (s.t == 0) return T.cmj[r.comp][s.comp] * g.MAA[r.idx * nA + s.idx];
     if (s.t == 1) {
@@ -147,7 +150,12 @@ __global__ void __launch_bounds__(256) integrate_gs_kernel(GsArgs g, double *A, 
     if (elast) {
       elast_cell_prepare(a, c, S, fq, false, threadIdx.x, blockDim.x);  // fq: -w f per point (nqv x D)
     } else {
-      if (threadIdx.x == 0) cell_factors(a, c, S.f);
+      if (threadIdx.x == 0) {
+        if (g.simplex)
+          cell_factors_simplex(a, c, S.f);
+        else
+          cell_factors(a, c, S.f);
+      }
       __syncthreads();
       source_values(a, S.f, c, fq, threadIdx.x, blockDim.x);  // fq: w (f_u, g) per point (nqv x (D+1))
       __syncthreads();
@@ -186,7 +194,12 @@ __global__ void __launch_bounds__(128) l2_errors_gs_kernel(GsArgs g, const doubl
   const int D = a.D, nA = g.nA, nB = g.nB, wA = g.ncA * nA, wB = g.ncB * nB;
   const bool elast = g.phys == HDG_PHYSICS_ELASTICITY;
   for (int c = blockIdx.x; c < a.ncells; c += gridDim.x) {
-    if (threadIdx.x == 0) cell_factors(a, c, f);
+    if (threadIdx.x == 0) {
+      if (g.simplex)
+        cell_factors_simplex(a, c, f);
+      else
+        cell_factors(a, c, f);
+    }
     __syncthreads();
     const double coef = a.kappa ? a.kappa[c] : (elast ? 0.3 : 1.0);
     double e1 = 0.0, e2 = 0.0;

@@ -681,6 +681,7 @@ cudaError_t launch_block_chol_inv(const PcgArgs &a, double *W, cudaStream_t s, i
     HDG_CHOL_CASE(6)
     HDG_CHOL_CASE(8)
     HDG_CHOL_CASE(9)
+    HDG_CHOL_CASE(10)
     HDG_CHOL_CASE(12)
     HDG_CHOL_CASE(16)
     HDG_CHOL_CASE(25)
@@ -712,7 +713,7 @@ static size_t cellop_dyn_smem(int nstage) {
 }
 
 #define HDG_CELLOP_CASES(X) \
-  X(4, 1) X(6, 1) X(4, 2) X(4, 3) X(4, 4) X(4, 5) X(4, 6) X(4, 8) X(6, 3) X(6, 4) X(6, 6) X(6, 9) X(6, 12) X(6, 16) X(6, 25) X(6, 27)
+  X(3, 1) X(3, 2) X(3, 3) X(3, 4) X(4, 10) X(4, 1) X(6, 1) X(4, 2) X(4, 3) X(4, 4) X(4, 5) X(4, 6) X(4, 8) X(6, 3) X(6, 4) X(6, 6) X(6, 9) X(6, 12) X(6, 16) X(6, 25) X(6, 27)
 
 bool cellop_supported(int nl, int nfd) {
 #define X(L, F) \
@@ -867,6 +868,7 @@ cudaError_t launch_outer_update(const OuterArgs &a, const float *e, cudaStream_t
     case 6: outer_residual_kernel<6><<<a.nparts, kPcgThreads, 0, s>>>(a); break;
     case 8: outer_residual_kernel<8><<<a.nparts, kPcgThreads, 0, s>>>(a); break;
     case 9: outer_residual_kernel<9><<<a.nparts, kPcgThreads, 0, s>>>(a); break;
+    case 10: outer_residual_kernel<10><<<a.nparts, kPcgThreads, 0, s>>>(a); break;
     case 12: outer_residual_kernel<12><<<a.nparts, kPcgThreads, 0, s>>>(a); break;
     case 16: outer_residual_kernel<16><<<a.nparts, kPcgThreads, 0, s>>>(a); break;
     case 25: outer_residual_kernel<25><<<a.nparts, kPcgThreads, 0, s>>>(a); break;

@@ -287,7 +287,7 @@ static int persistent_grid(size_t smem_optin, int num_sms, int want, int *nstage
 }
 
 #define HDG_PERSIST_CASES(X) \
-  X(4, 1) X(6, 1) X(4, 2) X(4, 3) X(4, 4) X(4, 5) X(4, 6) X(4, 8) X(6, 3) X(6, 4) X(6, 6) X(6, 9) X(6, 12) X(6, 16) X(6, 25) X(6, 27)
+  X(3, 1) X(3, 2) X(3, 3) X(3, 4) X(4, 10) X(4, 1) X(6, 1) X(4, 2) X(4, 3) X(4, 4) X(4, 5) X(4, 6) X(4, 8) X(6, 3) X(6, 4) X(6, 6) X(6, 9) X(6, 12) X(6, 16) X(6, 25) X(6, 27)
 
 int pcg32_persistent_config(int nl, int nfd, size_t smem_optin, int num_sms, int want, int *nstage, size_t *smem) {
 #define X(L, F) \

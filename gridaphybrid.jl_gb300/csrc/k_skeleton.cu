@@ -127,7 +127,8 @@ cudaError_t launch_assemble(const AssembleArgs &a, const double *S, const double
     }
     HDG_ASM(4, 2) HDG_ASM(4, 3) HDG_ASM(4, 4) HDG_ASM(4, 5) HDG_ASM(6, 1) HDG_ASM(6, 4) HDG_ASM(6, 9)
     HDG_ASM(6, 16) HDG_ASM(6, 25) HDG_ASM(4, 1) HDG_ASM(4, 6) HDG_ASM(4, 8) HDG_ASM(6, 12) HDG_ASM(6, 27)
-    HDG_ASM(6, 3) HDG_ASM(6, 6)
+    HDG_ASM(6, 3) HDG_ASM(6, 6) HDG_ASM(4, 10)
+    HDG_ASM(3, 1) HDG_ASM(3, 2) HDG_ASM(3, 3) HDG_ASM(3, 4) HDG_ASM(3, 5) HDG_ASM(3, 6) HDG_ASM(3, 8)
     else return cudaErrorInvalidValue;
 #undef HDG_ASM
     ++*launches;
@@ -489,6 +490,7 @@ static cudaError_t spmv_dispatch(const PcgArgs &a, const V *val, const double *p
     HDG_SPMV_CASE(6)
     HDG_SPMV_CASE(8)
     HDG_SPMV_CASE(9)
+    HDG_SPMV_CASE(10)
     HDG_SPMV_CASE(12)
     HDG_SPMV_CASE(16)
     HDG_SPMV_CASE(25)
@@ -505,7 +507,10 @@ static cudaError_t spmv_any(const PcgArgs &a, const double *po, double *pn, cuda
 }
 
 bool assemble_supports(int nl, int nfd) {
-  if (nl == 4) return nfd == 1 || nfd == 2 || nfd == 3 || nfd == 4 || nfd == 5 || nfd == 6 || nfd == 8;
+  // triangles (P_k traces and their copies), quads / tetrahedra, hexahedra
+  if (nl == 3) return nfd == 1 || nfd == 2 || nfd == 3 || nfd == 4 || nfd == 5 || nfd == 6 || nfd == 8;
+  if (nl == 4)
+    return nfd == 1 || nfd == 2 || nfd == 3 || nfd == 4 || nfd == 5 || nfd == 6 || nfd == 8 || nfd == 10;
   return nl == 6 && (nfd == 1 || nfd == 3 || nfd == 4 || nfd == 6 || nfd == 9 || nfd == 12 || nfd == 16 ||
                      nfd == 25 || nfd == 27);
 }
@@ -513,8 +518,8 @@ bool assemble_supports(int nl, int nfd) {
 bool pcg_supports_nfd(int nfd) {
   // scalar traces (k+1)^(D-1) (1: RT_0 / Q_0 multipliers); displacement traces D (k+1)^(D-1): 4, 6, 8
   // (2D), 12, 27 (3D k=1, 2)
-  return nfd == 1 || nfd == 2 || nfd == 3 || nfd == 4 || nfd == 5 || nfd == 6 || nfd == 8 || nfd == 9 || nfd == 12 ||
-         nfd == 16 || nfd == 25 || nfd == 27;
+  return nfd == 1 || nfd == 2 || nfd == 3 || nfd == 4 || nfd == 5 || nfd == 6 || nfd == 8 || nfd == 9 || nfd == 10 ||
+         nfd == 12 || nfd == 16 || nfd == 25 || nfd == 27;
 }
 
 cudaError_t launch_spmv(const PcgArgs &a, cudaStream_t s, long long *launches) {

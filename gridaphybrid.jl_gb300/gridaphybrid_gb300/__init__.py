@@ -13,7 +13,8 @@ from .operators import (CartesianDiscreteModel, DarcyHDG, ElasticityHDG, FEFunct
                         HybridAffineFEOperator, HybridFEOperator, MultiFieldFESpace,
                         NLSolver, ReferenceFE, Skeleton, TestFESpace, TrialFESpace,
                         Triangulation, darcy_spaces, elasticity_spaces, get_cell_normal_vector,
-                        get_cell_owner_normal_vector, lagrangian, raviart_thomas, solve, solve_)
+                        get_cell_owner_normal_vector, lagrangian, raviart_thomas, simplexify, solve,
+                        solve_)
 
 __all__ = [
     "ArrayBlock", "BackwardStaticCondensationMap", "CartesianDiscreteModel", "Context",
@@ -22,5 +23,5 @@ __all__ = [
     "ReferenceFE", "Scalar2ArrayBlockMap", "Skeleton", "StaticCondensationMap", "SumFacetsMap", "TestFESpace",
     "TrialFESpace", "Triangulation", "VectorBlock", "darcy_spaces", "default_context",
     "densify", "elasticity_spaces", "evaluate", "get_cell_normal_vector", "get_cell_owner_normal_vector",
-    "lagrangian", "lazy_map", "raviart_thomas", "return_cache", "solve", "solve_",
+    "lagrangian", "lazy_map", "raviart_thomas", "return_cache", "simplexify", "solve", "solve_",
 ]

@@ -85,6 +85,7 @@ SIGNATURES = {
     "hdg_problem_create": (_i, [_vp, _i, _i, _i, _i, _vp, _vp, _vp, _vp, ctypes.POINTER(_vp)]),
     "hdg_problem_create_cartesian_physics": (_i, [_vp, _i, _vp, _vp, _i, _i, ctypes.POINTER(_vp)]),
     "hdg_problem_create_cartesian_spaces": (_i, [_vp, _i, _vp, _vp, _i, _vp, _i, ctypes.POINTER(_vp)]),
+    "hdg_problem_create_simplex_spaces": (_i, [_vp, _i, _vp, _vp, _i, _vp, _i, ctypes.POINTER(_vp)]),
     "hdg_set_elasticity": (_i, [_vp, _d, _d, _i]),
     "hdg_problem_destroy": (_i, [_vp]),
     "hdg_problem_info": (_i, [_vp, _vp]),

@@ -58,6 +58,25 @@ class CartesianDiscreteModel:
         return np.broadcast_to(np.diag(h), (self.num_cells(), self.D, self.D))
 
 
+class SimplexifiedModel(CartesianDiscreteModel):
+    """simplexify(CartesianDiscreteModel(domain, partition)): every box split
+    into D! simplices around its diagonal from the lowest to the highest vertex
+    (2 triangles per square, 6 tetrahedra per cube), as the reference's
+    simplex test builds its mesh (test/DarcyHDGTests.jl:174-177)."""
+
+    simplex = True
+
+    def num_cells(self):
+        return int(np.prod(self.partition)) * (2 if self.D == 2 else 6)
+
+
+def simplexify(model):
+    return SimplexifiedModel(model.domain, model.partition)
+
+
+CartesianDiscreteModel.simplex = False
+
+
 class Triangulation:
     def __init__(self, model, dim=None):
         self.model = model
@@ -227,7 +246,11 @@ class _Problem:
         h = ctypes.c_void_p()
         cells = np.array(model.partition, dtype=np.int32)
         dom = np.array(model.domain, dtype=np.float64)
-        if spaces is None:
+        if model.simplex:
+            sp = np.ascontiguousarray(spaces, dtype=np.int32)
+            ctx.check(ctx.lib.hdg_problem_create_simplex_spaces(ctx.handle, model.D, _lib.ptr(cells), _lib.ptr(dom),
+                                                                physics, _lib.ptr(sp), copies, ctypes.byref(h)))
+        elif spaces is None:
             ctx.check(ctx.lib.hdg_problem_create_cartesian_physics(ctx.handle, model.D, _lib.ptr(cells),
                                                                    _lib.ptr(dom), k, physics, ctypes.byref(h)))
         else:
@@ -284,7 +307,8 @@ def _general_spaces(trial, bulk_fields, skeleton_fields, weakform):
         raise ValueError("the copies of a multi-field HDG space must use the same spaces")
     sp = per_copy[0]
     q = _lib.HDG_SPACE_Q
-    if c == 1 and not weakform.pm and sp[0::2] == (q, q, q) and len(set(sp[1::2])) == 1:
+    simplex = getattr(trial[0].trian.model, "simplex", False)
+    if not simplex and c == 1 and not weakform.pm and sp[0::2] == (q, q, q) and len(set(sp[1::2])) == 1:
         return None, 1
     return np.array(list(sp) + [1 if weakform.pm else 0], dtype=np.int32), c
 

@@ -226,6 +226,19 @@ int hdg_problem_create_cartesian_physics(hdg_context *ctx, int D, const int *cel
 #define HDG_SPACE_RT 2
 int hdg_problem_create_cartesian_spaces(hdg_context *ctx, int D, const int *cells, const double *domain,
                                         int physics, const int *spaces, int copies, hdg_problem **out);
+
+/* The same on simplexify(CartesianDiscreteModel(domain, cells))
+ * (test/DarcyHDGTests.jl:174-177): every box split into D! simplices around
+ * its diagonal from the lowest to the highest vertex (2 triangles per square,
+ * 6 tetrahedra per cube; boxes x fastest, then the axis orders of the path
+ * lexicographically); a cell lists its vertices in increasing global order
+ * (lattice points, x fastest), local facet lf is the face opposite local
+ * vertex D - lf, facets are numbered in first-met order over (cell, local
+ * facet) and the first cell of a facet is its owner.  The Darcy form
+ * (physics HDG_PHYSICS_DARCY) with P_k fields only (HDG_SPACE_P, pm = 0);
+ * everything else as hdg_problem_create_cartesian_spaces. */
+int hdg_problem_create_simplex_spaces(hdg_context *ctx, int D, const int *cells, const double *domain,
+                                      int physics, const int *spaces, int copies, hdg_problem **out);
 int hdg_problem_destroy(hdg_problem *pb);
 
 /* info[0..7] = ncells, nfacets, ni, nf, nfree, ndirichlet, nnz, nfacet_dofs */
