@@ -409,11 +409,13 @@ space [U_1..U_c, P_1..P_c, L_1..L_c] with bulk fields 1:2c and skeleton fields
 2c+1:3c, the block form repeated per copy
 (test/MultiFieldLagrangeMultipliersTests.jl:40-88); the free DOF values come
 back in that multi-field order.  Condensation in FP64 or FP32 with float-float
-refinement (`HDG_PREC_FF_BLOCK` needs equal-order Q_k fields).
+refinement (`HDG_PREC_FF_BLOCK` needs equal-order Q_k fields).  With
+`simplexified = true` the model is simplexified first (2 triangles per square,
+6 tetrahedra per cube) and the fields must be `:P`.
 """
 function HybridAffineFEOperator(form::DarcyHDGForm, model::CartesianDiscreteModel, spaces::Tuple;
                                 copies::Integer=1, precision=HDG_PREC_FP64, ctx=default_context(),
-                                trial=nothing, test=nothing)
+                                trial=nothing, test=nothing, simplexified::Bool=false)
   desc = get_cartesian_descriptor(model)
   D = length(desc.partition)
   cells = Cint[desc.partition...]
@@ -424,9 +426,16 @@ function HybridAffineFEOperator(form::DarcyHDGForm, model::CartesianDiscreteMode
   sp = Cint[_SPACE_KIND[spaces[1]], spaces[2], _SPACE_KIND[spaces[3]], spaces[4], _SPACE_KIND[spaces[5]],
             spaces[6], 0]
   h = Ref{Ptr{Cvoid}}(C_NULL)
-  check(ctx, ccall((:hdg_problem_create_cartesian_spaces, LIB), Cint,
-                   (Ptr{Cvoid}, Cint, Ptr{Cint}, Ptr{Float64}, Cint, Ptr{Cint}, Cint, Ptr{Ptr{Cvoid}}),
-                   ctx.handle, D, cells, domain, HDG_PHYSICS_DARCY, sp, copies, h))
+  if simplexified
+    # simplexify(model) with the library's own split and numbering (test/DarcyHDGTests.jl:174-177)
+    check(ctx, ccall((:hdg_problem_create_simplex_spaces, LIB), Cint,
+                     (Ptr{Cvoid}, Cint, Ptr{Cint}, Ptr{Float64}, Cint, Ptr{Cint}, Cint, Ptr{Ptr{Cvoid}}),
+                     ctx.handle, D, cells, domain, HDG_PHYSICS_DARCY, sp, copies, h))
+  else
+    check(ctx, ccall((:hdg_problem_create_cartesian_spaces, LIB), Cint,
+                     (Ptr{Cvoid}, Cint, Ptr{Cint}, Ptr{Float64}, Cint, Ptr{Cint}, Cint, Ptr{Ptr{Cvoid}}),
+                     ctx.handle, D, cells, domain, HDG_PHYSICS_DARCY, sp, copies, h))
+  end
   info = Vector{Clonglong}(undef, 8)
   check(ctx, ccall((:hdg_problem_info, LIB), Cint, (Ptr{Cvoid}, Ptr{Clonglong}), h[], info))
   op = GPUHybridOperator(ctx, h[], trial, test, D, info[1], info[3], info[5], Cint(precision))
