@@ -339,6 +339,83 @@ def run_elasticity(args, ctx):
     return out
 
 
+def run_skewed(args, ctx):
+    """The headline workload on an affine mesh whose cells are not
+    axis-aligned: the 32^3 Cartesian topology with every cell mapped by one
+    global skew x -> B x (hdg_problem_create, Gridap-style arrays), so the
+    integration and the block elimination take their general-Jacobian paths
+    (every flux component couples to every facet).  Same form, kappa and
+    solver tolerance; the float-float path timed, and compared once with the
+    plain FP64 path on the same mesh."""
+    from gridaphybrid_gb300 import _lib
+    lib = ctx.lib
+    n, D, k = args.skewed_n, 3, K_ORDER
+    B = np.array([[1.0, 0.3, 0.1], [0.1, 1.0, 0.2], [0.05, 0.1, 1.0]])
+    base = ctypes.c_void_p()
+    cells = np.array([n] * 3, dtype=np.int32)
+    dom = np.array([0, 1, 0, 1, 0, 1], dtype=np.float64)
+    ctx.check(lib.hdg_problem_create_cartesian(ctx.handle, D, _lib.ptr(cells), _lib.ptr(dom), k, ctypes.byref(base)))
+    info = np.zeros(8, dtype=np.int64)
+    ctx.check(lib.hdg_problem_info(base, _lib.ptr(info)))
+    ncells, nfacets, nfd = int(info[0]), int(info[1]), int(info[7])
+    cf = np.empty((ncells, 2 * D), dtype=np.int32)
+    fd = np.empty((nfacets, nfd), dtype=np.int32)
+    ctx.check(lib.hdg_get_topology(base, _lib.ptr(cf), None, _lib.ptr(fd)))
+    lib.hdg_problem_destroy(base)
+    idx = np.stack(np.unravel_index(np.arange(ncells), (n, n, n), order="F"), axis=1).astype(np.float64)
+    origin = np.ascontiguousarray((idx / n) @ B.T)
+    jac = np.ascontiguousarray(np.broadcast_to((B / n).T, (ncells, D, D)))  # per cell, column-major
+    h = ctypes.c_void_p()
+    ctx.check(lib.hdg_problem_create(ctx.handle, D, k, ncells, nfacets, _lib.ptr(origin), _lib.ptr(jac), _lib.ptr(cf),
+                                     _lib.ptr(fd), ctypes.byref(h)))
+    ctx.check(lib.hdg_set_darcy(h, _lib.HDG_STAB_TEXTBOOK, 1.0, _lib.HDG_PROBLEM_SIN))
+    kappa = np.exp(np.random.default_rng(SEED).normal(0.0, 1.0, ncells))  # the headline's field at n = 32
+    ctx.check(lib.hdg_set_permeability(h, _lib.ptr(kappa)))
+    ctx.check(lib.hdg_problem_info(h, _lib.ptr(info)))
+    ni, nfree = int(info[2]), int(info[4])
+
+    def run(prec, rtol):
+        ctx.check(lib.hdg_assemble(h, prec, None))
+        it, rel = ctypes.c_int(), ctypes.c_double()
+        ctx.check(lib.hdg_solve_skeleton(h, _lib.HDG_SOLVER_PCG, rtol, MAXIT, ctypes.byref(it), ctypes.byref(rel)))
+        ctx.check(lib.hdg_recover(h))
+        return it.value
+
+    out = {"workload": "the %d^3 k=2 Darcy workload with every cell mapped by the skew B = %s (non-diagonal "
+                       "Jacobians: general-Jacobian integration and elimination)" % (n, B.tolist()),
+           "cells": ncells}
+    sols = {}
+    for name, prec in (("fp64", _lib.HDG_PREC_FP64), ("ffblock", _lib.HDG_PREC_FF_BLOCK)):
+        run(prec, 1e-12)
+        sol = np.empty(ncells * ni + nfree)
+        ctx.check(lib.hdg_get_free_dof_values(h, _lib.ptr(sol)))
+        sols[name] = sol
+        if name == "ffblock":
+            for _ in range(args.warmup):
+                run(prec, RTOL)
+            ctx.synchronize()
+            ctx.check(lib.hdg_context_record(ctx.handle, 0))
+            phase, its = np.zeros(5), []
+            for _ in range(args.steps):
+                its.append(run(prec, RTOL))
+                t = np.zeros(5)
+                lib.hdg_get_timings(h, _lib.ptr(t))
+                phase += t
+            ctx.check(lib.hdg_context_record(ctx.handle, 1))
+            ctx.synchronize()
+            ms = ctypes.c_double()
+            ctx.check(lib.hdg_context_elapsed_ms(ctx.handle, 0, 1, ctypes.byref(ms)))
+            step_ms = ms.value / args.steps
+            out[name] = {"ms_per_step": step_ms, "cells_per_s": ncells / (step_ms / 1000.0),
+                         "phases_ms": dict(zip(["integrate", "condense", "assemble", "skeleton_pcg", "recover"],
+                                               [float(x) for x in phase / args.steps])),
+                         "pcg_iters": statistics.mean(its)}
+    ref = sols["fp64"]
+    out["ffblock"]["rel_err_vs_fp64"] = float(np.abs(sols["ffblock"] - ref).max() / np.abs(ref).max())
+    lib.hdg_problem_destroy(h)
+    return out
+
+
 ERR_GATE = 1e-8
 
 
@@ -530,6 +607,7 @@ def run_gpu(args, rank=0, nranks=1, device=0):
         return
     batching_out = run_batching(args, ctx) if args.batch_problems > 0 else None
     elasticity_out = run_elasticity(args, ctx) if args.elasticity_n > 0 else None
+    skewed_out = run_skewed(args, ctx) if args.skewed_n > 0 else None
     serving_out = run_serving(args, prec, precs["fp64"]) if args.serve_seconds > 0 else None
 
     peaks, peak_kind = measured_peaks()
@@ -584,6 +662,8 @@ def run_gpu(args, rank=0, nranks=1, device=0):
         line["batching"] = batching_out
     if elasticity_out:
         line["elasticity"] = elasticity_out
+    if skewed_out is not None:
+        line["skewed_mesh"] = skewed_out
     if serving_out:
         line["serving"] = serving_out
     line["setup_ms"] = setup_ms
@@ -633,9 +713,11 @@ def main():
     ap.add_argument("--serve-fp64-seconds", type=float, default=20.0,
                     help="part of the stream replayed on the plain FP64 path")
     ap.add_argument("--serve-rate", type=float, default=200.0)
-    ap.add_argument("--serve-slots", type=int, default=8)
+    ap.add_argument("--serve-slots", type=int, default=16)
     ap.add_argument("--batch-problems", type=int, default=64,
                     help="problems of the batching workload (0 skips it)")
+    ap.add_argument("--skewed-n", type=int, default=32,
+                    help="cells per side of the skewed-mesh run of the headline form (0: skip)")
     ap.add_argument("--elasticity-n", type=int, default=24,
                     help="cells per side of the elasticity precision workload (0 skips it)")
     ap.add_argument("--elasticity-k", type=int, default=2, choices=(1, 2),
