@@ -315,56 +315,152 @@ __global__ void __launch_bounds__(256) pack_cell_blocks_t(int ncells, int rec, d
 }
 
 // The same records for large cells (the whole S_c does not fit a CTA's
-// shared memory several times over): one work item per (cell, upper block),
-// the block and its transposed partner staged as two nfd x nfd tiles.
+// shared memory): one CTA per cell, the cell's nl facet factors W staged once
+// in FP32, then its upper blocks one after the other, each block and its
+// transposed partner staged as two nfd x nfd FP64 tiles.
 __global__ void pack_cell_blocks_tiled_kernel(int ncells, int nl, int nfd, int rec, double sign,
                                               const double *__restrict__ S, const int *__restrict__ cell_blk,
                                               const double *__restrict__ W, float *__restrict__ out) {
-  extern __shared__ double T[];  // 2 nb doubles, then 4 nb floats
+  extern __shared__ double T[];  // 2 nb doubles, then (nl + 2) nb floats
   const int nf = nl * nfd, nb = nfd * nfd, nblk = nl * (nl + 1) / 2;
   double *T1 = T, *T2 = T + nb;
-  float *Wl = reinterpret_cast<float *>(T + 2 * nb), *Wh = Wl + nb, *U = Wh + nb, *Ts = U + nb;
-  const long long items = (long long)ncells * nblk;
-  for (long long it = blockIdx.x; it < items; it += gridDim.x) {
-    const int c = (int)(it / nblk), blk = (int)(it - (long long)c * nblk);
-    int lo, hi;
-    upper_block(nl, blk, lo, hi);
+  float *Ws = reinterpret_cast<float *>(T + 2 * nb), *U = Ws + (size_t)nl * nb, *Ts = U + nb;
+  for (int c = blockIdx.x; c < ncells; c += gridDim.x) {
     const double *Sc = S + (size_t)c * nf * nf;
-    const int el = cell_blk[(size_t)c * nl + lo], eh = cell_blk[(size_t)c * nl + hi];
-    // T1[r + nfd s] = S(lo nfd + r, hi nfd + s), T2[r + nfd s] = S(hi nfd + r, lo nfd + s)
-    for (int e = threadIdx.x; e < nb; e += blockDim.x) {
-      const int sc = e / nfd, r = e - sc * nfd;
-      T1[e] = Sc[(size_t)(lo * nfd + r) + (size_t)nf * (hi * nfd + sc)];
-      T2[e] = Sc[(size_t)(hi * nfd + r) + (size_t)nf * (lo * nfd + sc)];
-      const int wr = e / nfd, wc = e - wr * nfd;  // row-major W index
-      Wl[e] = el >= 0 ? (float)W[(size_t)(el >> 1) * nb + e] : (wr == wc ? 1.0f : 0.0f);
-      Wh[e] = eh >= 0 ? (float)W[(size_t)(eh >> 1) * nb + e] : (wr == wc ? 1.0f : 0.0f);
+    for (int e = threadIdx.x; e < nl * nb; e += blockDim.x) {
+      const int lf = e / nb, w = e - lf * nb, wr = w / nfd, wc = w - wr * nfd;  // row-major W index
+      const int ent = cell_blk[(size_t)c * nl + lf];
+      Ws[e] = ent >= 0 ? (float)W[(size_t)(ent >> 1) * nb + w] : (wr == wc ? 1.0f : 0.0f);
+    }
+    for (int blk = 0; blk < nblk; ++blk) {
+      int lo, hi;
+      upper_block(nl, blk, lo, hi);
+      // T1[r + nfd s] = S(lo nfd + r, hi nfd + s), T2[r + nfd s] = S(hi nfd + r, lo nfd + s)
+      for (int e = threadIdx.x; e < nb; e += blockDim.x) {
+        const int sc = e / nfd, r = e - sc * nfd;
+        T1[e] = Sc[(size_t)(lo * nfd + r) + (size_t)nf * (hi * nfd + sc)];
+        T2[e] = Sc[(size_t)(hi * nfd + r) + (size_t)nf * (lo * nfd + sc)];
+      }
+      __syncthreads();
+      // Ts[p][q] = sign (S(lo p, hi q) + S(hi q, lo p))/2, one FP64 sum per entry
+      for (int e = threadIdx.x; e < nb; e += blockDim.x) {
+        const int p = e / nfd, q = e - p * nfd;
+        Ts[e] = (float)(0.5 * sign * (T1[p + nfd * q] + T2[q + nfd * p]));
+      }
+      __syncthreads();
+      // U[p][s] = sum_{q <= s} Ts[p][q] W_hi[s][q]
+      const float *Wh = Ws + (size_t)hi * nb, *Wl = Ws + (size_t)lo * nb;
+      for (int e = threadIdx.x; e < nb; e += blockDim.x) {
+        const int p = e / nfd, sc = e - p * nfd;
+        float u = 0.0f;
+        for (int q = 0; q <= sc; ++q) u = fmaf(Ts[p * nfd + q], Wh[sc * nfd + q], u);
+        U[e] = u;
+      }
+      __syncthreads();
+      float *o = out + (size_t)c * rec + (size_t)blk * nb;
+      for (int w = threadIdx.x; w < nb; w += blockDim.x) {
+        const int r = w / nfd, sc = w - r * nfd;
+        float v = 0.0f;
+        for (int p = 0; p <= r; ++p) v = fmaf(Wl[r * nfd + p], U[p * nfd + sc], v);
+        o[w] = v;
+      }
+    }
+    for (int e = nblk * nb + threadIdx.x; e < rec; e += blockDim.x) out[(size_t)c * rec + e] = 0.0f;  // padding
+    __syncthreads();
+  }
+}
+
+// Large cells with the block size at compile time: one CTA per cell, the
+// symmetric part of every upper block staged in FP32 (21 blocks of 27 x 27
+// for 3D elasticity k = 2: 61 KB) with the cell's facet factors W, then
+// U = T W_hi^T in place row by row (a thread keeps its row of T in registers)
+// and the record W_lo U column by column, all blocks at once: two barriers
+// per cell.
+template <int NL, int NFD>
+__global__ void __launch_bounds__(256) pack_cell_blocks_large_t(int ncells, int rec, double sign,
+                                                                const double *__restrict__ S,
+                                                                const int *__restrict__ cell_blk,
+                                                                const double *__restrict__ W, float *__restrict__ out) {
+  constexpr int NF = NL * NFD, NB = NFD * NFD, NBLK = NL * (NL + 1) / 2;
+  extern __shared__ float smx[];
+  float *Ts = smx, *Ws = smx + NBLK * NB;
+  __shared__ unsigned char blo[NBLK], bhi[NBLK];
+  if (threadIdx.x < NBLK) {
+    int lo, hi;
+    upper_block(NL, threadIdx.x, lo, hi);
+    blo[threadIdx.x] = (unsigned char)lo;
+    bhi[threadIdx.x] = (unsigned char)hi;
+  }
+  for (int c = blockIdx.x; c < ncells; c += gridDim.x) {
+    const double *Sc = S + (size_t)c * NF * NF;
+    for (int e = threadIdx.x; e < NL * NB; e += blockDim.x) {
+      const int lf = e / NB, w = e - lf * NB, wr = w / NFD, wc = w - wr * NFD;  // row-major W index
+      const int ent = cell_blk[(size_t)c * NL + lf];
+      Ws[e] = ent >= 0 ? (float)W[(size_t)(ent >> 1) * NB + w] : (wr == wc ? 1.0f : 0.0f);
+    }
+    __syncthreads();  // blo / bhi on the first cell
+    // T[blk][p][q] = sign (S(lo p, hi q) + S(hi q, lo p)) / 2, p fastest (the
+    // first read coalesced); eight entries per thread in flight at a time
+    constexpr int UNR = 8;
+    for (int e0 = threadIdx.x; e0 < NBLK * NB; e0 += UNR * blockDim.x) {
+      double a[UNR], b[UNR];
+#pragma unroll
+      for (int u = 0; u < UNR; ++u) {
+        const int e = e0 + u * blockDim.x;
+        a[u] = b[u] = 0.0;
+        if (e < NBLK * NB) {
+          const int blk = e / NB, w = e - blk * NB, q = w / NFD, p = w - q * NFD;
+          const int i = blo[blk] * NFD + p, j = bhi[blk] * NFD + q;
+          a[u] = __ldcs(Sc + i + (size_t)NF * j);
+          b[u] = __ldcs(Sc + j + (size_t)NF * i);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < UNR; ++u) {
+        const int e = e0 + u * blockDim.x;
+        if (e < NBLK * NB) {
+          const int blk = e / NB, w = e - blk * NB, q = w / NFD, p = w - q * NFD;
+          Ts[blk * NB + p * NFD + q] = (float)(0.5 * sign * (a[u] + b[u]));
+        }
+      }
     }
     __syncthreads();
-    // Ts[p][q] = sign (S(lo p, hi q) + S(hi q, lo p))/2, one FP64 sum per entry
-    for (int e = threadIdx.x; e < nb; e += blockDim.x) {
-      const int p = e / nfd, q = e - p * nfd;
-      Ts[e] = (float)(0.5 * sign * (T1[p + nfd * q] + T2[q + nfd * p]));
+    // U[blk][p][s] = sum_{q <= s} T[blk][p][q] W_hi[s][q], in place
+    for (int it = threadIdx.x; it < NBLK * NFD; it += blockDim.x) {
+      const int blk = it / NFD, p = it - blk * NFD;
+      float *row = Ts + blk * NB + p * NFD;
+      const float *Wh = Ws + bhi[blk] * NB;
+      float t[NFD];
+#pragma unroll
+      for (int q = 0; q < NFD; ++q) t[q] = row[q];
+#pragma unroll
+      for (int sc = 0; sc < NFD; ++sc) {
+        float u = 0.0f;
+#pragma unroll
+        for (int q = 0; q <= sc; ++q) u = fmaf(t[q], Wh[sc * NFD + q], u);
+        row[sc] = u;
+      }
     }
     __syncthreads();
-    // U[p][s] = sum_{q <= s} Ts[p][q] W_hi[s][q]
-    for (int e = threadIdx.x; e < nb; e += blockDim.x) {
-      const int p = e / nfd, sc = e - p * nfd;
-      float u = 0.0f;
-      for (int q = 0; q <= sc; ++q) u = fmaf(Ts[p * nfd + q], Wh[sc * nfd + q], u);
-      U[e] = u;
+    // record[blk][r][s] = sum_{p <= r} W_lo[r][p] U[blk][p][s]
+    float *o = out + (size_t)c * rec;
+    for (int it = threadIdx.x; it < NBLK * NFD; it += blockDim.x) {
+      const int blk = it / NFD, sc = it - blk * NFD;
+      const float *col = Ts + blk * NB + sc;
+      const float *Wl = Ws + blo[blk] * NB;
+      float u[NFD];
+#pragma unroll
+      for (int p = 0; p < NFD; ++p) u[p] = col[p * NFD];
+#pragma unroll
+      for (int r = 0; r < NFD; ++r) {
+        float v = 0.0f;
+#pragma unroll
+        for (int p = 0; p <= r; ++p) v = fmaf(Wl[r * NFD + p], u[p], v);
+        o[blk * NB + r * NFD + sc] = v;
+      }
     }
-    __syncthreads();
-    float *o = out + (size_t)c * rec + (size_t)blk * nb;
-    for (int w = threadIdx.x; w < nb; w += blockDim.x) {
-      const int r = w / nfd, sc = w - r * nfd;
-      float v = 0.0f;
-      for (int p = 0; p <= r; ++p) v = fmaf(Wl[r * nfd + p], U[p * nfd + sc], v);
-      o[w] = v;
-    }
-    if (blk == nblk - 1)  // the record's padding
-      for (int e = nblk * nb + threadIdx.x; e < rec; e += blockDim.x) out[(size_t)c * rec + e] = 0.0f;
-    __syncthreads();
+    for (int e = NBLK * NB + threadIdx.x; e < rec; e += blockDim.x) o[e] = 0.0f;  // padding
+    __syncthreads();  // Ts and Ws are read above until here
   }
 }
 
@@ -766,14 +862,34 @@ cudaError_t launch_pack_cell_blocks(int ncells, int nl, int nfd, double sign, co
                                     long long *launches) {
   const int nf = nl * nfd, nb = nfd * nfd, nblk = nl * (nl + 1) / 2;
   const size_t smem = sizeof(double) * nf * nf + sizeof(float) * (size_t)(nl + 2 * nblk) * nb;
-  if (smem > 64 * 1024) {  // large cells: block-pair tiles
-    const size_t tsmem = 2 * sizeof(double) * nb + 4 * sizeof(float) * nb;
+  if (smem > 64 * 1024) {  // large cells
+#define HDG_PACK_LARGE(L, F)                                                                                  \
+  if (nl == L && nfd == F) {                                                                                  \
+    const size_t lsmem = sizeof(float) * (size_t)(L * (L + 1) / 2 + L) * F * F;                               \
+    cudaError_t e = cudaFuncSetAttribute(pack_cell_blocks_large_t<L, F>,                                      \
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lsmem);             \
+    if (e != cudaSuccess) return e;                                                                           \
+    int per_sm = 0;                                                                                           \
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pack_cell_blocks_large_t<L, F>, 256, lsmem);   \
+    if (e != cudaSuccess) return e;                                                                           \
+    int grid = num_sms * (per_sm > 0 ? per_sm : 1);                                                           \
+    if (grid > ncells) grid = ncells;                                                                         \
+    if (grid < 1) grid = 1;                                                                                   \
+    pack_cell_blocks_large_t<L, F><<<grid, 256, lsmem, s>>>(ncells, cellop_rec(L, F), sign, S, cell_blk, W,  \
+                                                            out);                                             \
+    ++*launches;                                                                                              \
+    return cudaGetLastError();                                                                                \
+  }
+    HDG_PACK_LARGE(6, 27)
+    HDG_PACK_LARGE(6, 16)
+#undef HDG_PACK_LARGE
+    // other shapes: one cell per CTA, block by block
+    const size_t tsmem = 2 * sizeof(double) * nb + (size_t)(nl + 2) * sizeof(float) * nb;
     if (tsmem > 48 * 1024) return cudaErrorInvalidValue;
-    const long long items = (long long)ncells * nblk;
-    long long grid = items < (long long)num_sms * 16 ? items : (long long)num_sms * 16;
+    int grid = ncells < num_sms * 8 ? ncells : num_sms * 8;
     if (grid < 1) grid = 1;
-    pack_cell_blocks_tiled_kernel<<<(int)grid, 256, tsmem, s>>>(ncells, nl, nfd, cellop_rec(nl, nfd), sign, S,
-                                                                 cell_blk, W, out);
+    pack_cell_blocks_tiled_kernel<<<grid, 256, tsmem, s>>>(ncells, nl, nfd, cellop_rec(nl, nfd), sign, S,
+                                                           cell_blk, W, out);
     ++*launches;
     return cudaGetLastError();
   }
