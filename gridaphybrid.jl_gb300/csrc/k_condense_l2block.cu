@@ -169,6 +169,10 @@ struct Lists {
   // is set when a trace row or column of (facet lf, trace component j) has a
   // nonzero coupling to that component on the facet's nodes
   int fmask[C::NL][3];
+  // the same couplings as a list per (facet, trace component): the cell-block
+  // columns m (volume node on the facet x coupled component), node-major
+  short slist[C::NL][3][C::NK * (C::NC1 + C::NC2)];
+  int slen[C::NL][3];
   int piv, info;
   int pivs[8];        // the pivot rows of the current LU panel
   double cinv[6][6];  // C^{-1} / |J| of the cell (FP64)
@@ -498,6 +502,18 @@ __global__ void __launch_bounds__(C::NT, C::MI_SHARED ? 1 : 2) condense_l2block_
       }
     }
     __syncthreads();
+    // the coupling lists of the S phase, from the masks
+    for (int pr = t; pr < NL * (NFD / NFS); pr += NT) {
+      const int lf = pr / (NFD / NFS), kf = pr - lf * (NFD / NFS), msk = L.fmask[lf][kf];
+      int len = 0;
+      for (int q = 0; q < L.fn_cnt[lf]; ++q) {
+        const int node = L.fn_node[lf][q];
+        for (int cc = 0; cc < NSYM + NC2; ++cc)
+          if (msk >> cc & 1) L.slist[lf][kf][len++] = (short)(cc < NSYM ? cc * NK + node : NS + (cc - NSYM) * NK + node);
+      }
+      L.slen[lf][kf] = len;
+    }
+    __syncthreads();
     // 1. the b column of Z: A_ss^{-1} b_s (M^{-1} on each field-1 component,
     //    then the components mixed by C^{-1})
     for (int an = t; an < NK; an += NT) {
@@ -791,8 +807,9 @@ __global__ void __launch_bounds__(C::NT, C::MI_SHARED ? 1 : 2) condense_l2block_
     {
       constexpr int TF = C::TF, FT = NF / TF, CT = (NC + 3) / 4;
       for (int o = t; o < FT * CT; o += NT) {
-        const int f0 = (o % FT) * TF, c0 = (o / FT) * 4, lf = f0 / NFD, cnt = L.fn_cnt[lf];
-        const int msk = L.fmask[lf][(f0 - lf * NFD) / NFS];  // the tile's rows share (lf, trace component)
+        const int f0 = (o % FT) * TF, c0 = (o / FT) * 4, lf = f0 / NFD, kf = (f0 - lf * NFD) / NFS;
+        const short *lst = L.slist[lf][kf];  // the tile's rows share (lf, trace component)
+        const int len = L.slen[lf][kf];
         int cj[4];
 #pragma unroll
         for (int j = 0; j < 4; ++j) cj[j] = min(c0 + j, NC - 1);
@@ -801,23 +818,32 @@ __global__ void __launch_bounds__(C::NT, C::MI_SHARED ? 1 : 2) condense_l2block_
         for (int i = 0; i < TF; ++i)
 #pragma unroll
           for (int j = 0; j < 4; ++j) acc[i][j] = Ar::zero();
-        for (int q = 0; q < cnt; ++q) {
-          const int node = L.fn_node[lf][q];
+        auto load = [&](int m, V *av, V *xv) {
 #pragma unroll
-          for (int cc = 0; cc < NSYM + NC2; ++cc) {
-            if (!(msk >> cc & 1)) continue;
-            const bool s1 = cc < NSYM;
-            const int m = s1 ? cc * NK + node : NS + (cc - NSYM) * NK + node;
-            V av[TF], xv[4];
+          for (int i = 0; i < TF; ++i) av[i] = A(NI + f0 + i, m);
 #pragma unroll
-            for (int i = 0; i < TF; ++i) av[i] = A(NI + f0 + i, m);
+          for (int j = 0; j < 4; ++j) xv[j] = m < NS ? Z[m + (size_t)NS * cj[j]] : Q[(m - NS) * NC + cj[j]];
+        };
+        auto macs = [&](const V *av, const V *xv) {
 #pragma unroll
-            for (int j = 0; j < 4; ++j) xv[j] = s1 ? Z[m + (size_t)NS * cj[j]] : Q[(m - NS) * NC + cj[j]];
+          for (int i = 0; i < TF; ++i)
 #pragma unroll
-            for (int i = 0; i < TF; ++i)
-#pragma unroll
-              for (int j = 0; j < 4; ++j) Ar::mac(acc[i][j], av[i], xv[j]);
-          }
+            for (int j = 0; j < 4; ++j) Ar::mac(acc[i][j], av[i], xv[j]);
+        };
+        // two list entries per step, their loads issued together (the sums
+        // keep the list order: the same bits as one entry at a time)
+        int q = 0;
+        for (; q + 1 < len; q += 2) {
+          V av0[TF], xv0[4], av1[TF], xv1[4];
+          load(lst[q], av0, xv0);
+          load(lst[q + 1], av1, xv1);
+          macs(av0, xv0);
+          macs(av1, xv1);
+        }
+        if (q < len) {
+          V av0[TF], xv0[4];
+          load(lst[q], av0, xv0);
+          macs(av0, xv0);
         }
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
