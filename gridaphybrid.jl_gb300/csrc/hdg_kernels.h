@@ -242,7 +242,8 @@ struct L2BlockArgs {
   double *S, *g;
   void *X0, *X1;  // recovery X = A_ii^{-1} [A_if | b_i] (ni x (nf+1)), the same way; may be null
   int *info;
-  void *scratch;   // per-CTA panels (and the fused kernel's cell block)
+  void *scratch;   // per-CTA panels (and the fused kernel's cell block), then the per-cell factors
+  const void *prep;  // set by the launcher: the per-cell factors in the scratch
   MixedTables Tb;  // float-float reference tables (fused float-float integration)
   // sparse reference products M^{-1} G_e, M^{-1} H_F: index lists (ref_idx)
   // and values (ref_v0/ref_v1: FP64, or (hi, lo) float arrays)

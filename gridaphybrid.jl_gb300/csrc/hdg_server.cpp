@@ -122,8 +122,8 @@ double footprint_bound(int D, int n, int k, int precision, int solver) {
   b += ncells * (blocks + (double)s.nf * s.nf * 8 + 2.0 * s.nf * 8 + 4) + nnz * 8 + nfree * 8;
   b += fast || l2block ? 8.0 * ncells * s.ni * (s.nf + 1) : 8.0 * ncells * s.ni * (s.n + 1);
   if (precision == HDG_PREC_FF_BLOCK) b += ncells * 360.0;  // per-cell panel and integration coefficients
-  if (l2block)  // per-CTA slots (one CTA per SM): panels Y, Z and the cell block
-    b += 160.0 * 8.0 * ((double)s.ni * (s.nf + 1) * 2 + (double)s.n * s.n + s.n);
+  if (l2block)  // per-CTA slots (one CTA per SM): panels Y, Z and the cell block; per-cell factors
+    b += 160.0 * 8.0 * ((double)s.ni * (s.nf + 1) * 2 + (double)s.n * s.n + s.n) + ncells * 672.0;
   if (fast) b += ncells * cellop_rec(nl, s.nfd) * 4.0;
   // skeleton solve
   if (solver == HDG_SOLVER_DIRECT) {

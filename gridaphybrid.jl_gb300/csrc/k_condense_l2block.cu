@@ -184,6 +184,15 @@ constexpr size_t smem_bytes() {
   return C::smem_values * sizeof(typename Ar::V) + sizeof(Lists<C>) + 16;
 }
 
+// Per-cell factors computed before the elimination, one thread per cell: the
+// geometric factors and C^{-1}/|J| (elasticity: the inverse compliance;
+// Darcy: kappa/|J| on the diagonal).  Computed inside the elimination they
+// were FP64 divisions and square roots on one thread while the CTA waited.
+struct CellPrep {
+  CellFactors cf;
+  double cinv[6][6];
+};
+
 // the fused kernel's integration scratch: cell factors / terms, per-point
 // source values (nqv x (D+1)), the row decode table (elasticity)
 template <class C>
@@ -213,7 +222,7 @@ __device__ void integrate_into_slot(const L2BlockArgs &a, int cell, void *A0, vo
   if constexpr (C::ELAST) {
     ElastScratch &S = *reinterpret_cast<ElastScratch *>(integ);
     for (int i = t; i < N; i += NT) dec[i] = elast_pack(ca, i);
-    elast_cell_prepare(ca, cell, S, fq, FF, t, NT);  // barriers inside
+    elast_cell_prepare(ca, cell, S, fq, FF, t, NT, &static_cast<const CellPrep *>(a.prep)[cell].cf);  // barriers inside
     for (int e = t; e < NR * N; e += NT) {
       const int j = e / NR, i = NS + (e - j * NR);
       if constexpr (FF) {
@@ -336,6 +345,28 @@ __device__ void compliance_inverse(int D, int nsym, double E, double nu, double 
     for (int d = 0; d < nsym; ++d) Ci[c][d] = I[c][d] / detJ;
 }
 
+// One thread per cell (see CellPrep).
+__global__ void __launch_bounds__(128) l2block_prep_kernel(CellArgs ca, int ncells, int elast, int nsym,
+                                                           CellPrep *out) {
+  const int D = ca.D;
+  for (int cell = blockIdx.x * blockDim.x + threadIdx.x; cell < ncells; cell += gridDim.x * blockDim.x) {
+    CellPrep p;
+    cell_factors(ca, cell, p.cf);
+    const double *J = ca.jac + (size_t)cell * D * D;
+    const double det = D == 2 ? J[0] * J[3] - J[2] * J[1]
+                              : J[0] * (J[4] * J[8] - J[7] * J[5]) - J[3] * (J[1] * J[8] - J[7] * J[2]) +
+                                    J[6] * (J[1] * J[5] - J[4] * J[2]);
+    if (elast) {
+      compliance_inverse(D, nsym, ca.young, ca.kappa ? ca.kappa[cell] : 0.3, fabs(det), p.cinv);
+    } else {  // kappa / |J| on the diagonal
+      const double sc = (ca.kappa ? ca.kappa[cell] : 1.0) / fabs(det);
+      for (int c = 0; c < 6; ++c)
+        for (int d = 0; d < 6; ++d) p.cinv[c][d] = c == d ? sc : 0.0;
+    }
+    out[cell] = p;
+  }
+}
+
 template <class C, class Ar, bool FUSED>
 __global__ void __launch_bounds__(C::NT, C::MI_SHARED ? 1 : 2) condense_l2block_kernel(L2BlockArgs a) {
   using V = typename Ar::V;
@@ -431,26 +462,17 @@ __global__ void __launch_bounds__(C::NT, C::MI_SHARED ? 1 : 2) condense_l2block_
     };
     __syncthreads();  // the previous cell's readers of the lists / Ci / slot are done
     if constexpr (FUSED) integrate_into_slot<C, Ar>(a, cell, sA0, sA1, sb0, sb1, integ, t);
-    if (t == 0) {
-      const double *J = ca.jac + (size_t)cell * D * D;
-      const double det = D == 2 ? J[0] * J[3] - J[2] * J[1]
-                                : J[0] * (J[4] * J[8] - J[7] * J[5]) - J[3] * (J[1] * J[8] - J[7] * J[2]) +
-                                      J[6] * (J[1] * J[5] - J[4] * J[2]);
-      double Cinv[6][6];
-      if (C::ELAST) {
-        compliance_inverse(D, NSYM, ca.young, ca.kappa ? ca.kappa[cell] : 0.3, fabs(det), Cinv);
-      } else {  // kappa / |J| on the diagonal
-        const double s = (ca.kappa ? ca.kappa[cell] : 1.0) / fabs(det);
-        for (int c = 0; c < NSYM; ++c)
-          for (int d = 0; d < NSYM; ++d) Cinv[c][d] = c == d ? s : 0.0;
+    {  // the cell's factors and C^{-1}/|J|, computed beforehand (l2block_prep_kernel)
+      const CellPrep &pp = static_cast<const CellPrep *>(a.prep)[cell];
+      for (int e = t; e < NSYM * NSYM; e += NT) {
+        const int c = e / NSYM, d = e - c * NSYM;
+        const double v = pp.cinv[c][d];
+        Ci[c * 6 + d] = Ar::of(v);
+        L.cinv[c][d] = v;
       }
-      for (int c = 0; c < NSYM; ++c)
-        for (int d = 0; d < NSYM; ++d) {
-          Ci[c * 6 + d] = Ar::of(Cinv[c][d]);
-          L.cinv[c][d] = Cinv[c][d];
-        }
-      cell_factors(ca, cell, L.cf);
-      L.info = 0;
+      for (int e = t; e < (int)(sizeof(CellFactors) / sizeof(double)); e += NT)
+        reinterpret_cast<double *>(&L.cf)[e] = reinterpret_cast<const double *>(&pp.cf)[e];
+      if (t == 0) L.info = 0;
     }
     if (t < NL * 3) L.fmask[t / 3][t % 3] = 0;
     __syncthreads();
@@ -888,12 +910,21 @@ cudaError_t launch_cfg(const L2BlockArgs &args, const L2BlockLaunch &L, cudaStre
   long long grid = (long long)per_sm * L.num_sms;
   if (grid > args.ncells) grid = args.ncells;
   if (grid < 1) grid = 1;
-  const size_t need = (size_t)grid * (FUSED ? C::slot_values_fused : C::slot_values) * sizeof(typename Ar::V);
+  const size_t slots = ((size_t)grid * (FUSED ? C::slot_values_fused : C::slot_values) * sizeof(typename Ar::V) + 255) /
+                       256 * 256;
+  const size_t need = slots + (size_t)args.ncells * sizeof(CellPrep);
   if (L.scratch_bytes_out) *L.scratch_bytes_out = need;
   if (L.dry_run) return cudaSuccess;
   if (need > L.scratch_bytes || !args.scratch) return cudaErrorMemoryAllocation;
-  kern<<<(int)grid, C::NT, smem, s>>>(args);
-  ++*launches;
+  L2BlockArgs a2 = args;
+  CellPrep *prep = reinterpret_cast<CellPrep *>(static_cast<char *>(args.scratch) + slots);
+  a2.prep = prep;
+  int pg = (args.ncells + 127) / 128;
+  if (pg > L.num_sms * 16) pg = L.num_sms * 16;
+  if (pg < 1) pg = 1;
+  l2block_prep_kernel<<<pg, 128, 0, s>>>(args.cell, args.ncells, C::ELAST ? 1 : 0, C::NC1, prep);
+  kern<<<(int)grid, C::NT, smem, s>>>(a2);
+  *launches += 2;
   return cudaGetLastError();
 }
 

@@ -153,10 +153,16 @@ struct ElastScratch {
 // body-force values -w.f per quadrature point (fq: nqv x D).  Every thread of
 // the CTA calls it (CTA barriers); t / nt: this thread and the thread count.
 __device__ __forceinline__ void elast_cell_prepare(const CellArgs &a, int c, ElastScratch &S, double *fq, bool ff,
-                                                   int t, int nt) {
+                                                   int t, int nt, const CellFactors *pre = nullptr) {
   const int D = a.D;
   const double nu = a.kappa ? a.kappa[c] : 0.3;
-  if (t == 0) cell_factors(a, c, S.f);
+  if (pre) {  // the factors computed beforehand (one thread per cell): copied by the whole CTA
+    static_assert(sizeof(CellFactors) % sizeof(double) == 0, "CellFactors holds doubles only");
+    for (int e = t; e < (int)(sizeof(CellFactors) / sizeof(double)); e += nt)
+      reinterpret_cast<double *>(&S.f)[e] = reinterpret_cast<const double *>(pre)[e];
+  } else if (t == 0) {
+    cell_factors(a, c, S.f);
+  }
   __syncthreads();
   for (int e = t; e < 6 * 3 * 3 + 6 * 3 * 6 + 36; e += nt) {
     if (e < 54) {
