@@ -123,7 +123,7 @@ double footprint_bound(int D, int n, int k, int precision, int solver) {
   b += fast || l2block ? 8.0 * ncells * s.ni * (s.nf + 1) : 8.0 * ncells * s.ni * (s.n + 1);
   if (precision == HDG_PREC_FF_BLOCK) b += ncells * 360.0;  // per-cell panel and integration coefficients
   if (l2block)  // per-CTA slots (one CTA per SM): panels Y, Z and the cell block; per-cell factors
-    b += 160.0 * 8.0 * ((double)s.ni * (s.nf + 1) * 2 + (double)s.n * s.n + s.n) + ncells * 672.0;
+    b += 160.0 * 8.0 * ((double)s.ni * (s.nf + 1) * 2 + (double)s.n * s.n + s.n) + ncells * 1056.0;
   if (fast) b += ncells * cellop_rec(nl, s.nfd) * 4.0;
   // skeleton solve
   if (solver == HDG_SOLVER_DIRECT) {

@@ -191,6 +191,7 @@ constexpr size_t smem_bytes() {
 struct CellPrep {
   CellFactors cf;
   double cinv[6][6];
+  CellFactorsFF cff;  // Darcy: the float-float integration's factors
 };
 
 // the fused kernel's integration scratch: cell factors / terms, per-point
@@ -247,11 +248,13 @@ __device__ void integrate_into_slot(const L2BlockArgs &a, int cell, void *A0, vo
     // Darcy: the cell factors (float-float or FP64) and the source per point
     CellFactorsFF &fF = *reinterpret_cast<CellFactorsFF *>(integ);
     CellFactors &f6 = *reinterpret_cast<CellFactors *>(integ);
-    if (t == 0) {
-      if constexpr (FF)
-        cell_factors_ff(ca, cell, fF);
-      else
-        cell_factors(ca, cell, f6);
+    {  // computed beforehand (l2block_prep_kernel), copied by the whole CTA
+      const CellPrep &pp = static_cast<const CellPrep *>(a.prep)[cell];
+      static_assert(sizeof(CellFactorsFF) % 4 == 0 && sizeof(CellFactors) % 4 == 0, "word copies");
+      const unsigned *src = FF ? reinterpret_cast<const unsigned *>(&pp.cff) : reinterpret_cast<const unsigned *>(&pp.cf);
+      unsigned *dst = reinterpret_cast<unsigned *>(integ);
+      const int words = (int)((FF ? sizeof(CellFactorsFF) : sizeof(CellFactors)) / 4);
+      for (int e = t; e < words; e += NT) dst[e] = src[e];
     }
     __syncthreads();
     {
@@ -352,6 +355,7 @@ __global__ void __launch_bounds__(128) l2block_prep_kernel(CellArgs ca, int ncel
   for (int cell = blockIdx.x * blockDim.x + threadIdx.x; cell < ncells; cell += gridDim.x * blockDim.x) {
     CellPrep p;
     cell_factors(ca, cell, p.cf);
+    if (!elast) cell_factors_ff(ca, cell, p.cff);
     const double *J = ca.jac + (size_t)cell * D * D;
     const double det = D == 2 ? J[0] * J[3] - J[2] * J[1]
                               : J[0] * (J[4] * J[8] - J[7] * J[5]) - J[3] * (J[1] * J[8] - J[7] * J[2]) +
