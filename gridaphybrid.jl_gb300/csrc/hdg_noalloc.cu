@@ -16,10 +16,11 @@
 // Host code cannot use the array's name as a device address (in host code it
 // names a host-side stand-in).  The device address is looked up once per
 // device with cudaGetSymbolAddress, with that device current, on the first
-// call made on that device; make that first call before any stream capture.
+// call made on that device.
 // Every call waits for its own work to finish (it synchronises the context's
 // stream to read the pivot flag) before it returns, and leaves the caller's
-// current device as it found it.
+// current device as it found it.  Because of that synchronisation no call can
+// be captured into a CUDA graph.
 // All calls share the one array: calls whose work overlaps on the GPU race
 // with each other and must be serialised by the caller (one stream, or
 // events).  The array keeps the contents of the last call; everything that

@@ -151,9 +151,11 @@ int hdg_sum_facets(hdg_context *ctx, int nitems, int nfacets, int len,
  *    4*ncells more when info is NULL; a larger batch is rejected with
  *    HDG_ERR_INVALID (split it).
  *  - The first call on a device looks the array's address up
- *    (cudaGetSymbolAddress); make that first call before any stream capture.
+ *    (cudaGetSymbolAddress).
  *  - Each call waits for its own work (it synchronises the context's stream
- *    to read the pivot flag) and gives the caller's current device back.
+ *    to read the pivot flag) and gives the caller's current device back, so
+ *    no call can be captured into a CUDA graph: a call made while the
+ *    context's stream is capturing fails and ends that capture.
  *  - Pointers must be device memory of the context's GPU (or managed);
  *    host memory and other GPUs' memory are refused with HDG_ERR_INVALID.
  *  - Every call uses the same array: calls that overlap on the GPU race, so
