@@ -1260,6 +1260,8 @@ static PcgArgs pcg_args(hdg_problem *pb) {
   a.blk_off = pb->d_blk_off.as<int64_t>();
   a.blk_rowlen = pb->d_blk_rowlen.as<int>();
   a.sign = skeleton_sign(pb);
+  a.max_rowlen = pb->pat.max_rowlen;
+  a.tile_ctas = csr_tile_ctas(pb->pat.nblockrows, pb->mesh.nfd, pb->ctx->num_sms);
   return a;
 }
 
@@ -1308,8 +1310,13 @@ static int run_pcg64(hdg_problem *pb, const PcgArgs &a, int maxit, int *it_out, 
     cudaGraph_t g;
     long long dummy = 0;
     CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-    for (int i = 0; i < pairs; ++i) launch_pcg_iteration_pair(a, ctx->stream, ctx->num_sms, &dummy);
+    cudaError_t le = cudaSuccess;
+    for (int i = 0; i < pairs && le == cudaSuccess; ++i) le = launch_pcg_iteration_pair(a, ctx->stream, ctx->num_sms, &dummy);
     CUDA_TRY(ctx, cudaStreamEndCapture(ctx->stream, &g));
+    if (le != cudaSuccess) {
+      cudaGraphDestroy(g);
+      return ctx->fail(HDG_ERR_CUDA, "PCG iteration capture: %s", cudaGetErrorString(le));
+    }
     cudaError_t e = cudaGraphInstantiate(&pb->pcg_graph, g, 0);
     cudaGraphDestroy(g);
     CUDA_TRY(ctx, e);
@@ -1371,6 +1378,9 @@ static int solve_pcg_refined(hdg_problem *pb, double rtol, int maxit, int *it_ou
   hdg_context *ctx = pb->ctx;
   const size_t n = pb->mesh.nfree, nfd = pb->mesh.nfd, nbr = pb->pat.nblockrows;
   if (!pb->d_cellop.ptr) return ctx->fail(HDG_ERR_STATE, "the FP32 cell operator is missing (assemble in a fast precision)");
+  if (pb->pat.max_rowlen > kSkeletonRowBlocks * (int)nfd)
+    return ctx->fail(HDG_ERR_INVALID, "skeleton rows of %d entries exceed the residual kernel's %d", pb->pat.max_rowlen,
+                     kSkeletonRowBlocks * (int)nfd);
   const int nl = pb->mesh.nl;
   CUDA_TRY(ctx, cellop_configure(nl, (int)nfd, ctx->smem_optin, ctx->num_sms, &pb->cellop_nstage, &pb->cellop_ctas));
   {  // at least two stages of cells per CTA on small problems
@@ -1406,6 +1416,8 @@ static int solve_pcg_refined(hdg_problem *pb, double rtol, int maxit, int *it_ou
   oa.nparts = ia.nparts;
   oa.sign = skeleton_sign(pb);
   oa.W = pb->d_W.as<double>();
+  oa.max_rowlen = pb->pat.max_rowlen;
+  oa.tile_ctas = csr_tile_ctas((int)nbr, (int)nfd, ctx->num_sms);
   const int pairs = 8;
   // the inner iterations as one cooperative launch per chunk where its grid
   // can be co-resident (about two cell units per CTA on small problems), else
@@ -1422,8 +1434,13 @@ static int solve_pcg_refined(hdg_problem *pb, double rtol, int maxit, int *it_ou
     cudaGraph_t g;
     long long dummy = 0;
     CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-    for (int i = 0; i < pairs; ++i) launch_pcg32_iteration_pair(ia, ctx->stream, &dummy);
+    cudaError_t le = cudaSuccess;
+    for (int i = 0; i < pairs && le == cudaSuccess; ++i) le = launch_pcg32_iteration_pair(ia, ctx->stream, &dummy);
     CUDA_TRY(ctx, cudaStreamEndCapture(ctx->stream, &g));
+    if (le != cudaSuccess) {
+      cudaGraphDestroy(g);
+      return ctx->fail(HDG_ERR_CUDA, "inner PCG iteration capture: %s", cudaGetErrorString(le));
+    }
     cudaError_t e = cudaGraphInstantiate(&pb->pcg32_graph, g, 0);
     cudaGraphDestroy(g);
     CUDA_TRY(ctx, e);
@@ -1584,9 +1601,9 @@ int hdg_solve_skeleton(hdg_problem *pb, int solver, double rtol, int maxit, int 
     if (hinfo) status = ctx->fail(HDG_ERR_SINGULAR, "singular skeleton system (pivot %d)", hinfo);
     pb->d_z.release();
   } else {
-    if (pb->pat.max_rowlen > kMaxSkeletonRowLen)
+    if (pb->pat.max_rowlen > kMaxSkeletonRowLen || pb->pat.max_rowlen > kSkeletonRowBlocks * (int)nfd)
       return ctx->fail(HDG_ERR_INVALID, "skeleton rows of %d entries exceed the SpMV kernel's %d", pb->pat.max_rowlen,
-                       kMaxSkeletonRowLen);
+                       std::min(kMaxSkeletonRowLen, kSkeletonRowBlocks * (int)nfd));
     if (!pcg_supports_nfd((int)nfd))
       return ctx->fail(HDG_ERR_INVALID, "PCG has no kernel for %zu DOFs per facet", nfd);
     CUDA_TRY(ctx, pb->d_Binv.reserve(sizeof(double) * pb->pat.nblockrows * nfd * nfd));

@@ -304,6 +304,8 @@ struct PcgArgs {
   const int64_t *blk_off;
   const int *blk_rowlen;
   double sign;
+  int max_rowlen;  // longest skeleton row (at most 11 blocks: the SpMV's staged tile)
+  int tile_ctas;   // CTAs of the SpMV (tiles of whole block rows; at most 8 per SM)
 };
 cudaError_t launch_pcg_setup(const PcgArgs &a, double rtol, cudaStream_t s,
                              int num_sms, long long *launches);
@@ -357,6 +359,19 @@ cudaError_t launch_pcg32_persistent(const Pcg32Args &a, int grid, size_t smem, i
 // and the longest skeleton row their FP64 SpMV stages (kMaxRowLen)
 constexpr int kPcgThreadsHost = 256;
 constexpr int kMaxSkeletonRowLen = 304;
+// blocks in a skeleton row (a facet, the other facets of its two cells)
+constexpr int kSkeletonRowBlocks = 11;
+// CTAs for the FP64 CSR kernels that take tiles of kPcgThreadsHost / nfd
+// whole block rows: at most 8 per SM (their partials fit 8 per SM), with
+// the tiles spread evenly (every CTA the same count, up to one)
+inline int csr_tile_ctas(int nblockrows, int nfd, int num_sms) {
+  const long long br = kPcgThreadsHost / nfd;
+  const long long tiles = (nblockrows + br - 1) / br;
+  const long long cap = 8LL * num_sms;
+  const long long per = (tiles + cap - 1) / cap;
+  const long long g = per > 0 ? (tiles + per - 1) / per : 1;
+  return g < 1 ? 1 : (int)g;
+}
 // Cell-operator layout: threads per cell, cells per CTA stage, floats per record.
 HDG_HD constexpr int cellop_tpc(int nf) { return nf <= 8 ? 8 : nf <= 16 ? 16 : ((nf + 31) / 32) * 32; }
 HDG_HD constexpr int cellop_cps(int nf) { return cellop_tpc(nf) >= 256 ? 1 : 256 / cellop_tpc(nf); }
@@ -385,6 +400,8 @@ struct OuterArgs {
   int nparts;
   double sign;
   const double *W;  // the inner frame's scaling (x += W^T y), or null (x += y)
+  int max_rowlen;   // longest skeleton row (at most 11 blocks: the residual's staged tile)
+  int tile_ctas;    // CTAs of the residual (tiles of whole block rows; at most 8 per SM)
 };
 cudaError_t launch_pcg32_init(const Pcg32Args &a, double eta, cudaStream_t s, long long *launches);
 cudaError_t launch_pcg32_iteration_pair(const Pcg32Args &a, cudaStream_t s, long long *launches);

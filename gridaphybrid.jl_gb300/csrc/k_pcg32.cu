@@ -628,6 +628,7 @@ __global__ void __launch_bounds__(CellOp<NL, NFD>::THREADS, 2)
 // over the grid (a.uctas CTAs, up to eight per SM) with a grid-stride loop.
 static_assert(kPcgThreads == kPcgThreadsHost, "host and device PCG block sizes differ");
 static_assert(kMaxRowLen == kMaxSkeletonRowLen, "host and device skeleton row limits differ");
+static_assert(kRowBlocks == kSkeletonRowBlocks, "host and device skeleton row limits differ");
 
 template <int NFD>
 __global__ void __launch_bounds__(kPcgThreads) pcg32_update_rows_kernel(Pcg32Args a, const float *__restrict__ p) {
@@ -713,44 +714,30 @@ __global__ void outer_combine_kernel(int n, const double *__restrict__ xs, doubl
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) x[i] = xs[i] + sign * x[i];
 }
 
-// r = c - M x with the FP64 matrix (block-row gather of x), |r|^2
+// r = c - M x with the FP64 matrix, a lane pair per row over tiles of whole
+// block rows (x staged per block row), |r|^2
 template <int NFD>
 __global__ void __launch_bounds__(kPcgThreads) outer_residual_kernel(OuterArgs a) {
+  using T = RowTile<NFD>;
   __shared__ double red[32];
-  __shared__ double xs[kPcgThreads / 32][kMaxRowLen];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nw = (gridDim.x * blockDim.x) >> 5;
+  __shared__ double xs[T::BR * T::LMAX];
+  const double *__restrict__ x = a.x;
   double acc = 0.0;
-  for (int br = wid; br < a.nblockrows; br += nw) {
-    const int row0 = br * NFD;
-    const int64_t base = a.rowptr[row0];
-    const int rowlen = (int)(a.rowptr[row0 + 1] - base);
-    for (int j = lane; j < rowlen; j += 32) xs[w][j] = a.x[a.colind[base + j]];
-    __syncwarp();
-    constexpr int P = Pow2Ceil<NFD>::v;
-    double v[P];
-#pragma unroll
-    for (int r = 0; r < P; ++r) v[r] = 0.0;
-    for (int j = lane; j < rowlen; j += 32) {
-      const double xv = xs[w][j];
-      const double *vj = a.val + base + j;
-#pragma unroll
-      for (int r = 0; r < NFD; ++r) v[r] += __ldcs(vj + (int64_t)r * rowlen) * xv;
-    }
-    const double tot = warp_reduce_scatter<double, P>(v, lane);
-    const int myrow = reduce_scatter_row<P>(lane);
-    if (myrow < NFD && reduce_scatter_writer<P>(lane)) {
-      const double r = a.sign * a.rhs[row0 + myrow] - a.sign * tot;
-      a.r[row0 + myrow] = r;
+  for (int br0 = blockIdx.x * T::BR; br0 < a.nblockrows; br0 += gridDim.x * T::BR) {
+    const int nbr = min(T::BR, a.nblockrows - br0);
+    stage_tile_columns<NFD>(a.rowptr, a.colind, br0, nbr, xs, [&](int col) { return x[col]; });
+    __syncthreads();
+    tile_row_products<NFD>(a.rowptr, a.val, br0, nbr, xs, [&](int row, int, double t) {
+      const double r = a.sign * a.rhs[row] - a.sign * t;
+      a.r[row] = r;
       acc += r * r;
-    }
-    __syncwarp();
+    });
+    __syncthreads();  // xs is restaged for the next tile
   }
   const double t = block_sum(acc, red);
   if (threadIdx.x == 0) a.partials[blockIdx.x] = t;
   if (last_cta(a.counter)) {
-    const double v = sum_partials(a.partials, a.nparts, 0, red);
+    const double v = sum_partials(a.partials, (int)gridDim.x, 0, red);
     if (threadIdx.x == 0) {
       a.scal[1] = v;
       *a.counter = 0u;
@@ -968,6 +955,8 @@ cudaError_t launch_outer_combine(const OuterArgs &a, const double *xsaved, cudaS
 }
 
 cudaError_t launch_outer_update(const OuterArgs &a, const float *e, cudaStream_t s, long long *launches) {
+  if (a.max_rowlen > kRowBlocks * a.nfd) return cudaErrorInvalidValue;  // the staged tile holds 11 blocks a row
+  if (a.tile_ctas < 1 || a.tile_ctas > 8 * 1024) return cudaErrorInvalidValue;
   int g = (a.n + 255) / 256;
   if (g > 4096) g = 4096;
   if (g < 1) g = 1;
@@ -976,19 +965,19 @@ cudaError_t launch_outer_update(const OuterArgs &a, const float *e, cudaStream_t
   else
     outer_axpy_kernel<<<g, 256, 0, s>>>(a.n, e, a.x);
   switch (a.nfd) {
-    case 1: outer_residual_kernel<1><<<a.nparts, kPcgThreads, 0, s>>>(a); break;
-    case 2: outer_residual_kernel<2><<<a.nparts, kPcgThreads, 0, s>>>(a); break;
-    case 3: outer_residual_kernel<3><<<a.nparts, kPcgThreads, 0, s>>>(a); break;
-    case 4: outer_residual_kernel<4><<<a.nparts, kPcgThreads, 0, s>>>(a); break;
-    case 5: outer_residual_kernel<5><<<a.nparts, kPcgThreads, 0, s>>>(a); break;
-    case 6: outer_residual_kernel<6><<<a.nparts, kPcgThreads, 0, s>>>(a); break;
-    case 8: outer_residual_kernel<8><<<a.nparts, kPcgThreads, 0, s>>>(a); break;
-    case 9: outer_residual_kernel<9><<<a.nparts, kPcgThreads, 0, s>>>(a); break;
-    case 10: outer_residual_kernel<10><<<a.nparts, kPcgThreads, 0, s>>>(a); break;
-    case 12: outer_residual_kernel<12><<<a.nparts, kPcgThreads, 0, s>>>(a); break;
-    case 16: outer_residual_kernel<16><<<a.nparts, kPcgThreads, 0, s>>>(a); break;
-    case 25: outer_residual_kernel<25><<<a.nparts, kPcgThreads, 0, s>>>(a); break;
-    case 27: outer_residual_kernel<27><<<a.nparts, kPcgThreads, 0, s>>>(a); break;
+    case 1: outer_residual_kernel<1><<<a.tile_ctas, kPcgThreads, 0, s>>>(a); break;
+    case 2: outer_residual_kernel<2><<<a.tile_ctas, kPcgThreads, 0, s>>>(a); break;
+    case 3: outer_residual_kernel<3><<<a.tile_ctas, kPcgThreads, 0, s>>>(a); break;
+    case 4: outer_residual_kernel<4><<<a.tile_ctas, kPcgThreads, 0, s>>>(a); break;
+    case 5: outer_residual_kernel<5><<<a.tile_ctas, kPcgThreads, 0, s>>>(a); break;
+    case 6: outer_residual_kernel<6><<<a.tile_ctas, kPcgThreads, 0, s>>>(a); break;
+    case 8: outer_residual_kernel<8><<<a.tile_ctas, kPcgThreads, 0, s>>>(a); break;
+    case 9: outer_residual_kernel<9><<<a.tile_ctas, kPcgThreads, 0, s>>>(a); break;
+    case 10: outer_residual_kernel<10><<<a.tile_ctas, kPcgThreads, 0, s>>>(a); break;
+    case 12: outer_residual_kernel<12><<<a.tile_ctas, kPcgThreads, 0, s>>>(a); break;
+    case 16: outer_residual_kernel<16><<<a.tile_ctas, kPcgThreads, 0, s>>>(a); break;
+    case 25: outer_residual_kernel<25><<<a.tile_ctas, kPcgThreads, 0, s>>>(a); break;
+    case 27: outer_residual_kernel<27><<<a.tile_ctas, kPcgThreads, 0, s>>>(a); break;
     default: return cudaErrorInvalidValue;
   }
   *launches += 2;

@@ -1,6 +1,7 @@
 // k_pcg_common.cuh -- device helpers shared by the skeleton PCG kernels.
 #pragma once
 #include <cuda_runtime.h>
+#include <stdint.h>
 
 namespace hdg {
 
@@ -114,6 +115,108 @@ __device__ __forceinline__ double sum_partials_ff(const double *partials, int np
   }
   const float2 s = block_sum_ff(hi, lo, redf);
   return (double)s.x + (double)s.y;
+}
+
+// ---------------------------------------------------------------------------
+// FP64 CSR products, two lanes per row.  GB300's FP64 pipe is the bound of an
+// FP64 CSR SpMV (one DFMA per stored entry against 12 bytes of traffic), so
+// every FP64 instruction counts: a row per lane pair needs one DFMA per entry
+// and a single shuffle-add (a warp per block row with a reduce-scatter issued
+// about 1.9x that on 3D k = 2 rows), while each pair still reads its row in
+// 32-byte pieces (one row per lane left most of every sector to a later load
+// and ran at half the bandwidth).  A CTA takes a tile of whole block rows; the
+// vector at the tile's columns is staged once per block row in shared memory
+// and shared by the block row's NFD rows.
+// ---------------------------------------------------------------------------
+// A facet's row couples to its own block and to the other facets of its at
+// most two cells (at most six facets each): at most 11 blocks.  The host
+// checks every problem's longest row against kRowBlocks * nfd.
+constexpr int kRowBlocks = 11;
+
+template <int NFD>
+struct RowTile {
+  static constexpr int BR = kPcgThreads / NFD;   // block rows per tile
+  static constexpr int LMAX = kRowBlocks * NFD;  // staged entries per block row
+  static constexpr int ROWS = BR * NFD;          // rows per tile
+  static constexpr int RPP = kPcgThreads / 2;    // rows per pass of the CTA
+  static constexpr int PASSES = (ROWS + RPP - 1) / RPP;
+};
+
+// This lane's half of sum_j v[j] xk[j] (half = 0, 1 of the lane pair): the
+// row in 16-byte loads, the pair's two loads 32 contiguous bytes, after an
+// 8-byte one (half 0) where the row starts unaligned; the two halves summed
+// by the caller.  Four loads per lane are issued before their products: the
+// rows stream from HBM, and one load in flight per lane held the kernel to
+// about 2.7 TB/s.
+__device__ __forceinline__ double row_dot_half(const double *__restrict__ v, const double *xk, int len, int half) {
+  double t = 0.0;
+  int j = 0;
+  if (len > 0 && (reinterpret_cast<uintptr_t>(v) & 15u) != 0) {
+    if (half == 0) t = fma(__ldg(v), xk[0], t);
+    j = 1;
+  }
+  for (; j + 15 < len; j += 16) {
+    double2 w[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) w[u] = __ldg(reinterpret_cast<const double2 *>(v + j + 4 * u + 2 * half));
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int q = j + 4 * u + 2 * half;
+      t = fma(w[u].x, xk[q], t);
+      t = fma(w[u].y, xk[q + 1], t);
+    }
+  }
+  for (; j + 3 < len; j += 4) {
+    const int q = j + 2 * half;
+    const double2 w = __ldg(reinterpret_cast<const double2 *>(v + q));
+    t = fma(w.x, xk[q], t);
+    t = fma(w.y, xk[q + 1], t);
+  }
+  for (int q = j + half; q < len; q += 2) t = fma(__ldg(v + q), xk[q], t);
+  return t;
+}
+__device__ __forceinline__ double row_dot_half(const float *__restrict__ v, const double *xk, int len, int half) {
+  double t = 0.0;
+  for (int q = half; q < len; q += 2) t = fma((double)__ldg(v + q), xk[q], t);
+  return t;
+}
+
+// For every row of the tile (block rows br0 .. br0+nbr-1, staged columns in
+// xs): emit(row, k, sum_j val[row, j] x[col_j]) in the pair's even lane (k =
+// block row in the tile).  Called by the whole CTA.
+template <int NFD, typename V, typename E>
+__device__ __forceinline__ void tile_row_products(const int64_t *__restrict__ rowptr, const V *__restrict__ val,
+                                                  int br0, int nbr, const double *xs, E emit) {
+  using T = RowTile<NFD>;
+  const int half = threadIdx.x & 1;
+#pragma unroll 1
+  for (int pass = 0; pass < T::PASSES; ++pass) {
+    const int tr = pass * T::RPP + ((int)threadIdx.x >> 1);
+    const bool act = tr < nbr * NFD;
+    const int k = tr / NFD;
+    const int row = br0 * NFD + tr;
+    double t = 0.0;
+    if (act) {
+      const int64_t b = rowptr[row];
+      t = row_dot_half(val + b, xs + k * T::LMAX, (int)(rowptr[row + 1] - b), half);
+    }
+    t += __shfl_xor_sync(0xffffffffu, t, 1);  // the same bits in both lanes
+    if (act && half == 0) emit(row, k, t);
+  }
+}
+
+// Stages f(col) for the columns of block rows br0 .. br0+nbr-1 into
+// xs[k * LMAX + j] (k = block row in the tile, j = entry), warp by warp;
+// the caller synchronises before reading.
+template <int NFD, typename F>
+__device__ __forceinline__ void stage_tile_columns(const int64_t *__restrict__ rowptr, const int *__restrict__ colind,
+                                                   int br0, int nbr, double *xs, F f) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int k = w; k < nbr; k += nw) {
+    const int64_t base = rowptr[(int64_t)(br0 + k) * NFD];
+    const int len = (int)(rowptr[(int64_t)(br0 + k) * NFD + 1] - base);
+    for (int j = lane; j < len; j += 32) xs[k * RowTile<NFD>::LMAX + j] = f(colind[base + j]);
+  }
 }
 
 template <int N>

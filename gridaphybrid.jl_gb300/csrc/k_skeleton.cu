@@ -352,60 +352,37 @@ __global__ void __launch_bounds__(kPcgThreads) pcg_init_kernel(PcgArgs a, double
 // One warp per facet block row: its nfd rows share one column list, read
 // once; p_new on those columns is formed in shared memory, then the block
 // row's nfd*rowlen contiguous values are streamed.
+// q = sign A p with p = z + beta p_old formed at the staged columns (the
+// owner rows write p_new), a lane pair per row over tiles of whole block
+// rows; alpha = (r,z) / (p,q) by the last CTA
 template <typename V, int NFD>
 __global__ void __launch_bounds__(kPcgThreads) pcg_spmv_kernel(PcgArgs a, const V *__restrict__ val,
                                                                const double *__restrict__ p_old,
                                                                double *__restrict__ p_new) {
+  using T = RowTile<NFD>;
   __shared__ double red[32];
-  __shared__ double xs[kPcgThreads / 32][kMaxRowLen];
+  __shared__ double xs[T::BR * T::LMAX];
   if (a.scal[SC_DONE] != 0.0) return;
   const double beta = a.scal[SC_BETA];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nw = (gridDim.x * blockDim.x) >> 5;
+  const double *__restrict__ z = a.z;
   double acc = 0.0;
-  for (int br = wid; br < a.nblockrows; br += nw) {
-    const int row0 = br * NFD;
-    const int64_t base = a.rowptr[row0];
-    const int rowlen = (int)(a.rowptr[row0 + 1] - base);
-    for (int j = lane; j < rowlen; j += 32) {
-      const int col = a.colind[base + j];
-      xs[w][j] = a.z[col] + beta * p_old[col];
-    }
-    double pown = 0.0;
-    if (lane < NFD) {
-      pown = a.z[row0 + lane] + beta * p_old[row0 + lane];
-      p_new[row0 + lane] = pown;
-    }
-    __syncwarp();
-    // every row's loads are issued before any reduction (NFD independent streams)
-    double s[NFD];
-#pragma unroll
-    for (int r = 0; r < NFD; ++r) s[r] = 0.0;
-    for (int j = lane; j < rowlen; j += 32) {
-      const double xv = xs[w][j];
-      const V *vj = val + base + j;
-#pragma unroll
-      for (int r = 0; r < NFD; ++r) s[r] += (double)__ldcs(vj + (int64_t)r * rowlen) * xv;
-    }
-    constexpr int P = Pow2Ceil<NFD>::v;
-    double v[P];
-#pragma unroll
-    for (int r = 0; r < P; ++r) v[r] = r < NFD ? s[r] : 0.0;
-    const double tot = warp_reduce_scatter<double, P>(v, lane);
-    const int myrow = reduce_scatter_row<P>(lane);
-    const double pmine = __shfl_sync(0xffffffffu, pown, myrow < NFD ? myrow : 0);
-    if (myrow < NFD && reduce_scatter_writer<P>(lane)) {
-      const double q = a.sign * tot;
-      a.q[row0 + myrow] = q;
-      acc += q * pmine;
-    }
-    __syncwarp();
+  for (int br0 = blockIdx.x * T::BR; br0 < a.nblockrows; br0 += gridDim.x * T::BR) {
+    const int nbr = min(T::BR, a.nblockrows - br0);
+    stage_tile_columns<NFD>(a.rowptr, a.colind, br0, nbr, xs, [&](int col) { return z[col] + beta * p_old[col]; });
+    __syncthreads();
+    tile_row_products<NFD>(a.rowptr, val, br0, nbr, xs, [&](int row, int, double t) {
+      const double pown = z[row] + beta * p_old[row];
+      p_new[row] = pown;
+      const double q = a.sign * t;
+      a.q[row] = q;
+      acc += q * pown;
+    });
+    __syncthreads();  // xs is restaged for the next tile
   }
   const double t = block_sum(acc, red);
   if (threadIdx.x == 0) a.partials[blockIdx.x] = t;
   if (last_cta(a.counter)) {
-    const double pq = sum_partials(a.partials, a.nparts, 0, red);
+    const double pq = sum_partials(a.partials, (int)gridDim.x, 0, red);
     if (threadIdx.x == 0) {
       a.scal[SC_PAP] = pq;
       a.scal[SC_ALPHA] = a.scal[SC_RZ] / pq;
@@ -478,10 +455,11 @@ cudaError_t launch_pcg_setup(const PcgArgs &a, double rtol, cudaStream_t s, int 
 
 template <typename V>
 static cudaError_t spmv_dispatch(const PcgArgs &a, const V *val, const double *po, double *pn, cudaStream_t s) {
+  if (a.max_rowlen > kRowBlocks * a.nfd) return cudaErrorInvalidValue;  // the staged tile holds 11 blocks a row
   switch (a.nfd) {
 #define HDG_SPMV_CASE(N) \
   case N:                \
-    pcg_spmv_kernel<V, N><<<a.nparts, kPcgThreads, 0, s>>>(a, val, po, pn); break;
+    pcg_spmv_kernel<V, N><<<a.tile_ctas, kPcgThreads, 0, s>>>(a, val, po, pn); break;
     HDG_SPMV_CASE(1)
     HDG_SPMV_CASE(2)
     HDG_SPMV_CASE(3)
