@@ -615,7 +615,7 @@ def run_gpu(args, rank=0, nranks=1, device=0):
     # SpMV of the PCG iterations.  FP64 path: CSR values + one column list per
     # facet block row + two row pointers per block row + z and p_old gathered
     # once + p_new and q written once.  Fast paths (unassembled FP32 cell
-    # operator): the cell records (upper facet blocks, padded to 16 bytes) +
+    # operator): the cell records (facet blocks above the diagonal, padded to 16 bytes) +
     # the cell->block-row map + z and p_old read once + p_new written once +
     # the per-cell products written.
     nblockrows = nfree // nfd
@@ -625,13 +625,11 @@ def run_gpu(args, rank=0, nranks=1, device=0):
         spmv_kernel = "pcg_spmv_kernel<double,9>"
         spmv_traffic = None  # not captured
     else:
-        rec = (nl * (nl + 1) // 2 * nfd * nfd + 3) // 4 * 4
+        bstride = {9: 85, 27: 731}.get(nfd, nfd * nfd)  # blocks padded against bank conflicts
+        rec = (nl * (nl - 1) // 2 * bstride + 3) // 4 * 4  # the blocks above the diagonal
         spmv_bytes = ncells * rec * 4 + ncells * nl * 4 + 3 * nfree * 4 + ncells * nf * 4
         spmv_kernel = "cell_spmv32_kernel<6,9>"
-        # DRAM read + write of one launch from an ncu capture at 24^3 (97.45 + 2.69 MB
-        # over 13,824 cells, the bench configuration), scaled by cells: the kernel
-        # streams each cell record once, so traffic grows with the cells
-        spmv_traffic = 100.14e6 / 13824 * ncells
+        spmv_traffic = None  # set from an ncu capture of this record layout
     spmv_gbs = spmv_bytes / (spmv_ms.value * 1e-3) / 1e9
     # assembly: condensed blocks + vectors read, CSR values + rhs written
     asm_bytes = ncells * (nf * nf + nf) * 8 + nnz * 8 + nfree * 8

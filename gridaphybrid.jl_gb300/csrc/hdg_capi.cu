@@ -1102,7 +1102,8 @@ static int assemble_prepare(hdg_problem *pb, int precision, bool cell_blocks, bo
   CUDA_TRY(ctx, pb->d_rhs.reserve(sizeof(double) * (pb->mesh.nfree ? pb->mesh.nfree : 1)));
   if (mixed) {
     CUDA_TRY(ctx, pb->d_cellop.reserve(sizeof(float) * nc * cellop_rec(nl, (int)t.nfd)));
-    CUDA_TRY(ctx, pb->d_W.reserve(sizeof(double) * std::max<size_t>(pb->pat.nblockrows, 1) * t.nfd * t.nfd));
+    // W, then one double: set when a facet block is not positive definite
+    CUDA_TRY(ctx, pb->d_W.reserve(sizeof(double) * (std::max<size_t>(pb->pat.nblockrows, 1) * t.nfd * t.nfd + 1)));
   }
   pb->precision = precision;
   pb->assembled = pb->solved = pb->recovered = false;
@@ -1292,8 +1293,8 @@ static Pcg32Args pcg32_args(hdg_problem *pb) {
   ia.nstage = pb->cellop_nstage;
   ia.ctas = pb->cellop_ctas;
   ia.error = pb->d_counter.as<unsigned int>() + 1;
-  {  // update kernel: about two rows per thread, at most eight CTAs per SM
-    long long g = ((long long)n + 2 * kPcgThreadsHost - 1) / (2 * kPcgThreadsHost);
+  {  // update kernel: about eight rows per thread (four loads in flight), at most eight CTAs per SM
+    long long g = ((long long)n + 8 * kPcgThreadsHost - 1) / (8 * kPcgThreadsHost);
     const long long cap = (long long)pb->ctx->num_sms * 8;
     ia.uctas = g > cap ? (int)cap : g < 1 ? 1 : (int)g;
   }
@@ -1449,9 +1450,15 @@ static int solve_pcg_refined(hdg_problem *pb, double rtol, int maxit, int *it_ou
   double *ho = h + 16;
   CUDA_TRY(ctx, launch_outer_init(oa, ctx->stream, &ctx->launches));
   CUDA_TRY(ctx, cudaMemcpyAsync(ho, oa.scal, sizeof(double) * 2, cudaMemcpyDeviceToHost, ctx->stream));
+  CUDA_TRY(ctx, cudaMemcpyAsync(ho + 2, pb->d_W.as<double>() + nbr * nfd * nfd, sizeof(double), cudaMemcpyDeviceToHost,
+                                ctx->stream));
   CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   const double cc = ho[0];
   double rr = ho[1];
+  // a facet block that is not positive definite kept W_f = I, so the records
+  // (which leave out the diagonal blocks as the identity) do not hold for it:
+  // the FP64 solve below takes the whole system
+  const bool not_pd = ho[2] != 0.0;
   int total = 0, outer = 0;
   int status = HDG_OK;
   int base = 0;         // iterations counted before the last init (SC_ITERS restarts there)
@@ -1461,7 +1468,7 @@ static int solve_pcg_refined(hdg_problem *pb, double rtol, int maxit, int *it_ou
   int slow = 0;         // consecutive cycles that cut the FP64 residual less than 2x
   bool stalled = false;
   while (cc > 0.0 && rr > rtol * rtol * cc) {
-    if (total < maxit && (slow >= 3 || outer >= 60)) {
+    if (total < maxit && (not_pd || slow >= 3 || outer >= 60)) {
       stalled = true;  // finished below by an FP64 correction solve
       break;
     }

@@ -375,7 +375,16 @@ inline int csr_tile_ctas(int nblockrows, int nfd, int num_sms) {
 // Cell-operator layout: threads per cell, cells per CTA stage, floats per record.
 HDG_HD constexpr int cellop_tpc(int nf) { return nf <= 8 ? 8 : nf <= 16 ? 16 : ((nf + 31) / 32) * 32; }
 HDG_HD constexpr int cellop_cps(int nf) { return cellop_tpc(nf) >= 256 ? 1 : 256 / cellop_tpc(nf); }
-HDG_HD constexpr int cellop_rec(int nl, int nfd) { return (nl * (nl + 1) / 2 * nfd * nfd + 3) / 4 * 4; }
+// A cell record holds the nl (nl - 1) / 2 blocks (a, b), a < b, of the scaled
+// cell operator: the assembled diagonal blocks of the scaled operator are the
+// identity, so no cell stores its diagonal blocks.
+HDG_HD constexpr int cellop_blocks(int nl) { return nl * (nl - 1) / 2; }
+// Floats from one block of a record to the next: nfd^2, padded where that
+// spreads the SpMV's shared-memory reads over more banks (3D k = 2 Darcy
+// blocks: 85 instead of 81, about 1.5 instead of 2.1 wavefronts per load in a
+// model of the kernel's access pattern; 27-DOF elasticity blocks: 731).
+HDG_HD constexpr int cellop_bstride(int nfd) { return nfd == 9 ? 85 : nfd == 27 ? 731 : nfd * nfd; }
+HDG_HD constexpr int cellop_rec(int nl, int nfd) { return (cellop_blocks(nl) * cellop_bstride(nfd) + 3) / 4 * 4; }
 bool cellop_supported(int nl, int nfd);
 // pipeline depth and grid for the streaming kernel (sets its shared-memory limit)
 cudaError_t cellop_configure(int nl, int nfd, size_t smem_optin, int num_sms, int *nstage, int *ctas);

@@ -114,98 +114,107 @@ __global__ void __launch_bounds__(kPcgThreads) pcg32_replace_kernel(Pcg32Args a,
   }
 }
 
-// W = blockdiag(L_f^{-1}): one warp per free facet, right-looking Cholesky of
-// sign*D_f in shared memory, then each lane forms one column of L^{-1} by
-// forward substitution.  In FP32 (the FP64 pipe runs at 1/64 of the FP32
-// rate on this part): W is a scaling of the inner frame, and every use of it
-// (the records, the inner right-hand side, the correction back-transform)
-// reads the same values, so its own rounding does not enter the solution.  A
-// block that is not positive definite gets W = I.
-constexpr int kCholWarps = 8;
+// W = blockdiag(L_f^{-1}) in FP64, with the Cholesky factor of sign*D_f and
+// its inverse held in registers: a group of nfd lanes per free facet (32/nfd
+// facets per warp), lane i holding row i of L while it is factored and then
+// column i of L^{-1} (forward substitution of every column at once), the
+// other lanes' entries passed by shuffles.  In FP64: the scaled operator
+// W sign*A W^T then has the identity as its assembled diagonal blocks to FP64
+// rounding, and the cell records leave those blocks out (the inner iteration
+// adds p for them), so W's own rounding must not show there.  A block that is
+// not positive definite gets W = I and raises the flag after the last block
+// (W[nblockrows * nfd^2] = 1.0): the records do not hold for it, and the host
+// finishes such a solve in FP64.
 template <int NFD>
-__global__ void __launch_bounds__(32 * kCholWarps) block_chol_inv_kernel(PcgArgs a, double *W) {
-  constexpr int NB = NFD * NFD;
-  __shared__ float csm[kCholWarps][2][NB];
-  __shared__ float inv_diag[kCholWarps][NFD];
-  const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
-  float *L = csm[wl][0], *Li = csm[wl][1];
-  for (int br = blockIdx.x * kCholWarps + wl; br < a.nblockrows; br += gridDim.x * kCholWarps) {
-    const int blk = a.diag_blk[br];
-    const int64_t off = a.blk_off[blk];
-    const int rl = a.blk_rowlen[blk];
-    for (int e = lane; e < NB; e += 32) {
-      const int i = e / NFD, j = e - i * NFD;
-      L[e] = (float)(a.sign * a.val[off + (int64_t)i * rl + j]);
+__global__ void __launch_bounds__(128) block_chol_inv_kernel(PcgArgs a, double *W) {
+  constexpr int G = 32 / NFD;  // facets per warp
+  const int lane = threadIdx.x & 31;
+  const int sub = lane / NFD, i = lane - sub * NFD;
+  const int base = sub * NFD;  // the group's first lane (past 31 for the idle lanes: shuffles wrap, values unused)
+  const int nwarps = gridDim.x * (blockDim.x >> 5);
+  const int wid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  for (int br0 = wid * G; br0 < a.nblockrows; br0 += nwarps * G) {
+    const int br = br0 + sub;
+    const bool act = sub < G && br < a.nblockrows;
+    double Lr[NFD];  // row i of sign*D_f, then of L (entries j <= i used)
+    if (act) {
+      const int blk = a.diag_blk[br];
+      const int64_t off = a.blk_off[blk] + (int64_t)i * a.blk_rowlen[blk];
+#pragma unroll
+      for (int j = 0; j < NFD; ++j) Lr[j] = a.sign * a.val[off + j];
+    } else {
+#pragma unroll
+      for (int j = 0; j < NFD; ++j) Lr[j] = j == i ? 1.0 : 0.0;
     }
-    __syncwarp();
     bool ok = true;
+    double dinv[NFD];  // 1 / L[c][c], the same in the whole group
+    // fixed trip counts (fully unrolled: the rows stay in registers); one
+    // reciprocal square root per pivot and no division (FP64 runs at a small
+    // fraction of the FP32 rate here)
+#pragma unroll NFD
     for (int c = 0; c < NFD; ++c) {
-      const float d = L[c * NFD + c];
-      if (!(d > 0.0f) || !isfinite(d)) {  // the same value in every lane: a uniform exit
+      double d = __shfl_sync(0xffffffffu, Lr[c], base + c);  // the pivot, the same in the whole group
+      if (!(d > 0.0) || !isfinite(d)) {
         ok = false;
-        break;
+        d = 1.0;  // keep the arithmetic finite; the block gets W = I
       }
-      const float sd = sqrtf(d), inv = 1.0f / sd;
-      __syncwarp();
-      for (int i = c + 1 + lane; i < NFD; i += 32) L[i * NFD + c] *= inv;
-      if (lane == 0) {
-        L[c * NFD + c] = sd;
-        inv_diag[wl][c] = inv;
+      const double inv = rsqrt(d);
+      dinv[c] = inv;
+      Lr[c] = i == c ? d * inv : (i > c ? Lr[c] * inv : Lr[c]);
+#pragma unroll NFD
+      for (int j = 1; j < NFD; ++j) {
+        if (j <= c) continue;
+        const double ljc = __shfl_sync(0xffffffffu, Lr[c], base + j);  // L[j][c], scaled above
+        Lr[j] = j <= i ? fma(-Lr[c], ljc, Lr[j]) : Lr[j];
       }
-      __syncwarp();
-      for (int e = lane; e < NB; e += 32) {
-        const int i = e / NFD, j = e - i * NFD;
-        if (j > c && j <= i) L[i * NFD + j] -= L[i * NFD + c] * L[j * NFD + c];
-      }
-      __syncwarp();
     }
-    if (ok)
-      for (int j = lane; j < NFD; j += 32)
-        for (int i = 0; i < NFD; ++i) {
-          if (i < j) {
-            Li[i * NFD + j] = 0.0f;
-            continue;
-          }
-          float v = i == j ? 1.0f : 0.0f;
-          for (int k = j; k < i; ++k) v = fmaf(-L[i * NFD + k], Li[k * NFD + j], v);
-          Li[i * NFD + j] = v * inv_diag[wl][i];
-        }
-    __syncwarp();
-    double *out = W + (size_t)br * NB;
-    for (int e = lane; e < NB; e += 32) {
-      const int i = e / NFD, j = e - i * NFD;
-      out[e] = ok ? (double)Li[e] : (i == j ? 1.0 : 0.0);
+    // column i of L^{-1}: X[r] = (delta_ri - sum_{k<r} L[r][k] X[k]) / L[r][r]
+    double X[NFD];
+#pragma unroll
+    for (int r = 0; r < NFD; ++r) {
+      double v = r == i ? 1.0 : 0.0;
+#pragma unroll
+      for (int k = 0; k < r; ++k) v = fma(-__shfl_sync(0xffffffffu, Lr[k], base + r), X[k], v);
+      X[r] = v * dinv[r];
     }
-    __syncwarp();
+    if (act) {
+      double *out = W + (size_t)br * NFD * NFD + i;
+#pragma unroll
+      for (int r = 0; r < NFD; ++r) out[r * NFD] = ok ? X[r] : (r == i ? 1.0 : 0.0);
+      if (!ok && i == 0) W[(size_t)a.nblockrows * NFD * NFD] = 1.0;
+    }
   }
 }
 
 // ---------------------------------------------------------------------------
 // The unassembled FP32 operator.
 //
-// Cell record: the upper triangle of facet blocks (a <= b, row-major order of
+// Cell record: the facet blocks above the diagonal (a < b, row-major order of
 // (a, b)) of the scaled cell operator W_a sign*(S_c + S_c^T)/2 W_b^T (W_f the
 // facet's L_f^{-1}, the identity on Dirichlet facets, whose rows the SpMV
-// skips), each block nfd x nfd row-major, padded to a multiple of four floats
-// (16 bytes) so records can be bulk-copied.  The symmetric storage streams
-// 21/36 of the full 3D cell matrix; the lower blocks are read transposed from
-// shared memory.  The two triangular products run in FP32 from the FP64
-// symmetric part.
+// skips), each block nfd x nfd row-major at a stride of cellop_bstride(nfd)
+// floats, the record padded to a multiple of four floats (16 bytes) so it can
+// be bulk-copied.  The diagonal blocks are left out:
+// summed over a facet's cells they give W_f sign*D_f W_f^T = I, which the
+// inner iteration applies as p itself.  The storage streams 15/36 of the full
+// 3D cell matrix (21/36 with the diagonal blocks); the lower blocks are read
+// transposed from shared memory.  The two triangular products run in FP32
+// from the FP64 symmetric part.
 __device__ __forceinline__ void upper_block(int nl, int blk, int &lo, int &hi) {
   int l = 0, rem = blk;
-  while (rem >= nl - l) {
-    rem -= nl - l;
+  while (rem >= nl - 1 - l) {
+    rem -= nl - 1 - l;
     ++l;
   }
   lo = l;
-  hi = l + rem;
+  hi = l + 1 + rem;
 }
 
 __global__ void pack_cell_blocks_kernel(int ncells, int nl, int nfd, int rec, double sign,
                                         const double *__restrict__ S, const int *__restrict__ cell_blk,
                                         const double *__restrict__ W, float *__restrict__ out) {
   extern __shared__ double Ss[];  // nf^2 doubles, then nl nb + 2 nblk nb floats
-  const int nf = nl * nfd, nb = nfd * nfd, nblk = nl * (nl + 1) / 2;
+  const int nf = nl * nfd, nb = nfd * nfd, nblk = cellop_blocks(nl);
   float *Ws = reinterpret_cast<float *>(Ss + (size_t)nf * nf);
   float *Ts = Ws + nl * nb;    // the FP32 symmetric part sign (S + S^T)/2 of every upper block
   float *Us = Ts + nblk * nb;  // T W_hi^T
@@ -241,10 +250,12 @@ __global__ void pack_cell_blocks_kernel(int ncells, int nl, int nfd, int rec, do
     __syncthreads();
     // record[blk][r][s] = sum_{p <= r} W_lo[r][p] U[blk][p][s]
     float *o = out + (size_t)c * rec;
+    const int bs = cellop_bstride(nfd);
     for (int e = threadIdx.x; e < rec; e += blockDim.x) {
       float v = 0.0f;
-      if (e < nblk * nb) {
-        const int blk = e / nb, w = e - blk * nb, r = w / nfd, sc = w - r * nfd;
+      const int blk = e / bs, w = e - blk * bs;
+      if (blk < nblk && w < nb) {  // else: padding
+        const int r = w / nfd, sc = w - r * nfd;
         int lo, hi;
         upper_block(nl, blk, lo, hi);
         const float *Wl = Ws + lo * nb + r * nfd;
@@ -263,7 +274,7 @@ template <int NL, int NFD>
 __global__ void __launch_bounds__(256) pack_cell_blocks_t(int ncells, int rec, double sign,
                                                           const double *__restrict__ S, const int *__restrict__ cell_blk,
                                                           const double *__restrict__ W, float *__restrict__ out) {
-  constexpr int NF = NL * NFD, NB = NFD * NFD, NBLK = NL * (NL + 1) / 2;
+  constexpr int NF = NL * NFD, NB = NFD * NFD, NBLK = cellop_blocks(NL);
   extern __shared__ double Ss[];
   float *Ws = reinterpret_cast<float *>(Ss + NF * NF);
   float *Ts = Ws + NL * NB;
@@ -300,10 +311,12 @@ __global__ void __launch_bounds__(256) pack_cell_blocks_t(int ncells, int rec, d
     }
     __syncthreads();
     float *o = out + (size_t)c * rec;
+    constexpr int BS = cellop_bstride(NFD);
     for (int e = threadIdx.x; e < rec; e += blockDim.x) {
       float v = 0.0f;
-      if (e < NBLK * NB) {
-        const int blk = e / NB, w = e - blk * NB, r = w / NFD, sc = w - r * NFD;
+      const int blk = e / BS, w = e - blk * BS;
+      if (blk < NBLK && w < NB) {  // else: padding
+        const int r = w / NFD, sc = w - r * NFD;
         const float *Wl = Ws + blo[blk] * NB + r * NFD;
         const float *U = Us + blk * NB + sc;
         for (int p = 0; p <= r; ++p) v = fmaf(Wl[p], U[p * NFD], v);
@@ -322,7 +335,7 @@ __global__ void pack_cell_blocks_tiled_kernel(int ncells, int nl, int nfd, int r
                                               const double *__restrict__ S, const int *__restrict__ cell_blk,
                                               const double *__restrict__ W, float *__restrict__ out) {
   extern __shared__ double T[];  // 2 nb doubles, then (nl + 2) nb floats
-  const int nf = nl * nfd, nb = nfd * nfd, nblk = nl * (nl + 1) / 2;
+  const int nf = nl * nfd, nb = nfd * nfd, nblk = cellop_blocks(nl);
   double *T1 = T, *T2 = T + nb;
   float *Ws = reinterpret_cast<float *>(T + 2 * nb), *U = Ws + (size_t)nl * nb, *Ts = U + nb;
   for (int c = blockIdx.x; c < ncells; c += gridDim.x) {
@@ -357,7 +370,8 @@ __global__ void pack_cell_blocks_tiled_kernel(int ncells, int nl, int nfd, int r
         U[e] = u;
       }
       __syncthreads();
-      float *o = out + (size_t)c * rec + (size_t)blk * nb;
+      float *o = out + (size_t)c * rec + (size_t)blk * cellop_bstride(nfd);
+      for (int w = nb + threadIdx.x; w < cellop_bstride(nfd); w += blockDim.x) o[w] = 0.0f;  // padding
       for (int w = threadIdx.x; w < nb; w += blockDim.x) {
         const int r = w / nfd, sc = w - r * nfd;
         float v = 0.0f;
@@ -365,7 +379,8 @@ __global__ void pack_cell_blocks_tiled_kernel(int ncells, int nl, int nfd, int r
         o[w] = v;
       }
     }
-    for (int e = nblk * nb + threadIdx.x; e < rec; e += blockDim.x) out[(size_t)c * rec + e] = 0.0f;  // padding
+    for (int e = nblk * cellop_bstride(nfd) + threadIdx.x; e < rec; e += blockDim.x)
+      out[(size_t)c * rec + e] = 0.0f;  // padding
     __syncthreads();
   }
 }
@@ -381,7 +396,7 @@ __global__ void __launch_bounds__(256) pack_cell_blocks_large_t(int ncells, int 
                                                                 const double *__restrict__ S,
                                                                 const int *__restrict__ cell_blk,
                                                                 const double *__restrict__ W, float *__restrict__ out) {
-  constexpr int NF = NL * NFD, NB = NFD * NFD, NBLK = NL * (NL + 1) / 2;
+  constexpr int NF = NL * NFD, NB = NFD * NFD, NBLK = cellop_blocks(NL), BS = cellop_bstride(NFD);
   extern __shared__ float smx[];
   float *Ts = smx, *Ws = smx + NBLK * NB;
   __shared__ unsigned char blo[NBLK], bhi[NBLK];
@@ -456,10 +471,13 @@ __global__ void __launch_bounds__(256) pack_cell_blocks_large_t(int ncells, int 
         float v = 0.0f;
 #pragma unroll
         for (int p = 0; p <= r; ++p) v = fmaf(Wl[r * NFD + p], u[p], v);
-        o[blk * NB + r * NFD + sc] = v;
+        o[blk * BS + r * NFD + sc] = v;
       }
     }
-    for (int e = NBLK * NB + threadIdx.x; e < rec; e += blockDim.x) o[e] = 0.0f;  // padding
+    for (int e = threadIdx.x; e < rec; e += blockDim.x) {  // padding between and after the blocks
+      const int blk = e / BS, w = e - blk * BS;
+      if (blk >= NBLK || w >= NB) o[e] = 0.0f;
+    }
     __syncthreads();  // Ts and Ws are read above until here
   }
 }
@@ -476,7 +494,8 @@ struct CellOp {
 };
 
 // p_new = z + beta p_old (formed while gathering, stored by the owning cell);
-// qc_c = M_c p_c for every cell; alpha = (r,z) / sum_c (p_c, qc_c).
+// qc_c = M_c p_c for every cell without the diagonal blocks (whose sum over a
+// facet's cells is the identity); alpha = (r,z) / ((p, p) + sum_c (p_c, qc_c)).
 // Persistent CTAs take stages of CPS consecutive cells round-robin; thread 0
 // keeps `nstage` stages of cell records in flight with bulk copies (L2
 // evict-first: the records are read once per iteration, the vectors stay).
@@ -537,7 +556,10 @@ __global__ void __launch_bounds__(CellOp<NL, NFD>::THREADS, 2)
     float pv = 0.0f;
     if (ent_a >= 0) {
       pv = fmaf(beta, po_a, z_a);
-      if (ent_a & 1) p_new[(ent_a >> 1) * NFD + r] = pv;
+      if (ent_a & 1) {
+        p_new[(ent_a >> 1) * NFD + r] = pv;
+        acc.add_prod(pv, pv);  // (p, I p) over the facet's diagonal block, once per row
+      }
     }
     // stage t+1's values, stage t+2's entry
     ent_a = ent_b;
@@ -575,24 +597,30 @@ __global__ void __launch_bounds__(CellOp<NL, NFD>::THREADS, 2)
           pr[4 * v + 2] = t4.z;
           pr[4 * v + 3] = t4.w;
         }
+        // one partial sum per facet block (independent FMA chains), added in block order
+        float qb[NL];
 #pragma unroll
         for (int b = 0; b < NL; ++b) {
-          // block (lf, b) is stored for b >= lf; below the diagonal read (b, lf) transposed
-          const bool up = b >= lf;
+          // block (lf, b) is stored for b > lf; below the diagonal read (b, lf)
+          // transposed; the diagonal block's part is p itself (the update adds it)
+          qb[b] = 0.0f;
+          if (b == lf) continue;
+          const bool up = b > lf;
           const int lo = up ? lf : b, hi = up ? b : lf;
-          const int blk = lo * NL - (lo * (lo - 1)) / 2 + (hi - lo);
-          const float *Bb = B + blk * NFD * NFD + (up ? r * NFD : r);
+          const float *Bb = B + offdiag_block<NL>(lo, hi) * cellop_bstride(NFD) + (up ? r * NFD : r);
           const int st = up ? 1 : NFD;
 #pragma unroll
-          for (int s = 0; s < NFD; ++s) q = fmaf(Bb[s * st], pr[b * NFD + s], q);
+          for (int s = 0; s < NFD; ++s) qb[b] = fmaf(Bb[s * st], pr[b * NFD + s], qb[b]);
         }
+#pragma unroll
+        for (int b = 0; b < NL; ++b) q += qb[b];
       } else {
 #pragma unroll
         for (int b = 0; b < NL; ++b) {
-          const bool up = b >= lf;
+          if (b == lf) continue;
+          const bool up = b > lf;
           const int lo = up ? lf : b, hi = up ? b : lf;
-          const int blk = lo * NL - (lo * (lo - 1)) / 2 + (hi - lo);
-          const float *Bb = B + blk * NFD * NFD + (up ? r * NFD : r);
+          const float *Bb = B + offdiag_block<NL>(lo, hi) * cellop_bstride(NFD) + (up ? r * NFD : r);
           const int st = up ? 1 : NFD;
 #pragma unroll
           for (int s = 0; s < NFD; ++s) q = fmaf(Bb[s * st], ps[g][b * NFD + s], q);
@@ -621,11 +649,13 @@ __global__ void __launch_bounds__(CellOp<NL, NFD>::THREADS, 2)
   }
 }
 
-// q = qc(owner) + qc(other) per free row; x += alpha p; r -= alpha q; z = r
+// q = qc(owner) + qc(other) + p per free row (p: the identity diagonal
+// block); x += alpha p; r -= alpha q; z = r
 // (the preconditioner is in the scaled records); beta; convergence against
 // eta |rhs|.  Every load of a row is independent of the others (the products
 // sit by block row), so a row costs one memory round trip; rows are spread
-// over the grid (a.uctas CTAs, up to eight per SM) with a grid-stride loop.
+// over the grid (a.uctas CTAs: about eight rows per thread) with a
+// grid-stride loop.
 static_assert(kPcgThreads == kPcgThreadsHost, "host and device PCG block sizes differ");
 static_assert(kMaxRowLen == kMaxSkeletonRowLen, "host and device skeleton row limits differ");
 static_assert(kRowBlocks == kSkeletonRowBlocks, "host and device skeleton row limits differ");
@@ -639,13 +669,39 @@ __global__ void __launch_bounds__(kPcgThreads) pcg32_update_rows_kernel(Pcg32Arg
   float *__restrict__ xg = a.x;
   float *__restrict__ rg = a.r;
   FFSum rr;  // float-float: no FP64 in the per-row or per-CTA sums
-  for (int row = blockIdx.x * blockDim.x + threadIdx.x; row < a.n; row += gridDim.x * blockDim.x) {
+  const int stride = gridDim.x * blockDim.x;
+  int row = blockIdx.x * blockDim.x + threadIdx.x;
+  // four rows at a time, every load issued before the first product: each
+  // row is one L2 round trip, so a thread keeps four in flight
+  for (; row + 3 * stride < a.n; row += 4 * stride) {
+    float q0[4], q1[4], pv[4], xv[4], r0[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int rw = row + u * stride;
+      const int br = rw / NFD, i = rw - br * NFD;
+      const float *qb = qc + (size_t)br * (2 * NFD) + i;
+      q0[u] = qb[0];
+      q1[u] = qb[NFD];
+      pv[u] = p[rw];
+      xv[u] = xg[rw];
+      r0[u] = rg[rw];
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int rw = row + u * stride;
+      xg[rw] = fmaf(alpha, pv[u], xv[u]);
+      const float rv = fmaf(-alpha, (q0[u] + q1[u]) + pv[u], r0[u]);
+      rg[rw] = rv;
+      rr.add_prod(rv, rv);
+    }
+  }
+  for (; row < a.n; row += stride) {
     const int br = row / NFD, i = row - br * NFD;
     const float *qb = qc + (size_t)br * (2 * NFD) + i;
     const float q0 = qb[0], q1 = qb[NFD];
     const float pv = p[row], xv = xg[row], r0 = rg[row];
     xg[row] = fmaf(alpha, pv, xv);
-    const float rv = fmaf(-alpha, q0 + q1, r0);
+    const float rv = fmaf(-alpha, (q0 + q1) + pv, r0);
     rg[row] = rv;
     rr.add_prod(rv, rv);
   }
@@ -749,13 +805,19 @@ __global__ void __launch_bounds__(kPcgThreads) outer_residual_kernel(OuterArgs a
 // Launchers
 // ---------------------------------------------------------------------------
 cudaError_t launch_block_chol_inv(const PcgArgs &a, double *W, cudaStream_t s, int num_sms, long long *launches) {
-  if (a.nblockrows < 1) return cudaSuccess;
-  int g = (a.nblockrows + kCholWarps - 1) / kCholWarps;
-  if (g > num_sms * 8) g = num_sms * 8;
+  // the not-positive-definite flag after the last block starts at zero
+  cudaError_t e = cudaMemsetAsync(W + (size_t)a.nblockrows * a.nfd * a.nfd, 0, sizeof(double), s);
+  if (e != cudaSuccess || a.nblockrows < 1) return e;
   switch (a.nfd) {
-#define HDG_CHOL_CASE(N) \
-  case N:                \
-    block_chol_inv_kernel<N><<<g, 32 * kCholWarps, 0, s>>>(a, W); break;
+#define HDG_CHOL_CASE(N)                                    \
+  case N: {                                                 \
+    constexpr int G = 32 / N;                               \
+    const long long warps = (a.nblockrows + G - 1) / G;     \
+    long long g = (warps + 3) / 4;                          \
+    if (g > num_sms * 16) g = num_sms * 16;                 \
+    block_chol_inv_kernel<N><<<(int)g, 128, 0, s>>>(a, W);  \
+    break;                                                  \
+  }
     HDG_CHOL_CASE(1)
     HDG_CHOL_CASE(2)
     HDG_CHOL_CASE(3)
@@ -810,13 +872,13 @@ template <int NL, int NFD>
 static cudaError_t cellop_configure_t(size_t smem_optin, int num_sms, int *nstage, int *ctas) {
   using C = CellOp<NL, NFD>;
   const size_t stage = (size_t)C::CPS * C::REC * sizeof(float);
-  // Stages up to 32 KB (3D Darcy k=2: 4 cells, 27 KB): about 60 KB of records
+  // Stages up to 32 KB (3D Darcy k=2: 4 cells, 20 KB): up to 64 KB of records
   // in flight per CTA, so three CTAs fit an SM -- more warps to hide the
   // per-stage barriers and gathers (4.90 vs 4.56 TB/s against two CTAs with
-  // four stages each).  Larger stages: about 108 KB per CTA, two CTAs per SM
-  // where two stages each fit; otherwise (one cell of 3D elasticity k=2:
-  // 61 KB) one CTA with as many stages as fit.
-  int ns = (int)((stage <= 32 * 1024 ? 60 * 1024 : 110 * 1024) / stage);
+  // four stages each, measured with 27 KB stages).  Larger stages: about
+  // 108 KB per CTA, two CTAs per SM where two stages each fit; otherwise (one
+  // cell of 3D elasticity k=2: 43 KB) one CTA with as many stages as fit.
+  int ns = (int)((stage <= 32 * 1024 ? 64 * 1024 : 110 * 1024) / stage);
   ns = ns > kMaxBulkStages ? kMaxBulkStages : ns;
   if (2 * (2 * stage + 4096) > smem_optin) ns = (int)((smem_optin - 4096) / stage);
   ns = ns > kMaxBulkStages ? kMaxBulkStages : ns;
@@ -847,12 +909,12 @@ cudaError_t cellop_configure(int nl, int nfd, size_t smem_optin, int num_sms, in
 cudaError_t launch_pack_cell_blocks(int ncells, int nl, int nfd, double sign, const double *S, const int *cell_blk,
                                     const double *W, float *out, size_t smem_optin, cudaStream_t s, int num_sms,
                                     long long *launches) {
-  const int nf = nl * nfd, nb = nfd * nfd, nblk = nl * (nl + 1) / 2;
+  const int nf = nl * nfd, nb = nfd * nfd, nblk = cellop_blocks(nl);
   const size_t smem = sizeof(double) * nf * nf + sizeof(float) * (size_t)(nl + 2 * nblk) * nb;
   if (smem > 64 * 1024) {  // large cells
 #define HDG_PACK_LARGE(L, F)                                                                                  \
   if (nl == L && nfd == F) {                                                                                  \
-    const size_t lsmem = sizeof(float) * (size_t)(L * (L + 1) / 2 + L) * F * F;                               \
+    const size_t lsmem = sizeof(float) * (size_t)(cellop_blocks(L) + L) * F * F;                                  \
     cudaError_t e = cudaFuncSetAttribute(pack_cell_blocks_large_t<L, F>,                                      \
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lsmem);             \
     if (e != cudaSuccess) return e;                                                                           \

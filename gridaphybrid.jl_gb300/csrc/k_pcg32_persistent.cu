@@ -169,10 +169,10 @@ __global__ void __launch_bounds__(kPcgThreads) pcg32_persistent_kernel(Pcg32Args
           }
 #pragma unroll
           for (int b = 0; b < NL; ++b) {
-            const bool up = b >= lf;
+            if (b == lf) continue;  // the identity diagonal block: added in the update phase
+            const bool up = b > lf;
             const int lo = up ? lf : b, hi = up ? b : lf;
-            const int blk = lo * NL - (lo * (lo - 1)) / 2 + (hi - lo);
-            const float *Bb = B + blk * NFD * NFD + (up ? r * NFD : r);
+            const float *Bb = B + offdiag_block<NL>(lo, hi) * cellop_bstride(NFD) + (up ? r * NFD : r);
             const int st = up ? 1 : NFD;
 #pragma unroll
             for (int k = 0; k < NFD; ++k) q = fmaf(Bb[k * st], pr[b * NFD + k], q);
@@ -180,10 +180,10 @@ __global__ void __launch_bounds__(kPcgThreads) pcg32_persistent_kernel(Pcg32Args
         } else {
 #pragma unroll
           for (int b = 0; b < NL; ++b) {
-            const bool up = b >= lf;
+            if (b == lf) continue;
+            const bool up = b > lf;
             const int lo = up ? lf : b, hi = up ? b : lf;
-            const int blk = lo * NL - (lo * (lo - 1)) / 2 + (hi - lo);
-            const float *Bb = B + blk * NFD * NFD + (up ? r * NFD : r);
+            const float *Bb = B + offdiag_block<NL>(lo, hi) * cellop_bstride(NFD) + (up ? r * NFD : r);
             const int st = up ? 1 : NFD;
 #pragma unroll
             for (int k = 0; k < NFD; ++k) q = fmaf(Bb[k * st], ps[g][b * NFD + k], q);
@@ -191,6 +191,7 @@ __global__ void __launch_bounds__(kPcgThreads) pcg32_persistent_kernel(Pcg32Args
         }
         if (ent >= 0) a.qc[(size_t)(ent >> 1) * (2 * NFD) + ((ent & 1) ? 0 : NFD) + r] = q;
         acc += (double)pv * q;
+        if (ent >= 0 && (ent & 1)) acc += (double)pv * pv;  // the identity diagonal block, once per row
       }
       __syncthreads();  // the slot and ps are free again: refill with a later stage's records
       if (threadIdx.x == 0) {
@@ -217,7 +218,7 @@ __global__ void __launch_bounds__(kPcgThreads) pcg32_persistent_kernel(Pcg32Args
       const float q = __ldcg(qb) + __ldcg(qb + NFD);  // written by other CTAs: read through L2
       const float pv = __ldcg(p_new + row);
       a.x[row] = fmaf(alpha, pv, a.x[row]);
-      const float rv = fmaf(-alpha, q, a.r[row]);
+      const float rv = fmaf(-alpha, q + pv, a.r[row]);  // + p: the identity diagonal block
       a.r[row] = rv;
       rr += (double)rv * rv;
     }

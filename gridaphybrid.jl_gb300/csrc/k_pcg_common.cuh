@@ -35,11 +35,16 @@ __device__ __forceinline__ double block_sum(double v, double *red) {
 }
 
 // After every CTA has stored its partials: true in the CTA that arrives last.
+// Thread 0 stores a CTA's partials, so its fence before the arrival is the
+// one the last CTA's reads (through L2) need; a fence in every thread only
+// stalled them.
 __device__ __forceinline__ bool last_cta(unsigned int *counter) {
   __shared__ bool is_last;
-  __threadfence();
   __syncthreads();
-  if (threadIdx.x == 0) is_last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    is_last = atomicAdd(counter, 1u) == gridDim.x - 1;
+  }
   __syncthreads();
   return is_last;
 }
@@ -217,6 +222,13 @@ __device__ __forceinline__ void stage_tile_columns(const int64_t *__restrict__ r
     const int len = (int)(rowptr[(int64_t)(br0 + k) * NFD + 1] - base);
     for (int j = lane; j < len; j += 32) xs[k * RowTile<NFD>::LMAX + j] = f(colind[base + j]);
   }
+}
+
+// index of the facet block (lo, hi), lo < hi, in a cell record of the
+// unassembled FP32 operator (the blocks above the diagonal, row-major order)
+template <int NL>
+__device__ __forceinline__ int offdiag_block(int lo, int hi) {
+  return lo * (NL - 1) - (lo * (lo - 1)) / 2 + (hi - lo - 1);
 }
 
 template <int N>
