@@ -637,25 +637,22 @@ __global__ void __launch_bounds__(CellOp<NL, NFD>::THREADS, 2)
       ++issued;
     }
   }
+  // this CTA's part of (p, A p); the update kernel's CTAs sum the parts
+  // themselves (no last-CTA step at the end of this launch)
   const float2 tsum = block_sum_ff(acc.hi, acc.lo, redf);
   if (threadIdx.x == 0) store_partial_ff(a.partials, (int)gridDim.x, 0, tsum);
-  if (last_cta(a.counter)) {
-    const double pq = sum_partials_ff(a.partials, (int)gridDim.x, 0, redf);
-    if (threadIdx.x == 0) {
-      a.scal[SC_PAP] = pq;
-      a.scal[SC_ALPHA] = a.scal[SC_RZ] / pq;
-      *a.counter = 0u;
-    }
-  }
 }
 
+// alpha = (r, z) / (p, A p), every CTA summing the SpMV's per-CTA parts in
+// index order (the same value in all of them) while its first rows load;
 // q = qc(owner) + qc(other) + p per free row (p: the identity diagonal
-// block); x += alpha p; r -= alpha q; z = r
-// (the preconditioner is in the scaled records); beta; convergence against
-// eta |rhs|.  Every load of a row is independent of the others (the products
-// sit by block row), so a row costs one memory round trip; rows are spread
-// over the grid (a.uctas CTAs: about eight rows per thread) with a
-// grid-stride loop.
+// block); x += alpha p; r -= alpha q; z = r (the preconditioner is in the
+// scaled records); beta; convergence against eta |rhs|.  Every load of a row
+// is independent of the others (the products sit by block row), so a row
+// costs one memory round trip; rows are spread over the grid (a.uctas CTAs:
+// about eight rows per thread) with a grid-stride loop.  This kernel's own
+// parts go after the SpMV's (a.ctas of them), which other CTAs may still be
+// reading.
 static_assert(kPcgThreads == kPcgThreadsHost, "host and device PCG block sizes differ");
 static_assert(kMaxRowLen == kMaxSkeletonRowLen, "host and device skeleton row limits differ");
 static_assert(kRowBlocks == kSkeletonRowBlocks, "host and device skeleton row limits differ");
@@ -663,8 +660,8 @@ static_assert(kRowBlocks == kSkeletonRowBlocks, "host and device skeleton row li
 template <int NFD>
 __global__ void __launch_bounds__(kPcgThreads) pcg32_update_rows_kernel(Pcg32Args a, const float *__restrict__ p) {
   __shared__ float2 redf[32];
+  __shared__ float s_alpha;
   if (a.scal[SC_DONE] != 0.0) return;
-  const float alpha = (float)a.scal[SC_ALPHA];
   const float *__restrict__ qc = a.qc;
   float *__restrict__ xg = a.x;
   float *__restrict__ rg = a.r;
@@ -673,44 +670,62 @@ __global__ void __launch_bounds__(kPcgThreads) pcg32_update_rows_kernel(Pcg32Arg
   int row = blockIdx.x * blockDim.x + threadIdx.x;
   // four rows at a time, every load issued before the first product: each
   // row is one L2 round trip, so a thread keeps four in flight
-  for (; row + 3 * stride < a.n; row += 4 * stride) {
-    float q0[4], q1[4], pv[4], xv[4], r0[4];
+  float q0[4], q1[4], pv[4], xv[4], r0[4];
+  auto load4 = [&](int rb) {
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
-      const int rw = row + u * stride;
-      const int br = rw / NFD, i = rw - br * NFD;
-      const float *qb = qc + (size_t)br * (2 * NFD) + i;
-      q0[u] = qb[0];
-      q1[u] = qb[NFD];
-      pv[u] = p[rw];
-      xv[u] = xg[rw];
-      r0[u] = rg[rw];
+      const int rw = rb + u * stride;
+      if (rw < a.n) {
+        const int br = rw / NFD, i = rw - br * NFD;
+        const float *qb = qc + (size_t)br * (2 * NFD) + i;
+        q0[u] = qb[0];
+        q1[u] = qb[NFD];
+        pv[u] = p[rw];
+        xv[u] = xg[rw];
+        r0[u] = rg[rw];
+      }
     }
+  };
+  auto update4 = [&](int rb, float alpha) {
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
-      const int rw = row + u * stride;
-      xg[rw] = fmaf(alpha, pv[u], xv[u]);
-      const float rv = fmaf(-alpha, (q0[u] + q1[u]) + pv[u], r0[u]);
-      rg[rw] = rv;
-      rr.add_prod(rv, rv);
+      const int rw = rb + u * stride;
+      if (rw < a.n) {
+        xg[rw] = fmaf(alpha, pv[u], xv[u]);
+        const float rv = fmaf(-alpha, (q0[u] + q1[u]) + pv[u], r0[u]);
+        rg[rw] = rv;
+        rr.add_prod(rv, rv);
+      }
     }
+  };
+  load4(row);
+  const double pap = sum_partials_ff(a.partials, a.ctas, 0, redf);  // valid in thread 0
+  if (threadIdx.x == 0) s_alpha = (float)(a.scal[SC_RZ] / pap);
+  __syncthreads();
+  const float alpha = s_alpha;
+  update4(row, alpha);
+  for (row += 4 * stride; row + 3 * stride < a.n; row += 4 * stride) {
+    load4(row);
+    update4(row, alpha);
   }
   for (; row < a.n; row += stride) {
     const int br = row / NFD, i = row - br * NFD;
     const float *qb = qc + (size_t)br * (2 * NFD) + i;
-    const float q0 = qb[0], q1 = qb[NFD];
-    const float pv = p[row], xv = xg[row], r0 = rg[row];
-    xg[row] = fmaf(alpha, pv, xv);
-    const float rv = fmaf(-alpha, (q0 + q1) + pv, r0);
+    const float q0s = qb[0], q1s = qb[NFD];
+    const float pvs = p[row], xvs = xg[row], r0s = rg[row];
+    xg[row] = fmaf(alpha, pvs, xvs);
+    const float rv = fmaf(-alpha, (q0s + q1s) + pvs, r0s);
     rg[row] = rv;
     rr.add_prod(rv, rv);
   }
   const int np = (int)gridDim.x;
   const float2 s = block_sum_ff(rr.hi, rr.lo, redf);
-  if (threadIdx.x == 0) store_partial_ff(a.partials, np, 0, s);
+  if (threadIdx.x == 0) store_partial_ff(a.partials + a.ctas, np, 0, s);
   if (last_cta(a.counter)) {
-    const double vrr = sum_partials_ff(a.partials, np, 0, redf);
+    const double vrr = sum_partials_ff(a.partials + a.ctas, np, 0, redf);
     if (threadIdx.x == 0) {
+      a.scal[SC_PAP] = pap;
+      a.scal[SC_ALPHA] = a.scal[SC_RZ] / pap;
       a.scal[SC_BETA] = vrr / a.scal[SC_RZ];
       a.scal[SC_RZ] = vrr;
       a.scal[SC_RR] = vrr;
