@@ -629,7 +629,10 @@ def run_gpu(args, rank=0, nranks=1, device=0):
         rec = (nl * (nl - 1) // 2 * bstride + 3) // 4 * 4  # the blocks above the diagonal
         spmv_bytes = ncells * rec * 4 + ncells * nl * 4 + 3 * nfree * 4 + ncells * nf * 4
         spmv_kernel = "cell_spmv32_kernel<6,9>"
-        spmv_traffic = None  # set from an ncu capture of this record layout
+        # DRAM read + write of one launch from an ncu capture at 24^3 (73.78 + 1.15 MB
+        # over 13,824 cells, the bench configuration), scaled by cells: the kernel
+        # streams each cell record once, so traffic grows with the cells
+        spmv_traffic = 74.93e6 / 13824 * ncells
     spmv_gbs = spmv_bytes / (spmv_ms.value * 1e-3) / 1e9
     # assembly: condensed blocks + vectors read, CSR values + rhs written
     asm_bytes = ncells * (nf * nf + nf) * 8 + nnz * 8 + nfree * 8
