@@ -499,13 +499,17 @@ struct CellOp {
 // Persistent CTAs take stages of CPS consecutive cells round-robin; thread 0
 // keeps `nstage` stages of cell records in flight with bulk copies (L2
 // evict-first: the records are read once per iteration, the vectors stay).
+// One CTA barrier per stage: the gathered p alternates between two buffers by
+// stage parity, and the ring slot of stage t-1 is refilled once every thread
+// has passed stage t's barrier (a second barrier at the end of each stage
+// cost 40.7 against 39.1 us per launch at 32^3).
 template <int NL, int NFD>
 __global__ void __launch_bounds__(CellOp<NL, NFD>::THREADS, 2)
     cell_spmv32_kernel(Pcg32Args a, const float *__restrict__ p_old, float *__restrict__ p_new) {
   using C = CellOp<NL, NFD>;
   extern __shared__ __align__(128) float ring[];
   __shared__ __align__(8) uint64_t bars[kMaxBulkStages];
-  __shared__ __align__(16) float ps[C::CPS][C::TPC];
+  __shared__ __align__(16) float ps2[2][C::CPS][C::TPC];  // by stage parity: one CTA barrier per stage
   __shared__ float2 redf[32];
   __shared__ int abort_flag;
   if (a.scal[SC_DONE] != 0.0) return;
@@ -569,6 +573,7 @@ __global__ void __launch_bounds__(CellOp<NL, NFD>::THREADS, 2)
       z_a = a.z[row];
     }
     ent_b = load_ent(t + 2);
+    float (*ps)[C::TPC] = ps2[t & 1];
     ps[g][i] = pv;
     if (!mbar_wait_bounded(&bars[slot], (uint32_t)(t / nstage) & 1u)) abort_flag = 1;
     __syncthreads();
@@ -580,6 +585,12 @@ __global__ void __launch_bounds__(CellOp<NL, NFD>::THREADS, 2)
         for (int u = t; u < issued; ++u) mbar_wait_bounded(&bars[u % nstage], (uint32_t)(u / nstage) & 1u);
       }
       return;
+    }
+    // every thread is past stage t-1: its ring slot can be refilled
+    if (threadIdx.x == 0 && t >= 1 && issued < mine) {
+      async_proxy_fence();
+      issue(issued);
+      ++issued;
     }
     if (act) {
       const float *B = ring + (size_t)slot * C::CPS * C::REC + (size_t)g * C::REC;
@@ -629,12 +640,6 @@ __global__ void __launch_bounds__(CellOp<NL, NFD>::THREADS, 2)
       // by block row: the owner's product first, then the other cell's
       if (ent >= 0) a.qc[(size_t)(ent >> 1) * (2 * NFD) + ((ent & 1) ? 0 : NFD) + r] = q;
       acc.add_prod(pv, q);
-    }
-    __syncthreads();  // the slot and ps are free again
-    if (threadIdx.x == 0 && issued < mine) {
-      async_proxy_fence();
-      issue(issued);
-      ++issued;
     }
   }
   // this CTA's part of (p, A p); the update kernel's CTAs sum the parts
