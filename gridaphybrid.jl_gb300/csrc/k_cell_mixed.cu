@@ -97,9 +97,11 @@ __device__ __forceinline__ void ff_entry_cells(const float2 *cs, int ncg, unsign
 // axis: every cell's Jacobian is diagonal, so cg[e][d] = 0 for e != d and
 // cn[lf][d] = 0 unless d is the axis normal to facet lf; those terms (and
 // terms whose table value is zero) are skipped -- they add exact zeros, as
-// cell_entry_ff's zero-coefficient test does.
+// cell_entry_ff's zero-coefficient test does.  Four CTAs per SM (64
+// registers): the kernel is issue-bound, and the extra warps took the 32^3
+// integrate phase from 2.51 to 2.44 ms.
 template <int D, int K>
-__global__ void __launch_bounds__(256, 3) integrate_ffentries_kernel(int ncells, MixedTables T, bool axis,
+__global__ void __launch_bounds__(256, 4) integrate_ffentries_kernel(int ncells, MixedTables T, bool axis,
                                                                   const float2 *__restrict__ coef, float *Ahi,
                                                                   float *Alo) {
   using S = DarcyShape<D, K>;
