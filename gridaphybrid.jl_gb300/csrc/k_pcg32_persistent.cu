@@ -53,15 +53,14 @@ __device__ bool grid_barrier(unsigned *count, unsigned *gen, unsigned &my_gen, i
   return *flag != 0;
 }
 
-// sum of n per-CTA partials in one fixed order (every CTA gets the same bits)
-__device__ __forceinline__ double sum_all(const double *p, int n, double *red) {
-  double s = 0.0;
-  for (int i = threadIdx.x; i < n; i += blockDim.x) s += __ldcg(p + i);
-  s = block_sum(s, red);
+// sum of the n float-float per-CTA partials k*n .. k*n+n-1 in one fixed order,
+// returned in every thread (every CTA gets the same bits)
+__device__ __forceinline__ double sum_all_ff(const double *partials, int n, int k, float2 *redf) {
+  __shared__ double bc;
+  const double v0 = sum_partials_ff(partials, n, k, redf);  // valid in thread 0
+  if (threadIdx.x == 0) bc = v0;
   __syncthreads();
-  if (threadIdx.x == 0) red[0] = s;
-  __syncthreads();
-  const double v = red[0];
+  const double v = bc;
   __syncthreads();
   return v;
 }
@@ -75,7 +74,7 @@ __global__ void __launch_bounds__(kPcgThreads) pcg32_persistent_kernel(Pcg32Args
   extern __shared__ __align__(128) float ring[];
   __shared__ __align__(8) uint64_t bars[kPersistStagesMax];
   __shared__ __align__(16) float ps[CPS][TPC];
-  __shared__ double red[32];
+  __shared__ float2 redf[32];
   __shared__ int flag, abort_flag;
   if (a.scal[SC_DONE] != 0.0) return;
   unsigned *bar_count = a.counter + 2, *bar_gen = a.counter + 3;
@@ -128,8 +127,8 @@ __global__ void __launch_bounds__(kPcgThreads) pcg32_persistent_kernel(Pcg32Args
   float *p_new = a.p2;
   long long stage = 0;  // stages consumed
   for (int it = 0; it < iter_cap; ++it) {
-    // ---- SpMV phase
-    double acc = 0.0;
+    // ---- SpMV phase (dot products in float-float: GB300's FP64 pipe is narrow)
+    FFSum acc;
     const float fbeta = (float)beta;
     for (int s = 0; s < mine; ++s, ++stage) {
       const int slot = (int)(stage % nstage);
@@ -190,8 +189,8 @@ __global__ void __launch_bounds__(kPcgThreads) pcg32_persistent_kernel(Pcg32Args
           }
         }
         if (ent >= 0) a.qc[(size_t)(ent >> 1) * (2 * NFD) + ((ent & 1) ? 0 : NFD) + r] = q;
-        acc += (double)pv * q;
-        if (ent >= 0 && (ent & 1)) acc += (double)pv * pv;  // the identity diagonal block, once per row
+        acc.add_prod(pv, q);
+        if (ent >= 0 && (ent & 1)) acc.add_prod(pv, pv);  // the identity diagonal block, once per row
       }
       __syncthreads();  // the slot and ps are free again: refill with a later stage's records
       if (threadIdx.x == 0) {
@@ -200,18 +199,18 @@ __global__ void __launch_bounds__(kPcgThreads) pcg32_persistent_kernel(Pcg32Args
         ++issued;
       }
     }
-    double sp = block_sum(acc, red);
-    if (threadIdx.x == 0) a.partials[blockIdx.x] = sp;
+    const float2 sp = block_sum_ff(acc.hi, acc.lo, redf);
+    if (threadIdx.x == 0) store_partial_ff(a.partials, G, 0, sp);
     if (!grid_barrier(bar_count, bar_gen, my_gen, &flag)) {
       fail(stage);
       return;
     }
-    const double pq = sum_all(a.partials, G, red);
+    const double pq = sum_all_ff(a.partials, G, 0, redf);
     const double alpha_d = rz / pq;
     const float alpha = (float)alpha_d;
     // ---- update phase: rows round-robin over the grid (the same rows every
     // iteration, so x and r are only ever touched by this CTA)
-    double rr = 0.0;
+    FFSum rr;
     for (int row = blockIdx.x * kPcgThreads + threadIdx.x; row < a.n; row += G * kPcgThreads) {
       const int br = row / NFD, ri = row - br * NFD;
       const float *qb = a.qc + (size_t)br * (2 * NFD) + ri;
@@ -220,19 +219,16 @@ __global__ void __launch_bounds__(kPcgThreads) pcg32_persistent_kernel(Pcg32Args
       a.x[row] = fmaf(alpha, pv, a.x[row]);
       const float rv = fmaf(-alpha, q + pv, a.r[row]);  // + p: the identity diagonal block
       a.r[row] = rv;
-      rr += (double)rv * rv;
+      rr.add_prod(rv, rv);
     }
-    const double rzn = rr;
-    double s1 = block_sum(rzn, red);
-    if (threadIdx.x == 0) a.partials[G + blockIdx.x] = s1;
-    s1 = block_sum(rr, red);
-    if (threadIdx.x == 0) a.partials[2 * G + blockIdx.x] = s1;
+    const float2 s1 = block_sum_ff(rr.hi, rr.lo, redf);
+    if (threadIdx.x == 0) store_partial_ff(a.partials, G, 1, s1);
     if (!grid_barrier(bar_count, bar_gen, my_gen, &flag)) {
       fail(stage);
       return;
     }
-    const double vrz = sum_all(a.partials + G, G, red);
-    const double vrr = sum_all(a.partials + 2 * G, G, red);
+    const double vrr = sum_all_ff(a.partials, G, 1, redf);
+    const double vrz = vrr;  // z = r
     beta = vrz / rz;
     rz = vrz;
     iters += 1.0;
