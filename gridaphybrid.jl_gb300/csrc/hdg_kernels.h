@@ -326,9 +326,10 @@ bool assemble_supports(int nl, int nfd);
 // W = blockdiag(L_f^{-1}), CG runs on M^ = W M W^T (unit diagonal blocks) for
 // y = W^{-T} e with right-hand side W rhs -- the same iterates as PCG with
 // the preconditioner D^{-1}, without reading D^{-1} every iteration (z = r).
-// M^ is applied unassembled: per cell the upper triangle of facet blocks of
+// M^ is applied unassembled: per cell the facet blocks above the diagonal of
 // W_a sign*(S_c + S_c^T)/2 W_b^T in FP32, streamed with bulk async copies;
-// the two cells of a facet are summed in the update kernel.
+// the two cells of a facet are summed in the update kernel, which adds p for
+// the diagonal blocks (their sum over a facet's cells is the identity).
 struct Pcg32Args {
   int n, nfd, nblockrows;
   const double *W;    // nblockrows x nfd x nfd, row-major lower-triangular L_f^{-1}

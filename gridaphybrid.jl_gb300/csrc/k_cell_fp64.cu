@@ -3,7 +3,7 @@
 // condensation (BackwardStaticCondensationMap), recovery from stored factors,
 // SumFacetsMap and per-cell L2 errors.
 //
-// GB300 executes FP64 at ~1/62 of its FP32 rate (1.2 vs 74 TFLOP/s measured),
+// GB300 executes FP64 at ~1/74 of its FP32 rate (1.05 vs 78 TFLOP/s measured),
 // so this path is DFMA-bound: a CTA per cell, the cell block resident in
 // shared memory, no effort spent on memory-side tiling.
 #include <cuda_runtime.h>

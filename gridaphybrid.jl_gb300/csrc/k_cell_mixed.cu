@@ -1,7 +1,7 @@
 // k_cell_mixed.cu -- FP32 local factorisation with high-precision refinement,
 // for sm_103a.
 //
-// GB300 runs FP64 at ~1/62 of its FP32 rate, so "high precision" here is
+// GB300 runs FP64 at ~1/74 of its FP32 rate, so "high precision" here is
 // float-float arithmetic (a value is an unevaluated sum hi + lo of two FP32
 // numbers, ~48 significant bits) executed on the FP32 pipes:
 //  * integration produces every cell block as (A_hi, A_lo) FP32 pairs;

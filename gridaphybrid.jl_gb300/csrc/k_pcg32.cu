@@ -10,10 +10,10 @@
 //                  records (CG on W M W^T, W = blockdiag(L_f^{-1}) with
 //                  D_f = L_f L_f^T), so an iteration reads no block inverse;
 //                  its dot products accumulate in float-float.
-// GB300 executes FP64 at 1/62 of its FP32 rate, which makes even an FP64
-// SpMV arithmetic-bound; the inner iterations stay on the FP32 pipes and
-// stream about a quarter of the FP64 CSR bytes (FP32, upper blocks only),
-// the FP64 CSR residual runs once per outer step.
+// GB300 executes FP64 at about 1/74 of its FP32 rate, which makes even an
+// FP64 SpMV arithmetic-bound; the inner iterations stay on the FP32 pipes and
+// stream about a sixth of the FP64 CSR bytes (FP32, the facet blocks above the
+// diagonal only), the FP64 CSR residual runs once per outer step.
 #include <cuda_runtime.h>
 
 #include "hdg_kernels.h"
