@@ -58,6 +58,20 @@ __device__ __forceinline__ void div(float ah, float al, float bh, float bl, floa
   fast_two_sum(q1, q2, h, l);
 }
 
+
+// normalised (ah + al) - (bh + bl) * (ch + cl) without normalising the
+// product first (three FP32 operations fewer than mul then sub)
+__device__ __forceinline__ void fms(float ah, float al, float bh, float bl, float ch, float cl, float &h, float &l) {
+  const float p = bh * ch;
+  float pe = fmaf(bh, ch, -p);
+  pe = fmaf(bl, ch, pe);
+  pe = fmaf(bh, cl, pe);
+  float s, e;
+  two_sum(ah, -p, s, e);
+  e += al - pe;
+  fast_two_sum(s, e, h, l);
+}
+
 __device__ __forceinline__ void normalise(float &h, float &l) {
   float s, e;
   fast_two_sum(h, l, s, e);
@@ -151,9 +165,8 @@ __device__ __forceinline__ void lu_pivot_warp(float *Ph, float *Pl, int *perm, i
       Ph[lane * NK + j] = lh;
       Pl[lane * NK + j] = ll;
       for (int c = j + 1; c < NK; ++c) {
-        float ph, pl, rh, rl;
-        mul(lh, ll, Ph[p * NK + c], Pl[p * NK + c], ph, pl);
-        sub(Ph[lane * NK + c], Pl[lane * NK + c], ph, pl, rh, rl);
+        float rh, rl;
+        fms(Ph[lane * NK + c], Pl[lane * NK + c], lh, ll, Ph[p * NK + c], Pl[p * NK + c], rh, rl);
         Ph[lane * NK + c] = rh;
         Pl[lane * NK + c] = rl;
       }
@@ -258,9 +271,8 @@ __device__ __forceinline__ void solve_columns(const float *Ph, const float *Pl, 
         if (4 * s + 3 <= i) continue;  // no entry of slot s lies below row i
         const int j = 4 * s + sl;
         if (j > i && j < NK) {
-          float ph, pl, rh, rl;
-          mul(Ph[pr[s] * NK + i], Pl[pr[s] * NK + i], vh, vl, ph, pl);
-          sub(yh[s], yl[s], ph, pl, rh, rl);
+          float rh, rl;
+          fms(yh[s], yl[s], Ph[pr[s] * NK + i], Pl[pr[s] * NK + i], vh, vl, rh, rl);
           yh[s] = rh;
           yl[s] = rl;
         }
@@ -284,9 +296,8 @@ __device__ __forceinline__ void solve_columns(const float *Ph, const float *Pl, 
         if (4 * s >= i) continue;  // no entry of slot s lies above row i
         const int j = 4 * s + sl;
         if (j < i) {
-          float ph, pl, rh, rl;
-          mul(Ph[pr[s] * NK + i], Pl[pr[s] * NK + i], xh, xl, ph, pl);
-          sub(yh[s], yl[s], ph, pl, rh, rl);
+          float rh, rl;
+          fms(yh[s], yl[s], Ph[pr[s] * NK + i], Pl[pr[s] * NK + i], xh, xl, rh, rl);
           yh[s] = rh;
           yl[s] = rl;
         }
@@ -381,9 +392,8 @@ __device__ __forceinline__ void lu_solve_group(float *Ph, float *Pl, float *Qh, 
         th = Qh + i * NC + cc;
         tl = Ql + i * NC + cc;
       }
-      float ph, pl, rh, rl;
-      mul(lh, ll, uh, ul, ph, pl);
-      sub(*th, *tl, ph, pl, rh, rl);
+      float rh, rl;
+      fms(*th, *tl, lh, ll, uh, ul, rh, rl);
       *th = rh;
       *tl = rl;
     }
@@ -400,9 +410,8 @@ __device__ __forceinline__ void lu_solve_group(float *Ph, float *Pl, float *Qh, 
     __syncthreads();
     for (int e = t; e < j * NC; e += NT) {
       const int i = e / NC, c = e % NC;
-      float ph, pl, rh, rl;
-      mul(Ph[i * NK + j], Pl[i * NK + j], Qh[j * NC + c], Ql[j * NC + c], ph, pl);
-      sub(Qh[i * NC + c], Ql[i * NC + c], ph, pl, rh, rl);
+      float rh, rl;
+      fms(Qh[i * NC + c], Ql[i * NC + c], Ph[i * NK + j], Pl[i * NK + j], Qh[j * NC + c], Ql[j * NC + c], rh, rl);
       Qh[i * NC + c] = rh;
       Ql[i * NC + c] = rl;
     }
