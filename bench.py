@@ -450,8 +450,8 @@ FFBLOCK_FP32_FLOP_PER_CELL = 3.17e6
 
 
 def condense_roofline(phase, ncells, peaks):
-    """Compute roofline of the condensation: the SURVEY-defined algorithmic
-    FP64 flops of StaticCondensationMap per cell (2/3 ni^3 + 2 ni^2 nf +
+    """Compute roofline of the condensation: the algorithmic FP64 flops of
+    the reference's StaticCondensationMap per cell (2/3 ni^3 + 2 ni^2 nf +
     2 nf^2 ni + 2 ni^2 + 2 ni nf) over the event-timed condensation, against
     the measured FP64 peak (how far past native FP64 the float-float path
     goes), and, where the FP32 work per cell is known from ncu, the FP32-pipe
